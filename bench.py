@@ -1,0 +1,328 @@
+#!/usr/bin/env python
+"""Throughput benchmark: bead-force-steps/s of batched TI-PIMD on one GB300.
+
+Workload (one GPU): the 2-D six-well surface of mcmod_2dtest, P = 128 beads,
+1024 trajectories x 16 Gauss-Legendre lambda points = 16,384 ring polymers,
+Langevin thermostat, mixed precision (FP32 forces and state, split-BF16
+tensor-core normal-mode transform, FP64 estimator accumulation).  One bench
+"step" = MD_PER_STEP MD steps of every ring (one launch of the fused kernel).
+
+  value   = (sum over rings of P) * MD steps / device seconds, all ranks
+  e2e     = the same metric through pg_propagate_pimd (the reference-facing
+            drop-in for propagate_pimd_pile) with host x/p buffers: H2D of the
+            ring state, the MD steps, D2H of state and estimators, every step
+  plain / fused FP64: the same rings through the FP64 forms (denominators)
+  cpu_baseline: the CPU restatement of the reference step (ten dense NM
+            transforms per step, FP64) on all host cores, bounded sample
+
+--impl reference times only that CPU restatement (the reference's own
+Fortran/MKL/MPI build cannot be compiled on these machines).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "pimd-tunneling_gb300")
+for _p in (os.path.join(PKG, "python"), PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "bead-force-steps/s, batched mixed-prec vs plain FP64 on 1 GB300 at <=1% split err"
+UNIT = "bead-force-steps/s"
+MD_PER_STEP = 500
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = max(smax, float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _workload(rank):
+    import pgconfigs
+    c = dict(pgconfigs.load("c1"))
+    # weak scaling: every rank runs its own 1024 trajectories (distinct seeds)
+    c["seeds"] = [s + 1024 * rank for s in range(1024)]
+    ti = pgconfigs.TiInputs(c)
+    return c, ti
+
+
+def cpu_reference_rate(c, ti, target_s=12.0, nthreads=None):
+    """Bead-force-steps/s of the CPU restatement of the reference step on all host
+    cores (one ring per thread at a time), on a bounded sample of the workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.lib()
+    nthreads = nthreads or os.cpu_count() or 1
+    pes = O.Pes(c["pes_id"], c["ndim"], c["natom"], c["params"], V0=c["V0"])
+    mass = np.array(c["mass"])
+    prm = O.TiParams(ti.P, c["beta"], c["dt"], tau=c["tau"], gamma=c["gamma"], thermostat=2,
+                     nm_resident=False, imin=0, init_sigma=c["init_sigma"])
+    nd, P = ti.nd, ti.P
+
+    def run(nr, nsteps):
+        idx = np.arange(nr) % ti.nrings
+        lam = ti.ring_lambda[idx]
+        x = np.zeros(nr * nd * P)
+        p = np.zeros(nr * nd * P)
+        for k, r in enumerate(idx):
+            li = ti.ring_lambda[r]
+            xx, pp = O.ring_init(pes, mass, prm, ti.xref[li], int(ti.ring_seed[r]), int(ti.ring_stream[r]),
+                                 a=ti.a, b=ti.b[li])
+            x[k * nd * P:(k + 1) * nd * P] = xx
+            p[k * nd * P:(k + 1) * nd * P] = pp
+        t0 = time.perf_counter()
+        O.ti_run_batch(pes, mass, prm, lam, ti.ring_seed[idx], ti.ring_stream[idx], ti.a, ti.b, ti.dbdl,
+                       ti.xref, nsteps, nthreads, x, p)
+        return time.perf_counter() - t0
+
+    nr = nthreads
+    probe_steps = 20
+    dt = run(nr, probe_steps)
+    rate_ring_steps = nr * probe_steps / max(dt, 1e-9)
+    nsteps = max(20, int(target_s * rate_ring_steps / nr))
+    dt = run(nr, nsteps)
+    value = nr * nsteps * P / dt
+    sample = ("%d rings x %d MD steps of the workload (P=%d, 2-D six-well surface), reference step "
+              "order (10 dense NM transforms per step), FP64, %d threads, %.1f s" % (nr, nsteps, P, nthreads, dt))
+    return value, nthreads, sample
+
+
+def run_reference(args):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return 0
+    c, ti = _workload(0)
+    vals = []
+    for _ in range(max(args.warmup, 0)):
+        pass
+    per = max(3.0, 20.0 / max(args.steps, 1))
+    sample = ""
+    cores = 1
+    for _ in range(args.steps):
+        v, cores, sample = cpu_reference_rate(c, ti, target_s=per)
+        vals.append(v)
+    value = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "c1: mcmod_2dtest, P=128, 1024 traj x 16 lambda = 16384 rings, Langevin",
+                       "l2": "n/a (CPU)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "the reference Fortran/MKL/MPI build cannot be compiled here (no Fortran compiler, "
+                    "no MKL); this arm times the CPU restatement of the reference step"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--md-per-step", type=int, default=MD_PER_STEP)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-extras", action="store_true", help="skip the e2e and FP64 legs")
+    ap.add_argument("--form", default="auto", choices=["auto", "fused", "tensor"])
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    ws, rank, local = _dist()
+    import torch
+    import torch.distributed as dist
+    if ws > 1:
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+
+    import build as B
+    if rank == 0 or ws == 1:
+        B.build()
+    if ws > 1:
+        dist.barrier()
+    import pimdgpu as pg
+
+    c, ti = _workload(rank)
+    ctx = pg.Context(local)
+    ctx.set_system(c["ndim"], c["natom"], c["mass"], c["pes_id"], c["params"], c["V0"])
+    form = {"auto": pg.PG_FORM_AUTO, "fused": pg.PG_FORM_FUSED, "tensor": pg.PG_FORM_TENSOR}[args.form]
+    cfg = ti.ti_config(pg, pg.PG_MIXED, form)
+    ctx.ti_setup(cfg, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
+    K, W, M = args.steps, args.warmup, args.md_per_step
+    beads = ti.nrings * ti.P
+
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
+    for _ in range(W):
+        ctx.ti_advance(M)
+    sampler = ClockSampler(local)
+    sampler.start()
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    times = []
+    wall0 = time.perf_counter()
+    for _ in range(K):
+        flush.add_(1.0)  # evict L2 between timed steps
+        torch.cuda.synchronize()
+        times.append(ctx.ti_advance_timed(M) / 1e3)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    if ws > 1:
+        dist.barrier()
+    clocks = sampler.stop()
+    dev_s = sum(times)
+    if ws > 1:
+        t = torch.tensor([dev_s], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_s = float(t.item())
+    value = ws * beads * M * K / dev_s
+    kernel_ms = 1e3 * dev_s / K
+    s, n, _, st = ctx.ti_results()
+    nan_rings = int(np.sum(st != 0))
+
+    extras = {}
+    if not args.no_extras and rank == 0:
+        # e2e: the reference-facing drop-in with host buffers, copies inside the timed region
+        x0, p0 = ctx.ti_state()
+        xh = torch.from_numpy(x0).pin_memory().numpy()
+        ph = torch.from_numpy(p0).pin_memory().numpy()
+        bseq = ti.b
+        dseq = ti.dbdl
+        for _ in range(2):
+            ctx.propagate_pimd(cfg, M, ti.a, bseq[ti.ring_lambda], dseq[ti.ring_lambda], ti.ring_seed,
+                               ti.ring_stream, xh, ph)
+        te = []
+        for _ in range(max(3, K // 2)):
+            t0 = time.perf_counter()
+            xo, po, dh, _ = ctx.propagate_pimd(cfg, M, ti.a, bseq[ti.ring_lambda], dseq[ti.ring_lambda],
+                                               ti.ring_seed, ti.ring_stream, xh, ph)
+            te.append(time.perf_counter() - t0)
+        e2e_s = statistics.median(te)
+        h2d = xh.nbytes + ph.nbytes
+        d2h = xh.nbytes + ph.nbytes + dh.nbytes
+        extras["e2e"] = {"value": beads * M / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                         "d2h_bytes_per_step": int(d2h), "call": "pg_propagate_pimd (host buffers)"}
+        # FP64 denominators on the same rings
+        for name, form64, md in (("plain_fp64", pg.PG_FORM_PLAIN, 4), ("fused_fp64", pg.PG_FORM_FUSED, 20)):
+            cfg64 = ti.ti_config(pg, pg.PG_FP64, form64)
+            ctx.ti_setup(cfg64, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
+            ctx.ti_advance(md)
+            ms = ctx.ti_advance_timed(md)
+            extras[name] = {"value": beads * md / (ms / 1e3), "unit": UNIT, "md_steps": md}
+        extras["speedup_vs_plain_fp64"] = value / ws / extras["plain_fp64"]["value"]
+        extras["speedup_vs_fused_fp64"] = value / ws / extras["fused_fp64"]["value"]
+
+    peaks, peak_kind = _peaks()
+    # Algorithmic tensor work of the NM transforms: 2 transforms x 2*P*ndof flops per bead-step.
+    f_tc = 2 * 2 * ti.P * ti.nd
+    achieved_tf = f_tc * beads * M / (kernel_ms / 1e3) / 1e12
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "ti_fused_c1_traffic.json")) as f:
+            traffic = json.load(f).get("dram_bytes_per_launch")
+    except Exception:
+        pass
+    roof = {"bound": "tensor", "achieved": achieved_tf, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
+            "frac": achieved_tf / peaks["bf16_tflops"], "traffic": traffic,
+            "peak_source": peak_kind,
+            "note": "algorithmic NM-transform flops (2 x 2 P ndof per bead-step) / fused-kernel time; "
+                    "the kernel also runs the PES, RNG and thermostat on the SIMT pipes"}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
+            "ms_per_step": kernel_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "c1: mcmod_2dtest surface, P=128, 1024 traj x 16 lambda = 16384 rings "
+                                   "per GPU, Langevin, %d MD steps per bench step" % M,
+                       "precision": "FP32 forces/state, split-BF16 NM transform, FP64 estimator",
+                       "l2": "flushed (256 MB write) between timed steps", "form": args.form},
+            "roofline": roof, "clocks": clocks, "gpu_launches": 2 * K, "wall_s": wall,
+            "nan_rings": nan_rings}
+    line.update(extras)
+    if rank == 0 and not args.no_cpu:
+        v, cores, sample = cpu_reference_rate(c, ti, target_s=12.0)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+    if "e2e" not in line:
+        line["e2e"] = None
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if ws > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,220 @@
+/*
+ * pimdgpu.h -- C-ABI of the GB300 (sm_103a) ring-polymer library.
+ *
+ * Drop-in boundary for the ring-polymer hot path of pimd-tunneling: the PES
+ * module interface (mcmod_*.f90), the TI-PIMD propagation (verletmodule.f90),
+ * the ring-polymer-instanton action / gradient / Hessian and optimiser
+ * (instantonmod.f90) and the driver-level assembly (pimd_par.f90, rpi_ser.f90).
+ * Each entry point cites the reference routine it replaces.
+ *
+ * Conventions
+ *   - Every function returns PG_OK (0) or a PG_ERR_* code; pg_last_error()
+ *     returns the message of the last failure on the calling thread.
+ *   - Integers that the reference declares as default INTEGER are int64_t
+ *     (the reference builds with -i8); reals are double (-r8).
+ *   - One configuration x(ndim,natom) is x[dof], dof = atom*ndim + dim.
+ *     One ring x(P,ndim,natom) is x[dof*P + bead] (Fortran column-major, bead
+ *     fastest).  Batches of rings are ring-major: x[(ring*ndof + dof)*P + bead].
+ *   - Caller owns all host arrays.  The context owns its device memory and its
+ *     CUDA stream; calls are synchronous at return.  One host thread per context.
+ *   - There is no CPU fallback: a context cannot be created without a GPU.
+ */
+#ifndef PIMDGPU_H
+#define PIMDGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PG_OK 0
+#define PG_ERR_ARG 1        /* invalid argument or size */
+#define PG_ERR_CUDA 2       /* CUDA runtime failure */
+#define PG_ERR_STATE 3      /* call out of order (e.g. advance before setup) */
+#define PG_ERR_UNSUPPORTED 4
+#define PG_ERR_IO 5
+#define PG_ERR_NUMERIC 6    /* NaN / non-convergence reported by a kernel */
+
+/* PES identifiers (the mcmod_* module selected at build time in the reference). */
+#define PG_PES_1D 1        /* mcmod_1d.f90: quartic double well per coordinate */
+#define PG_PES_2DTEST 2    /* mcmod_2dtest.f90: 2-D ring of six Gaussian wells */
+#define PG_PES_SYNTH9 3    /* 9-atom Morse network + quartic proton-transfer well */
+#define PG_PES_SYNTH18 4   /* 18-atom flexible water hexamer (harmonic + LJ + charges) */
+#define PG_PES_HARMONIC 5  /* V = k/2 |x|^2, analytic test surface */
+
+/* Precision of the TI propagation. */
+#define PG_FP64 0          /* FP64 everywhere */
+#define PG_MIXED 1         /* FP32 forces/state, split-BF16 tensor-core NM transform
+                              where available, FP64 estimator accumulation */
+
+/* Execution form of the TI propagation. */
+#define PG_FORM_AUTO 0     /* fused persistent kernel; tensor-core variant when supported */
+#define PG_FORM_PLAIN 1    /* per-step kernel launches in the reference step order
+                              (10 NM transforms per Langevin step), FP64 only */
+#define PG_FORM_FUSED 2    /* fused persistent SIMT kernel (FP64 or FP32) */
+#define PG_FORM_TENSOR 3   /* fused persistent tcgen05 kernel (PG_MIXED only) */
+
+#define PG_ANDERSEN 1
+#define PG_LANGEVIN 2
+
+/* Ring status bits (pg_ti_get_results). */
+#define PG_RING_NAN 1
+#define PG_RING_TIMEOUT 2
+
+typedef struct pg_ctx pg_ctx;
+
+/* ---------------------------------------------------------------- context */
+int pg_create(pg_ctx **ctx, int32_t device);
+int pg_destroy(pg_ctx *ctx);
+const char *pg_last_error(void);
+int32_t pg_version(void);
+
+/* Module state of mcmod_mass: V_init + n/ndim/natom/mass/V0
+ * (mcmod_waterdimer.f90:1-17, pimd_par.f90:113-117,152-166). */
+int pg_set_system(pg_ctx *ctx, int64_t ndim, int64_t natom, const double *mass,
+                  int32_t pes_id, const double *params, int64_t nparams, double V0);
+
+/* ---------------------------------------------------------------- PES */
+/* Batched V / Vprime / potforce (mcmod_1d.f90:14-35, mcmod_2dtest.f90:29-61,
+ * mcmod_waterdimer.f90:60-81).  x[nconf*ndof]; V[nconf] and grad[nconf*ndof]
+ * may each be NULL.  precision: PG_FP64 or PG_MIXED (FP32 evaluation). */
+int pg_pes_eval(pg_ctx *ctx, int64_t nconf, const double *x, double *V, double *grad,
+                int32_t precision);
+/* Batched Vdoubleprime (mcmod_1d.f90:38-58, mcmod_2dtest.f90:64-102):
+ * hess[c*ndof*ndof + a + ndof*b] = d grad_b / d x_a.  quirks=1 reproduces the
+ * reference's mcmod_2dtest Hessian exactly (only the last well, its chain rule). */
+int pg_pes_hessian(pg_ctx *ctx, int64_t nconf, const double *x, double *hess, int32_t quirks);
+
+/* ---------------------------------------------------------------- normal modes */
+/* Batched fixed-end normal-mode transform out = T in, T_il = sqrt(2/(P+1))
+ * sin(pi i l/(P+1)) (init_nm / nmtransform_forward, verletmodule.f90:254-266,
+ * 306-338); T is symmetric and its own inverse, so this is also the backward
+ * transform.  in/out[ncol*P], column-major.  precision PG_MIXED runs the
+ * split-BF16 tcgen05 transform (P = 128) or FP32. */
+int pg_nm_transform(pg_ctx *ctx, int64_t P, int64_t ncol, const double *in, double *out,
+                    int32_t precision);
+
+/* ---------------------------------------------------------------- TI-PIMD */
+typedef struct pg_ti_config {
+    int64_t nbeads;      /* P (namelist n) */
+    double beta;         /* namelist beta; the ring uses betan = beta/(P+1) (pimd_par.f90:94) */
+    double dt;           /* namelist dt */
+    double tau;          /* namelist tau: NM mass scaling, all mode periods = 2 pi tau */
+    double gamma;        /* namelist gamma: c1 = exp(-gamma dt / tau) (verletmodule.f90:383) */
+    int32_t thermostat;  /* PG_ANDERSEN or PG_LANGEVIN (namelist thermostat) */
+    int32_t precision;   /* PG_FP64 or PG_MIXED */
+    int32_t form;        /* PG_FORM_* */
+    int32_t cayley;      /* namelist cayley */
+    int64_t imin;        /* namelist imin: estimator starts after imin steps */
+    int64_t noutput;     /* namelist Noutput: Andersen Poisson mean */
+    double dhdr_limit;   /* namelist dHdrlimit; < 0 disables */
+    double init_sigma;   /* Gaussian noise added to xref at (re)initialisation */
+} pg_ti_config;
+
+/* Set up a batch of rings (the task loop of pimd_par.f90:321-381, batched).
+ * Ring r uses endpoint row ring_lambda[r] of b/dbdl/xref, RNG key ring_seed[r]
+ * and stream id ring_stream[r].  a[ndof] is the fixed start point, b[nlambda*ndof]
+ * the ξ-dependent end points, dbdl[nlambda*ndof] their ξ-derivatives.
+ * Initial positions: x0 (nrings*ndof*P) if given, else xref[lambda] (nlambda*ndof*P)
+ * plus init_sigma N(0,1).  Initial momenta: p0 if given, else normal-mode Maxwell
+ * momenta (verletmodule.f90:102-115). */
+int pg_ti_setup(pg_ctx *ctx, const pg_ti_config *cfg, int64_t nrings, int64_t nlambda,
+                const int32_t *ring_lambda, const uint64_t *ring_seed,
+                const uint32_t *ring_stream, const double *a, const double *b,
+                const double *dbdl, const double *xref, const double *x0, const double *p0);
+/* Advance every ring by nsteps MD steps (the hot loop of propagate_pimd_pile /
+ * propagate_pimd_nm, verletmodule.f90:389-411 / 203-245).  Replays a captured
+ * CUDA graph when the same nsteps is requested again. */
+int pg_ti_advance(pg_ctx *ctx, int64_t nsteps);
+/* pg_ti_advance that also returns the device time of the launched work in
+ * milliseconds, measured with CUDA events recorded on the context's stream. */
+int pg_ti_advance_timed(pg_ctx *ctx, int64_t nsteps, double *device_ms);
+/* Cartesian positions and momenta of every ring (nrings*ndof*P each; either may be NULL). */
+int pg_ti_get_state(pg_ctx *ctx, double *x, double *p);
+/* Per-ring estimator sums: dhdr_sum[r] = sum of accepted contributions,
+ * nsamples[r] = steps past imin (the divisor of verletmodule.f90:413),
+ * nreinit[r] = dHdrlimit re-initialisations, status[r] = PG_RING_* bits.
+ * Any pointer may be NULL. */
+int pg_ti_get_results(pg_ctx *ctx, double *dhdr_sum, int64_t *nsamples, int64_t *nreinit,
+                      int32_t *status);
+/* Per-lambda reduction of integrand = dHdr/betan^2 over the rings of each lambda
+ * (pimd_par.f90:379, 401-409), on the device: mean[nlambda], var[nlambda]
+ * (E[I^2]-E[I]^2), count[nlambda]. */
+int pg_ti_lambda_reduce(pg_ctx *ctx, double *mean, double *var, int64_t *count);
+/* Global step counter of the batch (steps already taken). */
+int pg_ti_get_step(pg_ctx *ctx, int64_t *step);
+/* Bitwise checkpoint of the whole batch state (positions, momenta, estimator
+ * accumulators, RNG step counters); replaces write_restart / restart=2
+ * (verletmodule.f90:162-185, pimd_par.f90:331-370). */
+int pg_ti_checkpoint_save(pg_ctx *ctx, const char *path);
+int pg_ti_checkpoint_load(pg_ctx *ctx, const char *path);
+int pg_ti_release(pg_ctx *ctx);
+
+/* Drop-in for a batch of propagate_pimd_pile / propagate_pimd_nm calls
+ * (verletmodule.f90:372-416 / 190-250): ntask rings with end points b[task],
+ * dbdl[task]; x, p (ntask*ndof*P) in/out; dHdr[task] = averaged estimator
+ * (divided by nmc - imin, verletmodule.f90:413). */
+int pg_propagate_pimd(pg_ctx *ctx, const pg_ti_config *cfg, int64_t ntask, int64_t nmc,
+                      const double *a, const double *b, const double *dbdl,
+                      const uint64_t *seed, const uint32_t *stream, double *x, double *p,
+                      double *dHdr, int32_t *status);
+
+/* ---------------------------------------------------------------- TI host assembly */
+/* gauleg (verletmodule.f90:124-160). */
+int pg_gauleg(double x1, double x2, double *x, double *w, int64_t n);
+/* Natural cubic spline second derivatives (instantonmod.f90:397-442). */
+int pg_spline(const double *x, const double *y, int64_t n, double yp1, double ypn, double *y2);
+/* splint / splin_grad (instantonmod.f90:499-561). */
+int pg_splint(const double *xa, const double *ya, const double *y2a, int64_t n, double x,
+              double *y, double *dydx);
+/* Final TI assembly (pimd_par.f90:411-424): dA = sum w_i mean_i,
+ * sigmaA = sum w_i^2 var_i, qratio = exp(-dA*betan). */
+int pg_ti_assemble(int64_t nintegral, const double *weights, const double *mean,
+                   const double *var, double betan, double *dA, double *sigmaA,
+                   double *qratio);
+/* Tunnelling splitting from the fixed-end ratio q/q0 = tanh(beta Delta/2)
+ * (python_utils/multiwell_waterdimer.py:6-10). */
+int pg_splitting_from_ratio(double beta, double qratio, double *delta);
+
+/* ---------------------------------------------------------------- instanton */
+typedef struct pg_lbfgs_opts {
+    int32_t m;               /* history length (reference m = 8, instantonmod.f90:716) */
+    int32_t max_backtracks;  /* line-search backtrack cap (reference maxiter = 40) */
+    int64_t maxiter;         /* iteration cap */
+    double factr;            /* relative decrease tolerance factr*eps (reference 1e6) */
+    double pgtol;            /* gradient infinity-norm tolerance (reference eps2) */
+} pg_lbfgs_opts;
+
+/* Batched UMforceenergy over nbeta independent polymers (instantonmod.f90:17-151):
+ * x[nbeta*ndof*N], UM[nbeta], grad[nbeta*ndof*N] (either may be NULL);
+ * fixed ends a[ndof], b[nbeta*ndof]; betan[nbeta]. */
+int pg_instanton_fg(pg_ctx *ctx, int64_t nbeta, int64_t N, const double *x, const double *a,
+                    const double *b, const double *betan, double *UM, double *grad);
+/* Batched instanton optimisation (instantonmod.f90:679-777) by an on-device FP64
+ * L-BFGS driven by the adjoint gradient; x in/out; UM[nbeta], niter[nbeta],
+ * status[nbeta] (0 converged, 1 iteration cap, 2 line-search failure). */
+int pg_instanton_optimize(pg_ctx *ctx, int64_t nbeta, int64_t N, double *x, const double *a,
+                          const double *b, const double *betan, const pg_lbfgs_opts *opts,
+                          double *UM, int64_t *niter, int32_t *status);
+/* UMhessian in LAPACK lower band storage (instantonmod.f90:155-217):
+ * band[(ndof+1) * N*ndof], column-major.  quirks=1 reproduces the reference's
+ * spring-coupling placement (no bead 1-2 coupling) and mcmod_2dtest Hessian. */
+int pg_um_hessian(pg_ctx *ctx, int64_t N, double betan, const double *x, int32_t singlewell,
+                  int32_t quirks, double *band);
+/* detJ + the log-sum of rpi_ser.f90:222-237, 354-366 over nbeta polymers:
+ * lndet[k] = sum over eigenvalues eta^2 > 0 of log eta^2 of the mass-weighted
+ * Hessian, skipping the lowest eigenvalue when skip_lowest.  eta2_min[k] = lowest
+ * eigenvalue, nskipped[k] = number of eigenvalues left out. */
+int pg_instanton_logdet(pg_ctx *ctx, int64_t nbeta, int64_t N, const double *x,
+                        const double *betan, int32_t singlewell, int32_t skip_lowest,
+                        int32_t quirks, double *lndet, double *eta2_min, int64_t *nskipped);
+/* RPI assembly (rpi_ser.f90:368-381): S = betan*UM, Gamma = exp((lndetJ-lndetJ0)/2),
+ * omega = betan exp(-S) sqrt(S/2pi)/Gamma, delta = 2 omega/betan. */
+int pg_rpi_assemble(double betan, double UM, double lndetJ, double lndetJ0, double *S,
+                    double *omega, double *delta);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

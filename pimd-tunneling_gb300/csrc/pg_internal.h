@@ -1,0 +1,124 @@
+// pg_internal.h -- context layout and helpers shared by the library's translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/pimdgpu.h"
+#include "pg_device.cuh"
+
+namespace pg {
+
+void set_error(const std::string &msg);
+int fail(int code, const std::string &msg);
+int cuda_fail(cudaError_t e, const char *what);
+
+#define PG_CUDA(call)                                     \
+    do {                                                  \
+        cudaError_t _e = (call);                          \
+        if (_e != cudaSuccess) return cuda_fail(_e, #call); \
+    } while (0)
+
+// Device buffer owned by a context.
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    ~DevBuf() { release(); }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+    cudaError_t ensure(size_t nbytes) {
+        if (nbytes <= bytes && ptr) return cudaSuccess;
+        release();
+        cudaError_t e = cudaMalloc(&ptr, nbytes > 0 ? nbytes : 16);
+        if (e == cudaSuccess) bytes = nbytes;
+        return e;
+    }
+    template <typename T> T *as() const { return reinterpret_cast<T *>(ptr); }
+};
+
+// Per-ring accumulator and scalar state (FP64 estimator accumulation).
+struct RingAcc {
+    double dhdr_sum;
+    int64_t nsamples;
+    int64_t nreinit;
+    int64_t and_count;
+    int64_t and_rkick;
+    int32_t status;
+    int32_t pad;
+};
+
+// Per (atom, mode) constants of the normal-mode propagator.
+struct ModeCoef {
+    double rA, rB, rC, rD;  // half-step rotation [pi'; q'] = [rA rB; rC rD] [pi; q]
+    double ou_a;            // c1^2
+    double ou_s;            // sqrt(beadmass/betan) c2 sqrt(1 + c1^2)
+    double pscale;          // sqrt(beadmass/betan): NM Maxwell momentum scale
+    double bm;              // beadmass
+};
+
+struct TiState {
+    pg_ti_config cfg{};
+    int64_t nrings = 0, nlambda = 0;
+    int P = 0, nd = 0;
+    double betan = 0.0;
+    int64_t step = 0;
+    int form = 0;            // resolved PG_FORM_*
+    bool fp32 = false;       // state held in FP32
+    DevBuf q, pi, x, f;      // ring state (fused: NM q/pi + Cartesian x; plain: x/p in x/pi)
+    DevBuf T;                // P*P FP64 transform (reference values)
+    DevBuf Tbf;              // split-BF16 transform for the tensor-core kernel
+    DevBuf sintab;           // 2P+2 scaled sine table, FP64
+    DevBuf coef;             // natom*P ModeCoef
+    DevBuf bv;               // nlambda*nd*P endpoint shifts (beadvec)
+    DevBuf dbdl;             // nlambda*nd
+    DevBuf xref;             // nlambda*nd*P
+    DevBuf ringlam, ringseed, ringstream;
+    DevBuf acc;              // nrings RingAcc
+    DevBuf red;              // reduction output
+    std::map<int64_t, cudaGraphExec_t> graphs;
+    ~TiState();
+};
+
+}  // namespace pg
+
+struct pg_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int sm_count = 0;
+    // system (mcmod_mass module state)
+    bool have_system = false;
+    int ndim = 0, natom = 0, nd = 0, pes_id = 0;
+    double V0 = 0.0;
+    std::vector<double> mass, params;
+    pg::DevBuf d_params, d_mass;
+    pg::DevBuf scratch_a, scratch_b, scratch_c, scratch_d;
+    pg::TiState *ti = nullptr;
+    pg::PesArgs pes_args() const {
+        pg::PesArgs pa;
+        pa.id = pes_id;
+        pa.ndim = ndim;
+        pa.natom = natom;
+        pa.nd = nd;
+        pa.nparams = (int)params.size();
+        pa.V0 = V0;
+        pa.params = d_params.as<double>();
+        return pa;
+    }
+};
+
+namespace pg {
+int check_ctx(pg_ctx *ctx, bool need_system);
+// Launchers implemented in pg_ti.cu / pg_tc.cu / pg_instanton.cu.
+int ti_release(pg_ctx *ctx);
+int tc_built();
+int tc_supported(const TiState &st, const pg_ctx &ctx);
+int tc_prepare(pg_ctx *ctx, TiState &st);
+int tc_launch(pg_ctx *ctx, TiState &st, int64_t step0, int64_t nsteps, cudaStream_t s);
+int tc_nm_transform(pg_ctx *ctx, int64_t P, int64_t ncol, const double *in, double *out);
+}  // namespace pg

@@ -1,0 +1,1142 @@
+// pg_ti.cu -- TI-PIMD propagation on the GPU.
+//
+//  * Fused persistent SIMT kernel (FP64 or FP32 state): one CTA per ring runs
+//    many MD steps in one launch.  The state is held in normal-mode space
+//    (q = T x - beadvec, pi = T p), so a Langevin step needs two transforms
+//    (T F for the kick, T (q + beadvec) for the positions) instead of the
+//    reference's ten (verletmodule.f90:423-435, 494-561, 634-667); T is
+//    symmetric and its own inverse, so both orders give the same dynamics in
+//    exact arithmetic.
+//  * Plain form (FP64): per-step kernel launches in the reference step order
+//    with ten transforms per Langevin step -- the "plain FP64" denominator.
+//  * Device-side per-lambda reduction of the TI integrand (pimd_par.f90:379,
+//    401-409) and bitwise checkpoint / restart.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "pg_internal.h"
+
+namespace pg {
+
+void build_transmatrix(int P, std::vector<double> &T);
+
+TiState::~TiState() {
+    for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+    graphs.clear();
+}
+
+// ---------------------------------------------------------------- device params
+struct TiArgs {
+    PesArgs pes;
+    int P, nd, ndim, natom;
+    int64_t nrings;
+    double dt, betan;
+    int64_t imin;
+    double noutput;
+    double dhdr_limit, init_sigma;
+    const double *mass;       // natom
+    const ModeCoef *coef;     // natom*P
+    const double *T;          // P*P FP64
+    const float *Tf;          // P*P FP32 copy
+    const double *bv;         // nlambda*nd*P
+    const double *dbdl;       // nlambda*nd
+    const double *xref;       // nlambda*nd*P
+    const int32_t *ringlam;
+    const uint64_t *ringseed;
+    const uint32_t *ringstream;
+    RingAcc *acc;
+    const int64_t *step_dev;  // global step counter (device)
+};
+
+template <typename R> __device__ __forceinline__ const R *tmat(const TiArgs &a);
+template <> __device__ __forceinline__ const double *tmat<double>(const TiArgs &a) { return a.T; }
+template <> __device__ __forceinline__ const float *tmat<float>(const TiArgs &a) { return a.Tf; }
+
+template <typename R> __device__ __forceinline__ bool is_nan(R v) { return v != v; }
+
+// ---------------------------------------------------------------- fused kernel helpers
+// out[dof][i] = sum_k T[k][i] * (in[dof][k] + sh[dof][k])  for all (dof, i) of one ring.
+template <typename R>
+__device__ __forceinline__ void ring_matvec(const TiArgs &a, const R *__restrict__ in,
+                                            const double *__restrict__ sh, R *__restrict__ out,
+                                            R *__restrict__ sbuf) {
+    const R *T = tmat<R>(a);
+    const int P = a.P;
+    for (int dof = 0; dof < a.nd; dof++) {
+        for (int k = threadIdx.x; k < P; k += blockDim.x)
+            sbuf[k] = sh ? (R)((double)in[dof * P + k] + sh[dof * P + k]) : in[dof * P + k];
+        __syncthreads();
+        for (int i = threadIdx.x; i < P; i += blockDim.x) {
+            R s = 0;
+            for (int k = 0; k < P; k++) s += T[(size_t)k * P + i] * sbuf[k];
+            out[dof * P + i] = s;
+        }
+        __syncthreads();
+    }
+}
+
+// FP64 path: match the CPU restatement's (q + beadvec) arithmetic exactly.
+template <>
+__device__ __forceinline__ void ring_matvec<double>(const TiArgs &a, const double *__restrict__ in,
+                                                    const double *__restrict__ sh,
+                                                    double *__restrict__ out,
+                                                    double *__restrict__ sbuf) {
+    const double *T = a.T;
+    const int P = a.P;
+    for (int dof = 0; dof < a.nd; dof++) {
+        for (int k = threadIdx.x; k < P; k += blockDim.x)
+            sbuf[k] = sh ? in[dof * P + k] + sh[dof * P + k] : in[dof * P + k];
+        __syncthreads();
+        for (int i = threadIdx.x; i < P; i += blockDim.x) {
+            double s = 0.0;
+            for (int k = 0; k < P; k++) s += T[(size_t)k * P + i] * sbuf[k];
+            out[dof * P + i] = s;
+        }
+        __syncthreads();
+    }
+}
+
+template <typename R>
+__device__ __forceinline__ void ring_forces(const TiArgs &a, const R *__restrict__ x,
+                                            R *__restrict__ f) {
+    const int P = a.P;
+    for (int i = threadIdx.x; i < P; i += blockDim.x) {
+        R xb[kMaxDof], gb[kMaxDof];
+        for (int d = 0; d < a.nd; d++) xb[d] = x[d * P + i];
+        pes_vgrad<R>(a.pes, xb, gb);
+        for (int d = 0; d < a.nd; d++) f[d * P + i] = gb[d];
+    }
+}
+
+// Half-step free-polymer rotation of every normal mode of one ring.
+template <typename R>
+__device__ __forceinline__ void ring_rotate(const TiArgs &a, R *__restrict__ q, R *__restrict__ pi) {
+    const int P = a.P;
+    for (int e = threadIdx.x; e < a.nd * P; e += blockDim.x) {
+        int dof = e / P, k = e - dof * P;
+        const ModeCoef &c = a.coef[(dof / a.ndim) + a.natom * k];
+        R pv = pi[e], qv = q[e];
+        pi[e] = (R)c.rA * pv + (R)c.rB * qv;
+        q[e] = (R)c.rC * pv + (R)c.rD * qv;
+    }
+}
+
+// Ring (re)initialisation: x = xref + sigma N, pi = pscale N, q = T x - beadvec.
+template <typename R>
+__device__ void ring_init_state(const TiArgs &a, int64_t r, uint32_t step, uint32_t px,
+                                uint32_t pp, R *x, R *q, R *pi, R *sbuf, bool use_x,
+                                bool use_p) {
+    const int P = a.P;
+    const int lam = a.ringlam[r];
+    const uint64_t seed = a.ringseed[r];
+    const uint32_t stream = a.ringstream[r];
+    if (use_x) {
+        for (int e = threadIdx.x; e < a.nd * P; e += blockDim.x) {
+            double z = a.init_sigma != 0.0 ? normal_d(seed, stream, step, px, (uint32_t)e) : 0.0;
+            x[e] = (R)(a.xref[(size_t)lam * a.nd * P + e] + a.init_sigma * z);
+        }
+    }
+    if (use_p) {
+        for (int e = threadIdx.x; e < a.nd * P; e += blockDim.x) {
+            int dof = e / P, k = e - dof * P;
+            double z = normal_d(seed, stream, step, pp, (uint32_t)e);
+            pi[e] = (R)(z * sqrt(1.0 / a.betan) * sqrt(a.coef[(dof / a.ndim) + a.natom * k].bm));
+        }
+    }
+    __syncthreads();
+    // q = T x - beadvec
+    ring_matvec<R>(a, x, nullptr, q, sbuf);
+    const double *bv = a.bv + (size_t)lam * a.nd * P;
+    for (int e = threadIdx.x; e < a.nd * P; e += blockDim.x) q[e] = (R)((double)q[e] - bv[e]);
+    __syncthreads();
+}
+
+__device__ __forceinline__ double ring_contr(const TiArgs &a, const double *dbdl, double xlast,
+                                             int dof) {
+    return a.mass[dof / a.ndim] * (-xlast) * dbdl[dof];
+}
+
+// ---------------------------------------------------------------- fused kernel
+// One CTA per ring; nsteps MD steps per launch.  THERMO: 1 Andersen, 2 Langevin.
+template <typename R, int THERMO>
+__global__ void __launch_bounds__(128) k_ti_fused(TiArgs a, R *__restrict__ gq, R *__restrict__ gpi,
+                                                  R *__restrict__ gx, R *__restrict__ gf,
+                                                  int64_t nsteps) {
+    extern __shared__ unsigned char smem_raw[];
+    R *sbuf = reinterpret_cast<R *>(smem_raw);
+    __shared__ int s_flag;
+    __shared__ int s_kick;
+    const int64_t r = blockIdx.x;
+    if (r >= a.nrings) return;
+    const int P = a.P, nd = a.nd;
+    const size_t off = (size_t)r * nd * P;
+    R *q = gq + off, *pi = gpi + off, *x = gx + off, *f = gf + off;
+    const int lam = a.ringlam[r];
+    const double *bv = a.bv + (size_t)lam * nd * P;
+    const double *dbdl = a.dbdl + (size_t)lam * nd;
+    const uint64_t seed = a.ringseed[r];
+    const uint32_t stream = a.ringstream[r];
+    RingAcc acc = a.acc[r];
+    const int64_t step0 = *a.step_dev;
+    const R dt = (R)a.dt;
+    if (acc.status) return;  // a ring that saw a NaN stays frozen
+    for (int64_t s = step0; s < step0 + nsteps; s++) {
+        const uint32_t st = (uint32_t)s;
+        if (THERMO == 2) {
+            // kick: pi -= dt T grad V(x)
+            ring_forces<R>(a, x, f);
+            __syncthreads();
+            ring_matvec<R>(a, f, nullptr, f, sbuf);  // f <- T f (in place through sbuf per dof)
+            if (threadIdx.x == 0) s_flag = 0;
+            __syncthreads();
+            for (int e = threadIdx.x; e < nd * P; e += blockDim.x) {
+                int dof = e / P, k = e - dof * P;
+                const ModeCoef &c = a.coef[(dof / a.ndim) + a.natom * k];
+                R pv = pi[e] - dt * f[e];
+                R qv = q[e];
+                // rotate dt/2
+                R p1 = (R)c.rA * pv + (R)c.rB * qv;
+                R q1 = (R)c.rC * pv + (R)c.rD * qv;
+                // OU (verletmodule.f90:651-652)
+                R z = normal_r<R>(seed, stream, st, kRngLangevin, (uint32_t)e);
+                p1 = (R)c.ou_a * p1 + (R)c.ou_s * z;
+                // rotate dt/2
+                pi[e] = (R)c.rA * p1 + (R)c.rB * q1;
+                q[e] = (R)c.rC * p1 + (R)c.rD * q1;
+                if (is_nan(pi[e])) s_flag = 1;
+            }
+            __syncthreads();
+        } else {
+            // Andersen schedule (verletmodule.f90:204-234)
+            if (threadIdx.x == 0) {
+                acc.and_count += 1;
+                s_kick = acc.and_count >= acc.and_rkick;
+                if (s_kick) {
+                    acc.and_count = 0;
+                    acc.and_rkick = poisson_d(seed, stream, st, kRngPoisson, a.noutput);
+                }
+                s_flag = 0;
+            }
+            __syncthreads();
+            if (s_kick) {
+                for (int e = threadIdx.x; e < nd * P; e += blockDim.x) {
+                    int dof = e / P, k = e - dof * P;
+                    double z = normal_d(seed, stream, st, kRngAndersen, (uint32_t)e);
+                    pi[e] = (R)(z * sqrt(1.0 / a.betan) * sqrt(a.coef[(dof / a.ndim) + a.natom * k].bm));
+                }
+                __syncthreads();
+            }
+            ring_rotate<R>(a, q, pi);
+            __syncthreads();
+            ring_matvec<R>(a, q, bv, x, sbuf);
+            ring_forces<R>(a, x, f);
+            __syncthreads();
+            ring_matvec<R>(a, f, nullptr, f, sbuf);
+            for (int e = threadIdx.x; e < nd * P; e += blockDim.x) {
+                pi[e] = pi[e] - dt * f[e];
+                if (is_nan(pi[e])) s_flag = 1;
+            }
+            __syncthreads();
+            ring_rotate<R>(a, q, pi);
+            __syncthreads();
+        }
+        // positions x = T (q + beadvec)
+        ring_matvec<R>(a, q, bv, x, sbuf);
+        if (s_flag) {
+            if (threadIdx.x == 0) acc.status |= PG_RING_NAN;
+            break;
+        }
+        // estimator (verletmodule.f90:397-409), FP64 accumulation
+        if (s >= a.imin) {
+            if (threadIdx.x == 0) {
+                double contr = 0.0;  // same summation order as verletmodule.f90:399-403
+                for (int j = 0; j < a.ndim; j++)
+                    for (int k = 0; k < a.natom; k++) {
+                        int dof = k * a.ndim + j;
+                        contr = contr + ring_contr(a, dbdl, (double)x[dof * P + (P - 1)], dof);
+                    }
+                acc.nsamples += 1;
+                if (THERMO != 2 || fabs(contr) < a.dhdr_limit || a.dhdr_limit < 0.0) {
+                    acc.dhdr_sum += contr;
+                    s_flag = 0;
+                } else {
+                    acc.nreinit += 1;
+                    s_flag = 2;
+                }
+            }
+            __syncthreads();
+            if (s_flag == 2) {
+                ring_init_state<R>(a, r, st, kRngReinitX, kRngReinitP, x, q, pi, sbuf, true, true);
+                if (threadIdx.x == 0) s_flag = 0;
+                __syncthreads();
+            }
+        }
+    }
+    if (threadIdx.x == 0) a.acc[r] = acc;
+}
+
+// Initial state: x from x0 or xref + noise, momenta from p0 or NM Maxwell.
+template <typename R>
+__global__ void k_ti_init(TiArgs a, R *__restrict__ gq, R *__restrict__ gpi, R *__restrict__ gx,
+                          const double *__restrict__ x0, const double *__restrict__ p0) {
+    extern __shared__ unsigned char smem_raw[];
+    R *sbuf = reinterpret_cast<R *>(smem_raw);
+    const int64_t r = blockIdx.x;
+    if (r >= a.nrings) return;
+    const int P = a.P, nd = a.nd;
+    const size_t off = (size_t)r * nd * P;
+    R *q = gq + off, *pi = gpi + off, *x = gx + off;
+    if (x0)
+        for (int e = threadIdx.x; e < nd * P; e += blockDim.x) x[e] = (R)x0[off + e];
+    if (p0)
+        for (int e = threadIdx.x; e < nd * P; e += blockDim.x) pi[e] = (R)p0[off + e];
+    __syncthreads();
+    ring_init_state<R>(a, r, 0u, kRngInitX, kRngInitP, x, q, pi, sbuf, x0 == nullptr, p0 == nullptr);
+    if (p0) {
+        // pi = T p0 (the momenta were given in Cartesian form)
+        ring_matvec<R>(a, pi, nullptr, pi, sbuf);
+    }
+    if (threadIdx.x == 0) {
+        RingAcc z;
+        z.dhdr_sum = 0.0;
+        z.nsamples = 0;
+        z.nreinit = 0;
+        z.and_count = 0;
+        z.and_rkick = poisson_d(a.ringseed[r], a.ringstream[r], 0u, kRngPoisson0, a.noutput);
+        z.status = 0;
+        z.pad = 0;
+        a.acc[r] = z;
+    }
+}
+
+// Cartesian momenta p = T pi (state read-out).
+template <typename R>
+__global__ void k_ti_momenta(TiArgs a, const R *__restrict__ gpi, double *__restrict__ pout) {
+    extern __shared__ unsigned char smem_raw[];
+    R *sbuf = reinterpret_cast<R *>(smem_raw);
+    const int64_t r = blockIdx.x;
+    if (r >= a.nrings) return;
+    const int P = a.P, nd = a.nd;
+    const size_t off = (size_t)r * nd * P;
+    const R *T = tmat<R>(a);
+    for (int dof = 0; dof < nd; dof++) {
+        for (int k = threadIdx.x; k < P; k += blockDim.x) sbuf[k] = gpi[off + dof * P + k];
+        __syncthreads();
+        for (int i = threadIdx.x; i < P; i += blockDim.x) {
+            R s = 0;
+            for (int k = 0; k < P; k++) s += T[(size_t)k * P + i] * sbuf[k];
+            pout[off + dof * P + i] = (double)s;
+        }
+        __syncthreads();
+    }
+}
+
+template <typename R>
+__global__ void k_to_double(const R *__restrict__ in, double *__restrict__ out, size_t n) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (double)in[i];
+}
+
+__global__ void k_step_add(int64_t *step_dev, int64_t n) { *step_dev += n; }
+
+// ---------------------------------------------------------------- plain form (FP64)
+// State: x (Cartesian positions), p (Cartesian momenta); scratch wq, wp.
+// step_v: p -= dt grad V(x) (verletmodule.f90:565-585); one thread per (ring, bead).
+__global__ void k_plain_kick(TiArgs a, const double *__restrict__ x, double *__restrict__ p,
+                             double t) {
+    int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int64_t r = idx / a.P;
+    int i = (int)(idx - r * a.P);
+    if (r >= a.nrings) return;
+    if (a.acc[r].status) return;
+    const size_t off = (size_t)r * a.nd * a.P;
+    double xb[kMaxDof], gb[kMaxDof];
+    for (int d = 0; d < a.nd; d++) xb[d] = x[off + d * a.P + i];
+    pes_vgrad<double>(a.pes, xb, gb);
+    bool bad = false;
+    for (int d = 0; d < a.nd; d++) {
+        double v = p[off + d * a.P + i] - gb[d] * t;
+        p[off + d * a.P + i] = v;
+        bad |= (v != v);
+    }
+    if (bad) atomicOr(&a.acc[r].status, PG_RING_NAN);
+}
+
+// One dense symmetric matvec per dof, as dsymv (verletmodule.f90:254-286).
+__device__ __forceinline__ void plain_mv(const TiArgs &a, const double *__restrict__ in,
+                                         const double *__restrict__ sh, double sgn,
+                                         double *__restrict__ out, double *sbuf) {
+    const int P = a.P;
+    for (int dof = 0; dof < a.nd; dof++) {
+        for (int k = threadIdx.x; k < P; k += blockDim.x) sbuf[k] = in[dof * P + k];
+        __syncthreads();
+        for (int i = threadIdx.x; i < P; i += blockDim.x) {
+            double s = 0.0;
+            for (int k = 0; k < P; k++) s += a.T[(size_t)k * P + i] * sbuf[k];
+            out[dof * P + i] = sh ? s + sgn * sh[dof * P + i] : s;
+        }
+        __syncthreads();
+    }
+}
+
+// step_nm (verletmodule.f90:494-561): forward transforms, rotation, backward transforms.
+__global__ void k_plain_nm(TiArgs a, double *__restrict__ gx, double *__restrict__ gp,
+                           double *__restrict__ gq, double *__restrict__ gw) {
+    extern __shared__ double sb[];
+    const int64_t r = blockIdx.x;
+    if (r >= a.nrings || a.acc[r].status) return;
+    const int P = a.P, nd = a.nd;
+    const size_t off = (size_t)r * nd * P;
+    double *x = gx + off, *p = gp + off, *q = gq + off, *w = gw + off;
+    const double *bv = a.bv + (size_t)a.ringlam[r] * nd * P;
+    plain_mv(a, p, nullptr, 0.0, w, sb);   // pip = T p
+    plain_mv(a, x, bv, -1.0, q, sb);       // q = T x - beadvec
+    bool bad = false;
+    for (int e = threadIdx.x; e < nd * P; e += blockDim.x) {
+        int dof = e / P, k = e - dof * P;
+        const ModeCoef &c = a.coef[(dof / a.ndim) + a.natom * k];
+        double pv = w[e], qv = q[e];
+        double np = c.rA * pv + c.rB * qv;
+        double nq = c.rC * pv + c.rD * qv;
+        w[e] = np;
+        q[e] = nq;
+        bad |= (np != np);
+    }
+    if (bad) atomicOr(&a.acc[r].status, PG_RING_NAN);
+    __syncthreads();
+    plain_mv(a, w, nullptr, 0.0, p, sb);   // p = T pip
+    // x = T (q + beadvec)
+    for (int e = threadIdx.x; e < nd * P; e += blockDim.x) q[e] = q[e] + bv[e];
+    __syncthreads();
+    plain_mv(a, q, nullptr, 0.0, x, sb);
+}
+
+// step_langevin (verletmodule.f90:634-667).
+__global__ void k_plain_langevin(TiArgs a, double *__restrict__ gp, double *__restrict__ gw) {
+    extern __shared__ double sb[];
+    const int64_t r = blockIdx.x;
+    if (r >= a.nrings || a.acc[r].status) return;
+    const int P = a.P, nd = a.nd;
+    const size_t off = (size_t)r * nd * P;
+    double *p = gp + off, *w = gw + off;
+    const uint32_t st = (uint32_t)(*a.step_dev);
+    plain_mv(a, p, nullptr, 0.0, w, sb);
+    for (int e = threadIdx.x; e < nd * P; e += blockDim.x) {
+        int dof = e / P, k = e - dof * P;
+        const ModeCoef &c = a.coef[(dof / a.ndim) + a.natom * k];
+        double z = normal_d(a.ringseed[r], a.ringstream[r], st, kRngLangevin, (uint32_t)e);
+        w[e] = c.ou_a * w[e] + c.ou_s * z;
+    }
+    __syncthreads();
+    plain_mv(a, w, nullptr, 0.0, p, sb);
+}
+
+// Andersen resampling check (verletmodule.f90:204-234) for the plain form.
+__global__ void k_plain_andersen(TiArgs a, double *__restrict__ gp, double *__restrict__ gw) {
+    extern __shared__ double sb[];
+    __shared__ int s_kick;
+    const int64_t r = blockIdx.x;
+    if (r >= a.nrings || a.acc[r].status) return;
+    const int P = a.P, nd = a.nd;
+    const size_t off = (size_t)r * nd * P;
+    const uint32_t st = (uint32_t)(*a.step_dev);
+    if (threadIdx.x == 0) {
+        RingAcc &acc = a.acc[r];
+        acc.and_count += 1;
+        s_kick = acc.and_count >= acc.and_rkick;
+        if (s_kick) {
+            acc.and_count = 0;
+            acc.and_rkick = poisson_d(a.ringseed[r], a.ringstream[r], st, kRngPoisson, a.noutput);
+        }
+    }
+    __syncthreads();
+    if (!s_kick) return;
+    double *w = gw + off;
+    for (int e = threadIdx.x; e < nd * P; e += blockDim.x) {
+        int dof = e / P, k = e - dof * P;
+        double z = normal_d(a.ringseed[r], a.ringstream[r], st, kRngAndersen, (uint32_t)e);
+        w[e] = z * sqrt(1.0 / a.betan) * sqrt(a.coef[(dof / a.ndim) + a.natom * k].bm);
+    }
+    __syncthreads();
+    plain_mv(a, w, nullptr, 0.0, gp + off, sb);
+}
+
+// Estimator + dHdrlimit re-initialisation (verletmodule.f90:397-409) for the plain form.
+__global__ void k_plain_estimator(TiArgs a, int thermo, double *__restrict__ gx,
+                                  double *__restrict__ gp, double *__restrict__ gw) {
+    extern __shared__ double sb[];
+    __shared__ int s_re;
+    const int64_t r = blockIdx.x;
+    if (r >= a.nrings || a.acc[r].status) return;
+    const int P = a.P, nd = a.nd;
+    const size_t off = (size_t)r * nd * P;
+    const int64_t s = *a.step_dev;
+    if (s < a.imin) return;
+    const int lam = a.ringlam[r];
+    const double *dbdl = a.dbdl + (size_t)lam * nd;
+    if (threadIdx.x == 0) {
+        RingAcc &acc = a.acc[r];
+        double contr = 0.0;
+        for (int j = 0; j < a.ndim; j++)
+            for (int k = 0; k < a.natom; k++) {
+                int dof = k * a.ndim + j;
+                contr = contr + ring_contr(a, dbdl, gx[off + dof * P + P - 1], dof);
+            }
+        acc.nsamples += 1;
+        s_re = 0;
+        if (thermo != 2 || fabs(contr) < a.dhdr_limit || a.dhdr_limit < 0.0) {
+            acc.dhdr_sum += contr;
+        } else {
+            acc.nreinit += 1;
+            s_re = 1;
+        }
+    }
+    __syncthreads();
+    if (!s_re) return;
+    const uint32_t st = (uint32_t)s;
+    const uint64_t seed = a.ringseed[r];
+    const uint32_t stream = a.ringstream[r];
+    double *w = gw + off;
+    for (int e = threadIdx.x; e < nd * P; e += blockDim.x) {
+        int dof = e / P, k = e - dof * P;
+        double zx = a.init_sigma != 0.0 ? normal_d(seed, stream, st, kRngReinitX, (uint32_t)e) : 0.0;
+        gx[off + e] = a.xref[(size_t)lam * nd * P + e] + a.init_sigma * zx;
+        double z = normal_d(seed, stream, st, kRngReinitP, (uint32_t)e);
+        w[e] = z * sqrt(1.0 / a.betan) * sqrt(a.coef[(dof / a.ndim) + a.natom * k].bm);
+    }
+    __syncthreads();
+    plain_mv(a, w, nullptr, 0.0, gp + off, sb);
+}
+
+// Plain-form initial state: x, p Cartesian.
+__global__ void k_plain_init(TiArgs a, double *__restrict__ gx, double *__restrict__ gp,
+                             double *__restrict__ gw, const double *__restrict__ x0,
+                             const double *__restrict__ p0) {
+    extern __shared__ double sb[];
+    const int64_t r = blockIdx.x;
+    if (r >= a.nrings) return;
+    const int P = a.P, nd = a.nd;
+    const size_t off = (size_t)r * nd * P;
+    const int lam = a.ringlam[r];
+    const uint64_t seed = a.ringseed[r];
+    const uint32_t stream = a.ringstream[r];
+    for (int e = threadIdx.x; e < nd * P; e += blockDim.x) {
+        if (x0) {
+            gx[off + e] = x0[off + e];
+        } else {
+            double z = a.init_sigma != 0.0 ? normal_d(seed, stream, 0u, kRngInitX, (uint32_t)e) : 0.0;
+            gx[off + e] = a.xref[(size_t)lam * nd * P + e] + a.init_sigma * z;
+        }
+        if (p0) {
+            gp[off + e] = p0[off + e];
+        } else {
+            int dof = e / P, k = e - dof * P;
+            double z = normal_d(seed, stream, 0u, kRngInitP, (uint32_t)e);
+            gw[off + e] = z * sqrt(1.0 / a.betan) * sqrt(a.coef[(dof / a.ndim) + a.natom * k].bm);
+        }
+    }
+    __syncthreads();
+    if (!p0) plain_mv(a, gw + off, nullptr, 0.0, gp + off, sb);
+    if (threadIdx.x == 0) {
+        RingAcc z;
+        z.dhdr_sum = 0.0;
+        z.nsamples = 0;
+        z.nreinit = 0;
+        z.and_count = 0;
+        z.and_rkick = poisson_d(seed, stream, 0u, kRngPoisson0, a.noutput);
+        z.status = 0;
+        z.pad = 0;
+        a.acc[r] = z;
+    }
+}
+
+// ---------------------------------------------------------------- K4 reduction
+// Per lambda: mean / variance of integrand = dhdr_sum/nsamples/betan^2 over its
+// rings (pimd_par.f90:379, 401-409).  One CTA per lambda, warp shuffles.
+__global__ void k_lambda_reduce(const RingAcc *__restrict__ acc, const int32_t *__restrict__ ringlam,
+                                int64_t nrings, double betan, double *__restrict__ out) {
+    const int lam = blockIdx.x;
+    double s = 0.0, s2 = 0.0, n = 0.0;
+    for (int64_t r = threadIdx.x; r < nrings; r += blockDim.x) {
+        if (ringlam[r] != lam) continue;
+        double ns = (double)acc[r].nsamples;
+        double v = ns > 0.0 ? acc[r].dhdr_sum / ns / (betan * betan) : 0.0;
+        s += v;
+        s2 += v * v;
+        n += 1.0;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        s += __shfl_xor_sync(0xffffffffu, s, o);
+        s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+        n += __shfl_xor_sync(0xffffffffu, n, o);
+    }
+    __shared__ double sh[3][32];
+    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) {
+        sh[0][w] = s;
+        sh[1][w] = s2;
+        sh[2][w] = n;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double S = 0, S2 = 0, N = 0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++) {
+            S += sh[0][i];
+            S2 += sh[1][i];
+            N += sh[2][i];
+        }
+        double mean = N > 0 ? S / N : 0.0;
+        double var = N > 0 ? S2 / N - mean * mean : 0.0;
+        out[3 * lam + 0] = mean;
+        out[3 * lam + 1] = var;
+        out[3 * lam + 2] = N;
+    }
+}
+
+// ---------------------------------------------------------------- host side
+static TiArgs make_args(pg_ctx *ctx, TiState &st, int64_t *step_dev) {
+    TiArgs a;
+    a.pes = ctx->pes_args();
+    a.P = st.P;
+    a.nd = st.nd;
+    a.ndim = ctx->ndim;
+    a.natom = ctx->natom;
+    a.nrings = st.nrings;
+    a.dt = st.cfg.dt;
+    a.betan = st.betan;
+    a.imin = st.cfg.imin;
+    a.noutput = (double)st.cfg.noutput;
+    a.dhdr_limit = st.cfg.dhdr_limit;
+    a.init_sigma = st.cfg.init_sigma;
+    a.mass = ctx->d_mass.as<double>();
+    a.coef = st.coef.as<ModeCoef>();
+    a.T = st.T.as<double>();
+    a.Tf = reinterpret_cast<const float *>(st.T.as<double>() + (size_t)st.P * st.P);
+    a.bv = st.bv.as<double>();
+    a.dbdl = st.dbdl.as<double>();
+    a.xref = st.xref.as<double>();
+    a.ringlam = st.ringlam.as<int32_t>();
+    a.ringseed = st.ringseed.as<uint64_t>();
+    a.ringstream = st.ringstream.as<uint32_t>();
+    a.acc = st.acc.as<RingAcc>();
+    a.step_dev = step_dev;
+    return a;
+}
+
+static int64_t *step_ptr(TiState &st) {
+    // the global step counter lives in the tail of the reduction buffer
+    return reinterpret_cast<int64_t *>(st.red.as<double>() + 3 * st.nlambda);
+}
+
+static int threads_for(int P, int nd) {
+    int n = P * nd;
+    if (n >= 128 || P >= 128) return 128;
+    if (n >= 64) return 64;
+    return 32;
+}
+
+static int launch_steps(pg_ctx *ctx, TiState &st, int64_t nsteps, cudaStream_t s) {
+    TiArgs a = make_args(ctx, st, step_ptr(st));
+    const int P = st.P, nd = st.nd;
+    int th = threads_for(P, nd);
+    unsigned grid = (unsigned)st.nrings;
+    if (st.form == PG_FORM_TENSOR) return tc_launch(ctx, st, 0, nsteps, s);
+    if (st.form == PG_FORM_FUSED) {
+        size_t sm = (size_t)P * (st.fp32 ? sizeof(float) : sizeof(double));
+        int thermo = st.cfg.thermostat;
+        if (st.fp32) {
+            if (thermo == PG_LANGEVIN)
+                k_ti_fused<float, 2><<<grid, th, sm, s>>>(a, st.q.as<float>(), st.pi.as<float>(), st.x.as<float>(), st.f.as<float>(), nsteps);
+            else
+                k_ti_fused<float, 1><<<grid, th, sm, s>>>(a, st.q.as<float>(), st.pi.as<float>(), st.x.as<float>(), st.f.as<float>(), nsteps);
+        } else {
+            if (thermo == PG_LANGEVIN)
+                k_ti_fused<double, 2><<<grid, th, sm, s>>>(a, st.q.as<double>(), st.pi.as<double>(), st.x.as<double>(), st.f.as<double>(), nsteps);
+            else
+                k_ti_fused<double, 1><<<grid, th, sm, s>>>(a, st.q.as<double>(), st.pi.as<double>(), st.x.as<double>(), st.f.as<double>(), nsteps);
+        }
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return cuda_fail(e, "k_ti_fused launch");
+        k_step_add<<<1, 1, 0, s>>>(step_ptr(st), nsteps);
+        return PG_OK;
+    }
+    // plain form: per-step launches in the reference order
+    size_t sm = (size_t)P * sizeof(double);
+    int64_t nthr = st.nrings * P;
+    unsigned kgrid = (unsigned)((nthr + 127) / 128);
+    double *x = st.x.as<double>(), *p = st.pi.as<double>(), *q = st.q.as<double>(), *w = st.f.as<double>();
+    for (int64_t i = 0; i < nsteps; i++) {
+        if (st.cfg.thermostat == PG_LANGEVIN) {
+            k_plain_kick<<<kgrid, 128, 0, s>>>(a, x, p, st.cfg.dt);
+            k_plain_nm<<<grid, th, sm, s>>>(a, x, p, q, w);
+            k_plain_langevin<<<grid, th, sm, s>>>(a, p, w);
+            k_plain_nm<<<grid, th, sm, s>>>(a, x, p, q, w);
+        } else {
+            k_plain_andersen<<<grid, th, sm, s>>>(a, p, w);
+            k_plain_nm<<<grid, th, sm, s>>>(a, x, p, q, w);
+            k_plain_kick<<<kgrid, 128, 0, s>>>(a, x, p, st.cfg.dt);
+            k_plain_nm<<<grid, th, sm, s>>>(a, x, p, q, w);
+        }
+        k_plain_estimator<<<grid, th, sm, s>>>(a, st.cfg.thermostat, x, p, w);
+        k_step_add<<<1, 1, 0, s>>>(step_ptr(st), 1);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "plain-form launch");
+    return PG_OK;
+}
+
+int ti_release(pg_ctx *ctx) {
+    if (ctx && ctx->ti) {
+        delete ctx->ti;
+        ctx->ti = nullptr;
+    }
+    return PG_OK;
+}
+
+static int resolve_form(pg_ctx *ctx, TiState &st) {
+    int form = st.cfg.form;
+    if (st.cfg.precision == PG_FP64) {
+        if (form == PG_FORM_TENSOR) return fail(PG_ERR_UNSUPPORTED, "the tensor-core form needs PG_MIXED");
+        st.form = (form == PG_FORM_PLAIN) ? PG_FORM_PLAIN : PG_FORM_FUSED;
+        st.fp32 = false;
+        return PG_OK;
+    }
+    if (form == PG_FORM_PLAIN) return fail(PG_ERR_UNSUPPORTED, "the plain form is FP64 only");
+    st.fp32 = true;
+    if (form == PG_FORM_FUSED) {
+        st.form = PG_FORM_FUSED;
+        return PG_OK;
+    }
+    bool tc = tc_supported(st, *ctx) != 0;
+    if (form == PG_FORM_TENSOR && !tc)
+        return fail(PG_ERR_UNSUPPORTED,
+                    "the tensor-core form supports P = 128, ndof <= 4, Langevin, exact rotation, "
+                    "no dHdrlimit");
+    st.form = tc ? PG_FORM_TENSOR : PG_FORM_FUSED;
+    return PG_OK;
+}
+
+}  // namespace pg
+
+using namespace pg;
+
+extern "C" int pg_ti_setup(pg_ctx *ctx, const pg_ti_config *cfg, int64_t nrings, int64_t nlambda,
+                           const int32_t *ring_lambda, const uint64_t *ring_seed,
+                           const uint32_t *ring_stream, const double *a, const double *b,
+                           const double *dbdl, const double *xref, const double *x0,
+                           const double *p0) {
+    int rc = check_ctx(ctx, true);
+    if (rc) return rc;
+    if (!cfg) return fail(PG_ERR_ARG, "cfg is NULL");
+    if (cfg->nbeads < 2 || cfg->nbeads > 1024) return fail(PG_ERR_ARG, "nbeads must be in [2, 1024]");
+    if (nrings < 1 || nrings > (int64_t)1 << 30) return fail(PG_ERR_ARG, "nrings out of range");
+    if (nlambda < 1 || nlambda > 4096) return fail(PG_ERR_ARG, "nlambda out of range");
+    if (!ring_lambda || !ring_seed || !ring_stream || !a || !b || !dbdl)
+        return fail(PG_ERR_ARG, "NULL ring / endpoint array");
+    if (!x0 && !xref) return fail(PG_ERR_ARG, "need x0 or xref");
+    if (!(cfg->beta > 0.0) || !(cfg->dt > 0.0) || !(cfg->tau > 0.0) || cfg->gamma < 0.0)
+        return fail(PG_ERR_ARG, "beta, dt, tau must be > 0 and gamma >= 0");
+    if (cfg->thermostat != PG_LANGEVIN && cfg->thermostat != PG_ANDERSEN)
+        return fail(PG_ERR_ARG, "thermostat must be 1 (Andersen) or 2 (Langevin)");
+    if (cfg->precision != PG_FP64 && cfg->precision != PG_MIXED) return fail(PG_ERR_ARG, "bad precision");
+    if (cfg->form < PG_FORM_AUTO || cfg->form > PG_FORM_TENSOR) return fail(PG_ERR_ARG, "bad form");
+    if (cfg->imin < 0) return fail(PG_ERR_ARG, "imin must be >= 0");
+    for (int64_t r = 0; r < nrings; r++)
+        if (ring_lambda[r] < 0 || ring_lambda[r] >= nlambda) return fail(PG_ERR_ARG, "ring_lambda out of range");
+
+    // Reuse the device buffers of a previous batch (ensure() only grows them);
+    // captured graphs hold the old arguments and are dropped.
+    if (!ctx->ti) ctx->ti = new TiState();
+    TiState &st = *ctx->ti;
+    for (auto &kv : st.graphs) cudaGraphExecDestroy(kv.second);
+    st.graphs.clear();
+    st.cfg = *cfg;
+    st.nrings = nrings;
+    st.nlambda = nlambda;
+    st.P = (int)cfg->nbeads;
+    st.nd = ctx->nd;
+    st.betan = cfg->beta / (double)(cfg->nbeads + 1);  // pimd_par.f90:94
+    st.step = 0;
+    rc = resolve_form(ctx, st);
+    if (rc) {
+        ti_release(ctx);
+        return rc;
+    }
+    const int P = st.P, nd = st.nd, natom = ctx->natom, ndim = ctx->ndim;
+    const double betan = st.betan;
+
+    // init_nm (verletmodule.f90:306-338): lam, beadmass, beadvec; transmatrix
+    std::vector<double> T;
+    build_transmatrix(P, T);
+    std::vector<double> lam(P);
+    for (int i = 1; i <= P; i++) lam[i - 1] = 2.0 * std::sin((double)i * kPiRef / (double)(2 * P + 2)) / betan;
+    std::vector<ModeCoef> coef((size_t)natom * P);
+    const double t = 0.5 * cfg->dt;
+    for (int i = 0; i < P; i++)
+        for (int k = 0; k < natom; k++) {
+            double bm = ctx->mass[k] * (lam[i] * cfg->tau) * (lam[i] * cfg->tau);
+            double om = std::sqrt(ctx->mass[k] / bm) * lam[i];  // verletmodule.f90:519
+            ModeCoef c;
+            if (cfg->cayley) {  // verletmodule.f90:520-526
+                double den = 4.0 + om * om * t * t;
+                c.rA = (4.0 - om * om * t * t) / den;
+                c.rB = -4.0 * bm * om * om * t / den;
+                c.rC = 4.0 * t / (bm * den);
+                c.rD = c.rA;
+            } else {  // verletmodule.f90:528-531
+                c.rA = std::cos(t * om);
+                c.rB = -om * bm * std::sin(om * t);
+                c.rC = std::sin(om * t) / (om * bm);
+                c.rD = std::cos(t * om);
+            }
+            double c1 = std::exp(-cfg->gamma * cfg->dt * lam[i] * std::sqrt(ctx->mass[k] / bm));  // :383
+            double c2 = std::sqrt(1.0 - c1 * c1);
+            c.ou_a = c1 * c1;
+            c.ou_s = std::sqrt(bm / betan) * c2 * std::sqrt(1.0 + c1 * c1);
+            c.pscale = std::sqrt(bm / betan);
+            c.bm = bm;
+            coef[(size_t)k + (size_t)natom * i] = c;
+        }
+    std::vector<double> bv((size_t)nlambda * nd * P);
+    for (int64_t l = 0; l < nlambda; l++)
+        for (int i = 1; i <= P; i++)
+            for (int j = 0; j < ndim; j++)
+                for (int k = 0; k < natom; k++) {
+                    int dof = k * ndim + j;
+                    double v = a[dof] * std::sin((double)i * kPiRef / (double)(P + 1)) +
+                               b[l * nd + dof] * std::sin((double)(P * i) * kPiRef / (double)(P + 1));
+                    v = v * std::sqrt(2.0 / (double)(P + 1));
+                    v = v / ((lam[i - 1] * betan) * (lam[i - 1] * betan));
+                    bv[((size_t)l * nd + dof) * P + (i - 1)] = v;
+                }
+
+    size_t nstate = (size_t)nrings * nd * P;
+    size_t esz = st.fp32 ? sizeof(float) : sizeof(double);
+    cudaError_t e;
+#define ENS(buf, n)                                                   \
+    if ((e = (buf).ensure(n)) != cudaSuccess) {                       \
+        ti_release(ctx);                                              \
+        return cuda_fail(e, "device allocation for the ring batch");  \
+    }
+    ENS(st.q, nstate * esz);
+    ENS(st.pi, nstate * esz);
+    ENS(st.x, nstate * esz);
+    ENS(st.f, nstate * esz);
+    ENS(st.T, (size_t)P * P * (sizeof(double) + sizeof(float)));
+    ENS(st.coef, coef.size() * sizeof(ModeCoef));
+    ENS(st.bv, bv.size() * sizeof(double));
+    ENS(st.dbdl, (size_t)nlambda * nd * sizeof(double));
+    ENS(st.xref, (size_t)nlambda * nd * P * sizeof(double));
+    ENS(st.ringlam, (size_t)nrings * sizeof(int32_t));
+    ENS(st.ringseed, (size_t)nrings * sizeof(uint64_t));
+    ENS(st.ringstream, (size_t)nrings * sizeof(uint32_t));
+    ENS(st.acc, (size_t)nrings * sizeof(RingAcc));
+    ENS(st.red, (size_t)(3 * nlambda + 1) * sizeof(double));
+    DevBuf dx0, dp0;
+    if (x0) ENS(dx0, nstate * sizeof(double));
+    if (p0) ENS(dp0, nstate * sizeof(double));
+#undef ENS
+    std::vector<float> Tf(T.begin(), T.end());
+    cudaStream_t s = ctx->stream;
+    PG_CUDA(cudaMemcpyAsync(st.T.ptr, T.data(), T.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+    PG_CUDA(cudaMemcpyAsync(st.T.as<double>() + (size_t)P * P, Tf.data(), Tf.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+    PG_CUDA(cudaMemcpyAsync(st.coef.ptr, coef.data(), coef.size() * sizeof(ModeCoef), cudaMemcpyHostToDevice, s));
+    PG_CUDA(cudaMemcpyAsync(st.bv.ptr, bv.data(), bv.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+    PG_CUDA(cudaMemcpyAsync(st.dbdl.ptr, dbdl, (size_t)nlambda * nd * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (xref)
+        PG_CUDA(cudaMemcpyAsync(st.xref.ptr, xref, (size_t)nlambda * nd * P * sizeof(double), cudaMemcpyHostToDevice, s));
+    else
+        PG_CUDA(cudaMemsetAsync(st.xref.ptr, 0, (size_t)nlambda * nd * P * sizeof(double), s));
+    PG_CUDA(cudaMemcpyAsync(st.ringlam.ptr, ring_lambda, nrings * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    PG_CUDA(cudaMemcpyAsync(st.ringseed.ptr, ring_seed, nrings * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+    PG_CUDA(cudaMemcpyAsync(st.ringstream.ptr, ring_stream, nrings * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+    PG_CUDA(cudaMemsetAsync(st.red.ptr, 0, (size_t)(3 * nlambda + 1) * sizeof(double), s));
+    if (x0) PG_CUDA(cudaMemcpyAsync(dx0.ptr, x0, nstate * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (p0) PG_CUDA(cudaMemcpyAsync(dp0.ptr, p0, nstate * sizeof(double), cudaMemcpyHostToDevice, s));
+
+    TiArgs ta = make_args(ctx, st, step_ptr(st));
+    int th = threads_for(P, nd);
+    size_t sm = (size_t)P * esz;
+    if (st.form == PG_FORM_PLAIN) {
+        k_plain_init<<<(unsigned)nrings, th, (size_t)P * sizeof(double), s>>>(
+            ta, st.x.as<double>(), st.pi.as<double>(), st.f.as<double>(), dx0.as<double>(), dp0.as<double>());
+    } else if (st.fp32) {
+        k_ti_init<float><<<(unsigned)nrings, th, sm, s>>>(ta, st.q.as<float>(), st.pi.as<float>(), st.x.as<float>(),
+                                                          dx0.as<double>(), dp0.as<double>());
+    } else {
+        k_ti_init<double><<<(unsigned)nrings, th, sm, s>>>(ta, st.q.as<double>(), st.pi.as<double>(), st.x.as<double>(),
+                                                           dx0.as<double>(), dp0.as<double>());
+    }
+    PG_CUDA(cudaGetLastError());
+    if (st.form == PG_FORM_TENSOR) {
+        rc = tc_prepare(ctx, st);
+        if (rc) {
+            ti_release(ctx);
+            return rc;
+        }
+    }
+    PG_CUDA(cudaStreamSynchronize(s));
+    return PG_OK;
+}
+
+static int ti_advance_impl(pg_ctx *ctx, int64_t nsteps, double *device_ms);
+
+extern "C" int pg_ti_advance(pg_ctx *ctx, int64_t nsteps) { return ti_advance_impl(ctx, nsteps, nullptr); }
+
+extern "C" int pg_ti_advance_timed(pg_ctx *ctx, int64_t nsteps, double *device_ms) {
+    if (!device_ms) return fail(PG_ERR_ARG, "device_ms is NULL");
+    return ti_advance_impl(ctx, nsteps, device_ms);
+}
+
+static int ti_advance_impl(pg_ctx *ctx, int64_t nsteps, double *device_ms) {
+    int rc = check_ctx(ctx, true);
+    if (rc) return rc;
+    if (!ctx->ti) return fail(PG_ERR_STATE, "pg_ti_setup has not been called");
+    if (nsteps < 0) return fail(PG_ERR_ARG, "nsteps must be >= 0");
+    if (nsteps == 0) return PG_OK;
+    TiState &st = *ctx->ti;
+    if (st.step + nsteps > (int64_t)0xFFFFFFFFLL) return fail(PG_ERR_ARG, "step counter would exceed 2^32");
+    // Plain form: replay a captured graph of up to 64 steps; fused forms: one graph per nsteps.
+    int64_t chunk = (st.form == PG_FORM_PLAIN) ? (nsteps < 64 ? nsteps : 64) : nsteps;
+    int64_t done = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    if (device_ms) {
+        PG_CUDA(cudaEventCreate(&ev0));
+        PG_CUDA(cudaEventCreate(&ev1));
+        *device_ms = 0.0;
+    }
+    bool recorded = false;
+    while (done < nsteps) {
+        int64_t n = (nsteps - done) < chunk ? (nsteps - done) : chunk;
+        auto it = st.graphs.find(n);
+        cudaGraphExec_t exec = nullptr;
+        if (it == st.graphs.end()) {
+            cudaGraph_t g;
+            PG_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+            int lrc = launch_steps(ctx, st, n, ctx->stream);
+            cudaError_t ee = cudaStreamEndCapture(ctx->stream, &g);
+            if (lrc) return lrc;
+            if (ee != cudaSuccess) return cuda_fail(ee, "cudaStreamEndCapture");
+            ee = cudaGraphInstantiate(&exec, g, 0);
+            cudaGraphDestroy(g);
+            if (ee != cudaSuccess) return cuda_fail(ee, "cudaGraphInstantiate");
+            st.graphs[n] = exec;
+        } else {
+            exec = it->second;
+        }
+        if (device_ms && !recorded) {
+            PG_CUDA(cudaEventRecord(ev0, ctx->stream));
+            recorded = true;
+        }
+        PG_CUDA(cudaGraphLaunch(exec, ctx->stream));
+        done += n;
+    }
+    if (device_ms) PG_CUDA(cudaEventRecord(ev1, ctx->stream));
+    PG_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (device_ms) {
+        float ms = 0.f;
+        PG_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+        *device_ms = (double)ms;
+        cudaEventDestroy(ev0);
+        cudaEventDestroy(ev1);
+    }
+    st.step += nsteps;
+    return PG_OK;
+}
+
+extern "C" int pg_ti_get_step(pg_ctx *ctx, int64_t *step) {
+    int rc = check_ctx(ctx, true);
+    if (rc) return rc;
+    if (!ctx->ti) return fail(PG_ERR_STATE, "pg_ti_setup has not been called");
+    if (step) *step = ctx->ti->step;
+    return PG_OK;
+}
+
+extern "C" int pg_ti_get_state(pg_ctx *ctx, double *x, double *p) {
+    int rc = check_ctx(ctx, true);
+    if (rc) return rc;
+    if (!ctx->ti) return fail(PG_ERR_STATE, "pg_ti_setup has not been called");
+    TiState &st = *ctx->ti;
+    size_t n = (size_t)st.nrings * st.nd * st.P;
+    cudaStream_t s = ctx->stream;
+    PG_CUDA(ctx->scratch_a.ensure(n * sizeof(double)));
+    TiArgs ta = make_args(ctx, st, step_ptr(st));
+    int th = threads_for(st.P, st.nd);
+    if (st.form == PG_FORM_TENSOR) {
+        rc = tc_launch(ctx, st, 0, -1, s);  // read-out: writes x, pi back to the SIMT layout
+        if (rc) return rc;
+    }
+    if (x) {
+        if (st.fp32) {
+            k_to_double<float><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(st.x.as<float>(), ctx->scratch_a.as<double>(), n);
+            PG_CUDA(cudaMemcpyAsync(x, ctx->scratch_a.ptr, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+        } else {
+            PG_CUDA(cudaMemcpyAsync(x, st.x.ptr, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+        }
+        PG_CUDA(cudaStreamSynchronize(s));
+    }
+    if (p) {
+        if (st.form == PG_FORM_PLAIN) {
+            PG_CUDA(cudaMemcpyAsync(p, st.pi.ptr, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+        } else {
+            size_t sm = (size_t)st.P * (st.fp32 ? sizeof(float) : sizeof(double));
+            if (st.fp32)
+                k_ti_momenta<float><<<(unsigned)st.nrings, th, sm, s>>>(ta, st.pi.as<float>(), ctx->scratch_a.as<double>());
+            else
+                k_ti_momenta<double><<<(unsigned)st.nrings, th, sm, s>>>(ta, st.pi.as<double>(), ctx->scratch_a.as<double>());
+            PG_CUDA(cudaGetLastError());
+            PG_CUDA(cudaMemcpyAsync(p, ctx->scratch_a.ptr, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+        }
+    }
+    PG_CUDA(cudaStreamSynchronize(s));
+    return PG_OK;
+}
+
+extern "C" int pg_ti_get_results(pg_ctx *ctx, double *dhdr_sum, int64_t *nsamples, int64_t *nreinit,
+                                 int32_t *status) {
+    int rc = check_ctx(ctx, true);
+    if (rc) return rc;
+    if (!ctx->ti) return fail(PG_ERR_STATE, "pg_ti_setup has not been called");
+    TiState &st = *ctx->ti;
+    std::vector<RingAcc> acc(st.nrings);
+    PG_CUDA(cudaMemcpyAsync(acc.data(), st.acc.ptr, st.nrings * sizeof(RingAcc), cudaMemcpyDeviceToHost, ctx->stream));
+    PG_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (int64_t r = 0; r < st.nrings; r++) {
+        if (dhdr_sum) dhdr_sum[r] = acc[r].dhdr_sum;
+        if (nsamples) nsamples[r] = acc[r].nsamples;
+        if (nreinit) nreinit[r] = acc[r].nreinit;
+        if (status) status[r] = acc[r].status;
+    }
+    return PG_OK;
+}
+
+extern "C" int pg_ti_lambda_reduce(pg_ctx *ctx, double *mean, double *var, int64_t *count) {
+    int rc = check_ctx(ctx, true);
+    if (rc) return rc;
+    if (!ctx->ti) return fail(PG_ERR_STATE, "pg_ti_setup has not been called");
+    TiState &st = *ctx->ti;
+    k_lambda_reduce<<<(unsigned)st.nlambda, 256, 0, ctx->stream>>>(st.acc.as<RingAcc>(), st.ringlam.as<int32_t>(),
+                                                                     st.nrings, st.betan, st.red.as<double>());
+    PG_CUDA(cudaGetLastError());
+    std::vector<double> out(3 * st.nlambda);
+    PG_CUDA(cudaMemcpyAsync(out.data(), st.red.ptr, out.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    PG_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (int64_t l = 0; l < st.nlambda; l++) {
+        if (mean) mean[l] = out[3 * l];
+        if (var) var[l] = out[3 * l + 1];
+        if (count) count[l] = (int64_t)out[3 * l + 2];
+    }
+    return PG_OK;
+}
+
+// Checkpoint layout: header, then q, pi, x (state precision), then RingAcc[nrings].
+struct CkptHeader {
+    char magic[8];
+    int32_t version, form, fp32, P;
+    int64_t nrings, nd, step;
+    pg_ti_config cfg;
+};
+
+extern "C" int pg_ti_checkpoint_save(pg_ctx *ctx, const char *path) {
+    int rc = check_ctx(ctx, true);
+    if (rc) return rc;
+    if (!ctx->ti) return fail(PG_ERR_STATE, "pg_ti_setup has not been called");
+    if (!path) return fail(PG_ERR_ARG, "path is NULL");
+    TiState &st = *ctx->ti;
+    if (st.form == PG_FORM_TENSOR) {
+        rc = tc_launch(ctx, st, 0, -1, ctx->stream);
+        if (rc) return rc;
+    }
+    size_t n = (size_t)st.nrings * st.nd * st.P * (st.fp32 ? sizeof(float) : sizeof(double));
+    std::vector<unsigned char> buf(3 * n + st.nrings * sizeof(RingAcc));
+    PG_CUDA(cudaMemcpyAsync(buf.data(), st.q.ptr, n, cudaMemcpyDeviceToHost, ctx->stream));
+    PG_CUDA(cudaMemcpyAsync(buf.data() + n, st.pi.ptr, n, cudaMemcpyDeviceToHost, ctx->stream));
+    PG_CUDA(cudaMemcpyAsync(buf.data() + 2 * n, st.x.ptr, n, cudaMemcpyDeviceToHost, ctx->stream));
+    PG_CUDA(cudaMemcpyAsync(buf.data() + 3 * n, st.acc.ptr, st.nrings * sizeof(RingAcc), cudaMemcpyDeviceToHost, ctx->stream));
+    PG_CUDA(cudaStreamSynchronize(ctx->stream));
+    CkptHeader h;
+    memset(&h, 0, sizeof(h));
+    memcpy(h.magic, "PGCKPT01", 8);
+    h.version = 1;
+    h.form = st.form;
+    h.fp32 = st.fp32;
+    h.P = st.P;
+    h.nrings = st.nrings;
+    h.nd = st.nd;
+    h.step = st.step;
+    h.cfg = st.cfg;
+    FILE *fp = fopen(path, "wb");
+    if (!fp) return fail(PG_ERR_IO, std::string("cannot open ") + path);
+    bool ok = fwrite(&h, sizeof(h), 1, fp) == 1 && fwrite(buf.data(), 1, buf.size(), fp) == buf.size();
+    ok = (fclose(fp) == 0) && ok;
+    if (!ok) return fail(PG_ERR_IO, "checkpoint write failed");
+    return PG_OK;
+}
+
+extern "C" int pg_ti_checkpoint_load(pg_ctx *ctx, const char *path) {
+    int rc = check_ctx(ctx, true);
+    if (rc) return rc;
+    if (!ctx->ti) return fail(PG_ERR_STATE, "set up the same batch with pg_ti_setup before loading");
+    if (!path) return fail(PG_ERR_ARG, "path is NULL");
+    TiState &st = *ctx->ti;
+    FILE *fp = fopen(path, "rb");
+    if (!fp) return fail(PG_ERR_IO, std::string("cannot open ") + path);
+    CkptHeader h;
+    if (fread(&h, sizeof(h), 1, fp) != 1 || memcmp(h.magic, "PGCKPT01", 8) != 0) {
+        fclose(fp);
+        return fail(PG_ERR_IO, "not a pimdgpu checkpoint");
+    }
+    if (h.form != st.form || h.fp32 != (int)st.fp32 || h.P != st.P || h.nrings != st.nrings || h.nd != st.nd) {
+        fclose(fp);
+        return fail(PG_ERR_ARG, "checkpoint does not match the current batch (form/precision/P/nrings/ndof)");
+    }
+    size_t n = (size_t)st.nrings * st.nd * st.P * (st.fp32 ? sizeof(float) : sizeof(double));
+    std::vector<unsigned char> buf(3 * n + st.nrings * sizeof(RingAcc));
+    size_t got = fread(buf.data(), 1, buf.size(), fp);
+    fclose(fp);
+    if (got != buf.size()) return fail(PG_ERR_IO, "truncated checkpoint");
+    PG_CUDA(cudaMemcpyAsync(st.q.ptr, buf.data(), n, cudaMemcpyHostToDevice, ctx->stream));
+    PG_CUDA(cudaMemcpyAsync(st.pi.ptr, buf.data() + n, n, cudaMemcpyHostToDevice, ctx->stream));
+    PG_CUDA(cudaMemcpyAsync(st.x.ptr, buf.data() + 2 * n, n, cudaMemcpyHostToDevice, ctx->stream));
+    PG_CUDA(cudaMemcpyAsync(st.acc.ptr, buf.data() + 3 * n, st.nrings * sizeof(RingAcc), cudaMemcpyHostToDevice, ctx->stream));
+    int64_t stepv = h.step;
+    PG_CUDA(cudaMemcpyAsync(step_ptr(st), &stepv, sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+    PG_CUDA(cudaStreamSynchronize(ctx->stream));
+    st.step = h.step;
+    if (st.form == PG_FORM_TENSOR) {
+        rc = tc_prepare(ctx, st);
+        if (rc) return rc;
+    }
+    return PG_OK;
+}
+
+extern "C" int pg_ti_release(pg_ctx *ctx) {
+    int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    return ti_release(ctx);
+}
+
+extern "C" int pg_propagate_pimd(pg_ctx *ctx, const pg_ti_config *cfg, int64_t ntask, int64_t nmc,
+                                 const double *a, const double *b, const double *dbdl,
+                                 const uint64_t *seed, const uint32_t *stream, double *x, double *p,
+                                 double *dHdr, int32_t *status) {
+    int rc = check_ctx(ctx, true);
+    if (rc) return rc;
+    if (!x || !p || !dHdr || ntask < 1 || nmc < 0) return fail(PG_ERR_ARG, "bad propagate arguments");
+    std::vector<int32_t> lam(ntask);
+    for (int64_t i = 0; i < ntask; i++) lam[i] = (int32_t)i;
+    rc = pg_ti_setup(ctx, cfg, ntask, ntask, lam.data(), seed, stream, a, b, dbdl, x, x, p);
+    if (rc) return rc;
+    rc = pg_ti_advance(ctx, nmc);
+    if (rc) return rc;
+    rc = pg_ti_get_state(ctx, x, p);
+    if (rc) return rc;
+    std::vector<double> sum(ntask);
+    std::vector<int64_t> ns(ntask);
+    rc = pg_ti_get_results(ctx, sum.data(), ns.data(), nullptr, status);
+    if (rc) return rc;
+    for (int64_t i = 0; i < ntask; i++) dHdr[i] = ns[i] > 0 ? sum[i] / (double)ns[i] : 0.0;
+    return PG_OK;
+}

@@ -1,0 +1,268 @@
+"""GPU parity of the TI-PIMD path against the CPU oracle, through the C-ABI.
+
+FP64 forms are compared trajectory-by-trajectory over short runs (same Philox
+streams, so the only differences are libm / FMA rounding): fused NM-resident
+kernel vs the oracle's NM-resident step, plain per-step form vs the oracle's
+reference-order (ten-transform) step.  The mixed-precision forms are compared
+with the FP64 form over short runs (FP32 tolerance)."""
+import os
+
+import numpy as np
+import pytest
+
+import pgconfigs
+
+pytestmark = pytest.mark.gpu
+
+
+def _pes(oracle, c):
+    return oracle.Pes(c["pes_id"], c["ndim"], c["natom"], c["params"], V0=c["V0"])
+
+
+def _set_system(ctx, c):
+    ctx.set_system(c["ndim"], c["natom"], c["mass"], c["pes_id"], c["params"], c["V0"])
+
+
+def _small_2d(P=16, nrep=2, nint=3, beta=None):
+    c = dict(pgconfigs.load("c1"))
+    c["P"] = P
+    if beta is not None:
+        c["beta"] = beta
+    ti = pgconfigs.TiInputs(c, nrep=nrep, nintegral=nint)
+    return c, ti
+
+
+def _oracle_run(oracle, c, ti, prm, nsteps, x0=None, p0=None):
+    pes = _pes(oracle, c)
+    mass = np.array(c["mass"])
+    nd, P = ti.nd, ti.P
+    xs, ps, sums, ns, nre = [], [], [], [], []
+    for r in range(ti.nrings):
+        li = ti.ring_lambda[r]
+        if x0 is None:
+            x, p = oracle.ring_init(pes, mass, prm, ti.xref[li], int(ti.ring_seed[r]), int(ti.ring_stream[r]),
+                                    a=ti.a, b=ti.b[li])
+        else:
+            x = x0[r].copy()
+            p = p0[r].copy()
+        res = oracle.ring_propagate(pes, mass, prm, ti.a, ti.b[li], ti.dbdl[li], ti.xref[li],
+                                    int(ti.ring_seed[r]), int(ti.ring_stream[r]), 0, nsteps, x, p)
+        xs.append(x)
+        ps.append(p)
+        sums.append(res.dhdr_sum)
+        ns.append(res.nsamples)
+        nre.append(res.nreinit)
+    return np.array(xs), np.array(ps), np.array(sums), np.array(ns), np.array(nre)
+
+
+def _oracle_prm(oracle, c, ti, nm_resident, thermostat=2, cayley=False, dhdr_limit=-1.0, noutput=100000):
+    return oracle.TiParams(ti.P, c["beta"], c["dt"], tau=c["tau"], gamma=c["gamma"], thermostat=thermostat,
+                           cayley=cayley, nm_resident=nm_resident, imin=3,
+                           noutput=noutput, dhdr_limit=dhdr_limit, init_sigma=c["init_sigma"])
+
+
+def _gpu_cfg(pg, c, ti, precision, form, thermostat=2, cayley=False, dhdr_limit=-1.0, noutput=100000):
+    t = ti.ti_config(pg, precision, form)
+    t.thermostat = thermostat
+    t.cayley = int(cayley)
+    t.imin = 3
+    t.dhdr_limit = dhdr_limit
+    t.noutput = noutput
+    return t
+
+
+@pytest.mark.parametrize("name", ["c0", "c1", "c2", "c4"])
+def test_pes_eval_matches_oracle(ctx, pg, oracle, name):
+    c = pgconfigs.load(name)
+    _set_system(ctx, c)
+    pes = _pes(oracle, c)
+    rs = np.random.RandomState(4)
+    w = np.array(c["well1"])
+    X = np.array([w + 0.1 * rs.randn(w.size) for _ in range(64)])
+    V, G = ctx.pes_eval(X.ravel(), pg.PG_FP64)
+    for i in range(len(X)):
+        assert abs(V[i] - pes.V(X[i])) <= 1e-13 * max(1.0, abs(pes.V(X[i])))
+        np.testing.assert_allclose(G[i], pes.Vprime(X[i]), rtol=1e-12, atol=1e-14)
+    Vf, Gf = ctx.pes_eval(X.ravel(), pg.PG_MIXED)
+    gs = np.max(np.abs(G))
+    assert np.max(np.abs(Gf - G)) < 2e-5 * gs + 1e-6
+
+
+@pytest.mark.parametrize("name", ["c0", "c1", "c2", "c4"])
+def test_pes_hessian_matches_oracle(ctx, pg, oracle, name):
+    c = pgconfigs.load(name)
+    _set_system(ctx, c)
+    pes = _pes(oracle, c)
+    rs = np.random.RandomState(5)
+    w = np.array(c["well1"])
+    X = np.array([w + 0.05 * rs.randn(w.size) for _ in range(8)])
+    for quirks in (False, True):
+        H = ctx.pes_hessian(X.ravel(), quirks=quirks)
+        for i in range(len(X)):
+            np.testing.assert_allclose(H[i], pes.Vdoubleprime(X[i], quirks=quirks), rtol=1e-10, atol=1e-12)
+
+
+@pytest.mark.parametrize("P", [16, 32, 128, 256])
+def test_nm_transform_matches_oracle(ctx, pg, oracle, P):
+    T, _, _, _ = oracle.init_nm(P, 1, 1, [1.0], 1.0, 1.0, [0.0], [0.0])
+    cols = np.random.RandomState(P).randn(40, P)
+    out = ctx.nm_transform(P, cols.ravel(), pg.PG_FP64).reshape(40, P)
+    np.testing.assert_allclose(out, cols @ T.T, rtol=0, atol=1e-13 * P)
+    outf = ctx.nm_transform(P, cols.ravel(), pg.PG_MIXED).reshape(40, P)
+    assert np.max(np.abs(outf - out)) < 3e-5 * np.max(np.abs(out))
+
+
+@pytest.mark.parametrize("thermostat,cayley", [(2, False), (1, False), (2, True)])
+def test_fused_fp64_matches_oracle_nm_resident(ctx, pg, oracle, thermostat, cayley):
+    c, ti = _small_2d()
+    _set_system(ctx, c)
+    nsteps = 80
+    cfg = _gpu_cfg(pg, c, ti, pg.PG_FP64, pg.PG_FORM_FUSED, thermostat, cayley, noutput=9)
+    ctx.ti_setup(cfg, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
+    ctx.ti_advance(nsteps)
+    x, p = ctx.ti_state()
+    s, n, ri, st = ctx.ti_results()
+    prm = _oracle_prm(oracle, c, ti, True, thermostat, cayley, noutput=9)
+    xo, po, so, no, _ = _oracle_run(oracle, c, ti, prm, nsteps)
+    assert np.all(st == 0)
+    np.testing.assert_array_equal(n, no)
+    np.testing.assert_allclose(x.reshape(xo.shape), xo, rtol=0, atol=1e-9)
+    np.testing.assert_allclose(p.reshape(po.shape), po, rtol=0, atol=1e-7 * np.max(np.abs(po)))
+    np.testing.assert_allclose(s, so, rtol=1e-9, atol=1e-9)
+
+
+@pytest.mark.parametrize("thermostat", [2, 1])
+def test_plain_form_matches_oracle_reference_order(ctx, pg, oracle, thermostat):
+    c, ti = _small_2d()
+    _set_system(ctx, c)
+    nsteps = 60
+    cfg = _gpu_cfg(pg, c, ti, pg.PG_FP64, pg.PG_FORM_PLAIN, thermostat, noutput=9)
+    ctx.ti_setup(cfg, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
+    ctx.ti_advance(nsteps)
+    x, p = ctx.ti_state()
+    s, n, ri, st = ctx.ti_results()
+    prm = _oracle_prm(oracle, c, ti, False, thermostat, noutput=9)
+    xo, po, so, no, _ = _oracle_run(oracle, c, ti, prm, nsteps)
+    assert np.all(st == 0)
+    np.testing.assert_array_equal(n, no)
+    np.testing.assert_allclose(x.reshape(xo.shape), xo, rtol=0, atol=1e-9)
+    np.testing.assert_allclose(s, so, rtol=1e-9, atol=1e-9)
+
+
+def test_c0_plain_and_fused_fp64_match_oracle(ctx, pg, oracle):
+    c = pgconfigs.load("c0")
+    ti = pgconfigs.TiInputs(c)
+    _set_system(ctx, c)
+    nsteps = 100
+    prm_ref = _oracle_prm(oracle, c, ti, False)
+    xo, po, so, no, _ = _oracle_run(oracle, c, ti, prm_ref, nsteps)
+    for form in (pg.PG_FORM_PLAIN, pg.PG_FORM_FUSED):
+        cfg = _gpu_cfg(pg, c, ti, pg.PG_FP64, form)
+        ctx.ti_setup(cfg, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
+        ctx.ti_advance(nsteps)
+        x, p = ctx.ti_state()
+        s, n, _, st = ctx.ti_results()
+        np.testing.assert_allclose(x.reshape(xo.shape), xo, rtol=0, atol=1e-9)
+        np.testing.assert_allclose(s, so, rtol=1e-9)
+
+
+def test_dhdr_limit_reinit_matches_oracle(ctx, pg, oracle):
+    c, ti = _small_2d(nrep=1, nint=2)
+    _set_system(ctx, c)
+    nsteps = 30
+    lim = 2000.0
+    cfg = _gpu_cfg(pg, c, ti, pg.PG_FP64, pg.PG_FORM_FUSED, dhdr_limit=lim)
+    ctx.ti_setup(cfg, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
+    ctx.ti_advance(nsteps)
+    x, _ = ctx.ti_state()
+    s, n, ri, st = ctx.ti_results()
+    prm = _oracle_prm(oracle, c, ti, True, dhdr_limit=lim)
+    xo, po, so, no, reo = _oracle_run(oracle, c, ti, prm, nsteps)
+    np.testing.assert_array_equal(ri, reo)
+    assert np.sum(ri) > 0
+    np.testing.assert_allclose(x.reshape(xo.shape), xo, rtol=0, atol=1e-9)
+    np.testing.assert_allclose(s, so, rtol=1e-9, atol=1e-9)
+
+
+@pytest.mark.parametrize("form", ["fused64", "plain", "mixed"])
+def test_chunked_advance_and_checkpoint_are_bitwise(ctx, pg, tmp_path, form):
+    c, ti = _small_2d(P=32)
+    _set_system(ctx, c)
+    prec = pg.PG_MIXED if form == "mixed" else pg.PG_FP64
+    fm = {"fused64": pg.PG_FORM_FUSED, "plain": pg.PG_FORM_PLAIN, "mixed": pg.PG_FORM_AUTO}[form]
+    cfg = _gpu_cfg(pg, c, ti, prec, fm)
+    ctx.ti_setup(cfg, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
+    ctx.ti_advance(70)
+    x1, p1 = ctx.ti_state()
+    s1 = ctx.ti_results()[0]
+    ctx.ti_setup(cfg, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
+    ctx.ti_advance(30)
+    path = str(tmp_path / "ck.bin")
+    ctx.ti_checkpoint_save(path)
+    ctx.ti_advance(10)  # diverge, then restore
+    ctx.ti_checkpoint_load(path)
+    assert ctx.ti_step() == 30
+    ctx.ti_advance(40)
+    x2, p2 = ctx.ti_state()
+    s2 = ctx.ti_results()[0]
+    np.testing.assert_array_equal(x1, x2)
+    np.testing.assert_array_equal(p1, p2)
+    np.testing.assert_array_equal(s1, s2)
+
+
+def test_lambda_reduce_matches_host_formula(ctx, pg):
+    c, ti = _small_2d(nrep=5, nint=3)
+    _set_system(ctx, c)
+    cfg = _gpu_cfg(pg, c, ti, pg.PG_FP64, pg.PG_FORM_FUSED)
+    ctx.ti_setup(cfg, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
+    ctx.ti_advance(40)
+    s, n, _, _ = ctx.ti_results()
+    m, v, cnt = ctx.ti_lambda_reduce()
+    integ = (s / n / ti.betan ** 2).reshape(3, 5)
+    np.testing.assert_allclose(m, integ.mean(1), rtol=1e-13)
+    np.testing.assert_allclose(v, (integ ** 2).mean(1) - integ.mean(1) ** 2, rtol=1e-9, atol=1e-12)
+    assert list(cnt) == [5, 5, 5]
+
+
+@pytest.mark.parametrize("P", [16, 128])
+def test_mixed_forms_track_fp64(ctx, pg, P):
+    """Short runs from identical starts: FP32 state + FP32 forces (+ split-BF16
+    tensor-core transform at P = 128) stay within FP32 round-off of FP64."""
+    c, ti = _small_2d(P=P, nrep=4, nint=2)
+    _set_system(ctx, c)
+    nsteps = 20
+    cfg = _gpu_cfg(pg, c, ti, pg.PG_FP64, pg.PG_FORM_FUSED)
+    ctx.ti_setup(cfg, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
+    ctx.ti_advance(nsteps)
+    x64, p64 = ctx.ti_state()
+    s64 = ctx.ti_results()[0]
+    for form in (pg.PG_FORM_FUSED, pg.PG_FORM_AUTO):
+        cfg = _gpu_cfg(pg, c, ti, pg.PG_MIXED, form)
+        ctx.ti_setup(cfg, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
+        ctx.ti_advance(nsteps)
+        x32, p32 = ctx.ti_state()
+        s32 = ctx.ti_results()[0]
+        assert np.max(np.abs(x32 - x64)) < 2e-3, form
+        assert np.max(np.abs(p32 - p64)) < 2e-3 * np.max(np.abs(p64)), form
+        np.testing.assert_allclose(s32, s64, rtol=2e-4)
+
+
+def test_propagate_pimd_dropin(ctx, pg, oracle):
+    c, ti = _small_2d(nrep=1, nint=3)
+    _set_system(ctx, c)
+    pes = _pes(oracle, c)
+    mass = np.array(c["mass"])
+    prm = _oracle_prm(oracle, c, ti, True)
+    x0, p0 = [], []
+    for r in range(ti.nrings):
+        li = ti.ring_lambda[r]
+        x, p = oracle.ring_init(pes, mass, prm, ti.xref[li], int(ti.ring_seed[r]), int(ti.ring_stream[r]),
+                                a=ti.a, b=ti.b[li])
+        x0.append(x)
+        p0.append(p)
+    x0, p0 = np.array(x0), np.array(p0)
+    cfg = _gpu_cfg(pg, c, ti, pg.PG_FP64, pg.PG_FORM_FUSED)
+    x, p, dh, st = ctx.propagate_pimd(cfg, 50, ti.a, ti.b, ti.dbdl, ti.ring_seed, ti.ring_stream, x0, p0)
+    xo, po, so, no, _ = _oracle_run(oracle, c, ti, prm, 50, x0=x0, p0=p0)
+    np.testing.assert_allclose(x.reshape(xo.shape), xo, atol=1e-9)
+    np.testing.assert_allclose(dh, so / no, rtol=1e-9)
