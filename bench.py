@@ -187,6 +187,40 @@ def run_reference(args):
     return 0
 
 
+def _extras(ctx, pg, cfg, ti, M, K, value, ws, beads, extras):
+    import torch
+    # e2e: the reference-facing drop-in with host buffers, copies inside the timed region
+    x0, p0 = ctx.ti_state()
+    xh = torch.from_numpy(x0).pin_memory().numpy()
+    ph = torch.from_numpy(p0).pin_memory().numpy()
+    bseq = ti.b
+    dseq = ti.dbdl
+    for _ in range(2):
+        ctx.propagate_pimd(cfg, M, ti.a, bseq[ti.ring_lambda], dseq[ti.ring_lambda], ti.ring_seed,
+                           ti.ring_stream, xh, ph)
+    te = []
+    for _ in range(max(3, K // 2)):
+        t0 = time.perf_counter()
+        xo, po, dh, _ = ctx.propagate_pimd(cfg, M, ti.a, bseq[ti.ring_lambda], dseq[ti.ring_lambda],
+                                           ti.ring_seed, ti.ring_stream, xh, ph)
+        te.append(time.perf_counter() - t0)
+    e2e_s = statistics.median(te)
+    h2d = xh.nbytes + ph.nbytes
+    d2h = xh.nbytes + ph.nbytes + dh.nbytes
+    extras["e2e"] = {"value": beads * M / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                     "d2h_bytes_per_step": int(d2h), "call": "pg_propagate_pimd (host buffers)"}
+    # FP64 denominators on the same rings
+    for name, form64, md in (("plain_fp64", pg.PG_FORM_PLAIN, 4), ("fused_fp64", pg.PG_FORM_FUSED, 20)):
+        cfg64 = ti.ti_config(pg, pg.PG_FP64, form64)
+        ctx.ti_setup(cfg64, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
+        ctx.ti_advance(md)
+        ms = ctx.ti_advance_timed(md)
+        extras[name] = {"value": beads * md / (ms / 1e3), "unit": UNIT, "md_steps": md}
+    extras["speedup_vs_plain_fp64"] = value / ws / extras["plain_fp64"]["value"]
+    extras["speedup_vs_fused_fp64"] = value / ws / extras["fused_fp64"]["value"]
+
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -223,6 +257,7 @@ def main():
     ctx.ti_setup(cfg, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
     K, W, M = args.steps, args.warmup, args.md_per_step
     beads = ti.nrings * ti.P
+    form_used, launches_per_step = ctx.ti_form(M)
 
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
     for _ in range(W):
@@ -254,37 +289,13 @@ def main():
     nan_rings = int(np.sum(st != 0))
 
     extras = {}
-    if not args.no_extras and rank == 0:
-        # e2e: the reference-facing drop-in with host buffers, copies inside the timed region
-        x0, p0 = ctx.ti_state()
-        xh = torch.from_numpy(x0).pin_memory().numpy()
-        ph = torch.from_numpy(p0).pin_memory().numpy()
-        bseq = ti.b
-        dseq = ti.dbdl
-        for _ in range(2):
-            ctx.propagate_pimd(cfg, M, ti.a, bseq[ti.ring_lambda], dseq[ti.ring_lambda], ti.ring_seed,
-                               ti.ring_stream, xh, ph)
-        te = []
-        for _ in range(max(3, K // 2)):
-            t0 = time.perf_counter()
-            xo, po, dh, _ = ctx.propagate_pimd(cfg, M, ti.a, bseq[ti.ring_lambda], dseq[ti.ring_lambda],
-                                               ti.ring_seed, ti.ring_stream, xh, ph)
-            te.append(time.perf_counter() - t0)
-        e2e_s = statistics.median(te)
-        h2d = xh.nbytes + ph.nbytes
-        d2h = xh.nbytes + ph.nbytes + dh.nbytes
-        extras["e2e"] = {"value": beads * M / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                         "d2h_bytes_per_step": int(d2h), "call": "pg_propagate_pimd (host buffers)"}
-        # FP64 denominators on the same rings
-        for name, form64, md in (("plain_fp64", pg.PG_FORM_PLAIN, 4), ("fused_fp64", pg.PG_FORM_FUSED, 20)):
-            cfg64 = ti.ti_config(pg, pg.PG_FP64, form64)
-            ctx.ti_setup(cfg64, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
-            ctx.ti_advance(md)
-            ms = ctx.ti_advance_timed(md)
-            extras[name] = {"value": beads * md / (ms / 1e3), "unit": UNIT, "md_steps": md}
-        extras["speedup_vs_plain_fp64"] = value / ws / extras["plain_fp64"]["value"]
-        extras["speedup_vs_fused_fp64"] = value / ws / extras["fused_fp64"]["value"]
-
+    print("[bench] fused kernel: %.3f ms per step of %d MD steps, %.3e %s" % (kernel_ms, M, value, UNIT),
+          file=sys.stderr, flush=True)
+    try:
+        if not args.no_extras and rank == 0:
+            _extras(ctx, pg, cfg, ti, M, K, value, ws, beads, extras)
+    except Exception as e:  # report, keep the main measurement
+        extras["extras_error"] = repr(e)
     peaks, peak_kind = _peaks()
     # Algorithmic tensor work of the NM transforms: 2 transforms x 2*P*ndof flops per bead-step.
     f_tc = 2 * 2 * ti.P * ti.nd
@@ -308,7 +319,8 @@ def main():
                                    "per GPU, Langevin, %d MD steps per bench step" % M,
                        "precision": "FP32 forces/state, split-BF16 NM transform, FP64 estimator",
                        "l2": "flushed (256 MB write) between timed steps", "form": args.form},
-            "roofline": roof, "clocks": clocks, "gpu_launches": 2 * K, "wall_s": wall,
+            "roofline": roof, "clocks": clocks, "gpu_launches": K * launches_per_step, "wall_s": wall,
+            "form": {pg.PG_FORM_FUSED: "fused-simt", pg.PG_FORM_TENSOR: "tcgen05", pg.PG_FORM_PLAIN: "plain"}[form_used],
             "nan_rings": nan_rings}
     line.update(extras)
     if rank == 0 and not args.no_cpu:

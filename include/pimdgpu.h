@@ -144,6 +144,9 @@ int pg_ti_get_results(pg_ctx *ctx, double *dhdr_sum, int64_t *nsamples, int64_t 
 int pg_ti_lambda_reduce(pg_ctx *ctx, double *mean, double *var, int64_t *count);
 /* Global step counter of the batch (steps already taken). */
 int pg_ti_get_step(pg_ctx *ctx, int64_t *step);
+/* Execution form chosen for the batch (PG_FORM_PLAIN / _FUSED / _TENSOR) and the
+ * number of kernel launches one pg_ti_advance(nsteps) issues. */
+int pg_ti_get_form(pg_ctx *ctx, int64_t nsteps, int32_t *form, int64_t *launches);
 /* Bitwise checkpoint of the whole batch state (positions, momenta, estimator
  * accumulators, RNG step counters); replaces write_restart / restart=2
  * (verletmodule.f90:162-185, pimd_par.f90:331-370). */

@@ -204,9 +204,12 @@ extern "C" int pg_set_system(pg_ctx *ctx, int64_t ndim, int64_t natom, const dou
     ctx->params.assign(params, params + nparams);
     PG_CUDA(ctx->d_params.ensure(sizeof(double) * (nparams > 0 ? nparams : 1)));
     if (nparams > 0)
-        PG_CUDA(cudaMemcpy(ctx->d_params.ptr, params, sizeof(double) * nparams, cudaMemcpyHostToDevice));
+        PG_CUDA(cudaMemcpyAsync(ctx->d_params.ptr, ctx->params.data(), sizeof(double) * nparams,
+                                cudaMemcpyHostToDevice, ctx->stream));
     PG_CUDA(ctx->d_mass.ensure(sizeof(double) * natom));
-    PG_CUDA(cudaMemcpy(ctx->d_mass.ptr, mass, sizeof(double) * natom, cudaMemcpyHostToDevice));
+    PG_CUDA(cudaMemcpyAsync(ctx->d_mass.ptr, ctx->mass.data(), sizeof(double) * natom, cudaMemcpyHostToDevice,
+                            ctx->stream));
+    PG_CUDA(cudaStreamSynchronize(ctx->stream));
     ctx->have_system = true;
     return PG_OK;
 }

@@ -117,7 +117,9 @@ __device__ __forceinline__ void sincos_turn_f(uint32_t w, float &s, float &c) {
 
 __device__ __forceinline__ void box_muller_f(uint32_t wa, uint32_t wb, float &z0, float &z1) {
     float ua = ((float)(wa >> 8) + 0.5f) * 5.9604644775390625e-08f;
-    float t = -2.0f * 0.69314718055994531f * __log2f(ua);
+    // lg2.approx has an absolute error near u = 1 and can return 0 (or a tiny
+    // positive value) there; clamp so that r stays finite (r -> ~0 for u -> 1).
+    float t = fmaxf(-2.0f * 0.69314718055994531f * __log2f(ua), 1.0e-30f);
     float r = t * rsqrtf(t);
     float s, c;
     sincos_turn_f(wb, s, c);

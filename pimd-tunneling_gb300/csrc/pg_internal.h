@@ -50,7 +50,7 @@ struct RingAcc {
     int64_t and_count;
     int64_t and_rkick;
     int32_t status;
-    int32_t pad;
+    int32_t pad;  // step at which a NaN was first seen
 };
 
 // Per (atom, mode) constants of the normal-mode propagator.
@@ -77,6 +77,7 @@ struct TiState {
     DevBuf coef;             // natom*P ModeCoef
     DevBuf bv;               // nlambda*nd*P endpoint shifts (beadvec)
     DevBuf dbdl;             // nlambda*nd
+    DevBuf avec, bvec;       // nd start point, nlambda*nd end points
     DevBuf xref;             // nlambda*nd*P
     DevBuf ringlam, ringseed, ringstream;
     DevBuf acc;              // nrings RingAcc
@@ -121,4 +122,5 @@ int tc_supported(const TiState &st, const pg_ctx &ctx);
 int tc_prepare(pg_ctx *ctx, TiState &st);
 int tc_launch(pg_ctx *ctx, TiState &st, int64_t step0, int64_t nsteps, cudaStream_t s);
 int tc_nm_transform(pg_ctx *ctx, int64_t P, int64_t ncol, const double *in, double *out);
+int32_t tc_error(pg_ctx *ctx, TiState &st);
 }  // namespace pg

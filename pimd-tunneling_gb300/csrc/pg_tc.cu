@@ -1,17 +1,729 @@
 // pg_tc.cu -- tcgen05 (5th-generation tensor core) kernels for sm_103a.
+//
+// The fixed-end normal-mode transform T (P x P, DST-I, symmetric, T T = I) is
+// the only dense contraction of the TI-PIMD step.  Here it runs on the tensor
+// cores as a split-BF16 product with FP32 accumulation in tensor memory:
+//     T X ~= T_hi X_hi + T_hi X_lo + T_lo X_hi,   v_hi = bf16(v), v_lo = bf16(v - v_hi)
+// (relative error ~ 2^-17 per element).
+//
+// Layout: one CTA owns 128 ring-dof rows (64 rings of a 2-D surface, or 128
+// rings of a 1-D one) with one thread per row.  The MMA computes
+//     D[row][n] = sum_k A[row][k] B[n][k],  A = data (K-major rows written by the
+//     thread that owns the TMEM lane), B = T (K-major, loaded by bulk async copy).
+// M = 128 (TMEM lanes = ring-dofs), N = 128 (TMEM columns = beads or modes),
+// K = 128 in 8 steps of 16, three MMAs per step, one commit per launch.
+//
+// State lives in HBM/L2 as FP32 [ring][dof][P] (q, pi, x, F), the same layout
+// as the SIMT kernels, so state read-out and checkpoints are shared.
+#include <cuda_bf16.h>
+
+#include <cstdio>
+#include <vector>
+
 #include "pg_internal.h"
 
 namespace pg {
 
-int tc_built() { return 0; }
-int tc_supported(const TiState &, const pg_ctx &) { return 0; }
-int tc_prepare(pg_ctx *, TiState &) { return fail(PG_ERR_UNSUPPORTED, "tensor-core form not built"); }
-int tc_launch(pg_ctx *, TiState &, int64_t, int64_t nsteps, cudaStream_t) {
-    if (nsteps < 0) return PG_OK;
-    return fail(PG_ERR_UNSUPPORTED, "tensor-core form not built");
+void build_transmatrix(int P, std::vector<double> &T);
+
+namespace {
+
+constexpr int kP = 128;            // beads (= modes = MMA K)
+constexpr int kRows = 128;         // ring-dof columns per CTA (MMA M)
+constexpr int kOpBytes = kRows * kP * 2;  // one bf16 operand image: 32 KB
+constexpr uint32_t kLBO = 128;     // byte offset between K-adjacent 8x16B core matrices
+constexpr uint32_t kSBO = 2048;    // byte offset between M/N-adjacent 8-row groups
+constexpr long long kSpinLimit = 20000000LL;
+constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s
+
+// Byte offset of element (row, k) in a K-major, no-swizzle core-matrix image.
+__host__ __device__ __forceinline__ uint32_t op_offset(int row, int k) {
+    return (uint32_t)((row >> 3) * kSBO + (k >> 3) * kLBO + (row & 7) * 16 + (k & 7) * 2);
 }
-int tc_nm_transform(pg_ctx *, int64_t, int64_t, const double *, double *) {
-    return fail(PG_ERR_UNSUPPORTED, "tensor-core transform not built");
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// 64-bit shared-memory matrix descriptor (no swizzle, K-major).
+__device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
+    d |= (uint64_t)(kLBO >> 4) << 16;
+    d |= (uint64_t)(kSBO >> 4) << 32;
+    d |= (uint64_t)1 << 46;  // descriptor version for sm_100-family tcgen05
+    return d;                // base offset 0, layout type 0 (no swizzle)
+}
+
+// Instruction descriptor, kind::f16: D = F32, A = B = BF16, K-major, M = 128, N = 128.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(128 >> 3) << 17) |
+                            ((uint32_t)(128 >> 4) << 24);
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// Bounded wait: gives up (returns false) after ~2 s of wall time.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+    const uint64_t t0 = globaltimer_ns();
+    for (long long i = 0; i < kSpinLimit; i++) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((i & 63) == 63 && globaltimer_ns() - t0 > kWaitLimitNs) return false;
+    }
+    return false;
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ void fence_barrier_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_alloc(uint32_t *slot, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
+                 "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+            dtmem),
+        "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(acc)
+        : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+#define PG_R32(v)                                                                                       \
+    "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),     \
+        "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),       \
+        "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),     \
+        "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),     \
+        "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+#define PG_W32(v)                                                                                         \
+    "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]), "r"(v[8]),  \
+        "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15]), "r"(v[16]), \
+        "r"(v[17]), "r"(v[18]), "r"(v[19]), "r"(v[20]), "r"(v[21]), "r"(v[22]), "r"(v[23]), "r"(v[24]), \
+        "r"(v[25]), "r"(v[26]), "r"(v[27]), "r"(v[28]), "r"(v[29]), "r"(v[30]), "r"(v[31])
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+    __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<uint32_t *>(&h);
+}
+
+// 32 consecutive FP32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&out)[32]) {
+    uint32_t v[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,"
+        "%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : PG_R32(v)
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; i++) out[i] = __uint_as_float(v[i]);
+}
+// Write 32 FP32 values of row `row`, K = k0..k0+31, into the hi / lo operand images.
+__device__ __forceinline__ void write_split32(unsigned char *Ahi, unsigned char *Alo, int row, int k0,
+                                              const float (&v)[32]) {
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        uint32_t h[4], l[4];
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            float a0 = v[8 * c + 2 * e], a1 = v[8 * c + 2 * e + 1];
+            __nv_bfloat16 h0 = __float2bfloat16_rn(a0), h1 = __float2bfloat16_rn(a1);
+            float r0 = a0 - __bfloat162float(h0), r1 = a1 - __bfloat162float(h1);
+            __nv_bfloat162 hh;
+            hh.x = h0;
+            hh.y = h1;
+            h[e] = *reinterpret_cast<uint32_t *>(&hh);
+            l[e] = pack_bf16(r0, r1);
+        }
+        uint32_t off = op_offset(row, k0 + 8 * c);
+        *reinterpret_cast<uint4 *>(Ahi + off) = make_uint4(h[0], h[1], h[2], h[3]);
+        *reinterpret_cast<uint4 *>(Alo + off) = make_uint4(l[0], l[1], l[2], l[3]);
+    }
+}
+
+// D(tmem col dcol) = A * B^T over K = 128, split-BF16 (3 products per K step).
+__device__ __forceinline__ void issue_gemm(uint32_t tmem, uint32_t dcol, uint32_t a_hi, uint32_t a_lo,
+                                           uint32_t b_hi, uint32_t b_lo, uint64_t *bar) {
+#pragma unroll
+    for (int ks = 0; ks < kP / 16; ks++) {
+        uint32_t koff = (uint32_t)ks * 2 * kLBO;
+        uint64_t ah = make_desc(a_hi + koff), al = make_desc(a_lo + koff);
+        uint64_t bh = make_desc(b_hi + koff), bl = make_desc(b_lo + koff);
+        mma_bf16(tmem + dcol, ah, bh, ks > 0 ? 1u : 0u);
+        mma_bf16(tmem + dcol, ah, bl, 1u);
+        mma_bf16(tmem + dcol, al, bh, 1u);
+    }
+    mma_commit(bar);
+}
+
+struct TcShared {
+    uint64_t mma_bar;
+    uint64_t tma_bar;
+    uint32_t tmem_slot;
+    int32_t err;
+};
+
+// Dynamic shared memory: [T_hi | T_lo | A_hi | A_lo] (32 KB each, 1024-aligned),
+// then per-atom mode coefficients, then TcShared.
+constexpr int kSmemOps = 4 * kOpBytes;
+
+__device__ __forceinline__ unsigned char *align1k(unsigned char *p) {
+    return reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(p) + 1023) & ~(uintptr_t)1023);
+}
+
+// Load the split-BF16 transform image (64 KB) with bulk async copies.
+__device__ __forceinline__ void load_transform(unsigned char *Thi, const unsigned char *gT, TcShared *sh) {
+    if (threadIdx.x == 0) {
+        mbar_expect_tx(&sh->tma_bar, 2 * kOpBytes);
+#pragma unroll
+        for (int i = 0; i < 4; i++) bulk_g2s(Thi + i * 16384, gT + i * 16384, 16384, &sh->tma_bar);
+    }
+}
+
+// ---------------------------------------------------------------- standalone transform
+// out[c][:] = T in[c][:] for 128 columns per CTA (used by pg_nm_transform, P = 128).
+__global__ void __launch_bounds__(128, 1) k_tc_transform(const unsigned char *__restrict__ gT,
+                                                          const double *__restrict__ in,
+                                                          double *__restrict__ out, int64_t ncol,
+                                                          int32_t *__restrict__ err) {
+    extern __shared__ unsigned char dsm[];
+    unsigned char *base = align1k(dsm);
+    unsigned char *Thi = base, *Tlo = base + kOpBytes, *Ahi = base + 2 * kOpBytes, *Alo = base + 3 * kOpBytes;
+    TcShared *sh = reinterpret_cast<TcShared *>(base + kSmemOps);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    if (tid == 0) {
+        mbar_init(&sh->mma_bar, 1);
+        mbar_init(&sh->tma_bar, 1);
+        sh->err = 0;
+        fence_barrier_init();
+    }
+    __syncthreads();
+    if (warp == 0) tmem_alloc(&sh->tmem_slot, 128);
+    load_transform(Thi, gT, sh);
+    // rows = columns of the input
+    const int64_t c = (int64_t)blockIdx.x * kRows + tid;
+    for (int k0 = 0; k0 < kP; k0 += 32) {
+        float v[32];
+#pragma unroll
+        for (int i = 0; i < 32; i++) v[i] = c < ncol ? (float)in[c * kP + k0 + i] : 0.f;
+        write_split32(Ahi, Alo, tid, k0, v);
+    }
+    fence_async_smem();
+    tc_before();
+    __syncthreads();
+    tc_after();
+    const uint32_t tmem = sh->tmem_slot;
+    bool ok = mbar_wait(&sh->tma_bar, 0);
+    if (tid == 0) {
+        if (ok) {
+            issue_gemm(tmem, 0, smem_u32(Ahi), smem_u32(Alo), smem_u32(Thi), smem_u32(Tlo), &sh->mma_bar);
+        } else {
+            sh->err = 1;
+        }
+    }
+    __syncthreads();
+    bool issued = sh->err == 0;
+    if (issued && !mbar_wait(&sh->mma_bar, 0)) atomicOr(&sh->err, 2);
+    tc_after();
+    __syncthreads();
+    if (sh->err == 0) {
+        const uint32_t lane_addr = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
+        for (int n0 = 0; n0 < kP; n0 += 32) {
+            float v[32];
+            tmem_ld32(lane_addr + (uint32_t)n0, v);
+            if (c < ncol)
+#pragma unroll
+                for (int i = 0; i < 32; i++) out[c * kP + n0 + i] = (double)v[i];
+        }
+    } else if (tid == 0) {
+        atomicOr(err, sh->err);
+    }
+    tc_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, 128);
+}
+
+// ---------------------------------------------------------------- TI step on the tensor cores
+// One MD step = two launches, each with the single-GEMM structure of
+// k_tc_transform (128 threads = 128 ring-dof rows, one split-BF16 GEMM, 128
+// TMEM columns, one commit):
+//   G1: x = T q + x* (positions), the estimator of the previous step (bead P),
+//       forces F = grad V(x) from the FP32 surface, written to HBM/L2;
+//   G2: (T F) per mode, then kick / half rotation / OU / half rotation of
+//       (q, pi) with Philox normals, written back.
+// The ring state (q, pi, F, x) stays resident in L2 between launches; the
+// launches of an advance are replayed from one captured CUDA graph.
+struct TcArgs {
+    int64_t nrings;
+    int nd, ndim, natom;
+    float dt;
+    int64_t imin;
+    const unsigned char *gT;  // split-BF16 transform image (64 KB)
+    const float *coef;        // natom x P x 8: rA rB rC rD ou_a ou_s
+    const double *mass;       // natom
+    const double *avec;       // nd
+    const double *bvec;       // nlambda*nd
+    const double *dbdl;       // nlambda*nd
+    const int32_t *ringlam;
+    const uint64_t *ringseed;
+    const uint32_t *ringstream;
+    float *q, *pi, *x, *f;    // [ring][dof][P]
+    RingAcc *acc;
+    int64_t *stepA;           // current step: written by G2, read by G1
+    int64_t *stepB;           // copy for G2: written by G1, read by G2
+    int32_t *err;
+    // PES parameters (FP32)
+    float wc[12];
+    int nwell;
+    float a0, b0;
+    int pow10;
+    float H, x0;
+};
+
+// Forces for the 32 beads of one chunk.  PESK 1: 1-D quartic well, one
+// coordinate per lane.  PESK 2: 2-D six-well surface, lanes 2r / 2r+1 hold x / y
+// of ring r; the even lane computes beads 0..15, the odd lane beads 16..31, and
+// the pair swaps halves with warp shuffles before and after.
+template <int PESK>
+__device__ __forceinline__ void chunk_forces(const TcArgs &a, const float (&xv)[32], float (&fv)[32],
+                                             bool odd) {
+    if constexpr (PESK == 1) {
+#pragma unroll
+        for (int t = 0; t < 32; t++) {
+            float u = xv[t] / a.x0;
+            float w = u * u - 1.0f;
+            fv[t] = w * 4.0f * a.H * xv[t] / (a.x0 * a.x0);
+        }
+    } else {
+        float px[16], py[16];
+#pragma unroll
+        for (int t = 0; t < 16; t++) {
+            float send = odd ? xv[t] : xv[16 + t];
+            float recv = __shfl_xor_sync(0xffffffffu, send, 1);
+            px[t] = odd ? recv : xv[t];
+            py[t] = odd ? xv[16 + t] : recv;
+        }
+        float fx[16], fy[16];
+#pragma unroll
+        for (int t = 0; t < 16; t++) {
+            float gx = 0.f, gy = 0.f;
+            for (int k = 0; k < a.nwell; k++) {
+                float dx = px[t] - a.wc[2 * k], dy = py[t] - a.wc[2 * k + 1];
+                float u = dx * dx + dy * dy;
+                float eb = __expf(-a.b0 * u);
+                float ea;
+                if (a.pow10) {
+                    float e2 = eb * eb, e4 = e2 * e2, e8 = e4 * e4;
+                    ea = e8 * e2;
+                } else {
+                    ea = __expf(-a.a0 * u);
+                }
+                float cc = a.a0 * ea + a.b0 * eb;
+                gx += cc * dx;
+                gy += cc * dy;
+            }
+            fx[t] = gx;
+            fy[t] = gy;
+        }
+#pragma unroll
+        for (int t = 0; t < 16; t++) {
+            float send = odd ? fx[t] : fy[t];
+            float recv = __shfl_xor_sync(0xffffffffu, send, 1);
+            if (odd) {
+                fv[16 + t] = fy[t];
+                fv[t] = recv;
+            } else {
+                fv[t] = fx[t];
+                fv[16 + t] = recv;
+            }
+        }
+    }
+}
+
+// Common prologue: barriers, TMEM (128 columns), T image by bulk copy, the
+// thread's row of `src` (FP32, 128 values) split into the A image, GEMM issued
+// and waited.  Returns the TMEM base (lane-quadrant address in *laddr) and
+// whether the accumulator is valid (same sequence as k_tc_transform).
+__device__ __forceinline__ bool tc_row_gemm(unsigned char *base, TcShared *sh, const unsigned char *gT,
+                                            const float *row_src, bool valid, uint32_t *tmem_out) {
+    unsigned char *Thi = base, *Tlo = base + kOpBytes, *Ahi = base + 2 * kOpBytes, *Alo = base + 3 * kOpBytes;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    if (tid == 0) {
+        mbar_init(&sh->mma_bar, 1);
+        mbar_init(&sh->tma_bar, 1);
+        sh->err = 0;
+        fence_barrier_init();
+    }
+    __syncthreads();
+    if (warp == 0) tmem_alloc(&sh->tmem_slot, 128);
+    load_transform(Thi, gT, sh);
+    for (int k0 = 0; k0 < kP; k0 += 32) {
+        float v[32];
+#pragma unroll
+        for (int i = 0; i < 32; i += 4) {
+            float4 w = valid ? *reinterpret_cast<const float4 *>(row_src + k0 + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+            v[i] = w.x;
+            v[i + 1] = w.y;
+            v[i + 2] = w.z;
+            v[i + 3] = w.w;
+        }
+        write_split32(Ahi, Alo, tid, k0, v);
+    }
+    fence_async_smem();
+    tc_before();
+    __syncthreads();
+    tc_after();
+    const uint32_t tmem = sh->tmem_slot;
+    bool ok = mbar_wait(&sh->tma_bar, 0);
+    if (tid == 0) {
+        if (ok)
+            issue_gemm(tmem, 0, smem_u32(Ahi), smem_u32(Alo), smem_u32(Thi), smem_u32(Tlo), &sh->mma_bar);
+        else
+            sh->err = 1;
+    }
+    __syncthreads();
+    bool issued = sh->err == 0;
+    if (issued && !mbar_wait(&sh->mma_bar, 0)) atomicOr(&sh->err, 2);
+    tc_after();
+    __syncthreads();
+    *tmem_out = tmem;
+    return sh->err == 0;
+}
+
+__device__ __forceinline__ void tc_row_release(TcShared *sh, uint32_t tmem, int32_t *gerr) {
+    const int tid = threadIdx.x, warp = tid >> 5;
+    if (tid == 0 && sh->err) atomicOr(gerr, sh->err);
+    if (sh->err & 2) mbar_wait(&sh->mma_bar, 0);  // let an overdue MMA drain (bounded)
+    tc_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, 128);
+}
+
+// G1: positions, estimator of the previous step, forces.
+template <int PESK>
+__global__ void __launch_bounds__(128, 1) k_tc_g1(TcArgs a, int do_est, int write_x) {
+    extern __shared__ unsigned char dsm[];
+    unsigned char *base = align1k(dsm);
+    TcShared *sh = reinterpret_cast<TcShared *>(base + kSmemOps);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int nd = a.nd, rpc = kRows / nd;
+    const int rloc = tid / nd, j = tid - rloc * nd;
+    const int64_t ring = (int64_t)blockIdx.x * rpc + rloc;
+    const bool valid = ring < a.nrings;
+    const bool odd = (j & 1) != 0;
+    const size_t off = valid ? ((size_t)ring * nd + j) * kP : 0;
+    const int64_t s = *a.stepA;
+    uint32_t tmem;
+    bool ok = tc_row_gemm(base, sh, a.gT, a.q + off, valid, &tmem);
+    if (ok) {
+        const int lam = valid ? a.ringlam[ring] : 0;
+        const float xa = (float)a.avec[j];
+        const float xslope = valid ? (float)((a.bvec[(size_t)lam * nd + j] - a.avec[j]) / (double)(kP + 1)) : 0.f;
+        const uint32_t laddr = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
+        for (int n0 = 0; n0 < kP; n0 += 32) {
+            float xv[32];
+            __syncwarp();  // tcgen05.ld is .sync.aligned: issue it from a converged warp
+            tmem_ld32(laddr + (uint32_t)n0, xv);
+#pragma unroll
+            for (int t = 0; t < 32; t++) xv[t] += xa + xslope * (float)(n0 + t + 1);
+            if (n0 == kP - 32 && do_est) {
+                // estimator of step s-1 (verletmodule.f90:397-403): bead P is the last column
+                const int atom = j / a.ndim;
+                double contr = valid ? a.mass[atom] * (-(double)xv[31]) * a.dbdl[(size_t)lam * nd + j] : 0.0;
+                if (nd == 2) contr += __shfl_xor_sync(0xffffffffu, contr, 1);
+                if (valid && j == 0 && (s - 1) >= a.imin) {
+                    RingAcc *r = &a.acc[ring];
+                    if (r->status == 0) r->dhdr_sum += contr;
+                    r->nsamples += 1;
+                }
+            }
+            if (valid && write_x)
+#pragma unroll
+                for (int t = 0; t < 32; t += 4)
+                    *reinterpret_cast<float4 *>(a.x + off + n0 + t) = make_float4(xv[t], xv[t + 1], xv[t + 2], xv[t + 3]);
+            float fv[32];
+            chunk_forces<PESK>(a, xv, fv, odd);
+            if (valid)
+#pragma unroll
+                for (int t = 0; t < 32; t += 4)
+                    *reinterpret_cast<float4 *>(a.f + off + n0 + t) = make_float4(fv[t], fv[t + 1], fv[t + 2], fv[t + 3]);
+        }
+    }
+    if (blockIdx.x == 0 && tid == 0) *a.stepB = s;
+    tc_row_release(sh, tmem, a.err);
+}
+
+// G2: kick with T F, half rotation, OU, half rotation (verletmodule.f90:423-435).
+__global__ void __launch_bounds__(128, 1) k_tc_g2(TcArgs a) {
+    extern __shared__ unsigned char dsm[];
+    unsigned char *base = align1k(dsm);
+    float *scoef = reinterpret_cast<float *>(base + kSmemOps + 256);
+    TcShared *sh = reinterpret_cast<TcShared *>(base + kSmemOps);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int nd = a.nd, rpc = kRows / nd;
+    const int rloc = tid / nd, j = tid - rloc * nd;
+    const int64_t ring = (int64_t)blockIdx.x * rpc + rloc;
+    const bool valid = ring < a.nrings;
+    const size_t off = valid ? ((size_t)ring * nd + j) * kP : 0;
+    const int64_t s = *a.stepB;
+    for (int i = tid; i < a.natom * kP * 8; i += 128) scoef[i] = a.coef[i];
+    uint32_t tmem;
+    bool ok = tc_row_gemm(base, sh, a.gT, a.f + off, valid, &tmem);
+    if (ok) {
+        const uint64_t seed = valid ? a.ringseed[ring] : 0;
+        const uint32_t stream = valid ? a.ringstream[ring] : 0;
+        const float *cf = scoef + (size_t)(j / a.ndim) * kP * 8;
+        const float dt = a.dt;
+        const uint32_t st = (uint32_t)s;
+        const uint32_t laddr = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
+        bool bad = false;
+        for (int n0 = 0; n0 < kP; n0 += 32) {
+            float gv[32];
+            __syncwarp();  // tcgen05.ld is .sync.aligned: issue it from a converged warp
+            tmem_ld32(laddr + (uint32_t)n0, gv);
+            if (!valid) continue;
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int kk = n0 + 4 * u;
+                U4 o = philox_block(seed, stream, st, kRngLangevin, (uint32_t)((j * kP + kk) >> 2));
+                float z[4];
+                box_muller_f(o.x, o.y, z[0], z[1]);
+                box_muller_f(o.z, o.w, z[2], z[3]);
+                float4 qv = *reinterpret_cast<const float4 *>(a.q + off + kk);
+                float4 pv = *reinterpret_cast<const float4 *>(a.pi + off + kk);
+                float qa[4] = {qv.x, qv.y, qv.z, qv.w}, pa[4] = {pv.x, pv.y, pv.z, pv.w};
+#pragma unroll
+                for (int e = 0; e < 4; e++) {
+                    const float4 c4 = *reinterpret_cast<const float4 *>(cf + (kk + e) * 8);
+                    const float2 c2 = *reinterpret_cast<const float2 *>(cf + (kk + e) * 8 + 4);
+                    float p0 = pa[e] - dt * gv[4 * u + e];
+                    float q0 = qa[e];
+                    float p1 = c4.x * p0 + c4.y * q0;
+                    float q1 = c4.z * p0 + c4.w * q0;
+                    p1 = c2.x * p1 + c2.y * z[e];
+                    pa[e] = c4.x * p1 + c4.y * q1;
+                    qa[e] = c4.z * p1 + c4.w * q1;
+                    bad |= (pa[e] != pa[e]);
+                }
+                *reinterpret_cast<float4 *>(a.q + off + kk) = make_float4(qa[0], qa[1], qa[2], qa[3]);
+                *reinterpret_cast<float4 *>(a.pi + off + kk) = make_float4(pa[0], pa[1], pa[2], pa[3]);
+            }
+        }
+        if (bad && valid) {
+            if (atomicOr(&a.acc[ring].status, PG_RING_NAN) == 0) a.acc[ring].pad = (int32_t)s;
+        }
+    }
+    if (blockIdx.x == 0 && tid == 0) *a.stepA = s + 1;
+    tc_row_release(sh, tmem, a.err);
+}
+
+// Host: split-BF16 image of T in the K-major core-matrix layout (B operand, rows = beads).
+static void build_split_image(int P, std::vector<unsigned char> &img) {
+    std::vector<double> T;
+    build_transmatrix(P, T);
+    img.assign(2 * kOpBytes, 0);
+    for (int n = 0; n < P; n++)
+        for (int k = 0; k < P; k++) {
+            double v = T[(size_t)n + (size_t)P * k];
+            __nv_bfloat16 hi = __float2bfloat16_rn((float)v);
+            double r = v - (double)__bfloat162float(hi);
+            __nv_bfloat16 lo = __float2bfloat16_rn((float)r);
+            uint32_t off = op_offset(n, k);
+            memcpy(&img[off], &hi, 2);
+            memcpy(&img[kOpBytes + off], &lo, 2);
+        }
+}
+
+static size_t tc_smem_bytes(int natom) {
+    return (size_t)kSmemOps + 1024 + 256 + (size_t)natom * kP * 8 * sizeof(float) + 64;
+}
+
+// Tbf layout: [T image 64 KB | FP32 coefficients | error word | stepB | pad]
+static size_t tbf_coef_off() { return 2 * (size_t)kOpBytes; }
+static size_t tbf_err_off(int natom) { return tbf_coef_off() + (size_t)natom * kP * 8 * sizeof(float); }
+
+}  // namespace
+
+int tc_built() { return 1; }
+
+int tc_supported(const TiState &st, const pg_ctx &ctx) {
+    if (st.P != kP) return 0;
+    if (st.cfg.thermostat != PG_LANGEVIN) return 0;
+    if (st.cfg.dhdr_limit >= 0.0) return 0;
+    if (ctx.pes_id == PG_PES_2DTEST && ctx.nd == 2) return 1;
+    if (ctx.pes_id == PG_PES_1D && ctx.nd == 1) return 1;
+    return 0;
+}
+
+int tc_prepare(pg_ctx *ctx, TiState &st) {
+    std::vector<unsigned char> img;
+    build_split_image(st.P, img);
+    size_t ncoef = (size_t)ctx->natom * kP * 8;
+    size_t bytes = tbf_err_off(ctx->natom) + 64;
+    cudaError_t e = st.Tbf.ensure(bytes);
+    if (e != cudaSuccess) return cuda_fail(e, "tensor-core tables");
+    std::vector<ModeCoef> mc((size_t)ctx->natom * st.P);
+    PG_CUDA(cudaMemcpyAsync(mc.data(), st.coef.ptr, mc.size() * sizeof(ModeCoef), cudaMemcpyDeviceToHost,
+                            ctx->stream));
+    PG_CUDA(cudaStreamSynchronize(ctx->stream));
+    std::vector<float> cf(ncoef, 0.f);
+    for (int at = 0; at < ctx->natom; at++)
+        for (int k = 0; k < kP; k++) {
+            const ModeCoef &c = mc[(size_t)at + (size_t)ctx->natom * k];
+            float *o = &cf[((size_t)at * kP + k) * 8];
+            o[0] = (float)c.rA;
+            o[1] = (float)c.rB;
+            o[2] = (float)c.rC;
+            o[3] = (float)c.rD;
+            o[4] = (float)c.ou_a;
+            o[5] = (float)c.ou_s;
+        }
+    unsigned char *d = st.Tbf.as<unsigned char>();
+    PG_CUDA(cudaMemcpyAsync(d, img.data(), img.size(), cudaMemcpyHostToDevice, ctx->stream));
+    PG_CUDA(cudaMemcpyAsync(d + tbf_coef_off(), cf.data(), cf.size() * sizeof(float), cudaMemcpyHostToDevice,
+                            ctx->stream));
+    PG_CUDA(cudaMemsetAsync(d + tbf_err_off(ctx->natom), 0, 64, ctx->stream));
+    PG_CUDA(cudaStreamSynchronize(ctx->stream));
+    size_t sm = tc_smem_bytes(ctx->natom);
+    PG_CUDA(cudaFuncSetAttribute(k_tc_g1<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    PG_CUDA(cudaFuncSetAttribute(k_tc_g1<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    PG_CUDA(cudaFuncSetAttribute(k_tc_g2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    return PG_OK;
+}
+
+int32_t tc_error(pg_ctx *ctx, TiState &st) {
+    const unsigned char *d = st.Tbf.as<unsigned char>();
+    int32_t e = 0;
+    if (cudaMemcpyAsync(&e, d + tbf_err_off(ctx->natom), sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream) !=
+        cudaSuccess)
+        return -1;
+    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return -1;
+    return e;
+}
+
+int tc_launch(pg_ctx *ctx, TiState &st, int64_t, int64_t nsteps, cudaStream_t s) {
+    if (nsteps < 0) return PG_OK;  // the HBM copy of the state is current after every launch
+    TcArgs a;
+    memset(&a, 0, sizeof(a));
+    a.nrings = st.nrings;
+    a.nd = st.nd;
+    a.ndim = ctx->ndim;
+    a.natom = ctx->natom;
+    a.dt = (float)st.cfg.dt;
+    a.imin = st.cfg.imin;
+    unsigned char *d = st.Tbf.as<unsigned char>();
+    a.gT = d;
+    a.coef = reinterpret_cast<const float *>(d + tbf_coef_off());
+    a.err = reinterpret_cast<int32_t *>(d + tbf_err_off(ctx->natom));
+    a.stepB = reinterpret_cast<int64_t *>(d + tbf_err_off(ctx->natom) + 8);
+    a.stepA = reinterpret_cast<int64_t *>(st.red.as<double>() + 3 * st.nlambda);
+    a.mass = ctx->d_mass.as<double>();
+    a.avec = st.avec.as<double>();
+    a.bvec = st.bvec.as<double>();
+    a.dbdl = st.dbdl.as<double>();
+    a.ringlam = st.ringlam.as<int32_t>();
+    a.ringseed = st.ringseed.as<uint64_t>();
+    a.ringstream = st.ringstream.as<uint32_t>();
+    a.q = st.q.as<float>();
+    a.pi = st.pi.as<float>();
+    a.x = st.x.as<float>();
+    a.f = st.f.as<float>();
+    a.acc = st.acc.as<RingAcc>();
+    int pesk = ctx->pes_id == PG_PES_2DTEST ? 2 : 1;
+    const std::vector<double> &p = ctx->params;
+    if (pesk == 2) {
+        int m = p.size() >= 4 ? (int)p[0] : 6;
+        double a0 = p.size() >= 4 ? p[1] : 2.0, b0 = p.size() >= 4 ? p[2] : 0.2, rho0 = p.size() >= 4 ? p[3] : 3.0;
+        a.nwell = m;
+        for (int k = 0; k < m; k++) {
+            a.wc[2 * k] = (float)(rho0 * std::cos((double)(k + 1) * 2.0 * kPiRef / (double)m));
+            a.wc[2 * k + 1] = (float)(rho0 * std::sin((double)(k + 1) * 2.0 * kPiRef / (double)m));
+        }
+        a.a0 = (float)a0;
+        a.b0 = (float)b0;
+        a.pow10 = ((float)a0 == 10.0f * (float)b0) ? 1 : 0;
+    } else {
+        a.H = p.size() >= 2 ? (float)p[0] : 1.0f;
+        a.x0 = p.size() >= 2 ? (float)p[1] : 1.0f;
+    }
+    int rpc = kRows / st.nd;
+    unsigned grid = (unsigned)((st.nrings + rpc - 1) / rpc);
+    size_t sm = tc_smem_bytes(ctx->natom);
+    for (int64_t i = 0; i <= nsteps; i++) {
+        const int do_est = i > 0 ? 1 : 0, final_pass = (i == nsteps) ? 1 : 0;
+        if (pesk == 2)
+            k_tc_g1<2><<<grid, 128, sm, s>>>(a, do_est, final_pass);
+        else
+            k_tc_g1<1><<<grid, 128, sm, s>>>(a, do_est, final_pass);
+        if (final_pass) break;
+        k_tc_g2<<<grid, 128, sm, s>>>(a);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "tensor-core step launch");
+    return PG_OK;
+}
+
+int tc_nm_transform(pg_ctx *ctx, int64_t P, int64_t ncol, const double *in, double *out) {
+    if (P != kP) return fail(PG_ERR_UNSUPPORTED, "tensor-core transform needs P = 128");
+    std::vector<unsigned char> img;
+    build_split_image((int)P, img);
+    size_t n = (size_t)P * ncol;
+    PG_CUDA(ctx->scratch_a.ensure(n * sizeof(double)));
+    PG_CUDA(ctx->scratch_b.ensure(n * sizeof(double)));
+    PG_CUDA(ctx->scratch_c.ensure(img.size() + 64));
+    cudaStream_t s = ctx->stream;
+    unsigned char *dimg = ctx->scratch_c.as<unsigned char>();
+    int32_t *derr = reinterpret_cast<int32_t *>(dimg + img.size());
+    PG_CUDA(cudaMemcpyAsync(dimg, img.data(), img.size(), cudaMemcpyHostToDevice, s));
+    PG_CUDA(cudaMemsetAsync(derr, 0, sizeof(int32_t), s));
+    PG_CUDA(cudaMemcpyAsync(ctx->scratch_a.ptr, in, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    size_t sm = (size_t)kSmemOps + 1024 + sizeof(TcShared) + 64;
+    PG_CUDA(cudaFuncSetAttribute(k_tc_transform, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    unsigned grid = (unsigned)((ncol + kRows - 1) / kRows);
+    k_tc_transform<<<grid, 128, sm, s>>>(dimg, ctx->scratch_a.as<double>(), ctx->scratch_b.as<double>(), ncol, derr);
+    PG_CUDA(cudaGetLastError());
+    int32_t herr = 0;
+    PG_CUDA(cudaMemcpyAsync(&herr, derr, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    PG_CUDA(cudaMemcpyAsync(out, ctx->scratch_b.ptr, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    PG_CUDA(cudaStreamSynchronize(s));
+    if (herr) return fail(PG_ERR_NUMERIC, "tensor-core transform: barrier wait timed out");
+    return PG_OK;
 }
 
 }  // namespace pg

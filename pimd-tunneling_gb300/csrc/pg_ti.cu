@@ -14,6 +14,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "pg_internal.h"
@@ -41,6 +42,8 @@ struct TiArgs {
     const double *T;          // P*P FP64
     const float *Tf;          // P*P FP32 copy
     const double *bv;         // nlambda*nd*P
+    const double *avec;       // nd: fixed start point a
+    const double *bvec;       // nlambda*nd: end points b
     const double *dbdl;       // nlambda*nd
     const double *xref;       // nlambda*nd*P
     const int32_t *ringlam;
@@ -123,6 +126,61 @@ __device__ __forceinline__ void ring_rotate(const TiArgs &a, R *__restrict__ q, 
     }
 }
 
+__device__ __forceinline__ double ring_contr(const TiArgs &a, const double *dbdl, double xlast,
+                                             int dof) {
+    return a.mass[dof / a.ndim] * (-xlast) * dbdl[dof];
+}
+
+// Spring line of the fixed-end polymer: x*_i = a + (b - a) i/(P+1), i = 1..P.
+// T x* = beadvec (verletmodule.f90:326-335), so x = T (q + beadvec) = T q + x*.
+__device__ __forceinline__ double xstar(const TiArgs &a, int lam, int dof, int bead) {
+    double av = a.avec[dof], bv = a.bvec[(size_t)lam * a.nd + dof];
+    return av + (bv - av) * (double)(bead + 1) / (double)(a.P + 1);
+}
+
+// Positions x = T (q + beadvec).  FP64: the reference arithmetic.  FP32: T q + x*,
+// so the large end-point shift never passes through FP32 rounding.
+template <typename R>
+__device__ __forceinline__ void ring_positions(const TiArgs &a, int lam, const R *__restrict__ q,
+                                               R *__restrict__ x, R *__restrict__ sbuf) {
+    if constexpr (sizeof(R) == sizeof(double)) {
+        ring_matvec<R>(a, q, a.bv + (size_t)lam * a.nd * a.P, x, sbuf);
+    } else {
+        ring_matvec<R>(a, q, nullptr, x, sbuf);
+        for (int e = threadIdx.x; e < a.nd * a.P; e += blockDim.x) {
+            int dof = e / a.P, i = e - dof * a.P;
+            x[e] = (R)((double)x[e] + xstar(a, lam, dof, i));
+        }
+        __syncthreads();
+    }
+}
+
+// NM coordinates q = T x - beadvec (FP64) or T (x - x*) (FP32).
+template <typename R>
+__device__ __forceinline__ void ring_nm_coords(const TiArgs &a, int lam, const R *__restrict__ x,
+                                               R *__restrict__ q, R *__restrict__ sbuf) {
+    const int P = a.P;
+    if constexpr (sizeof(R) == sizeof(double)) {
+        ring_matvec<R>(a, x, nullptr, q, sbuf);
+        const double *bv = a.bv + (size_t)lam * a.nd * P;
+        for (int e = threadIdx.x; e < a.nd * P; e += blockDim.x) q[e] = q[e] - bv[e];
+        __syncthreads();
+    } else {
+        const R *T = tmat<R>(a);
+        for (int dof = 0; dof < a.nd; dof++) {
+            for (int k = threadIdx.x; k < P; k += blockDim.x)
+                sbuf[k] = (R)((double)x[dof * P + k] - xstar(a, lam, dof, k));
+            __syncthreads();
+            for (int i = threadIdx.x; i < P; i += blockDim.x) {
+                R s = 0;
+                for (int k = 0; k < P; k++) s += T[(size_t)k * P + i] * sbuf[k];
+                q[dof * P + i] = s;
+            }
+            __syncthreads();
+        }
+    }
+}
+
 // Ring (re)initialisation: x = xref + sigma N, pi = pscale N, q = T x - beadvec.
 template <typename R>
 __device__ void ring_init_state(const TiArgs &a, int64_t r, uint32_t step, uint32_t px,
@@ -146,16 +204,7 @@ __device__ void ring_init_state(const TiArgs &a, int64_t r, uint32_t step, uint3
         }
     }
     __syncthreads();
-    // q = T x - beadvec
-    ring_matvec<R>(a, x, nullptr, q, sbuf);
-    const double *bv = a.bv + (size_t)lam * a.nd * P;
-    for (int e = threadIdx.x; e < a.nd * P; e += blockDim.x) q[e] = (R)((double)q[e] - bv[e]);
-    __syncthreads();
-}
-
-__device__ __forceinline__ double ring_contr(const TiArgs &a, const double *dbdl, double xlast,
-                                             int dof) {
-    return a.mass[dof / a.ndim] * (-xlast) * dbdl[dof];
+    ring_nm_coords<R>(a, lam, x, q, sbuf);
 }
 
 // ---------------------------------------------------------------- fused kernel
@@ -230,7 +279,7 @@ __global__ void __launch_bounds__(128) k_ti_fused(TiArgs a, R *__restrict__ gq, 
             }
             ring_rotate<R>(a, q, pi);
             __syncthreads();
-            ring_matvec<R>(a, q, bv, x, sbuf);
+            ring_positions<R>(a, lam, q, x, sbuf);
             ring_forces<R>(a, x, f);
             __syncthreads();
             ring_matvec<R>(a, f, nullptr, f, sbuf);
@@ -243,9 +292,12 @@ __global__ void __launch_bounds__(128) k_ti_fused(TiArgs a, R *__restrict__ gq, 
             __syncthreads();
         }
         // positions x = T (q + beadvec)
-        ring_matvec<R>(a, q, bv, x, sbuf);
+        ring_positions<R>(a, lam, q, x, sbuf);
         if (s_flag) {
-            if (threadIdx.x == 0) acc.status |= PG_RING_NAN;
+            if (threadIdx.x == 0) {
+                acc.status |= PG_RING_NAN;
+                acc.pad = (int32_t)s;  // step at which the NaN was seen
+            }
             break;
         }
         // estimator (verletmodule.f90:397-409), FP64 accumulation
@@ -615,6 +667,8 @@ static TiArgs make_args(pg_ctx *ctx, TiState &st, int64_t *step_dev) {
     a.T = st.T.as<double>();
     a.Tf = reinterpret_cast<const float *>(st.T.as<double>() + (size_t)st.P * st.P);
     a.bv = st.bv.as<double>();
+    a.avec = st.avec.as<double>();
+    a.bvec = st.bvec.as<double>();
     a.dbdl = st.dbdl.as<double>();
     a.xref = st.xref.as<double>();
     a.ringlam = st.ringlam.as<int32_t>();
@@ -732,7 +786,7 @@ extern "C" int pg_ti_setup(pg_ctx *ctx, const pg_ti_config *cfg, int64_t nrings,
     if (!cfg) return fail(PG_ERR_ARG, "cfg is NULL");
     if (cfg->nbeads < 2 || cfg->nbeads > 1024) return fail(PG_ERR_ARG, "nbeads must be in [2, 1024]");
     if (nrings < 1 || nrings > (int64_t)1 << 30) return fail(PG_ERR_ARG, "nrings out of range");
-    if (nlambda < 1 || nlambda > 4096) return fail(PG_ERR_ARG, "nlambda out of range");
+    if (nlambda < 1 || nlambda > ((int64_t)1 << 26)) return fail(PG_ERR_ARG, "nlambda out of range");
     if (!ring_lambda || !ring_seed || !ring_stream || !a || !b || !dbdl)
         return fail(PG_ERR_ARG, "NULL ring / endpoint array");
     if (!x0 && !xref) return fail(PG_ERR_ARG, "need x0 or xref");
@@ -828,6 +882,8 @@ extern "C" int pg_ti_setup(pg_ctx *ctx, const pg_ti_config *cfg, int64_t nrings,
     ENS(st.coef, coef.size() * sizeof(ModeCoef));
     ENS(st.bv, bv.size() * sizeof(double));
     ENS(st.dbdl, (size_t)nlambda * nd * sizeof(double));
+    ENS(st.avec, (size_t)nd * sizeof(double));
+    ENS(st.bvec, (size_t)nlambda * nd * sizeof(double));
     ENS(st.xref, (size_t)nlambda * nd * P * sizeof(double));
     ENS(st.ringlam, (size_t)nrings * sizeof(int32_t));
     ENS(st.ringseed, (size_t)nrings * sizeof(uint64_t));
@@ -845,6 +901,8 @@ extern "C" int pg_ti_setup(pg_ctx *ctx, const pg_ti_config *cfg, int64_t nrings,
     PG_CUDA(cudaMemcpyAsync(st.coef.ptr, coef.data(), coef.size() * sizeof(ModeCoef), cudaMemcpyHostToDevice, s));
     PG_CUDA(cudaMemcpyAsync(st.bv.ptr, bv.data(), bv.size() * sizeof(double), cudaMemcpyHostToDevice, s));
     PG_CUDA(cudaMemcpyAsync(st.dbdl.ptr, dbdl, (size_t)nlambda * nd * sizeof(double), cudaMemcpyHostToDevice, s));
+    PG_CUDA(cudaMemcpyAsync(st.avec.ptr, a, (size_t)nd * sizeof(double), cudaMemcpyHostToDevice, s));
+    PG_CUDA(cudaMemcpyAsync(st.bvec.ptr, b, (size_t)nlambda * nd * sizeof(double), cudaMemcpyHostToDevice, s));
     if (xref)
         PG_CUDA(cudaMemcpyAsync(st.xref.ptr, xref, (size_t)nlambda * nd * P * sizeof(double), cudaMemcpyHostToDevice, s));
     else
@@ -870,6 +928,7 @@ extern "C" int pg_ti_setup(pg_ctx *ctx, const pg_ti_config *cfg, int64_t nrings,
                                                            dx0.as<double>(), dp0.as<double>());
     }
     PG_CUDA(cudaGetLastError());
+    PG_CUDA(cudaStreamSynchronize(s));
     if (st.form == PG_FORM_TENSOR) {
         rc = tc_prepare(ctx, st);
         if (rc) {
@@ -877,7 +936,6 @@ extern "C" int pg_ti_setup(pg_ctx *ctx, const pg_ti_config *cfg, int64_t nrings,
             return rc;
         }
     }
-    PG_CUDA(cudaStreamSynchronize(s));
     return PG_OK;
 }
 
@@ -943,6 +1001,11 @@ static int ti_advance_impl(pg_ctx *ctx, int64_t nsteps, double *device_ms) {
         cudaEventDestroy(ev1);
     }
     st.step += nsteps;
+    if (st.form == PG_FORM_TENSOR) {
+        int32_t kerr = tc_error(ctx, st);
+        if (kerr) return fail(PG_ERR_NUMERIC, "tensor-core kernel: a barrier wait timed out (error word " +
+                                                  std::to_string(kerr) + ")");
+    }
     return PG_OK;
 }
 
@@ -951,6 +1014,23 @@ extern "C" int pg_ti_get_step(pg_ctx *ctx, int64_t *step) {
     if (rc) return rc;
     if (!ctx->ti) return fail(PG_ERR_STATE, "pg_ti_setup has not been called");
     if (step) *step = ctx->ti->step;
+    return PG_OK;
+}
+
+extern "C" int pg_ti_get_form(pg_ctx *ctx, int64_t nsteps, int32_t *form, int64_t *launches) {
+    int rc = check_ctx(ctx, true);
+    if (rc) return rc;
+    if (!ctx->ti) return fail(PG_ERR_STATE, "pg_ti_setup has not been called");
+    TiState &st = *ctx->ti;
+    if (form) *form = st.form;
+    if (launches) {
+        if (st.form == PG_FORM_TENSOR)
+            *launches = nsteps > 0 ? 2 * nsteps + 1 : 0;  // G1 + G2 per step, final G1
+        else if (st.form == PG_FORM_FUSED)
+            *launches = nsteps > 0 ? 2 : 0;  // fused kernel + step counter
+        else
+            *launches = 6 * nsteps;  // kick, nm, langevin (or Andersen), nm, estimator, step counter
+    }
     return PG_OK;
 }
 

@@ -266,3 +266,54 @@ def test_propagate_pimd_dropin(ctx, pg, oracle):
     xo, po, so, no, _ = _oracle_run(oracle, c, ti, prm, 50, x0=x0, p0=p0)
     np.testing.assert_allclose(x.reshape(xo.shape), xo, atol=1e-9)
     np.testing.assert_allclose(dh, so / no, rtol=1e-9)
+
+
+def _run(ctx, pg, c, ti, precision, form, nsteps, thermostat=2):
+    cfg = _gpu_cfg(pg, c, ti, precision, form, thermostat)
+    ctx.ti_setup(cfg, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
+    ctx.ti_advance(nsteps)
+    x, p = ctx.ti_state()
+    s, n, ri, st = ctx.ti_results()
+    return x, p, s, n, st
+
+
+@pytest.mark.parametrize("nrep,nint", [(4, 2), (50, 3)])
+def test_tensor_form_tracks_simt_fp32(ctx, pg, nrep, nint):
+    """tcgen05 split-BF16 kernel vs the FP32 SIMT kernel over a short run from the
+    same state (150 rings = 2 full CTAs + a partial one in the second case)."""
+    c, ti = _small_2d(P=128, nrep=nrep, nint=nint)
+    _set_system(ctx, c)
+    x1, p1, s1, n1, st1 = _run(ctx, pg, c, ti, pg.PG_MIXED, pg.PG_FORM_FUSED, 20)
+    x2, p2, s2, n2, st2 = _run(ctx, pg, c, ti, pg.PG_MIXED, pg.PG_FORM_TENSOR, 20)
+    assert np.all(st1 == 0) and np.all(st2 == 0)
+    np.testing.assert_array_equal(n1, n2)
+    assert np.max(np.abs(x1 - x2)) < 2e-3
+    assert np.max(np.abs(p1 - p2)) < 2e-3 * np.max(np.abs(p1))
+    np.testing.assert_allclose(s2, s1, rtol=2e-4)
+
+
+def test_tensor_form_1d_surface(ctx, pg):
+    c = dict(pgconfigs.load("c0"))
+    c["P"] = 128
+    ti = pgconfigs.TiInputs(c, nrep=3, nintegral=3)
+    _set_system(ctx, c)
+    x1, p1, s1, n1, st1 = _run(ctx, pg, c, ti, pg.PG_FP64, pg.PG_FORM_FUSED, 20)
+    x2, p2, s2, n2, st2 = _run(ctx, pg, c, ti, pg.PG_MIXED, pg.PG_FORM_TENSOR, 20)
+    assert np.all(st2 == 0)
+    assert np.max(np.abs(x1 - x2)) < 2e-3
+    np.testing.assert_allclose(s2, s1, rtol=2e-4)
+
+
+@pytest.mark.parametrize("form", ["fused", "tensor"])
+def test_mixed_long_run_has_no_nan(ctx, pg, form):
+    """Regression: thousands of steps over a thousand rings stay finite (the FP32
+    Box-Muller radius once hit rsqrt(0) near u = 1)."""
+    c, ti = _small_2d(P=128, nrep=64, nint=16)
+    _set_system(ctx, c)
+    fm = pg.PG_FORM_FUSED if form == "fused" else pg.PG_FORM_TENSOR
+    cfg = _gpu_cfg(pg, c, ti, pg.PG_MIXED, fm)
+    ctx.ti_setup(cfg, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
+    ctx.ti_advance(3000)
+    s, n, _, st = ctx.ti_results()
+    assert np.all(st == 0), np.sum(st != 0)
+    assert np.all(np.isfinite(s))
