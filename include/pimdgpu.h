@@ -130,6 +130,13 @@ int pg_ti_advance(pg_ctx *ctx, int64_t nsteps);
 /* pg_ti_advance that also returns the device time of the launched work in
  * milliseconds, measured with CUDA events recorded on the context's stream. */
 int pg_ti_advance_timed(pg_ctx *ctx, int64_t nsteps, double *device_ms);
+/* Advance nsteps with one CUDA-event pair around every kernel launch (no graph)
+ * and report, for up to 4 kernel kinds of the chosen form, the mean device time
+ * per launch (ms_per_launch[k]), the launches (count[k]), and the algorithmic
+ * HBM bytes one launch moves (bytes_per_launch[k]); names[k] points to a static
+ * kernel name.  Returns the number of kinds in *nkinds. */
+int pg_ti_kernel_times(pg_ctx *ctx, int64_t nsteps, int32_t *nkinds, double *ms_per_launch,
+                       int64_t *count, double *bytes_per_launch, const char **names);
 /* Cartesian positions and momenta of every ring (nrings*ndof*P each; either may be NULL). */
 int pg_ti_get_state(pg_ctx *ctx, double *x, double *p);
 /* Per-ring estimator sums: dhdr_sum[r] = sum of accepted contributions,

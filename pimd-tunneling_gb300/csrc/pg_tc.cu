@@ -637,9 +637,7 @@ int32_t tc_error(pg_ctx *ctx, TiState &st) {
     return e;
 }
 
-int tc_launch(pg_ctx *ctx, TiState &st, int64_t, int64_t nsteps, cudaStream_t s) {
-    if (nsteps < 0) return PG_OK;  // the HBM copy of the state is current after every launch
-    TcArgs a;
+static void tc_make_args(pg_ctx *ctx, TiState &st, TcArgs &a, int &pesk) {
     memset(&a, 0, sizeof(a));
     a.nrings = st.nrings;
     a.nd = st.nd;
@@ -665,7 +663,7 @@ int tc_launch(pg_ctx *ctx, TiState &st, int64_t, int64_t nsteps, cudaStream_t s)
     a.x = st.x.as<float>();
     a.f = st.f.as<float>();
     a.acc = st.acc.as<RingAcc>();
-    int pesk = ctx->pes_id == PG_PES_2DTEST ? 2 : 1;
+    pesk = ctx->pes_id == PG_PES_2DTEST ? 2 : 1;
     const std::vector<double> &p = ctx->params;
     if (pesk == 2) {
         int m = p.size() >= 4 ? (int)p[0] : 6;
@@ -682,20 +680,89 @@ int tc_launch(pg_ctx *ctx, TiState &st, int64_t, int64_t nsteps, cudaStream_t s)
         a.H = p.size() >= 2 ? (float)p[0] : 1.0f;
         a.x0 = p.size() >= 2 ? (float)p[1] : 1.0f;
     }
+}
+
+static unsigned tc_grid(const TiState &st) {
     int rpc = kRows / st.nd;
-    unsigned grid = (unsigned)((st.nrings + rpc - 1) / rpc);
+    return (unsigned)((st.nrings + rpc - 1) / rpc);
+}
+
+int tc_launch_one(pg_ctx *ctx, TiState &st, int do_est, int final_pass, cudaStream_t s) {
+    TcArgs a;
+    int pesk;
+    tc_make_args(ctx, st, a, pesk);
     size_t sm = tc_smem_bytes(ctx->natom);
+    if (pesk == 2)
+        k_tc_g1<2><<<tc_grid(st), 128, sm, s>>>(a, do_est, final_pass);
+    else
+        k_tc_g1<1><<<tc_grid(st), 128, sm, s>>>(a, do_est, final_pass);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? PG_OK : cuda_fail(e, "k_tc_g1 launch");
+}
+
+int tc_launch_g2(pg_ctx *ctx, TiState &st, cudaStream_t s) {
+    TcArgs a;
+    int pesk;
+    tc_make_args(ctx, st, a, pesk);
+    k_tc_g2<<<tc_grid(st), 128, tc_smem_bytes(ctx->natom), s>>>(a);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? PG_OK : cuda_fail(e, "k_tc_g2 launch");
+}
+
+int tc_launch(pg_ctx *ctx, TiState &st, int64_t, int64_t nsteps, cudaStream_t s) {
+    if (nsteps < 0) return PG_OK;  // the HBM copy of the state is current after every launch
     for (int64_t i = 0; i <= nsteps; i++) {
         const int do_est = i > 0 ? 1 : 0, final_pass = (i == nsteps) ? 1 : 0;
-        if (pesk == 2)
-            k_tc_g1<2><<<grid, 128, sm, s>>>(a, do_est, final_pass);
-        else
-            k_tc_g1<1><<<grid, 128, sm, s>>>(a, do_est, final_pass);
+        int rc = tc_launch_one(ctx, st, do_est, final_pass, s);
+        if (rc) return rc;
         if (final_pass) break;
-        k_tc_g2<<<grid, 128, sm, s>>>(a);
+        rc = tc_launch_g2(ctx, st, s);
+        if (rc) return rc;
     }
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return cuda_fail(e, "tensor-core step launch");
+    return PG_OK;
+}
+
+// Per-kernel event timing of nsteps steps (direct launches, no graph): ms[0] = G1, ms[1] = G2.
+int tc_kernel_times(pg_ctx *ctx, TiState &st, int64_t nsteps, double *ms, int64_t *count) {
+    cudaStream_t s = ctx->stream;
+    std::vector<cudaEvent_t> ev(4 * nsteps + 2);
+    for (auto &e : ev) PG_CUDA(cudaEventCreate(&e));
+    // record G1/G2 separately by launching one step at a time through tc_launch's
+    // kernels: a step is G1 (no estimator skip after the first) + G2; the final G1
+    // is launched once at the end.
+    double t1 = 0.0, t2 = 0.0;
+    int64_t n1 = 0, n2 = 0;
+    for (int64_t i = 0; i < nsteps; i++) {
+        PG_CUDA(cudaEventRecord(ev[4 * i], s));
+        int rc = tc_launch_one(ctx, st, i > 0 ? 1 : 0, 0, s);
+        if (rc) return rc;
+        PG_CUDA(cudaEventRecord(ev[4 * i + 1], s));
+        PG_CUDA(cudaEventRecord(ev[4 * i + 2], s));
+        rc = tc_launch_g2(ctx, st, s);
+        if (rc) return rc;
+        PG_CUDA(cudaEventRecord(ev[4 * i + 3], s));
+    }
+    PG_CUDA(cudaEventRecord(ev[4 * nsteps], s));
+    int rc = tc_launch_one(ctx, st, 1, 1, s);
+    if (rc) return rc;
+    PG_CUDA(cudaEventRecord(ev[4 * nsteps + 1], s));
+    PG_CUDA(cudaStreamSynchronize(s));
+    for (int64_t i = 0; i <= nsteps; i++) {
+        float a = 0.f;
+        PG_CUDA(cudaEventElapsedTime(&a, ev[4 * i], ev[4 * i + 1]));
+        t1 += a;
+        n1++;
+        if (i < nsteps) {
+            PG_CUDA(cudaEventElapsedTime(&a, ev[4 * i + 2], ev[4 * i + 3]));
+            t2 += a;
+            n2++;
+        }
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    ms[0] = t1 / (double)n1;
+    ms[1] = n2 ? t2 / (double)n2 : 0.0;
+    count[0] = n1;
+    count[1] = n2;
     return PG_OK;
 }
 

@@ -1017,6 +1017,48 @@ extern "C" int pg_ti_get_step(pg_ctx *ctx, int64_t *step) {
     return PG_OK;
 }
 
+extern "C" int pg_ti_kernel_times(pg_ctx *ctx, int64_t nsteps, int32_t *nkinds, double *ms_per_launch,
+                                  int64_t *count, double *bytes_per_launch, const char **names) {
+    int rc = check_ctx(ctx, true);
+    if (rc) return rc;
+    if (!ctx->ti) return fail(PG_ERR_STATE, "pg_ti_setup has not been called");
+    if (nsteps < 1 || !nkinds || !ms_per_launch || !count || !bytes_per_launch)
+        return fail(PG_ERR_ARG, "bad kernel-time arguments");
+    TiState &st = *ctx->ti;
+    const double arr = (double)st.nrings * st.nd * st.P * (st.fp32 ? 4.0 : 8.0);  // one state array
+    if (st.form == PG_FORM_TENSOR) {
+        double ms[2];
+        int64_t n[2];
+        rc = tc_kernel_times(ctx, st, nsteps, ms, n);
+        if (rc) return rc;
+        *nkinds = 2;
+        ms_per_launch[0] = ms[0];
+        ms_per_launch[1] = ms[1];
+        count[0] = n[0];
+        count[1] = n[1];
+        bytes_per_launch[0] = 2.0 * arr;  // G1: read q, write F
+        bytes_per_launch[1] = 5.0 * arr;  // G2: read F, q, pi; write q, pi
+        if (names) {
+            names[0] = "k_tc_g1 (positions, estimator, forces; split-BF16 tcgen05 GEMM)";
+            names[1] = "k_tc_g2 (kick, rotation, OU; split-BF16 tcgen05 GEMM)";
+        }
+        st.step += nsteps;
+        int32_t kerr = tc_error(ctx, st);
+        if (kerr) return fail(PG_ERR_NUMERIC, "tensor-core kernel error word " + std::to_string(kerr));
+        return PG_OK;
+    }
+    // fused / plain: one timed advance (graph) = one launch of the dominant kernel
+    double ms = 0.0;
+    rc = pg_ti_advance_timed(ctx, nsteps, &ms);
+    if (rc) return rc;
+    *nkinds = 1;
+    ms_per_launch[0] = ms;
+    count[0] = 1;
+    bytes_per_launch[0] = 4.0 * arr;  // state in and out once per launch (q, pi, x, acc)
+    if (names) names[0] = st.form == PG_FORM_FUSED ? "k_ti_fused (SIMT)" : "plain-form step sequence";
+    return PG_OK;
+}
+
 extern "C" int pg_ti_get_form(pg_ctx *ctx, int64_t nsteps, int32_t *form, int64_t *launches) {
     int rc = check_ctx(ctx, true);
     if (rc) return rc;

@@ -24,7 +24,7 @@ PG_ANDERSEN, PG_LANGEVIN = 1, 2
 EXPORTS = [
     "pg_create", "pg_destroy", "pg_last_error", "pg_version", "pg_set_system", "pg_pes_eval",
     "pg_pes_hessian", "pg_nm_transform", "pg_ti_setup", "pg_ti_advance", "pg_ti_get_state",
-    "pg_ti_get_results", "pg_ti_lambda_reduce", "pg_ti_get_step", "pg_ti_advance_timed", "pg_ti_get_form", "pg_ti_checkpoint_save",
+    "pg_ti_get_results", "pg_ti_lambda_reduce", "pg_ti_get_step", "pg_ti_advance_timed", "pg_ti_get_form", "pg_ti_kernel_times", "pg_ti_checkpoint_save",
     "pg_ti_checkpoint_load", "pg_ti_release", "pg_propagate_pimd", "pg_gauleg", "pg_spline",
     "pg_splint", "pg_ti_assemble", "pg_splitting_from_ratio", "pg_instanton_fg",
     "pg_instanton_optimize", "pg_um_hessian", "pg_instanton_logdet", "pg_rpi_assemble",
@@ -77,6 +77,7 @@ def lib():
         L.pg_ti_lambda_reduce.argtypes = [P, P, P, P]
         L.pg_ti_get_step.argtypes = [P, P]
         L.pg_ti_get_form.argtypes = [P, I64, P, P]
+        L.pg_ti_kernel_times.argtypes = [P, I64, P, P, P, P, P]
         L.pg_ti_checkpoint_save.argtypes = [P, C.c_char_p]
         L.pg_ti_checkpoint_load.argtypes = [P, C.c_char_p]
         L.pg_ti_release.argtypes = [P]
@@ -265,6 +266,16 @@ class Context:
         n = np.zeros(1, dtype=np.int64)
         check(lib().pg_ti_get_form(self.h, nsteps, _p(f), _p(n)))
         return int(f[0]), int(n[0])
+
+    def ti_kernel_times(self, nsteps):
+        """[(name, mean ms per launch, launches, algorithmic bytes per launch)] over nsteps steps."""
+        nk = C.c_int32()
+        ms = np.zeros(4)
+        cnt = np.zeros(4, dtype=np.int64)
+        by = np.zeros(4)
+        names = (C.c_char_p * 4)()
+        check(lib().pg_ti_kernel_times(self.h, nsteps, C.byref(nk), _p(ms), _p(cnt), _p(by), names))
+        return [(names[i].decode(), float(ms[i]), int(cnt[i]), float(by[i])) for i in range(nk.value)]
 
     def ti_checkpoint_save(self, path):
         check(lib().pg_ti_checkpoint_save(self.h, path.encode()))
