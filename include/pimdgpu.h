@@ -95,6 +95,19 @@ int pg_pes_hessian(pg_ctx *ctx, int64_t nconf, const double *x, double *hess, in
 int pg_nm_transform(pg_ctx *ctx, int64_t P, int64_t ncol, const double *in, double *out,
                     int32_t precision);
 
+/* Allocation-free variant of the split-BF16 tcgen05 transform (pg_nm_transform
+ * with PG_MIXED, P = 128), for callers that cannot call cudaMalloc: applications
+ * whose device memory is owned by their own pool allocator, or code running
+ * while a CUDA graph is captured.  No counterpart in the reference.  d_in / d_out
+ * are caller-owned device buffers of ncol*128 doubles; stream is a cudaStream_t
+ * (NULL = default stream); synchronous at return.  The only scratch is a static
+ * 64 KB device array (the split image of T plus an error word) that every GPU
+ * loading the library holds until exit; P must be 128 (anything else is
+ * PG_ERR_ARG).  The first call on a device builds the image there, so make it
+ * before any stream capture.  All calls share the array: calls that overlap on
+ * the GPU race.  Allocates no device or pinned memory. */
+int pg_nm_transform_noalloc(int64_t P, int64_t ncol, const double *d_in, double *d_out, void *stream);
+
 /* ---------------------------------------------------------------- TI-PIMD */
 typedef struct pg_ti_config {
     int64_t nbeads;      /* P (namelist n) */

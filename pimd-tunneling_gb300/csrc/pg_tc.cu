@@ -279,6 +279,20 @@ __global__ void __launch_bounds__(128, 1) k_tc_transform(const unsigned char *__
     if (warp == 0) tmem_dealloc(tmem, 128);
 }
 
+// Writes the split-BF16 image of T (P = 128, K-major core-matrix layout) on the
+// device: one thread per (n, k) element.
+__global__ void k_build_split_image(unsigned char *img) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= kP * kP) return;
+    const int n = e / kP, k = e - n * kP;
+    double v = sin((double)((n + 1) * (k + 1)) * kPiRef / (double)(kP + 1)) * sqrt(2.0 / (double)(kP + 1));
+    __nv_bfloat16 hi = __float2bfloat16_rn((float)v);
+    __nv_bfloat16 lo = __float2bfloat16_rn((float)(v - (double)__bfloat162float(hi)));
+    const uint32_t off = op_offset(n, k);
+    *reinterpret_cast<__nv_bfloat16 *>(img + off) = hi;
+    *reinterpret_cast<__nv_bfloat16 *>(img + kOpBytes + off) = lo;
+}
+
 // ---------------------------------------------------------------- TI step on the tensor cores
 // One MD step = two launches, each with the single-GEMM structure of
 // k_tc_transform (128 threads = 128 ring-dof rows, one split-BF16 GEMM, 128
@@ -794,3 +808,65 @@ int tc_nm_transform(pg_ctx *ctx, int64_t P, int64_t ncol, const double *in, doub
 }
 
 }  // namespace pg
+
+// ---------------------------------------------------------------- allocation-free transform
+// Some callers cannot call cudaMalloc: a host application that hands all device
+// memory to its own pool allocator at start-up (an MPI / Fortran driver that
+// pre-allocates the GPU), or code that must not allocate while a CUDA graph is
+// being captured or a latency-critical stream is running, because cudaMalloc
+// can synchronise the device.  For them, pg_nm_transform_noalloc runs the
+// split-BF16 tcgen05 transform on caller-owned device buffers and keeps its only
+// scratch -- the 64 KB split-BF16 image of T and an error word -- in the static
+// device array below, sized for P = 128 (every GPU that loads the library holds
+// it until the process exits).
+namespace pg {
+namespace {
+constexpr size_t kNoAllocScratchBytes = 2 * (size_t)kOpBytes + 256;  // image + error word
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+constexpr int kMaxDevices = 64;
+static void *g_noalloc_ptr[kMaxDevices];  // device address of g_noalloc_scratch, per device
+static bool g_noalloc_ready[kMaxDevices];
+}  // namespace
+}  // namespace pg
+
+extern "C" int pg_nm_transform_noalloc(int64_t P, int64_t ncol, const double *d_in, double *d_out,
+                                       void *stream) {
+    using namespace pg;
+    if (P != kP)
+        return fail(PG_ERR_ARG, "pg_nm_transform_noalloc: the static scratch holds one 128 x 128 split-BF16 "
+                                "image, so P must be 128");
+    if (ncol < 0 || ncol > ((int64_t)1 << 31) * kRows) return fail(PG_ERR_ARG, "pg_nm_transform_noalloc: bad ncol");
+    if (ncol == 0) return PG_OK;
+    if (!d_in || !d_out) return fail(PG_ERR_ARG, "pg_nm_transform_noalloc: NULL device buffer");
+    int dev = 0;
+    PG_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return fail(PG_ERR_ARG, "pg_nm_transform_noalloc: device index too large");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    if (!g_noalloc_ready[dev]) {
+        // one-time set-up on this device (must come before any stream capture):
+        // the host-side name of the array is not a device address; ask the runtime.
+        void *ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+        k_build_split_image<<<(kP * kP + 255) / 256, 256, 0, s>>>(reinterpret_cast<unsigned char *>(ptr));
+        PG_CUDA(cudaGetLastError());
+        PG_CUDA(cudaStreamSynchronize(s));
+        size_t sm = (size_t)kSmemOps + 1024 + sizeof(TcShared) + 64;
+        PG_CUDA(cudaFuncSetAttribute(k_tc_transform, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        g_noalloc_ptr[dev] = ptr;
+        g_noalloc_ready[dev] = true;
+    }
+    unsigned char *img = reinterpret_cast<unsigned char *>(g_noalloc_ptr[dev]);
+    int32_t *derr = reinterpret_cast<int32_t *>(img + 2 * kOpBytes);
+    // the array keeps the previous call's contents: clear the error word
+    PG_CUDA(cudaMemsetAsync(derr, 0, sizeof(int32_t), s));
+    size_t sm = (size_t)kSmemOps + 1024 + sizeof(TcShared) + 64;
+    unsigned grid = (unsigned)((ncol + kRows - 1) / kRows);
+    k_tc_transform<<<grid, 128, sm, s>>>(img, d_in, d_out, ncol, derr);
+    PG_CUDA(cudaGetLastError());
+    int32_t herr = 0;
+    PG_CUDA(cudaMemcpyAsync(&herr, derr, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    PG_CUDA(cudaStreamSynchronize(s));
+    if (herr) return fail(PG_ERR_NUMERIC, "pg_nm_transform_noalloc: a barrier wait timed out");
+    return PG_OK;
+}

@@ -28,6 +28,7 @@ EXPORTS = [
     "pg_ti_checkpoint_load", "pg_ti_release", "pg_propagate_pimd", "pg_gauleg", "pg_spline",
     "pg_splint", "pg_ti_assemble", "pg_splitting_from_ratio", "pg_instanton_fg",
     "pg_instanton_optimize", "pg_um_hessian", "pg_instanton_logdet", "pg_rpi_assemble",
+    "pg_nm_transform_noalloc",
 ]
 
 
@@ -69,6 +70,7 @@ def lib():
         L.pg_pes_eval.argtypes = [P, I64, P, P, P, I32]
         L.pg_pes_hessian.argtypes = [P, I64, P, P, I32]
         L.pg_nm_transform.argtypes = [P, I64, I64, P, P, I32]
+        L.pg_nm_transform_noalloc.argtypes = [I64, I64, P, P, P]
         L.pg_ti_setup.argtypes = [P, P, I64, I64, P, P, P, P, P, P, P, P, P]
         L.pg_ti_advance.argtypes = [P, I64]
         L.pg_ti_advance_timed.argtypes = [P, I64, P]
