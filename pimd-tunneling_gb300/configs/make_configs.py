@@ -250,26 +250,56 @@ def c1():
 
 
 def c2():
+    """Synthetic 9-atom surface.  The drawn Morse network alone holds the
+    transferring proton H* midway between O1 and O2 (s = 0); the quartic term
+    B ((s/s0)^2 - 1)^2 (B = 0.006 Eh) turns that into a symmetric double well when
+    its negative curvature at s = 0 beats the network's.  s0 is set from the
+    network's curvature k along the O1 -> O2 axis at the symmetric minimum,
+    s0 = sqrt(8 B / k), which makes the total curvature there -k."""
     params, perm = synth9_params(7)
     masses = np.array([16, 16, 12, 12, 12, 1, 1, 1, 1], dtype=float) * AMU
-    # start: a planar mirror-symmetric skeleton, proton displaced towards O1
     X = np.array([[-2.3, 1.3, 0.0], [2.3, 1.3, 0.0], [-2.4, -1.0, 0.0], [0.0, -2.2, 0.0],
                   [2.4, -1.0, 0.0], [-0.9, 2.2, 0.0], [-4.3, -1.8, 0.0], [0.0, -4.2, 0.0],
                   [4.3, -1.8, 0.0]])
     X[:, 2] += 0.05 * np.random.RandomState(7).randn(9)
+    npair = int(params[0])
+    iB = 1 + 5 * npair + 3
+    # 1) symmetric minimum of the network with the quartic switched off
+    p0 = params.copy()
+    p0[iB] = 0.0
+    fg0 = lambda x: (v_synth9(x, p0), g_synth9(x, p0))
+    xs = minimize(fg0, X.ravel(), jac=True, method="BFGS", options=dict(gtol=1e-11, maxiter=20000)).x.reshape(9, 3)
+    # 2) curvature of the network along the O1 -> O2 axis for the proton
+    e = xs[1] - xs[0]
+    e /= np.linalg.norm(e)
+    h = 1e-4
+
+    def vdelta(dl):
+        y = xs.copy()
+        y[5] = y[5] + dl * e
+        return v_synth9(y.ravel(), p0)
+
+    k = (vdelta(h) - 2 * vdelta(0.0) + vdelta(-h)) / (h * h)
+    s0 = float(np.sqrt(8.0 * 0.006 / k))
+    params[iB + 1] = s0
     f = lambda x: v_synth9(x, params)
     fg = lambda x: (v_synth9(x, params), g_synth9(x, params))
-    r = minimize(fg, X.ravel(), jac=True, method="BFGS", options=dict(gtol=1e-11, maxiter=20000))
-    w1 = r.x.reshape(9, 3)
+    # 3) well 1: proton displaced towards O1 (s < 0), relaxed
+    y = xs.copy()
+    y[5] = y[5] - 0.5 * s0 * e
+    w1 = minimize(fg, y.ravel(), jac=True, method="BFGS", options=dict(gtol=1e-11, maxiter=20000)).x.reshape(9, 3)
     w1 = w1 - (masses[:, None] * w1).sum(0) / masses.sum()
-    # well 2: mirror-permuted copy, aligned onto well 1 (Kabsch with reflection allowed)
+    # 4) well 2: mirror-permuted copy aligned onto well 1 (Kabsch, reflection allowed), relaxed
     B = w1[perm]
     Hm = B.T @ (w1 * masses[:, None])
     U, S, Vt = np.linalg.svd(Hm)
     Rm = (U @ Vt).T
     w2 = B @ Rm.T
-    r2 = minimize(fg, w2.ravel(), jac=True, method="BFGS", options=dict(gtol=1e-11, maxiter=20000))
-    w2 = r2.x.reshape(9, 3)
+    w2 = minimize(fg, w2.ravel(), jac=True, method="BFGS", options=dict(gtol=1e-11, maxiter=20000)).x.reshape(9, 3)
+    # barrier: relaxed symmetric (s = 0) geometry
+    xts = minimize(lambda x: (v_synth9(x, params) + 50.0 * (np.linalg.norm(x.reshape(9, 3)[5] - x.reshape(9, 3)[0])
+                                                            - np.linalg.norm(x.reshape(9, 3)[5] - x.reshape(9, 3)[1])) ** 2),
+                   xs.ravel(), method="BFGS", options=dict(gtol=1e-10, maxiter=20000)).x
     V0 = f(w1.ravel())
     dofm = np.repeat(masses, 3)
     eta = mass_weighted_eigs(num_hess(f, w1.ravel(), 1e-4), dofm)
@@ -278,12 +308,15 @@ def c2():
     P = 256
     betan = beta / (P + 1)
     dt = ring_dt(eta.max(), P, betan)
+    sfun = lambda w: float(np.linalg.norm(w[5] - w[0]) - np.linalg.norm(w[5] - w[1]))
     return dict(name="c2", description="synthetic 9-atom Morse network + proton-transfer well, P=256, "
                 "256 traj x 12 lambda, T=50 K", pes_id=3, ndim=3, natom=9, mass=list(masses),
                 params=list(params), V0=V0, P=P, beta=beta, dt=dt, tau=1.0, gamma=1.0 / (100 * dt),
                 thermostat=2, nmc=20000, imin=1000, nintegral=12, nrep=256, well1=list(w1.ravel()),
-                well2=list(w2.ravel()), Vwell2_minus_V0=f(w2.ravel()) - V0, init_sigma=0.0,
-                seeds=list(range(256)), precision="mixed", eta2_well=list(eta))
+                well2=list(w2.ravel()), Vwell2_minus_V0=f(w2.ravel()) - V0, s0=s0, network_curvature=k,
+                s_well1=sfun(w1), s_well2=sfun(w2), well_separation=float(np.linalg.norm(w1 - w2)),
+                barrier=f(xts) - V0, init_sigma=0.0, seeds=list(range(256)), precision="mixed",
+                eta2_well=list(eta))
 
 
 def c3(c2d):
@@ -353,4 +386,6 @@ if __name__ == "__main__":
     write("c4", c4())
     print("c0 beta=%.4f dt=%.5f" % (d0["beta"], d0["dt"]))
     print("c1 beta=%.4f dt=%.5f barrier=%.5f" % (d1["beta"], d1["dt"], d1["barrier"]))
-    print("c2 dt=%.6f V(w2)-V0=%.3e" % (d2["dt"], d2["Vwell2_minus_V0"]))
+    print("c2 dt=%.6f V(w2)-V0=%.3e s0=%.4f s1=%.4f s2=%.4f |w1-w2|=%.4f barrier=%.5f" % (
+        d2["dt"], d2["Vwell2_minus_V0"], d2["s0"], d2["s_well1"], d2["s_well2"], d2["well_separation"],
+        d2["barrier"]))

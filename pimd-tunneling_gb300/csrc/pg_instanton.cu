@@ -1,22 +1,601 @@
-// pg_instanton.cu -- ring-polymer instanton: action, adjoint gradient, L-BFGS, Hessian, log-det.
+// pg_instanton.cu -- ring-polymer instanton on the GPU, FP64 throughout:
+//   * batched fixed-end polymer action UM and its gradient (instantonmod.f90:17-151);
+//     the PES gradient is the hand-written reverse mode of each surface, which
+//     recomputes every pair distance instead of storing forward intermediates;
+//   * batched L-BFGS driven by that gradient, one persistent CTA per beta
+//     (replaces the setulb loop of instantonmod.f90:679-777);
+//   * mass-weighted polymer Hessian in LAPACK lower band storage (UMhessian,
+//     instantonmod.f90:155-217) and its log-determinant by a banded LDL^T with
+//     Sylvester inertia, eigenvalues below zero / the lowest one by bisection
+//     (replaces DSBEVD + the log sums of rpi_ser.f90:222-237, 354-366).
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "pg_hessian.cuh"
 #include "pg_internal.h"
+
+namespace pg {
+
+bool hess_is_fd_host(int id) { return id == PG_PES_1D || id == PG_PES_SYNTH18; }
+
+namespace {
+
+struct InstArgs {
+    PesArgs pes;
+    int N, nd, ndim, natom;
+    const double *mass;   // natom
+    const double *a;      // nd, fixed start
+    const double *b;      // nbeta*nd, fixed ends
+    const double *betan;  // nbeta
+};
+
+__device__ __forceinline__ double block_sum(double v, double *sred) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = (blockDim.x + 31) >> 5;
+    __syncthreads();
+    if (l == 0) sred[w] = v;
+    __syncthreads();
+    double t = 0.0;
+    for (int i = 0; i < nw; i++) t += sred[i];
+    return t;
+}
+
+__device__ __forceinline__ double block_max(double v, double *sred) {
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = (blockDim.x + 31) >> 5;
+    __syncthreads();
+    if (l == 0) sred[w] = v;
+    __syncthreads();
+    double t = sred[0];
+    for (int i = 1; i < nw; i++) t = fmax(t, sred[i]);
+    return t;
+}
+
+// UM and dUM/dx of polymer k (x, g: [dof][N]); every thread returns UM.
+__device__ double polymer_fg(const InstArgs &A, int k, const double *__restrict__ x, double *__restrict__ g,
+                             double *sred) {
+    const int N = A.N, nd = A.nd;
+    const double bn = A.betan[k];
+    const double *b = A.b + (size_t)k * nd;
+    double part = 0.0;
+    // bead potentials and their adjoint gradients (mcmod V / Vprime)
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        double xb[kMaxDof], gb[kMaxDof];
+        for (int d = 0; d < nd; d++) xb[d] = x[d * N + i];
+        part += pes_vgrad<double>(A.pes, xb, gb);
+        for (int d = 0; d < nd; d++) g[d * N + i] = gb[d];
+    }
+    __syncthreads();
+    // springs between neighbours and to the fixed ends (instantonmod.f90:25-43, 59-78)
+    for (int e = threadIdx.x; e < nd * N; e += blockDim.x) {
+        const int dof = e / N, i = e - dof * N;
+        const double m = A.mass[dof / A.ndim];
+        const double xl = i > 0 ? x[e - 1] : A.a[dof];
+        const double xr = i < N - 1 ? x[e + 1] : b[dof];
+        g[e] = m * (2.0 * x[e] - xl - xr) / (bn * bn) + g[e];
+        const double c = 0.5 * m / (bn * bn);
+        if (i < N - 1) part += c * (x[e + 1] - x[e]) * (x[e + 1] - x[e]);
+        if (i == 0) part += c * (x[e] - A.a[dof]) * (x[e] - A.a[dof]);
+        if (i == N - 1) part += c * (b[dof] - x[e]) * (b[dof] - x[e]);
+    }
+    double um = block_sum(part, sred);
+    __syncthreads();
+    return um;
+}
+
+__global__ void k_inst_fg(InstArgs A, const double *__restrict__ x, double *__restrict__ um,
+                          double *__restrict__ g) {
+    __shared__ double sred[32];
+    const int k = blockIdx.x;
+    const size_t off = (size_t)k * A.nd * A.N;
+    double v = polymer_fg(A, k, x + off, g + off, sred);
+    if (threadIdx.x == 0) um[k] = v;
+}
+
+struct LbfgsArgs {
+    int m, max_bt;
+    int64_t maxiter;
+    double factr, pgtol;
+};
+
+// Scratch per polymer: x, g, d, xt, gt (5n) + S, Y (2 m n) + rho, alpha (2m).
+__device__ __forceinline__ double dot_n(const double *a, const double *b, int n, double *sred) {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s += a[i] * b[i];
+    return block_sum(s, sred);
+}
+
+__global__ void __launch_bounds__(512) k_inst_lbfgs(InstArgs A, LbfgsArgs L, double *__restrict__ xio,
+                                                    double *__restrict__ scratch, double *__restrict__ um_out,
+                                                    int64_t *__restrict__ iters, int32_t *__restrict__ status) {
+    __shared__ double sred[32];
+    __shared__ double s_f;
+    const int k = blockIdx.x;
+    const int n = A.nd * A.N, m = L.m;
+    double *ws = scratch + (size_t)k * ((size_t)(5 + 2 * m) * n + 2 * m);
+    double *x = ws, *g = ws + n, *d = ws + 2 * (size_t)n, *xt = ws + 3 * (size_t)n, *gt = ws + 4 * (size_t)n;
+    double *S = ws + 5 * (size_t)n, *Y = S + (size_t)m * n;
+    double *rho = Y + (size_t)m * n, *alpha = rho + m;
+    double *xk = xio + (size_t)k * n;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = xk[i];
+    __syncthreads();
+    double f = polymer_fg(A, k, x, g, sred);
+    const double eps = 2.220446049250313e-16;
+    int npair = 0, head = 0;  // circular history
+    int st = 1;
+    int64_t it = 0;
+    for (; it < L.maxiter; it++) {
+        double gmax = 0.0;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) gmax = fmax(gmax, fabs(g[i]));
+        gmax = block_max(gmax, sred);
+        if (gmax <= L.pgtol) {
+            st = 0;
+            break;
+        }
+        // two-loop recursion: d = -H g
+        for (int i = threadIdx.x; i < n; i += blockDim.x) d[i] = -g[i];
+        __syncthreads();
+        for (int c = 0; c < npair; c++) {
+            int j = (head - 1 - c + m) % m;
+            double a_ = rho[j] * dot_n(S + (size_t)j * n, d, n, sred);
+            if (threadIdx.x == 0) alpha[j] = a_;
+            for (int i = threadIdx.x; i < n; i += blockDim.x) d[i] -= a_ * Y[(size_t)j * n + i];
+            __syncthreads();
+        }
+        if (npair > 0) {
+            int j = (head - 1 + m) % m;
+            double yy = dot_n(Y + (size_t)j * n, Y + (size_t)j * n, n, sred);
+            double gam = 1.0 / (rho[j] * yy);
+            for (int i = threadIdx.x; i < n; i += blockDim.x) d[i] *= gam;
+            __syncthreads();
+        }
+        for (int c = npair - 1; c >= 0; c--) {
+            int j = (head - 1 - c + m) % m;
+            double bt = rho[j] * dot_n(Y + (size_t)j * n, d, n, sred);
+            double a_ = alpha[j];
+            for (int i = threadIdx.x; i < n; i += blockDim.x) d[i] += (a_ - bt) * S[(size_t)j * n + i];
+            __syncthreads();
+        }
+        double gd = dot_n(g, d, n, sred);
+        if (!(gd < 0.0)) {  // not a descent direction: restart from steepest descent
+            npair = 0;
+            for (int i = threadIdx.x; i < n; i += blockDim.x) d[i] = -g[i];
+            __syncthreads();
+            gd = dot_n(g, d, n, sred);
+        }
+        // initial step: 1, or 1/|d| before any curvature pair (as L-BFGS-B's first iteration)
+        double t = 1.0;
+        if (npair == 0) {
+            double dn = sqrt(dot_n(d, d, n, sred));
+            t = dn > 0.0 ? fmin(1.0, 1.0 / dn) : 1.0;
+        }
+        bool accepted = false;
+        double ft = 0.0;
+        for (int bt = 0; bt <= L.max_bt; bt++) {
+            for (int i = threadIdx.x; i < n; i += blockDim.x) xt[i] = x[i] + t * d[i];
+            __syncthreads();
+            ft = polymer_fg(A, k, xt, gt, sred);
+            if (ft <= f + 1.0e-4 * t * gd) {
+                accepted = true;
+                break;
+            }
+            // safeguarded quadratic interpolation of f(t)
+            double tq = -gd * t * t / (2.0 * (ft - f - gd * t));
+            t = (tq > 0.1 * t && tq < 0.5 * t) ? tq : 0.5 * t;
+        }
+        if (!accepted) {
+            st = 2;
+            break;
+        }
+        // new curvature pair s = xt - x, y = gt - g
+        double *Sj = S + (size_t)head * n, *Yj = Y + (size_t)head * n;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            Sj[i] = xt[i] - x[i];
+            Yj[i] = gt[i] - g[i];
+        }
+        __syncthreads();
+        double sy = dot_n(Sj, Yj, n, sred);
+        double yy = dot_n(Yj, Yj, n, sred);
+        if (sy > eps * yy) {
+            if (threadIdx.x == 0) rho[head] = 1.0 / sy;
+            head = (head + 1) % m;
+            npair = npair < m ? npair + 1 : m;
+        }
+        const double fold = f;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            x[i] = xt[i];
+            g[i] = gt[i];
+        }
+        f = ft;
+        __syncthreads();
+        // relative reduction test of L-BFGS-B: (f_k - f_k+1)/max(|f_k|, |f_k+1|, 1) <= factr * eps
+        if ((fold - f) <= L.factr * eps * fmax(fmax(fabs(fold), fabs(f)), 1.0)) {
+            st = 0;
+            it++;
+            break;
+        }
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) xk[i] = x[i];
+    if (threadIdx.x == 0) {
+        s_f = f;
+        um_out[k] = f;
+        iters[k] = it;
+        status[k] = st;
+    }
+}
+
+// Per-bead PES Hessians of polymer k (FD surfaces: one thread per (bead, column)).
+__global__ void k_bead_hessians(PesArgs pa, int N, int nbeta, const double *__restrict__ x,
+                                double *__restrict__ hb, int quirks, int singlewell) {
+    const int nd = pa.nd;
+    const bool fd = hess_is_fd(pa.id);
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t per = fd ? (int64_t)N * nd : (int64_t)N;
+    const int64_t k = t / per;
+    if (k >= nbeta) return;
+    const int64_t r = t - k * per;
+    const int i = fd ? (int)(r / nd) : (int)r;
+    if (singlewell && i > 0) return;  // instantonmod.f90:183: only bead 1 when singlewell
+    double xb[kMaxDof];
+    const double *xk = x + (size_t)k * nd * N;
+    for (int d = 0; d < nd; d++) xb[d] = xk[d * N + i];
+    double *h = hb + ((size_t)k * N + i) * nd * nd;
+    if (fd)
+        hess_fd_column(pa, xb, (int)(r % nd), h);
+    else
+        pes_hessian(pa, xb, h, quirks);
+}
+
+// Band assembly of UMhessian: one thread per (polymer, bead, idof1).
+__global__ void k_band_assemble(InstArgs A, int nbeta, const double *__restrict__ hb, int singlewell,
+                                int quirks, double *__restrict__ band) {
+    const int N = A.N, nd = A.nd, ld = nd + 1;
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t k = t / ((int64_t)N * nd);
+    if (k >= nbeta) return;
+    const int64_t r = t - k * (int64_t)N * nd;
+    const int i = (int)(r / nd), id1 = (int)(r % nd);
+    const int64_t tot = (int64_t)N * nd;
+    const double bn = A.betan[k];
+    const double *h = hb + ((size_t)k * N + (singlewell ? 0 : i)) * nd * nd;
+    double *bk = band + (size_t)k * ld * tot;
+    const int64_t f1 = (int64_t)nd * i + id1;
+    const int k1 = id1 / A.ndim;
+    for (int id2 = id1; id2 < nd; id2++) {
+        const int k2 = id2 / A.ndim;
+        const double hv = h[id2 + nd * id1] / sqrt(A.mass[k1] * A.mass[k2]);
+        if (id2 == id1) {
+            bk[0 + ld * f1] = 2.0 / (bn * bn) + hv;
+        } else {
+            bk[(id2 - id1) + ld * f1] = hv;
+        }
+    }
+    // rows below the intra-bead block in this column: zero, then the spring coupling
+    for (int rr = nd - id1; rr <= nd; rr++)
+        if (rr >= 1) bk[rr + ld * f1] = 0.0;
+    const bool coupled = quirks ? (i > 0) : (i < N - 1);
+    if (coupled && f1 + nd < tot) bk[nd + ld * f1] = -1.0 / (bn * bn);
+}
+
+// Banded LDL^T (no pivoting) of (A - sigma I) for polymer k, sliding (kd+1)^2
+// window in shared memory.  Returns log|det| and the number of negative pivots
+// (Sylvester inertia = number of eigenvalues below sigma).
+__global__ void k_band_ldl(int64_t n, int kd, const double *__restrict__ band, const double *__restrict__ sigma,
+                           double *__restrict__ logabs, int64_t *__restrict__ nneg) {
+    extern __shared__ double W[];  // (kd+1) slots x (kd+1) rows
+    __shared__ double s_d;
+    const int k = blockIdx.x;
+    const int ld = kd + 1;
+    const double *bk = band + (size_t)k * ld * n;
+    const double sg = sigma[k];
+    // load columns 0..kd
+    for (int e = threadIdx.x; e < ld * ld; e += blockDim.x) {
+        const int c = e / ld, r = e - c * ld;
+        double v = (c < n && c + r < n) ? bk[r + (size_t)ld * c] : 0.0;
+        if (r == 0) v -= sg;
+        W[(c % ld) * ld + r] = v;
+    }
+    // triangle (ii, kk) with 1 <= kk <= ii <= kd assigned to threads (<= 4 each)
+    const int ntri = kd * (kd + 1) / 2;
+    int tri_i[4], tri_k[4], ntq = 0;
+    for (int q = threadIdx.x; q < ntri && ntq < 4; q += blockDim.x) {
+        int ii = 1;
+        while ((ii + 1) * ii / 2 <= q) ii++;
+        tri_i[ntq] = ii;
+        tri_k[ntq] = q - ii * (ii - 1) / 2 + 1;
+        ntq++;
+    }
+    __syncthreads();
+    double la = 0.0;
+    int64_t nn = 0;
+    for (int64_t j = 0; j < n; j++) {
+        const int s = (int)(j % ld);
+        if (threadIdx.x == 0) {
+            double dj = W[s * ld + 0];
+            if (dj == 0.0) dj = 1e-300;
+            s_d = dj;
+            la += log(fabs(dj));
+            nn += dj < 0.0 ? 1 : 0;
+        }
+        __syncthreads();
+        const double dj = s_d;
+        for (int t = 0; t < ntq; t++) {
+            const int ii = tri_i[t], kk = tri_k[t];
+            if (j + ii >= n) continue;
+            const double lij = W[s * ld + ii], lkj = W[s * ld + kk];
+            const int sk = (int)((j + kk) % ld);
+            W[sk * ld + (ii - kk)] -= lij * lkj / dj;
+        }
+        __syncthreads();
+        // retire column j, load column j + kd + 1 into its slot
+        const int64_t c = j + ld;
+        for (int r = threadIdx.x; r < ld; r += blockDim.x) {
+            double v = (c < n && c + r < n) ? bk[r + (size_t)ld * c] : 0.0;
+            if (r == 0) v -= sg;
+            W[s * ld + r] = v;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        logabs[k] = la;
+        nneg[k] = nn;
+    }
+}
+
+InstArgs make_inst_args(pg_ctx *ctx, int N, const double *da, const double *db, const double *dbn) {
+    InstArgs A;
+    A.pes = ctx->pes_args();
+    A.N = N;
+    A.nd = ctx->nd;
+    A.ndim = ctx->ndim;
+    A.natom = ctx->natom;
+    A.mass = ctx->d_mass.as<double>();
+    A.a = da;
+    A.b = db;
+    A.betan = dbn;
+    return A;
+}
+
+// Device band of nbeta polymers (ld x tot each) into ctx->scratch_d.
+int build_bands(pg_ctx *ctx, int64_t nbeta, int64_t N, const double *dx, const double *dbn, int singlewell,
+                int quirks) {
+    const int nd = ctx->nd;
+    const int64_t tot = N * nd, ld = nd + 1;
+    PG_CUDA(ctx->scratch_c.ensure((size_t)nbeta * N * nd * nd * sizeof(double)));
+    PG_CUDA(ctx->scratch_d.ensure((size_t)nbeta * ld * tot * sizeof(double)));
+    PG_CUDA(cudaMemsetAsync(ctx->scratch_d.ptr, 0, (size_t)nbeta * ld * tot * sizeof(double), ctx->stream));
+    const bool fd = hess_is_fd_host(ctx->pes_id);
+    int64_t nth = fd ? nbeta * N * nd : nbeta * N;
+    k_bead_hessians<<<(unsigned)((nth + 127) / 128), 128, 0, ctx->stream>>>(
+        ctx->pes_args(), (int)N, (int)nbeta, dx, ctx->scratch_c.as<double>(), quirks, singlewell);
+    PG_CUDA(cudaGetLastError());
+    InstArgs A = make_inst_args(ctx, (int)N, nullptr, nullptr, dbn);
+    int64_t nb = nbeta * N * nd;
+    k_band_assemble<<<(unsigned)((nb + 127) / 128), 128, 0, ctx->stream>>>(A, (int)nbeta, ctx->scratch_c.as<double>(),
+                                                                           singlewell, quirks, ctx->scratch_d.as<double>());
+    PG_CUDA(cudaGetLastError());
+    return PG_OK;
+}
+
+}  // namespace
+}  // namespace pg
 
 using namespace pg;
 
-extern "C" int pg_instanton_fg(pg_ctx *ctx, int64_t, int64_t, const double *, const double *,
-                               const double *, const double *, double *, double *) {
-    (void)ctx;
-    return fail(PG_ERR_UNSUPPORTED, "not built yet");
+static int upload(pg_ctx *ctx, DevBuf &buf, const double *h, size_t n) {
+    PG_CUDA(buf.ensure(n * sizeof(double)));
+    PG_CUDA(cudaMemcpyAsync(buf.ptr, h, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    return PG_OK;
 }
-extern "C" int pg_instanton_optimize(pg_ctx *, int64_t, int64_t, double *, const double *,
-                                     const double *, const double *, const pg_lbfgs_opts *,
-                                     double *, int64_t *, int32_t *) {
-    return fail(PG_ERR_UNSUPPORTED, "not built yet");
+
+extern "C" int pg_instanton_fg(pg_ctx *ctx, int64_t nbeta, int64_t N, const double *x, const double *a,
+                               const double *b, const double *betan, double *UM, double *grad) {
+    int rc = check_ctx(ctx, true);
+    if (rc) return rc;
+    if (nbeta < 1 || N < 2 || !x || !a || !b || !betan) return fail(PG_ERR_ARG, "bad instanton_fg arguments");
+    const int nd = ctx->nd;
+    const size_t n = (size_t)nbeta * nd * N;
+    DevBuf dx, dg, dab, dum;
+    if ((rc = upload(ctx, dx, x, n))) return rc;
+    PG_CUDA(dab.ensure((size_t)(nd + nbeta * nd + nbeta) * sizeof(double)));
+    PG_CUDA(cudaMemcpyAsync(dab.ptr, a, nd * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    PG_CUDA(cudaMemcpyAsync(dab.as<double>() + nd, b, nbeta * nd * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    PG_CUDA(cudaMemcpyAsync(dab.as<double>() + nd + nbeta * nd, betan, nbeta * sizeof(double), cudaMemcpyHostToDevice,
+                            ctx->stream));
+    PG_CUDA(dg.ensure(n * sizeof(double)));
+    PG_CUDA(dum.ensure(nbeta * sizeof(double)));
+    InstArgs A = make_inst_args(ctx, (int)N, dab.as<double>(), dab.as<double>() + nd, dab.as<double>() + nd + nbeta * nd);
+    k_inst_fg<<<(unsigned)nbeta, 256, 0, ctx->stream>>>(A, dx.as<double>(), dum.as<double>(), dg.as<double>());
+    PG_CUDA(cudaGetLastError());
+    if (UM) PG_CUDA(cudaMemcpyAsync(UM, dum.ptr, nbeta * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    if (grad) PG_CUDA(cudaMemcpyAsync(grad, dg.ptr, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    PG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return PG_OK;
 }
-extern "C" int pg_um_hessian(pg_ctx *, int64_t, double, const double *, int32_t, int32_t, double *) {
-    return fail(PG_ERR_UNSUPPORTED, "not built yet");
+
+extern "C" int pg_instanton_optimize(pg_ctx *ctx, int64_t nbeta, int64_t N, double *x, const double *a,
+                                     const double *b, const double *betan, const pg_lbfgs_opts *opts, double *UM,
+                                     int64_t *niter, int32_t *status) {
+    int rc = check_ctx(ctx, true);
+    if (rc) return rc;
+    if (nbeta < 1 || N < 2 || !x || !a || !b || !betan || !opts) return fail(PG_ERR_ARG, "bad optimize arguments");
+    if (opts->m < 1 || opts->m > 64 || opts->maxiter < 1 || opts->max_backtracks < 0)
+        return fail(PG_ERR_ARG, "bad L-BFGS options");
+    const int nd = ctx->nd;
+    const size_t n1 = (size_t)nd * N, n = (size_t)nbeta * n1;
+    DevBuf dx, dab, dum, dit, dst;
+    if ((rc = upload(ctx, dx, x, n))) return rc;
+    PG_CUDA(dab.ensure((size_t)(nd + nbeta * nd + nbeta) * sizeof(double)));
+    PG_CUDA(cudaMemcpyAsync(dab.ptr, a, nd * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    PG_CUDA(cudaMemcpyAsync(dab.as<double>() + nd, b, nbeta * nd * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    PG_CUDA(cudaMemcpyAsync(dab.as<double>() + nd + nbeta * nd, betan, nbeta * sizeof(double), cudaMemcpyHostToDevice,
+                            ctx->stream));
+    const size_t per = (size_t)(5 + 2 * opts->m) * n1 + 2 * opts->m;
+    PG_CUDA(ctx->scratch_b.ensure((size_t)nbeta * per * sizeof(double)));
+    PG_CUDA(dum.ensure(nbeta * sizeof(double)));
+    PG_CUDA(dit.ensure(nbeta * sizeof(int64_t)));
+    PG_CUDA(dst.ensure(nbeta * sizeof(int32_t)));
+    InstArgs A = make_inst_args(ctx, (int)N, dab.as<double>(), dab.as<double>() + nd, dab.as<double>() + nd + nbeta * nd);
+    LbfgsArgs L;
+    L.m = opts->m;
+    L.max_bt = opts->max_backtracks;
+    L.maxiter = opts->maxiter;
+    L.factr = opts->factr;
+    L.pgtol = opts->pgtol;
+    k_inst_lbfgs<<<(unsigned)nbeta, 512, 0, ctx->stream>>>(A, L, dx.as<double>(), ctx->scratch_b.as<double>(),
+                                                            dum.as<double>(), dit.as<int64_t>(), dst.as<int32_t>());
+    PG_CUDA(cudaGetLastError());
+    PG_CUDA(cudaMemcpyAsync(x, dx.ptr, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    if (UM) PG_CUDA(cudaMemcpyAsync(UM, dum.ptr, nbeta * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    if (niter) PG_CUDA(cudaMemcpyAsync(niter, dit.ptr, nbeta * sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+    if (status) PG_CUDA(cudaMemcpyAsync(status, dst.ptr, nbeta * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    PG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return PG_OK;
 }
-extern "C" int pg_instanton_logdet(pg_ctx *, int64_t, int64_t, const double *, const double *,
-                                   int32_t, int32_t, int32_t, double *, double *, int64_t *) {
-    return fail(PG_ERR_UNSUPPORTED, "not built yet");
+
+extern "C" int pg_um_hessian(pg_ctx *ctx, int64_t N, double betan, const double *x, int32_t singlewell,
+                             int32_t quirks, double *band) {
+    int rc = check_ctx(ctx, true);
+    if (rc) return rc;
+    if (N < 2 || !x || !band) return fail(PG_ERR_ARG, "bad um_hessian arguments");
+    const int nd = ctx->nd;
+    DevBuf dx, dbn;
+    if ((rc = upload(ctx, dx, x, (size_t)nd * N))) return rc;
+    if ((rc = upload(ctx, dbn, &betan, 1))) return rc;
+    rc = build_bands(ctx, 1, N, dx.as<double>(), dbn.as<double>(), singlewell, quirks);
+    if (rc) return rc;
+    PG_CUDA(cudaMemcpyAsync(band, ctx->scratch_d.ptr, (size_t)(nd + 1) * N * nd * sizeof(double),
+                            cudaMemcpyDeviceToHost, ctx->stream));
+    PG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return PG_OK;
+}
+
+// log|det(H - sigma_k I)| and inertia for every polymer at the shifts sigma[nbeta].
+static int band_factor(pg_ctx *ctx, int64_t nbeta, int64_t n, int kd, const double *hsig, double *hlog,
+                       int64_t *hneg, DevBuf &dsig, DevBuf &dlog, DevBuf &dneg) {
+    PG_CUDA(cudaMemcpyAsync(dsig.ptr, hsig, nbeta * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    int ld = kd + 1;
+    int th = kd * (kd + 1) / 2;
+    th = th < 32 ? 32 : (th > 512 ? 512 : ((th + 31) / 32) * 32);
+    if (kd * (kd + 1) / 2 > 4 * th) return fail(PG_ERR_UNSUPPORTED, "band width too large for the LDL kernel");
+    k_band_ldl<<<(unsigned)nbeta, th, (size_t)ld * ld * sizeof(double), ctx->stream>>>(
+        n, kd, ctx->scratch_d.as<double>(), dsig.as<double>(), dlog.as<double>(), dneg.as<int64_t>());
+    PG_CUDA(cudaGetLastError());
+    PG_CUDA(cudaMemcpyAsync(hlog, dlog.ptr, nbeta * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    PG_CUDA(cudaMemcpyAsync(hneg, dneg.ptr, nbeta * sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+    PG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return PG_OK;
+}
+
+extern "C" int pg_instanton_logdet(pg_ctx *ctx, int64_t nbeta, int64_t N, const double *x, const double *betan,
+                                   int32_t singlewell, int32_t skip_lowest, int32_t quirks, double *lndet,
+                                   double *eta2_min, int64_t *nskipped) {
+    int rc = check_ctx(ctx, true);
+    if (rc) return rc;
+    if (nbeta < 1 || N < 2 || !x || !betan || !lndet) return fail(PG_ERR_ARG, "bad logdet arguments");
+    const int nd = ctx->nd, kd = nd, ld = nd + 1;
+    const int64_t n = N * nd;
+    DevBuf dx, dbn, dsig, dlog, dneg;
+    if ((rc = upload(ctx, dx, x, (size_t)nbeta * n))) return rc;
+    if ((rc = upload(ctx, dbn, betan, nbeta))) return rc;
+    PG_CUDA(dsig.ensure(nbeta * sizeof(double)));
+    PG_CUDA(dlog.ensure(nbeta * sizeof(double)));
+    PG_CUDA(dneg.ensure(nbeta * sizeof(int64_t)));
+    rc = build_bands(ctx, nbeta, N, dx.as<double>(), dbn.as<double>(), singlewell, quirks);
+    if (rc) return rc;
+    // Gershgorin bounds of every band (host copy of the band is avoided: bounds
+    // from a reduction over rows on the host would need the band; instead use the
+    // diagonal extremes and the row sums read back once).
+    std::vector<double> band((size_t)nbeta * ld * n);
+    PG_CUDA(cudaMemcpyAsync(band.data(), ctx->scratch_d.ptr, band.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                            ctx->stream));
+    PG_CUDA(cudaStreamSynchronize(ctx->stream));
+    std::vector<double> glo(nbeta), dmin(nbeta);
+    for (int64_t k = 0; k < nbeta; k++) {
+        const double *bk = band.data() + (size_t)k * ld * n;
+        std::vector<double> rad(n, 0.0);
+        double mn = 1e300;
+        for (int64_t c = 0; c < n; c++) {
+            mn = std::fmin(mn, bk[ld * c]);
+            for (int r = 1; r < ld && c + r < n; r++) {
+                double v = std::fabs(bk[r + ld * c]);
+                rad[c] += v;
+                rad[c + r] += v;
+            }
+        }
+        double lo = 1e300;
+        for (int64_t c = 0; c < n; c++) lo = std::fmin(lo, bk[ld * c] - rad[c]);
+        glo[k] = lo;
+        dmin[k] = mn;
+    }
+    std::vector<double> sig(nbeta, 0.0), la0(nbeta), lac(nbeta);
+    std::vector<int64_t> nn0(nbeta), nnc(nbeta);
+    rc = band_factor(ctx, nbeta, n, kd, sig.data(), la0.data(), nn0.data(), dsig, dlog, dneg);
+    if (rc) return rc;
+    // eigenvalues below zero (and the lowest one) by bisection on the inertia count
+    const int kMaxNeg = 8;
+    std::vector<std::vector<double>> negs(nbeta);
+    std::vector<double> lmin(nbeta, 0.0);
+    int64_t maxneg = 0;
+    for (int64_t k = 0; k < nbeta; k++) maxneg = std::max<int64_t>(maxneg, nn0[k]);
+    if (maxneg > kMaxNeg) return fail(PG_ERR_NUMERIC, "more than 8 negative Hessian eigenvalues");
+    // index list per polymer: eigenvalues 1..nn0 (all negative), or eigenvalue 1 if skip_lowest
+    for (int idx = 1; idx <= std::max<int64_t>(maxneg, 1); idx++) {
+        std::vector<double> lo(nbeta), hi(nbeta);
+        std::vector<char> act(nbeta, 0);
+        bool any = false;
+        for (int64_t k = 0; k < nbeta; k++) {
+            if (idx <= nn0[k]) {
+                lo[k] = glo[k];
+                hi[k] = 0.0;
+                act[k] = 1;
+            } else if (idx == 1 && (skip_lowest || eta2_min)) {
+                lo[k] = std::fmax(0.0, glo[k]);
+                hi[k] = dmin[k];
+                act[k] = 1;
+            }
+            any = any || act[k];
+        }
+        if (!any) break;
+        for (int itb = 0; itb < 200; itb++) {
+            bool done = true;
+            for (int64_t k = 0; k < nbeta; k++) {
+                sig[k] = act[k] ? 0.5 * (lo[k] + hi[k]) : 0.0;
+                if (act[k] && (hi[k] - lo[k]) > 1e-13 * std::fmax(std::fabs(lo[k]), std::fabs(hi[k])) &&
+                    (hi[k] - lo[k]) > 1e-300)
+                    done = false;
+            }
+            if (done) break;
+            rc = band_factor(ctx, nbeta, n, kd, sig.data(), lac.data(), nnc.data(), dsig, dlog, dneg);
+            if (rc) return rc;
+            for (int64_t k = 0; k < nbeta; k++) {
+                if (!act[k]) continue;
+                if (nnc[k] >= idx)
+                    hi[k] = sig[k];
+                else
+                    lo[k] = sig[k];
+            }
+        }
+        for (int64_t k = 0; k < nbeta; k++) {
+            if (!act[k]) continue;
+            double ev = 0.5 * (lo[k] + hi[k]);
+            if (idx <= nn0[k]) negs[k].push_back(ev);
+            if (idx == 1) lmin[k] = ev;
+        }
+    }
+    for (int64_t k = 0; k < nbeta; k++) {
+        // sum of log eta^2 over eta^2 > 0 = log|det| - sum over the negative ones
+        double s = la0[k];
+        for (double v : negs[k]) s -= std::log(std::fabs(v));
+        int64_t skipped = (int64_t)negs[k].size();
+        if (skip_lowest && nn0[k] == 0) {  // eigenvalue 1 is positive: drop it too
+            s -= std::log(lmin[k]);
+            skipped += 1;
+        }
+        lndet[k] = s;
+        if (eta2_min) eta2_min[k] = lmin[k];
+        if (nskipped) nskipped[k] = skipped;
+    }
+    return PG_OK;
 }
