@@ -16,6 +16,7 @@ NVCC = os.environ.get("NVCC", "nvcc")
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-I" + os.path.join(HERE, "..", "include")]
 SOURCES = ["pg_api.cu", "pg_ti.cu", "pg_tc.cu", "pg_instanton.cu"]
+DRIVERS = ["pimd_ti", "rpi"]  # C++ front ends (host/*.cpp), linked against libpimdgpu.so
 
 
 def _compile(src, verbose=False):
@@ -48,6 +49,17 @@ def build(verbose=False):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
+    for d in DRIVERS:
+        src = os.path.join(HERE, "host", d + ".cpp")
+        exe = os.path.join(OUT, d)
+        hdr = os.path.join(HERE, "host", "namelist.hpp")
+        if os.path.exists(exe) and os.path.getmtime(exe) >= max(os.path.getmtime(p) for p in (src, hdr, so)):
+            continue
+        cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-o", exe, src, "-L" + OUT, "-lpimdgpu",
+               "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("driver build failed for %s:\n%s\n%s" % (d, r.stdout, r.stderr))
     return so
 
 

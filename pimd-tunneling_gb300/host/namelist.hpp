@@ -1,0 +1,170 @@
+// namelist.hpp -- reader for the Fortran namelist groups the reference drivers
+// take on standard input (&MCDATA in pimd_par.f90:42-45, &RPIDATA in
+// rpi_ser.f90:22-24) and for the plain-text data files they open
+// (masses.dat, well1.dat, well2.dat, path.xyz).
+#pragma once
+#include <cctype>
+#include <cstdlib>
+#include <fstream>
+#include <map>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace pgdrv {
+
+inline std::string lower(std::string s) {
+    for (auto &c : s) c = (char)std::tolower((unsigned char)c);
+    return s;
+}
+
+// Key -> raw value text (lower-case keys, quotes stripped from strings).
+class Namelist {
+  public:
+    std::map<std::string, std::string> kv;
+
+    // Parses the first group named `group` ("&group ... /") from text.
+    static Namelist parse(const std::string &text, const std::string &group) {
+        Namelist nl;
+        std::string t = text;
+        std::string low = lower(t);
+        size_t p = low.find("&" + lower(group));
+        if (p == std::string::npos) throw std::runtime_error("namelist group &" + group + " not found");
+        p += group.size() + 1;
+        // body ends at an unquoted '/' or '&end'
+        std::string body;
+        bool inq = false;
+        char q = 0;
+        for (size_t i = p; i < t.size(); i++) {
+            char c = t[i];
+            if (inq) {
+                if (c == q) inq = false;
+                body += c;
+                continue;
+            }
+            if (c == '\'' || c == '"') {
+                inq = true;
+                q = c;
+                body += c;
+                continue;
+            }
+            if (c == '/') break;
+            if (c == '!') {  // comment to end of line
+                while (i < t.size() && t[i] != '\n') i++;
+                body += ' ';
+                continue;
+            }
+            body += c;
+        }
+        // split into key = value pairs at top-level commas / whitespace before "key ="
+        size_t i = 0;
+        auto skip = [&]() {
+            while (i < body.size() && (std::isspace((unsigned char)body[i]) || body[i] == ',')) i++;
+        };
+        while (true) {
+            skip();
+            if (i >= body.size()) break;
+            size_t ks = i;
+            while (i < body.size() && body[i] != '=' && !std::isspace((unsigned char)body[i])) i++;
+            std::string key = lower(body.substr(ks, i - ks));
+            while (i < body.size() && std::isspace((unsigned char)body[i])) i++;
+            if (i >= body.size() || body[i] != '=') throw std::runtime_error("namelist: expected '=' after " + key);
+            i++;
+            while (i < body.size() && std::isspace((unsigned char)body[i])) i++;
+            std::string val;
+            if (i < body.size() && (body[i] == '\'' || body[i] == '"')) {
+                char qq = body[i++];
+                while (i < body.size() && body[i] != qq) val += body[i++];
+                i++;
+            } else {
+                while (i < body.size() && body[i] != ',' && !std::isspace((unsigned char)body[i])) val += body[i++];
+            }
+            nl.kv[key] = val;
+        }
+        return nl;
+    }
+
+    bool has(const std::string &k) const { return kv.count(lower(k)) > 0; }
+
+    double real(const std::string &k, double def) const {
+        auto it = kv.find(lower(k));
+        if (it == kv.end()) return def;
+        std::string v = it->second;
+        for (auto &c : v)
+            if (c == 'd' || c == 'D') c = 'e';  // Fortran double exponent
+        return std::strtod(v.c_str(), nullptr);
+    }
+    long long integer(const std::string &k, long long def) const {
+        auto it = kv.find(lower(k));
+        if (it == kv.end()) return def;
+        return (long long)real(k, (double)def);  // accepts 5e6-style integers
+    }
+    bool logical(const std::string &k, bool def) const {
+        auto it = kv.find(lower(k));
+        if (it == kv.end()) return def;
+        std::string v = lower(it->second);
+        if (v.size() && v[0] == '.') v = v.substr(1);
+        return !v.empty() && v[0] == 't';
+    }
+    std::string str(const std::string &k, const std::string &def) const {
+        auto it = kv.find(lower(k));
+        return it == kv.end() ? def : it->second;
+    }
+};
+
+inline std::string read_all(std::istream &in) {
+    std::stringstream ss;
+    ss << in.rdbuf();
+    return ss.str();
+}
+
+// masses.dat: "label mass" per atom (pimd_par.f90:154-158).
+inline void read_masses(const std::string &path, int natom, std::vector<std::string> &label,
+                        std::vector<double> &mass) {
+    std::ifstream f(path);
+    if (!f) throw std::runtime_error("cannot open " + path);
+    label.resize(natom);
+    mass.resize(natom);
+    for (int j = 0; j < natom; j++)
+        if (!(f >> label[j] >> mass[j])) throw std::runtime_error("short masses file " + path);
+}
+
+// well*.dat: ndim coordinates per atom (pimd_par.f90:123-130), stored as x[atom*ndim + dim].
+inline std::vector<double> read_well(const std::string &path, int ndim, int natom, int xunit) {
+    std::ifstream f(path);
+    if (!f) throw std::runtime_error("cannot open " + path);
+    std::vector<double> w((size_t)ndim * natom);
+    for (auto &v : w)
+        if (!(f >> v)) throw std::runtime_error("short well file " + path);
+    if (xunit == 2)
+        for (auto &v : w) v /= 0.529177;  // Angstrom -> bohr (pimd_par.f90:133-136)
+    return w;
+}
+
+// path.xyz: npath frames of "natom / comment / label x y z" (instantonmod.f90:916-935).
+inline std::vector<std::vector<double>> read_path_xyz(const std::string &path, int npath, int ndim, int natom,
+                                                      int xunit) {
+    std::ifstream f(path);
+    if (!f) throw std::runtime_error("cannot open " + path);
+    std::vector<std::vector<double>> frames;
+    std::string line;
+    for (int i = 0; i < npath; i++) {
+        if (!std::getline(f, line)) throw std::runtime_error("short path file");
+        if (!std::getline(f, line)) throw std::runtime_error("short path file");
+        std::vector<double> fr((size_t)ndim * natom);
+        for (int j = 0; j < natom; j++) {
+            if (!std::getline(f, line)) throw std::runtime_error("short path file");
+            std::istringstream ls(line);
+            std::string lab;
+            ls >> lab;
+            for (int k = 0; k < ndim; k++) ls >> fr[(size_t)j * ndim + k];
+        }
+        if (xunit == 2)
+            for (auto &v : fr) v /= 0.529177;
+        frames.push_back(fr);
+    }
+    return frames;
+}
+
+}  // namespace pgdrv

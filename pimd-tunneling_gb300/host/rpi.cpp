@@ -1,0 +1,169 @@
+// rpi.cpp -- C++ front end of the ring-polymer-instanton path: the rpi_ser.f90
+// flow (namelist &RPIDATA on standard input, masses.dat / well1.dat /
+// well2.dat / path.xyz) on one GPU through the C-ABI:
+//   betan = beta/n (rpi_ser.f90:45); V0 = V(well1); start path by linear
+//   interpolation or from path.xyz (rpi_ser.f90:133-174); instanton by the
+//   on-device L-BFGS; lndetJ0 at all beads in well 1 (single well, every
+//   eigenvalue); lndetJ at the instanton (eigenvalue 1 dropped); S, Omega, Delta
+//   (rpi_ser.f90:222-237, 354-381).
+// Keys beyond the reference's namelist: pes, pes_params (as pimd_ti), m (L-BFGS
+// history, reference 8), pgtol (reference eps2 = 1e-5), factr (1e6), maxiter,
+// quirks (1: the reference's Hessian band and mcmod_2dtest Hessian).
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <iostream>
+#include <string>
+#include <vector>
+
+#include "../../include/pimdgpu.h"
+#include "namelist.hpp"
+
+using namespace pgdrv;
+
+static int pes_id_of(const std::string &s) {
+    std::string p = lower(s);
+    if (p == "1d") return PG_PES_1D;
+    if (p == "2dtest") return PG_PES_2DTEST;
+    if (p == "synth9") return PG_PES_SYNTH9;
+    if (p == "synth18") return PG_PES_SYNTH18;
+    if (p == "harmonic") return PG_PES_HARMONIC;
+    throw std::runtime_error("unknown pes '" + s + "'");
+}
+
+static std::vector<double> read_numbers(const std::string &path) {
+    std::vector<double> v;
+    if (path.empty()) return v;
+    std::ifstream f(path);
+    if (!f) throw std::runtime_error("cannot open " + path);
+    double x;
+    while (f >> x) v.push_back(x);
+    return v;
+}
+
+#define CHECK(call)                                                                    \
+    do {                                                                               \
+        int _rc = (call);                                                              \
+        if (_rc != PG_OK) {                                                            \
+            std::fprintf(stderr, "pimdgpu error %d in %s: %s\n", _rc, #call, pg_last_error()); \
+            return 2;                                                                  \
+        }                                                                              \
+    } while (0)
+
+int main(int argc, char **argv) {
+    bool parse_only = argc > 1 && std::string(argv[1]) == "--parse-only";
+    Namelist nl;
+    try {
+        nl = Namelist::parse(read_all(std::cin), "RPIDATA");
+    } catch (std::exception &e) {
+        std::fprintf(stderr, "%s\n", e.what());
+        return 1;
+    }
+    // defaults: rpi_ser.f90:28-42
+    const int64_t n = nl.integer("n", 100);
+    const double beta = nl.real("beta", 30.0);
+    const int ndim = (int)nl.integer("ndim", 3);
+    const int natom = (int)nl.integer("natom", 1);
+    const int xunit = (int)nl.integer("xunit", 1);
+    const int64_t npath = nl.integer("npath", 0);
+    const bool readpath = nl.logical("readpath", true);
+    const std::string pes = nl.str("pes", "1d");
+    const std::string pesfile = nl.str("pes_params", "");
+    const int m = (int)nl.integer("m", 8);
+    const double pgtol = nl.real("pgtol", 1.0e-5);
+    const double factr = nl.real("factr", 1.0e6);
+    const int64_t maxiter = nl.integer("maxiter", 200000);
+    const int quirks = (int)nl.integer("quirks", 0);
+    if (parse_only) {
+        std::printf("{\"n\": %lld, \"beta\": %.17g, \"ndim\": %d, \"natom\": %d, \"xunit\": %d, \"npath\": %lld, "
+                    "\"readpath\": %s, \"pes\": \"%s\", \"m\": %d, \"pgtol\": %.17g, \"factr\": %.17g, "
+                    "\"maxiter\": %lld, \"quirks\": %d}\n",
+                    (long long)n, beta, ndim, natom, xunit, (long long)npath, readpath ? "true" : "false",
+                    pes.c_str(), m, pgtol, factr, (long long)maxiter, quirks);
+        return 0;
+    }
+    auto t0 = std::chrono::steady_clock::now();
+    const int nd = ndim * natom;
+    const double betan = beta / (double)n;  // rpi_ser.f90:45
+    std::vector<std::string> label;
+    std::vector<double> mass, w1, w2, params;
+    int pid;
+    try {
+        read_masses("masses.dat", natom, label, mass);
+        w1 = read_well("well1.dat", ndim, natom, xunit);
+        w2 = read_well("well2.dat", ndim, natom, xunit);
+        params = read_numbers(pesfile);
+        pid = pes_id_of(pes);
+    } catch (std::exception &e) {
+        std::fprintf(stderr, "%s\n", e.what());
+        return 1;
+    }
+    pg_ctx *ctx = nullptr;
+    CHECK(pg_create(&ctx, 0));
+    CHECK(pg_set_system(ctx, ndim, natom, mass.data(), pid, params.data(), (int64_t)params.size(), 0.0));
+    double v0 = 0.0;
+    CHECK(pg_pes_eval(ctx, 1, w1.data(), &v0, nullptr, PG_FP64));
+    CHECK(pg_set_system(ctx, ndim, natom, mass.data(), pid, params.data(), (int64_t)params.size(), v0));
+    std::printf(" beta= %.10g n= %lld\n beta_n= %.10g\n", beta, (long long)n, betan);
+    // start path (x[dof*n + bead])
+    std::vector<double> x((size_t)nd * n);
+    if (readpath && npath >= 2) {
+        std::vector<std::vector<double>> fr;
+        try {
+            fr = read_path_xyz("path.xyz", (int)npath, ndim, natom, xunit);
+        } catch (std::exception &e) {
+            std::fprintf(stderr, "%s\n", e.what());
+            return 1;
+        }
+        std::vector<double> lam(fr.size(), 0.0);
+        for (size_t i = 1; i < fr.size(); i++) {
+            double d = 0.0;
+            for (int k = 0; k < nd; k++) d += (fr[i][k] - fr[i - 1][k]) * (fr[i][k] - fr[i - 1][k]);
+            lam[i] = lam[i - 1] + std::sqrt(d);
+        }
+        for (auto &l : lam) l /= lam.back();
+        for (int k = 0; k < nd; k++) {
+            std::vector<double> y(fr.size()), y2(fr.size());
+            for (size_t i = 0; i < fr.size(); i++) y[i] = fr[i][k];
+            CHECK(pg_spline(lam.data(), y.data(), (int64_t)fr.size(), 1.0e31, 1.0e31, y2.data()));
+            for (int64_t bead = 0; bead < n; bead++)
+                CHECK(pg_splint(lam.data(), y.data(), y2.data(), (int64_t)fr.size(), (double)bead / (double)(n - 1),
+                                &x[(size_t)k * n + bead], nullptr));
+        }
+    } else {
+        for (int k = 0; k < nd; k++)
+            for (int64_t bead = 1; bead <= n; bead++)  // rpi_ser.f90:157-163
+                x[(size_t)k * n + bead - 1] = ((double)(n - bead) * w1[k] + (double)(bead - 1) * w2[k]) / (double)(n - 1);
+    }
+    std::printf(" Locating instanton\n");
+    pg_lbfgs_opts o;
+    o.m = m;
+    o.max_backtracks = 40;
+    o.maxiter = maxiter;
+    o.factr = factr;
+    o.pgtol = pgtol;
+    double UM = 0.0;
+    int64_t it = 0;
+    int32_t st = 0;
+    CHECK(pg_instanton_optimize(ctx, 1, n, x.data(), w1.data(), w2.data(), &betan, &o, &UM, &it, &st));
+    std::printf(" Found instanton after %lld iterations (status %d).\n", (long long)it, st);
+    std::vector<double> xharm((size_t)nd * n);
+    for (int k = 0; k < nd; k++)
+        for (int64_t bead = 0; bead < n; bead++) xharm[(size_t)k * n + bead] = w1[k];
+    double ld0 = 0.0, ld = 0.0, emin = 0.0;
+    int64_t nsk0 = 0, nsk = 0;
+    CHECK(pg_instanton_logdet(ctx, 1, n, xharm.data(), &betan, 1, 0, quirks, &ld0, nullptr, &nsk0));
+    std::printf(" Skipped %lld states\n", (long long)nsk0);
+    CHECK(pg_instanton_logdet(ctx, 1, n, x.data(), &betan, 0, 1, quirks, &ld, &emin, &nsk));
+    std::printf(" 1 %.15g\n Skipped %lld states\n lndetJ %.15g %.15g\n", emin, (long long)(nsk > 0 ? nsk - 1 : 0), ld, ld0);
+    double S, omega, delta;
+    CHECK(pg_rpi_assemble(betan, UM, ld, ld0, &S, &omega, &delta));
+    const double gam = std::exp(0.5 * (ld - ld0));
+    std::printf(" phi= %.15g\n s_kink= %.15g\n theta, N*theta= %.15g %.15g\n", gam, S, omega, omega * (double)n);
+    std::printf(" h_ij= %.15g %.15g\n RPI delta= %.15g %.15g\n", omega / betan, 219475.0 * omega / betan, delta,
+                delta * 219475.0);
+    double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    std::printf(" Ran in %.3f s\n", secs);
+    pg_destroy(ctx);
+    return 0;
+}

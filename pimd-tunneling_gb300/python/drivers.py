@@ -1,0 +1,108 @@
+"""TI-PIMD and RPI drivers over the C-ABI (the pimd_par.f90 / rpi_ser.f90 flow).
+
+run_ti   -- Gauss-Legendre points on the straight path between the wells, nrep
+            replicas per point, one batched propagation of every ring, the
+            per-point mean / variance of dHdr/betan^2 on the device, then
+            dA = sum w_i I_i, sigma_A^2 = sum w_i^2 var_i, q/q0 = exp(-dA betan)
+            (pimd_par.f90:212-221, 379-424) and Delta = (2/beta) artanh(q/q0).
+run_rpi  -- rpi_ser.f90:157-177, 222-237, 354-381 for a batch of beta values:
+            linear-interpolation guess, instanton by on-device L-BFGS, log-det at
+            the wells (single well, all eigenvalues) and at the instanton
+            (lowest eigenvalue dropped), S = betan UM, Omega and Delta.
+Every number is computed by libpimdgpu on the GPU; this module only sequences
+the calls and assembles the scalars.
+"""
+import time
+
+import numpy as np
+
+import pgconfigs
+import pimdgpu as pg
+
+
+def run_ti(cfg, precision=pg.PG_MIXED, form=pg.PG_FORM_AUTO, nmc=None, nrep=None, nintegral=None,
+           seed_offset=0, chunk=2000, device=0, ctx=None, verbose=False):
+    c = dict(cfg)
+    if nrep is not None:
+        c["nrep"] = nrep
+    nrep = c.get("nrep", 1)
+    c["seeds"] = [seed_offset + s for s in range(nrep)] if "seeds" not in cfg or seed_offset else c["seeds"]
+    ti = pgconfigs.TiInputs(c, nrep=nrep, nintegral=nintegral, gauleg=pg.gauleg)
+    nmc = int(nmc if nmc is not None else c["nmc"])
+    own = ctx is None
+    if own:
+        ctx = pg.Context(device)
+    try:
+        ctx.set_system(c["ndim"], c["natom"], c["mass"], c["pes_id"], c["params"], c["V0"])
+        tcfg = ti.ti_config(pg, precision, form)
+        ctx.ti_setup(tcfg, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
+        form_used, _ = ctx.ti_form(1)
+        t0 = time.perf_counter()
+        dev_ms = 0.0
+        done = 0
+        while done < nmc:
+            n = min(chunk, nmc - done)
+            dev_ms += ctx.ti_advance_timed(n)
+            done += n
+            if verbose:
+                print("  %d / %d steps" % (done, nmc), flush=True)
+        wall = time.perf_counter() - t0
+        mean, var, cnt = ctx.ti_lambda_reduce()
+        _, _, _, status = ctx.ti_results()
+    finally:
+        if own:
+            ctx.close()
+    dA, sigA, q = pg.ti_assemble(ti.w, mean, var, ti.betan)
+    try:
+        delta = pg.splitting_from_ratio(c["beta"], q)
+    except pg.PgError:
+        delta = float("nan")
+    lnq = -dA * ti.betan
+    lnq_err = ti.betan * np.sqrt(max(sigA, 0.0) / max(nrep, 1))
+    beads = ti.nrings * ti.P
+    return dict(dA=dA, sigmaA=sigA, qratio=q, ln_qratio=lnq, ln_qratio_stderr=lnq_err, delta=delta,
+                integrand_mean=list(mean), integrand_var=list(var), nrings=ti.nrings, P=ti.P, nmc=nmc,
+                nrep=nrep, nintegral=ti.nint, betan=ti.betan, form=form_used, device_s=dev_ms / 1e3,
+                wall_s=wall, bead_steps_per_s=beads * nmc / (dev_ms / 1e3), nan_rings=int(np.sum(status != 0)))
+
+
+def linear_guess(w1, w2, N):
+    """rpi_ser.f90:157-163."""
+    k = np.arange(1, N + 1)
+    return np.concatenate([((N - k) * w1[d] + (k - 1) * w2[d]) / (N - 1) for d in range(len(w1))])
+
+
+def run_rpi(cfg, N=None, betas=None, m=8, factr=1.0e6, pgtol=1.0e-5, maxiter=200000, quirks=False,
+            device=0, ctx=None):
+    c = dict(cfg)
+    N = int(N if N is not None else c["N"])
+    betas = np.asarray(betas if betas is not None else c["betas"], dtype=float)
+    nb = len(betas)
+    betan = betas / N  # rpi_ser.f90:45
+    w1, w2 = np.asarray(c["well1"], float), np.asarray(c["well2"], float)
+    nd = len(w1)
+    own = ctx is None
+    if own:
+        ctx = pg.Context(device)
+    try:
+        ctx.set_system(c["ndim"], c["natom"], c["mass"], c["pes_id"], c["params"], c["V0"])
+        x0 = np.concatenate([linear_guess(w1, w2, N) for _ in range(nb)])
+        t0 = time.perf_counter()
+        x, UM, it, st = ctx.instanton_optimize(N, x0, w1, np.tile(w2, nb), betan, m=m, factr=factr, pgtol=pgtol,
+                                               maxiter=maxiter)
+        t_opt = time.perf_counter() - t0
+        xharm = np.concatenate([np.repeat(w1, N) for _ in range(nb)])
+        t0 = time.perf_counter()
+        ld0, _, _ = ctx.instanton_logdet(N, xharm, betan, singlewell=True, skip_lowest=False, quirks=quirks)
+        ld, emin, nsk = ctx.instanton_logdet(N, x, betan, singlewell=False, skip_lowest=True, quirks=quirks)
+        t_det = time.perf_counter() - t0
+    finally:
+        if own:
+            ctx.close()
+    out = []
+    for k in range(nb):
+        S, om, de = pg.rpi_assemble(betan[k], UM[k], ld[k], ld0[k])
+        out.append(dict(beta=float(betas[k]), betan=float(betan[k]), UM=float(UM[k]), S=S, omega=om, delta=de,
+                        lndetJ=float(ld[k]), lndetJ0=float(ld0[k]), eta2_min=float(emin[k]),
+                        skipped=int(nsk[k]), iterations=int(it[k]), status=int(st[k])))
+    return dict(N=N, results=out, x=x, optimize_s=t_opt, logdet_s=t_det)
