@@ -288,14 +288,6 @@ def main():
     s, n, _, st = ctx.ti_results()
     nan_rings = int(np.sum(st != 0))
 
-    extras = {}
-    print("[bench] fused kernel: %.3f ms per step of %d MD steps, %.3e %s" % (kernel_ms, M, value, UNIT),
-          file=sys.stderr, flush=True)
-    try:
-        if not args.no_extras and rank == 0:
-            _extras(ctx, pg, cfg, ti, M, K, value, ws, beads, extras)
-    except Exception as e:  # report, keep the main measurement
-        extras["extras_error"] = repr(e)
     peaks, peak_kind = _peaks()
     # Dominant kernel, timed live with CUDA events on the library stream.
     kt = ctx.ti_kernel_times(20) if not (ws > 1 and rank != 0) else []
@@ -319,6 +311,14 @@ def main():
                 "tensor_view": {"achieved_tflops": tflops, "peak_tflops": peaks["bf16_tflops"],
                                 "frac": tflops / peaks["bf16_tflops"]}}
 
+    extras = {}
+    print("[bench] fused kernel: %.3f ms per step of %d MD steps, %.3e %s" % (kernel_ms, M, value, UNIT),
+          file=sys.stderr, flush=True)
+    try:
+        if not args.no_extras and rank == 0:
+            _extras(ctx, pg, cfg, ti, M, K, value, ws, beads, extras)
+    except Exception as e:  # report, keep the main measurement
+        extras["extras_error"] = repr(e)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
             "ms_per_step": kernel_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",

@@ -1,0 +1,202 @@
+! pimdgpu_mod.f90 -- ISO_C_BINDING interface of libpimdgpu (include/pimdgpu.h)
+! for the reference's Fortran drivers.  Default INTEGER is 8 bytes and default
+! REAL 8 bytes in the reference build (-i8 -r8), which is what integer(c_int64_t)
+! and real(c_double) mirror; no CHARACTER or LOGICAL crosses the boundary except
+! the NUL-terminated checkpoint path.
+!
+! Not compiled on the build machines (no Fortran compiler is installed there);
+! the C prototypes it binds are exercised by the C++ drivers and the tests.
+module pimdgpu
+  use, intrinsic :: iso_c_binding
+  implicit none
+
+  integer(c_int), parameter :: PG_OK = 0
+  integer(c_int32_t), parameter :: PG_PES_1D = 1, PG_PES_2DTEST = 2, PG_PES_SYNTH9 = 3, &
+       PG_PES_SYNTH18 = 4, PG_PES_HARMONIC = 5
+  integer(c_int32_t), parameter :: PG_FP64 = 0, PG_MIXED = 1
+  integer(c_int32_t), parameter :: PG_FORM_AUTO = 0, PG_FORM_PLAIN = 1, PG_FORM_FUSED = 2, &
+       PG_FORM_TENSOR = 3
+  integer(c_int32_t), parameter :: PG_ANDERSEN = 1, PG_LANGEVIN = 2
+
+  type, bind(c) :: pg_ti_config
+     integer(c_int64_t) :: nbeads
+     real(c_double)     :: beta, dt, tau, gamma
+     integer(c_int32_t) :: thermostat, precision, form, cayley
+     integer(c_int64_t) :: imin, noutput
+     real(c_double)     :: dhdr_limit, init_sigma
+  end type pg_ti_config
+
+  type, bind(c) :: pg_lbfgs_opts
+     integer(c_int32_t) :: m, max_backtracks
+     integer(c_int64_t) :: maxiter
+     real(c_double)     :: factr, pgtol
+  end type pg_lbfgs_opts
+
+  interface
+     integer(c_int) function pg_create(ctx, device) bind(c, name="pg_create")
+       import :: c_int, c_int32_t, c_ptr
+       type(c_ptr), intent(out) :: ctx
+       integer(c_int32_t), value :: device
+     end function pg_create
+
+     integer(c_int) function pg_destroy(ctx) bind(c, name="pg_destroy")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function pg_destroy
+
+     type(c_ptr) function pg_last_error() bind(c, name="pg_last_error")
+       import :: c_ptr
+     end function pg_last_error
+
+     ! replaces V_init + the mcmod_mass module variables
+     integer(c_int) function pg_set_system(ctx, ndim, natom, mass, pes_id, params, nparams, V0) &
+          bind(c, name="pg_set_system")
+       import :: c_int, c_int32_t, c_int64_t, c_double, c_ptr
+       type(c_ptr), value :: ctx
+       integer(c_int64_t), value :: ndim, natom, nparams
+       real(c_double), intent(in) :: mass(*), params(*)
+       integer(c_int32_t), value :: pes_id
+       real(c_double), value :: V0
+     end function pg_set_system
+
+     ! batched V / Vprime (mcmod_*: V, Vprime, potforce)
+     integer(c_int) function pg_pes_eval(ctx, nconf, x, V, grad, precision) bind(c, name="pg_pes_eval")
+       import :: c_int, c_int32_t, c_int64_t, c_double, c_ptr
+       type(c_ptr), value :: ctx
+       integer(c_int64_t), value :: nconf
+       real(c_double), intent(in) :: x(*)
+       real(c_double), intent(out) :: V(*), grad(*)
+       integer(c_int32_t), value :: precision
+     end function pg_pes_eval
+
+     ! batched Vdoubleprime
+     integer(c_int) function pg_pes_hessian(ctx, nconf, x, hess, quirks) bind(c, name="pg_pes_hessian")
+       import :: c_int, c_int32_t, c_int64_t, c_double, c_ptr
+       type(c_ptr), value :: ctx
+       integer(c_int64_t), value :: nconf
+       real(c_double), intent(in) :: x(*)
+       real(c_double), intent(out) :: hess(*)
+       integer(c_int32_t), value :: quirks
+     end function pg_pes_hessian
+
+     ! a batch of propagate_pimd_pile / propagate_pimd_nm calls
+     integer(c_int) function pg_propagate_pimd(ctx, cfg, ntask, nmc, a, b, dbdl, seed, stream, x, p, &
+          dHdr, status) bind(c, name="pg_propagate_pimd")
+       import :: c_int, c_int32_t, c_int64_t, c_double, c_ptr, pg_ti_config
+       type(c_ptr), value :: ctx
+       type(pg_ti_config), intent(in) :: cfg
+       integer(c_int64_t), value :: ntask, nmc
+       real(c_double), intent(in) :: a(*), b(*), dbdl(*)
+       integer(c_int64_t), intent(in) :: seed(*)   ! uint64 on the C side
+       integer(c_int32_t), intent(in) :: stream(*) ! uint32 on the C side
+       real(c_double), intent(inout) :: x(*), p(*)
+       real(c_double), intent(out) :: dHdr(*)
+       integer(c_int32_t), intent(out) :: status(*)
+     end function pg_propagate_pimd
+
+     integer(c_int) function pg_ti_setup(ctx, cfg, nrings, nlambda, ring_lambda, ring_seed, ring_stream, &
+          a, b, dbdl, xref, x0, p0) bind(c, name="pg_ti_setup")
+       import :: c_int, c_int32_t, c_int64_t, c_double, c_ptr, pg_ti_config
+       type(c_ptr), value :: ctx
+       type(pg_ti_config), intent(in) :: cfg
+       integer(c_int64_t), value :: nrings, nlambda
+       integer(c_int32_t), intent(in) :: ring_lambda(*), ring_stream(*)
+       integer(c_int64_t), intent(in) :: ring_seed(*)
+       real(c_double), intent(in) :: a(*), b(*), dbdl(*), xref(*)
+       type(c_ptr), value :: x0, p0      ! c_null_ptr or c_loc(array)
+     end function pg_ti_setup
+
+     integer(c_int) function pg_ti_advance(ctx, nsteps) bind(c, name="pg_ti_advance")
+       import :: c_int, c_int64_t, c_ptr
+       type(c_ptr), value :: ctx
+       integer(c_int64_t), value :: nsteps
+     end function pg_ti_advance
+
+     integer(c_int) function pg_ti_lambda_reduce(ctx, mean, var, count) bind(c, name="pg_ti_lambda_reduce")
+       import :: c_int, c_int64_t, c_double, c_ptr
+       type(c_ptr), value :: ctx
+       real(c_double), intent(out) :: mean(*), var(*)
+       integer(c_int64_t), intent(out) :: count(*)
+     end function pg_ti_lambda_reduce
+
+     integer(c_int) function pg_ti_checkpoint_save(ctx, path) bind(c, name="pg_ti_checkpoint_save")
+       import :: c_int, c_char, c_ptr
+       type(c_ptr), value :: ctx
+       character(kind=c_char), intent(in) :: path(*)
+     end function pg_ti_checkpoint_save
+
+     integer(c_int) function pg_ti_checkpoint_load(ctx, path) bind(c, name="pg_ti_checkpoint_load")
+       import :: c_int, c_char, c_ptr
+       type(c_ptr), value :: ctx
+       character(kind=c_char), intent(in) :: path(*)
+     end function pg_ti_checkpoint_load
+
+     integer(c_int) function pg_gauleg(x1, x2, x, w, n) bind(c, name="pg_gauleg")
+       import :: c_int, c_int64_t, c_double
+       real(c_double), value :: x1, x2
+       real(c_double), intent(out) :: x(*), w(*)
+       integer(c_int64_t), value :: n
+     end function pg_gauleg
+
+     integer(c_int) function pg_ti_assemble(nintegral, weights, mean, var, betan, dA, sigmaA, qratio) &
+          bind(c, name="pg_ti_assemble")
+       import :: c_int, c_int64_t, c_double
+       integer(c_int64_t), value :: nintegral
+       real(c_double), intent(in) :: weights(*), mean(*), var(*)
+       real(c_double), value :: betan
+       real(c_double), intent(out) :: dA, sigmaA, qratio
+     end function pg_ti_assemble
+
+     ! instanton: UMforceenergy, instanton, UMhessian, detJ + log sums
+     integer(c_int) function pg_instanton_fg(ctx, nbeta, N, x, a, b, betan, UM, grad) &
+          bind(c, name="pg_instanton_fg")
+       import :: c_int, c_int64_t, c_double, c_ptr
+       type(c_ptr), value :: ctx
+       integer(c_int64_t), value :: nbeta, N
+       real(c_double), intent(in) :: x(*), a(*), b(*), betan(*)
+       real(c_double), intent(out) :: UM(*), grad(*)
+     end function pg_instanton_fg
+
+     integer(c_int) function pg_instanton_optimize(ctx, nbeta, N, x, a, b, betan, opts, UM, niter, status) &
+          bind(c, name="pg_instanton_optimize")
+       import :: c_int, c_int32_t, c_int64_t, c_double, c_ptr, pg_lbfgs_opts
+       type(c_ptr), value :: ctx
+       integer(c_int64_t), value :: nbeta, N
+       real(c_double), intent(inout) :: x(*)
+       real(c_double), intent(in) :: a(*), b(*), betan(*)
+       type(pg_lbfgs_opts), intent(in) :: opts
+       real(c_double), intent(out) :: UM(*)
+       integer(c_int64_t), intent(out) :: niter(*)
+       integer(c_int32_t), intent(out) :: status(*)
+     end function pg_instanton_optimize
+
+     integer(c_int) function pg_um_hessian(ctx, N, betan, x, singlewell, quirks, band) &
+          bind(c, name="pg_um_hessian")
+       import :: c_int, c_int32_t, c_int64_t, c_double, c_ptr
+       type(c_ptr), value :: ctx
+       integer(c_int64_t), value :: N
+       real(c_double), value :: betan
+       real(c_double), intent(in) :: x(*)
+       integer(c_int32_t), value :: singlewell, quirks
+       real(c_double), intent(out) :: band(*)
+     end function pg_um_hessian
+
+     integer(c_int) function pg_instanton_logdet(ctx, nbeta, N, x, betan, singlewell, skip_lowest, quirks, &
+          lndet, eta2_min, nskipped) bind(c, name="pg_instanton_logdet")
+       import :: c_int, c_int32_t, c_int64_t, c_double, c_ptr
+       type(c_ptr), value :: ctx
+       integer(c_int64_t), value :: nbeta, N
+       real(c_double), intent(in) :: x(*), betan(*)
+       integer(c_int32_t), value :: singlewell, skip_lowest, quirks
+       real(c_double), intent(out) :: lndet(*), eta2_min(*)
+       integer(c_int64_t), intent(out) :: nskipped(*)
+     end function pg_instanton_logdet
+
+     integer(c_int) function pg_rpi_assemble(betan, UM, lndetJ, lndetJ0, S, omega, delta) &
+          bind(c, name="pg_rpi_assemble")
+       import :: c_int, c_double
+       real(c_double), value :: betan, UM, lndetJ, lndetJ0
+       real(c_double), intent(out) :: S, omega, delta
+     end function pg_rpi_assemble
+  end interface
+end module pimdgpu
