@@ -118,6 +118,14 @@ def _workload(rank):
     return c, ti
 
 
+def _config(M, form):
+    """The workload description shared by both arms."""
+    return {"workload": "c1: mcmod_2dtest surface, P=128, 1024 traj x 16 lambda = 16384 rings per GPU, "
+                        "Langevin, %d MD steps per bench step" % M,
+            "precision": "FP32 forces/state, split-BF16 NM transform, FP64 estimator",
+            "l2": "flushed (256 MB write) between timed steps", "form": form}
+
+
 def cpu_reference_rate(c, ti, target_s=12.0, nthreads=None):
     """Bead-force-steps/s of the CPU restatement of the reference step on all host
     cores (one ring per thread at a time), on a bounded sample of the workload."""
@@ -166,7 +174,7 @@ def run_reference(args):
     c, ti = _workload(0)
     vals = []
     for _ in range(max(args.warmup, 0)):
-        pass
+        cpu_reference_rate(c, ti, target_s=1.0)
     per = max(3.0, 20.0 / max(args.steps, 1))
     sample = ""
     cores = 1
@@ -177,8 +185,7 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "c1: mcmod_2dtest, P=128, 1024 traj x 16 lambda = 16384 rings, Langevin",
-                       "l2": "n/a (CPU)"},
+            "config": _config(args.md_per_step, args.form),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "the reference Fortran/MKL/MPI build cannot be compiled here (no Fortran compiler, "
@@ -312,7 +319,7 @@ def main():
                                 "frac": tflops / peaks["bf16_tflops"]}}
 
     extras = {}
-    print("[bench] fused kernel: %.3f ms per step of %d MD steps, %.3e %s" % (kernel_ms, M, value, UNIT),
+    print("[bench] timed advance: %.3f ms per step of %d MD steps, %.3e %s" % (kernel_ms, M, value, UNIT),
           file=sys.stderr, flush=True)
     try:
         if not args.no_extras and rank == 0:
@@ -322,10 +329,7 @@ def main():
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
             "ms_per_step": kernel_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "c1: mcmod_2dtest surface, P=128, 1024 traj x 16 lambda = 16384 rings "
-                                   "per GPU, Langevin, %d MD steps per bench step" % M,
-                       "precision": "FP32 forces/state, split-BF16 NM transform, FP64 estimator",
-                       "l2": "flushed (256 MB write) between timed steps", "form": args.form},
+            "config": _config(M, args.form),
             "roofline": roof, "clocks": clocks, "gpu_launches": K * launches_per_step, "wall_s": wall,
             "form": {pg.PG_FORM_FUSED: "fused-simt", pg.PG_FORM_TENSOR: "tcgen05", pg.PG_FORM_PLAIN: "plain"}[form_used],
             "nan_rings": nan_rings}

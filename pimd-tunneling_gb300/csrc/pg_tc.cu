@@ -6,12 +6,13 @@
 //     T X ~= T_hi X_hi + T_hi X_lo + T_lo X_hi,   v_hi = bf16(v), v_lo = bf16(v - v_hi)
 // (relative error ~ 2^-17 per element).
 //
-// Layout: one CTA owns 128 ring-dof rows (64 rings of a 2-D surface, or 128
-// rings of a 1-D one) with one thread per row.  The MMA computes
-//     D[row][n] = sum_k A[row][k] B[n][k],  A = data (K-major rows written by the
-//     thread that owns the TMEM lane), B = T (K-major, loaded by bulk async copy).
-// M = 128 (TMEM lanes = ring-dofs), N = 128 (TMEM columns = beads or modes),
-// K = 128 in 8 steps of 16, three MMAs per step, one commit per launch.
+// Two layouts.  The standalone transform (k_tc_transform) gives one CTA 128
+// input columns, one thread per column: D[col][n] = sum_k X[col][k] T[n][k]
+// (A = data written by the thread that owns the TMEM lane, B = T).  The TI step
+// kernels (k_tc_g1, k_tc_g2) swap the roles: A = T (M = 128 beads or modes), B =
+// a tile of 64 state columns (N = 64), so a TMEM lane holds one bead of all
+// columns and two 256-thread CTAs fit on an SM.  K = 128 in 8 steps of 16,
+// three MMAs per step, one commit per launch.
 //
 // State lives in HBM/L2 as FP32 [ring][dof][P] (q, pi, x, F), the same layout
 // as the SIMT kernels, so state read-out and checkpoints are shared.
@@ -294,9 +295,7 @@ __global__ void k_build_split_image(unsigned char *img) {
 }
 
 // ---------------------------------------------------------------- TI step on the tensor cores
-// One MD step = two launches, each with the single-GEMM structure of
-// k_tc_transform (128 threads = 128 ring-dof rows, one split-BF16 GEMM, 128
-// TMEM columns, one commit):
+// One MD step = two launches, each one split-BF16 GEMM per column tile:
 //   G1: x = T q + x* (positions), the estimator of the previous step (bead P),
 //       forces F = grad V(x) from the FP32 surface, written to HBM/L2;
 //   G2: (T F) per mode, then kick / half rotation / OU / half rotation of
@@ -330,74 +329,65 @@ struct TcArgs {
     float H, x0;
 };
 
-// Forces for the 32 beads of one chunk.  PESK 1: 1-D quartic well, one
-// coordinate per lane.  PESK 2: 2-D six-well surface, lanes 2r / 2r+1 hold x / y
-// of ring r; the even lane computes beads 0..15, the odd lane beads 16..31, and
-// the pair swaps halves with warp shuffles before and after.
-template <int PESK>
-__device__ __forceinline__ void chunk_forces(const TcArgs &a, const float (&xv)[32], float (&fv)[32],
-                                             bool odd) {
-    if constexpr (PESK == 1) {
-#pragma unroll
-        for (int t = 0; t < 32; t++) {
-            float u = xv[t] / a.x0;
-            float w = u * u - 1.0f;
-            fv[t] = w * 4.0f * a.H * xv[t] / (a.x0 * a.x0);
-        }
-    } else {
-        float px[16], py[16];
-#pragma unroll
-        for (int t = 0; t < 16; t++) {
-            float send = odd ? xv[t] : xv[16 + t];
-            float recv = __shfl_xor_sync(0xffffffffu, send, 1);
-            px[t] = odd ? recv : xv[t];
-            py[t] = odd ? xv[16 + t] : recv;
-        }
-        float fx[16], fy[16];
-#pragma unroll
-        for (int t = 0; t < 16; t++) {
-            float gx = 0.f, gy = 0.f;
-            for (int k = 0; k < a.nwell; k++) {
-                float dx = px[t] - a.wc[2 * k], dy = py[t] - a.wc[2 * k + 1];
-                float u = dx * dx + dy * dy;
-                float eb = __expf(-a.b0 * u);
-                float ea;
-                if (a.pow10) {
-                    float e2 = eb * eb, e4 = e2 * e2, e8 = e4 * e4;
-                    ea = e8 * e2;
-                } else {
-                    ea = __expf(-a.a0 * u);
-                }
-                float cc = a.a0 * ea + a.b0 * eb;
-                gx += cc * dx;
-                gy += cc * dy;
-            }
-            fx[t] = gx;
-            fy[t] = gy;
-        }
-#pragma unroll
-        for (int t = 0; t < 16; t++) {
-            float send = odd ? fx[t] : fy[t];
-            float recv = __shfl_xor_sync(0xffffffffu, send, 1);
-            if (odd) {
-                fv[16 + t] = fy[t];
-                fv[t] = recv;
-            } else {
-                fv[t] = fx[t];
-                fv[16 + t] = recv;
-            }
-        }
-    }
+// ---------------------------------------------------------------- column tiles
+// The TI step kernels work on tiles of kNc = 64 ring-dof columns with 256
+// threads (8 warps), two CTAs per SM.  One split-BF16 GEMM per launch,
+//     D[m][c] = sum_k T[m][k] X[c][k]     (M = 128 beads or modes, N = 64, K = 128),
+// takes T as the A operand (the bulk-copied image) and the FP32 state rows
+// X[c][:] of the tile, split by the CTA's threads, as the B operand.  TMEM lane m
+// then holds bead (or mode) m of all 64 columns: warp w reads lane quadrant
+// w % 4 and column half w / 4, so every epilogue access of a warp covers 32
+// consecutive beads of one column (128 contiguous bytes), and the x / y columns
+// of a ring (2r, 2r+1) sit in the same thread.
+constexpr int kNc = 64;
+constexpr int kTileThreads = 256;
+constexpr int kDataBytes = kNc * kP * 2;                     // one bf16 plane of a tile: 16 KB
+constexpr int kTileSmemOps = 2 * kOpBytes + 2 * kDataBytes;  // T hi/lo + X hi/lo: 96 KB
+constexpr uint32_t kIdescN64 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kNc >> 3) << 17) |
+                               ((uint32_t)(128 >> 4) << 24);
+
+// Per-column values staged in shared memory by the CTA.
+struct TileAux {
+    float xa[kNc];       // spring-line start a_j
+    float xs[kNc];       // spring-line slope (b_j - a_j) / (P + 1)
+    float xP[kNc];       // bead-P position for the estimator
+    uint64_t seed[kNc];  // Philox key of the column's ring
+    uint32_t stream[kNc];
+};
+
+__device__ __forceinline__ void mma_bf16_n64(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+            dtmem),
+        "l"(adesc), "l"(bdesc), "r"(kIdescN64), "r"(acc)
+        : "memory");
 }
 
-// Common prologue: barriers, TMEM (128 columns), T image by bulk copy, the
-// thread's row of `src` (FP32, 128 values) split into the A image, GEMM issued
-// and waited.  Returns the TMEM base (lane-quadrant address in *laddr) and
-// whether the accumulator is valid (same sequence as k_tc_transform).
-__device__ __forceinline__ bool tc_row_gemm(unsigned char *base, TcShared *sh, const unsigned char *gT,
-                                            const float *row_src, bool valid, uint32_t *tmem_out) {
-    unsigned char *Thi = base, *Tlo = base + kOpBytes, *Ahi = base + 2 * kOpBytes, *Alo = base + 3 * kOpBytes;
-    const int tid = threadIdx.x, warp = tid >> 5;
+// Splits 8 FP32 values into one 16-byte row of the hi and of the lo plane.
+__device__ __forceinline__ void split8(const float (&v)[8], uint4 &hi, uint4 &lo) {
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+        __nv_bfloat16 h0 = __float2bfloat16_rn(v[2 * e]), h1 = __float2bfloat16_rn(v[2 * e + 1]);
+        float r0 = v[2 * e] - __bfloat162float(h0), r1 = v[2 * e + 1] - __bfloat162float(h1);
+        __nv_bfloat162 hh;
+        hh.x = h0;
+        hh.y = h1;
+        h[e] = *reinterpret_cast<uint32_t *>(&hh);
+        l[e] = pack_bf16(r0, r1);
+    }
+    hi = make_uint4(h[0], h[1], h[2], h[3]);
+    lo = make_uint4(l[0], l[1], l[2], l[3]);
+}
+
+// Barriers, kNc TMEM columns, the T image by bulk copy, the tile
+// X[c][k] = src[c * P + k] (zero for c >= nvalid) split into the B operand, the
+// GEMM issued by thread 0 and waited for by every thread.  Returns whether the
+// accumulator is valid (the CTA-uniform error word is zero).
+__device__ __forceinline__ bool tc_tile_gemm(unsigned char *base, TcShared *sh, const unsigned char *gT,
+                                             const float *src, int nvalid, uint32_t *tmem_out) {
+    unsigned char *Thi = base, *Tlo = base + kOpBytes, *Xhi = base + 2 * kOpBytes, *Xlo = Xhi + kDataBytes;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (tid == 0) {
         mbar_init(&sh->mma_bar, 1);
         mbar_init(&sh->tma_bar, 1);
@@ -405,19 +395,31 @@ __device__ __forceinline__ bool tc_row_gemm(unsigned char *base, TcShared *sh, c
         fence_barrier_init();
     }
     __syncthreads();
-    if (warp == 0) tmem_alloc(&sh->tmem_slot, 128);
+    if (warp == 0) tmem_alloc(&sh->tmem_slot, kNc);
     load_transform(Thi, gT, sh);
-    for (int k0 = 0; k0 < kP; k0 += 32) {
-        float v[32];
+    // Warp w fills rows 8w..8w+7.  Lane: row 8w + lane % 8, K chunks
+    // 8 (4 it + lane / 8): the 8 lanes of one chunk write one 128-byte core
+    // matrix, a warp store covers 512 contiguous bytes.
+    const int c = 8 * warp + (lane & 7);
+    const bool v = c < nvalid;
+    const float *row = src + (size_t)(v ? c : 0) * kP;
+    float4 w[8];
 #pragma unroll
-        for (int i = 0; i < 32; i += 4) {
-            float4 w = valid ? *reinterpret_cast<const float4 *>(row_src + k0 + i) : make_float4(0.f, 0.f, 0.f, 0.f);
-            v[i] = w.x;
-            v[i + 1] = w.y;
-            v[i + 2] = w.z;
-            v[i + 3] = w.w;
-        }
-        write_split32(Ahi, Alo, tid, k0, v);
+    for (int it = 0; it < 4; it++) {
+        const int k0 = 8 * (4 * it + (lane >> 3));
+        w[2 * it] = v ? __ldg(reinterpret_cast<const float4 *>(row + k0)) : make_float4(0.f, 0.f, 0.f, 0.f);
+        w[2 * it + 1] = v ? __ldg(reinterpret_cast<const float4 *>(row + k0 + 4)) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+#pragma unroll
+    for (int it = 0; it < 4; it++) {
+        const int k0 = 8 * (4 * it + (lane >> 3));
+        const float e8[8] = {w[2 * it].x,     w[2 * it].y,     w[2 * it].z,     w[2 * it].w,
+                             w[2 * it + 1].x, w[2 * it + 1].y, w[2 * it + 1].z, w[2 * it + 1].w};
+        uint4 hi, lo;
+        split8(e8, hi, lo);
+        const uint32_t off = op_offset(c, k0);
+        *reinterpret_cast<uint4 *>(Xhi + off) = hi;
+        *reinterpret_cast<uint4 *>(Xlo + off) = lo;
     }
     fence_async_smem();
     tc_before();
@@ -426,13 +428,24 @@ __device__ __forceinline__ bool tc_row_gemm(unsigned char *base, TcShared *sh, c
     const uint32_t tmem = sh->tmem_slot;
     bool ok = mbar_wait(&sh->tma_bar, 0);
     if (tid == 0) {
-        if (ok)
-            issue_gemm(tmem, 0, smem_u32(Ahi), smem_u32(Alo), smem_u32(Thi), smem_u32(Tlo), &sh->mma_bar);
-        else
+        if (ok) {
+            const uint32_t th = smem_u32(Thi), tl = smem_u32(Tlo), xh = smem_u32(Xhi), xl = smem_u32(Xlo);
+#pragma unroll
+            for (int ks = 0; ks < kP / 16; ks++) {
+                const uint32_t koff = (uint32_t)ks * 2 * kLBO;
+                const uint64_t dth = make_desc(th + koff), dtl = make_desc(tl + koff);
+                const uint64_t dxh = make_desc(xh + koff), dxl = make_desc(xl + koff);
+                mma_bf16_n64(tmem, dth, dxh, ks > 0 ? 1u : 0u);
+                mma_bf16_n64(tmem, dth, dxl, 1u);
+                mma_bf16_n64(tmem, dtl, dxh, 1u);
+            }
+            mma_commit(&sh->mma_bar);
+        } else {
             sh->err = 1;
+        }
     }
     __syncthreads();
-    bool issued = sh->err == 0;
+    const bool issued = sh->err == 0;
     if (issued && !mbar_wait(&sh->mma_bar, 0)) atomicOr(&sh->err, 2);
     tc_after();
     __syncthreads();
@@ -440,131 +453,216 @@ __device__ __forceinline__ bool tc_row_gemm(unsigned char *base, TcShared *sh, c
     return sh->err == 0;
 }
 
-__device__ __forceinline__ void tc_row_release(TcShared *sh, uint32_t tmem, int32_t *gerr) {
+__device__ __forceinline__ void tc_tile_release(TcShared *sh, uint32_t tmem, int32_t *gerr) {
     const int tid = threadIdx.x, warp = tid >> 5;
     if (tid == 0 && sh->err) atomicOr(gerr, sh->err);
     if (sh->err & 2) mbar_wait(&sh->mma_bar, 0);  // let an overdue MMA drain (bounded)
     tc_before();
     __syncthreads();
-    if (warp == 0) tmem_dealloc(tmem, 128);
+    if (warp == 0) tmem_dealloc(tmem, kNc);
 }
 
-// G1: positions, estimator of the previous step, forces.
+// Gradient of the FP32 six-well surface (mcmod_2dtest.f90:39-60) at (px, py).
+__device__ __forceinline__ void grad_2d(const TcArgs &a, float px, float py, float &gx, float &gy) {
+    gx = 0.f;
+    gy = 0.f;
+    for (int k = 0; k < a.nwell; k++) {
+        const float dx = px - a.wc[2 * k], dy = py - a.wc[2 * k + 1];
+        const float u = dx * dx + dy * dy;
+        const float eb = __expf(-a.b0 * u);
+        float ea;
+        if (a.pow10) {
+            const float e2 = eb * eb, e4 = e2 * e2, e8 = e4 * e4;
+            ea = e8 * e2;
+        } else {
+            ea = __expf(-a.a0 * u);
+        }
+        const float cc = a.a0 * ea + a.b0 * eb;
+        gx += cc * dx;
+        gy += cc * dy;
+    }
+}
+
+__device__ __forceinline__ float sel4(const float (&v)[4], int i) {
+    float r = v[0];
+    r = i == 1 ? v[1] : r;
+    r = i == 2 ? v[2] : r;
+    r = i == 3 ? v[3] : r;
+    return r;
+}
+
+// G1: positions x = T q + x*, the estimator of the previous step, forces.
 template <int PESK>
-__global__ void __launch_bounds__(128, 1) k_tc_g1(TcArgs a, int do_est, int write_x) {
+__global__ void __launch_bounds__(kTileThreads, 2) k_tc_g1(TcArgs a, int do_est, int write_x) {
     extern __shared__ unsigned char dsm[];
     unsigned char *base = align1k(dsm);
-    TcShared *sh = reinterpret_cast<TcShared *>(base + kSmemOps);
-    const int tid = threadIdx.x, warp = tid >> 5;
-    const int nd = a.nd, rpc = kRows / nd;
-    const int rloc = tid / nd, j = tid - rloc * nd;
-    const int64_t ring = (int64_t)blockIdx.x * rpc + rloc;
-    const bool valid = ring < a.nrings;
-    const bool odd = (j & 1) != 0;
-    const size_t off = valid ? ((size_t)ring * nd + j) * kP : 0;
+    TcShared *sh = reinterpret_cast<TcShared *>(base + kTileSmemOps);
+    TileAux *ax = reinterpret_cast<TileAux *>(base + kTileSmemOps + 256);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int nd = a.nd;
+    const int64_t col0 = (int64_t)blockIdx.x * kNc;
+    const int nvalid = (int)min((int64_t)kNc, a.nrings * nd - col0);
     const int64_t s = *a.stepA;
+    if (tid < kNc) {
+        float xa = 0.f, xs = 0.f;
+        if (tid < nvalid) {
+            const int64_t ring = (col0 + tid) / nd;
+            const int j = (int)(col0 + tid - ring * nd);
+            const int lam = a.ringlam[ring];
+            xa = (float)a.avec[j];
+            xs = (float)((a.bvec[(size_t)lam * nd + j] - a.avec[j]) / (double)(kP + 1));
+        }
+        ax->xa[tid] = xa;
+        ax->xs[tid] = xs;
+    }
     uint32_t tmem;
-    bool ok = tc_row_gemm(base, sh, a.gT, a.q + off, valid, &tmem);
+    const bool ok = tc_tile_gemm(base, sh, a.gT, a.q + col0 * kP, nvalid, &tmem);
     if (ok) {
-        const int lam = valid ? a.ringlam[ring] : 0;
-        const float xa = (float)a.avec[j];
-        const float xslope = valid ? (float)((a.bvec[(size_t)lam * nd + j] - a.avec[j]) / (double)(kP + 1)) : 0.f;
-        const uint32_t laddr = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
-        for (int n0 = 0; n0 < kP; n0 += 32) {
-            float xv[32];
-            __syncwarp();  // tcgen05.ld is .sync.aligned: issue it from a converged warp
-            tmem_ld32(laddr + (uint32_t)n0, xv);
+        const int m = 32 * (warp & 3) + lane;  // bead
+        const int cb = 32 * (warp >> 2);        // first column of this thread's half
+        const int nv = nvalid - cb;              // valid columns in the half (may be <= 0)
+        float xv[32];
+        __syncwarp();  // tcgen05.ld is .sync.aligned: issue it from a converged warp
+        tmem_ld32(tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)cb, xv);
+        const float fm = (float)(m + 1);
 #pragma unroll
-            for (int t = 0; t < 32; t++) xv[t] += xa + xslope * (float)(n0 + t + 1);
-            if (n0 == kP - 32 && do_est) {
-                // estimator of step s-1 (verletmodule.f90:397-403): bead P is the last column
-                const int atom = j / a.ndim;
-                double contr = valid ? a.mass[atom] * (-(double)xv[31]) * a.dbdl[(size_t)lam * nd + j] : 0.0;
-                if (nd == 2) contr += __shfl_xor_sync(0xffffffffu, contr, 1);
-                if (valid && j == 0 && (s - 1) >= a.imin) {
-                    RingAcc *r = &a.acc[ring];
-                    if (r->status == 0) r->dhdr_sum += contr;
-                    r->nsamples += 1;
+        for (int i = 0; i < 32; i++) xv[i] += ax->xa[cb + i] + ax->xs[cb + i] * fm;
+        if (do_est && m == kP - 1)
+#pragma unroll
+            for (int i = 0; i < 32; i++) ax->xP[cb + i] = xv[i];
+        float *xo = a.x + (size_t)(col0 + cb) * kP + m;
+        float *fo = a.f + (size_t)(col0 + cb) * kP + m;
+        if (write_x)
+#pragma unroll
+            for (int i = 0; i < 32; i++)
+                if (i < nv) xo[(size_t)i * kP] = xv[i];
+        if constexpr (PESK == 2) {
+#pragma unroll
+            for (int r = 0; r < 16; r++) {
+                float gx, gy;
+                grad_2d(a, xv[2 * r], xv[2 * r + 1], gx, gy);
+                if (2 * r < nv) {
+                    fo[(size_t)(2 * r) * kP] = gx;
+                    fo[(size_t)(2 * r + 1) * kP] = gy;
                 }
             }
-            if (valid && write_x)
+        } else {
 #pragma unroll
-                for (int t = 0; t < 32; t += 4)
-                    *reinterpret_cast<float4 *>(a.x + off + n0 + t) = make_float4(xv[t], xv[t + 1], xv[t + 2], xv[t + 3]);
-            float fv[32];
-            chunk_forces<PESK>(a, xv, fv, odd);
-            if (valid)
-#pragma unroll
-                for (int t = 0; t < 32; t += 4)
-                    *reinterpret_cast<float4 *>(a.f + off + n0 + t) = make_float4(fv[t], fv[t + 1], fv[t + 2], fv[t + 3]);
+            for (int i = 0; i < 32; i++) {
+                const float u = xv[i] / a.x0;
+                const float w = u * u - 1.0f;
+                if (i < nv) fo[(size_t)i * kP] = w * 4.0f * a.H * xv[i] / (a.x0 * a.x0);
+            }
         }
     }
+    __syncthreads();  // xP complete
+    if (ok && do_est && tid < nvalid / nd && (s - 1) >= a.imin) {
+        // estimator of step s-1 (verletmodule.f90:397-403), one thread per ring
+        const int64_t ring = col0 / nd + tid;
+        const int lam = a.ringlam[ring];
+        double contr = 0.0;
+        for (int j = 0; j < nd; j++)
+            contr += a.mass[j / a.ndim] * (-(double)ax->xP[tid * nd + j]) * a.dbdl[(size_t)lam * nd + j];
+        RingAcc *r = &a.acc[ring];
+        if (r->status == 0) r->dhdr_sum += contr;
+        r->nsamples += 1;
+    }
     if (blockIdx.x == 0 && tid == 0) *a.stepB = s;
-    tc_row_release(sh, tmem, a.err);
+    tc_tile_release(sh, tmem, a.err);
 }
 
 // G2: kick with T F, half rotation, OU, half rotation (verletmodule.f90:423-435).
-__global__ void __launch_bounds__(128, 1) k_tc_g2(TcArgs a) {
+// The coefficient table is per (atom, mode); the tensor form runs one-atom
+// systems, so a thread keeps its mode's six coefficients in registers.
+__global__ void __launch_bounds__(kTileThreads, 2) k_tc_g2(TcArgs a) {
     extern __shared__ unsigned char dsm[];
     unsigned char *base = align1k(dsm);
-    float *scoef = reinterpret_cast<float *>(base + kSmemOps + 256);
-    TcShared *sh = reinterpret_cast<TcShared *>(base + kSmemOps);
-    const int tid = threadIdx.x, warp = tid >> 5;
-    const int nd = a.nd, rpc = kRows / nd;
-    const int rloc = tid / nd, j = tid - rloc * nd;
-    const int64_t ring = (int64_t)blockIdx.x * rpc + rloc;
-    const bool valid = ring < a.nrings;
-    const size_t off = valid ? ((size_t)ring * nd + j) * kP : 0;
+    TcShared *sh = reinterpret_cast<TcShared *>(base + kTileSmemOps);
+    TileAux *ax = reinterpret_cast<TileAux *>(base + kTileSmemOps + 256);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int nd = a.nd;
+    const int64_t col0 = (int64_t)blockIdx.x * kNc;
+    const int nvalid = (int)min((int64_t)kNc, a.nrings * nd - col0);
     const int64_t s = *a.stepB;
-    for (int i = tid; i < a.natom * kP * 8; i += 128) scoef[i] = a.coef[i];
+    if (tid < kNc) {
+        uint64_t sd = 0;
+        uint32_t sm = 0;
+        if (tid < nvalid) {
+            const int64_t ring = (col0 + tid) / nd;
+            sd = a.ringseed[ring];
+            sm = a.ringstream[ring];
+        }
+        ax->seed[tid] = sd;
+        ax->stream[tid] = sm;
+    }
     uint32_t tmem;
-    bool ok = tc_row_gemm(base, sh, a.gT, a.f + off, valid, &tmem);
+    const bool ok = tc_tile_gemm(base, sh, a.gT, a.f + col0 * kP, nvalid, &tmem);
     if (ok) {
-        const uint64_t seed = valid ? a.ringseed[ring] : 0;
-        const uint32_t stream = valid ? a.ringstream[ring] : 0;
-        const float *cf = scoef + (size_t)(j / a.ndim) * kP * 8;
+        const int m = 32 * (warp & 3) + lane;  // mode
+        const int cb = 32 * (warp >> 2);
+        const int nv = nvalid - cb;
+        const int e = lane & 3;
+        float gv[32];
+        __syncwarp();
+        tmem_ld32(tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)cb, gv);
+        const float4 c4 = *reinterpret_cast<const float4 *>(a.coef + (size_t)m * 8);
+        const float2 c2 = *reinterpret_cast<const float2 *>(a.coef + (size_t)m * 8 + 4);
         const float dt = a.dt;
         const uint32_t st = (uint32_t)s;
-        const uint32_t laddr = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
-        bool bad = false;
-        for (int n0 = 0; n0 < kP; n0 += 32) {
-            float gv[32];
-            __syncwarp();  // tcgen05.ld is .sync.aligned: issue it from a converged warp
-            tmem_ld32(laddr + (uint32_t)n0, gv);
-            if (!valid) continue;
+        float *qo = a.q + (size_t)(col0 + cb) * kP + m;
+        float *po = a.pi + (size_t)(col0 + cb) * kP + m;
+        uint32_t badbits = 0;
 #pragma unroll
-            for (int u = 0; u < 8; u++) {
-                const int kk = n0 + 4 * u;
-                U4 o = philox_block(seed, stream, st, kRngLangevin, (uint32_t)((j * kP + kk) >> 2));
-                float z[4];
-                box_muller_f(o.x, o.y, z[0], z[1]);
-                box_muller_f(o.z, o.w, z[2], z[3]);
-                float4 qv = *reinterpret_cast<const float4 *>(a.q + off + kk);
-                float4 pv = *reinterpret_cast<const float4 *>(a.pi + off + kk);
-                float qa[4] = {qv.x, qv.y, qv.z, qv.w}, pa[4] = {pv.x, pv.y, pv.z, pv.w};
+        for (int g = 0; g < 8; g++) {
+            float qv[4], pv[4];
 #pragma unroll
-                for (int e = 0; e < 4; e++) {
-                    const float4 c4 = *reinterpret_cast<const float4 *>(cf + (kk + e) * 8);
-                    const float2 c2 = *reinterpret_cast<const float2 *>(cf + (kk + e) * 8 + 4);
-                    float p0 = pa[e] - dt * gv[4 * u + e];
-                    float q0 = qa[e];
-                    float p1 = c4.x * p0 + c4.y * q0;
-                    float q1 = c4.z * p0 + c4.w * q0;
-                    p1 = c2.x * p1 + c2.y * z[e];
-                    pa[e] = c4.x * p1 + c4.y * q1;
-                    qa[e] = c4.z * p1 + c4.w * q1;
-                    bad |= (pa[e] != pa[e]);
+            for (int k = 0; k < 4; k++) {
+                const int i = 4 * g + k;
+                qv[k] = i < nv ? qo[(size_t)i * kP] : 0.f;
+                pv[k] = i < nv ? po[(size_t)i * kP] : 0.f;
+            }
+            // Lane e of a quad draws the Philox block of column 4g + e: normal
+            // number j P + m of the ring's stream, i.e. the four modes of the quad.
+            const int cc = cb + 4 * g + e;
+            const int j = (int)((col0 + cc) % nd);
+            const U4 o = philox_block(ax->seed[cc], ax->stream[cc], st, kRngLangevin, (uint32_t)((j * kP + m) >> 2));
+            float z[4];
+            box_muller_f(o.x, o.y, z[0], z[1]);
+            box_muller_f(o.z, o.w, z[2], z[3]);
+            // 4 x 4 transpose within the quad: rv[r] = this mode's normal for column 4g + (e ^ r)
+            float rv[4];
+            rv[0] = sel4(z, e);
+#pragma unroll
+            for (int r = 1; r < 4; r++) rv[r] = __shfl_xor_sync(0xffffffffu, sel4(z, e ^ r), r);
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const int i = 4 * g + k;
+                const float zk = sel4(rv, e ^ k);
+                const float p0 = pv[k] - dt * gv[i];
+                const float q0 = qv[k];
+                float p1 = c4.x * p0 + c4.y * q0;
+                const float q1 = c4.z * p0 + c4.w * q0;
+                p1 = c2.x * p1 + c2.y * zk;
+                const float pn = c4.x * p1 + c4.y * q1;
+                const float qn = c4.z * p1 + c4.w * q1;
+                if (i < nv) {
+                    qo[(size_t)i * kP] = qn;
+                    po[(size_t)i * kP] = pn;
+                    if (pn != pn) badbits |= 1u << i;
                 }
-                *reinterpret_cast<float4 *>(a.q + off + kk) = make_float4(qa[0], qa[1], qa[2], qa[3]);
-                *reinterpret_cast<float4 *>(a.pi + off + kk) = make_float4(pa[0], pa[1], pa[2], pa[3]);
             }
         }
-        if (bad && valid) {
-            if (atomicOr(&a.acc[ring].status, PG_RING_NAN) == 0) a.acc[ring].pad = (int32_t)s;
+        badbits = __reduce_or_sync(0xffffffffu, badbits);
+        if (lane == 0 && badbits) {
+            for (int i = 0; i < 32; i++)
+                if (badbits & (1u << i)) {
+                    const int64_t ring = (col0 + cb + i) / nd;
+                    if (atomicOr(&a.acc[ring].status, PG_RING_NAN) == 0) a.acc[ring].pad = (int32_t)s;
+                }
         }
     }
     if (blockIdx.x == 0 && tid == 0) *a.stepA = s + 1;
-    tc_row_release(sh, tmem, a.err);
+    tc_tile_release(sh, tmem, a.err);
 }
 
 // Host: split-BF16 image of T in the K-major core-matrix layout (B operand, rows = beads).
@@ -584,9 +682,7 @@ static void build_split_image(int P, std::vector<unsigned char> &img) {
         }
 }
 
-static size_t tc_smem_bytes(int natom) {
-    return (size_t)kSmemOps + 1024 + 256 + (size_t)natom * kP * 8 * sizeof(float) + 64;
-}
+static size_t tc_smem_bytes() { return (size_t)kTileSmemOps + 1024 + 256 + sizeof(TileAux) + 64; }
 
 // Tbf layout: [T image 64 KB | FP32 coefficients | error word | stepB | pad]
 static size_t tbf_coef_off() { return 2 * (size_t)kOpBytes; }
@@ -600,6 +696,7 @@ int tc_supported(const TiState &st, const pg_ctx &ctx) {
     if (st.P != kP) return 0;
     if (st.cfg.thermostat != PG_LANGEVIN) return 0;
     if (st.cfg.dhdr_limit >= 0.0) return 0;
+    if (ctx.natom != 1) return 0;  // G2 keeps one atom's mode coefficients in registers
     if (ctx.pes_id == PG_PES_2DTEST && ctx.nd == 2) return 1;
     if (ctx.pes_id == PG_PES_1D && ctx.nd == 1) return 1;
     return 0;
@@ -634,7 +731,7 @@ int tc_prepare(pg_ctx *ctx, TiState &st) {
                             ctx->stream));
     PG_CUDA(cudaMemsetAsync(d + tbf_err_off(ctx->natom), 0, 64, ctx->stream));
     PG_CUDA(cudaStreamSynchronize(ctx->stream));
-    size_t sm = tc_smem_bytes(ctx->natom);
+    size_t sm = tc_smem_bytes();
     PG_CUDA(cudaFuncSetAttribute(k_tc_g1<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     PG_CUDA(cudaFuncSetAttribute(k_tc_g1<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     PG_CUDA(cudaFuncSetAttribute(k_tc_g2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
@@ -696,20 +793,17 @@ static void tc_make_args(pg_ctx *ctx, TiState &st, TcArgs &a, int &pesk) {
     }
 }
 
-static unsigned tc_grid(const TiState &st) {
-    int rpc = kRows / st.nd;
-    return (unsigned)((st.nrings + rpc - 1) / rpc);
-}
+static unsigned tc_grid(const TiState &st) { return (unsigned)((st.nrings * st.nd + kNc - 1) / kNc); }
 
 int tc_launch_one(pg_ctx *ctx, TiState &st, int do_est, int final_pass, cudaStream_t s) {
     TcArgs a;
     int pesk;
     tc_make_args(ctx, st, a, pesk);
-    size_t sm = tc_smem_bytes(ctx->natom);
+    size_t sm = tc_smem_bytes();
     if (pesk == 2)
-        k_tc_g1<2><<<tc_grid(st), 128, sm, s>>>(a, do_est, final_pass);
+        k_tc_g1<2><<<tc_grid(st), kTileThreads, sm, s>>>(a, do_est, final_pass);
     else
-        k_tc_g1<1><<<tc_grid(st), 128, sm, s>>>(a, do_est, final_pass);
+        k_tc_g1<1><<<tc_grid(st), kTileThreads, sm, s>>>(a, do_est, final_pass);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? PG_OK : cuda_fail(e, "k_tc_g1 launch");
 }
@@ -718,7 +812,7 @@ int tc_launch_g2(pg_ctx *ctx, TiState &st, cudaStream_t s) {
     TcArgs a;
     int pesk;
     tc_make_args(ctx, st, a, pesk);
-    k_tc_g2<<<tc_grid(st), 128, tc_smem_bytes(ctx->natom), s>>>(a);
+    k_tc_g2<<<tc_grid(st), kTileThreads, tc_smem_bytes(), s>>>(a);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? PG_OK : cuda_fail(e, "k_tc_g2 launch");
 }
