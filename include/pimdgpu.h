@@ -143,6 +143,14 @@ int pg_ti_advance(pg_ctx *ctx, int64_t nsteps);
 /* pg_ti_advance that also returns the device time of the launched work in
  * milliseconds, measured with CUDA events recorded on the context's stream. */
 int pg_ti_advance_timed(pg_ctx *ctx, int64_t nsteps, double *device_ms);
+
+/* Advances the TI batches of nctx contexts on one device by nsteps each, every
+ * context's steps launched on its own stream before any is waited for, so that
+ * batches of different bead numbers (one context per P) run concurrently: the
+ * mixed-P task list of pimd_par.f90:245-381 as one call.  device_ms (may be
+ * NULL) is the device time from the first launch to the last completion.
+ * No counterpart in the reference (its ranks run one task at a time). */
+int pg_ti_advance_group(pg_ctx *const *ctxs, int64_t nctx, int64_t nsteps, double *device_ms);
 /* Advance nsteps with one CUDA-event pair around every kernel launch (no graph)
  * and report, for up to 4 kernel kinds of the chosen form, the mean device time
  * per launch (ms_per_launch[k]), the launches (count[k]), and the algorithmic

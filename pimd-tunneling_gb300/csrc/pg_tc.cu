@@ -155,6 +155,32 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&out)[32]) {
 #pragma unroll
     for (int i = 0; i < 32; i++) out[i] = __uint_as_float(v[i]);
 }
+// N = 8 or 16 consecutive FP32 columns of this thread's TMEM lane.
+template <int N>
+__device__ __forceinline__ void tmem_ldn(uint32_t taddr, float (&out)[N]) {
+    static_assert(N == 8 || N == 16 || N == 32, "TMEM load width");
+    if constexpr (N == 32) {
+        tmem_ld32(taddr, out);
+    } else if constexpr (N == 16) {
+        uint32_t v[16];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+              "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int i = 0; i < 16; i++) out[i] = __uint_as_float(v[i]);
+    } else {
+        uint32_t v[8];
+        asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                     : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
+                     : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int i = 0; i < 8; i++) out[i] = __uint_as_float(v[i]);
+    }
+}
 // Write 32 FP32 values of row `row`, K = k0..k0+31, into the hi / lo operand images.
 __device__ __forceinline__ void write_split32(unsigned char *Ahi, unsigned char *Alo, int row, int k0,
                                               const float (&v)[32]) {
@@ -341,6 +367,18 @@ struct TcArgs {
 // of a ring (2r, 2r+1) sit in the same thread.
 constexpr int kNc = 64;
 constexpr int kTileThreads = 256;
+// Epilogue group widths (columns per TMEM load): a thread walks its 32 columns
+// in groups, which bounds registers and code size.
+#ifndef PG_G1_COLS
+#define PG_G1_COLS 8
+#endif
+#ifndef PG_G2_COLS
+#define PG_G2_COLS 8
+#endif
+constexpr int kG1Cols = PG_G1_COLS;
+constexpr int kG2Cols = PG_G2_COLS;
+static_assert(kG1Cols == 8 || kG1Cols == 16 || kG1Cols == 32, "G1 group width");
+static_assert(kG2Cols == 8 || kG2Cols == 16 || kG2Cols == 32, "G2 group width");
 constexpr int kDataBytes = kNc * kP * 2;                     // one bf16 plane of a tile: 16 KB
 constexpr int kTileSmemOps = 2 * kOpBytes + 2 * kDataBytes;  // T hi/lo + X hi/lo: 96 KB
 constexpr uint32_t kIdescN64 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kNc >> 3) << 17) |
@@ -395,8 +433,8 @@ __device__ __forceinline__ bool tc_tile_gemm(unsigned char *base, TcShared *sh, 
         fence_barrier_init();
     }
     __syncthreads();
-    if (warp == 0) tmem_alloc(&sh->tmem_slot, kNc);
     load_transform(Thi, gT, sh);
+    if (warp == 0) tmem_alloc(&sh->tmem_slot, kNc);
     // Warp w fills rows 8w..8w+7.  Lane: row 8w + lane % 8, K chunks
     // 8 (4 it + lane / 8): the 8 lanes of one chunk write one 128-byte core
     // matrix, a warp store covers 512 contiguous bytes.
@@ -462,24 +500,36 @@ __device__ __forceinline__ void tc_tile_release(TcShared *sh, uint32_t tmem, int
     if (warp == 0) tmem_dealloc(tmem, kNc);
 }
 
-// Gradient of the FP32 six-well surface (mcmod_2dtest.f90:39-60) at (px, py).
-__device__ __forceinline__ void grad_2d(const TcArgs &a, float px, float py, float &gx, float &gy) {
-    gx = 0.f;
-    gy = 0.f;
+// Gradient of the FP32 six-well surface (mcmod_2dtest.f90:39-60) at the NR
+// beads (x, y) = (xv[2r], xv[2r+1]) of one thread.  Wells are the outer loop so
+// that the beads give NR independent chains per well; every bead still sums
+// its wells in order k = 1..m.  POW10: a0 = 10 b0, so e^{-a0 u} = (e^{-b0 u})^10.
+template <bool POW10, int NR>
+__device__ __forceinline__ void grad_2d_n(const TcArgs &a, const float (&xv)[2 * NR], float (&gx)[NR],
+                                          float (&gy)[NR]) {
+#pragma unroll
+    for (int r = 0; r < NR; r++) {
+        gx[r] = 0.f;
+        gy[r] = 0.f;
+    }
     for (int k = 0; k < a.nwell; k++) {
-        const float dx = px - a.wc[2 * k], dy = py - a.wc[2 * k + 1];
-        const float u = dx * dx + dy * dy;
-        const float eb = __expf(-a.b0 * u);
-        float ea;
-        if (a.pow10) {
-            const float e2 = eb * eb, e4 = e2 * e2, e8 = e4 * e4;
-            ea = e8 * e2;
-        } else {
-            ea = __expf(-a.a0 * u);
+        const float wx = a.wc[2 * k], wy = a.wc[2 * k + 1];
+#pragma unroll
+        for (int r = 0; r < NR; r++) {
+            const float dx = xv[2 * r] - wx, dy = xv[2 * r + 1] - wy;
+            const float u = dx * dx + dy * dy;
+            const float eb = __expf(-a.b0 * u);
+            float ea;
+            if (POW10) {
+                const float e2 = eb * eb, e4 = e2 * e2, e8 = e4 * e4;
+                ea = e8 * e2;
+            } else {
+                ea = __expf(-a.a0 * u);
+            }
+            const float cc = a.a0 * ea + a.b0 * eb;
+            gx[r] += cc * dx;
+            gy[r] += cc * dy;
         }
-        const float cc = a.a0 * ea + a.b0 * eb;
-        gx += cc * dx;
-        gy += cc * dy;
     }
 }
 
@@ -521,37 +571,45 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_g1(TcArgs a, int do_est,
         const int m = 32 * (warp & 3) + lane;  // bead
         const int cb = 32 * (warp >> 2);        // first column of this thread's half
         const int nv = nvalid - cb;              // valid columns in the half (may be <= 0)
-        float xv[32];
-        __syncwarp();  // tcgen05.ld is .sync.aligned: issue it from a converged warp
-        tmem_ld32(tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)cb, xv);
+        const uint32_t taddr = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)cb;
         const float fm = (float)(m + 1);
+#pragma unroll 1
+        for (int c0 = 0; c0 < 32; c0 += kG1Cols) {
+            float xv[kG1Cols];
+            __syncwarp();  // tcgen05.ld is .sync.aligned: issue it from a converged warp
+            tmem_ldn<kG1Cols>(taddr + (uint32_t)c0, xv);
 #pragma unroll
-        for (int i = 0; i < 32; i++) xv[i] += ax->xa[cb + i] + ax->xs[cb + i] * fm;
-        if (do_est && m == kP - 1)
+            for (int i = 0; i < kG1Cols; i++) xv[i] += ax->xa[cb + c0 + i] + ax->xs[cb + c0 + i] * fm;
+            if (do_est && m == kP - 1)
 #pragma unroll
-            for (int i = 0; i < 32; i++) ax->xP[cb + i] = xv[i];
-        float *xo = a.x + (size_t)(col0 + cb) * kP + m;
-        float *fo = a.f + (size_t)(col0 + cb) * kP + m;
-        if (write_x)
+                for (int i = 0; i < kG1Cols; i++) ax->xP[cb + c0 + i] = xv[i];
+            const int nvg = nv - c0;  // valid columns of this group (may be <= 0)
+            float *xo = a.x + (size_t)(col0 + cb + c0) * kP + m;
+            float *fo = a.f + (size_t)(col0 + cb + c0) * kP + m;
+            if (write_x)
 #pragma unroll
-            for (int i = 0; i < 32; i++)
-                if (i < nv) xo[(size_t)i * kP] = xv[i];
-        if constexpr (PESK == 2) {
+                for (int i = 0; i < kG1Cols; i++)
+                    if (i < nvg) xo[(size_t)i * kP] = xv[i];
+            if constexpr (PESK == 2) {
+                constexpr int NR = kG1Cols / 2;
+                float gx[NR], gy[NR];
+                if (a.pow10)
+                    grad_2d_n<true, NR>(a, xv, gx, gy);
+                else
+                    grad_2d_n<false, NR>(a, xv, gx, gy);
 #pragma unroll
-            for (int r = 0; r < 16; r++) {
-                float gx, gy;
-                grad_2d(a, xv[2 * r], xv[2 * r + 1], gx, gy);
-                if (2 * r < nv) {
-                    fo[(size_t)(2 * r) * kP] = gx;
-                    fo[(size_t)(2 * r + 1) * kP] = gy;
+                for (int r = 0; r < NR; r++)
+                    if (2 * r < nvg) {
+                        fo[(size_t)(2 * r) * kP] = gx[r];
+                        fo[(size_t)(2 * r + 1) * kP] = gy[r];
+                    }
+            } else {
+#pragma unroll
+                for (int i = 0; i < kG1Cols; i++) {
+                    const float u = xv[i] / a.x0;
+                    const float w = u * u - 1.0f;
+                    if (i < nvg) fo[(size_t)i * kP] = w * 4.0f * a.H * xv[i] / (a.x0 * a.x0);
                 }
-            }
-        } else {
-#pragma unroll
-            for (int i = 0; i < 32; i++) {
-                const float u = xv[i] / a.x0;
-                const float w = u * u - 1.0f;
-                if (i < nv) fo[(size_t)i * kP] = w * 4.0f * a.H * xv[i] / (a.x0 * a.x0);
             }
         }
     }
@@ -602,53 +660,64 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_g2(TcArgs a) {
         const int cb = 32 * (warp >> 2);
         const int nv = nvalid - cb;
         const int e = lane & 3;
-        float gv[32];
-        __syncwarp();
-        tmem_ld32(tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)cb, gv);
+        const uint32_t taddr = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)cb;
         const float4 c4 = *reinterpret_cast<const float4 *>(a.coef + (size_t)m * 8);
         const float2 c2 = *reinterpret_cast<const float2 *>(a.coef + (size_t)m * 8 + 4);
         const float dt = a.dt;
         const uint32_t st = (uint32_t)s;
-        float *qo = a.q + (size_t)(col0 + cb) * kP + m;
-        float *po = a.pi + (size_t)(col0 + cb) * kP + m;
         uint32_t badbits = 0;
+        // Groups of kG2Cols columns.  Per group, the state loads are issued
+        // first, then the independent Philox blocks, then the updates.
+#pragma unroll 1
+        for (int c0 = 0; c0 < 32; c0 += kG2Cols) {
+            constexpr int NQ = kG2Cols / 4;  // column quads of the group
+            float gv[kG2Cols];
+            __syncwarp();
+            tmem_ldn<kG2Cols>(taddr + (uint32_t)c0, gv);
+            const int nvg = nv - c0;
+            float *qo = a.q + (size_t)(col0 + cb + c0) * kP + m;
+            float *po = a.pi + (size_t)(col0 + cb + c0) * kP + m;
+            float qv[kG2Cols], pv[kG2Cols];
 #pragma unroll
-        for (int g = 0; g < 8; g++) {
-            float qv[4], pv[4];
-#pragma unroll
-            for (int k = 0; k < 4; k++) {
-                const int i = 4 * g + k;
-                qv[k] = i < nv ? qo[(size_t)i * kP] : 0.f;
-                pv[k] = i < nv ? po[(size_t)i * kP] : 0.f;
+            for (int i = 0; i < kG2Cols; i++) {
+                qv[i] = i < nvg ? qo[(size_t)i * kP] : 0.f;
+                pv[i] = i < nvg ? po[(size_t)i * kP] : 0.f;
             }
-            // Lane e of a quad draws the Philox block of column 4g + e: normal
-            // number j P + m of the ring's stream, i.e. the four modes of the quad.
-            const int cc = cb + 4 * g + e;
-            const int j = (int)((col0 + cc) % nd);
-            const U4 o = philox_block(ax->seed[cc], ax->stream[cc], st, kRngLangevin, (uint32_t)((j * kP + m) >> 2));
-            float z[4];
-            box_muller_f(o.x, o.y, z[0], z[1]);
-            box_muller_f(o.z, o.w, z[2], z[3]);
-            // 4 x 4 transpose within the quad: rv[r] = this mode's normal for column 4g + (e ^ r)
-            float rv[4];
-            rv[0] = sel4(z, e);
+            // Lane e of a quad draws the Philox block of column 4g + e: normals
+            // j P + 4 (m / 4) .. + 3 of the ring's stream, the four modes of the quad.
+            U4 o[NQ];
 #pragma unroll
-            for (int r = 1; r < 4; r++) rv[r] = __shfl_xor_sync(0xffffffffu, sel4(z, e ^ r), r);
+            for (int g = 0; g < NQ; g++) {
+                const int cc = cb + c0 + 4 * g + e;
+                const int j = (int)((col0 + cc) % nd);
+                o[g] = philox_block(ax->seed[cc], ax->stream[cc], st, kRngLangevin, (uint32_t)((j * kP + m) >> 2));
+            }
 #pragma unroll
-            for (int k = 0; k < 4; k++) {
-                const int i = 4 * g + k;
-                const float zk = sel4(rv, e ^ k);
-                const float p0 = pv[k] - dt * gv[i];
-                const float q0 = qv[k];
-                float p1 = c4.x * p0 + c4.y * q0;
-                const float q1 = c4.z * p0 + c4.w * q0;
-                p1 = c2.x * p1 + c2.y * zk;
-                const float pn = c4.x * p1 + c4.y * q1;
-                const float qn = c4.z * p1 + c4.w * q1;
-                if (i < nv) {
-                    qo[(size_t)i * kP] = qn;
-                    po[(size_t)i * kP] = pn;
-                    if (pn != pn) badbits |= 1u << i;
+            for (int g = 0; g < NQ; g++) {
+                float z[4];
+                box_muller_f(o[g].x, o[g].y, z[0], z[1]);
+                box_muller_f(o[g].z, o[g].w, z[2], z[3]);
+                // 4 x 4 transpose within the quad: rv[r] = this mode's normal for column 4g + (e ^ r)
+                float rv[4];
+                rv[0] = sel4(z, e);
+#pragma unroll
+                for (int r = 1; r < 4; r++) rv[r] = __shfl_xor_sync(0xffffffffu, sel4(z, e ^ r), r);
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const int i = 4 * g + k;
+                    const float zk = sel4(rv, e ^ k);
+                    const float p0 = pv[i] - dt * gv[i];
+                    const float q0 = qv[i];
+                    float p1 = c4.x * p0 + c4.y * q0;
+                    const float q1 = c4.z * p0 + c4.w * q0;
+                    p1 = c2.x * p1 + c2.y * zk;
+                    const float pn = c4.x * p1 + c4.y * q1;
+                    const float qn = c4.z * p1 + c4.w * q1;
+                    if (i < nvg) {
+                        qo[(size_t)i * kP] = qn;
+                        po[(size_t)i * kP] = pn;
+                        if (pn != pn) badbits |= 1u << (c0 + i);
+                    }
                 }
             }
         }

@@ -60,45 +60,62 @@ template <> __device__ __forceinline__ const float *tmat<float>(const TiArgs &a)
 template <typename R> __device__ __forceinline__ bool is_nan(R v) { return v != v; }
 
 // ---------------------------------------------------------------- fused kernel helpers
-// out[dof][i] = sum_k T[k][i] * (in[dof][k] + sh[dof][k])  for all (dof, i) of one ring.
-template <typename R>
-__device__ __forceinline__ void ring_matvec(const TiArgs &a, const R *__restrict__ in,
-                                            const double *__restrict__ sh, R *__restrict__ out,
-                                            R *__restrict__ sbuf) {
+// Up to kMvDofs dofs of a ring share every read of T in the ring transforms.
+constexpr int kMvDofs = 8;
+
+// Shared memory of the kernels that run ring transforms: kMvDofs P-vectors.
+inline size_t ring_smem_bytes(int P, bool fp32) {
+    return (size_t)kMvDofs * (size_t)P * (fp32 ? sizeof(float) : sizeof(double));
+}
+
+// store(dof, i, sum_k T[k][i] v[dof][k]) for every (dof, i) of one ring, where
+// v[dof][k] = load(dof, k).  Passes of up to kMvDofs dofs: v is staged in
+// shared memory as sbuf[k][dd], each thread owns outputs i and reads T[k][i]
+// once per pass for all dofs of the pass.  Every output sums k = 0..P-1 in
+// order (the dsymv-order sum of the CPU restatement).
+template <typename R, typename Load, typename Store>
+__device__ __forceinline__ void ring_tmv(const TiArgs &a, R *__restrict__ sbuf, Load load, Store store) {
     const R *T = tmat<R>(a);
-    const int P = a.P;
-    for (int dof = 0; dof < a.nd; dof++) {
-        for (int k = threadIdx.x; k < P; k += blockDim.x)
-            sbuf[k] = sh ? (R)((double)in[dof * P + k] + sh[dof * P + k]) : in[dof * P + k];
+    const int P = a.P, nd = a.nd;
+    for (int d0 = 0; d0 < nd; d0 += kMvDofs) {
+        const int nb = min(kMvDofs, nd - d0);
+        for (int e = threadIdx.x; e < nb * P; e += blockDim.x) {
+            const int dd = e / P, k = e - dd * P;
+            sbuf[k * kMvDofs + dd] = load(d0 + dd, k);
+        }
         __syncthreads();
         for (int i = threadIdx.x; i < P; i += blockDim.x) {
-            R s = 0;
-            for (int k = 0; k < P; k++) s += T[(size_t)k * P + i] * sbuf[k];
-            out[dof * P + i] = s;
+            R acc[kMvDofs];
+#pragma unroll
+            for (int dd = 0; dd < kMvDofs; dd++) acc[dd] = (R)0;
+            for (int k = 0; k < P; k++) {
+                const R t = T[(size_t)k * P + i];
+                const R *v = sbuf + k * kMvDofs;
+#pragma unroll
+                for (int dd = 0; dd < kMvDofs; dd++)
+                    if (dd < nb) acc[dd] += t * v[dd];
+            }
+#pragma unroll
+            for (int dd = 0; dd < kMvDofs; dd++)
+                if (dd < nb) store(d0 + dd, i, acc[dd]);
         }
         __syncthreads();
     }
 }
 
-// FP64 path: match the CPU restatement's (q + beadvec) arithmetic exactly.
-template <>
-__device__ __forceinline__ void ring_matvec<double>(const TiArgs &a, const double *__restrict__ in,
-                                                    const double *__restrict__ sh,
-                                                    double *__restrict__ out,
-                                                    double *__restrict__ sbuf) {
-    const double *T = a.T;
+// out[dof][i] = sum_k T[k][i] * (in[dof][k] + sh[dof][k])  for all (dof, i) of one ring
+// (in == out allowed: a pass stages its dofs before writing them).
+template <typename R>
+__device__ __forceinline__ void ring_matvec(const TiArgs &a, const R *in, const double *__restrict__ sh, R *out,
+                                            R *__restrict__ sbuf) {
     const int P = a.P;
-    for (int dof = 0; dof < a.nd; dof++) {
-        for (int k = threadIdx.x; k < P; k += blockDim.x)
-            sbuf[k] = sh ? in[dof * P + k] + sh[dof * P + k] : in[dof * P + k];
-        __syncthreads();
-        for (int i = threadIdx.x; i < P; i += blockDim.x) {
-            double s = 0.0;
-            for (int k = 0; k < P; k++) s += T[(size_t)k * P + i] * sbuf[k];
-            out[dof * P + i] = s;
-        }
-        __syncthreads();
-    }
+    if (sh)
+        ring_tmv<R>(
+            a, sbuf, [&](int dof, int k) { return (R)((double)in[dof * P + k] + sh[dof * P + k]); },
+            [&](int dof, int i, R v) { out[dof * P + i] = v; });
+    else
+        ring_tmv<R>(
+            a, sbuf, [&](int dof, int k) { return in[dof * P + k]; }, [&](int dof, int i, R v) { out[dof * P + i] = v; });
 }
 
 template <typename R>
@@ -166,18 +183,9 @@ __device__ __forceinline__ void ring_nm_coords(const TiArgs &a, int lam, const R
         for (int e = threadIdx.x; e < a.nd * P; e += blockDim.x) q[e] = q[e] - bv[e];
         __syncthreads();
     } else {
-        const R *T = tmat<R>(a);
-        for (int dof = 0; dof < a.nd; dof++) {
-            for (int k = threadIdx.x; k < P; k += blockDim.x)
-                sbuf[k] = (R)((double)x[dof * P + k] - xstar(a, lam, dof, k));
-            __syncthreads();
-            for (int i = threadIdx.x; i < P; i += blockDim.x) {
-                R s = 0;
-                for (int k = 0; k < P; k++) s += T[(size_t)k * P + i] * sbuf[k];
-                q[dof * P + i] = s;
-            }
-            __syncthreads();
-        }
+        ring_tmv<R>(
+            a, sbuf, [&](int dof, int k) { return (R)((double)x[dof * P + k] - xstar(a, lam, dof, k)); },
+            [&](int dof, int i, R v) { q[dof * P + i] = v; });
     }
 }
 
@@ -372,17 +380,9 @@ __global__ void k_ti_momenta(TiArgs a, const R *__restrict__ gpi, double *__rest
     if (r >= a.nrings) return;
     const int P = a.P, nd = a.nd;
     const size_t off = (size_t)r * nd * P;
-    const R *T = tmat<R>(a);
-    for (int dof = 0; dof < nd; dof++) {
-        for (int k = threadIdx.x; k < P; k += blockDim.x) sbuf[k] = gpi[off + dof * P + k];
-        __syncthreads();
-        for (int i = threadIdx.x; i < P; i += blockDim.x) {
-            R s = 0;
-            for (int k = 0; k < P; k++) s += T[(size_t)k * P + i] * sbuf[k];
-            pout[off + dof * P + i] = (double)s;
-        }
-        __syncthreads();
-    }
+    ring_tmv<R>(
+        a, sbuf, [&](int dof, int k) { return gpi[off + dof * P + k]; },
+        [&](int dof, int i, R v) { pout[off + dof * P + i] = (double)v; });
 }
 
 template <typename R>
@@ -698,7 +698,7 @@ static int launch_steps(pg_ctx *ctx, TiState &st, int64_t nsteps, cudaStream_t s
     unsigned grid = (unsigned)st.nrings;
     if (st.form == PG_FORM_TENSOR) return tc_launch(ctx, st, 0, nsteps, s);
     if (st.form == PG_FORM_FUSED) {
-        size_t sm = (size_t)P * (st.fp32 ? sizeof(float) : sizeof(double));
+        size_t sm = ring_smem_bytes(P, st.fp32);
         int thermo = st.cfg.thermostat;
         if (st.fp32) {
             if (thermo == PG_LANGEVIN)
@@ -916,7 +916,13 @@ extern "C" int pg_ti_setup(pg_ctx *ctx, const pg_ti_config *cfg, int64_t nrings,
 
     TiArgs ta = make_args(ctx, st, step_ptr(st));
     int th = threads_for(P, nd);
-    size_t sm = (size_t)P * esz;
+    size_t sm = ring_smem_bytes(P, st.fp32);
+    if (sm > 48 * 1024) {  // FP64 with P > 768: opt in to more than 48 KB
+        PG_CUDA(cudaFuncSetAttribute(k_ti_fused<double, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        PG_CUDA(cudaFuncSetAttribute(k_ti_fused<double, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        PG_CUDA(cudaFuncSetAttribute(k_ti_init<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        PG_CUDA(cudaFuncSetAttribute(k_ti_momenta<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    }
     if (st.form == PG_FORM_PLAIN) {
         k_plain_init<<<(unsigned)nrings, th, (size_t)P * sizeof(double), s>>>(
             ta, st.x.as<double>(), st.pi.as<double>(), st.f.as<double>(), dx0.as<double>(), dp0.as<double>());
@@ -940,6 +946,7 @@ extern "C" int pg_ti_setup(pg_ctx *ctx, const pg_ti_config *cfg, int64_t nrings,
 }
 
 static int ti_advance_impl(pg_ctx *ctx, int64_t nsteps, double *device_ms);
+static int ti_advance_group(pg_ctx *const *ctxs, int64_t nctx, int64_t nsteps, double *device_ms);
 
 extern "C" int pg_ti_advance(pg_ctx *ctx, int64_t nsteps) { return ti_advance_impl(ctx, nsteps, nullptr); }
 
@@ -948,58 +955,57 @@ extern "C" int pg_ti_advance_timed(pg_ctx *ctx, int64_t nsteps, double *device_m
     return ti_advance_impl(ctx, nsteps, device_ms);
 }
 
-static int ti_advance_impl(pg_ctx *ctx, int64_t nsteps, double *device_ms) {
+// The executable graph of an n-step advance (captured on first use).
+static int ti_graph(pg_ctx *ctx, int64_t n, cudaGraphExec_t *out) {
+    TiState &st = *ctx->ti;
+    auto it = st.graphs.find(n);
+    if (it != st.graphs.end()) {
+        *out = it->second;
+        return PG_OK;
+    }
+    cudaGraph_t g;
+    cudaGraphExec_t exec = nullptr;
+    PG_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    int lrc = launch_steps(ctx, st, n, ctx->stream);
+    cudaError_t ee = cudaStreamEndCapture(ctx->stream, &g);
+    if (lrc) return lrc;
+    if (ee != cudaSuccess) return cuda_fail(ee, "cudaStreamEndCapture");
+    ee = cudaGraphInstantiate(&exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ee != cudaSuccess) return cuda_fail(ee, "cudaGraphInstantiate");
+    st.graphs[n] = exec;
+    *out = exec;
+    return PG_OK;
+}
+
+// Checks an advance of nsteps and captures the graphs it needs.  launch = true
+// also replays them on the context's stream (without waiting).  Plain form:
+// graphs of up to 64 steps; fused forms: one graph per nsteps.
+static int ti_enqueue(pg_ctx *ctx, int64_t nsteps, bool launch) {
     int rc = check_ctx(ctx, true);
     if (rc) return rc;
     if (!ctx->ti) return fail(PG_ERR_STATE, "pg_ti_setup has not been called");
     if (nsteps < 0) return fail(PG_ERR_ARG, "nsteps must be >= 0");
-    if (nsteps == 0) return PG_OK;
     TiState &st = *ctx->ti;
     if (st.step + nsteps > (int64_t)0xFFFFFFFFLL) return fail(PG_ERR_ARG, "step counter would exceed 2^32");
-    // Plain form: replay a captured graph of up to 64 steps; fused forms: one graph per nsteps.
     int64_t chunk = (st.form == PG_FORM_PLAIN) ? (nsteps < 64 ? nsteps : 64) : nsteps;
     int64_t done = 0;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    if (device_ms) {
-        PG_CUDA(cudaEventCreate(&ev0));
-        PG_CUDA(cudaEventCreate(&ev1));
-        *device_ms = 0.0;
-    }
-    bool recorded = false;
     while (done < nsteps) {
         int64_t n = (nsteps - done) < chunk ? (nsteps - done) : chunk;
-        auto it = st.graphs.find(n);
         cudaGraphExec_t exec = nullptr;
-        if (it == st.graphs.end()) {
-            cudaGraph_t g;
-            PG_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-            int lrc = launch_steps(ctx, st, n, ctx->stream);
-            cudaError_t ee = cudaStreamEndCapture(ctx->stream, &g);
-            if (lrc) return lrc;
-            if (ee != cudaSuccess) return cuda_fail(ee, "cudaStreamEndCapture");
-            ee = cudaGraphInstantiate(&exec, g, 0);
-            cudaGraphDestroy(g);
-            if (ee != cudaSuccess) return cuda_fail(ee, "cudaGraphInstantiate");
-            st.graphs[n] = exec;
-        } else {
-            exec = it->second;
-        }
-        if (device_ms && !recorded) {
-            PG_CUDA(cudaEventRecord(ev0, ctx->stream));
-            recorded = true;
-        }
-        PG_CUDA(cudaGraphLaunch(exec, ctx->stream));
+        rc = ti_graph(ctx, n, &exec);
+        if (rc) return rc;
+        if (launch) PG_CUDA(cudaGraphLaunch(exec, ctx->stream));
         done += n;
     }
-    if (device_ms) PG_CUDA(cudaEventRecord(ev1, ctx->stream));
+    return PG_OK;
+}
+
+// Completes an enqueued advance: waits for the stream, moves the host step
+// counter, reads the tensor-core kernels' error word.
+static int ti_finish(pg_ctx *ctx, int64_t nsteps) {
+    TiState &st = *ctx->ti;
     PG_CUDA(cudaStreamSynchronize(ctx->stream));
-    if (device_ms) {
-        float ms = 0.f;
-        PG_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
-        *device_ms = (double)ms;
-        cudaEventDestroy(ev0);
-        cudaEventDestroy(ev1);
-    }
     st.step += nsteps;
     if (st.form == PG_FORM_TENSOR) {
         int32_t kerr = tc_error(ctx, st);
@@ -1007,6 +1013,87 @@ static int ti_advance_impl(pg_ctx *ctx, int64_t nsteps, double *device_ms) {
                                                   std::to_string(kerr) + ")");
     }
     return PG_OK;
+}
+
+static int ti_advance_impl(pg_ctx *ctx, int64_t nsteps, double *device_ms) {
+    pg_ctx *one[1] = {ctx};
+    return ti_advance_group(one, 1, nsteps, device_ms);
+}
+
+// Advances several contexts on one device together: every context's graph is
+// launched on its own stream before any is waited for, so batches of different
+// bead numbers run concurrently.  device_ms (optional) spans all of them.
+static int ti_advance_group(pg_ctx *const *ctxs, int64_t nctx, int64_t nsteps, double *device_ms) {
+    if (!ctxs || nctx <= 0) return fail(PG_ERR_ARG, "no contexts");
+    for (int64_t i = 0; i < nctx; i++) {
+        int rc = check_ctx(ctxs[i], true);
+        if (rc) return rc;
+        if (!ctxs[i]->ti) return fail(PG_ERR_STATE, "pg_ti_setup has not been called");
+        if (ctxs[i]->device != ctxs[0]->device) return fail(PG_ERR_ARG, "contexts on different devices");
+        for (int64_t k = 0; k < i; k++)
+            if (ctxs[k] == ctxs[i]) return fail(PG_ERR_ARG, "a context appears twice");
+    }
+    if (nsteps < 0) return fail(PG_ERR_ARG, "nsteps must be >= 0");
+    if (nsteps == 0) {
+        if (device_ms) *device_ms = 0.0;
+        return PG_OK;
+    }
+    PG_CUDA(cudaSetDevice(ctxs[0]->device));
+    for (int64_t i = 0; i < nctx; i++) {
+        int rc = ti_enqueue(ctxs[i], nsteps, false);  // capture outside the timed span
+        if (rc) return rc;
+    }
+    cudaStream_t s0 = ctxs[0]->stream;
+    std::vector<cudaEvent_t> ev;
+    auto cleanup = [&]() {
+        for (auto e : ev) cudaEventDestroy(e);
+    };
+    if (device_ms || nctx > 1) {
+        ev.resize((size_t)nctx + 2, nullptr);
+        for (auto &e : ev) {
+            cudaError_t ce = cudaEventCreate(&e);
+            if (ce != cudaSuccess) {
+                cleanup();
+                return cuda_fail(ce, "cudaEventCreate");
+            }
+        }
+        // start: the other streams wait for the start event on stream 0
+        cudaEventRecord(ev[0], s0);
+        for (int64_t i = 1; i < nctx; i++) cudaStreamWaitEvent(ctxs[i]->stream, ev[0], 0);
+    }
+    for (int64_t i = 0; i < nctx; i++) {
+        int rc = ti_enqueue(ctxs[i], nsteps, true);
+        if (rc) {
+            for (int64_t k = 0; k < nctx; k++) cudaStreamSynchronize(ctxs[k]->stream);
+            cleanup();
+            return rc;
+        }
+    }
+    if (!ev.empty()) {
+        // join: stream 0 waits for every other stream, then records the end
+        for (int64_t i = 1; i < nctx; i++) {
+            cudaEventRecord(ev[1 + i], ctxs[i]->stream);
+            cudaStreamWaitEvent(s0, ev[1 + i], 0);
+        }
+        cudaEventRecord(ev[1], s0);
+    }
+    int rc = PG_OK;
+    for (int64_t i = nctx - 1; i >= 0; i--) {
+        int r = ti_finish(ctxs[i], nsteps);
+        if (r && !rc) rc = r;
+    }
+    if (!rc && device_ms) {
+        float ms = 0.f;
+        cudaError_t ce = cudaEventElapsedTime(&ms, ev[0], ev[1]);
+        if (ce != cudaSuccess) rc = cuda_fail(ce, "cudaEventElapsedTime");
+        *device_ms = (double)ms;
+    }
+    cleanup();
+    return rc;
+}
+
+extern "C" int pg_ti_advance_group(pg_ctx *const *ctxs, int64_t nctx, int64_t nsteps, double *device_ms) {
+    return ti_advance_group(ctxs, nctx, nsteps, device_ms);
 }
 
 extern "C" int pg_ti_get_step(pg_ctx *ctx, int64_t *step) {
@@ -1103,7 +1190,7 @@ extern "C" int pg_ti_get_state(pg_ctx *ctx, double *x, double *p) {
         if (st.form == PG_FORM_PLAIN) {
             PG_CUDA(cudaMemcpyAsync(p, st.pi.ptr, n * sizeof(double), cudaMemcpyDeviceToHost, s));
         } else {
-            size_t sm = (size_t)st.P * (st.fp32 ? sizeof(float) : sizeof(double));
+            size_t sm = ring_smem_bytes(st.P, st.fp32);
             if (st.fp32)
                 k_ti_momenta<float><<<(unsigned)st.nrings, th, sm, s>>>(ta, st.pi.as<float>(), ctx->scratch_a.as<double>());
             else

@@ -5,6 +5,10 @@ run_ti   -- Gauss-Legendre points on the straight path between the wells, nrep
             per-point mean / variance of dHdr/betan^2 on the device, then
             dA = sum w_i I_i, sigma_A^2 = sum w_i^2 var_i, q/q0 = exp(-dA betan)
             (pimd_par.f90:212-221, 379-424) and Delta = (2/beta) artanh(q/q0).
+run_ti_mixed -- a task list whose rings have different bead numbers P (one
+            context per P, all advanced together by pg_ti_advance_group on
+            concurrent streams); TI is assembled per P, since betan = beta/(P+1)
+            and the estimate itself depend on P.
 run_rpi  -- rpi_ser.f90:157-177, 222-237, 354-381 for a batch of beta values:
             linear-interpolation guess, instanton by on-device L-BFGS, log-det at
             the wells (single well, all eigenvalues) and at the instanton
@@ -64,6 +68,66 @@ def run_ti(cfg, precision=pg.PG_MIXED, form=pg.PG_FORM_AUTO, nmc=None, nrep=None
                 integrand_mean=list(mean), integrand_var=list(var), nrings=ti.nrings, P=ti.P, nmc=nmc,
                 nrep=nrep, nintegral=ti.nint, betan=ti.betan, form=form_used, device_s=dev_ms / 1e3,
                 wall_s=wall, bead_steps_per_s=beads * nmc / (dev_ms / 1e3), nan_rings=int(np.sum(status != 0)))
+
+
+def run_ti_mixed(cfg, precision=pg.PG_MIXED, form=pg.PG_FORM_AUTO, nmc=None, chunk=1000, device=0,
+                 verbose=False):
+    """Rings r = i*nrep + j (lambda point i, replica j) with bead number
+    cfg["P_per_ring"][r]; the time step of a group is cfg["dt_per_P"][P] when
+    given.  Returns per-P TI results and the throughput of the whole batch."""
+    c = dict(cfg)
+    Pr = np.asarray(c["P_per_ring"], dtype=np.int64)
+    nint = int(c["nintegral"])
+    if len(Pr) % nint:
+        raise ValueError("P_per_ring length is not a multiple of nintegral")
+    nrep = len(Pr) // nint
+    nmc = int(nmc if nmc is not None else c["nmc"])
+    groups = []
+    try:
+        for P in sorted(set(int(v) for v in Pr)):
+            idx = np.nonzero(Pr == P)[0]
+            cg = dict(c, P=P)
+            if "dt_per_P" in c:
+                cg["dt"] = c["dt_per_P"][str(P)]
+            ti = pgconfigs.TiInputs(cg, nrep=nrep, nintegral=nint, P=P, gauleg=pg.gauleg)
+            ctx = pg.Context(device)
+            groups.append((P, idx, ti, ctx))
+            ctx.set_system(c["ndim"], c["natom"], c["mass"], c["pes_id"], c["params"], c["V0"])
+            ctx.ti_setup(ti.ti_config(pg, precision, form), ti.ring_lambda[idx], ti.ring_seed[idx],
+                         ti.ring_stream[idx], ti.a, ti.b, ti.dbdl, ti.xref)
+        t0 = time.perf_counter()
+        dev_ms = 0.0
+        done = 0
+        ctxs = [g[3] for g in groups]
+        while done < nmc:
+            n = min(chunk, nmc - done)
+            dev_ms += pg.Context.ti_advance_group(ctxs, n)
+            done += n
+            if verbose:
+                print("  %d / %d steps" % (done, nmc), flush=True)
+        wall = time.perf_counter() - t0
+        per_P = []
+        beads = 0
+        for P, idx, ti, ctx in groups:
+            mean, var, cnt = ctx.ti_lambda_reduce()
+            _, _, _, status = ctx.ti_results()
+            form_used, _ = ctx.ti_form(1)
+            dA, sigA, q = pg.ti_assemble(ti.w, mean, var, ti.betan)
+            try:
+                delta = pg.splitting_from_ratio(c["beta"], q)
+            except pg.PgError:
+                delta = float("nan")
+            nper = max(int(np.min(cnt)), 1)
+            per_P.append(dict(P=P, nrings=int(len(idx)), dA=dA, sigmaA=sigA, qratio=q, ln_qratio=-dA * ti.betan,
+                              ln_qratio_stderr=ti.betan * np.sqrt(max(sigA, 0.0) / nper), delta=delta,
+                              betan=ti.betan, dt=ti.cfg["dt"], form=form_used,
+                              nan_rings=int(np.sum(status != 0))))
+            beads += len(idx) * P
+    finally:
+        for g in groups:
+            g[3].close()
+    return dict(per_P=per_P, nrings=int(len(Pr)), beads=int(beads), nmc=nmc, device_s=dev_ms / 1e3, wall_s=wall,
+                bead_steps_per_s=beads * nmc / (dev_ms / 1e3))
 
 
 def linear_guess(w1, w2, N):

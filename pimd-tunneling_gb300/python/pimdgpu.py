@@ -28,7 +28,7 @@ EXPORTS = [
     "pg_ti_checkpoint_load", "pg_ti_release", "pg_propagate_pimd", "pg_gauleg", "pg_spline",
     "pg_splint", "pg_ti_assemble", "pg_splitting_from_ratio", "pg_instanton_fg",
     "pg_instanton_optimize", "pg_um_hessian", "pg_instanton_logdet", "pg_rpi_assemble",
-    "pg_nm_transform_noalloc",
+    "pg_nm_transform_noalloc", "pg_ti_advance_group",
 ]
 
 
@@ -74,6 +74,7 @@ def lib():
         L.pg_ti_setup.argtypes = [P, P, I64, I64, P, P, P, P, P, P, P, P, P]
         L.pg_ti_advance.argtypes = [P, I64]
         L.pg_ti_advance_timed.argtypes = [P, I64, P]
+        L.pg_ti_advance_group.argtypes = [P, I64, I64, P]
         L.pg_ti_get_state.argtypes = [P, P, P]
         L.pg_ti_get_results.argtypes = [P, P, P, P, P]
         L.pg_ti_lambda_reduce.argtypes = [P, P, P, P]
@@ -231,6 +232,15 @@ class Context:
         """Advance and return the device milliseconds (CUDA events on the library stream)."""
         ms = C.c_double()
         check(lib().pg_ti_advance_timed(self.h, nsteps, C.byref(ms)))
+        return ms.value
+
+    @staticmethod
+    def ti_advance_group(contexts, nsteps):
+        """Advance several contexts (e.g. one per bead number) concurrently;
+        returns the device milliseconds spanning all of them."""
+        arr = (C.c_void_p * len(contexts))(*[c.h for c in contexts])
+        ms = C.c_double()
+        check(lib().pg_ti_advance_group(arr, len(contexts), nsteps, C.byref(ms)))
         return ms.value
 
     def ti_state(self):

@@ -317,3 +317,62 @@ def test_mixed_long_run_has_no_nan(ctx, pg, form):
     s, n, _, st = ctx.ti_results()
     assert np.all(st == 0), np.sum(st != 0)
     assert np.all(np.isfinite(s))
+
+
+def _small_synth9(P=16, nrep=2, nint=2):
+    c = dict(pgconfigs.load("c2"))
+    c["P"] = P
+    ti = pgconfigs.TiInputs(c, nrep=nrep, nintegral=nint)
+    return c, ti
+
+
+def test_fused_fp64_many_dofs_matches_oracle(ctx, pg, oracle):
+    """27 dofs: the ring transforms run in four passes of up to eight dofs."""
+    c, ti = _small_synth9()
+    _set_system(ctx, c)
+    nsteps = 30
+    cfg = _gpu_cfg(pg, c, ti, pg.PG_FP64, pg.PG_FORM_FUSED)
+    ctx.ti_setup(cfg, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
+    ctx.ti_advance(nsteps)
+    x, p = ctx.ti_state()
+    s, n, _, st = ctx.ti_results()
+    prm = _oracle_prm(oracle, c, ti, True)
+    xo, po, so, no, _ = _oracle_run(oracle, c, ti, prm, nsteps)
+    assert np.all(st == 0)
+    np.testing.assert_array_equal(n, no)
+    np.testing.assert_allclose(x.reshape(xo.shape), xo, rtol=0, atol=1e-9)
+    np.testing.assert_allclose(s, so, rtol=1e-9, atol=1e-12)
+    # FP32 state + forces track FP64 over the same steps
+    cfg = _gpu_cfg(pg, c, ti, pg.PG_MIXED, pg.PG_FORM_FUSED)
+    ctx.ti_setup(cfg, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
+    ctx.ti_advance(nsteps)
+    x32, _ = ctx.ti_state()
+    assert np.max(np.abs(x32.reshape(xo.shape) - xo)) < 2e-3
+
+
+def test_advance_group_equals_separate_advances(pg):
+    """Two bead numbers in two contexts, advanced together on concurrent streams,
+    give bitwise the results of advancing each alone."""
+    runs = []
+    for together in (False, True):
+        ctxs, tis = [], []
+        for P in (16, 32):
+            c, ti = _small_2d(P=P, nrep=3, nint=2)
+            cx = pg.Context(0)
+            _set_system(cx, c)
+            cfg = _gpu_cfg(pg, c, ti, pg.PG_MIXED, pg.PG_FORM_FUSED)
+            cx.ti_setup(cfg, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
+            ctxs.append(cx)
+        if together:
+            ms = pg.Context.ti_advance_group(ctxs, 40)
+            assert ms > 0.0
+        else:
+            for cx in ctxs:
+                cx.ti_advance(40)
+        runs.append([(cx.ti_state(), cx.ti_results()[:2], cx.ti_step()) for cx in ctxs])
+        for cx in ctxs:
+            cx.close()
+    for (st_a, res_a, step_a), (st_b, res_b, step_b) in zip(*runs):
+        assert step_a == step_b == 40
+        for u, v in zip(st_a + res_a, st_b + res_b):
+            np.testing.assert_array_equal(u, v)

@@ -1,7 +1,7 @@
 """Full-scale validation runs (GPU + CPU oracle); writes a JSON summary.
 
 Not collected by pytest (long).  Run on a GB300:
-    python tests/validation/validate_full_scale.py [--out results.json] [--parts c0,c1,c2,c3]
+    python tests/validation/validate_full_scale.py [--out results.json] [--parts c0,c1,c2,c3,c4]
 
   c0: mcmod_1d, P=32, 11 lambda points, 20000 steps: the GPU plain (reference
       step order) and fused FP64 forms against the CPU restatement.
@@ -84,6 +84,17 @@ def part_c2(out, nmc=2000):
     fp64 = drivers.run_ti(c, precision=pg.PG_FP64, form=pg.PG_FORM_FUSED, nmc=nmc, chunk=250)
     out["c2"] = dict(mixed=mixed, fp64=fp64, ln_qratio_diff=mixed["ln_qratio"] - fp64["ln_qratio"],
                      ln_qratio_stderr=fp64["ln_qratio_stderr"])
+
+
+def part_c4(out, nmc=None):
+    """18-atom surface, 4096 rings with P in {64, 128, 256, 512}: one context
+    per P, advanced together; FP32 mixed precision and, on a shorter run, FP64."""
+    import drivers
+    import pgconfigs
+    import pimdgpu as pg
+    c = pgconfigs.load("c4")
+    mixed = drivers.run_ti_mixed(c, precision=pg.PG_MIXED, nmc=nmc, chunk=500)
+    out["c4"] = dict(mixed=mixed)
 
 
 def part_c3(out, factr=1e2, pgtol=1e-8):
