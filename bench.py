@@ -304,7 +304,7 @@ def main():
         achieved_gbs = kbytes / (kms / 1e3) / 1e9
         traffic = None
         try:
-            with open(os.path.join(ROOT, "profiles", "ti_tcgen05_c1_traffic.json")) as f:
+            with open(os.path.join(ROOT, "profiles", "k_tc_step_c1_traffic.json")) as f:
                 traffic = json.load(f).get(name.split()[0])
         except Exception:
             pass

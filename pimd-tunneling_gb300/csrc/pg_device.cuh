@@ -21,14 +21,10 @@ __host__ __device__ __forceinline__ U4 philox4x32_10(uint32_t c0, uint32_t c1, u
                                                      uint32_t c3, uint32_t k0, uint32_t k1) {
 #pragma unroll
     for (int r = 0; r < 10; r++) {
-#ifdef __CUDA_ARCH__
-        uint32_t lo0 = 0xD2511F53u * c0, hi0 = __umulhi(0xD2511F53u, c0);
-        uint32_t lo1 = 0xCD9E8D57u * c2, hi1 = __umulhi(0xCD9E8D57u, c2);
-#else
-        uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
-        uint32_t lo0 = (uint32_t)p0, hi0 = (uint32_t)(p0 >> 32);
-        uint32_t lo1 = (uint32_t)p1, hi1 = (uint32_t)(p1 >> 32);
-#endif
+        // 32 x 32 -> 64-bit products (one wide multiply each on the device)
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+        const uint32_t lo0 = (uint32_t)p0, hi0 = (uint32_t)(p0 >> 32);
+        const uint32_t lo1 = (uint32_t)p1, hi1 = (uint32_t)(p1 >> 32);
         uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
         c0 = n0;
         c1 = lo1;
@@ -89,42 +85,21 @@ __device__ __forceinline__ double normal_d(uint64_t seed, uint32_t stream, uint3
     return (n & 1) ? z1 : z0;
 }
 
-// FP32 Box-Muller from the top 24 bits of the same words.  The angle uses a
-// quadrant split and Taylor polynomials for sin / cos on [-pi/4, pi/4]
-// (|error| < 2e-9), so one Philox block yields four normals for one MUFU lg2
-// and one MUFU rsqrt per pair.
-__device__ __forceinline__ void sincos_turn_f(uint32_t w, float &s, float &c) {
-    // angle = 2 pi ((w >> 8) + 0.5) 2^-24 = q pi/2 + pi/4 + phi
-    uint32_t q = w >> 30;
-    float g = (float)((w >> 8) & 0x3FFFFFu) + 0.5f;                  // [0, 2^22)
-    float phi = (g * 2.384185791015625e-07f - 0.5f) * 1.5707963267948966f;  // [-pi/4, pi/4)
-    float p2 = phi * phi;
-    float sp = phi * (1.0f + p2 * (-1.6666667e-1f + p2 * (8.3333333e-3f +
-                p2 * (-1.9841270e-4f + p2 * 2.7557319e-6f))));
-    float cp = 1.0f + p2 * (-0.5f + p2 * (4.1666668e-2f + p2 * (-1.3888889e-3f +
-                p2 * 2.4801587e-5f)));
-    // rotate by pi/4
-    const float r2 = 0.70710678118654752f;
-    float s1 = (sp + cp) * r2, c1 = (cp - sp) * r2;
-    // rotate by q * pi/2
-    switch (q) {
-    case 0: s = s1; c = c1; break;
-    case 1: s = c1; c = -s1; break;
-    case 2: s = -s1; c = -c1; break;
-    default: s = -c1; c = s1; break;
-    }
-}
-
+// FP32 Box-Muller from the top 24 bits of the same words: radius from one
+// MUFU lg2 and one rsqrt, angle 2 pi u from the hardware sine / cosine on
+// [-pi, pi) (2 pi u = theta + pi, so sin and cos change sign); absolute error
+// of a normal below 1e-5, far inside the thermostat's statistical noise.
 __device__ __forceinline__ void box_muller_f(uint32_t wa, uint32_t wb, float &z0, float &z1) {
     float ua = ((float)(wa >> 8) + 0.5f) * 5.9604644775390625e-08f;
     // lg2.approx has an absolute error near u = 1 and can return 0 (or a tiny
     // positive value) there; clamp so that r stays finite (r -> ~0 for u -> 1).
     float t = fmaxf(-2.0f * 0.69314718055994531f * __log2f(ua), 1.0e-30f);
     float r = t * rsqrtf(t);
+    const float ub = ((float)(wb >> 8) + 0.5f) * 5.9604644775390625e-08f;  // (0, 1)
     float s, c;
-    sincos_turn_f(wb, s, c);
-    z0 = r * c;
-    z1 = r * s;
+    __sincosf(6.2831853071795865f * (ub - 0.5f), &s, &c);
+    z0 = -r * c;
+    z1 = -r * s;
 }
 
 __device__ __forceinline__ float normal_f(uint64_t seed, uint32_t stream, uint32_t step,

@@ -124,6 +124,4 @@ int tc_launch(pg_ctx *ctx, TiState &st, int64_t step0, int64_t nsteps, cudaStrea
 int tc_nm_transform(pg_ctx *ctx, int64_t P, int64_t ncol, const double *in, double *out);
 int32_t tc_error(pg_ctx *ctx, TiState &st);
 int tc_kernel_times(pg_ctx *ctx, TiState &st, int64_t nsteps, double *ms, int64_t *count);
-int tc_launch_one(pg_ctx *ctx, TiState &st, int do_est, int final_pass, cudaStream_t s);
-int tc_launch_g2(pg_ctx *ctx, TiState &st, cudaStream_t s);
 }  // namespace pg

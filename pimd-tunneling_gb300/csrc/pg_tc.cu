@@ -321,13 +321,11 @@ __global__ void k_build_split_image(unsigned char *img) {
 }
 
 // ---------------------------------------------------------------- TI step on the tensor cores
-// One MD step = two launches, each one split-BF16 GEMM per column tile:
-//   G1: x = T q + x* (positions), the estimator of the previous step (bead P),
-//       forces F = grad V(x) from the FP32 surface, written to HBM/L2;
-//   G2: (T F) per mode, then kick / half rotation / OU / half rotation of
-//       (q, pi) with Philox normals, written back.
-// The ring state (q, pi, F, x) stays resident in L2 between launches; the
-// launches of an advance are replayed from one captured CUDA graph.
+// One launch per MD step (k_tc_step): two split-BF16 GEMMs per column tile
+// with the forces in between, and one final launch per advance (k_tc_final)
+// for the positions and the estimator of the last step.  The ring state
+// (q, pi, x) stays resident in L2 between launches; the launches of an advance
+// are replayed from one captured CUDA graph, followed by one step-counter add.
 struct TcArgs {
     int64_t nrings;
     int nd, ndim, natom;
@@ -342,10 +340,11 @@ struct TcArgs {
     const int32_t *ringlam;
     const uint64_t *ringseed;
     const uint32_t *ringstream;
-    float *q, *pi, *x, *f;    // [ring][dof][P]
+    float *q, *pi, *x;        // [ring][dof][P]
     RingAcc *acc;
-    int64_t *stepA;           // current step: written by G2, read by G1
-    int64_t *stepB;           // copy for G2: written by G1, read by G2
+    const int64_t *step0;     // step counter at the start of the advance (not written by these kernels)
+    int64_t sofs;             // this launch's step offset within the advance
+    int do_est;               // accumulate the estimator of step s-1
     int32_t *err;
     // PES parameters (FP32)
     float wc[12];
@@ -357,32 +356,40 @@ struct TcArgs {
 
 // ---------------------------------------------------------------- column tiles
 // The TI step kernels work on tiles of kNc = 64 ring-dof columns with 256
-// threads (8 warps), two CTAs per SM.  One split-BF16 GEMM per launch,
-//     D[m][c] = sum_k T[m][k] X[c][k]     (M = 128 beads or modes, N = 64, K = 128),
-// takes T as the A operand (the bulk-copied image) and the FP32 state rows
-// X[c][:] of the tile, split by the CTA's threads, as the B operand.  TMEM lane m
-// then holds bead (or mode) m of all 64 columns: warp w reads lane quadrant
-// w % 4 and column half w / 4, so every epilogue access of a warp covers 32
-// consecutive beads of one column (128 contiguous bytes), and the x / y columns
-// of a ring (2r, 2r+1) sit in the same thread.
+// threads (8 warps), two CTAs per SM.  A split-BF16 GEMM
+//     D[m][c] = sum_k T[m][k] X[c][k]     (M = 128 beads or modes, N = 64, K = 128)
+// takes T as the A operand (the bulk-copied image) and a tile X of FP32 state
+// columns, split by the CTA's threads, as the B operand.  TMEM lane m then
+// holds bead (or mode) m of all 64 columns: warp w reads lane quadrant w % 4
+// and column half w / 4, so every epilogue access of a warp covers 32
+// consecutive beads of one column (128 contiguous bytes), and the x / y
+// columns of a ring (2r, 2r+1) sit in the same thread.  Tiles hold whole rings
+// (64 is a multiple of the 1 or 2 dofs of the surfaces this form runs).
 constexpr int kNc = 64;
 constexpr int kTileThreads = 256;
-// Epilogue group widths (columns per TMEM load): a thread walks its 32 columns
-// in groups, which bounds registers and code size.
-#ifndef PG_G1_COLS
-#define PG_G1_COLS 8
-#endif
-#ifndef PG_G2_COLS
-#define PG_G2_COLS 8
-#endif
-constexpr int kG1Cols = PG_G1_COLS;
-constexpr int kG2Cols = PG_G2_COLS;
-static_assert(kG1Cols == 8 || kG1Cols == 16 || kG1Cols == 32, "G1 group width");
-static_assert(kG2Cols == 8 || kG2Cols == 16 || kG2Cols == 32, "G2 group width");
-constexpr int kDataBytes = kNc * kP * 2;                     // one bf16 plane of a tile: 16 KB
-constexpr int kTileSmemOps = 2 * kOpBytes + 2 * kDataBytes;  // T hi/lo + X hi/lo: 96 KB
+constexpr int kGrp = 8;  // columns per TMEM load in the epilogues
+// B operand layout: K-major core matrices (8 rows x 16 bytes) as for T, but
+// K-adjacent core matrices kXLbo = 160 bytes apart (32 bytes of padding), so
+// that warp stores of one column's 32 beads (4 core matrices) and of the next
+// column (16 bytes further) fall in distinct banks.
+constexpr uint32_t kXLbo = 160;
+constexpr uint32_t kXSbo = 16 * kXLbo;                                 // 8-row groups: 2560 bytes
+constexpr int kXPlane = (kNc / 8) * (int)kXSbo;                        // one bf16 plane: 20 KB
+constexpr int kTileSmemOps = 2 * kOpBytes + 2 * kXPlane;               // T hi/lo + X hi/lo: 104 KB
 constexpr uint32_t kIdescN64 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kNc >> 3) << 17) |
                                ((uint32_t)(128 >> 4) << 24);
+
+__host__ __device__ __forceinline__ uint32_t x_offset(int row, int k) {
+    return (uint32_t)((row >> 3) * kXSbo + (k >> 3) * kXLbo + (row & 7) * 16 + (k & 7) * 2);
+}
+__device__ __forceinline__ uint64_t make_desc_x(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
+    d |= (uint64_t)(kXLbo >> 4) << 16;
+    d |= (uint64_t)(kXSbo >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
 
 // Per-column values staged in shared memory by the CTA.
 struct TileAux {
@@ -418,13 +425,13 @@ __device__ __forceinline__ void split8(const float (&v)[8], uint4 &hi, uint4 &lo
     lo = make_uint4(l[0], l[1], l[2], l[3]);
 }
 
-// Barriers, kNc TMEM columns, the T image by bulk copy, the tile
-// X[c][k] = src[c * P + k] (zero for c >= nvalid) split into the B operand, the
-// GEMM issued by thread 0 and waited for by every thread.  Returns whether the
-// accumulator is valid (the CTA-uniform error word is zero).
-__device__ __forceinline__ bool tc_tile_gemm(unsigned char *base, TcShared *sh, const unsigned char *gT,
-                                             const float *src, int nvalid, uint32_t *tmem_out) {
-    unsigned char *Thi = base, *Tlo = base + kOpBytes, *Xhi = base + 2 * kOpBytes, *Xlo = Xhi + kDataBytes;
+// Tile set-up: barriers, the T image by bulk copy, kNc TMEM columns, and the
+// tile X[c][k] = src[c * P + k] (zero for c >= nvalid) split into the B
+// operand.  Ends with a CTA barrier after which the operands are visible to
+// the tensor core.  Returns the TMEM base address.
+__device__ __forceinline__ uint32_t tile_begin(unsigned char *base, TcShared *sh, const unsigned char *gT,
+                                               const float *src, int nvalid) {
+    unsigned char *Thi = base, *Xhi = base + 2 * kOpBytes, *Xlo = Xhi + kXPlane;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (tid == 0) {
         mbar_init(&sh->mma_bar, 1);
@@ -434,10 +441,12 @@ __device__ __forceinline__ bool tc_tile_gemm(unsigned char *base, TcShared *sh, 
     }
     __syncthreads();
     load_transform(Thi, gT, sh);
-    if (warp == 0) tmem_alloc(&sh->tmem_slot, kNc);
+    if (warp == 0) {
+        __syncwarp();
+        tmem_alloc(&sh->tmem_slot, kNc);
+    }
     // Warp w fills rows 8w..8w+7.  Lane: row 8w + lane % 8, K chunks
-    // 8 (4 it + lane / 8): the 8 lanes of one chunk write one 128-byte core
-    // matrix, a warp store covers 512 contiguous bytes.
+    // 8 (4 it + lane / 8): the 8 lanes of one chunk write one core matrix.
     const int c = 8 * warp + (lane & 7);
     const bool v = c < nvalid;
     const float *row = src + (size_t)(v ? c : 0) * kP;
@@ -455,7 +464,7 @@ __device__ __forceinline__ bool tc_tile_gemm(unsigned char *base, TcShared *sh, 
                              w[2 * it + 1].x, w[2 * it + 1].y, w[2 * it + 1].z, w[2 * it + 1].w};
         uint4 hi, lo;
         split8(e8, hi, lo);
-        const uint32_t off = op_offset(c, k0);
+        const uint32_t off = x_offset(c, k0);
         *reinterpret_cast<uint4 *>(Xhi + off) = hi;
         *reinterpret_cast<uint4 *>(Xlo + off) = lo;
     }
@@ -463,41 +472,53 @@ __device__ __forceinline__ bool tc_tile_gemm(unsigned char *base, TcShared *sh, 
     tc_before();
     __syncthreads();
     tc_after();
-    const uint32_t tmem = sh->tmem_slot;
-    bool ok = mbar_wait(&sh->tma_bar, 0);
-    if (tid == 0) {
-        if (ok) {
-            const uint32_t th = smem_u32(Thi), tl = smem_u32(Tlo), xh = smem_u32(Xhi), xl = smem_u32(Xlo);
-#pragma unroll
-            for (int ks = 0; ks < kP / 16; ks++) {
-                const uint32_t koff = (uint32_t)ks * 2 * kLBO;
-                const uint64_t dth = make_desc(th + koff), dtl = make_desc(tl + koff);
-                const uint64_t dxh = make_desc(xh + koff), dxl = make_desc(xl + koff);
-                mma_bf16_n64(tmem, dth, dxh, ks > 0 ? 1u : 0u);
-                mma_bf16_n64(tmem, dth, dxl, 1u);
-                mma_bf16_n64(tmem, dtl, dxh, 1u);
-            }
-            mma_commit(&sh->mma_bar);
-        } else {
-            sh->err = 1;
-        }
+    return sh->tmem_slot;
+}
+
+// Thread 0 issues D = T X (3 split products per K step of 16) and commits it
+// to mma_bar; wait_t: first wait for the bulk copy of T.  A failed wait sets
+// the CTA error word instead of issuing.
+__device__ __forceinline__ void tile_issue(unsigned char *base, TcShared *sh, uint32_t tmem, bool wait_t) {
+    if (threadIdx.x != 0) return;
+    if (sh->err) return;
+    if (wait_t && !mbar_wait(&sh->tma_bar, 0)) {
+        sh->err |= 1;
+        return;
     }
-    __syncthreads();
+    const uint32_t th = smem_u32(base), tl = th + kOpBytes, xh = th + 2 * kOpBytes, xl = xh + kXPlane;
+#pragma unroll
+    for (int ks = 0; ks < kP / 16; ks++) {
+        const uint64_t dth = make_desc(th + (uint32_t)ks * 2 * kLBO), dtl = make_desc(tl + (uint32_t)ks * 2 * kLBO);
+        const uint64_t dxh = make_desc_x(xh + (uint32_t)ks * 2 * kXLbo),
+                       dxl = make_desc_x(xl + (uint32_t)ks * 2 * kXLbo);
+        mma_bf16_n64(tmem, dth, dxh, ks > 0 ? 1u : 0u);
+        mma_bf16_n64(tmem, dth, dxl, 1u);
+        mma_bf16_n64(tmem, dtl, dxh, 1u);
+    }
+    mma_commit(&sh->mma_bar);
+}
+
+// Every thread waits for the GEMM of the given mbarrier phase; returns whether
+// the accumulator is valid (CTA-uniform after the barrier).
+__device__ __forceinline__ bool tile_wait(TcShared *sh, uint32_t parity) {
+    __syncthreads();  // thread 0 has issued (or recorded an error)
     const bool issued = sh->err == 0;
-    if (issued && !mbar_wait(&sh->mma_bar, 0)) atomicOr(&sh->err, 2);
+    if (issued && !mbar_wait(&sh->mma_bar, parity)) atomicOr(&sh->err, 2);
     tc_after();
     __syncthreads();
-    *tmem_out = tmem;
     return sh->err == 0;
 }
 
-__device__ __forceinline__ void tc_tile_release(TcShared *sh, uint32_t tmem, int32_t *gerr) {
+__device__ __forceinline__ void tile_release(TcShared *sh, uint32_t tmem, int32_t *gerr, uint32_t parity) {
     const int tid = threadIdx.x, warp = tid >> 5;
     if (tid == 0 && sh->err) atomicOr(gerr, sh->err);
-    if (sh->err & 2) mbar_wait(&sh->mma_bar, 0);  // let an overdue MMA drain (bounded)
+    if (sh->err & 2) mbar_wait(&sh->mma_bar, parity);  // let an overdue MMA drain (bounded)
     tc_before();
     __syncthreads();
-    if (warp == 0) tmem_dealloc(tmem, kNc);
+    if (warp == 0) {
+        __syncwarp();
+        tmem_dealloc(tmem, kNc);
+    }
 }
 
 // Gradient of the FP32 six-well surface (mcmod_2dtest.f90:39-60) at the NR
@@ -533,6 +554,62 @@ __device__ __forceinline__ void grad_2d_n(const TcArgs &a, const float (&xv)[2 *
     }
 }
 
+// Forces of kGrp columns of one bead (PESK 2: kGrp/2 rings of the 2-D surface;
+// PESK 1: kGrp rings of the 1-D quartic).
+template <int PESK>
+__device__ __forceinline__ void group_forces(const TcArgs &a, const float (&xv)[kGrp], float (&fv)[kGrp]) {
+    if constexpr (PESK == 2) {
+        constexpr int NR = kGrp / 2;
+        float gx[NR], gy[NR];
+        if (a.pow10)
+            grad_2d_n<true, NR>(a, xv, gx, gy);
+        else
+            grad_2d_n<false, NR>(a, xv, gx, gy);
+#pragma unroll
+        for (int r = 0; r < NR; r++) {
+            fv[2 * r] = gx[r];
+            fv[2 * r + 1] = gy[r];
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < kGrp; i++) {
+            const float u = xv[i] / a.x0;
+            const float w = u * u - 1.0f;
+            fv[i] = w * 4.0f * a.H * xv[i] / (a.x0 * a.x0);
+        }
+    }
+}
+
+// Positions x = T q + x* of one group (kGrp columns from c0 of this thread's
+// half), read from TMEM; the bead-P values go to the estimator staging.
+__device__ __forceinline__ void group_positions(const TileAux *ax, uint32_t taddr, int cb, int c0, int m,
+                                                bool stage_p, float (&xv)[kGrp], float *xP) {
+    __syncwarp();  // tcgen05.ld is .sync.aligned: issue it from a converged warp
+    tmem_ldn<kGrp>(taddr + (uint32_t)c0, xv);
+    const float fm = (float)(m + 1);
+#pragma unroll
+    for (int i = 0; i < kGrp; i++) xv[i] += ax->xa[cb + c0 + i] + ax->xs[cb + c0 + i] * fm;
+    if (stage_p && m == kP - 1)
+#pragma unroll
+        for (int i = 0; i < kGrp; i++) xP[cb + c0 + i] = xv[i];
+}
+
+// Estimator of step s-1 (verletmodule.f90:397-403) from the staged bead-P
+// positions, one thread per ring of the tile.
+__device__ __forceinline__ void tile_estimator(const TcArgs &a, const TileAux *ax, int64_t col0, int nvalid,
+                                               int64_t s) {
+    const int nd = a.nd, tid = threadIdx.x;
+    if (tid >= nvalid / nd || (s - 1) < a.imin) return;
+    const int64_t ring = col0 / nd + tid;
+    const int lam = a.ringlam[ring];
+    double contr = 0.0;
+    for (int j = 0; j < nd; j++)
+        contr += a.mass[j / a.ndim] * (-(double)ax->xP[tid * nd + j]) * a.dbdl[(size_t)lam * nd + j];
+    RingAcc *r = &a.acc[ring];
+    if (r->status == 0) r->dhdr_sum += contr;
+    r->nsamples += 1;
+}
+
 __device__ __forceinline__ float sel4(const float (&v)[4], int i) {
     float r = v[0];
     r = i == 1 ? v[1] : r;
@@ -541,9 +618,65 @@ __device__ __forceinline__ float sel4(const float (&v)[4], int i) {
     return r;
 }
 
-// G1: positions x = T q + x*, the estimator of the previous step, forces.
-template <int PESK>
-__global__ void __launch_bounds__(kTileThreads, 2) k_tc_g1(TcArgs a, int do_est, int write_x) {
+// This thread's OU normals for its mode m and the 32 columns of its half:
+// zc[i] = normal j P + m of the Philox stream of column cb + i at step st.
+// Lane e of a quad draws the block of column 4g + e (normals j P + 4 (m/4) ..
+// +3, the four modes of the quad), then the quad transposes the 4 x 4 values.
+__device__ __forceinline__ void tile_normals(const TileAux *ax, int64_t col0, int nd, int cb, int m, uint32_t st,
+                                             float (&zc)[32]) {
+    const int e = threadIdx.x & 3;
+#pragma unroll
+    for (int g0 = 0; g0 < 8; g0 += 4) {
+        U4 o[4];
+#pragma unroll
+        for (int g = 0; g < 4; g++) {
+            const int cc = cb + 4 * (g0 + g) + e;
+            const int j = (int)((col0 + cc) % nd);
+            o[g] = philox_block(ax->seed[cc], ax->stream[cc], st, kRngLangevin, (uint32_t)((j * kP + m) >> 2));
+        }
+#pragma unroll
+        for (int g = 0; g < 4; g++) {
+            float z[4];
+            box_muller_f(o[g].x, o[g].y, z[0], z[1]);
+            box_muller_f(o[g].z, o[g].w, z[2], z[3]);
+            float rv[4];  // rv[r]: this mode's normal for column 4g + (e ^ r)
+            rv[0] = sel4(z, e);
+#pragma unroll
+            for (int r = 1; r < 4; r++) rv[r] = __shfl_xor_sync(0xffffffffu, sel4(z, e ^ r), r);
+#pragma unroll
+            for (int k = 0; k < 4; k++) zc[4 * (g0 + g) + k] = sel4(rv, e ^ k);
+        }
+    }
+}
+
+// Writes the kGrp force values of bead m (one per column c0 + i of this
+// thread's half) into the B operand as rows c, K index m.  Adjacent lanes pair
+// up with one shuffle per column pair: the even lane stores (m, m+1) of column
+// c, the odd lane (m-1, m) of column c+1, 4 bytes each per plane.
+__device__ __forceinline__ void group_store_operand(unsigned char *Xhi, unsigned char *Xlo, int cb, int c0, int m,
+                                                    const float (&fv)[kGrp]) {
+    const bool odd = (m & 1) != 0;
+#pragma unroll
+    for (int i = 0; i < kGrp; i += 2) {
+        const float send = odd ? fv[i] : fv[i + 1];
+        const float recv = __shfl_xor_sync(0xffffffffu, send, 1);
+        const float v0 = odd ? recv : fv[i];          // bead m & ~1
+        const float v1 = odd ? fv[i + 1] : recv;      // bead m | 1
+        const int col = cb + c0 + i + (odd ? 1 : 0);
+        __nv_bfloat16 h0 = __float2bfloat16_rn(v0), h1 = __float2bfloat16_rn(v1);
+        __nv_bfloat162 hh;
+        hh.x = h0;
+        hh.y = h1;
+        const uint32_t lo = pack_bf16(v0 - __bfloat162float(h0), v1 - __bfloat162float(h1));
+        const uint32_t off = x_offset(col, m & ~1);
+        *reinterpret_cast<uint32_t *>(Xhi + off) = *reinterpret_cast<uint32_t *>(&hh);
+        *reinterpret_cast<uint32_t *>(Xlo + off) = lo;
+    }
+}
+
+// Final pass of an advance: positions x = T q + x* written out, and the
+// estimator of the last step.
+__global__ void __launch_bounds__(kTileThreads, 2) k_tc_final(TcArgs a) {
     extern __shared__ unsigned char dsm[];
     unsigned char *base = align1k(dsm);
     TcShared *sh = reinterpret_cast<TcShared *>(base + kTileSmemOps);
@@ -552,7 +685,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_g1(TcArgs a, int do_est,
     const int nd = a.nd;
     const int64_t col0 = (int64_t)blockIdx.x * kNc;
     const int nvalid = (int)min((int64_t)kNc, a.nrings * nd - col0);
-    const int64_t s = *a.stepA;
+    const int64_t s = *a.step0 + a.sofs;
     if (tid < kNc) {
         float xa = 0.f, xs = 0.f;
         if (tid < nvalid) {
@@ -565,159 +698,125 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_g1(TcArgs a, int do_est,
         ax->xa[tid] = xa;
         ax->xs[tid] = xs;
     }
-    uint32_t tmem;
-    const bool ok = tc_tile_gemm(base, sh, a.gT, a.q + col0 * kP, nvalid, &tmem);
+    const uint32_t tmem = tile_begin(base, sh, a.gT, a.q + col0 * kP, nvalid);
+    tile_issue(base, sh, tmem, true);
+    const bool ok = tile_wait(sh, 0);
     if (ok) {
-        const int m = 32 * (warp & 3) + lane;  // bead
-        const int cb = 32 * (warp >> 2);        // first column of this thread's half
-        const int nv = nvalid - cb;              // valid columns in the half (may be <= 0)
+        const int m = 32 * (warp & 3) + lane;
+        const int cb = 32 * (warp >> 2);
         const uint32_t taddr = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)cb;
-        const float fm = (float)(m + 1);
 #pragma unroll 1
-        for (int c0 = 0; c0 < 32; c0 += kG1Cols) {
-            float xv[kG1Cols];
-            __syncwarp();  // tcgen05.ld is .sync.aligned: issue it from a converged warp
-            tmem_ldn<kG1Cols>(taddr + (uint32_t)c0, xv);
-#pragma unroll
-            for (int i = 0; i < kG1Cols; i++) xv[i] += ax->xa[cb + c0 + i] + ax->xs[cb + c0 + i] * fm;
-            if (do_est && m == kP - 1)
-#pragma unroll
-                for (int i = 0; i < kG1Cols; i++) ax->xP[cb + c0 + i] = xv[i];
-            const int nvg = nv - c0;  // valid columns of this group (may be <= 0)
+        for (int c0 = 0; c0 < 32; c0 += kGrp) {
+            float xv[kGrp];
+            group_positions(ax, taddr, cb, c0, m, a.do_est != 0, xv, ax->xP);
+            const int nvg = nvalid - cb - c0;
             float *xo = a.x + (size_t)(col0 + cb + c0) * kP + m;
-            float *fo = a.f + (size_t)(col0 + cb + c0) * kP + m;
-            if (write_x)
 #pragma unroll
-                for (int i = 0; i < kG1Cols; i++)
-                    if (i < nvg) xo[(size_t)i * kP] = xv[i];
-            if constexpr (PESK == 2) {
-                constexpr int NR = kG1Cols / 2;
-                float gx[NR], gy[NR];
-                if (a.pow10)
-                    grad_2d_n<true, NR>(a, xv, gx, gy);
-                else
-                    grad_2d_n<false, NR>(a, xv, gx, gy);
-#pragma unroll
-                for (int r = 0; r < NR; r++)
-                    if (2 * r < nvg) {
-                        fo[(size_t)(2 * r) * kP] = gx[r];
-                        fo[(size_t)(2 * r + 1) * kP] = gy[r];
-                    }
-            } else {
-#pragma unroll
-                for (int i = 0; i < kG1Cols; i++) {
-                    const float u = xv[i] / a.x0;
-                    const float w = u * u - 1.0f;
-                    if (i < nvg) fo[(size_t)i * kP] = w * 4.0f * a.H * xv[i] / (a.x0 * a.x0);
-                }
-            }
+            for (int i = 0; i < kGrp; i++)
+                if (i < nvg) xo[(size_t)i * kP] = xv[i];
         }
     }
     __syncthreads();  // xP complete
-    if (ok && do_est && tid < nvalid / nd && (s - 1) >= a.imin) {
-        // estimator of step s-1 (verletmodule.f90:397-403), one thread per ring
-        const int64_t ring = col0 / nd + tid;
-        const int lam = a.ringlam[ring];
-        double contr = 0.0;
-        for (int j = 0; j < nd; j++)
-            contr += a.mass[j / a.ndim] * (-(double)ax->xP[tid * nd + j]) * a.dbdl[(size_t)lam * nd + j];
-        RingAcc *r = &a.acc[ring];
-        if (r->status == 0) r->dhdr_sum += contr;
-        r->nsamples += 1;
-    }
-    if (blockIdx.x == 0 && tid == 0) *a.stepB = s;
-    tc_tile_release(sh, tmem, a.err);
+    if (ok && a.do_est) tile_estimator(a, ax, col0, nvalid, s);
+    tile_release(sh, tmem, a.err, 0);
 }
 
-// G2: kick with T F, half rotation, OU, half rotation (verletmodule.f90:423-435).
-// The coefficient table is per (atom, mode); the tensor form runs one-atom
-// systems, so a thread keeps its mode's six coefficients in registers.
-__global__ void __launch_bounds__(kTileThreads, 2) k_tc_g2(TcArgs a) {
+// One MD step of a tile (verletmodule.f90:423-435 in normal-mode form):
+//   GEMM 1: x = T q + x*; estimator of step s-1; forces F(x) split straight
+//           into the B operand;
+//   GEMM 2: T F; kick, half rotation, OU (normals drawn while GEMM 1 runs),
+//           half rotation of (q, pi), written back.
+template <int PESK>
+__global__ void __launch_bounds__(kTileThreads, 2) k_tc_step(TcArgs a) {
     extern __shared__ unsigned char dsm[];
     unsigned char *base = align1k(dsm);
+    unsigned char *Xhi = base + 2 * kOpBytes, *Xlo = Xhi + kXPlane;
     TcShared *sh = reinterpret_cast<TcShared *>(base + kTileSmemOps);
     TileAux *ax = reinterpret_cast<TileAux *>(base + kTileSmemOps + 256);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int nd = a.nd;
     const int64_t col0 = (int64_t)blockIdx.x * kNc;
     const int nvalid = (int)min((int64_t)kNc, a.nrings * nd - col0);
-    const int64_t s = *a.stepB;
+    const int64_t s = *a.step0 + a.sofs;
     if (tid < kNc) {
+        float xa = 0.f, xs = 0.f;
         uint64_t sd = 0;
         uint32_t sm = 0;
         if (tid < nvalid) {
             const int64_t ring = (col0 + tid) / nd;
+            const int j = (int)(col0 + tid - ring * nd);
+            const int lam = a.ringlam[ring];
+            xa = (float)a.avec[j];
+            xs = (float)((a.bvec[(size_t)lam * nd + j] - a.avec[j]) / (double)(kP + 1));
             sd = a.ringseed[ring];
             sm = a.ringstream[ring];
         }
+        ax->xa[tid] = xa;
+        ax->xs[tid] = xs;
         ax->seed[tid] = sd;
         ax->stream[tid] = sm;
     }
-    uint32_t tmem;
-    const bool ok = tc_tile_gemm(base, sh, a.gT, a.f + col0 * kP, nvalid, &tmem);
+    const uint32_t tmem = tile_begin(base, sh, a.gT, a.q + col0 * kP, nvalid);
+    tile_issue(base, sh, tmem, true);
+    const int m = 32 * (warp & 3) + lane;  // bead (GEMM 1) / mode (GEMM 2)
+    const int cb = 32 * (warp >> 2);        // first column of this thread's half
+    const int nv = nvalid - cb;              // valid columns of the half (may be <= 0)
+    const uint32_t taddr = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)cb;
+    float zc[32];
+    tile_normals(ax, col0, nd, cb, m, (uint32_t)s, zc);
+    bool ok = tile_wait(sh, 0);
     if (ok) {
-        const int m = 32 * (warp & 3) + lane;  // mode
-        const int cb = 32 * (warp >> 2);
-        const int nv = nvalid - cb;
-        const int e = lane & 3;
-        const uint32_t taddr = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)cb;
+#pragma unroll 1
+        for (int c0 = 0; c0 < 32; c0 += kGrp) {
+            float xv[kGrp], fv[kGrp];
+            group_positions(ax, taddr, cb, c0, m, a.do_est != 0, xv, ax->xP);
+            group_forces<PESK>(a, xv, fv);
+            group_store_operand(Xhi, Xlo, cb, c0, m, fv);
+        }
+        fence_async_smem();
+    }
+    tc_before();
+    __syncthreads();  // F operand complete, TMEM reads of GEMM 1 done, xP staged
+    tc_after();
+    uint32_t last_phase = 0;  // parity of the last GEMM issued (for the drain on a timeout)
+    if (ok) {
+        tile_issue(base, sh, tmem, false);
+        last_phase = 1;
+    }
+    if (ok && a.do_est) tile_estimator(a, ax, col0, nvalid, s);
+    if (ok) ok = tile_wait(sh, 1);
+    if (ok) {
         const float4 c4 = *reinterpret_cast<const float4 *>(a.coef + (size_t)m * 8);
         const float2 c2 = *reinterpret_cast<const float2 *>(a.coef + (size_t)m * 8 + 4);
         const float dt = a.dt;
-        const uint32_t st = (uint32_t)s;
         uint32_t badbits = 0;
-        // Groups of kG2Cols columns.  Per group, the state loads are issued
-        // first, then the independent Philox blocks, then the updates.
-#pragma unroll 1
-        for (int c0 = 0; c0 < 32; c0 += kG2Cols) {
-            constexpr int NQ = kG2Cols / 4;  // column quads of the group
-            float gv[kG2Cols];
-            __syncwarp();
-            tmem_ldn<kG2Cols>(taddr + (uint32_t)c0, gv);
+#pragma unroll
+        for (int c0 = 0; c0 < 32; c0 += kGrp) {
             const int nvg = nv - c0;
             float *qo = a.q + (size_t)(col0 + cb + c0) * kP + m;
             float *po = a.pi + (size_t)(col0 + cb + c0) * kP + m;
-            float qv[kG2Cols], pv[kG2Cols];
+            float qv[kGrp], pv[kGrp], gv[kGrp];
 #pragma unroll
-            for (int i = 0; i < kG2Cols; i++) {
+            for (int i = 0; i < kGrp; i++) {
                 qv[i] = i < nvg ? qo[(size_t)i * kP] : 0.f;
                 pv[i] = i < nvg ? po[(size_t)i * kP] : 0.f;
             }
-            // Lane e of a quad draws the Philox block of column 4g + e: normals
-            // j P + 4 (m / 4) .. + 3 of the ring's stream, the four modes of the quad.
-            U4 o[NQ];
+            __syncwarp();
+            tmem_ldn<kGrp>(taddr + (uint32_t)c0, gv);
 #pragma unroll
-            for (int g = 0; g < NQ; g++) {
-                const int cc = cb + c0 + 4 * g + e;
-                const int j = (int)((col0 + cc) % nd);
-                o[g] = philox_block(ax->seed[cc], ax->stream[cc], st, kRngLangevin, (uint32_t)((j * kP + m) >> 2));
-            }
-#pragma unroll
-            for (int g = 0; g < NQ; g++) {
-                float z[4];
-                box_muller_f(o[g].x, o[g].y, z[0], z[1]);
-                box_muller_f(o[g].z, o[g].w, z[2], z[3]);
-                // 4 x 4 transpose within the quad: rv[r] = this mode's normal for column 4g + (e ^ r)
-                float rv[4];
-                rv[0] = sel4(z, e);
-#pragma unroll
-                for (int r = 1; r < 4; r++) rv[r] = __shfl_xor_sync(0xffffffffu, sel4(z, e ^ r), r);
-#pragma unroll
-                for (int k = 0; k < 4; k++) {
-                    const int i = 4 * g + k;
-                    const float zk = sel4(rv, e ^ k);
-                    const float p0 = pv[i] - dt * gv[i];
-                    const float q0 = qv[i];
-                    float p1 = c4.x * p0 + c4.y * q0;
-                    const float q1 = c4.z * p0 + c4.w * q0;
-                    p1 = c2.x * p1 + c2.y * zk;
-                    const float pn = c4.x * p1 + c4.y * q1;
-                    const float qn = c4.z * p1 + c4.w * q1;
-                    if (i < nvg) {
-                        qo[(size_t)i * kP] = qn;
-                        po[(size_t)i * kP] = pn;
-                        if (pn != pn) badbits |= 1u << (c0 + i);
-                    }
+            for (int i = 0; i < kGrp; i++) {
+                const float zk = zc[c0 + i];
+                const float p0 = pv[i] - dt * gv[i];
+                const float q0 = qv[i];
+                float p1 = c4.x * p0 + c4.y * q0;
+                const float q1 = c4.z * p0 + c4.w * q0;
+                p1 = c2.x * p1 + c2.y * zk;
+                const float pn = c4.x * p1 + c4.y * q1;
+                const float qn = c4.z * p1 + c4.w * q1;
+                if (i < nvg) {
+                    qo[(size_t)i * kP] = qn;
+                    po[(size_t)i * kP] = pn;
+                    if (pn != pn) badbits |= 1u << (c0 + i);
                 }
             }
         }
@@ -730,9 +829,10 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_g2(TcArgs a) {
                 }
         }
     }
-    if (blockIdx.x == 0 && tid == 0) *a.stepA = s + 1;
-    tc_tile_release(sh, tmem, a.err);
+    tile_release(sh, tmem, a.err, last_phase);
 }
+
+__global__ void k_tc_step_add(int64_t *step, int64_t n) { *step += n; }
 
 // Host: split-BF16 image of T in the K-major core-matrix layout (B operand, rows = beads).
 static void build_split_image(int P, std::vector<unsigned char> &img) {
@@ -801,9 +901,9 @@ int tc_prepare(pg_ctx *ctx, TiState &st) {
     PG_CUDA(cudaMemsetAsync(d + tbf_err_off(ctx->natom), 0, 64, ctx->stream));
     PG_CUDA(cudaStreamSynchronize(ctx->stream));
     size_t sm = tc_smem_bytes();
-    PG_CUDA(cudaFuncSetAttribute(k_tc_g1<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    PG_CUDA(cudaFuncSetAttribute(k_tc_g1<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    PG_CUDA(cudaFuncSetAttribute(k_tc_g2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    PG_CUDA(cudaFuncSetAttribute(k_tc_step<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    PG_CUDA(cudaFuncSetAttribute(k_tc_step<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    PG_CUDA(cudaFuncSetAttribute(k_tc_final, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     return PG_OK;
 }
 
@@ -829,8 +929,7 @@ static void tc_make_args(pg_ctx *ctx, TiState &st, TcArgs &a, int &pesk) {
     a.gT = d;
     a.coef = reinterpret_cast<const float *>(d + tbf_coef_off());
     a.err = reinterpret_cast<int32_t *>(d + tbf_err_off(ctx->natom));
-    a.stepB = reinterpret_cast<int64_t *>(d + tbf_err_off(ctx->natom) + 8);
-    a.stepA = reinterpret_cast<int64_t *>(st.red.as<double>() + 3 * st.nlambda);
+    a.step0 = reinterpret_cast<const int64_t *>(st.red.as<double>() + 3 * st.nlambda);
     a.mass = ctx->d_mass.as<double>();
     a.avec = st.avec.as<double>();
     a.bvec = st.bvec.as<double>();
@@ -841,7 +940,6 @@ static void tc_make_args(pg_ctx *ctx, TiState &st, TcArgs &a, int &pesk) {
     a.q = st.q.as<float>();
     a.pi = st.pi.as<float>();
     a.x = st.x.as<float>();
-    a.f = st.f.as<float>();
     a.acc = st.acc.as<RingAcc>();
     pesk = ctx->pes_id == PG_PES_2DTEST ? 2 : 1;
     const std::vector<double> &p = ctx->params;
@@ -864,82 +962,74 @@ static void tc_make_args(pg_ctx *ctx, TiState &st, TcArgs &a, int &pesk) {
 
 static unsigned tc_grid(const TiState &st) { return (unsigned)((st.nrings * st.nd + kNc - 1) / kNc); }
 
-int tc_launch_one(pg_ctx *ctx, TiState &st, int do_est, int final_pass, cudaStream_t s) {
+// Step i of an advance (k_tc_step), or the final pass after n steps (k_tc_final).
+static int tc_launch_step(pg_ctx *ctx, TiState &st, int64_t i, cudaStream_t s) {
     TcArgs a;
     int pesk;
     tc_make_args(ctx, st, a, pesk);
-    size_t sm = tc_smem_bytes();
+    a.sofs = i;
+    a.do_est = i > 0 ? 1 : 0;
+    const size_t sm = tc_smem_bytes();
     if (pesk == 2)
-        k_tc_g1<2><<<tc_grid(st), kTileThreads, sm, s>>>(a, do_est, final_pass);
+        k_tc_step<2><<<tc_grid(st), kTileThreads, sm, s>>>(a);
     else
-        k_tc_g1<1><<<tc_grid(st), kTileThreads, sm, s>>>(a, do_est, final_pass);
+        k_tc_step<1><<<tc_grid(st), kTileThreads, sm, s>>>(a);
     cudaError_t e = cudaGetLastError();
-    return e == cudaSuccess ? PG_OK : cuda_fail(e, "k_tc_g1 launch");
+    return e == cudaSuccess ? PG_OK : cuda_fail(e, "k_tc_step launch");
 }
 
-int tc_launch_g2(pg_ctx *ctx, TiState &st, cudaStream_t s) {
+static int tc_launch_final(pg_ctx *ctx, TiState &st, int64_t n, cudaStream_t s) {
     TcArgs a;
     int pesk;
     tc_make_args(ctx, st, a, pesk);
-    k_tc_g2<<<tc_grid(st), kTileThreads, tc_smem_bytes(), s>>>(a);
+    a.sofs = n;
+    a.do_est = n > 0 ? 1 : 0;
+    k_tc_final<<<tc_grid(st), kTileThreads, tc_smem_bytes(), s>>>(a);
     cudaError_t e = cudaGetLastError();
-    return e == cudaSuccess ? PG_OK : cuda_fail(e, "k_tc_g2 launch");
+    if (e != cudaSuccess) return cuda_fail(e, "k_tc_final launch");
+    k_tc_step_add<<<1, 1, 0, s>>>(const_cast<int64_t *>(a.step0), n);
+    e = cudaGetLastError();
+    return e == cudaSuccess ? PG_OK : cuda_fail(e, "step counter launch");
 }
 
 int tc_launch(pg_ctx *ctx, TiState &st, int64_t, int64_t nsteps, cudaStream_t s) {
-    if (nsteps < 0) return PG_OK;  // the HBM copy of the state is current after every launch
-    for (int64_t i = 0; i <= nsteps; i++) {
-        const int do_est = i > 0 ? 1 : 0, final_pass = (i == nsteps) ? 1 : 0;
-        int rc = tc_launch_one(ctx, st, do_est, final_pass, s);
-        if (rc) return rc;
-        if (final_pass) break;
-        rc = tc_launch_g2(ctx, st, s);
+    if (nsteps < 0) return PG_OK;  // the HBM copy of the state is current after every advance
+    for (int64_t i = 0; i < nsteps; i++) {
+        int rc = tc_launch_step(ctx, st, i, s);
         if (rc) return rc;
     }
-    return PG_OK;
+    return tc_launch_final(ctx, st, nsteps, s);
 }
 
-// Per-kernel event timing of nsteps steps (direct launches, no graph): ms[0] = G1, ms[1] = G2.
+// Per-kernel event timing of nsteps steps (direct launches, no graph):
+// ms[0] = k_tc_step, ms[1] = k_tc_final.
 int tc_kernel_times(pg_ctx *ctx, TiState &st, int64_t nsteps, double *ms, int64_t *count) {
     cudaStream_t s = ctx->stream;
-    std::vector<cudaEvent_t> ev(4 * nsteps + 2);
+    std::vector<cudaEvent_t> ev(nsteps + 3);
     for (auto &e : ev) PG_CUDA(cudaEventCreate(&e));
-    // record G1/G2 separately by launching one step at a time through tc_launch's
-    // kernels: a step is G1 (no estimator skip after the first) + G2; the final G1
-    // is launched once at the end.
-    double t1 = 0.0, t2 = 0.0;
-    int64_t n1 = 0, n2 = 0;
     for (int64_t i = 0; i < nsteps; i++) {
-        PG_CUDA(cudaEventRecord(ev[4 * i], s));
-        int rc = tc_launch_one(ctx, st, i > 0 ? 1 : 0, 0, s);
+        PG_CUDA(cudaEventRecord(ev[i], s));
+        int rc = tc_launch_step(ctx, st, i, s);
         if (rc) return rc;
-        PG_CUDA(cudaEventRecord(ev[4 * i + 1], s));
-        PG_CUDA(cudaEventRecord(ev[4 * i + 2], s));
-        rc = tc_launch_g2(ctx, st, s);
-        if (rc) return rc;
-        PG_CUDA(cudaEventRecord(ev[4 * i + 3], s));
     }
-    PG_CUDA(cudaEventRecord(ev[4 * nsteps], s));
-    int rc = tc_launch_one(ctx, st, 1, 1, s);
+    PG_CUDA(cudaEventRecord(ev[nsteps], s));
+    int rc = tc_launch_final(ctx, st, nsteps, s);  // includes the step-counter add
     if (rc) return rc;
-    PG_CUDA(cudaEventRecord(ev[4 * nsteps + 1], s));
+    PG_CUDA(cudaEventRecord(ev[nsteps + 1], s));
     PG_CUDA(cudaStreamSynchronize(s));
-    for (int64_t i = 0; i <= nsteps; i++) {
+    double t1 = 0.0;
+    for (int64_t i = 0; i < nsteps; i++) {
         float a = 0.f;
-        PG_CUDA(cudaEventElapsedTime(&a, ev[4 * i], ev[4 * i + 1]));
+        PG_CUDA(cudaEventElapsedTime(&a, ev[i], ev[i + 1]));
         t1 += a;
-        n1++;
-        if (i < nsteps) {
-            PG_CUDA(cudaEventElapsedTime(&a, ev[4 * i + 2], ev[4 * i + 3]));
-            t2 += a;
-            n2++;
-        }
     }
+    float a2 = 0.f;
+    PG_CUDA(cudaEventElapsedTime(&a2, ev[nsteps], ev[nsteps + 1]));
     for (auto &e : ev) cudaEventDestroy(e);
-    ms[0] = t1 / (double)n1;
-    ms[1] = n2 ? t2 / (double)n2 : 0.0;
-    count[0] = n1;
-    count[1] = n2;
+    ms[0] = t1 / (double)nsteps;
+    ms[1] = a2;
+    count[0] = nsteps;
+    count[1] = 1;
     return PG_OK;
 }
 

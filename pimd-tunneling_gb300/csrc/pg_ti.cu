@@ -68,8 +68,33 @@ inline size_t ring_smem_bytes(int P, bool fp32) {
     return (size_t)kMvDofs * (size_t)P * (fp32 ? sizeof(float) : sizeof(double));
 }
 
+// One pass of ring_tmv over NB dofs d0..d0+NB-1 (NB a compile-time width).
+template <int NB, typename R, typename Load, typename Store>
+__device__ __forceinline__ void ring_tmv_pass(const R *__restrict__ T, int P, int d0, R *__restrict__ sbuf, Load &load,
+                                              Store &store) {
+    for (int e = threadIdx.x; e < NB * P; e += blockDim.x) {
+        const int dd = e / P, k = e - dd * P;
+        sbuf[k * NB + dd] = load(d0 + dd, k);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < P; i += blockDim.x) {
+        R acc[NB];
+#pragma unroll
+        for (int dd = 0; dd < NB; dd++) acc[dd] = (R)0;
+        for (int k = 0; k < P; k++) {
+            const R t = T[(size_t)k * P + i];
+            const R *v = sbuf + k * NB;
+#pragma unroll
+            for (int dd = 0; dd < NB; dd++) acc[dd] += t * v[dd];
+        }
+#pragma unroll
+        for (int dd = 0; dd < NB; dd++) store(d0 + dd, i, acc[dd]);
+    }
+    __syncthreads();
+}
+
 // store(dof, i, sum_k T[k][i] v[dof][k]) for every (dof, i) of one ring, where
-// v[dof][k] = load(dof, k).  Passes of up to kMvDofs dofs: v is staged in
+// v[dof][k] = load(dof, k).  Passes of 8, 4, 2 or 1 dofs: v is staged in
 // shared memory as sbuf[k][dd], each thread owns outputs i and reads T[k][i]
 // once per pass for all dofs of the pass.  Every output sums k = 0..P-1 in
 // order (the dsymv-order sum of the CPU restatement).
@@ -77,29 +102,22 @@ template <typename R, typename Load, typename Store>
 __device__ __forceinline__ void ring_tmv(const TiArgs &a, R *__restrict__ sbuf, Load load, Store store) {
     const R *T = tmat<R>(a);
     const int P = a.P, nd = a.nd;
-    for (int d0 = 0; d0 < nd; d0 += kMvDofs) {
-        const int nb = min(kMvDofs, nd - d0);
-        for (int e = threadIdx.x; e < nb * P; e += blockDim.x) {
-            const int dd = e / P, k = e - dd * P;
-            sbuf[k * kMvDofs + dd] = load(d0 + dd, k);
+    int d0 = 0;
+    while (d0 < nd) {
+        const int left = nd - d0;
+        if (left >= 8) {
+            ring_tmv_pass<8>(T, P, d0, sbuf, load, store);
+            d0 += 8;
+        } else if (left >= 4) {
+            ring_tmv_pass<4>(T, P, d0, sbuf, load, store);
+            d0 += 4;
+        } else if (left >= 2) {
+            ring_tmv_pass<2>(T, P, d0, sbuf, load, store);
+            d0 += 2;
+        } else {
+            ring_tmv_pass<1>(T, P, d0, sbuf, load, store);
+            d0 += 1;
         }
-        __syncthreads();
-        for (int i = threadIdx.x; i < P; i += blockDim.x) {
-            R acc[kMvDofs];
-#pragma unroll
-            for (int dd = 0; dd < kMvDofs; dd++) acc[dd] = (R)0;
-            for (int k = 0; k < P; k++) {
-                const R t = T[(size_t)k * P + i];
-                const R *v = sbuf + k * kMvDofs;
-#pragma unroll
-                for (int dd = 0; dd < kMvDofs; dd++)
-                    if (dd < nb) acc[dd] += t * v[dd];
-            }
-#pragma unroll
-            for (int dd = 0; dd < kMvDofs; dd++)
-                if (dd < nb) store(d0 + dd, i, acc[dd]);
-        }
-        __syncthreads();
     }
 }
 
@@ -1123,11 +1141,11 @@ extern "C" int pg_ti_kernel_times(pg_ctx *ctx, int64_t nsteps, int32_t *nkinds, 
         ms_per_launch[1] = ms[1];
         count[0] = n[0];
         count[1] = n[1];
-        bytes_per_launch[0] = 2.0 * arr;  // G1: read q, write F
-        bytes_per_launch[1] = 5.0 * arr;  // G2: read F, q, pi; write q, pi
+        bytes_per_launch[0] = 4.0 * arr;  // k_tc_step: read q, pi; write q, pi
+        bytes_per_launch[1] = 2.0 * arr;  // k_tc_final: read q, write x
         if (names) {
-            names[0] = "k_tc_g1 (positions, estimator, forces; split-BF16 tcgen05 GEMM)";
-            names[1] = "k_tc_g2 (kick, rotation, OU; split-BF16 tcgen05 GEMM)";
+            names[0] = "k_tc_step (one MD step: two split-BF16 tcgen05 GEMMs, forces, OU)";
+            names[1] = "k_tc_final (positions and last estimator; one split-BF16 tcgen05 GEMM)";
         }
         st.step += nsteps;
         int32_t kerr = tc_error(ctx, st);
