@@ -69,6 +69,8 @@ struct TiState {
     double betan = 0.0;
     int64_t step = 0;
     int form = 0;            // resolved PG_FORM_*
+    int tc_blocked = 0;      // tensor form: 0 = fused 64-column tiles (P = 128), 1 = blocked GEMMs (any P)
+    int tc_mb = 1;           // blocked tensor form: 128-row blocks of the zero-padded T
     bool fp32 = false;       // state held in FP32
     DevBuf q, pi, x, f;      // ring state (fused: NM q/pi + Cartesian x; plain: x/p in x/pi)
     DevBuf T;                // P*P FP64 transform (reference values)

@@ -834,59 +834,380 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_step(TcArgs a) {
 
 __global__ void k_tc_step_add(int64_t *step, int64_t n) { *step += n; }
 
-// Host: split-BF16 image of T in the K-major core-matrix layout (B operand, rows = beads).
+// ---------------------------------------------------------------- blocked tensor form (any P <= 512, P % 4 == 0)
+// For many-dof surfaces and bead numbers other than 128, an MD step is three
+// launches:
+//   k_tb_pos:   x = T q + x*                        (blocked split-BF16 GEMM)
+//   k_tb_force: F = grad V(x) per (ring, bead), and the estimator of step s-1
+//               at bead P (FP32 surface, one thread per ring-bead)
+//   k_tb_kick:  T F; kick, half rotation, OU, half rotation of (q, pi)
+// T is zero-padded to Pp = 128 mb rows and columns and stored as mb x mb
+// blocks of 128 x 128.  A CTA owns 64 state columns (ring-dofs, in any ring
+// alignment); its mb accumulators D_i = sum_k T_ik X_k (TMEM columns 64 i ..
+// 64 i + 63) are built block by block: per K block k the FP32 rows X_k (zero
+// beyond P) are split into the B operand, then for each i the block T_ik is
+// bulk-copied in and one 128 x 64 x 128 split-BF16 GEMM is issued and waited for.
+constexpr int kMaxMb = 4;
+
+struct TbArgs {
+    int64_t nrings;
+    int nd, ndim, natom, P, mb;
+    float dt;
+    int64_t imin;
+    const unsigned char *gT;  // mb x mb block image
+    const float *coef;        // natom x P x 8: rA rB rC rD ou_a ou_s
+    const double *mass;
+    const double *avec, *bvec, *dbdl;
+    const int32_t *ringlam;
+    const uint64_t *ringseed;
+    const uint32_t *ringstream;
+    float *q, *pi, *x, *f;    // [ring][dof][P]
+    RingAcc *acc;
+    const int64_t *step0;
+    int64_t sofs;
+    int do_est, do_force;
+    int32_t *err;
+    PesArgs pes;
+};
+
+__device__ __forceinline__ uint32_t tb_tmem_cols(int mb) { return mb == 1 ? 64u : (mb == 2 ? 128u : 256u); }
+
+// Barriers and TMEM for the blocked GEMM; returns the TMEM base.
+__device__ __forceinline__ uint32_t tb_begin(TcShared *sh, int mb) {
+    const int tid = threadIdx.x, warp = tid >> 5;
+    if (tid == 0) {
+        mbar_init(&sh->mma_bar, 1);
+        mbar_init(&sh->tma_bar, 1);
+        sh->err = 0;
+        fence_barrier_init();
+    }
+    __syncthreads();
+    if (warp == 0) {
+        __syncwarp();
+        tmem_alloc(&sh->tmem_slot, tb_tmem_cols(mb));
+    }
+    tc_before();
+    __syncthreads();
+    tc_after();
+    return sh->tmem_slot;
+}
+
+// D_i = sum_k T_ik X_k for the tile whose column c is src[c * P ..].  Returns
+// whether every GEMM completed (CTA-uniform); *phase counts the mbarrier phases
+// used (the parity of the last one is (*phase - 1) & 1).
+__device__ __forceinline__ bool tb_gemm(unsigned char *base, TcShared *sh, const TbArgs &a, const float *src,
+                                        int nvalid, uint32_t tmem, uint32_t *phase) {
+    unsigned char *Xhi = base + 2 * kOpBytes, *Xlo = Xhi + kXPlane;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int P = a.P, mb = a.mb;
+    const int c = 8 * warp + (lane & 7);  // operand row written by this thread
+    const bool v = c < nvalid;
+    const float *row = src + (size_t)(v ? c : 0) * P;
+    for (int kb = 0; kb < mb; kb++) {
+        // X_kb: K = beads 128 kb .. 128 kb + 127 of every column (zero beyond P;
+        // P % 4 == 0, so each float4 is wholly inside or outside a row)
+        float4 w[8];
+#pragma unroll
+        for (int it = 0; it < 4; it++) {
+            const int kg = 128 * kb + 8 * (4 * it + (lane >> 3));
+            const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+            w[2 * it] = (v && kg + 4 <= P) ? __ldg(reinterpret_cast<const float4 *>(row + kg)) : z4;
+            w[2 * it + 1] = (v && kg + 8 <= P) ? __ldg(reinterpret_cast<const float4 *>(row + kg + 4)) : z4;
+        }
+#pragma unroll
+        for (int it = 0; it < 4; it++) {
+            const int kl = 8 * (4 * it + (lane >> 3));
+            const float e8[8] = {w[2 * it].x,     w[2 * it].y,     w[2 * it].z,     w[2 * it].w,
+                                 w[2 * it + 1].x, w[2 * it + 1].y, w[2 * it + 1].z, w[2 * it + 1].w};
+            uint4 hi, lo;
+            split8(e8, hi, lo);
+            const uint32_t off = x_offset(c, kl);
+            *reinterpret_cast<uint4 *>(Xhi + off) = hi;
+            *reinterpret_cast<uint4 *>(Xlo + off) = lo;
+        }
+        fence_async_smem();
+        tc_before();
+        __syncthreads();
+        tc_after();
+        for (int ib = 0; ib < mb; ib++) {
+            const uint32_t par = *phase & 1u;
+            if (tid == 0 && sh->err == 0) {
+                const unsigned char *blk = a.gT + (size_t)(ib * mb + kb) * 2 * kOpBytes;
+                mbar_expect_tx(&sh->tma_bar, 2 * kOpBytes);
+#pragma unroll
+                for (int i = 0; i < 4; i++) bulk_g2s(base + i * 16384, blk + i * 16384, 16384, &sh->tma_bar);
+                if (!mbar_wait(&sh->tma_bar, par)) {
+                    sh->err |= 1;
+                } else {
+                    const uint32_t th = smem_u32(base), tl = th + kOpBytes, xh = smem_u32(Xhi), xl = smem_u32(Xlo);
+                    const uint32_t d = tmem + (uint32_t)(64 * ib);
+#pragma unroll
+                    for (int ks = 0; ks < kP / 16; ks++) {
+                        const uint64_t dth = make_desc(th + (uint32_t)ks * 2 * kLBO),
+                                       dtl = make_desc(tl + (uint32_t)ks * 2 * kLBO);
+                        const uint64_t dxh = make_desc_x(xh + (uint32_t)ks * 2 * kXLbo),
+                                       dxl = make_desc_x(xl + (uint32_t)ks * 2 * kXLbo);
+                        mma_bf16_n64(d, dth, dxh, (kb > 0 || ks > 0) ? 1u : 0u);
+                        mma_bf16_n64(d, dth, dxl, 1u);
+                        mma_bf16_n64(d, dtl, dxh, 1u);
+                    }
+                    mma_commit(&sh->mma_bar);
+                }
+            }
+            *phase += 1;
+            // the GEMM has read T and X before either is overwritten
+            if (!tile_wait(sh, par)) return false;
+        }
+    }
+    return true;
+}
+
+__device__ __forceinline__ void tb_release(TcShared *sh, uint32_t tmem, int mb, int32_t *gerr, uint32_t phase) {
+    const int tid = threadIdx.x, warp = tid >> 5;
+    if (tid == 0 && sh->err) atomicOr(gerr, sh->err);
+    if ((sh->err & 2) && phase > 0) mbar_wait(&sh->mma_bar, (phase - 1) & 1u);  // drain (bounded)
+    tc_before();
+    __syncthreads();
+    if (warp == 0) {
+        __syncwarp();
+        tmem_dealloc(tmem, tb_tmem_cols(mb));
+    }
+}
+
+// Positions x = T q + x* of a 64-column tile.
+__global__ void __launch_bounds__(kTileThreads, 2) k_tb_pos(TbArgs a) {
+    extern __shared__ unsigned char dsm[];
+    unsigned char *base = align1k(dsm);
+    TcShared *sh = reinterpret_cast<TcShared *>(base + kTileSmemOps);
+    TileAux *ax = reinterpret_cast<TileAux *>(base + kTileSmemOps + 256);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int nd = a.nd, P = a.P;
+    const int64_t col0 = (int64_t)blockIdx.x * kNc;
+    const int nvalid = (int)min((int64_t)kNc, a.nrings * nd - col0);
+    if (tid < kNc) {
+        float xa = 0.f, xs = 0.f;
+        if (tid < nvalid) {
+            const int64_t ring = (col0 + tid) / nd;
+            const int j = (int)(col0 + tid - ring * nd);
+            const int lam = a.ringlam[ring];
+            xa = (float)a.avec[j];
+            xs = (float)((a.bvec[(size_t)lam * nd + j] - a.avec[j]) / (double)(P + 1));
+        }
+        ax->xa[tid] = xa;
+        ax->xs[tid] = xs;
+    }
+    const uint32_t tmem = tb_begin(sh, a.mb);
+    uint32_t phase = 0;
+    const bool ok = tb_gemm(base, sh, a, a.q + col0 * P, nvalid, tmem, &phase);
+    if (ok) {
+        const int cb = 32 * (warp >> 2);
+        const int nv = nvalid - cb;
+        for (int ib = 0; ib < a.mb; ib++) {
+            const int m = 128 * ib + 32 * (warp & 3) + lane;  // bead
+            const uint32_t taddr = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(64 * ib + cb);
+            const float fm = (float)(m + 1);
+#pragma unroll 1
+            for (int c0 = 0; c0 < 32; c0 += kGrp) {
+                float xv[kGrp];
+                __syncwarp();
+                tmem_ldn<kGrp>(taddr + (uint32_t)c0, xv);
+                float *xo = a.x + (size_t)(col0 + cb + c0) * P + m;
+#pragma unroll
+                for (int i = 0; i < kGrp; i++)
+                    if (m < P && c0 + i < nv) xo[(size_t)i * P] = xv[i] + ax->xa[cb + c0 + i] + ax->xs[cb + c0 + i] * fm;
+            }
+        }
+    }
+    tb_release(sh, tmem, a.mb, a.err, phase);
+}
+
+// Forces (and the estimator of step s-1 at bead P), one thread per ring-bead.
+__global__ void __launch_bounds__(128) k_tb_force(TbArgs a) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int P = a.P, nd = a.nd;
+    if (t >= a.nrings * P) return;
+    const int64_t ring = t / P;
+    const int bead = (int)(t - ring * P);
+    const size_t off = (size_t)ring * nd * P + bead;
+    float xb[kMaxDof], gb[kMaxDof];
+    for (int j = 0; j < nd; j++) xb[j] = a.x[off + (size_t)j * P];
+    if (a.do_force) {
+        pes_vgrad<float>(a.pes, xb, gb);
+        for (int j = 0; j < nd; j++) a.f[off + (size_t)j * P] = gb[j];
+    }
+    const int64_t s = *a.step0 + a.sofs;
+    if (a.do_est && bead == P - 1 && (s - 1) >= a.imin) {
+        // verletmodule.f90:397-403
+        const int lam = a.ringlam[ring];
+        double contr = 0.0;
+        for (int j = 0; j < nd; j++)
+            contr += a.mass[j / a.ndim] * (-(double)xb[j]) * a.dbdl[(size_t)lam * nd + j];
+        RingAcc *r = &a.acc[ring];
+        if (r->status == 0) r->dhdr_sum += contr;
+        r->nsamples += 1;
+    }
+}
+
+// T F, then kick / half rotation / OU / half rotation of a 64-column tile.
+__global__ void __launch_bounds__(kTileThreads, 2) k_tb_kick(TbArgs a) {
+    extern __shared__ unsigned char dsm[];
+    unsigned char *base = align1k(dsm);
+    TcShared *sh = reinterpret_cast<TcShared *>(base + kTileSmemOps);
+    TileAux *ax = reinterpret_cast<TileAux *>(base + kTileSmemOps + 256);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int nd = a.nd, P = a.P;
+    const int64_t col0 = (int64_t)blockIdx.x * kNc;
+    const int nvalid = (int)min((int64_t)kNc, a.nrings * nd - col0);
+    const int64_t s = *a.step0 + a.sofs;
+    if (tid < kNc) {
+        uint64_t sd = 0;
+        uint32_t sm = 0;
+        if (tid < nvalid) {
+            const int64_t ring = (col0 + tid) / nd;
+            sd = a.ringseed[ring];
+            sm = a.ringstream[ring];
+        }
+        ax->seed[tid] = sd;
+        ax->stream[tid] = sm;
+    }
+    const uint32_t tmem = tb_begin(sh, a.mb);
+    uint32_t phase = 0;
+    const bool ok = tb_gemm(base, sh, a, a.f + col0 * P, nvalid, tmem, &phase);
+    if (ok) {
+        const int cb = 32 * (warp >> 2);
+        const int nv = nvalid - cb;
+        const int e = lane & 3;
+        const float dt = a.dt;
+        uint32_t badbits = 0;
+        for (int ib = 0; ib < a.mb; ib++) {
+            const int m = 128 * ib + 32 * (warp & 3) + lane;  // mode
+            const int mc = m < P ? m : P - 1;
+            const uint32_t taddr = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(64 * ib + cb);
+#pragma unroll 1
+            for (int c0 = 0; c0 < 32; c0 += kGrp) {
+                const int nvg = nv - c0;
+                float *qo = a.q + (size_t)(col0 + cb + c0) * P + m;
+                float *po = a.pi + (size_t)(col0 + cb + c0) * P + m;
+                float gv[kGrp];
+                __syncwarp();
+                tmem_ldn<kGrp>(taddr + (uint32_t)c0, gv);
+#pragma unroll
+                for (int g = 0; g < kGrp / 4; g++) {
+                    // normals j P + 4 (m / 4) .. + 3 of column c0 + 4g + e, transposed within the quad
+                    const int cc = cb + c0 + 4 * g + e;
+                    const int j = (int)((col0 + cc) % nd);
+                    const U4 o = philox_block(ax->seed[cc], ax->stream[cc], (uint32_t)s, kRngLangevin,
+                                              (uint32_t)((j * P + m) >> 2));
+                    float z[4];
+                    box_muller_f(o.x, o.y, z[0], z[1]);
+                    box_muller_f(o.z, o.w, z[2], z[3]);
+                    float rv[4];
+                    rv[0] = sel4(z, e);
+#pragma unroll
+                    for (int r = 1; r < 4; r++) rv[r] = __shfl_xor_sync(0xffffffffu, sel4(z, e ^ r), r);
+#pragma unroll
+                    for (int k = 0; k < 4; k++) {
+                        const int i = 4 * g + k;
+                        if (m < P && i < nvg) {
+                            const int jc = (int)((col0 + cb + c0 + i) % nd);
+                            const float *cf = a.coef + ((size_t)(jc / a.ndim) * P + mc) * 8;
+                            const float4 c4 = __ldg(reinterpret_cast<const float4 *>(cf));
+                            const float2 c2 = __ldg(reinterpret_cast<const float2 *>(cf + 4));
+                            const float zk = sel4(rv, e ^ k);
+                            const float p0 = po[(size_t)i * P] - dt * gv[i];
+                            const float q0 = qo[(size_t)i * P];
+                            float p1 = c4.x * p0 + c4.y * q0;
+                            const float q1 = c4.z * p0 + c4.w * q0;
+                            p1 = c2.x * p1 + c2.y * zk;
+                            const float pn = c4.x * p1 + c4.y * q1;
+                            const float qn = c4.z * p1 + c4.w * q1;
+                            qo[(size_t)i * P] = qn;
+                            po[(size_t)i * P] = pn;
+                            if (pn != pn) badbits |= 1u << (c0 + i);
+                        }
+                    }
+                }
+            }
+        }
+        badbits = __reduce_or_sync(0xffffffffu, badbits);
+        if (lane == 0 && badbits) {
+            for (int i = 0; i < 32; i++)
+                if (badbits & (1u << i)) {
+                    const int64_t ring = (col0 + cb + i) / nd;
+                    if (atomicOr(&a.acc[ring].status, PG_RING_NAN) == 0) a.acc[ring].pad = (int32_t)s;
+                }
+        }
+    }
+    tb_release(sh, tmem, a.mb, a.err, phase);
+}
+
+
+// Host: split-BF16 image of T, zero-padded to mb x mb blocks of 128 x 128
+// (mb = ceil(P / 128)); block (ib, kb) is a 64 KB [hi | lo] pair in the K-major
+// core-matrix layout of the A operand, at (ib mb + kb) 64 KB.
+static int blocks_for(int P) { return (P + kP - 1) / kP; }
+
 static void build_split_image(int P, std::vector<unsigned char> &img) {
     std::vector<double> T;
     build_transmatrix(P, T);
-    img.assign(2 * kOpBytes, 0);
+    const int mb = blocks_for(P);
+    img.assign((size_t)mb * mb * 2 * kOpBytes, 0);
     for (int n = 0; n < P; n++)
         for (int k = 0; k < P; k++) {
             double v = T[(size_t)n + (size_t)P * k];
             __nv_bfloat16 hi = __float2bfloat16_rn((float)v);
             double r = v - (double)__bfloat162float(hi);
             __nv_bfloat16 lo = __float2bfloat16_rn((float)r);
-            uint32_t off = op_offset(n, k);
-            memcpy(&img[off], &hi, 2);
-            memcpy(&img[kOpBytes + off], &lo, 2);
+            const size_t blk = ((size_t)(n / kP) * mb + (size_t)(k / kP)) * 2 * kOpBytes;
+            const uint32_t off = op_offset(n % kP, k % kP);
+            memcpy(&img[blk + off], &hi, 2);
+            memcpy(&img[blk + kOpBytes + off], &lo, 2);
         }
 }
 
 static size_t tc_smem_bytes() { return (size_t)kTileSmemOps + 1024 + 256 + sizeof(TileAux) + 64; }
 
-// Tbf layout: [T image 64 KB | FP32 coefficients | error word | stepB | pad]
-static size_t tbf_coef_off() { return 2 * (size_t)kOpBytes; }
-static size_t tbf_err_off(int natom) { return tbf_coef_off() + (size_t)natom * kP * 8 * sizeof(float); }
+// Tbf layout: [T image mb^2 x 64 KB | FP32 coefficients natom x P x 8 | error word | pad]
+static size_t tbf_coef_off(const TiState &st) { return (size_t)st.tc_mb * st.tc_mb * 2 * kOpBytes; }
+static size_t tbf_err_off(const TiState &st, int natom) {
+    return tbf_coef_off(st) + (size_t)natom * st.P * 8 * sizeof(float);
+}
 
 }  // namespace
 
 int tc_built() { return 1; }
 
+// 0: unsupported; 1: fused 64-column tiles (P = 128, one-atom 1-D or 2-D
+// surface); 2: blocked GEMMs (P <= 512 with P % 4 == 0, any surface).
+// Both: Langevin thermostat, no dHdrlimit re-initialisation.
 int tc_supported(const TiState &st, const pg_ctx &ctx) {
-    if (st.P != kP) return 0;
     if (st.cfg.thermostat != PG_LANGEVIN) return 0;
     if (st.cfg.dhdr_limit >= 0.0) return 0;
-    if (ctx.natom != 1) return 0;  // G2 keeps one atom's mode coefficients in registers
-    if (ctx.pes_id == PG_PES_2DTEST && ctx.nd == 2) return 1;
-    if (ctx.pes_id == PG_PES_1D && ctx.nd == 1) return 1;
+    if (st.P == kP && ctx.natom == 1 &&
+        ((ctx.pes_id == PG_PES_2DTEST && ctx.nd == 2) || (ctx.pes_id == PG_PES_1D && ctx.nd == 1)))
+        return 1;
+    if (st.P % 4 == 0 && st.P <= kMaxMb * kP && ctx.nd <= kMaxDof) return 2;
     return 0;
 }
 
 int tc_prepare(pg_ctx *ctx, TiState &st) {
+    st.tc_mb = blocks_for(st.P);
     std::vector<unsigned char> img;
     build_split_image(st.P, img);
-    size_t ncoef = (size_t)ctx->natom * kP * 8;
-    size_t bytes = tbf_err_off(ctx->natom) + 64;
+    const int P = st.P;
+    size_t ncoef = (size_t)ctx->natom * P * 8;
+    size_t bytes = tbf_err_off(st, ctx->natom) + 64;
     cudaError_t e = st.Tbf.ensure(bytes);
     if (e != cudaSuccess) return cuda_fail(e, "tensor-core tables");
-    std::vector<ModeCoef> mc((size_t)ctx->natom * st.P);
+    std::vector<ModeCoef> mc((size_t)ctx->natom * P);
     PG_CUDA(cudaMemcpyAsync(mc.data(), st.coef.ptr, mc.size() * sizeof(ModeCoef), cudaMemcpyDeviceToHost,
                             ctx->stream));
     PG_CUDA(cudaStreamSynchronize(ctx->stream));
     std::vector<float> cf(ncoef, 0.f);
     for (int at = 0; at < ctx->natom; at++)
-        for (int k = 0; k < kP; k++) {
+        for (int k = 0; k < P; k++) {
             const ModeCoef &c = mc[(size_t)at + (size_t)ctx->natom * k];
-            float *o = &cf[((size_t)at * kP + k) * 8];
+            float *o = &cf[((size_t)at * P + k) * 8];
             o[0] = (float)c.rA;
             o[1] = (float)c.rB;
             o[2] = (float)c.rC;
@@ -896,21 +1217,23 @@ int tc_prepare(pg_ctx *ctx, TiState &st) {
         }
     unsigned char *d = st.Tbf.as<unsigned char>();
     PG_CUDA(cudaMemcpyAsync(d, img.data(), img.size(), cudaMemcpyHostToDevice, ctx->stream));
-    PG_CUDA(cudaMemcpyAsync(d + tbf_coef_off(), cf.data(), cf.size() * sizeof(float), cudaMemcpyHostToDevice,
+    PG_CUDA(cudaMemcpyAsync(d + tbf_coef_off(st), cf.data(), cf.size() * sizeof(float), cudaMemcpyHostToDevice,
                             ctx->stream));
-    PG_CUDA(cudaMemsetAsync(d + tbf_err_off(ctx->natom), 0, 64, ctx->stream));
+    PG_CUDA(cudaMemsetAsync(d + tbf_err_off(st, ctx->natom), 0, 64, ctx->stream));
     PG_CUDA(cudaStreamSynchronize(ctx->stream));
     size_t sm = tc_smem_bytes();
     PG_CUDA(cudaFuncSetAttribute(k_tc_step<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     PG_CUDA(cudaFuncSetAttribute(k_tc_step<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     PG_CUDA(cudaFuncSetAttribute(k_tc_final, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    PG_CUDA(cudaFuncSetAttribute(k_tb_pos, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    PG_CUDA(cudaFuncSetAttribute(k_tb_kick, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     return PG_OK;
 }
 
 int32_t tc_error(pg_ctx *ctx, TiState &st) {
     const unsigned char *d = st.Tbf.as<unsigned char>();
     int32_t e = 0;
-    if (cudaMemcpyAsync(&e, d + tbf_err_off(ctx->natom), sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream) !=
+    if (cudaMemcpyAsync(&e, d + tbf_err_off(st, ctx->natom), sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream) !=
         cudaSuccess)
         return -1;
     if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return -1;
@@ -927,8 +1250,8 @@ static void tc_make_args(pg_ctx *ctx, TiState &st, TcArgs &a, int &pesk) {
     a.imin = st.cfg.imin;
     unsigned char *d = st.Tbf.as<unsigned char>();
     a.gT = d;
-    a.coef = reinterpret_cast<const float *>(d + tbf_coef_off());
-    a.err = reinterpret_cast<int32_t *>(d + tbf_err_off(ctx->natom));
+    a.coef = reinterpret_cast<const float *>(d + tbf_coef_off(st));
+    a.err = reinterpret_cast<int32_t *>(d + tbf_err_off(st, ctx->natom));
     a.step0 = reinterpret_cast<const int64_t *>(st.red.as<double>() + 3 * st.nlambda);
     a.mass = ctx->d_mass.as<double>();
     a.avec = st.avec.as<double>();
@@ -992,8 +1315,75 @@ static int tc_launch_final(pg_ctx *ctx, TiState &st, int64_t n, cudaStream_t s) 
     return e == cudaSuccess ? PG_OK : cuda_fail(e, "step counter launch");
 }
 
+static void tb_make_args(pg_ctx *ctx, TiState &st, TbArgs &a) {
+    memset(&a, 0, sizeof(a));
+    a.nrings = st.nrings;
+    a.nd = st.nd;
+    a.ndim = ctx->ndim;
+    a.natom = ctx->natom;
+    a.P = st.P;
+    a.mb = st.tc_mb;
+    a.dt = (float)st.cfg.dt;
+    a.imin = st.cfg.imin;
+    unsigned char *d = st.Tbf.as<unsigned char>();
+    a.gT = d;
+    a.coef = reinterpret_cast<const float *>(d + tbf_coef_off(st));
+    a.err = reinterpret_cast<int32_t *>(d + tbf_err_off(st, ctx->natom));
+    a.step0 = reinterpret_cast<const int64_t *>(st.red.as<double>() + 3 * st.nlambda);
+    a.mass = ctx->d_mass.as<double>();
+    a.avec = st.avec.as<double>();
+    a.bvec = st.bvec.as<double>();
+    a.dbdl = st.dbdl.as<double>();
+    a.ringlam = st.ringlam.as<int32_t>();
+    a.ringseed = st.ringseed.as<uint64_t>();
+    a.ringstream = st.ringstream.as<uint32_t>();
+    a.q = st.q.as<float>();
+    a.pi = st.pi.as<float>();
+    a.x = st.x.as<float>();
+    a.f = st.f.as<float>();
+    a.acc = st.acc.as<RingAcc>();
+    a.pes = ctx->pes_args();
+}
+
+// Blocked form: kernel k (0 positions, 1 forces / estimator, 2 kick) of step
+// offset i; final = the positions and estimator pass after the last step.
+static int tb_launch_kernel(pg_ctx *ctx, TiState &st, int k, int64_t i, bool final_pass, cudaStream_t s) {
+    TbArgs a;
+    tb_make_args(ctx, st, a);
+    a.sofs = i;
+    a.do_est = i > 0 ? 1 : 0;
+    a.do_force = final_pass ? 0 : 1;
+    const unsigned grid = (unsigned)((st.nrings * st.nd + kNc - 1) / kNc);
+    if (k == 0)
+        k_tb_pos<<<grid, kTileThreads, tc_smem_bytes(), s>>>(a);
+    else if (k == 1)
+        k_tb_force<<<(unsigned)((st.nrings * st.P + 127) / 128), 128, 0, s>>>(a);
+    else
+        k_tb_kick<<<grid, kTileThreads, tc_smem_bytes(), s>>>(a);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? PG_OK : cuda_fail(e, "blocked tensor-form launch");
+}
+
+static int tb_launch(pg_ctx *ctx, TiState &st, int64_t nsteps, cudaStream_t s) {
+    for (int64_t i = 0; i < nsteps; i++)
+        for (int k = 0; k < 3; k++) {
+            int rc = tb_launch_kernel(ctx, st, k, i, false, s);
+            if (rc) return rc;
+        }
+    for (int k = 0; k < 2; k++) {
+        int rc = tb_launch_kernel(ctx, st, k, nsteps, true, s);
+        if (rc) return rc;
+    }
+    TbArgs a;
+    tb_make_args(ctx, st, a);
+    k_tc_step_add<<<1, 1, 0, s>>>(const_cast<int64_t *>(a.step0), nsteps);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? PG_OK : cuda_fail(e, "step counter launch");
+}
+
 int tc_launch(pg_ctx *ctx, TiState &st, int64_t, int64_t nsteps, cudaStream_t s) {
     if (nsteps < 0) return PG_OK;  // the HBM copy of the state is current after every advance
+    if (st.tc_blocked) return tb_launch(ctx, st, nsteps, s);
     for (int64_t i = 0; i < nsteps; i++) {
         int rc = tc_launch_step(ctx, st, i, s);
         if (rc) return rc;
@@ -1003,7 +1393,44 @@ int tc_launch(pg_ctx *ctx, TiState &st, int64_t, int64_t nsteps, cudaStream_t s)
 
 // Per-kernel event timing of nsteps steps (direct launches, no graph):
 // ms[0] = k_tc_step, ms[1] = k_tc_final.
+// Blocked form: ms[0..2] = k_tb_pos, k_tb_force, k_tb_kick per launch over nsteps steps.
+static int tb_kernel_times(pg_ctx *ctx, TiState &st, int64_t nsteps, double *ms, int64_t *count) {
+    cudaStream_t s = ctx->stream;
+    std::vector<cudaEvent_t> ev(3 * nsteps + 1);
+    for (auto &e : ev) PG_CUDA(cudaEventCreate(&e));
+    PG_CUDA(cudaEventRecord(ev[0], s));
+    for (int64_t i = 0; i < nsteps; i++)
+        for (int k = 0; k < 3; k++) {
+            int rc = tb_launch_kernel(ctx, st, k, i, false, s);
+            if (rc) return rc;
+            PG_CUDA(cudaEventRecord(ev[3 * i + k + 1], s));
+        }
+    for (int k = 0; k < 2; k++) {
+        int rc = tb_launch_kernel(ctx, st, k, nsteps, true, s);
+        if (rc) return rc;
+    }
+    TbArgs a;
+    tb_make_args(ctx, st, a);
+    k_tc_step_add<<<1, 1, 0, s>>>(const_cast<int64_t *>(a.step0), nsteps);
+    PG_CUDA(cudaGetLastError());
+    PG_CUDA(cudaStreamSynchronize(s));
+    double t[3] = {0.0, 0.0, 0.0};
+    for (int64_t i = 0; i < nsteps; i++)
+        for (int k = 0; k < 3; k++) {
+            float v = 0.f;
+            PG_CUDA(cudaEventElapsedTime(&v, ev[3 * i + k], ev[3 * i + k + 1]));
+            t[k] += v;
+        }
+    for (auto &e : ev) cudaEventDestroy(e);
+    for (int k = 0; k < 3; k++) {
+        ms[k] = t[k] / (double)nsteps;
+        count[k] = nsteps;
+    }
+    return PG_OK;
+}
+
 int tc_kernel_times(pg_ctx *ctx, TiState &st, int64_t nsteps, double *ms, int64_t *count) {
+    if (st.tc_blocked) return tb_kernel_times(ctx, st, nsteps, ms, count);
     cudaStream_t s = ctx->stream;
     std::vector<cudaEvent_t> ev(nsteps + 3);
     for (auto &e : ev) PG_CUDA(cudaEventCreate(&e));

@@ -781,12 +781,16 @@ static int resolve_form(pg_ctx *ctx, TiState &st) {
         st.form = PG_FORM_FUSED;
         return PG_OK;
     }
-    bool tc = tc_supported(st, *ctx) != 0;
-    if (form == PG_FORM_TENSOR && !tc)
+    const int tcv = tc_supported(st, *ctx);
+    if (form == PG_FORM_TENSOR && !tcv)
         return fail(PG_ERR_UNSUPPORTED,
-                    "the tensor-core form supports P = 128, ndof <= 4, Langevin, exact rotation, "
-                    "no dHdrlimit");
-    st.form = tc ? PG_FORM_TENSOR : PG_FORM_FUSED;
+                    "the tensor-core form supports the Langevin thermostat without dHdrlimit, and P <= 512 "
+                    "with P % 4 == 0");
+    // AUTO: the fused tiles whenever they apply; the blocked GEMMs for batches of at
+    // least 2^20 bead-dofs (smaller batches leave most of the GPU idle in them).
+    bool use = tcv == 1 || (tcv == 2 && (form == PG_FORM_TENSOR || st.nrings * st.nd * st.P >= (1 << 20)));
+    st.form = use ? PG_FORM_TENSOR : PG_FORM_FUSED;
+    st.tc_blocked = (use && tcv == 2) ? 1 : 0;
     return PG_OK;
 }
 
@@ -1134,18 +1138,38 @@ extern "C" int pg_ti_kernel_times(pg_ctx *ctx, int64_t nsteps, int32_t *nkinds, 
     if (st.form == PG_FORM_TENSOR) {
         double ms[2];
         int64_t n[2];
-        rc = tc_kernel_times(ctx, st, nsteps, ms, n);
-        if (rc) return rc;
-        *nkinds = 2;
-        ms_per_launch[0] = ms[0];
-        ms_per_launch[1] = ms[1];
-        count[0] = n[0];
-        count[1] = n[1];
-        bytes_per_launch[0] = 4.0 * arr;  // k_tc_step: read q, pi; write q, pi
-        bytes_per_launch[1] = 2.0 * arr;  // k_tc_final: read q, write x
-        if (names) {
-            names[0] = "k_tc_step (one MD step: two split-BF16 tcgen05 GEMMs, forces, OU)";
-            names[1] = "k_tc_final (positions and last estimator; one split-BF16 tcgen05 GEMM)";
+        if (st.tc_blocked) {
+            double ms3[3];
+            int64_t n3[3];
+            rc = tc_kernel_times(ctx, st, nsteps, ms3, n3);
+            if (rc) return rc;
+            *nkinds = 3;
+            for (int k = 0; k < 3; k++) {
+                ms_per_launch[k] = ms3[k];
+                count[k] = n3[k];
+            }
+            bytes_per_launch[0] = 2.0 * arr;  // k_tb_pos: read q, write x
+            bytes_per_launch[1] = 2.0 * arr;  // k_tb_force: read x, write F
+            bytes_per_launch[2] = 5.0 * arr;  // k_tb_kick: read F, q, pi; write q, pi
+            if (names) {
+                names[0] = "k_tb_pos (positions: blocked split-BF16 tcgen05 GEMM)";
+                names[1] = "k_tb_force (FP32 surface forces and estimator, SIMT)";
+                names[2] = "k_tb_kick (T F: blocked split-BF16 tcgen05 GEMM; kick, rotation, OU)";
+            }
+        } else {
+            rc = tc_kernel_times(ctx, st, nsteps, ms, n);
+            if (rc) return rc;
+            *nkinds = 2;
+            ms_per_launch[0] = ms[0];
+            ms_per_launch[1] = ms[1];
+            count[0] = n[0];
+            count[1] = n[1];
+            bytes_per_launch[0] = 4.0 * arr;  // k_tc_step: read q, pi; write q, pi
+            bytes_per_launch[1] = 2.0 * arr;  // k_tc_final: read q, write x
+            if (names) {
+                names[0] = "k_tc_step (one MD step: two split-BF16 tcgen05 GEMMs, forces, OU)";
+                names[1] = "k_tc_final (positions and last estimator; one split-BF16 tcgen05 GEMM)";
+            }
         }
         st.step += nsteps;
         int32_t kerr = tc_error(ctx, st);
@@ -1171,8 +1195,10 @@ extern "C" int pg_ti_get_form(pg_ctx *ctx, int64_t nsteps, int32_t *form, int64_
     TiState &st = *ctx->ti;
     if (form) *form = st.form;
     if (launches) {
-        if (st.form == PG_FORM_TENSOR)
-            *launches = nsteps > 0 ? 2 * nsteps + 1 : 0;  // G1 + G2 per step, final G1
+        if (st.form == PG_FORM_TENSOR && st.tc_blocked)
+            *launches = nsteps > 0 ? 3 * nsteps + 3 : 0;  // pos, force, kick per step; pos, estimator, counter
+        else if (st.form == PG_FORM_TENSOR)
+            *launches = nsteps > 0 ? nsteps + 2 : 0;  // one step kernel per step; final pass, counter
         else if (st.form == PG_FORM_FUSED)
             *launches = nsteps > 0 ? 2 : 0;  // fused kernel + step counter
         else

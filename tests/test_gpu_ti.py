@@ -184,12 +184,13 @@ def test_dhdr_limit_reinit_matches_oracle(ctx, pg, oracle):
     np.testing.assert_allclose(s, so, rtol=1e-9, atol=1e-9)
 
 
-@pytest.mark.parametrize("form", ["fused64", "plain", "mixed"])
+@pytest.mark.parametrize("form", ["fused64", "plain", "mixed", "tensor_tile", "tensor_blocked"])
 def test_chunked_advance_and_checkpoint_are_bitwise(ctx, pg, tmp_path, form):
-    c, ti = _small_2d(P=32)
+    c, ti = _small_2d(P=128 if form == "tensor_tile" else 32)
     _set_system(ctx, c)
-    prec = pg.PG_MIXED if form == "mixed" else pg.PG_FP64
-    fm = {"fused64": pg.PG_FORM_FUSED, "plain": pg.PG_FORM_PLAIN, "mixed": pg.PG_FORM_AUTO}[form]
+    prec = pg.PG_FP64 if form in ("fused64", "plain") else pg.PG_MIXED
+    fm = {"fused64": pg.PG_FORM_FUSED, "plain": pg.PG_FORM_PLAIN, "mixed": pg.PG_FORM_AUTO,
+          "tensor_tile": pg.PG_FORM_TENSOR, "tensor_blocked": pg.PG_FORM_TENSOR}[form]
     cfg = _gpu_cfg(pg, c, ti, prec, fm)
     ctx.ti_setup(cfg, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
     ctx.ti_advance(70)
@@ -376,3 +377,36 @@ def test_advance_group_equals_separate_advances(pg):
         assert step_a == step_b == 40
         for u, v in zip(st_a + res_a, st_b + res_b):
             np.testing.assert_array_equal(u, v)
+
+
+def _tensor_vs_simt(ctx, pg, c, ti, nsteps=20):
+    _set_system(ctx, c)
+    x1, p1, s1, n1, st1 = _run(ctx, pg, c, ti, pg.PG_MIXED, pg.PG_FORM_FUSED, nsteps)
+    x2, p2, s2, n2, st2 = _run(ctx, pg, c, ti, pg.PG_MIXED, pg.PG_FORM_TENSOR, nsteps)
+    assert ctx.ti_form(1)[0] == pg.PG_FORM_TENSOR
+    assert np.all(st1 == 0) and np.all(st2 == 0)
+    np.testing.assert_array_equal(n1, n2)
+    return x1, p1, s1, x2, p2, s2
+
+
+@pytest.mark.parametrize("P,nrep", [(256, 3), (384, 2)])
+def test_tensor_blocked_many_dofs_tracks_simt(ctx, pg, P, nrep):
+    """Blocked split-BF16 GEMMs (P = 256: 2 x 2 blocks of T; P = 384: 3 x 3, 192 TMEM
+    columns) on the 27-dof surface, 6 or 4 rings = 162 or 108 columns (a partial
+    64-column tile), against the FP32 SIMT form from the same state."""
+    c = dict(pgconfigs.load("c2"))
+    c["P"] = P
+    ti = pgconfigs.TiInputs(c, nrep=nrep, nintegral=2)
+    x1, p1, s1, x2, p2, s2 = _tensor_vs_simt(ctx, pg, c, ti)
+    assert np.max(np.abs(x1 - x2)) < 2e-3
+    assert np.max(np.abs(p1 - p2)) < 2e-3 * np.max(np.abs(p1))
+    np.testing.assert_allclose(s2, s1, rtol=2e-4)
+
+
+def test_tensor_blocked_padded_small_p(ctx, pg):
+    """P = 32 on the 1-D surface: T zero-padded into one 128 x 128 block."""
+    c = dict(pgconfigs.load("c0"))
+    ti = pgconfigs.TiInputs(c, nrep=5, nintegral=3)
+    x1, p1, s1, x2, p2, s2 = _tensor_vs_simt(ctx, pg, c, ti)
+    assert np.max(np.abs(x1 - x2)) < 2e-3
+    np.testing.assert_allclose(s2, s1, rtol=2e-4)

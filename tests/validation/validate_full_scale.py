@@ -80,21 +80,25 @@ def part_c2(out, nmc=2000):
     import pgconfigs
     import pimdgpu as pg
     c = pgconfigs.load("c2")
-    mixed = drivers.run_ti(c, precision=pg.PG_MIXED, form=pg.PG_FORM_FUSED, nmc=nmc, chunk=500)
+    mixed = drivers.run_ti(c, precision=pg.PG_MIXED, form=pg.PG_FORM_AUTO, nmc=nmc, chunk=500)
+    simt = drivers.run_ti(c, precision=pg.PG_MIXED, form=pg.PG_FORM_FUSED, nmc=nmc, chunk=500)
     fp64 = drivers.run_ti(c, precision=pg.PG_FP64, form=pg.PG_FORM_FUSED, nmc=nmc, chunk=250)
-    out["c2"] = dict(mixed=mixed, fp64=fp64, ln_qratio_diff=mixed["ln_qratio"] - fp64["ln_qratio"],
+    out["c2"] = dict(mixed=mixed, mixed_simt=simt, fp64=fp64, ln_qratio_diff=mixed["ln_qratio"] - fp64["ln_qratio"],
+                     ln_qratio_diff_simt=simt["ln_qratio"] - fp64["ln_qratio"],
                      ln_qratio_stderr=fp64["ln_qratio_stderr"])
 
 
 def part_c4(out, nmc=None):
     """18-atom surface, 4096 rings with P in {64, 128, 256, 512}: one context
-    per P, advanced together; FP32 mixed precision and, on a shorter run, FP64."""
+    per P, advanced together; mixed precision on the tensor-core form (AUTO) and
+    on the SIMT form."""
     import drivers
     import pgconfigs
     import pimdgpu as pg
     c = pgconfigs.load("c4")
     mixed = drivers.run_ti_mixed(c, precision=pg.PG_MIXED, nmc=nmc, chunk=500)
-    out["c4"] = dict(mixed=mixed)
+    simt = drivers.run_ti_mixed(c, precision=pg.PG_MIXED, form=pg.PG_FORM_FUSED, nmc=nmc, chunk=500)
+    out["c4"] = dict(mixed=mixed, mixed_simt=simt)
 
 
 def part_c3(out, factr=1e2, pgtol=1e-8):
