@@ -206,6 +206,25 @@ extern "C" int pg_set_system(pg_ctx *ctx, int64_t ndim, int64_t natom, const dou
     if (nparams > 0)
         PG_CUDA(cudaMemcpyAsync(ctx->d_params.ptr, ctx->params.data(), sizeof(double) * nparams,
                                 cudaMemcpyHostToDevice, ctx->stream));
+    {
+        // FP32 copy for the FP32 surfaces; the 2-D surface's well centres follow
+        // (FP64 cos / sin as in mcmod_2dtest.f90:16-24, rounded once)
+        std::vector<float> fp(params, params + nparams);
+        if (pes_id == PG_PES_2DTEST) {
+            int m = nparams >= 4 ? (int)params[0] : 6;
+            double rho0 = nparams >= 4 ? params[3] : 3.0;
+            for (int k = 0; k < 6; k++) {
+                bool in = k < m;
+                fp.push_back(in ? (float)(rho0 * std::cos((double)(k + 1) * 2.0 * kPiRef / (double)m)) : 0.f);
+                fp.push_back(in ? (float)(rho0 * std::sin((double)(k + 1) * 2.0 * kPiRef / (double)m)) : 0.f);
+            }
+        }
+        ctx->fparams = fp;
+        PG_CUDA(ctx->d_fparams.ensure(sizeof(float) * (fp.size() > 0 ? fp.size() : 1)));
+        if (!fp.empty())
+            PG_CUDA(cudaMemcpyAsync(ctx->d_fparams.ptr, ctx->fparams.data(), sizeof(float) * fp.size(),
+                                    cudaMemcpyHostToDevice, ctx->stream));
+    }
     PG_CUDA(ctx->d_mass.ensure(sizeof(double) * natom));
     PG_CUDA(cudaMemcpyAsync(ctx->d_mass.ptr, ctx->mass.data(), sizeof(double) * natom, cudaMemcpyHostToDevice,
                             ctx->stream));

@@ -171,15 +171,27 @@ struct PesArgs {
     int id, ndim, natom, nd, nparams;
     double V0;
     const double *params;  // device (or shared) pointer
+    // FP32 copy of params (device or shared), read by the FP32 surfaces so that
+    // no FP64 conversion runs per evaluation; for the 2-D surface it is followed
+    // by the 12 well-centre coordinates (x1, y1, ..., x6, y6), rounded from FP64.
+    const float *fparams;
 };
+
+// Number of extra FP32 values that follow the parameters in fparams.
+__host__ __device__ __forceinline__ int pes_fparams_extra(int id) { return id == 2 ? 12 : 0; }
+
+// Parameter vector of the surface in the arithmetic type R.
+template <typename R> __device__ __forceinline__ const R *pes_params(const PesArgs &pa);
+template <> __device__ __forceinline__ const double *pes_params<double>(const PesArgs &pa) { return pa.params; }
+template <> __device__ __forceinline__ const float *pes_params<float>(const PesArgs &pa) { return pa.fparams; }
 
 // mcmod_1d.f90:14-35.  No V0 (the reference module does not subtract it).
 template <typename R>
 __device__ __forceinline__ R pes_1d(const PesArgs &pa, const R *x, R *g) {
     R H = (R)1.0, x0 = (R)1.0;
     if (pa.nparams >= 2) {
-        H = (R)pa.params[0];
-        x0 = (R)pa.params[1];
+        H = pes_params<R>(pa)[0];
+        x0 = pes_params<R>(pa)[1];
     }
     R v = 0;
     for (int i = 0; i < pa.nd; i++) {
@@ -252,7 +264,7 @@ __device__ __forceinline__ float pes_2d_f(const PesArgs &pa, const float *wc, in
 
 template <typename R>
 __device__ __forceinline__ R pes_harm(const PesArgs &pa, const R *x, R *g) {
-    R k = pa.nparams >= 1 ? (R)pa.params[0] : (R)1.0;
+    R k = pa.nparams >= 1 ? pes_params<R>(pa)[0] : (R)1.0;
     R v = 0;
     for (int i = 0; i < pa.nd; i++) {
         v += (R)0.5 * k * x[i] * x[i];
@@ -261,9 +273,15 @@ __device__ __forceinline__ R pes_harm(const PesArgs &pa, const R *x, R *g) {
     return v - (R)pa.V0;
 }
 
+// Square root and division in the surfaces: the IEEE operations of the CPU
+// restatement in FP64; in FP32 the hardware approximations (rsqrt, fast
+// divide: relative error ~1e-7, below the rounding of the FP32 state).
 template <typename R> __device__ __forceinline__ R my_sqrt(R v);
 template <> __device__ __forceinline__ double my_sqrt<double>(double v) { return sqrt(v); }
-template <> __device__ __forceinline__ float my_sqrt<float>(float v) { return sqrtf(v); }
+template <> __device__ __forceinline__ float my_sqrt<float>(float v) { return v > 0.f ? v * rsqrtf(v) : 0.f; }
+template <typename R> __device__ __forceinline__ R pdiv(R a, R b);
+template <> __device__ __forceinline__ double pdiv<double>(double a, double b) { return a / b; }
+template <> __device__ __forceinline__ float pdiv<float>(float a, float b) { return __fdividef(a, b); }
 template <typename R> __device__ __forceinline__ R my_exp(R v);
 template <> __device__ __forceinline__ double my_exp<double>(double v) { return exp(v); }
 template <> __device__ __forceinline__ float my_exp<float>(float v) { return __expf(v); }
@@ -276,13 +294,13 @@ template <> __device__ __forceinline__ float my_acos<float>(float v) { return ac
 // distance is recomputed, dV/dr is scattered through dr/dx (Wilson B row).
 template <typename R>
 __device__ __forceinline__ R pes_synth9(const PesArgs &pa, const R *x, R *g) {
-    const double *pp = pa.params;
+    const R *pp = pes_params<R>(pa);
     int npair = (int)pp[0];
     if (g)
         for (int i = 0; i < pa.nd; i++) g[i] = 0;
     R v = 0;
     for (int q = 0; q < npair; q++) {
-        const double *r = pp + 1 + 5 * q;
+        const R *r = pp + 1 + 5 * q;
         int i = (int)r[0], j = (int)r[1];
         R D = (R)r[2], a = (R)r[3], r0 = (R)r[4];
         R d0 = x[3 * i] - x[3 * j], d1 = x[3 * i + 1] - x[3 * j + 1], d2 = x[3 * i + 2] - x[3 * j + 2];
@@ -291,7 +309,7 @@ __device__ __forceinline__ R pes_synth9(const PesArgs &pa, const R *x, R *g) {
         R om = (R)1.0 - e;
         v += D * om * om;
         if (g) {
-            R dvdr = (R)2.0 * D * a * om * e / rr;
+            R dvdr = pdiv<R>((R)2.0 * D * a * om * e, rr);
             g[3 * i] += dvdr * d0;
             g[3 * i + 1] += dvdr * d1;
             g[3 * i + 2] += dvdr * d2;
@@ -300,7 +318,7 @@ __device__ __forceinline__ R pes_synth9(const PesArgs &pa, const R *x, R *g) {
             g[3 * j + 2] -= dvdr * d2;
         }
     }
-    const double *w = pp + 1 + 5 * npair;
+    const R *w = pp + 1 + 5 * npair;
     int iH = (int)w[0], iO1 = (int)w[1], iO2 = (int)w[2];
     R B = (R)w[3], s0 = (R)w[4];
     R e1[3], e2[3], r1 = 0, r2 = 0;
@@ -331,7 +349,7 @@ __device__ __forceinline__ R pes_synth9(const PesArgs &pa, const R *x, R *g) {
 // Lennard-Jones, intermolecular point charges).
 template <typename R>
 __device__ __forceinline__ R pes_synth18(const PesArgs &pa, const R *x, R *g) {
-    const double *pp = pa.params;
+    const R *pp = pes_params<R>(pa);
     int nmol = (int)pp[0];
     R kr = (R)pp[1], re = (R)pp[2], kth = (R)pp[3], the = (R)pp[4], eps = (R)pp[5], sig = (R)pp[6];
     R qO = (R)pp[7], qH = (R)pp[8];
@@ -349,7 +367,7 @@ __device__ __forceinline__ R pes_synth18(const PesArgs &pa, const R *x, R *g) {
         }
         r1 = my_sqrt<R>(r1);
         r2 = my_sqrt<R>(r2);
-        R ct = (u1[0] * u2[0] + u1[1] * u2[1] + u1[2] * u2[2]) / (r1 * r2);
+        R ct = pdiv<R>(u1[0] * u2[0] + u1[1] * u2[1] + u1[2] * u2[2], r1 * r2);
         ct = ct > (R)1.0 ? (R)1.0 : (ct < (R)-1.0 ? (R)-1.0 : ct);
         R th = my_acos<R>(ct);
         v += (R)0.5 * kr * ((r1 - re) * (r1 - re) + (r2 - re) * (r2 - re));
@@ -359,10 +377,10 @@ __device__ __forceinline__ R pes_synth18(const PesArgs &pa, const R *x, R *g) {
             if (st < (R)1e-12) st = (R)1e-12;
             R dth = kth * (th - the);
             for (int c = 0; c < 3; c++) {
-                R n1 = u1[c] / r1, n2 = u2[c] / r2;
+                R n1 = pdiv<R>(u1[c], r1), n2 = pdiv<R>(u2[c], r2);
                 R gb1 = kr * (r1 - re) * n1, gb2 = kr * (r2 - re) * n2;
-                R ga1 = -dth * (n2 - ct * n1) / (r1 * st);
-                R ga2 = -dth * (n1 - ct * n2) / (r2 * st);
+                R ga1 = pdiv<R>(-dth * (n2 - ct * n1), r1 * st);
+                R ga2 = pdiv<R>(-dth * (n1 - ct * n2), r2 * st);
                 g[9 * m + 3 + c] += gb1 + ga1;
                 g[9 * m + 6 + c] += gb2 + ga2;
                 g[9 * m + c] -= gb1 + ga1 + gb2 + ga2;
@@ -378,14 +396,14 @@ __device__ __forceinline__ R pes_synth18(const PesArgs &pa, const R *x, R *g) {
                     R r2 = d0 * d0 + d1 * d1 + d2 * d2;
                     R r = my_sqrt<R>(r2);
                     R qa = ia == 0 ? qO : qH, qb = ib == 0 ? qO : qH;
-                    R e = qa * qb / r;
-                    R dvr = -e / r2;
+                    R e = pdiv<R>(qa * qb, r);
+                    R dvr = pdiv<R>(-e, r2);
                     if (ia == 0 && ib == 0) {
-                        R sr2 = sig * sig / r2;
+                        R sr2 = pdiv<R>(sig * sig, r2);
                         R sr6 = sr2 * sr2 * sr2;
                         R sr12 = sr6 * sr6;
                         e += (R)4.0 * eps * (sr12 - sr6);
-                        dvr += (R)4.0 * eps * ((R)-12.0 * sr12 + (R)6.0 * sr6) / r2;
+                        dvr += pdiv<R>((R)4.0 * eps * ((R)-12.0 * sr12 + (R)6.0 * sr6), r2);
                     }
                     v += e;
                     if (g) {
@@ -422,21 +440,15 @@ __device__ __forceinline__ float pes_vgrad<float>(const PesArgs &pa, const float
     switch (pa.id) {
     case kPes1D: return pes_1d<float>(pa, x, g);
     case kPes2D: {
-        float wc[12];
         int m = 6;
-        float a0 = 2.f, b0 = 0.2f, rho0 = 3.f;
+        float a0 = 2.f, b0 = 0.2f;
         if (pa.nparams >= 4) {
-            m = (int)pa.params[0];
-            a0 = (float)pa.params[1];
-            b0 = (float)pa.params[2];
-            rho0 = (float)pa.params[3];
+            m = (int)pa.fparams[0];
+            a0 = pa.fparams[1];
+            b0 = pa.fparams[2];
         }
         if (m > 6) m = 6;
-        for (int k = 0; k < m; k++) {
-            wc[2 * k] = (float)(rho0 * cos((double)(k + 1) * 2.0 * kPiRef / (double)m));
-            wc[2 * k + 1] = (float)(rho0 * sin((double)(k + 1) * 2.0 * kPiRef / (double)m));
-        }
-        return pes_2d_f(pa, wc, m, a0, b0, a0 == 10.f * b0, x, g);
+        return pes_2d_f(pa, pa.fparams + pa.nparams, m, a0, b0, a0 == 10.f * b0, x, g);
     }
     case kPesSynth9: return pes_synth9<float>(pa, x, g);
     case kPesSynth18: return pes_synth18<float>(pa, x, g);

@@ -99,7 +99,8 @@ struct pg_ctx {
     int ndim = 0, natom = 0, nd = 0, pes_id = 0;
     double V0 = 0.0;
     std::vector<double> mass, params;
-    pg::DevBuf d_params, d_mass;
+    std::vector<float> fparams;  // host copy of the FP32 surface parameters (PesArgs::fparams)
+    pg::DevBuf d_params, d_fparams, d_mass;
     pg::DevBuf scratch_a, scratch_b, scratch_c, scratch_d;
     pg::TiState *ti = nullptr;
     pg::PesArgs pes_args() const {
@@ -111,6 +112,7 @@ struct pg_ctx {
         pa.nparams = (int)params.size();
         pa.V0 = V0;
         pa.params = d_params.as<double>();
+        pa.fparams = d_fparams.as<float>();
         return pa;
     }
 };

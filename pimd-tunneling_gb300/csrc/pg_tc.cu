@@ -1022,18 +1022,37 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tb_pos(TbArgs a) {
 }
 
 // Forces (and the estimator of step s-1 at bead P), one thread per ring-bead.
-__global__ void __launch_bounds__(128) k_tb_force(TbArgs a) {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+// The surface indexes a bead's coordinates by atom numbers read from its
+// parameter table, so each thread keeps its coordinates and gradient in shared
+// memory (row stride nd | 1, odd: conflict-free) and the table is staged there
+// too, instead of thread-local arrays and global reads.
+constexpr int kForceThreads = 128;
+__host__ __device__ __forceinline__ int force_stride(int nd) { return nd | 1; }
+static size_t tb_force_smem(int nd, int nfparams) {
+    return ((size_t)nfparams * sizeof(float) + 15) / 16 * 16 + 2 * (size_t)kForceThreads * force_stride(nd) * sizeof(float);
+}
+
+__global__ void __launch_bounds__(kForceThreads) k_tb_force(TbArgs a) {
+    extern __shared__ __align__(16) unsigned char fsm[];
+    const int np = a.pes.nparams + pes_fparams_extra(a.pes.id);
+    float *sp = reinterpret_cast<float *>(fsm);
+    const int ldx = force_stride(a.nd);
+    float *sx = reinterpret_cast<float *>(fsm + ((size_t)np * sizeof(float) + 15) / 16 * 16) + threadIdx.x * ldx;
+    float *sg = sx + kForceThreads * ldx;
+    for (int i = threadIdx.x; i < np; i += kForceThreads) sp[i] = a.pes.fparams[i];
+    __syncthreads();
+    PesArgs pa = a.pes;
+    pa.fparams = sp;
+    const int64_t t = (int64_t)blockIdx.x * kForceThreads + threadIdx.x;
     const int P = a.P, nd = a.nd;
     if (t >= a.nrings * P) return;
     const int64_t ring = t / P;
     const int bead = (int)(t - ring * P);
     const size_t off = (size_t)ring * nd * P + bead;
-    float xb[kMaxDof], gb[kMaxDof];
-    for (int j = 0; j < nd; j++) xb[j] = a.x[off + (size_t)j * P];
+    for (int j = 0; j < nd; j++) sx[j] = a.x[off + (size_t)j * P];
     if (a.do_force) {
-        pes_vgrad<float>(a.pes, xb, gb);
-        for (int j = 0; j < nd; j++) a.f[off + (size_t)j * P] = gb[j];
+        pes_vgrad<float>(pa, sx, sg);
+        for (int j = 0; j < nd; j++) a.f[off + (size_t)j * P] = sg[j];
     }
     const int64_t s = *a.step0 + a.sofs;
     if (a.do_est && bead == P - 1 && (s - 1) >= a.imin) {
@@ -1041,7 +1060,7 @@ __global__ void __launch_bounds__(128) k_tb_force(TbArgs a) {
         const int lam = a.ringlam[ring];
         double contr = 0.0;
         for (int j = 0; j < nd; j++)
-            contr += a.mass[j / a.ndim] * (-(double)xb[j]) * a.dbdl[(size_t)lam * nd + j];
+            contr += a.mass[j / a.ndim] * (-(double)sx[j]) * a.dbdl[(size_t)lam * nd + j];
         RingAcc *r = &a.acc[ring];
         if (r->status == 0) r->dhdr_sum += contr;
         r->nsamples += 1;
@@ -1088,6 +1107,19 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tb_kick(TbArgs a) {
                 const int nvg = nv - c0;
                 float *qo = a.q + (size_t)(col0 + cb + c0) * P + m;
                 float *po = a.pi + (size_t)(col0 + cb + c0) * P + m;
+                float qv[kGrp], pv[kGrp];
+                float4 cfa[kGrp];
+                float2 cfb[kGrp];
+#pragma unroll
+                for (int i = 0; i < kGrp; i++) {  // state and coefficients first, then the normals
+                    const bool in = m < P && i < nvg;
+                    qv[i] = in ? qo[(size_t)i * P] : 0.f;
+                    pv[i] = in ? po[(size_t)i * P] : 0.f;
+                    const int jc = (int)((col0 + cb + c0 + i) % nd);
+                    const float *cf = a.coef + ((size_t)(jc / a.ndim) * P + mc) * 8;
+                    cfa[i] = __ldg(reinterpret_cast<const float4 *>(cf));
+                    cfb[i] = __ldg(reinterpret_cast<const float2 *>(cf + 4));
+                }
                 float gv[kGrp];
                 __syncwarp();
                 tmem_ldn<kGrp>(taddr + (uint32_t)c0, gv);
@@ -1109,13 +1141,11 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tb_kick(TbArgs a) {
                     for (int k = 0; k < 4; k++) {
                         const int i = 4 * g + k;
                         if (m < P && i < nvg) {
-                            const int jc = (int)((col0 + cb + c0 + i) % nd);
-                            const float *cf = a.coef + ((size_t)(jc / a.ndim) * P + mc) * 8;
-                            const float4 c4 = __ldg(reinterpret_cast<const float4 *>(cf));
-                            const float2 c2 = __ldg(reinterpret_cast<const float2 *>(cf + 4));
+                            const float4 c4 = cfa[i];
+                            const float2 c2 = cfb[i];
                             const float zk = sel4(rv, e ^ k);
-                            const float p0 = po[(size_t)i * P] - dt * gv[i];
-                            const float q0 = qo[(size_t)i * P];
+                            const float p0 = pv[i] - dt * gv[i];
+                            const float q0 = qv[i];
                             float p1 = c4.x * p0 + c4.y * q0;
                             const float q1 = c4.z * p0 + c4.w * q0;
                             p1 = c2.x * p1 + c2.y * zk;
@@ -1227,6 +1257,8 @@ int tc_prepare(pg_ctx *ctx, TiState &st) {
     PG_CUDA(cudaFuncSetAttribute(k_tc_final, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     PG_CUDA(cudaFuncSetAttribute(k_tb_pos, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     PG_CUDA(cudaFuncSetAttribute(k_tb_kick, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    PG_CUDA(cudaFuncSetAttribute(k_tb_force, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)tb_force_smem(st.nd, (int)ctx->fparams.size())));
     return PG_OK;
 }
 
@@ -1357,7 +1389,8 @@ static int tb_launch_kernel(pg_ctx *ctx, TiState &st, int k, int64_t i, bool fin
     if (k == 0)
         k_tb_pos<<<grid, kTileThreads, tc_smem_bytes(), s>>>(a);
     else if (k == 1)
-        k_tb_force<<<(unsigned)((st.nrings * st.P + 127) / 128), 128, 0, s>>>(a);
+        k_tb_force<<<(unsigned)((st.nrings * st.P + kForceThreads - 1) / kForceThreads), kForceThreads,
+                     tb_force_smem(st.nd, a.pes.nparams + pes_fparams_extra(a.pes.id)), s>>>(a);
     else
         k_tb_kick<<<grid, kTileThreads, tc_smem_bytes(), s>>>(a);
     cudaError_t e = cudaGetLastError();
