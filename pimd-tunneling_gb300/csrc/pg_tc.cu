@@ -18,6 +18,8 @@
 // as the SIMT kernels, so state read-out and checkpoints are shared.
 #include <cuda_bf16.h>
 
+#include <algorithm>
+
 #include <cstdio>
 #include <vector>
 
@@ -425,14 +427,10 @@ __device__ __forceinline__ void split8(const float (&v)[8], uint4 &hi, uint4 &lo
     lo = make_uint4(l[0], l[1], l[2], l[3]);
 }
 
-// Tile set-up: barriers, the T image by bulk copy, kNc TMEM columns, and the
-// tile X[c][k] = src[c * P + k] (zero for c >= nvalid) split into the B
-// operand.  Ends with a CTA barrier after which the operands are visible to
-// the tensor core.  Returns the TMEM base address.
-__device__ __forceinline__ uint32_t tile_begin(unsigned char *base, TcShared *sh, const unsigned char *gT,
-                                               const float *src, int nvalid) {
-    unsigned char *Thi = base, *Xhi = base + 2 * kOpBytes, *Xlo = Xhi + kXPlane;
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+// One-time set-up of a CTA: barriers, the T image by bulk copy (completes
+// tma_bar phase 0), kNc TMEM columns.  Returns the TMEM base address.
+__device__ __forceinline__ uint32_t tile_setup(unsigned char *base, TcShared *sh, const unsigned char *gT) {
+    const int tid = threadIdx.x, warp = tid >> 5;
     if (tid == 0) {
         mbar_init(&sh->mma_bar, 1);
         mbar_init(&sh->tma_bar, 1);
@@ -440,11 +438,23 @@ __device__ __forceinline__ uint32_t tile_begin(unsigned char *base, TcShared *sh
         fence_barrier_init();
     }
     __syncthreads();
-    load_transform(Thi, gT, sh);
+    load_transform(base, gT, sh);
     if (warp == 0) {
         __syncwarp();
         tmem_alloc(&sh->tmem_slot, kNc);
     }
+    tc_before();
+    __syncthreads();
+    tc_after();
+    return sh->tmem_slot;
+}
+
+// The tile X[c][k] = src[c * P + k] (zero for c >= nvalid) split into the B
+// operand.  Ends with a CTA barrier after which the operand (and anything the
+// CTA wrote to shared memory before the call) is visible to the tensor core.
+__device__ __forceinline__ void tile_load(unsigned char *base, const float *src, int nvalid) {
+    unsigned char *Xhi = base + 2 * kOpBytes, *Xlo = Xhi + kXPlane;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     // Warp w fills rows 8w..8w+7.  Lane: row 8w + lane % 8, K chunks
     // 8 (4 it + lane / 8): the 8 lanes of one chunk write one core matrix.
     const int c = 8 * warp + (lane & 7);
@@ -472,7 +482,14 @@ __device__ __forceinline__ uint32_t tile_begin(unsigned char *base, TcShared *sh
     tc_before();
     __syncthreads();
     tc_after();
-    return sh->tmem_slot;
+}
+
+// Set-up and first tile in one (single-tile kernels).
+__device__ __forceinline__ uint32_t tile_begin(unsigned char *base, TcShared *sh, const unsigned char *gT,
+                                               const float *src, int nvalid) {
+    const uint32_t tmem = tile_setup(base, sh, gT);
+    tile_load(base, src, nvalid);
+    return tmem;
 }
 
 // Thread 0 issues D = T X (3 split products per K step of 16) and commits it
@@ -623,10 +640,15 @@ __device__ __forceinline__ float sel4(const float (&v)[4], int i) {
 // Lane e of a quad draws the block of column 4g + e (normals j P + 4 (m/4) ..
 // +3, the four modes of the quad), then the quad transposes the 4 x 4 values.
 __device__ __forceinline__ void tile_normals(const TileAux *ax, int64_t col0, int nd, int cb, int m, uint32_t st,
-                                             float (&zc)[32]) {
+                                             int nv, float (&zc)[32]) {
     const int e = threadIdx.x & 3;
 #pragma unroll
     for (int g0 = 0; g0 < 8; g0 += 4) {
+        if (4 * g0 >= nv) {  // no valid column in these 16 (warp-uniform)
+#pragma unroll
+            for (int k = 0; k < 16; k++) zc[4 * g0 + k] = 0.f;
+            continue;
+        }
         U4 o[4];
 #pragma unroll
         for (int g = 0; g < 4; g++) {
@@ -721,11 +743,15 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_final(TcArgs a) {
     tile_release(sh, tmem, a.err, 0);
 }
 
-// One MD step of a tile (verletmodule.f90:423-435 in normal-mode form):
+// One MD step (verletmodule.f90:423-435 in normal-mode form) of the rings
+// [r0, r1) of this CTA, r0 = floor(b R / G), r1 = floor((b + 1) R / G) for
+// CTA b of G (so every SM gets the same number of rings), walked in chunks of
+// up to 64 columns.  T is copied in and TMEM allocated once per CTA.  Per chunk:
 //   GEMM 1: x = T q + x*; estimator of step s-1; forces F(x) split straight
 //           into the B operand;
 //   GEMM 2: T F; kick, half rotation, OU (normals drawn while GEMM 1 runs),
 //           half rotation of (q, pi), written back.
+// mma_bar completes two phases per chunk (parities 0 and 1).
 template <int PESK>
 __global__ void __launch_bounds__(kTileThreads, 2) k_tc_step(TcArgs a) {
     extern __shared__ unsigned char dsm[];
@@ -735,99 +761,115 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_step(TcArgs a) {
     TileAux *ax = reinterpret_cast<TileAux *>(base + kTileSmemOps + 256);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int nd = a.nd;
-    const int64_t col0 = (int64_t)blockIdx.x * kNc;
-    const int nvalid = (int)min((int64_t)kNc, a.nrings * nd - col0);
     const int64_t s = *a.step0 + a.sofs;
-    if (tid < kNc) {
-        float xa = 0.f, xs = 0.f;
-        uint64_t sd = 0;
-        uint32_t sm = 0;
-        if (tid < nvalid) {
-            const int64_t ring = (col0 + tid) / nd;
-            const int j = (int)(col0 + tid - ring * nd);
-            const int lam = a.ringlam[ring];
-            xa = (float)a.avec[j];
-            xs = (float)((a.bvec[(size_t)lam * nd + j] - a.avec[j]) / (double)(kP + 1));
-            sd = a.ringseed[ring];
-            sm = a.ringstream[ring];
-        }
-        ax->xa[tid] = xa;
-        ax->xs[tid] = xs;
-        ax->seed[tid] = sd;
-        ax->stream[tid] = sm;
-    }
-    const uint32_t tmem = tile_begin(base, sh, a.gT, a.q + col0 * kP, nvalid);
-    tile_issue(base, sh, tmem, true);
+    const int64_t r0 = (int64_t)blockIdx.x * a.nrings / gridDim.x;
+    const int64_t r1 = ((int64_t)blockIdx.x + 1) * a.nrings / gridDim.x;
+    const int rpc = kNc / nd;  // rings per chunk
     const int m = 32 * (warp & 3) + lane;  // bead (GEMM 1) / mode (GEMM 2)
     const int cb = 32 * (warp >> 2);        // first column of this thread's half
-    const int nv = nvalid - cb;              // valid columns of the half (may be <= 0)
+    const uint32_t tmem = tile_setup(base, sh, a.gT);
     const uint32_t taddr = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)cb;
-    float zc[32];
-    tile_normals(ax, col0, nd, cb, m, (uint32_t)s, zc);
-    bool ok = tile_wait(sh, 0);
-    if (ok) {
-#pragma unroll 1
-        for (int c0 = 0; c0 < 32; c0 += kGrp) {
-            float xv[kGrp], fv[kGrp];
-            group_positions(ax, taddr, cb, c0, m, a.do_est != 0, xv, ax->xP);
-            group_forces<PESK>(a, xv, fv);
-            group_store_operand(Xhi, Xlo, cb, c0, m, fv);
-        }
-        fence_async_smem();
-    }
-    tc_before();
-    __syncthreads();  // F operand complete, TMEM reads of GEMM 1 done, xP staged
-    tc_after();
+    bool ok = true;
     uint32_t last_phase = 0;  // parity of the last GEMM issued (for the drain on a timeout)
-    if (ok) {
-        tile_issue(base, sh, tmem, false);
-        last_phase = 1;
-    }
-    if (ok && a.do_est) tile_estimator(a, ax, col0, nvalid, s);
-    if (ok) ok = tile_wait(sh, 1);
-    if (ok) {
-        const float4 c4 = *reinterpret_cast<const float4 *>(a.coef + (size_t)m * 8);
-        const float2 c2 = *reinterpret_cast<const float2 *>(a.coef + (size_t)m * 8 + 4);
-        const float dt = a.dt;
-        uint32_t badbits = 0;
-#pragma unroll
-        for (int c0 = 0; c0 < 32; c0 += kGrp) {
-            const int nvg = nv - c0;
-            float *qo = a.q + (size_t)(col0 + cb + c0) * kP + m;
-            float *po = a.pi + (size_t)(col0 + cb + c0) * kP + m;
-            float qv[kGrp], pv[kGrp], gv[kGrp];
-#pragma unroll
-            for (int i = 0; i < kGrp; i++) {
-                qv[i] = i < nvg ? qo[(size_t)i * kP] : 0.f;
-                pv[i] = i < nvg ? po[(size_t)i * kP] : 0.f;
+    bool first = true;
+    for (int64_t rc = r0; rc < r1 && ok; rc += rpc) {
+        const int64_t col0 = rc * nd;
+        const int nvalid = (int)(min((int64_t)rpc, r1 - rc) * nd);
+        const int nv = nvalid - cb;  // valid columns of the half (may be <= 0)
+        if (tid < kNc) {
+            float xa = 0.f, xs = 0.f;
+            uint64_t sd = 0;
+            uint32_t sm = 0;
+            if (tid < nvalid) {
+                const int64_t ring = (col0 + tid) / nd;
+                const int j = (int)(col0 + tid - ring * nd);
+                const int lam = a.ringlam[ring];
+                xa = (float)a.avec[j];
+                xs = (float)((a.bvec[(size_t)lam * nd + j] - a.avec[j]) / (double)(kP + 1));
+                sd = a.ringseed[ring];
+                sm = a.ringstream[ring];
             }
-            __syncwarp();
-            tmem_ldn<kGrp>(taddr + (uint32_t)c0, gv);
+            ax->xa[tid] = xa;
+            ax->xs[tid] = xs;
+            ax->seed[tid] = sd;
+            ax->stream[tid] = sm;
+        }
+        tile_load(base, a.q + col0 * kP, nvalid);
+        tile_issue(base, sh, tmem, first);
+        last_phase = 0;
+        first = false;
+        float zc[32];
+        tile_normals(ax, col0, nd, cb, m, (uint32_t)s, nv, zc);
+        ok = tile_wait(sh, 0);
+        if (ok) {
+#pragma unroll 1
+            for (int c0 = 0; c0 < 32; c0 += kGrp) {
+                if (c0 >= nv) break;  // warp-uniform
+                float xv[kGrp], fv[kGrp];
+                group_positions(ax, taddr, cb, c0, m, a.do_est != 0, xv, ax->xP);
+                group_forces<PESK>(a, xv, fv);
+                group_store_operand(Xhi, Xlo, cb, c0, m, fv);
+            }
+            fence_async_smem();
+        }
+        tc_before();
+        __syncthreads();  // F operand complete, TMEM reads of GEMM 1 done, xP staged
+        tc_after();
+        if (ok) {
+            tile_issue(base, sh, tmem, false);
+            last_phase = 1;
+            if (a.do_est) tile_estimator(a, ax, col0, nvalid, s);
+            ok = tile_wait(sh, 1);
+        }
+        if (ok) {
+            const float4 c4 = *reinterpret_cast<const float4 *>(a.coef + (size_t)m * 8);
+            const float2 c2 = *reinterpret_cast<const float2 *>(a.coef + (size_t)m * 8 + 4);
+            const float dt = a.dt;
+            uint32_t badbits = 0;
 #pragma unroll
-            for (int i = 0; i < kGrp; i++) {
-                const float zk = zc[c0 + i];
-                const float p0 = pv[i] - dt * gv[i];
-                const float q0 = qv[i];
-                float p1 = c4.x * p0 + c4.y * q0;
-                const float q1 = c4.z * p0 + c4.w * q0;
-                p1 = c2.x * p1 + c2.y * zk;
-                const float pn = c4.x * p1 + c4.y * q1;
-                const float qn = c4.z * p1 + c4.w * q1;
-                if (i < nvg) {
-                    qo[(size_t)i * kP] = qn;
-                    po[(size_t)i * kP] = pn;
-                    if (pn != pn) badbits |= 1u << (c0 + i);
+            for (int c0 = 0; c0 < 32; c0 += kGrp) {
+                if (c0 < nv) {  // warp-uniform
+                    const int nvg = nv - c0;
+                    float *qo = a.q + (size_t)(col0 + cb + c0) * kP + m;
+                    float *po = a.pi + (size_t)(col0 + cb + c0) * kP + m;
+                    float qv[kGrp], pv[kGrp], gv[kGrp];
+#pragma unroll
+                    for (int i = 0; i < kGrp; i++) {
+                        qv[i] = i < nvg ? qo[(size_t)i * kP] : 0.f;
+                        pv[i] = i < nvg ? po[(size_t)i * kP] : 0.f;
+                    }
+                    __syncwarp();
+                    tmem_ldn<kGrp>(taddr + (uint32_t)c0, gv);
+#pragma unroll
+                    for (int i = 0; i < kGrp; i++) {
+                        const float zk = zc[c0 + i];
+                        const float p0 = pv[i] - dt * gv[i];
+                        const float q0 = qv[i];
+                        float p1 = c4.x * p0 + c4.y * q0;
+                        const float q1 = c4.z * p0 + c4.w * q0;
+                        p1 = c2.x * p1 + c2.y * zk;
+                        const float pn = c4.x * p1 + c4.y * q1;
+                        const float qn = c4.z * p1 + c4.w * q1;
+                        if (i < nvg) {
+                            qo[(size_t)i * kP] = qn;
+                            po[(size_t)i * kP] = pn;
+                            if (pn != pn) badbits |= 1u << (c0 + i);
+                        }
+                    }
                 }
             }
+            badbits = __reduce_or_sync(0xffffffffu, badbits);
+            if (lane == 0 && badbits) {
+                for (int i = 0; i < 32; i++)
+                    if (badbits & (1u << i)) {
+                        const int64_t ring = (col0 + cb + i) / nd;
+                        if (atomicOr(&a.acc[ring].status, PG_RING_NAN) == 0) a.acc[ring].pad = (int32_t)s;
+                    }
+            }
         }
-        badbits = __reduce_or_sync(0xffffffffu, badbits);
-        if (lane == 0 && badbits) {
-            for (int i = 0; i < 32; i++)
-                if (badbits & (1u << i)) {
-                    const int64_t ring = (col0 + cb + i) / nd;
-                    if (atomicOr(&a.acc[ring].status, PG_RING_NAN) == 0) a.acc[ring].pad = (int32_t)s;
-                }
-        }
+        tc_before();
+        __syncthreads();  // TMEM and shared memory of this chunk fully read
+        tc_after();
     }
     tile_release(sh, tmem, a.err, last_phase);
 }
@@ -1325,10 +1367,13 @@ static int tc_launch_step(pg_ctx *ctx, TiState &st, int64_t i, cudaStream_t s) {
     a.sofs = i;
     a.do_est = i > 0 ? 1 : 0;
     const size_t sm = tc_smem_bytes();
+    // persistent: two CTAs per SM (the shared-memory limit), equal ring ranges
+    const unsigned grid = (unsigned)std::min<int64_t>(2 * (int64_t)(ctx->sm_count > 0 ? ctx->sm_count : 1),
+                                                      (int64_t)tc_grid(st));
     if (pesk == 2)
-        k_tc_step<2><<<tc_grid(st), kTileThreads, sm, s>>>(a);
+        k_tc_step<2><<<grid, kTileThreads, sm, s>>>(a);
     else
-        k_tc_step<1><<<tc_grid(st), kTileThreads, sm, s>>>(a);
+        k_tc_step<1><<<grid, kTileThreads, sm, s>>>(a);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? PG_OK : cuda_fail(e, "k_tc_step launch");
 }
