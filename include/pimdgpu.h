@@ -166,6 +166,12 @@ int pg_ti_get_state(pg_ctx *ctx, double *x, double *p);
  * Any pointer may be NULL. */
 int pg_ti_get_results(pg_ctx *ctx, double *dhdr_sum, int64_t *nsamples, int64_t *nreinit,
                       int32_t *status);
+/* Restores the per-ring estimator sums and sample counts and the batch step
+ * counter (the Philox streams continue from it): the continuation of
+ * propagate_pimd_pile after its restart file is read (verletmodule.f90:388, 413;
+ * pimd_par.f90:356-369), for state set by pg_ti_setup(x0, p0) from that file.
+ * The status, re-initialisation and Andersen counters are left as they are. */
+int pg_ti_set_accumulators(pg_ctx *ctx, const double *dhdr_sum, const int64_t *nsamples, int64_t step);
 /* Per-lambda reduction of integrand = dHdr/betan^2 over the rings of each lambda
  * (pimd_par.f90:379, 401-409), on the device: mean[nlambda], var[nlambda]
  * (E[I^2]-E[I]^2), count[nlambda]. */

@@ -1265,6 +1265,29 @@ extern "C" int pg_ti_get_results(pg_ctx *ctx, double *dhdr_sum, int64_t *nsample
     return PG_OK;
 }
 
+extern "C" int pg_ti_set_accumulators(pg_ctx *ctx, const double *dhdr_sum, const int64_t *nsamples, int64_t step) {
+    int rc = check_ctx(ctx, true);
+    if (rc) return rc;
+    if (!ctx->ti) return fail(PG_ERR_STATE, "pg_ti_setup has not been called");
+    if (!dhdr_sum || !nsamples) return fail(PG_ERR_ARG, "dhdr_sum and nsamples are required");
+    if (step < 0 || step > (int64_t)0xFFFFFFFFLL) return fail(PG_ERR_ARG, "step out of range");
+    TiState &st = *ctx->ti;
+    for (int64_t r = 0; r < st.nrings; r++)
+        if (nsamples[r] < 0) return fail(PG_ERR_ARG, "negative sample count");
+    std::vector<RingAcc> acc(st.nrings);
+    PG_CUDA(cudaMemcpyAsync(acc.data(), st.acc.ptr, st.nrings * sizeof(RingAcc), cudaMemcpyDeviceToHost, ctx->stream));
+    PG_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (int64_t r = 0; r < st.nrings; r++) {
+        acc[r].dhdr_sum = dhdr_sum[r];
+        acc[r].nsamples = nsamples[r];
+    }
+    PG_CUDA(cudaMemcpyAsync(st.acc.ptr, acc.data(), st.nrings * sizeof(RingAcc), cudaMemcpyHostToDevice, ctx->stream));
+    PG_CUDA(cudaMemcpyAsync(step_ptr(st), &step, sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+    PG_CUDA(cudaStreamSynchronize(ctx->stream));
+    st.step = step;
+    return PG_OK;
+}
+
 extern "C" int pg_ti_lambda_reduce(pg_ctx *ctx, double *mean, double *var, int64_t *count) {
     int rc = check_ctx(ctx, true);
     if (rc) return rc;

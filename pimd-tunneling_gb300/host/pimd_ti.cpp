@@ -11,11 +11,20 @@
 // init ('path': beads on the path as init_path does, verletmodule.f90:40-48;
 // 'well': every bead at well 1), init_sigma (Gaussian noise on the start
 // positions), chunk (steps per device launch sequence).
-// restart = 1 writes restart.ckpt after the run, restart = 2 continues from it
-// (a bitwise checkpoint of the device state; replaces restart_proc*.xyz).
+// restart >= 1 writes, after the run, the reference's restart files
+// restart_proc<iproc>_<ii>.xyz (verletmodule.f90:162-185; the task -> (rank,
+// local index) split of pimd_par.f90:109-110, 332-353 for nproc ranks, key
+// nproc, default 1) and restart.ckpt, a bitwise checkpoint of the device state.
+// restart = 2 continues from restart.ckpt when present, else from the restart
+// files (positions, momenta, dHdr sums, step count), and runs NMC further
+// steps as the reference does.  Deviation: the estimator is divided by the
+// number of accumulated samples (the reference divides by NMC + restartnmc -
+// imin although it skips imin steps again after a restart).
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <fstream>
 #include <iostream>
 #include <string>
 #include <vector>
@@ -43,6 +52,64 @@ static std::vector<double> read_numbers(const std::string &path) {
     double x;
     while (f >> x) v.push_back(x);
     return v;
+}
+
+// restart_proc<iproc>_<ii>.xyz of task r: nproc contiguous blocks of
+// ncalcs = ceil(ntask / nproc) tasks (pimd_par.f90:109-110, 352).
+static std::string restart_name(int64_t r, int64_t ntask, int64_t nproc) {
+    const int64_t ncalcs = (ntask + nproc - 1) / nproc;
+    return "restart_proc" + std::to_string(r / ncalcs) + "_" + std::to_string(r % ncalcs + 1) + ".xyz";
+}
+
+// write_restart (verletmodule.f90:162-185): per bead natom, dHdr, label x y z;
+// then per bead natom, step, label px py pz.  Coordinates beyond ndim are 0.
+// x, p: [dof][bead] of one ring, dof = atom * ndim + dim.
+static bool write_restart_xyz(const std::string &path, int64_t n, int ndim, int natom,
+                              const std::vector<std::string> &label, const double *x, const double *p,
+                              double dhdr, int64_t step) {
+    FILE *f = std::fopen(path.c_str(), "w");
+    if (!f) return false;
+    for (int pass = 0; pass < 2; pass++)
+        for (int64_t i = 0; i < n; i++) {
+            std::fprintf(f, " %d\n", natom);
+            if (pass == 0)
+                std::fprintf(f, " %.17g\n", dhdr);
+            else
+                std::fprintf(f, " %lld\n", (long long)step);
+            const double *v = pass == 0 ? x : p;
+            for (int j = 0; j < natom; j++) {
+                std::fprintf(f, " %s", label[j].c_str());
+                for (int d = 0; d < 3; d++) std::fprintf(f, " %.17g", d < ndim ? v[((int64_t)j * ndim + d) * n + i] : 0.0);
+                std::fprintf(f, "\n");
+            }
+        }
+    return std::fclose(f) == 0;
+}
+
+static bool read_restart_xyz(const std::string &path, int64_t n, int ndim, int natom, double *x, double *p,
+                             double *dhdr, int64_t *step) {
+    std::ifstream f(path);
+    if (!f) return false;
+    for (int pass = 0; pass < 2; pass++)
+        for (int64_t i = 0; i < n; i++) {
+            int na = 0;
+            if (!(f >> na) || na != natom) return false;
+            if (pass == 0) {
+                if (!(f >> *dhdr)) return false;
+            } else {
+                long long st = 0;
+                if (!(f >> st)) return false;
+                *step = st;
+            }
+            double *v = pass == 0 ? x : p;
+            for (int j = 0; j < natom; j++) {
+                std::string lab;
+                double c[3];
+                if (!(f >> lab >> c[0] >> c[1] >> c[2])) return false;
+                for (int d = 0; d < ndim && d < 3; d++) v[((int64_t)j * ndim + d) * n + i] = c[d];
+            }
+        }
+    return true;
 }
 
 #define CHECK(call)                                                                    \
@@ -84,6 +151,10 @@ int main(int argc, char **argv) {
     const bool iprint = nl.logical("iprint", false);
     const int64_t npath = nl.integer("npath", 0);
     const int restart = (int)nl.integer("restart", 0);
+    const int64_t nproc = std::max<int64_t>(1, nl.integer("nproc", 1));
+    const bool instapath = nl.logical("instapath", false);  // pimd_par.f90:76
+    const bool centre = nl.logical("centre", false);        // pimd_par.f90:77
+    const bool fixedends = nl.logical("fixedends", true);   // pimd_par.f90:81
     const std::string pes = nl.str("pes", "1d");
     const std::string prec = lower(nl.str("precision", "mixed"));
     const std::string form = lower(nl.str("form", "auto"));
@@ -98,11 +169,14 @@ int main(int argc, char **argv) {
                     "\"xunit\": %d, \"imin\": %lld, \"tau\": %.17g, \"gamma\": %.17g, \"dHdrlimit\": %.17g, "
                     "\"readpath\": %s, \"cayley\": %s, \"npath\": %lld, \"restart\": %d, \"pes\": \"%s\", "
                     "\"precision\": \"%s\", \"form\": \"%s\", \"seed\": %llu, \"init\": \"%s\", "
-                    "\"init_sigma\": %.17g}\n",
+                    "\"init_sigma\": %.17g, \"nproc\": %lld, \"instapath\": %s, \"centre\": %s, "
+                    "\"fixedends\": %s}\n",
                     (long long)n, beta, (long long)NMC, (long long)Noutput, dt, (long long)nintegral,
                     (long long)nrep, thermostat, ndim, natom, xunit, (long long)imin, tau, gamma, dHdrlimit,
                     readpath ? "true" : "false", cayley ? "true" : "false", (long long)npath, restart,
-                    pes.c_str(), prec.c_str(), form.c_str(), (unsigned long long)seed, init.c_str(), init_sigma);
+                    pes.c_str(), prec.c_str(), form.c_str(), (unsigned long long)seed, init.c_str(), init_sigma,
+                    (long long)nproc, instapath ? "true" : "false", centre ? "true" : "false",
+                    fixedends ? "true" : "false");
         return 0;
     }
     auto t0 = std::chrono::steady_clock::now();
@@ -152,14 +226,103 @@ int main(int argc, char **argv) {
     } else {
         frames = {w1, w2};
     }
-    const int64_t np = (int64_t)frames.size();
-    std::vector<double> lam(np, 0.0);
-    for (int64_t i = 1; i < np; i++) {
-        double d = 0.0;
-        for (int k = 0; k < nd; k++) d += (frames[i][k] - frames[i - 1][k]) * (frames[i][k] - frames[i - 1][k]);
-        lam[i] = lam[i - 1] + std::sqrt(d);
+    // normalised arc length of the path frames (instantonmod.f90:928-937, no alignment)
+    auto arc_length = [&](const std::vector<std::vector<double>> &fr) {
+        std::vector<double> l(fr.size(), 0.0);
+        for (size_t i = 1; i < fr.size(); i++) {
+            double d = 0.0;
+            for (int k = 0; k < nd; k++) d += (fr[i][k] - fr[i - 1][k]) * (fr[i][k] - fr[i - 1][k]);
+            l[i] = l[i - 1] + std::sqrt(d);
+        }
+        for (auto &v : l) v /= l.back();
+        return l;
+    };
+    std::vector<double> lam = arc_length(frames);
+    if (instapath) {
+        // instanton from the path guess (instantonmod.f90:945-983): beads at
+        // xi = (k-1)/(n-1) on the spline, optimised with fixed ends at the wells
+        // (the action's betan is that of the driver, pimd_par.f90:94)
+        if (!fixedends) {
+            std::fprintf(stderr, "instapath needs fixedends = .true. (the free-ended action is not built)\n");
+            return 1;
+        }
+        const int64_t npf = (int64_t)frames.size();
+        std::vector<double> xt((size_t)nd * n), yk(npf), y2k(npf);
+        for (int k = 0; k < nd; k++) {
+            for (int64_t i = 0; i < npf; i++) yk[i] = frames[i][k];
+            CHECK(pg_spline(lam.data(), yk.data(), npf, 1.0e31, 1.0e31, y2k.data()));
+            for (int64_t bead = 0; bead < n; bead++)
+                CHECK(pg_splint(lam.data(), yk.data(), y2k.data(), npf, (double)bead / (double)(n - 1),
+                                &xt[(size_t)k * n + bead], nullptr));
+        }
+        std::printf(" Finding instanton\n");
+        pg_lbfgs_opts o;
+        o.m = 8;  // instantonmod.f90:716
+        o.max_backtracks = 40;
+        o.maxiter = 200000;
+        o.factr = 1.0e6;
+        o.pgtol = 1.0e-5;
+        double um = 0.0;
+        int64_t it = 0;
+        int32_t ist = 0;
+        CHECK(pg_instanton_optimize(ctx, 1, n, xt.data(), w1.data(), w2.data(), &betan, &o, &um, &it, &ist));
+        std::printf(" Found instanton after %lld iterations (status %d).\n", (long long)it, ist);
+        frames.assign(1, w1);
+        for (int64_t bead = 0; bead < n; bead++) {
+            std::vector<double> f(nd);
+            for (int k = 0; k < nd; k++) f[k] = xt[(size_t)k * n + bead];
+            frames.push_back(f);
+        }
+        frames.push_back(w2);
+        FILE *fi = std::fopen("instanton.xyz", "w");
+        if (fi) {
+            for (int64_t bead = 0; bead < n; bead++) {
+                std::fprintf(fi, " %d\n Energy of minimum %lld\n", natom, (long long)(bead + 1));
+                for (int j = 0; j < natom; j++) {
+                    std::fprintf(fi, " %s", label[j].c_str());
+                    for (int d = 0; d < ndim; d++) std::fprintf(fi, " %.17g", xt[(size_t)(j * ndim + d) * n + bead] * 0.529177);
+                    std::fprintf(fi, "\n");
+                }
+            }
+            std::fclose(fi);
+        }
+        lam = arc_length(frames);
     }
-    for (auto &l : lam) l /= lam[np - 1];
+    if (centre) {
+        // barrier top xm = the zero of dV/dlambda on (0.3, 0.7) by bisection
+        // (instantonmod.f90:832-871), then lambda = a l^2 + b l with
+        // a = 2 - 4 xm, b = 4 xm - 1 (instantonmod.f90:993-1004), solved as
+        // l = 2 lambda / (b + sqrt(b^2 + 4 a lambda)): the reference's root for
+        // either sign of a, finite for a -> 0 (a symmetric barrier).
+        const int64_t npf = (int64_t)frames.size();
+        std::vector<double> vpath(npf), vy2(npf);
+        std::vector<double> flat((size_t)npf * nd);
+        for (int64_t i = 0; i < npf; i++)
+            for (int k = 0; k < nd; k++) flat[(size_t)i * nd + k] = frames[i][k];
+        CHECK(pg_pes_eval(ctx, npf, flat.data(), vpath.data(), nullptr, PG_FP64));
+        CHECK(pg_spline(lam.data(), vpath.data(), npf, 1.0e31, 1.0e31, vy2.data()));
+        auto dv = [&](double l) {
+            double y = 0.0, g = 0.0;
+            pg_splint(lam.data(), vpath.data(), vy2.data(), npf, l, &y, &g);
+            return g;
+        };
+        double x1 = 0.3, x2 = 0.7, f1 = dv(x1), f2 = dv(x2);
+        if (f1 * f2 >= 0.0) {
+            std::fprintf(stderr, "centre: the barrier top is not bracketed in (0.3, 0.7)\n");
+            return 1;
+        }
+        double xm = f1 < 0.0 ? x1 : x2, dx = f1 < 0.0 ? x2 - x1 : x1 - x2;
+        for (int j = 0; j < 40; j++) {
+            dx *= 0.5;
+            const double xmid = xm + dx, fm = dv(xmid);
+            if (fm <= 0.0) xm = xmid;
+            if (std::fabs(dx) < 1.0e-6 || fm == 0.0) break;
+        }
+        const double ca = 2.0 - 4.0 * xm, cb = 4.0 * xm - 1.0;
+        for (auto &l : lam) l = 2.0 * l / (cb + std::sqrt(cb * cb + 4.0 * ca * l));
+        std::printf(" Centred, %.15g %.15g %.15g\n", ca, cb, xm);
+    }
+    const int64_t np = (int64_t)frames.size();
     std::vector<std::vector<double>> ycol(nd, std::vector<double>(np)), y2(nd, std::vector<double>(np));
     for (int k = 0; k < nd; k++) {
         for (int64_t i = 0; i < np; i++) ycol[k][i] = frames[i][k];
@@ -212,18 +375,59 @@ int main(int argc, char **argv) {
     cfg.noutput = Noutput;
     cfg.dhdr_limit = dHdrlimit;
     cfg.init_sigma = init_sigma;
+    const int64_t nstate = nrings * nd * n;
+    bool from_files = false;
+    std::vector<double> x0, p0, dsum(nrings);
+    int64_t step0 = 0;
+    if (restart == 2 && !std::ifstream("restart.ckpt")) {
+        x0.resize(nstate);
+        p0.resize(nstate);
+        for (int64_t r = 0; r < nrings; r++) {
+            int64_t st = 0;
+            const std::string name = restart_name(r, nrings, nproc);
+            if (!read_restart_xyz(name, n, ndim, natom, &x0[r * nd * n], &p0[r * nd * n], &dsum[r], &st)) {
+                std::fprintf(stderr, "cannot read restart file %s\n", name.c_str());
+                return 1;
+            }
+            if (r == 0) step0 = st;
+            if (st != step0) {
+                std::fprintf(stderr, "restart files disagree on the step count (%s)\n", name.c_str());
+                return 1;
+            }
+        }
+        from_files = true;
+    }
     CHECK(pg_ti_setup(ctx, &cfg, nrings, nintegral, rlam.data(), rseed.data(), rstream.data(), a.data(), b.data(),
-                      dbdl.data(), xref.data(), nullptr, nullptr));
-    if (restart == 2) CHECK(pg_ti_checkpoint_load(ctx, "restart.ckpt"));
+                      dbdl.data(), xref.data(), from_files ? x0.data() : nullptr, from_files ? p0.data() : nullptr));
+    if (restart == 2) {
+        if (from_files) {
+            std::vector<int64_t> ns(nrings, std::max<int64_t>(0, step0 - imin));
+            CHECK(pg_ti_set_accumulators(ctx, dsum.data(), ns.data(), step0));
+        } else {
+            CHECK(pg_ti_checkpoint_load(ctx, "restart.ckpt"));
+        }
+    }
     int64_t done = 0;
     CHECK(pg_ti_get_step(ctx, &done));
-    while (done < NMC) {
-        int64_t k = std::min(chunk, NMC - done);
+    const int64_t target = restart == 2 ? done + NMC : NMC;
+    while (done < target) {
+        int64_t k = std::min(chunk, target - done);
         CHECK(pg_ti_advance(ctx, k));
         done += k;
-        if (iprint) std::printf(" %.2f %% of the steps done\n", 100.0 * (double)done / (double)NMC);
+        if (iprint) std::printf(" %.2f %% of the steps done\n", 100.0 * (double)done / (double)target);
     }
-    if (restart >= 1) CHECK(pg_ti_checkpoint_save(ctx, "restart.ckpt"));
+    if (restart >= 1) {
+        CHECK(pg_ti_checkpoint_save(ctx, "restart.ckpt"));
+        std::vector<double> xs(nstate), ps(nstate), ds(nrings);
+        CHECK(pg_ti_get_state(ctx, xs.data(), ps.data()));
+        CHECK(pg_ti_get_results(ctx, ds.data(), nullptr, nullptr, nullptr));
+        for (int64_t r = 0; r < nrings; r++)
+            if (!write_restart_xyz(restart_name(r, nrings, nproc), n, ndim, natom, label, &xs[r * nd * n],
+                                   &ps[r * nd * n], ds[r], done)) {
+                std::fprintf(stderr, "cannot write restart file for task %lld\n", (long long)r);
+                return 1;
+            }
+    }
     std::vector<double> mean(nintegral), var(nintegral);
     std::vector<int64_t> cnt(nintegral);
     CHECK(pg_ti_lambda_reduce(ctx, mean.data(), var.data(), cnt.data()));

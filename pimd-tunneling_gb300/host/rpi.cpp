@@ -9,6 +9,7 @@
 // Keys beyond the reference's namelist: pes, pes_params (as pimd_ti), m (L-BFGS
 // history, reference 8), pgtol (reference eps2 = 1e-5), factr (1e6), maxiter,
 // quirks (1: the reference's Hessian band and mcmod_2dtest Hessian).
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -74,12 +75,17 @@ int main(int argc, char **argv) {
     const double factr = nl.real("factr", 1.0e6);
     const int64_t maxiter = nl.integer("maxiter", 200000);
     const int quirks = (int)nl.integer("quirks", 0);
+    const bool angular = nl.logical("angular", false);                  // rpi_ser.f90:35
+    const int64_t npoints = nl.integer("npoints", 10);                  // rpi_ser.f90:34
+    const double cutofftheta = nl.real("cutofftheta", 2.0 * 3.14159265358979);  // no reference default
+    const double cutoffphi = nl.real("cutoffphi", 3.14159265358979);            // no reference default
     if (parse_only) {
         std::printf("{\"n\": %lld, \"beta\": %.17g, \"ndim\": %d, \"natom\": %d, \"xunit\": %d, \"npath\": %lld, "
                     "\"readpath\": %s, \"pes\": \"%s\", \"m\": %d, \"pgtol\": %.17g, \"factr\": %.17g, "
-                    "\"maxiter\": %lld, \"quirks\": %d}\n",
+                    "\"maxiter\": %lld, \"quirks\": %d, \"angular\": %s, \"npoints\": %lld}\n",
                     (long long)n, beta, ndim, natom, xunit, (long long)npath, readpath ? "true" : "false",
-                    pes.c_str(), m, pgtol, factr, (long long)maxiter, quirks);
+                    pes.c_str(), m, pgtol, factr, (long long)maxiter, quirks, angular ? "true" : "false",
+                    (long long)npoints);
         return 0;
     }
     auto t0 = std::chrono::steady_clock::now();
@@ -162,6 +168,84 @@ int main(int argc, char **argv) {
     std::printf(" phi= %.15g\n s_kink= %.15g\n theta, N*theta= %.15g %.15g\n", gam, S, omega, omega * (double)n);
     std::printf(" h_ij= %.15g %.15g\n RPI delta= %.15g %.15g\n", omega / betan, 219475.0 * omega / betan, delta,
                 delta * 219475.0);
+    if (angular) {
+        // Solid-angle grid (rpi_ser.f90:241-348): well 2 rotated by Gauss-Legendre
+        // angles, the instanton re-optimised from the one above for every
+        // orientation -- all orientations in one batched optimisation and one
+        // batched log-det -- and I(beta) = tanh(Omega N) per point (3-D: 1 when
+        // Omega N > 1).  3-D: R_x(theta) R_z(phi) R_x(eta) on every atom
+        // (rotate_atoms, instantonmod.f90:346-376); 2-D: rotation by eta in the
+        // plane (the reference applies its 3 x 3 x-axis matrix to 2-vectors there).
+        const double twopi = 2.0 * 3.14159265358979, pi = 3.14159265358979;
+        std::vector<double> th(npoints), wth(npoints), ph(npoints), wph(npoints), et(npoints), wet(npoints);
+        CHECK(pg_gauleg(0.0, std::min(twopi, cutofftheta), et.data(), wet.data(), npoints));
+        const bool three = ndim == 3;
+        if (three) {
+            CHECK(pg_gauleg(0.0, std::min(twopi, cutofftheta), th.data(), wth.data(), npoints));
+            CHECK(pg_gauleg(0.0, std::min(pi, cutoffphi), ph.data(), wph.data(), npoints));
+        } else if (ndim != 2) {
+            std::fprintf(stderr, "angular needs ndim = 2 or 3\n");
+            return 1;
+        }
+        auto rot = [&](std::vector<double> &w, int axis, double ang) {  // rotate_atoms
+            if (std::fabs(ang) <= 1e-10) return;
+            const double c = std::cos(ang), s = std::sin(ang);
+            const int j = axis == 1 ? 1 : 0, k = axis == 1 ? 2 : 1;
+            for (int at = 0; at < natom; at++) {
+                double *v = &w[(size_t)at * ndim];
+                const double vj = v[j], vk = v[k];
+                v[j] = c * vj + s * vk;
+                v[k] = -s * vj + c * vk;
+            }
+        };
+        const int64_t nb = three ? npoints * npoints * npoints : npoints;
+        std::vector<double> bb((size_t)nb * nd), wts(nb), xs((size_t)nb * nd * n), bn(nb, betan), ang((size_t)nb * 3);
+        for (int64_t q = 0; q < nb; q++) {
+            std::vector<double> w(w2);
+            const int64_t ii = three ? q / (npoints * npoints) : 0, jj = three ? (q / npoints) % npoints : 0,
+                          kk = q % npoints;
+            if (three) {
+                rot(w, 1, et[kk]);
+                rot(w, 3, ph[jj]);
+                rot(w, 1, th[ii]);
+                wts[q] = wth[ii] * wph[jj] * wet[kk];
+                ang[3 * q] = th[ii];
+                ang[3 * q + 1] = ph[jj];
+            } else {
+                rot(w, 3, et[kk]);
+                wts[q] = wet[kk];
+            }
+            ang[3 * q + 2] = et[kk];
+            std::copy(w.begin(), w.end(), bb.begin() + q * nd);
+            std::copy(x.begin(), x.end(), xs.begin() + q * nd * n);
+        }
+        std::vector<double> um(nb), ld(nb);
+        std::vector<int64_t> its(nb), nsk(nb);
+        std::vector<int32_t> sts(nb);
+        CHECK(pg_instanton_optimize(ctx, nb, n, xs.data(), w1.data(), bb.data(), bn.data(), &o, um.data(), its.data(),
+                                    sts.data()));
+        CHECK(pg_instanton_logdet(ctx, nb, n, xs.data(), bn.data(), 0, 1, quirks, ld.data(), nullptr, nsk.data()));
+        FILE *fa = std::fopen("angularI.dat", "w");
+        if (!fa) {
+            std::fprintf(stderr, "cannot write angularI.dat\n");
+            return 1;
+        }
+        for (int64_t q = 0; q < nb; q++) {
+            double Sq, om, dq;
+            CHECK(pg_rpi_assemble(betan, um[q], ld[q], ld0, &Sq, &om, &dq));
+            double ib = std::tanh(om * (double)n);
+            if (three && om * (double)n > 1.0) ib = 1.0;
+            if (three) {
+                std::fprintf(fa, " %.17g %.17g %.17g %.17g %.17g\n", ang[3 * q], ang[3 * q + 1], ang[3 * q + 2], wts[q], ib);
+                std::printf(" %.10g %.10g %.10g %.10g %.10g %.15g\n", ang[3 * q], ang[3 * q + 1], ang[3 * q + 2], wts[q],
+                            ib, ld[q]);
+            } else {
+                std::fprintf(fa, " %.17g %.17g %.17g\n", ang[3 * q + 2], wts[q], ib);
+                std::printf(" %.10g %.10g %.10g %.15g %.15g\n", ang[3 * q + 2], wts[q], ib, ld[q], Sq);
+            }
+        }
+        std::fclose(fa);
+    }
     double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     std::printf(" Ran in %.3f s\n", secs);
     pg_destroy(ctx);

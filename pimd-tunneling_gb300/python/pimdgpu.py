@@ -28,7 +28,7 @@ EXPORTS = [
     "pg_ti_checkpoint_load", "pg_ti_release", "pg_propagate_pimd", "pg_gauleg", "pg_spline",
     "pg_splint", "pg_ti_assemble", "pg_splitting_from_ratio", "pg_instanton_fg",
     "pg_instanton_optimize", "pg_um_hessian", "pg_instanton_logdet", "pg_rpi_assemble",
-    "pg_nm_transform_noalloc", "pg_ti_advance_group",
+    "pg_nm_transform_noalloc", "pg_ti_advance_group", "pg_ti_set_accumulators",
 ]
 
 
@@ -75,6 +75,7 @@ def lib():
         L.pg_ti_advance.argtypes = [P, I64]
         L.pg_ti_advance_timed.argtypes = [P, I64, P]
         L.pg_ti_advance_group.argtypes = [P, I64, I64, P]
+        L.pg_ti_set_accumulators.argtypes = [P, P, P, I64]
         L.pg_ti_get_state.argtypes = [P, P, P]
         L.pg_ti_get_results.argtypes = [P, P, P, P, P]
         L.pg_ti_lambda_reduce.argtypes = [P, P, P, P]
@@ -242,6 +243,11 @@ class Context:
         ms = C.c_double()
         check(lib().pg_ti_advance_group(arr, len(contexts), nsteps, C.byref(ms)))
         return ms.value
+
+    def ti_set_accumulators(self, dhdr_sum, nsamples, step):
+        d = np.ascontiguousarray(dhdr_sum, dtype=np.float64)
+        n = np.ascontiguousarray(nsamples, dtype=np.int64)
+        check(lib().pg_ti_set_accumulators(self.h, _p(d), _p(n), int(step)))
 
     def ti_state(self):
         P, nr, _ = self._ti

@@ -102,3 +102,114 @@ def test_rpi_driver_matches_python_driver(drivers_built, tmp_path):
     S = float(re.search(r"s_kink=\s*(\S+)", r.stdout).group(1))
     ref = drivers.run_rpi(c, N=64, betas=[beta], m=10, factr=1e2, pgtol=1e-8)["results"][0]
     assert abs(S - ref["S"]) <= 1e-10 * abs(ref["S"])
+
+
+@pytest.mark.gpu
+def test_pimd_ti_restart_files_roundtrip(drivers_built, tmp_path):
+    """restart = 1 writes the reference's restart_proc<iproc>_<ii>.xyz files (two
+    ranks' worth here); restart = 2 without restart.ckpt reads them back: with
+    NMC = 0 the answer is unchanged, and 200 + 200 steps through the files match
+    one 400-step run."""
+    c = dict(pgconfigs.load("c0"))
+    _write_inputs(tmp_path, c, ["H"])
+
+    def text(nmc, restart):
+        return ("&MCDATA n=16, beta=%.17g, NMC=%d, dt=%.17g, imin=50, tau=1.0, gamma=%.17g, nintegral=2,\n"
+                " nrep=3, thermostat=2, ndim=1, natom=1, readpath=F, pes='1d', pes_params='pes.dat',\n"
+                " precision='fp64', form='fused', init='well', init_sigma=0.01, seed=0, restart=%d, nproc=2 /\n"
+                % (c["beta"], nmc, c["dt"], c["gamma"], restart))
+
+    def dA(out):
+        return float(re.search(r"final Delta A=\s*(\S+)", out).group(1))
+
+    r = _run("pimd_ti", text(200, 1), cwd=str(tmp_path))
+    assert r.returncode == 0, r.stderr
+    names = sorted(p.name for p in tmp_path.glob("restart_proc*.xyz"))
+    assert names == ["restart_proc0_1.xyz", "restart_proc0_2.xyz", "restart_proc0_3.xyz",
+                     "restart_proc1_1.xyz", "restart_proc1_2.xyz", "restart_proc1_3.xyz"]
+    lines = (tmp_path / "restart_proc0_1.xyz").read_text().split("\n")
+    assert lines[0].strip() == "1" and lines[2].split()[0] == "H" and len(lines) == 2 * 16 * 3 + 1
+    assert lines[16 * 3 + 1].strip() == "200"  # step count of the momentum block
+    first = dA(r.stdout)
+    (tmp_path / "restart.ckpt").unlink()
+    r = _run("pimd_ti", text(0, 2), cwd=str(tmp_path))
+    assert r.returncode == 0, r.stderr
+    assert abs(dA(r.stdout) - first) <= 1e-14 * abs(first)
+    (tmp_path / "restart.ckpt").unlink()
+    r = _run("pimd_ti", text(200, 2), cwd=str(tmp_path))
+    assert r.returncode == 0, r.stderr
+    two_legs = dA(r.stdout)
+    other = tmp_path / "one"
+    other.mkdir()
+    _write_inputs(other, c, ["H"])
+    r = _run("pimd_ti", text(400, 0), cwd=str(other))
+    assert r.returncode == 0, r.stderr
+    assert abs(two_legs - dA(r.stdout)) <= 1e-8 * abs(dA(r.stdout))
+
+
+@pytest.mark.gpu
+def test_pimd_ti_instanton_path_and_centre(drivers_built, tmp_path):
+    """readpath + instapath + centre (instantonmod.f90:895-1004) on the 2-D
+    surface: the instanton between adjacent wells is optimised on the GPU,
+    written to instanton.xyz, and the path is centred on its barrier top, which
+    the reflection symmetry of the surface puts at lambda = 1/2."""
+    c = dict(pgconfigs.load("c1"))
+    _write_inputs(tmp_path, c, ["H"])
+    w1, w2 = np.array(c["well1"]), np.array(c["well2"])
+    (tmp_path / "path.xyz").write_text("".join(" 1\n frame %d\n H %.17g %.17g\n" % (i, *w) for i, w in
+                                               enumerate((w1, w2))))
+    n = 24
+    text = ("&MCDATA n=%d, beta=%.17g, NMC=100, dt=%.17g, imin=10, tau=1.0, gamma=%.17g, nintegral=3,\n"
+            " nrep=2, thermostat=2, ndim=2, natom=1, readpath=T, npath=2, instapath=T, centre=T,\n"
+            " pes='2dtest', pes_params='pes.dat', precision='fp64', form='fused', init='path', seed=0 /\n"
+            % (n, c["beta"], c["dt"], c["gamma"]))
+    r = _run("pimd_ti", text, cwd=str(tmp_path))
+    assert r.returncode == 0, r.stderr
+    assert "Found instanton" in r.stdout
+    lines = (tmp_path / "instanton.xyz").read_text().strip().split("\n")
+    assert len(lines) == 3 * n
+    beads = np.array([[float(v) for v in lines[3 * i + 2].split()[1:]] for i in range(n)]) / 0.529177
+    # the optimised path is mirror-symmetric: bead i and bead n-1-i reflect into each other
+    mid = 0.5 * (w1 + w2)
+    u = (w2 - w1) / np.linalg.norm(w2 - w1)
+    refl = beads - 2.0 * np.outer((beads - mid) @ u, u)
+    assert np.max(np.abs(refl[::-1] - beads)) < 1e-4
+    xm = float(re.search(r"Centred,\s*\S+\s+\S+\s+(\S+)", r.stdout).group(1))
+    assert abs(xm - 0.5) < 1e-4
+    assert np.isfinite(float(re.search(r"final Delta A=\s*(\S+)", r.stdout).group(1)))
+
+
+@pytest.mark.gpu
+def test_rpi_angular_grid_batch_matches_single_solves(drivers_built, tmp_path):
+    """angular = T (rpi_ser.f90:241-348) on the 2-D surface: every orientation of
+    well 2 is re-optimised in one batched call; each row of angularI.dat equals an
+    independent single-orientation solve through the Python binding."""
+    import drivers
+    import pimdgpu as pg
+    c = dict(pgconfigs.load("c1"))
+    _write_inputs(tmp_path, c, ["H"])
+    N, npts = 16, 3
+    beta = c["beta"]
+    text = ("&RPIDATA n=%d, beta=%.17g, ndim=2, natom=1, readpath=.false., pes='2dtest', pes_params='pes.dat',\n"
+            " angular=.true., npoints=%d /\n" % (N, beta, npts))
+    r = _run("rpi", text, cwd=str(tmp_path))
+    assert r.returncode == 0, r.stderr
+    rows = np.loadtxt(tmp_path / "angularI.dat")
+    assert rows.shape == (npts, 3)
+    assert abs(rows[:, 1].sum() - 2.0 * 3.14159265358979) < 1e-12
+    betan = beta / N
+    w1, w2 = np.array(c["well1"]), np.array(c["well2"])
+    with pg.Context(0) as ctx:
+        ctx.set_system(c["ndim"], c["natom"], c["mass"], c["pes_id"], c["params"], c["V0"])
+        kw = dict(m=8, factr=1e6, pgtol=1e-5, maxiter=200000)
+        x, _, _, _ = ctx.instanton_optimize(N, drivers.linear_guess(w1, w2, N), w1, w2, [betan], **kw)
+        ld0, _, _ = ctx.instanton_logdet(N, np.repeat(w1, N), [betan], singlewell=True, skip_lowest=False)
+        eta, _ = pg.gauleg(0.0, 2.0 * 3.14159265358979, npts)
+        for k in range(npts):
+            cth, sth = np.cos(eta[k]), np.sin(eta[k])
+            b = np.array([cth * w2[0] + sth * w2[1], -sth * w2[0] + cth * w2[1]])
+            xk, UM, _, st = ctx.instanton_optimize(N, x, w1, b, [betan], **kw)
+            ld, _, _ = ctx.instanton_logdet(N, xk, [betan], singlewell=False, skip_lowest=True)
+            S, om, _ = pg.rpi_assemble(betan, UM[0], ld[0], ld0[0])
+            assert abs(rows[k, 0] - eta[k]) < 1e-14
+            np.testing.assert_allclose(rows[k, 2], np.tanh(om * N), rtol=1e-9, atol=1e-300)
