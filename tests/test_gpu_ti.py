@@ -410,3 +410,23 @@ def test_tensor_blocked_padded_small_p(ctx, pg):
     x1, p1, s1, x2, p2, s2 = _tensor_vs_simt(ctx, pg, c, ti)
     assert np.max(np.abs(x1 - x2)) < 2e-3
     np.testing.assert_allclose(s2, s1, rtol=2e-4)
+
+
+@pytest.mark.parametrize("cfgname,P", [("c1", 128), ("c2", 256)])
+def test_tensor_forms_with_cayley_rotation(ctx, pg, cfgname, P):
+    """cayley = 1 (verletmodule.f90:520-526): the per-mode rotation coefficients
+    the tensor forms apply are the Cayley ones; fused tile (P = 128) and blocked
+    (P = 256, 27 dofs) forms track the FP32 SIMT form."""
+    c = dict(pgconfigs.load(cfgname))
+    c["P"] = P
+    ti = pgconfigs.TiInputs(c, nrep=3, nintegral=2)
+    _set_system(ctx, c)
+    out = []
+    for form in (pg.PG_FORM_FUSED, pg.PG_FORM_TENSOR):
+        cfg = _gpu_cfg(pg, c, ti, pg.PG_MIXED, form, cayley=True)
+        ctx.ti_setup(cfg, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
+        assert ctx.ti_form(1)[0] == form
+        ctx.ti_advance(20)
+        out.append((ctx.ti_state()[0], ctx.ti_results()[0]))
+    assert np.max(np.abs(out[0][0] - out[1][0])) < 2e-3
+    np.testing.assert_allclose(out[1][1], out[0][1], rtol=2e-4)
