@@ -78,6 +78,8 @@ struct TiState {
     DevBuf sintab;           // 2P+2 scaled sine table, FP64
     DevBuf coef;             // natom*P ModeCoef
     DevBuf bv;               // nlambda*nd*P endpoint shifts (beadvec)
+    DevBuf bvtab;            // 3P: the sine and scale tables beadvec is formed from
+    DevBuf x0, p0;           // FP64 staging of caller-given start positions / momenta
     DevBuf dbdl;             // nlambda*nd
     DevBuf avec, bvec;       // nd start point, nlambda*nd end points
     DevBuf xref;             // nlambda*nd*P

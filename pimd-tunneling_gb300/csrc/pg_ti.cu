@@ -411,6 +411,23 @@ __global__ void k_to_double(const R *__restrict__ in, double *__restrict__ out, 
 
 __global__ void k_step_add(int64_t *step_dev, int64_t n) { *step_dev += n; }
 
+// beadvec(i, dof) of every lambda point (verletmodule.f90:326-335) from the
+// host's tables: tab[i] = sin(i pi/(P+1)), tab[P + i] = sin(P i pi/(P+1)),
+// tab[2P + i] = (lam_i betan)^2, sq = sqrt(2/(P+1)).
+__global__ void k_beadvec(const double *__restrict__ a, const double *__restrict__ b,
+                          const double *__restrict__ tab, double sq, int64_t nlambda, int nd, int P,
+                          double *__restrict__ bv) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nlambda * nd * P) return;
+    const int i = (int)(e % P);
+    const int64_t ld = e / P;
+    const int dof = (int)(ld % nd);
+    const int64_t l = ld / nd;
+    double v = a[dof] * tab[i] + b[l * nd + dof] * tab[P + i];
+    v = v * sq;
+    bv[e] = v / tab[2 * P + i];
+}
+
 // ---------------------------------------------------------------- plain form (FP64)
 // State: x (Cartesian positions), p (Cartesian momenta); scratch wq, wp.
 // step_v: p -= dt grad V(x) (verletmodule.f90:565-585); one thread per (ring, bead).
@@ -875,18 +892,18 @@ extern "C" int pg_ti_setup(pg_ctx *ctx, const pg_ti_config *cfg, int64_t nrings,
             c.bm = bm;
             coef[(size_t)k + (size_t)natom * i] = c;
         }
-    std::vector<double> bv((size_t)nlambda * nd * P);
-    for (int64_t l = 0; l < nlambda; l++)
-        for (int i = 1; i <= P; i++)
-            for (int j = 0; j < ndim; j++)
-                for (int k = 0; k < natom; k++) {
-                    int dof = k * ndim + j;
-                    double v = a[dof] * std::sin((double)i * kPiRef / (double)(P + 1)) +
-                               b[l * nd + dof] * std::sin((double)(P * i) * kPiRef / (double)(P + 1));
-                    v = v * std::sqrt(2.0 / (double)(P + 1));
-                    v = v / ((lam[i - 1] * betan) * (lam[i - 1] * betan));
-                    bv[((size_t)l * nd + dof) * P + (i - 1)] = v;
-                }
+    // beadvec tables (verletmodule.f90:326-335); the nlambda x nd x P values are
+    // formed on the device by k_beadvec
+    std::vector<double> bvtab(3 * (size_t)P);
+    for (int i = 1; i <= P; i++) {
+        bvtab[i - 1] = std::sin((double)i * kPiRef / (double)(P + 1));
+        bvtab[P + i - 1] = std::sin((double)(P * i) * kPiRef / (double)(P + 1));
+        bvtab[2 * P + i - 1] = (lam[i - 1] * betan) * (lam[i - 1] * betan);
+    }
+    const double bvsq = std::sqrt(2.0 / (double)(P + 1));
+    // the reference positions are read only to initialise rings without x0 and
+    // by dHdrlimit re-initialisation
+    const bool need_xref = !x0 || cfg->dhdr_limit >= 0.0;
 
     size_t nstate = (size_t)nrings * nd * P;
     size_t esz = st.fp32 ? sizeof(float) : sizeof(double);
@@ -902,7 +919,8 @@ extern "C" int pg_ti_setup(pg_ctx *ctx, const pg_ti_config *cfg, int64_t nrings,
     ENS(st.f, nstate * esz);
     ENS(st.T, (size_t)P * P * (sizeof(double) + sizeof(float)));
     ENS(st.coef, coef.size() * sizeof(ModeCoef));
-    ENS(st.bv, bv.size() * sizeof(double));
+    ENS(st.bv, (size_t)nlambda * nd * P * sizeof(double));
+    ENS(st.bvtab, bvtab.size() * sizeof(double));
     ENS(st.dbdl, (size_t)nlambda * nd * sizeof(double));
     ENS(st.avec, (size_t)nd * sizeof(double));
     ENS(st.bvec, (size_t)nlambda * nd * sizeof(double));
@@ -912,23 +930,33 @@ extern "C" int pg_ti_setup(pg_ctx *ctx, const pg_ti_config *cfg, int64_t nrings,
     ENS(st.ringstream, (size_t)nrings * sizeof(uint32_t));
     ENS(st.acc, (size_t)nrings * sizeof(RingAcc));
     ENS(st.red, (size_t)(3 * nlambda + 1) * sizeof(double));
-    DevBuf dx0, dp0;
-    if (x0) ENS(dx0, nstate * sizeof(double));
-    if (p0) ENS(dp0, nstate * sizeof(double));
+    if (x0) ENS(st.x0, nstate * sizeof(double));
+    if (p0) ENS(st.p0, nstate * sizeof(double));
+    DevBuf &dx0 = st.x0, &dp0 = st.p0;
 #undef ENS
     std::vector<float> Tf(T.begin(), T.end());
     cudaStream_t s = ctx->stream;
     PG_CUDA(cudaMemcpyAsync(st.T.ptr, T.data(), T.size() * sizeof(double), cudaMemcpyHostToDevice, s));
     PG_CUDA(cudaMemcpyAsync(st.T.as<double>() + (size_t)P * P, Tf.data(), Tf.size() * sizeof(float), cudaMemcpyHostToDevice, s));
     PG_CUDA(cudaMemcpyAsync(st.coef.ptr, coef.data(), coef.size() * sizeof(ModeCoef), cudaMemcpyHostToDevice, s));
-    PG_CUDA(cudaMemcpyAsync(st.bv.ptr, bv.data(), bv.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+    PG_CUDA(cudaMemcpyAsync(st.bvtab.ptr, bvtab.data(), bvtab.size() * sizeof(double), cudaMemcpyHostToDevice, s));
     PG_CUDA(cudaMemcpyAsync(st.dbdl.ptr, dbdl, (size_t)nlambda * nd * sizeof(double), cudaMemcpyHostToDevice, s));
     PG_CUDA(cudaMemcpyAsync(st.avec.ptr, a, (size_t)nd * sizeof(double), cudaMemcpyHostToDevice, s));
     PG_CUDA(cudaMemcpyAsync(st.bvec.ptr, b, (size_t)nlambda * nd * sizeof(double), cudaMemcpyHostToDevice, s));
-    if (xref)
-        PG_CUDA(cudaMemcpyAsync(st.xref.ptr, xref, (size_t)nlambda * nd * P * sizeof(double), cudaMemcpyHostToDevice, s));
-    else
-        PG_CUDA(cudaMemsetAsync(st.xref.ptr, 0, (size_t)nlambda * nd * P * sizeof(double), s));
+    {
+        const int64_t nbv = nlambda * nd * P;
+        k_beadvec<<<(unsigned)((nbv + 255) / 256), 256, 0, s>>>(st.avec.as<double>(), st.bvec.as<double>(),
+                                                               st.bvtab.as<double>(), bvsq, nlambda, nd, P,
+                                                               st.bv.as<double>());
+        PG_CUDA(cudaGetLastError());
+    }
+    if (need_xref) {
+        if (xref)
+            PG_CUDA(cudaMemcpyAsync(st.xref.ptr, xref, (size_t)nlambda * nd * P * sizeof(double),
+                                    cudaMemcpyHostToDevice, s));
+        else
+            PG_CUDA(cudaMemsetAsync(st.xref.ptr, 0, (size_t)nlambda * nd * P * sizeof(double), s));
+    }
     PG_CUDA(cudaMemcpyAsync(st.ringlam.ptr, ring_lambda, nrings * sizeof(int32_t), cudaMemcpyHostToDevice, s));
     PG_CUDA(cudaMemcpyAsync(st.ringseed.ptr, ring_seed, nrings * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
     PG_CUDA(cudaMemcpyAsync(st.ringstream.ptr, ring_stream, nrings * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
@@ -1215,34 +1243,30 @@ extern "C" int pg_ti_get_state(pg_ctx *ctx, double *x, double *p) {
     size_t n = (size_t)st.nrings * st.nd * st.P;
     cudaStream_t s = ctx->stream;
     PG_CUDA(ctx->scratch_a.ensure(n * sizeof(double)));
+    PG_CUDA(ctx->scratch_b.ensure(n * sizeof(double)));
     TiArgs ta = make_args(ctx, st, step_ptr(st));
     int th = threads_for(st.P, st.nd);
     if (st.form == PG_FORM_TENSOR) {
         rc = tc_launch(ctx, st, 0, -1, s);  // read-out: writes x, pi back to the SIMT layout
         if (rc) return rc;
     }
-    if (x) {
-        if (st.fp32) {
-            k_to_double<float><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(st.x.as<float>(), ctx->scratch_a.as<double>(), n);
-            PG_CUDA(cudaMemcpyAsync(x, ctx->scratch_a.ptr, n * sizeof(double), cudaMemcpyDeviceToHost, s));
-        } else {
-            PG_CUDA(cudaMemcpyAsync(x, st.x.ptr, n * sizeof(double), cudaMemcpyDeviceToHost, s));
-        }
-        PG_CUDA(cudaStreamSynchronize(s));
+    // both conversions first, then both copies, one wait
+    const double *xs = st.x.as<double>(), *ps = st.pi.as<double>();
+    if (x && st.fp32) {
+        k_to_double<float><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(st.x.as<float>(), ctx->scratch_a.as<double>(), n);
+        xs = ctx->scratch_a.as<double>();
     }
-    if (p) {
-        if (st.form == PG_FORM_PLAIN) {
-            PG_CUDA(cudaMemcpyAsync(p, st.pi.ptr, n * sizeof(double), cudaMemcpyDeviceToHost, s));
-        } else {
-            size_t sm = ring_smem_bytes(st.P, st.fp32);
-            if (st.fp32)
-                k_ti_momenta<float><<<(unsigned)st.nrings, th, sm, s>>>(ta, st.pi.as<float>(), ctx->scratch_a.as<double>());
-            else
-                k_ti_momenta<double><<<(unsigned)st.nrings, th, sm, s>>>(ta, st.pi.as<double>(), ctx->scratch_a.as<double>());
-            PG_CUDA(cudaGetLastError());
-            PG_CUDA(cudaMemcpyAsync(p, ctx->scratch_a.ptr, n * sizeof(double), cudaMemcpyDeviceToHost, s));
-        }
+    if (p && st.form != PG_FORM_PLAIN) {
+        size_t sm = ring_smem_bytes(st.P, st.fp32);
+        if (st.fp32)
+            k_ti_momenta<float><<<(unsigned)st.nrings, th, sm, s>>>(ta, st.pi.as<float>(), ctx->scratch_b.as<double>());
+        else
+            k_ti_momenta<double><<<(unsigned)st.nrings, th, sm, s>>>(ta, st.pi.as<double>(), ctx->scratch_b.as<double>());
+        ps = ctx->scratch_b.as<double>();
     }
+    PG_CUDA(cudaGetLastError());
+    if (x) PG_CUDA(cudaMemcpyAsync(x, xs, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (p) PG_CUDA(cudaMemcpyAsync(p, ps, n * sizeof(double), cudaMemcpyDeviceToHost, s));
     PG_CUDA(cudaStreamSynchronize(s));
     return PG_OK;
 }
