@@ -202,14 +202,15 @@ def _extras(ctx, pg, cfg, ti, M, K, value, ws, beads, extras):
     ph = torch.from_numpy(p0).pin_memory().numpy()
     bseq = ti.b
     dseq = ti.dbdl
+    bl = np.ascontiguousarray(bseq[ti.ring_lambda])
+    dl = np.ascontiguousarray(dseq[ti.ring_lambda])
     for _ in range(2):
-        ctx.propagate_pimd(cfg, M, ti.a, bseq[ti.ring_lambda], dseq[ti.ring_lambda], ti.ring_seed,
-                           ti.ring_stream, xh, ph)
+        ctx.propagate_pimd(cfg, M, ti.a, bl, dl, ti.ring_seed, ti.ring_stream, xh, ph, inplace=True)
     te = []
     for _ in range(max(3, K // 2)):
         t0 = time.perf_counter()
-        xo, po, dh, _ = ctx.propagate_pimd(cfg, M, ti.a, bseq[ti.ring_lambda], dseq[ti.ring_lambda],
-                                           ti.ring_seed, ti.ring_stream, xh, ph)
+        xo, po, dh, _ = ctx.propagate_pimd(cfg, M, ti.a, bl, dl, ti.ring_seed, ti.ring_stream, xh, ph,
+                                           inplace=True)
         te.append(time.perf_counter() - t0)
     e2e_s = statistics.median(te)
     h2d = xh.nbytes + ph.nbytes

@@ -87,6 +87,7 @@ struct TiState {
     DevBuf acc;              // nrings RingAcc
     DevBuf red;              // reduction output
     std::map<int64_t, cudaGraphExec_t> graphs;
+    std::string graph_sig;   // signature of the batch the graphs were captured for
     ~TiState();
 };
 

@@ -784,6 +784,30 @@ int ti_release(pg_ctx *ctx) {
     return PG_OK;
 }
 
+// Everything a captured advance graph bakes into its launches: the batch
+// shape and configuration, the surface and masses (the tensor kernels take
+// surface constants by value), and every device buffer address.
+static std::string graph_signature(const pg_ctx *ctx, const TiState &st) {
+    std::string sig;
+    auto add = [&](const void *p, size_t n) { sig.append(reinterpret_cast<const char *>(p), n); };
+    add(&st.cfg, sizeof(st.cfg));
+    add(&st.nrings, sizeof(st.nrings));
+    add(&st.nlambda, sizeof(st.nlambda));
+    int ints[6] = {st.P, st.nd, st.form, st.tc_blocked, st.fp32 ? 1 : 0, ctx->sm_count};
+    add(ints, sizeof(ints));
+    int sys[4] = {ctx->pes_id, ctx->ndim, ctx->natom, ctx->nd};
+    add(sys, sizeof(sys));
+    add(&ctx->V0, sizeof(double));
+    add(ctx->params.data(), ctx->params.size() * sizeof(double));
+    add(ctx->mass.data(), ctx->mass.size() * sizeof(double));
+    const void *ptrs[] = {st.q.ptr, st.pi.ptr, st.x.ptr, st.f.ptr, st.T.ptr, st.Tbf.ptr, st.coef.ptr, st.bv.ptr,
+                          st.dbdl.ptr, st.avec.ptr, st.bvec.ptr, st.xref.ptr, st.ringlam.ptr, st.ringseed.ptr,
+                          st.ringstream.ptr, st.acc.ptr, st.red.ptr, ctx->d_params.ptr, ctx->d_fparams.ptr,
+                          ctx->d_mass.ptr};
+    add(ptrs, sizeof(ptrs));
+    return sig;
+}
+
 static int resolve_form(pg_ctx *ctx, TiState &st) {
     int form = st.cfg.form;
     if (st.cfg.precision == PG_FP64) {
@@ -839,12 +863,11 @@ extern "C" int pg_ti_setup(pg_ctx *ctx, const pg_ti_config *cfg, int64_t nrings,
     for (int64_t r = 0; r < nrings; r++)
         if (ring_lambda[r] < 0 || ring_lambda[r] >= nlambda) return fail(PG_ERR_ARG, "ring_lambda out of range");
 
-    // Reuse the device buffers of a previous batch (ensure() only grows them);
-    // captured graphs hold the old arguments and are dropped.
+    // Reuse the device buffers of a previous batch (ensure() only grows them).
+    // Captured graphs bake in launch arguments: they are kept only when the
+    // new batch has the same signature (see graph_signature), else dropped.
     if (!ctx->ti) ctx->ti = new TiState();
     TiState &st = *ctx->ti;
-    for (auto &kv : st.graphs) cudaGraphExecDestroy(kv.second);
-    st.graphs.clear();
     st.cfg = *cfg;
     st.nrings = nrings;
     st.nlambda = nlambda;
@@ -934,6 +957,14 @@ extern "C" int pg_ti_setup(pg_ctx *ctx, const pg_ti_config *cfg, int64_t nrings,
     if (p0) ENS(st.p0, nstate * sizeof(double));
     DevBuf &dx0 = st.x0, &dp0 = st.p0;
 #undef ENS
+    {
+        const std::string sig = graph_signature(ctx, st);
+        if (sig != st.graph_sig) {
+            for (auto &kv : st.graphs) cudaGraphExecDestroy(kv.second);
+            st.graphs.clear();
+            st.graph_sig = sig;
+        }
+    }
     std::vector<float> Tf(T.begin(), T.end());
     cudaStream_t s = ctx->stream;
     PG_CUDA(cudaMemcpyAsync(st.T.ptr, T.data(), T.size() * sizeof(double), cudaMemcpyHostToDevice, s));

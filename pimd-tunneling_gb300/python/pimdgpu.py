@@ -304,10 +304,19 @@ class Context:
     def ti_release(self):
         check(lib().pg_ti_release(self.h))
 
-    def propagate_pimd(self, cfg, nmc, a, b, dbdl, seed, stream, x, p):
+    def propagate_pimd(self, cfg, nmc, a, b, dbdl, seed, stream, x, p, inplace=False):
+        """A batch of propagate_pimd_pile / _nm calls.  inplace=True updates the
+        caller's contiguous float64 x and p (the reference's inout arrays, and
+        what the C-ABI does; pinned arrays then copy at full speed); otherwise
+        copies are returned."""
         a, b, dbdl = map(_f64, (a, b, dbdl))
-        x = np.array(x, dtype=np.float64)
-        p = np.array(p, dtype=np.float64)
+        if inplace:
+            if not (isinstance(x, np.ndarray) and isinstance(p, np.ndarray) and x.dtype == np.float64
+                    and p.dtype == np.float64 and x.flags.c_contiguous and p.flags.c_contiguous):
+                raise ValueError("inplace=True needs contiguous float64 arrays")
+        else:
+            x = np.array(x, dtype=np.float64)
+            p = np.array(p, dtype=np.float64)
         nt = b.size // self.ndof
         sd = np.ascontiguousarray(seed, dtype=np.uint64)
         stv = np.ascontiguousarray(stream, dtype=np.uint32)
