@@ -109,19 +109,25 @@ def _dist():
     return ws, rank, local
 
 
-def _workload(rank):
+def _workload(rank, name="c1"):
     import pgconfigs
-    c = dict(pgconfigs.load("c1"))
-    # weak scaling: every rank runs its own 1024 trajectories (distinct seeds)
-    c["seeds"] = [s + 1024 * rank for s in range(1024)]
+    c = dict(pgconfigs.load(name))
+    # weak scaling: every rank runs its own trajectories (distinct seeds)
+    nrep = int(c.get("nrep", 1))
+    c["seeds"] = [s + nrep * rank for s in range(nrep)]
     ti = pgconfigs.TiInputs(c)
     return c, ti
 
 
-def _config(M, form):
+WORKLOADS = {
+    "c1": "c1: mcmod_2dtest surface, P=128, 1024 traj x 16 lambda = 16384 rings per GPU",
+    "c2": "c2: synthetic 9-atom surface (27 dof), P=256, 256 traj x 12 lambda = 3072 rings per GPU",
+}
+
+
+def _config(M, form, name="c1"):
     """The workload description shared by both arms."""
-    return {"workload": "c1: mcmod_2dtest surface, P=128, 1024 traj x 16 lambda = 16384 rings per GPU, "
-                        "Langevin, %d MD steps per bench step" % M,
+    return {"workload": WORKLOADS[name] + ", Langevin, %d MD steps per bench step" % M,
             "precision": "FP32 forces/state, split-BF16 NM transform, FP64 estimator",
             "l2": "flushed (256 MB write) between timed steps", "form": form}
 
@@ -162,8 +168,8 @@ def cpu_reference_rate(c, ti, target_s=12.0, nthreads=None):
     nsteps = max(20, int(target_s * rate_ring_steps / nr))
     dt = run(nr, nsteps)
     value = nr * nsteps * P / dt
-    sample = ("%d rings x %d MD steps of the workload (P=%d, 2-D six-well surface), reference step "
-              "order (10 dense NM transforms per step), FP64, %d threads, %.1f s" % (nr, nsteps, P, nthreads, dt))
+    sample = ("%d rings x %d MD steps of the workload (P=%d, %d dofs), reference step "
+              "order (10 dense NM transforms per step), FP64, %d threads, %.1f s" % (nr, nsteps, P, nd, nthreads, dt))
     return value, nthreads, sample
 
 
@@ -171,7 +177,7 @@ def run_reference(args):
     ws, rank, _ = _dist()
     if rank != 0:
         return 0
-    c, ti = _workload(0)
+    c, ti = _workload(0, args.workload)
     vals = []
     for _ in range(max(args.warmup, 0)):
         cpu_reference_rate(c, ti, target_s=1.0)
@@ -185,7 +191,7 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": _config(args.md_per_step, args.form),
+            "config": _config(args.md_per_step, args.form, args.workload),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "the reference Fortran/MKL/MPI build cannot be compiled here (no Fortran compiler, "
@@ -239,6 +245,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-extras", action="store_true", help="skip the e2e and FP64 legs")
     ap.add_argument("--form", default="auto", choices=["auto", "fused", "tensor"])
+    ap.add_argument("--workload", default="c1", choices=sorted(WORKLOADS),
+                    help="c1 (the headline configuration) or c2 (27-dof surface, P = 256)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -257,7 +265,7 @@ def main():
         dist.barrier()
     import pimdgpu as pg
 
-    c, ti = _workload(rank)
+    c, ti = _workload(rank, args.workload)
     ctx = pg.Context(local)
     ctx.set_system(c["ndim"], c["natom"], c["mass"], c["pes_id"], c["params"], c["V0"])
     form = {"auto": pg.PG_FORM_AUTO, "fused": pg.PG_FORM_FUSED, "tensor": pg.PG_FORM_TENSOR}[args.form]
@@ -305,7 +313,7 @@ def main():
         achieved_gbs = kbytes / (kms / 1e3) / 1e9
         traffic = None
         try:
-            with open(os.path.join(ROOT, "profiles", "k_tc_step_c1_traffic.json")) as f:
+            with open(os.path.join(ROOT, "profiles", "tensor_kernels_traffic.json")) as f:
                 traffic = json.load(f).get(name.split()[0])
         except Exception:
             pass
@@ -330,7 +338,7 @@ def main():
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
             "ms_per_step": kernel_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
-            "config": _config(M, args.form),
+            "config": _config(M, args.form, args.workload),
             "roofline": roof, "clocks": clocks, "gpu_launches": K * launches_per_step, "wall_s": wall,
             "form": {pg.PG_FORM_FUSED: "fused-simt", pg.PG_FORM_TENSOR: "tcgen05", pg.PG_FORM_PLAIN: "plain"}[form_used],
             "nan_rings": nan_rings}
