@@ -400,6 +400,8 @@ struct TileAux {
     float xP[kNc];       // bead-P position for the estimator
     uint64_t seed[kNc];  // Philox key of the column's ring
     uint32_t stream[kNc];
+    int32_t jdof[kNc];   // the column's dof index within its ring
+    int32_t atom[kNc];   // the column's atom
 };
 
 __device__ __forceinline__ void mma_bf16_n64(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t acc) {
@@ -1123,13 +1125,16 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tb_kick(TbArgs a) {
     if (tid < kNc) {
         uint64_t sd = 0;
         uint32_t sm = 0;
+        const int64_t ring = (col0 + tid) / nd;
+        const int j = (int)(col0 + tid - ring * nd);
         if (tid < nvalid) {
-            const int64_t ring = (col0 + tid) / nd;
             sd = a.ringseed[ring];
             sm = a.ringstream[ring];
         }
         ax->seed[tid] = sd;
         ax->stream[tid] = sm;
+        ax->jdof[tid] = j;
+        ax->atom[tid] = j / a.ndim;
     }
     const uint32_t tmem = tb_begin(sh, a.mb);
     uint32_t phase = 0;
@@ -1157,8 +1162,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tb_kick(TbArgs a) {
                     const bool in = m < P && i < nvg;
                     qv[i] = in ? qo[(size_t)i * P] : 0.f;
                     pv[i] = in ? po[(size_t)i * P] : 0.f;
-                    const int jc = (int)((col0 + cb + c0 + i) % nd);
-                    const float *cf = a.coef + ((size_t)(jc / a.ndim) * P + mc) * 8;
+                    const float *cf = a.coef + ((size_t)ax->atom[cb + c0 + i] * P + mc) * 8;
                     cfa[i] = __ldg(reinterpret_cast<const float4 *>(cf));
                     cfb[i] = __ldg(reinterpret_cast<const float2 *>(cf + 4));
                 }
@@ -1169,9 +1173,8 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tb_kick(TbArgs a) {
                 for (int g = 0; g < kGrp / 4; g++) {
                     // normals j P + 4 (m / 4) .. + 3 of column c0 + 4g + e, transposed within the quad
                     const int cc = cb + c0 + 4 * g + e;
-                    const int j = (int)((col0 + cc) % nd);
                     const U4 o = philox_block(ax->seed[cc], ax->stream[cc], (uint32_t)s, kRngLangevin,
-                                              (uint32_t)((j * P + m) >> 2));
+                                              (uint32_t)((ax->jdof[cc] * P + m) >> 2));
                     float z[4];
                     box_muller_f(o.x, o.y, z[0], z[1]);
                     box_muller_f(o.z, o.w, z[2], z[3]);
