@@ -112,6 +112,40 @@ module pimdgpu
        integer(c_int64_t), value :: nsteps
      end function pg_ti_advance
 
+     ! one context per bead number, advanced together on concurrent streams
+     integer(c_int) function pg_ti_advance_group(ctxs, nctx, nsteps, device_ms) &
+          bind(c, name="pg_ti_advance_group")
+       import :: c_int, c_int64_t, c_double, c_ptr
+       type(c_ptr), intent(in) :: ctxs(*)
+       integer(c_int64_t), value :: nctx, nsteps
+       real(c_double), intent(out) :: device_ms
+     end function pg_ti_advance_group
+
+     ! restart continuation: dHdr sums, sample counts and the step counter
+     integer(c_int) function pg_ti_set_accumulators(ctx, dhdr_sum, nsamples, step) &
+          bind(c, name="pg_ti_set_accumulators")
+       import :: c_int, c_int64_t, c_double, c_ptr
+       type(c_ptr), value :: ctx
+       real(c_double), intent(in) :: dhdr_sum(*)
+       integer(c_int64_t), intent(in) :: nsamples(*)
+       integer(c_int64_t), value :: step
+     end function pg_ti_set_accumulators
+
+     integer(c_int) function pg_ti_get_state(ctx, x, p) bind(c, name="pg_ti_get_state")
+       import :: c_int, c_double, c_ptr
+       type(c_ptr), value :: ctx
+       real(c_double), intent(out) :: x(*), p(*)
+     end function pg_ti_get_state
+
+     integer(c_int) function pg_ti_get_results(ctx, dhdr_sum, nsamples, nreinit, status) &
+          bind(c, name="pg_ti_get_results")
+       import :: c_int, c_int32_t, c_int64_t, c_double, c_ptr
+       type(c_ptr), value :: ctx
+       real(c_double), intent(out) :: dhdr_sum(*)
+       integer(c_int64_t), intent(out) :: nsamples(*), nreinit(*)
+       integer(c_int32_t), intent(out) :: status(*)
+     end function pg_ti_get_results
+
      integer(c_int) function pg_ti_lambda_reduce(ctx, mean, var, count) bind(c, name="pg_ti_lambda_reduce")
        import :: c_int, c_int64_t, c_double, c_ptr
        type(c_ptr), value :: ctx
