@@ -273,15 +273,14 @@ __device__ __forceinline__ R pes_harm(const PesArgs &pa, const R *x, R *g) {
     return v - (R)pa.V0;
 }
 
-// Square root and division in the surfaces: the IEEE operations of the CPU
-// restatement in FP64; in FP32 the hardware approximations (rsqrt, fast
-// divide: relative error ~1e-7, below the rounding of the FP32 state).
+// Square root and division in the surfaces: IEEE in both precisions.  (An
+// rsqrt-based square root and the fast divide in FP32 let one ring of the
+// 18-atom surface at P = 512 run away within 100 steps where the IEEE
+// operations, and FP64, keep it bounded.)
 template <typename R> __device__ __forceinline__ R my_sqrt(R v);
 template <> __device__ __forceinline__ double my_sqrt<double>(double v) { return sqrt(v); }
-template <> __device__ __forceinline__ float my_sqrt<float>(float v) { return v > 0.f ? v * rsqrtf(v) : 0.f; }
-template <typename R> __device__ __forceinline__ R pdiv(R a, R b);
-template <> __device__ __forceinline__ double pdiv<double>(double a, double b) { return a / b; }
-template <> __device__ __forceinline__ float pdiv<float>(float a, float b) { return __fdividef(a, b); }
+template <> __device__ __forceinline__ float my_sqrt<float>(float v) { return sqrtf(v); }
+template <typename R> __device__ __forceinline__ R pdiv(R a, R b) { return a / b; }
 template <typename R> __device__ __forceinline__ R my_exp(R v);
 template <> __device__ __forceinline__ double my_exp<double>(double v) { return exp(v); }
 template <> __device__ __forceinline__ float my_exp<float>(float v) { return __expf(v); }

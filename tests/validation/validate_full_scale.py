@@ -98,7 +98,13 @@ def part_c4(out, nmc=None):
     c = pgconfigs.load("c4")
     mixed = drivers.run_ti_mixed(c, precision=pg.PG_MIXED, nmc=nmc, chunk=500)
     simt = drivers.run_ti_mixed(c, precision=pg.PG_MIXED, form=pg.PG_FORM_FUSED, nmc=nmc, chunk=500)
-    out["c4"] = dict(mixed=mixed, mixed_simt=simt)
+    # FP64 on a shorter run (GB300's FP64 rate), against mixed precision on the same steps
+    short = min(int(nmc if nmc is not None else c["nmc"]), 1000)
+    fp64 = drivers.run_ti_mixed(c, precision=pg.PG_FP64, nmc=short, chunk=250)
+    mixed_short = drivers.run_ti_mixed(c, precision=pg.PG_MIXED, nmc=short, chunk=500)
+    diff = [m["ln_qratio"] - f["ln_qratio"] for m, f in zip(mixed_short["per_P"], fp64["per_P"])]
+    out["c4"] = dict(mixed=mixed, mixed_simt=simt, fp64_short=fp64, mixed_short=mixed_short,
+                     ln_qratio_diff_mixed_minus_fp64_short=diff)
 
 
 def part_c3(out, factr=1e2, pgtol=1e-8):
