@@ -573,6 +573,76 @@ __device__ __forceinline__ void grad_2d_n(const TcArgs &a, const float (&xv)[2 *
     }
 }
 
+// Packed FP32 pairs (two lanes per register pair, Blackwell f32x2 ops).
+__device__ __forceinline__ uint64_t pk2(float a, float b) {
+    uint64_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void upk2(uint64_t v, float &a, float &b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ uint64_t ffma2(uint64_t a, uint64_t b, uint64_t c) {
+    uint64_t d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ uint64_t fmul2(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t fadd2(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ float ex2f(float v) {
+    float r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(v));
+    return r;
+}
+
+// The POW10 six-well gradient of grad_2d_n for NR beads (NR even), two rings
+// per packed f32x2 operation: per well dx, dy, u = dx^2 + dy^2,
+// eb = 2^(u (-b0 log2 e)), ea = eb^10, cc = a0 ea + b0 eb, g += cc d.
+template <int NR>
+__device__ __forceinline__ void grad_2d_pow10_x2(const TcArgs &a, const float (&xv)[2 * NR], float (&gx)[NR],
+                                                 float (&gy)[NR]) {
+    static_assert(NR % 2 == 0, "pairs of rings");
+    uint64_t X[NR / 2], Y[NR / 2], GX[NR / 2], GY[NR / 2];
+#pragma unroll
+    for (int r = 0; r < NR / 2; r++) {
+        X[r] = pk2(xv[4 * r], xv[4 * r + 2]);
+        Y[r] = pk2(xv[4 * r + 1], xv[4 * r + 3]);
+        GX[r] = pk2(0.f, 0.f);
+        GY[r] = pk2(0.f, 0.f);
+    }
+    const float nb = -a.b0 * 1.4426950408889634f;
+    const uint64_t A0 = pk2(a.a0, a.a0), B0 = pk2(a.b0, a.b0), NB = pk2(nb, nb);
+    for (int k = 0; k < a.nwell; k++) {
+        const uint64_t MWX = pk2(-a.wc[2 * k], -a.wc[2 * k]), MWY = pk2(-a.wc[2 * k + 1], -a.wc[2 * k + 1]);
+#pragma unroll
+        for (int r = 0; r < NR / 2; r++) {
+            const uint64_t dx = fadd2(X[r], MWX), dy = fadd2(Y[r], MWY);
+            const uint64_t u = ffma2(dy, dy, fmul2(dx, dx));
+            float t0, t1;
+            upk2(fmul2(u, NB), t0, t1);
+            const uint64_t eb = pk2(ex2f(t0), ex2f(t1));
+            const uint64_t e2 = fmul2(eb, eb), e4 = fmul2(e2, e2), e8 = fmul2(e4, e4);
+            const uint64_t ea = fmul2(e8, e2);
+            const uint64_t cc = ffma2(B0, eb, fmul2(A0, ea));
+            GX[r] = ffma2(cc, dx, GX[r]);
+            GY[r] = ffma2(cc, dy, GY[r]);
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < NR / 2; r++) {
+        upk2(GX[r], gx[2 * r], gx[2 * r + 1]);
+        upk2(GY[r], gy[2 * r], gy[2 * r + 1]);
+    }
+}
+
 // Forces of kGrp columns of one bead (PESK 2: kGrp/2 rings of the 2-D surface;
 // PESK 1: kGrp rings of the 1-D quartic).
 template <int PESK>
@@ -581,7 +651,7 @@ __device__ __forceinline__ void group_forces(const TcArgs &a, const float (&xv)[
         constexpr int NR = kGrp / 2;
         float gx[NR], gy[NR];
         if (a.pow10)
-            grad_2d_n<true, NR>(a, xv, gx, gy);
+            grad_2d_pow10_x2<NR>(a, xv, gx, gy);
         else
             grad_2d_n<false, NR>(a, xv, gx, gy);
 #pragma unroll
