@@ -42,6 +42,8 @@ extern "C" {
 #define PG_PES_SYNTH9 3    /* 9-atom Morse network + quartic proton-transfer well */
 #define PG_PES_SYNTH18 4   /* 18-atom flexible water hexamer (harmonic + LJ + charges) */
 #define PG_PES_HARMONIC 5  /* V = k/2 |x|^2, analytic test surface */
+#define PG_PES_DISTGAUSS 6 /* Morse + 1/2/3-D Gaussians in interatomic distances, tables as parameters:
+                              the form of pes_malonaldehyde.f90 (layout in pg_device.cuh) */
 
 /* Precision of the TI propagation. */
 #define PG_FP64 0          /* FP64 everywhere */

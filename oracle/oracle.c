@@ -244,6 +244,74 @@ static double v_synth18(const or_pes *pes, const double *x, double *g) {
     return v - pes->V0;
 }
 
+/* Morse terms and 1-, 2-, 3-D Gaussians in the interatomic distances, the
+ * functional form of pes_malonaldehyde.f90 (distances :9357-9365, v_morse
+ * :9598-9610, v_gauss :9650-9670, energy sums :9406-9440); the gradient by
+ * the chain rule through the distances (the B matrix of :9368-9384).
+ * params = [natom, shift, nmorse, ng1, ng2, ng3, nmorse x (k, re, al, de),
+ *           ng1 x (k, x, a, d, s), ng2 x (k1, k2, x1, x2, a1, a2, d, s),
+ *           ng3 x (k1, k2, k3, x1, x2, x3, a1, a2, a3, d, s)],
+ * k = i (i - 1) / 2 + j for atoms i > j (0-based). */
+static double v_distgauss(const or_pes *pes, const double *x, double *g) {
+    const double *pp = pes->params;
+    const int na = pes->natom, npair = na * (na - 1) / 2;
+    double *r = (double *)calloc((size_t)npair, sizeof(double));
+    double *dv = (double *)calloc((size_t)npair, sizeof(double));
+    int k = 0;
+    for (int i = 1; i < na; i++)
+        for (int j = 0; j < i; j++) {
+            double s2 = 0.0;
+            for (int c = 0; c < 3; c++) s2 += (x[3 * i + c] - x[3 * j + c]) * (x[3 * i + c] - x[3 * j + c]);
+            r[k++] = sqrt(s2);
+        }
+    double v = pp[1];
+    const int nm = (int)pp[2], n1 = (int)pp[3], n2 = (int)pp[4], n3 = (int)pp[5];
+    const double *q = pp + 6;
+    for (int t = 0; t < nm; t++, q += 4) {
+        int kk = (int)q[0];
+        double e = exp(q[2] * (q[1] - r[kk])), w = e - 1.0;
+        v += (q[3] * w) * (q[3] * w);
+        dv[kk] -= 2.0 * q[3] * q[3] * w * e * q[2];
+    }
+    for (int t = 0; t < n1; t++, q += 5) {
+        int kk = (int)q[0];
+        double u = r[kk] - q[1], e = exp(-0.5 * q[2] * u * u);
+        v += q[3] * (e - q[4]);
+        dv[kk] -= q[3] * e * q[2] * u;
+    }
+    for (int t = 0; t < n2; t++, q += 8) {
+        int k1 = (int)q[0], k2 = (int)q[1];
+        double u1 = r[k1] - q[2], u2 = r[k2] - q[3];
+        double e = exp(-0.5 * (q[4] * u1 * u1 + q[5] * u2 * u2));
+        v += q[6] * (e - q[7]);
+        dv[k1] -= q[6] * e * q[4] * u1;
+        dv[k2] -= q[6] * e * q[5] * u2;
+    }
+    for (int t = 0; t < n3; t++, q += 11) {
+        int k1 = (int)q[0], k2 = (int)q[1], k3 = (int)q[2];
+        double u1 = r[k1] - q[3], u2 = r[k2] - q[4], u3 = r[k3] - q[5];
+        double e = exp(-0.5 * (q[6] * u1 * u1 + q[7] * u2 * u2 + q[8] * u3 * u3));
+        v += q[9] * (e - q[10]);
+        dv[k1] -= q[9] * e * q[6] * u1;
+        dv[k2] -= q[9] * e * q[7] * u2;
+        dv[k3] -= q[9] * e * q[8] * u3;
+    }
+    if (g) {
+        memset(g, 0, sizeof(double) * 3 * na);
+        k = 0;
+        for (int i = 1; i < na; i++)
+            for (int j = 0; j < i; j++, k++)
+                for (int c = 0; c < 3; c++) {
+                    double d = (x[3 * i + c] - x[3 * j + c]) / r[k];
+                    g[3 * i + c] += dv[k] * d;
+                    g[3 * j + c] -= dv[k] * d;
+                }
+    }
+    free(r);
+    free(dv);
+    return v - pes->V0;
+}
+
 static double pes_eval(const or_pes *pes, const double *x, double *g) {
     switch (pes->id) {
     case OR_PES_1D: return v_1d(pes, x, g);
@@ -251,6 +319,7 @@ static double pes_eval(const or_pes *pes, const double *x, double *g) {
     case OR_PES_SYNTH9: return v_synth9(pes, x, g);
     case OR_PES_SYNTH18: return v_synth18(pes, x, g);
     case OR_PES_HARMONIC: return v_harm(pes, x, g);
+    case OR_PES_DISTGAUSS: return v_distgauss(pes, x, g);
     default: return NAN;
     }
 }

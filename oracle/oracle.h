@@ -35,7 +35,7 @@ extern "C" {
 
 /* PES identifiers (same numbering as the product library). */
 enum { OR_PES_1D = 1, OR_PES_2DTEST = 2, OR_PES_SYNTH9 = 3, OR_PES_SYNTH18 = 4,
-       OR_PES_HARMONIC = 5 };
+       OR_PES_HARMONIC = 5, OR_PES_DISTGAUSS = 6 };
 
 typedef struct or_pes {
     int32_t id;

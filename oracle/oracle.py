@@ -22,7 +22,7 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB = None
 
-PES_1D, PES_2DTEST, PES_SYNTH9, PES_SYNTH18, PES_HARMONIC = 1, 2, 3, 4, 5
+PES_1D, PES_2DTEST, PES_SYNTH9, PES_SYNTH18, PES_HARMONIC, PES_DISTGAUSS = 1, 2, 3, 4, 5, 6
 PI_REF = 3.14159265358979
 
 

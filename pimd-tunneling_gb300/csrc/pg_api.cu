@@ -166,7 +166,7 @@ extern "C" int pg_set_system(pg_ctx *ctx, int64_t ndim, int64_t natom, const dou
     if (ndim < 1 || natom < 1 || ndim * natom > kMaxDof)
         return fail(PG_ERR_ARG, "ndim*natom must be in [1, 64]");
     if (!mass) return fail(PG_ERR_ARG, "mass is NULL");
-    if (pes_id < PG_PES_1D || pes_id > PG_PES_HARMONIC) return fail(PG_ERR_ARG, "unknown pes_id");
+    if (pes_id < PG_PES_1D || pes_id > PG_PES_DISTGAUSS) return fail(PG_ERR_ARG, "unknown pes_id");
     if (nparams < 0 || (nparams > 0 && !params)) return fail(PG_ERR_ARG, "bad params");
     if (pes_id == PG_PES_2DTEST && (ndim * natom != 2)) return fail(PG_ERR_ARG, "2dtest needs ndof = 2");
     if (pes_id == PG_PES_2DTEST && nparams >= 1 && (params[0] < 1 || params[0] > 6))
@@ -191,6 +191,22 @@ extern "C" int pg_set_system(pg_ctx *ctx, int64_t ndim, int64_t natom, const dou
     if (pes_id == PG_PES_SYNTH18) {
         if (nparams < 9 || (int64_t)params[0] * 3 != natom)
             return fail(PG_ERR_ARG, "synth18 needs 9 parameters and natom = 3*nmol");
+    }
+    if (pes_id == PG_PES_DISTGAUSS) {
+        if (ndim != 3 || natom < 2) return fail(PG_ERR_ARG, "distgauss needs ndim = 3 and natom >= 2");
+        if (nparams < 6 || (int64_t)params[0] != natom) return fail(PG_ERR_ARG, "distgauss header: natom mismatch");
+        const int64_t nm = (int64_t)params[2], n1 = (int64_t)params[3], n2 = (int64_t)params[4],
+                      n3 = (int64_t)params[5];
+        if (nm < 0 || n1 < 0 || n2 < 0 || n3 < 0 || nparams != 6 + 4 * nm + 5 * n1 + 8 * n2 + 11 * n3)
+            return fail(PG_ERR_ARG, "distgauss: parameter count does not match the term counts");
+        const int64_t npair = natom * (natom - 1) / 2;
+        const double *q = params + 6;
+        const int64_t width[4] = {4, 5, 8, 11}, nidx[4] = {1, 1, 2, 3}, count[4] = {nm, n1, n2, n3};
+        for (int t = 0; t < 4; t++)
+            for (int64_t i = 0; i < count[t]; i++, q += width[t])
+                for (int64_t c = 0; c < nidx[t]; c++)
+                    if (!(q[c] >= 0.0 && q[c] < (double)npair && q[c] == std::floor(q[c])))
+                        return fail(PG_ERR_ARG, "distgauss: distance index out of range");
     }
     for (int64_t i = 0; i < natom; i++)
         if (!(mass[i] > 0.0)) return fail(PG_ERR_ARG, "masses must be positive");
@@ -271,7 +287,7 @@ extern "C" int pg_pes_hessian(pg_ctx *ctx, int64_t nconf, const double *x, doubl
     PG_CUDA(ctx->scratch_a.ensure(nx * sizeof(double)));
     PG_CUDA(ctx->scratch_b.ensure(nh * sizeof(double)));
     PG_CUDA(cudaMemcpyAsync(ctx->scratch_a.ptr, x, nx * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-    int fd = (ctx->pes_id == PG_PES_1D || ctx->pes_id == PG_PES_SYNTH18) ? 1 : 0;
+    int fd = (ctx->pes_id == PG_PES_1D || ctx->pes_id == PG_PES_SYNTH18 || ctx->pes_id == PG_PES_DISTGAUSS) ? 1 : 0;
     int64_t nthreads = fd ? nconf * ctx->nd : nconf;
     int bs = 128;
     k_pes_hessian<<<(unsigned)((nthreads + bs - 1) / bs), bs, 0, ctx->stream>>>(

@@ -165,7 +165,9 @@ __device__ __forceinline__ int64_t poisson_d(uint64_t seed, uint32_t stream, uin
 //   SYNTH9:   [npair, (i, j, D, a, r0) x npair, iH, iO1, iO2, B, s0]
 //   SYNTH18:  [nmol, kr, re, ktheta, theta_e, eps, sigma, qO, qH]
 //   HARMONIC: [k]
-enum : int { kPes1D = 1, kPes2D = 2, kPesSynth9 = 3, kPesSynth18 = 4, kPesHarm = 5 };
+//   DISTGAUSS: [natom, shift, nmorse, ng1, ng2, ng3, terms...] (pes_distgauss)
+enum : int { kPes1D = 1, kPes2D = 2, kPesSynth9 = 3, kPesSynth18 = 4, kPesHarm = 5, kPesDistGauss = 6 };
+constexpr int kMaxDofPes = 64;  // = kMaxDof (the largest surface: 18 atoms x 3 = 54 dofs)
 
 struct PesArgs {
     int id, ndim, natom, nd, nparams;
@@ -419,6 +421,84 @@ __device__ __forceinline__ R pes_synth18(const PesArgs &pa, const R *x, R *g) {
 }
 
 // Generic dispatch (FP64 and the generic FP32 path).
+// Morse terms and 1-, 2- and 3-D Gaussians in the interatomic distances: the
+// functional form of pes_malonaldehyde.f90 (distances :9357-9365, v_morse
+// :9598-9610, v_gauss :9650-9670, the energy sums :9406-9440), with the term
+// tables as parameters:
+//   [natom, shift, nmorse, ng1, ng2, ng3,
+//    nmorse x (k, re, al, de)                          (de (e^{al (re - r_k)} - 1))^2
+//    ng1 x (k, x, a, d, s)                             d (e^{-a (r_k - x)^2 / 2} - s)
+//    ng2 x (k1, k2, x1, x2, a1, a2, d, s)              d (e^{-(a1 u1^2 + a2 u2^2) / 2} - s)
+//    ng3 x (k1, k2, k3, x1, x2, x3, a1, a2, a3, d, s)]
+// where r_k is the distance of atom pair k: i > j, k = i (i - 1) / 2 + j
+// (0-based), the reference's ordering.  V = shift + sum of terms - V0.
+constexpr int kMaxPairs = (kMaxDofPes / 3) * (kMaxDofPes / 3 - 1) / 2;
+template <typename R>
+__device__ R pes_distgauss(const PesArgs &pa, const R *x, R *g) {
+    const R *pp = pes_params<R>(pa);
+    const int na = pa.natom;
+    R r[kMaxPairs], dv[kMaxPairs];
+    int k = 0;
+    for (int i = 1; i < na; i++)
+        for (int j = 0; j < i; j++) {
+            const R d0 = x[3 * i] - x[3 * j], d1 = x[3 * i + 1] - x[3 * j + 1], d2 = x[3 * i + 2] - x[3 * j + 2];
+            r[k] = my_sqrt<R>(d0 * d0 + d1 * d1 + d2 * d2);
+            dv[k] = (R)0;
+            k++;
+        }
+    R v = pp[1];
+    const int nm = (int)pp[2], n1 = (int)pp[3], n2 = (int)pp[4], n3 = (int)pp[5];
+    const R *q = pp + 6;
+    for (int t = 0; t < nm; t++, q += 4) {
+        const int kk = (int)q[0];
+        const R e = my_exp<R>(q[2] * (q[1] - r[kk]));
+        const R w = e - (R)1.0;
+        v += (q[3] * w) * (q[3] * w);
+        dv[kk] -= (R)2.0 * q[3] * q[3] * w * e * q[2];
+    }
+    for (int t = 0; t < n1; t++, q += 5) {
+        const int kk = (int)q[0];
+        const R u = r[kk] - q[1];
+        const R e = my_exp<R>((R)-0.5 * q[2] * u * u);
+        v += q[3] * (e - q[4]);
+        dv[kk] -= q[3] * e * q[2] * u;
+    }
+    for (int t = 0; t < n2; t++, q += 8) {
+        const int k1 = (int)q[0], k2 = (int)q[1];
+        const R u1 = r[k1] - q[2], u2 = r[k2] - q[3];
+        const R e = my_exp<R>((R)-0.5 * (q[4] * u1 * u1 + q[5] * u2 * u2));
+        v += q[6] * (e - q[7]);
+        const R de = q[6] * e;
+        dv[k1] -= de * q[4] * u1;
+        dv[k2] -= de * q[5] * u2;
+    }
+    for (int t = 0; t < n3; t++, q += 11) {
+        const int k1 = (int)q[0], k2 = (int)q[1], k3 = (int)q[2];
+        const R u1 = r[k1] - q[3], u2 = r[k2] - q[4], u3 = r[k3] - q[5];
+        const R e = my_exp<R>((R)-0.5 * (q[6] * u1 * u1 + q[7] * u2 * u2 + q[8] * u3 * u3));
+        v += q[9] * (e - q[10]);
+        const R de = q[9] * e;
+        dv[k1] -= de * q[6] * u1;
+        dv[k2] -= de * q[7] * u2;
+        dv[k3] -= de * q[8] * u3;
+    }
+    if (g) {
+        for (int i = 0; i < 3 * na; i++) g[i] = (R)0;
+        k = 0;
+        for (int i = 1; i < na; i++)
+            for (int j = 0; j < i; j++) {
+                const R f = pdiv<R>(dv[k], r[k]);
+                for (int c = 0; c < 3; c++) {
+                    const R d = x[3 * i + c] - x[3 * j + c];
+                    g[3 * i + c] += f * d;
+                    g[3 * j + c] -= f * d;
+                }
+                k++;
+            }
+    }
+    return v - (R)pa.V0;
+}
+
 template <typename R>
 __device__ __forceinline__ R pes_vgrad(const PesArgs &pa, const R *x, R *g);
 
@@ -430,6 +510,7 @@ __device__ __forceinline__ double pes_vgrad<double>(const PesArgs &pa, const dou
     case kPesSynth9: return pes_synth9<double>(pa, x, g);
     case kPesSynth18: return pes_synth18<double>(pa, x, g);
     case kPesHarm: return pes_harm<double>(pa, x, g);
+    case kPesDistGauss: return pes_distgauss<double>(pa, x, g);
     default: return 0.0;
     }
 }
@@ -452,6 +533,7 @@ __device__ __forceinline__ float pes_vgrad<float>(const PesArgs &pa, const float
     case kPesSynth9: return pes_synth9<float>(pa, x, g);
     case kPesSynth18: return pes_synth18<float>(pa, x, g);
     case kPesHarm: return pes_harm<float>(pa, x, g);
+    case kPesDistGauss: return pes_distgauss<float>(pa, x, g);
     default: return 0.f;
     }
 }

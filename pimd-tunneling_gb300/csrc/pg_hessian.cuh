@@ -119,7 +119,7 @@ __device__ inline void hess_synth9(const PesArgs &pa, const double *x, double *h
         for (int bb = 0; bb < nd; bb++) hess[aa + nd * bb] += d2vds2 * gs[aa] * gs[bb];
 }
 
-__device__ inline bool hess_is_fd(int id) { return id == kPes1D || id == kPesSynth18; }
+__device__ inline bool hess_is_fd(int id) { return id == kPes1D || id == kPesSynth18 || id == kPesDistGauss; }
 
 // Full Hessian of one configuration by one thread (analytic surfaces) or the
 // FD column a (FD surfaces; a < 0 computes every column).

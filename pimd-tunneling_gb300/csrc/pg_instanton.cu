@@ -17,7 +17,7 @@
 
 namespace pg {
 
-bool hess_is_fd_host(int id) { return id == PG_PES_1D || id == PG_PES_SYNTH18; }
+bool hess_is_fd_host(int id) { return id == PG_PES_1D || id == PG_PES_SYNTH18 || id == PG_PES_DISTGAUSS; }
 
 namespace {
 

@@ -1141,14 +1141,17 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tb_pos(TbArgs a) {
 // memory (row stride nd | 1, odd: conflict-free) and the table is staged there
 // too, instead of thread-local arrays and global reads.
 constexpr int kForceThreads = 128;
+constexpr int kStageParams = 4096;  // parameter tables up to 16 KB are staged in shared memory
 __host__ __device__ __forceinline__ int force_stride(int nd) { return nd | 1; }
+__host__ __device__ __forceinline__ int staged_params(int nfparams) { return nfparams <= kStageParams ? nfparams : 0; }
 static size_t tb_force_smem(int nd, int nfparams) {
-    return ((size_t)nfparams * sizeof(float) + 15) / 16 * 16 + 2 * (size_t)kForceThreads * force_stride(nd) * sizeof(float);
+    return ((size_t)staged_params(nfparams) * sizeof(float) + 15) / 16 * 16 +
+           2 * (size_t)kForceThreads * force_stride(nd) * sizeof(float);
 }
 
 __global__ void __launch_bounds__(kForceThreads) k_tb_force(TbArgs a) {
     extern __shared__ __align__(16) unsigned char fsm[];
-    const int np = a.pes.nparams + pes_fparams_extra(a.pes.id);
+    const int np = staged_params(a.pes.nparams + pes_fparams_extra(a.pes.id));
     float *sp = reinterpret_cast<float *>(fsm);
     const int ldx = force_stride(a.nd);
     float *sx = reinterpret_cast<float *>(fsm + ((size_t)np * sizeof(float) + 15) / 16 * 16) + threadIdx.x * ldx;
@@ -1156,7 +1159,7 @@ __global__ void __launch_bounds__(kForceThreads) k_tb_force(TbArgs a) {
     for (int i = threadIdx.x; i < np; i += kForceThreads) sp[i] = a.pes.fparams[i];
     __syncthreads();
     PesArgs pa = a.pes;
-    pa.fparams = sp;
+    if (np > 0) pa.fparams = sp;  // large tables are read through L1 (uniform addresses)
     const int64_t t = (int64_t)blockIdx.x * kForceThreads + threadIdx.x;
     const int P = a.P, nd = a.nd;
     if (t >= a.nrings * P) return;

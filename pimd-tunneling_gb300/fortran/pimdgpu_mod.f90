@@ -12,7 +12,7 @@ module pimdgpu
 
   integer(c_int), parameter :: PG_OK = 0
   integer(c_int32_t), parameter :: PG_PES_1D = 1, PG_PES_2DTEST = 2, PG_PES_SYNTH9 = 3, &
-       PG_PES_SYNTH18 = 4, PG_PES_HARMONIC = 5
+       PG_PES_SYNTH18 = 4, PG_PES_HARMONIC = 5, PG_PES_DISTGAUSS = 6
   integer(c_int32_t), parameter :: PG_FP64 = 0, PG_MIXED = 1
   integer(c_int32_t), parameter :: PG_FORM_AUTO = 0, PG_FORM_PLAIN = 1, PG_FORM_FUSED = 2, &
        PG_FORM_TENSOR = 3

@@ -40,6 +40,7 @@ static int pes_id_of(const std::string &s) {
     if (p == "2dtest") return PG_PES_2DTEST;
     if (p == "synth9") return PG_PES_SYNTH9;
     if (p == "synth18") return PG_PES_SYNTH18;
+    if (p == "distgauss") return PG_PES_DISTGAUSS;
     if (p == "harmonic") return PG_PES_HARMONIC;
     throw std::runtime_error("unknown pes '" + s + "'");
 }

@@ -15,7 +15,7 @@ _PKG = os.path.dirname(_HERE)
 LIBPATH = os.path.join(_PKG, "lib", "libpimdgpu.so")
 
 PG_OK, PG_ERR_ARG, PG_ERR_CUDA, PG_ERR_STATE, PG_ERR_UNSUPPORTED, PG_ERR_IO, PG_ERR_NUMERIC = range(7)
-PG_PES_1D, PG_PES_2DTEST, PG_PES_SYNTH9, PG_PES_SYNTH18, PG_PES_HARMONIC = 1, 2, 3, 4, 5
+PG_PES_1D, PG_PES_2DTEST, PG_PES_SYNTH9, PG_PES_SYNTH18, PG_PES_HARMONIC, PG_PES_DISTGAUSS = 1, 2, 3, 4, 5, 6
 PG_FP64, PG_MIXED = 0, 1
 PG_FORM_AUTO, PG_FORM_PLAIN, PG_FORM_FUSED, PG_FORM_TENSOR = 0, 1, 2, 3
 PG_ANDERSEN, PG_LANGEVIN = 1, 2

@@ -430,3 +430,36 @@ def test_tensor_forms_with_cayley_rotation(ctx, pg, cfgname, P):
         out.append((ctx.ti_state()[0], ctx.ti_results()[0]))
     assert np.max(np.abs(out[0][0] - out[1][0])) < 2e-3
     np.testing.assert_allclose(out[1][1], out[0][1], rtol=2e-4)
+
+
+@pytest.mark.parametrize("P,nrep,nint", [(15, 1, 1), (7, 3, 1), (33, 1, 3)])
+def test_fused_fp64_odd_shapes_match_oracle(ctx, pg, oracle, P, nrep, nint):
+    """Ragged shapes: odd bead numbers (not a multiple of the transform passes or
+    of a warp) and a single ring."""
+    c, ti = _small_2d(P=P, nrep=nrep, nint=nint)
+    _set_system(ctx, c)
+    nsteps = 40
+    cfg = _gpu_cfg(pg, c, ti, pg.PG_FP64, pg.PG_FORM_FUSED)
+    ctx.ti_setup(cfg, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
+    ctx.ti_advance(nsteps)
+    x, _ = ctx.ti_state()
+    s, n, _, st = ctx.ti_results()
+    prm = _oracle_prm(oracle, c, ti, True)
+    xo, po, so, no, _ = _oracle_run(oracle, c, ti, prm, nsteps)
+    assert np.all(st == 0)
+    np.testing.assert_array_equal(n, no)
+    np.testing.assert_allclose(x.reshape(xo.shape), xo, rtol=0, atol=1e-9)
+    np.testing.assert_allclose(s, so, rtol=1e-9, atol=1e-12)
+
+
+def test_tensor_form_single_ring_and_rejections(ctx, pg):
+    """One ring on the fused tiles (a 2-column chunk) tracks the SIMT form; the
+    tensor form is refused where it does not apply (Andersen, P % 4 != 0)."""
+    c, ti = _small_2d(P=128, nrep=1, nint=1)
+    x1, p1, s1, x2, p2, s2 = _tensor_vs_simt(ctx, pg, c, ti)
+    assert np.max(np.abs(x1 - x2)) < 2e-3
+    for P, thermostat in ((128, 1), (30, 2)):
+        c, ti = _small_2d(P=P, nrep=1, nint=1)
+        cfg = _gpu_cfg(pg, c, ti, pg.PG_MIXED, pg.PG_FORM_TENSOR, thermostat)
+        with pytest.raises(pg.PgError):
+            ctx.ti_setup(cfg, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
