@@ -80,6 +80,7 @@ struct TiState {
     DevBuf bv;               // nlambda*nd*P endpoint shifts (beadvec)
     DevBuf bvtab;            // 3P: the sine and scale tables beadvec is formed from
     DevBuf x0, p0;           // FP64 staging of caller-given start positions / momenta
+    DevBuf kickflag;         // per-ring Andersen kick flag (blocked tensor form)
     DevBuf dbdl;             // nlambda*nd
     DevBuf avec, bvec;       // nd start point, nlambda*nd end points
     DevBuf xref;             // nlambda*nd*P

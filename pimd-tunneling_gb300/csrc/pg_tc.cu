@@ -969,9 +969,12 @@ struct TbArgs {
     float dt;
     int64_t imin;
     const unsigned char *gT;  // mb x mb block image
-    const float *coef;        // natom x P x 8: rA rB rC rD ou_a ou_s
+    const float *coef;        // natom x P x 8: rA rB rC rD ou_a ou_s pscale
     const double *mass;
     const double *avec, *bvec, *dbdl;
+    const float *Tf;          // P x P FP32 transform (the bead-P row for the Andersen estimator)
+    double betan, noutput;
+    uint8_t *kick;            // per-ring Andersen kick flag of the current step
     const int32_t *ringlam;
     const uint64_t *ringseed;
     const uint32_t *ringstream;
@@ -1290,6 +1293,142 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tb_kick(TbArgs a) {
 }
 
 
+// ---------------------------------------------------------------- Andersen thermostat, blocked form
+// The Andersen step of time_step_nm (verletmodule.f90:204-234, 291-302):
+// resample pi on a Poisson schedule, rotate dt/2, kick with the forces at the
+// rotated positions, rotate dt/2; the estimator uses the positions after the
+// step (verletmodule.f90:236-245).  Per step: k_tb_and_sched (one thread per
+// ring), k_tb_and_pre (resample + first half rotation, one thread per
+// element), k_tb_pos, k_tb_force (forces only), k_tb_kick_nm (T F, kick,
+// second half rotation), k_tb_and_est (bead-P positions and the estimator).
+__global__ void k_tb_and_sched(TbArgs a) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= a.nrings) return;
+    const uint32_t st = (uint32_t)(*a.step0 + a.sofs);
+    RingAcc *acc = &a.acc[r];
+    acc->and_count += 1;
+    const bool kick = acc->and_count >= acc->and_rkick;
+    if (kick) {
+        acc->and_count = 0;
+        acc->and_rkick = poisson_d(a.ringseed[r], a.ringstream[r], st, kRngPoisson, a.noutput);
+    }
+    a.kick[r] = kick ? 1 : 0;
+}
+
+__global__ void k_tb_and_pre(TbArgs a) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int P = a.P, nd = a.nd;
+    if (e >= a.nrings * nd * P) return;
+    const int k = (int)(e % P);
+    const int64_t rd = e / P;
+    const int dof = (int)(rd % nd);
+    const int64_t r = rd / nd;
+    const float *cf = a.coef + ((size_t)(dof / a.ndim) * P + k) * 8;
+    float pv = a.pi[e], qv = a.q[e];
+    if (a.kick[r]) {
+        const uint32_t st = (uint32_t)(*a.step0 + a.sofs);
+        const double z = normal_d(a.ringseed[r], a.ringstream[r], st, kRngAndersen, (uint32_t)(dof * P + k));
+        pv = (float)(z * (double)cf[6]);
+    }
+    a.pi[e] = cf[0] * pv + cf[1] * qv;
+    a.q[e] = cf[2] * pv + cf[3] * qv;
+}
+
+// T F, kick, half rotation (no OU): the tile structure of k_tb_kick.
+__global__ void __launch_bounds__(kTileThreads, 2) k_tb_kick_nm(TbArgs a) {
+    extern __shared__ unsigned char dsm[];
+    unsigned char *base = align1k(dsm);
+    TcShared *sh = reinterpret_cast<TcShared *>(base + kTileSmemOps);
+    TileAux *ax = reinterpret_cast<TileAux *>(base + kTileSmemOps + 256);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int nd = a.nd, P = a.P;
+    const int64_t col0 = (int64_t)blockIdx.x * kNc;
+    const int nvalid = (int)min((int64_t)kNc, a.nrings * nd - col0);
+    if (tid < kNc) {
+        const int64_t ring = (col0 + tid) / nd;
+        const int j = (int)(col0 + tid - ring * nd);
+        ax->jdof[tid] = j;
+        ax->atom[tid] = j / a.ndim;
+    }
+    const uint32_t tmem = tb_begin(sh, a.mb);
+    uint32_t phase = 0;
+    const bool ok = tb_gemm(base, sh, a, a.f + col0 * P, nvalid, tmem, &phase);
+    if (ok) {
+        const int cb = 32 * (warp >> 2);
+        const int nv = nvalid - cb;
+        const float dt = a.dt;
+        uint32_t badbits = 0;
+        for (int ib = 0; ib < a.mb; ib++) {
+            const int m = 128 * ib + 32 * (warp & 3) + lane;  // mode
+            const int mc = m < P ? m : P - 1;
+            const uint32_t taddr = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(64 * ib + cb);
+#pragma unroll 1
+            for (int c0 = 0; c0 < 32; c0 += kGrp) {
+                const int nvg = nv - c0;
+                float *qo = a.q + (size_t)(col0 + cb + c0) * P + m;
+                float *po = a.pi + (size_t)(col0 + cb + c0) * P + m;
+                float gv[kGrp];
+                __syncwarp();
+                tmem_ldn<kGrp>(taddr + (uint32_t)c0, gv);
+#pragma unroll
+                for (int i = 0; i < kGrp; i++) {
+                    if (m < P && i < nvg) {
+                        const float *cf = a.coef + ((size_t)ax->atom[cb + c0 + i] * P + mc) * 8;
+                        const float4 c4 = __ldg(reinterpret_cast<const float4 *>(cf));
+                        const float p0 = po[(size_t)i * P] - dt * gv[i];
+                        const float q0 = qo[(size_t)i * P];
+                        const float pn = c4.x * p0 + c4.y * q0;
+                        const float qn = c4.z * p0 + c4.w * q0;
+                        qo[(size_t)i * P] = qn;
+                        po[(size_t)i * P] = pn;
+                        if (pn != pn) badbits |= 1u << (c0 + i);
+                    }
+                }
+            }
+        }
+        badbits = __reduce_or_sync(0xffffffffu, badbits);
+        if (lane == 0 && badbits) {
+            const int64_t s = *a.step0 + a.sofs;
+            for (int i = 0; i < 32; i++)
+                if (badbits & (1u << i)) {
+                    const int64_t ring = (col0 + cb + i) / nd;
+                    if (atomicOr(&a.acc[ring].status, PG_RING_NAN) == 0) a.acc[ring].pad = (int32_t)s;
+                }
+        }
+    }
+    tb_release(sh, tmem, a.mb, a.err, phase);
+}
+
+// Estimator of step s from the positions after the step at bead P:
+// x_P = sum_m T[P-1][m] q[m] + x*_P per dof, one warp per ring.
+__global__ void k_tb_and_est(TbArgs a) {
+    const int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (r >= a.nrings) return;
+    const int64_t s = *a.step0 + a.sofs;
+    const int P = a.P, nd = a.nd;
+    const int lam = a.ringlam[r];
+    const float *trow = a.Tf + (size_t)(P - 1) * P;  // T is symmetric: row P-1 = column P-1
+    double contr = 0.0;  // summation order of verletmodule.f90:399-403 (dimension outer, atom inner)
+    for (int jd = 0; jd < a.ndim; jd++)
+        for (int at = 0; at < nd / a.ndim; at++) {
+            const int j = at * a.ndim + jd;
+            const float *q = a.q + ((size_t)r * nd + j) * P;
+            float sum = 0.f;
+            for (int m = lane; m < P; m += 32) sum += trow[m] * q[m];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+            const double av = a.avec[j], bv = a.bvec[(size_t)lam * nd + j];
+            const double xp = (double)sum + av + (bv - av) * (double)P / (double)(P + 1);
+            contr += a.mass[at] * (-xp) * a.dbdl[(size_t)lam * nd + j];
+        }
+    if (lane == 0 && s >= a.imin) {
+        RingAcc *acc = &a.acc[r];
+        acc->nsamples += 1;
+        if (acc->status == 0) acc->dhdr_sum += contr;
+    }
+}
+
 // Host: split-BF16 image of T, zero-padded to mb x mb blocks of 128 x 128
 // (mb = ceil(P / 128)); block (ib, kb) is a 64 KB [hi | lo] pair in the K-major
 // core-matrix layout of the A operand, at (ib mb + kb) 64 KB.
@@ -1326,11 +1465,12 @@ static size_t tbf_err_off(const TiState &st, int natom) {
 int tc_built() { return 1; }
 
 // 0: unsupported; 1: fused 64-column tiles (P = 128, one-atom 1-D or 2-D
-// surface); 2: blocked GEMMs (P <= 512 with P % 4 == 0, any surface).
-// Both: Langevin thermostat, no dHdrlimit re-initialisation.
+// surface, Langevin); 2: blocked GEMMs (P <= 512 with P % 4 == 0, any surface,
+// Langevin or Andersen).  dHdrlimit re-initialisation (a Langevin option) is
+// not built into either.
 int tc_supported(const TiState &st, const pg_ctx &ctx) {
-    if (st.cfg.thermostat != PG_LANGEVIN) return 0;
-    if (st.cfg.dhdr_limit >= 0.0) return 0;
+    if (st.cfg.dhdr_limit >= 0.0 && st.cfg.thermostat == PG_LANGEVIN) return 0;
+    if (st.cfg.thermostat == PG_ANDERSEN) return (st.P % 4 == 0 && st.P <= kMaxMb * kP && ctx.nd <= kMaxDof) ? 2 : 0;
     if (st.P == kP && ctx.natom == 1 &&
         ((ctx.pes_id == PG_PES_2DTEST && ctx.nd == 2) || (ctx.pes_id == PG_PES_1D && ctx.nd == 1)))
         return 1;
@@ -1362,6 +1502,7 @@ int tc_prepare(pg_ctx *ctx, TiState &st) {
             o[3] = (float)c.rD;
             o[4] = (float)c.ou_a;
             o[5] = (float)c.ou_s;
+            o[6] = (float)c.pscale;  // sqrt(beadmass / betan): Andersen momentum scale
         }
     unsigned char *d = st.Tbf.as<unsigned char>();
     PG_CUDA(cudaMemcpyAsync(d, img.data(), img.size(), cudaMemcpyHostToDevice, ctx->stream));
@@ -1375,6 +1516,7 @@ int tc_prepare(pg_ctx *ctx, TiState &st) {
     PG_CUDA(cudaFuncSetAttribute(k_tc_final, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     PG_CUDA(cudaFuncSetAttribute(k_tb_pos, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     PG_CUDA(cudaFuncSetAttribute(k_tb_kick, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    PG_CUDA(cudaFuncSetAttribute(k_tb_kick_nm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     PG_CUDA(cudaFuncSetAttribute(k_tb_force, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)tb_force_smem(st.nd, (int)ctx->fparams.size())));
     return PG_OK;
@@ -1496,6 +1638,10 @@ static void tb_make_args(pg_ctx *ctx, TiState &st, TbArgs &a) {
     a.f = st.f.as<float>();
     a.acc = st.acc.as<RingAcc>();
     a.pes = ctx->pes_args();
+    a.Tf = reinterpret_cast<const float *>(st.T.as<double>() + (size_t)st.P * st.P);
+    a.betan = st.betan;
+    a.noutput = (double)st.cfg.noutput;
+    a.kick = st.kickflag.as<uint8_t>();
 }
 
 // Blocked form: kernel k (0 positions, 1 forces / estimator, 2 kick) of step
@@ -1518,7 +1664,42 @@ static int tb_launch_kernel(pg_ctx *ctx, TiState &st, int k, int64_t i, bool fin
     return e == cudaSuccess ? PG_OK : cuda_fail(e, "blocked tensor-form launch");
 }
 
+// Andersen step i of the blocked form: schedule, resample + half rotation,
+// positions, forces, T F kick + half rotation, estimator.
+static int tb_launch_andersen_step(pg_ctx *ctx, TiState &st, int64_t i, cudaStream_t s) {
+    TbArgs a;
+    tb_make_args(ctx, st, a);
+    a.sofs = i;
+    a.do_est = 0;
+    a.do_force = 1;
+    const int64_t nel = st.nrings * st.nd * st.P;
+    const unsigned grid = (unsigned)((st.nrings * st.nd + kNc - 1) / kNc);
+    k_tb_and_sched<<<(unsigned)((st.nrings + 127) / 128), 128, 0, s>>>(a);
+    k_tb_and_pre<<<(unsigned)((nel + 255) / 256), 256, 0, s>>>(a);
+    k_tb_pos<<<grid, kTileThreads, tc_smem_bytes(), s>>>(a);
+    k_tb_force<<<(unsigned)((st.nrings * st.P + kForceThreads - 1) / kForceThreads), kForceThreads,
+                 tb_force_smem(st.nd, a.pes.nparams + pes_fparams_extra(a.pes.id)), s>>>(a);
+    k_tb_kick_nm<<<grid, kTileThreads, tc_smem_bytes(), s>>>(a);
+    k_tb_and_est<<<(unsigned)((st.nrings + 3) / 4), 128, 0, s>>>(a);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? PG_OK : cuda_fail(e, "blocked Andersen step launch");
+}
+
 static int tb_launch(pg_ctx *ctx, TiState &st, int64_t nsteps, cudaStream_t s) {
+    if (st.cfg.thermostat == PG_ANDERSEN) {
+        for (int64_t i = 0; i < nsteps; i++) {
+            int rc = tb_launch_andersen_step(ctx, st, i, s);
+            if (rc) return rc;
+        }
+        // positions after the last step for read-out (the estimator ran per step)
+        TbArgs a;
+        tb_make_args(ctx, st, a);
+        a.sofs = nsteps;
+        k_tb_pos<<<(unsigned)((st.nrings * st.nd + kNc - 1) / kNc), kTileThreads, tc_smem_bytes(), s>>>(a);
+        k_tc_step_add<<<1, 1, 0, s>>>(const_cast<int64_t *>(a.step0), nsteps);
+        cudaError_t e = cudaGetLastError();
+        return e == cudaSuccess ? PG_OK : cuda_fail(e, "blocked Andersen final launch");
+    }
     for (int64_t i = 0; i < nsteps; i++)
         for (int k = 0; k < 3; k++) {
             int rc = tb_launch_kernel(ctx, st, k, i, false, s);
@@ -1550,6 +1731,25 @@ int tc_launch(pg_ctx *ctx, TiState &st, int64_t, int64_t nsteps, cudaStream_t s)
 // Blocked form: ms[0..2] = k_tb_pos, k_tb_force, k_tb_kick per launch over nsteps steps.
 static int tb_kernel_times(pg_ctx *ctx, TiState &st, int64_t nsteps, double *ms, int64_t *count) {
     cudaStream_t s = ctx->stream;
+    if (st.cfg.thermostat == PG_ANDERSEN) {  // one kind: the six-launch step
+        cudaEvent_t e0, e1;
+        PG_CUDA(cudaEventCreate(&e0));
+        PG_CUDA(cudaEventCreate(&e1));
+        PG_CUDA(cudaEventRecord(e0, s));
+        int rc = tb_launch(ctx, st, nsteps, s);
+        if (rc) return rc;
+        PG_CUDA(cudaEventRecord(e1, s));
+        PG_CUDA(cudaEventSynchronize(e1));
+        float v = 0.f;
+        PG_CUDA(cudaEventElapsedTime(&v, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        ms[0] = v / (double)nsteps;
+        count[0] = nsteps;
+        ms[1] = ms[2] = 0.0;
+        count[1] = count[2] = 0;
+        return PG_OK;
+    }
     std::vector<cudaEvent_t> ev(3 * nsteps + 1);
     for (auto &e : ev) PG_CUDA(cudaEventCreate(&e));
     PG_CUDA(cudaEventRecord(ev[0], s));

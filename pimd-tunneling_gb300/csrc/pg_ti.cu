@@ -800,7 +800,7 @@ static std::string graph_signature(const pg_ctx *ctx, const TiState &st) {
     add(&ctx->V0, sizeof(double));
     add(ctx->params.data(), ctx->params.size() * sizeof(double));
     add(ctx->mass.data(), ctx->mass.size() * sizeof(double));
-    const void *ptrs[] = {st.q.ptr, st.pi.ptr, st.x.ptr, st.f.ptr, st.T.ptr, st.Tbf.ptr, st.coef.ptr, st.bv.ptr,
+    const void *ptrs[] = {st.q.ptr, st.pi.ptr, st.x.ptr, st.f.ptr, st.T.ptr, st.Tbf.ptr, st.coef.ptr, st.bv.ptr, st.kickflag.ptr,
                           st.dbdl.ptr, st.avec.ptr, st.bvec.ptr, st.xref.ptr, st.ringlam.ptr, st.ringseed.ptr,
                           st.ringstream.ptr, st.acc.ptr, st.red.ptr, ctx->d_params.ptr, ctx->d_fparams.ptr,
                           ctx->d_mass.ptr};
@@ -825,8 +825,8 @@ static int resolve_form(pg_ctx *ctx, TiState &st) {
     const int tcv = tc_supported(st, *ctx);
     if (form == PG_FORM_TENSOR && !tcv)
         return fail(PG_ERR_UNSUPPORTED,
-                    "the tensor-core form supports the Langevin thermostat without dHdrlimit, and P <= 512 "
-                    "with P % 4 == 0");
+                    "the tensor-core form supports the Langevin thermostat without dHdrlimit and the Andersen "
+                    "thermostat, with P <= 512 and P % 4 == 0");
     // AUTO: the fused tiles whenever they apply; the blocked GEMMs for batches of at
     // least 2^20 bead-dofs (smaller batches leave most of the GPU idle in them).
     bool use = tcv == 1 || (tcv == 2 && (form == PG_FORM_TENSOR || st.nrings * st.nd * st.P >= (1 << 20)));
@@ -953,6 +953,7 @@ extern "C" int pg_ti_setup(pg_ctx *ctx, const pg_ti_config *cfg, int64_t nrings,
     ENS(st.ringstream, (size_t)nrings * sizeof(uint32_t));
     ENS(st.acc, (size_t)nrings * sizeof(RingAcc));
     ENS(st.red, (size_t)(3 * nlambda + 1) * sizeof(double));
+    ENS(st.kickflag, (size_t)nrings);  // Andersen kick flags of the blocked tensor form
     if (x0) ENS(st.x0, nstate * sizeof(double));
     if (p0) ENS(st.p0, nstate * sizeof(double));
     DevBuf &dx0 = st.x0, &dp0 = st.p0;
@@ -1021,6 +1022,12 @@ extern "C" int pg_ti_setup(pg_ctx *ctx, const pg_ti_config *cfg, int64_t nrings,
         if (rc) {
             ti_release(ctx);
             return rc;
+        }
+        const std::string sig = graph_signature(ctx, st);  // tc_prepare may have moved the tensor tables
+        if (sig != st.graph_sig) {
+            for (auto &kv : st.graphs) cudaGraphExecDestroy(kv.second);
+            st.graphs.clear();
+            st.graph_sig = sig;
         }
     }
     return PG_OK;
@@ -1197,7 +1204,17 @@ extern "C" int pg_ti_kernel_times(pg_ctx *ctx, int64_t nsteps, int32_t *nkinds, 
     if (st.form == PG_FORM_TENSOR) {
         double ms[2];
         int64_t n[2];
-        if (st.tc_blocked) {
+        if (st.tc_blocked && st.cfg.thermostat == PG_ANDERSEN) {
+            double ms3[3];
+            int64_t n3[3];
+            rc = tc_kernel_times(ctx, st, nsteps, ms3, n3);
+            if (rc) return rc;
+            *nkinds = 1;
+            ms_per_launch[0] = ms3[0];
+            count[0] = n3[0];
+            bytes_per_launch[0] = 14.0 * arr;  // q, pi twice; x, F, the GEMM operands
+            if (names) names[0] = "blocked Andersen step (schedule, resample + rotation, k_tb_pos, k_tb_force, k_tb_kick_nm, estimator)";
+        } else if (st.tc_blocked) {
             double ms3[3];
             int64_t n3[3];
             rc = tc_kernel_times(ctx, st, nsteps, ms3, n3);
@@ -1254,7 +1271,9 @@ extern "C" int pg_ti_get_form(pg_ctx *ctx, int64_t nsteps, int32_t *form, int64_
     TiState &st = *ctx->ti;
     if (form) *form = st.form;
     if (launches) {
-        if (st.form == PG_FORM_TENSOR && st.tc_blocked)
+        if (st.form == PG_FORM_TENSOR && st.tc_blocked && st.cfg.thermostat == PG_ANDERSEN)
+            *launches = nsteps > 0 ? 6 * nsteps + 2 : 0;  // six per step; positions, counter
+        else if (st.form == PG_FORM_TENSOR && st.tc_blocked)
             *launches = nsteps > 0 ? 3 * nsteps + 3 : 0;  // pos, force, kick per step; pos, estimator, counter
         else if (st.form == PG_FORM_TENSOR)
             *launches = nsteps > 0 ? nsteps + 2 : 0;  // one step kernel per step; final pass, counter

@@ -454,12 +454,41 @@ def test_fused_fp64_odd_shapes_match_oracle(ctx, pg, oracle, P, nrep, nint):
 
 def test_tensor_form_single_ring_and_rejections(ctx, pg):
     """One ring on the fused tiles (a 2-column chunk) tracks the SIMT form; the
-    tensor form is refused where it does not apply (Andersen, P % 4 != 0)."""
+    tensor form is refused where it does not apply (P % 4 != 0 with either
+    thermostat; dHdrlimit re-initialisation)."""
     c, ti = _small_2d(P=128, nrep=1, nint=1)
     x1, p1, s1, x2, p2, s2 = _tensor_vs_simt(ctx, pg, c, ti)
     assert np.max(np.abs(x1 - x2)) < 2e-3
-    for P, thermostat in ((128, 1), (30, 2)):
+    for P, thermostat, lim in ((30, 1, -1.0), (30, 2, -1.0), (128, 2, 1.0)):
         c, ti = _small_2d(P=P, nrep=1, nint=1)
-        cfg = _gpu_cfg(pg, c, ti, pg.PG_MIXED, pg.PG_FORM_TENSOR, thermostat)
+        cfg = _gpu_cfg(pg, c, ti, pg.PG_MIXED, pg.PG_FORM_TENSOR, thermostat, dhdr_limit=lim)
         with pytest.raises(pg.PgError):
             ctx.ti_setup(cfg, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
+
+
+@pytest.mark.parametrize("cfgname,P,nrep", [("c1", 128, 3), ("c2", 256, 3), ("c0", 64, 5)])
+def test_tensor_blocked_andersen_tracks_simt(ctx, pg, cfgname, P, nrep):
+    """Andersen thermostat (verletmodule.f90:204-234) on the blocked tcgen05 form:
+    with noutput = 9 every ring is resampled several times in 40 steps; the
+    same Poisson schedule and Andersen normals as the FP32 SIMT form, so the
+    runs track each other at the FP32 / split-BF16 tolerance."""
+    c = dict(pgconfigs.load(cfgname))
+    c["P"] = P
+    ti = pgconfigs.TiInputs(c, nrep=nrep, nintegral=2)
+    _set_system(ctx, c)
+    out = []
+    for form in (pg.PG_FORM_FUSED, pg.PG_FORM_TENSOR):
+        cfg = _gpu_cfg(pg, c, ti, pg.PG_MIXED, form, thermostat=1, noutput=9)
+        ctx.ti_setup(cfg, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
+        assert ctx.ti_form(1)[0] == form
+        ctx.ti_advance(25)
+        ctx.ti_advance(15)  # a second graph, continuing the schedule
+        x, p = ctx.ti_state()
+        s, n, _, st = ctx.ti_results()
+        out.append((x, p, s, n, st))
+    (x1, p1, s1, n1, st1), (x2, p2, s2, n2, st2) = out
+    assert np.all(st1 == 0) and np.all(st2 == 0)
+    np.testing.assert_array_equal(n1, n2)
+    assert np.max(np.abs(x1 - x2)) < 2e-3
+    assert np.max(np.abs(p1 - p2)) < 2e-3 * np.max(np.abs(p1))
+    np.testing.assert_allclose(s2, s1, rtol=2e-4)
