@@ -676,18 +676,27 @@ __device__ __forceinline__ void group_positions(const TileAux *ax, uint32_t tadd
     __syncwarp();  // tcgen05.ld is .sync.aligned: issue it from a converged warp
     tmem_ldn<kGrp>(taddr + (uint32_t)c0, xv);
     const float fm = (float)(m + 1);
+    float xa[kGrp], xs[kGrp];  // 16-byte shared loads (cb + c0 is a multiple of 8)
 #pragma unroll
-    for (int i = 0; i < kGrp; i++) xv[i] += ax->xa[cb + c0 + i] + ax->xs[cb + c0 + i] * fm;
+    for (int i = 0; i < kGrp; i += 4) {
+        const float4 va = *reinterpret_cast<const float4 *>(&ax->xa[cb + c0 + i]);
+        const float4 vs = *reinterpret_cast<const float4 *>(&ax->xs[cb + c0 + i]);
+        xa[i] = va.x, xa[i + 1] = va.y, xa[i + 2] = va.z, xa[i + 3] = va.w;
+        xs[i] = vs.x, xs[i + 1] = vs.y, xs[i + 2] = vs.z, xs[i + 3] = vs.w;
+    }
+#pragma unroll
+    for (int i = 0; i < kGrp; i++) xv[i] += xa[i] + xs[i] * fm;
     if (stage_p && m == kP - 1)
 #pragma unroll
         for (int i = 0; i < kGrp; i++) xP[cb + c0 + i] = xv[i];
 }
 
 // Estimator of step s-1 (verletmodule.f90:397-403) from the staged bead-P
-// positions, one thread per ring of the tile.
+// positions, one thread per ring of the tile, counted down from the last
+// thread (thread 0 issues the GEMMs).
 __device__ __forceinline__ void tile_estimator(const TcArgs &a, const TileAux *ax, int64_t col0, int nvalid,
                                                int64_t s) {
-    const int nd = a.nd, tid = threadIdx.x;
+    const int nd = a.nd, tid = kTileThreads - 1 - (int)threadIdx.x;
     if (tid >= nvalid / nd || (s - 1) < a.imin) return;
     const int64_t ring = col0 / nd + tid;
     const int lam = a.ringlam[ring];
@@ -699,20 +708,32 @@ __device__ __forceinline__ void tile_estimator(const TcArgs &a, const TileAux *a
     r->nsamples += 1;
 }
 
-__device__ __forceinline__ float sel4(const float (&v)[4], int i) {
-    float r = v[0];
-    r = i == 1 ? v[1] : r;
-    r = i == 2 ? v[2] : r;
-    r = i == 3 ? v[3] : r;
-    return r;
-}
-
 // This thread's OU normals for its mode m and the 32 columns of its half:
 // zc[i] = normal j P + m of the Philox stream of column cb + i at step st.
 // Lane e of a quad draws the block of column 4g + e (normals j P + 4 (m/4) ..
 // +3, the four modes of the quad), then the quad transposes the 4 x 4 values.
-__device__ __forceinline__ void tile_normals(const TileAux *ax, int64_t col0, int nd, int cb, int m, uint32_t st,
-                                             int nv, float (&zc)[32]) {
+// The quad holds M[e][t] = normal (column 4g + e, mode 4 (m/4) + t) in lane e;
+// two exchange stages (lane bit 1, then bit 0) leave M[t][e] in lane e.
+__device__ __forceinline__ void quad_transpose(float (&z)[4], int e) {
+    const bool b1 = (e & 2) != 0, b0 = (e & 1) != 0;
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+        const float r = __shfl_xor_sync(0xffffffffu, b1 ? z[j] : z[j + 2], 2);
+        const float lo = b1 ? r : z[j], hi = b1 ? z[j + 2] : r;
+        z[j] = lo;
+        z[j + 2] = hi;
+    }
+#pragma unroll
+    for (int j = 0; j < 4; j += 2) {
+        const float r = __shfl_xor_sync(0xffffffffu, b0 ? z[j] : z[j + 1], 1);
+        const float lo = b0 ? r : z[j], hi = b0 ? z[j + 1] : r;
+        z[j] = lo;
+        z[j + 1] = hi;
+    }
+}
+
+__device__ __forceinline__ void tile_normals(const TileAux *ax, int cb, int m, uint32_t st, int nv,
+                                             float (&zc)[32]) {
     const int e = threadIdx.x & 3;
 #pragma unroll
     for (int g0 = 0; g0 < 8; g0 += 4) {
@@ -725,20 +746,17 @@ __device__ __forceinline__ void tile_normals(const TileAux *ax, int64_t col0, in
 #pragma unroll
         for (int g = 0; g < 4; g++) {
             const int cc = cb + 4 * (g0 + g) + e;
-            const int j = (int)((col0 + cc) % nd);
-            o[g] = philox_block(ax->seed[cc], ax->stream[cc], st, kRngLangevin, (uint32_t)((j * kP + m) >> 2));
+            o[g] = philox_block(ax->seed[cc], ax->stream[cc], st, kRngLangevin,
+                                (uint32_t)((ax->jdof[cc] * kP + m) >> 2));
         }
 #pragma unroll
         for (int g = 0; g < 4; g++) {
             float z[4];
             box_muller_f(o[g].x, o[g].y, z[0], z[1]);
             box_muller_f(o[g].z, o[g].w, z[2], z[3]);
-            float rv[4];  // rv[r]: this mode's normal for column 4g + (e ^ r)
-            rv[0] = sel4(z, e);
+            quad_transpose(z, e);
 #pragma unroll
-            for (int r = 1; r < 4; r++) rv[r] = __shfl_xor_sync(0xffffffffu, sel4(z, e ^ r), r);
-#pragma unroll
-            for (int k = 0; k < 4; k++) zc[4 * (g0 + g) + k] = sel4(rv, e ^ k);
+            for (int k = 0; k < 4; k++) zc[4 * (g0 + g) + k] = z[k];
         }
     }
 }
@@ -747,24 +765,24 @@ __device__ __forceinline__ void tile_normals(const TileAux *ax, int64_t col0, in
 // thread's half) into the B operand as rows c, K index m.  Adjacent lanes pair
 // up with one shuffle per column pair: the even lane stores (m, m+1) of column
 // c, the odd lane (m-1, m) of column c+1, 4 bytes each per plane.
+// Each lane splits its own values (columns i, i+1 of bead m) into packed hi
+// and lo words and swaps them with the partner lane (bead m ^ 1); a byte
+// permute then forms the even lane's (m, m+1) word of column i and the odd
+// lane's (m-1, m) word of column i+1.  cb + c0 is a multiple of 8.
 __device__ __forceinline__ void group_store_operand(unsigned char *Xhi, unsigned char *Xlo, int cb, int c0, int m,
                                                     const float (&fv)[kGrp]) {
     const bool odd = (m & 1) != 0;
+    const uint32_t psel = odd ? 0x3276u : 0x5410u;
+    const uint32_t off0 = (uint32_t)((cb + c0) >> 3) * kXSbo + (uint32_t)(m >> 3) * kXLbo +
+                          (uint32_t)(m & 6) * 2 + (odd ? 16u : 0u);
 #pragma unroll
     for (int i = 0; i < kGrp; i += 2) {
-        const float send = odd ? fv[i] : fv[i + 1];
-        const float recv = __shfl_xor_sync(0xffffffffu, send, 1);
-        const float v0 = odd ? recv : fv[i];          // bead m & ~1
-        const float v1 = odd ? fv[i + 1] : recv;      // bead m | 1
-        const int col = cb + c0 + i + (odd ? 1 : 0);
-        __nv_bfloat16 h0 = __float2bfloat16_rn(v0), h1 = __float2bfloat16_rn(v1);
-        __nv_bfloat162 hh;
-        hh.x = h0;
-        hh.y = h1;
-        const uint32_t lo = pack_bf16(v0 - __bfloat162float(h0), v1 - __bfloat162float(h1));
-        const uint32_t off = x_offset(col, m & ~1);
-        *reinterpret_cast<uint32_t *>(Xhi + off) = *reinterpret_cast<uint32_t *>(&hh);
-        *reinterpret_cast<uint32_t *>(Xlo + off) = lo;
+        const uint32_t h = pack_bf16(fv[i], fv[i + 1]);
+        const uint32_t l = pack_bf16(fv[i] - __uint_as_float(h << 16), fv[i + 1] - __uint_as_float(h & 0xFFFF0000u));
+        const uint32_t hp = __shfl_xor_sync(0xffffffffu, h, 1), lp = __shfl_xor_sync(0xffffffffu, l, 1);
+        const uint32_t off = off0 + (uint32_t)i * 16;
+        *reinterpret_cast<uint32_t *>(Xhi + off) = __byte_perm(h, hp, psel);
+        *reinterpret_cast<uint32_t *>(Xlo + off) = __byte_perm(l, lp, psel);
     }
 }
 
@@ -865,13 +883,14 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_step(TcArgs a) {
             ax->xs[tid] = xs;
             ax->seed[tid] = sd;
             ax->stream[tid] = sm;
+            ax->jdof[tid] = (int32_t)((col0 + tid) % nd);
         }
         tile_load(base, a.q + col0 * kP, nvalid);
         tile_issue(base, sh, tmem, first);
         last_phase = 0;
         first = false;
         float zc[32];
-        tile_normals(ax, col0, nd, cb, m, (uint32_t)s, nv, zc);
+        tile_normals(ax, cb, m, (uint32_t)s, nv, zc);
         ok = tile_wait(sh, 0);
         if (ok) {
 #pragma unroll 1
@@ -1254,17 +1273,14 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tb_kick(TbArgs a) {
                     float z[4];
                     box_muller_f(o.x, o.y, z[0], z[1]);
                     box_muller_f(o.z, o.w, z[2], z[3]);
-                    float rv[4];
-                    rv[0] = sel4(z, e);
-#pragma unroll
-                    for (int r = 1; r < 4; r++) rv[r] = __shfl_xor_sync(0xffffffffu, sel4(z, e ^ r), r);
+                    quad_transpose(z, e);  // z[k]: this mode's normal for column 4g + k
 #pragma unroll
                     for (int k = 0; k < 4; k++) {
                         const int i = 4 * g + k;
                         if (m < P && i < nvg) {
                             const float4 c4 = cfa[i];
                             const float2 c2 = cfb[i];
-                            const float zk = sel4(rv, e ^ k);
+                            const float zk = z[k];
                             const float p0 = pv[i] - dt * gv[i];
                             const float q0 = qv[i];
                             float p1 = c4.x * p0 + c4.y * q0;
