@@ -81,6 +81,7 @@ struct TiState {
     DevBuf bvtab;            // 3P: the sine and scale tables beadvec is formed from
     DevBuf x0, p0;           // FP64 staging of caller-given start positions / momenta
     DevBuf kickflag;         // per-ring Andersen kick flag (blocked tensor form)
+    DevBuf tccol;            // per-column table of the tcgen05 step kernel (spring line, Philox key, weight)
     DevBuf dbdl;             // nlambda*nd
     DevBuf avec, bvec;       // nd start point, nlambda*nd end points
     DevBuf xref;             // nlambda*nd*P

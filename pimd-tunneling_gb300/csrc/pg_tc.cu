@@ -145,15 +145,18 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
     return *reinterpret_cast<uint32_t *>(&h);
 }
 
-// 32 consecutive FP32 columns of this thread's TMEM lane.
+// 32 consecutive FP32 columns of this thread's TMEM lane.  The load and its
+// wait are one asm statement, so no use of the outputs can be scheduled
+// between them.
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&out)[32]) {
     uint32_t v[32];
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,"
-        "%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        "%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+        "tcgen05.wait::ld.sync.aligned;"
         : PG_R32(v)
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        : "r"(taddr)
+        : "memory");
 #pragma unroll
     for (int i = 0; i < 32; i++) out[i] = __uint_as_float(v[i]);
 }
@@ -166,19 +169,21 @@ __device__ __forceinline__ void tmem_ldn(uint32_t taddr, float (&out)[N]) {
     } else if constexpr (N == 16) {
         uint32_t v[16];
         asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+            "tcgen05.wait::ld.sync.aligned;"
             : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
               "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-            : "r"(taddr));
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            : "r"(taddr)
+            : "memory");
 #pragma unroll
         for (int i = 0; i < 16; i++) out[i] = __uint_as_float(v[i]);
     } else {
         uint32_t v[8];
-        asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+                     "tcgen05.wait::ld.sync.aligned;"
                      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
-                     : "r"(taddr));
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                     : "r"(taddr)
+                     : "memory");
 #pragma unroll
         for (int i = 0; i < 8; i++) out[i] = __uint_as_float(v[i]);
     }
@@ -344,6 +349,13 @@ struct TcArgs {
     const uint32_t *ringstream;
     float *q, *pi, *x;        // [ring][dof][P]
     RingAcc *acc;
+    // per state column (ring-major, nrings * nd), built once per batch by k_tc_cols
+    const float *cxa, *cxs;   // spring line x*_m = xa + xs (m + 1)
+    const uint64_t *cseed;
+    const uint32_t *cstream;
+    const int32_t *cjdof;     // dof index of the column within its ring
+    const double *cwest;      // estimator weight mass * db/dlambda
+    const float *fold;        // P x 8: K11 K12 N1 K11 dt | K21 K22 N2 K21 dt (kick + rotation + OU + rotation)
     const int64_t *step0;     // step counter at the start of the advance (not written by these kernels)
     int64_t sofs;             // this launch's step offset within the advance
     int do_est;               // accumulate the estimator of step s-1
@@ -403,6 +415,63 @@ struct TileAux {
     int32_t jdof[kNc];   // the column's dof index within its ring
     int32_t atom[kNc];   // the column's atom
 };
+
+// Per-column values of one chunk of the step kernel, copied in from the
+// column table (cp.async, one chunk ahead).
+struct StepStage {
+    float xa[kNc], xs[kNc];
+    uint64_t seed[kNc];
+    double west[kNc];
+    uint32_t stream[kNc];
+    int32_t jdof[kNc];
+};
+struct StepAux {
+    float xP[kNc];  // bead-P positions for the estimator
+    StepStage stg[2];
+};
+
+__device__ __forceinline__ void cp_async4(void *dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void *dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// Thread t < kNc of the CTA: column col0 + t of the table into sg (zeros for
+// t >= nvalid).  async: cp.async (the caller commits and waits), else loads.
+__device__ __forceinline__ void stage_columns(StepStage *sg, const TcArgs &a, int64_t col0, int nvalid, bool async) {
+    const int t = threadIdx.x;
+    if (t < nvalid) {
+        const int64_t c = col0 + t;
+        if (async) {
+            cp_async4(&sg->xa[t], a.cxa + c);
+            cp_async4(&sg->xs[t], a.cxs + c);
+            cp_async8(&sg->seed[t], a.cseed + c);
+            cp_async8(&sg->west[t], a.cwest + c);
+            cp_async4(&sg->stream[t], a.cstream + c);
+            cp_async4(&sg->jdof[t], a.cjdof + c);
+        } else {
+            sg->xa[t] = a.cxa[c];
+            sg->xs[t] = a.cxs[c];
+            sg->seed[t] = a.cseed[c];
+            sg->west[t] = a.cwest[c];
+            sg->stream[t] = a.cstream[c];
+            sg->jdof[t] = a.cjdof[c];
+        }
+    } else {
+        sg->xa[t] = 0.f;
+        sg->xs[t] = 0.f;
+        sg->seed[t] = 0;
+        sg->west[t] = 0.0;
+        sg->stream[t] = 0;
+        sg->jdof[t] = 0;
+    }
+}
 
 __device__ __forceinline__ void mma_bf16_n64(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t acc) {
     asm volatile(
@@ -671,16 +740,16 @@ __device__ __forceinline__ void group_forces(const TcArgs &a, const float (&xv)[
 
 // Positions x = T q + x* of one group (kGrp columns from c0 of this thread's
 // half), read from TMEM; the bead-P values go to the estimator staging.
-__device__ __forceinline__ void group_positions(const TileAux *ax, uint32_t taddr, int cb, int c0, int m,
-                                                bool stage_p, float (&xv)[kGrp], float *xP) {
+__device__ __forceinline__ void group_positions(const float *sxa, const float *sxs, uint32_t taddr, int cb, int c0,
+                                                int m, bool stage_p, float (&xv)[kGrp], float *xP) {
     __syncwarp();  // tcgen05.ld is .sync.aligned: issue it from a converged warp
     tmem_ldn<kGrp>(taddr + (uint32_t)c0, xv);
     const float fm = (float)(m + 1);
     float xa[kGrp], xs[kGrp];  // 16-byte shared loads (cb + c0 is a multiple of 8)
 #pragma unroll
     for (int i = 0; i < kGrp; i += 4) {
-        const float4 va = *reinterpret_cast<const float4 *>(&ax->xa[cb + c0 + i]);
-        const float4 vs = *reinterpret_cast<const float4 *>(&ax->xs[cb + c0 + i]);
+        const float4 va = *reinterpret_cast<const float4 *>(&sxa[cb + c0 + i]);
+        const float4 vs = *reinterpret_cast<const float4 *>(&sxs[cb + c0 + i]);
         xa[i] = va.x, xa[i + 1] = va.y, xa[i + 2] = va.z, xa[i + 3] = va.w;
         xs[i] = vs.x, xs[i + 1] = vs.y, xs[i + 2] = vs.z, xs[i + 3] = vs.w;
     }
@@ -694,15 +763,13 @@ __device__ __forceinline__ void group_positions(const TileAux *ax, uint32_t tadd
 // Estimator of step s-1 (verletmodule.f90:397-403) from the staged bead-P
 // positions, one thread per ring of the tile, counted down from the last
 // thread (thread 0 issues the GEMMs).
-__device__ __forceinline__ void tile_estimator(const TcArgs &a, const TileAux *ax, int64_t col0, int nvalid,
-                                               int64_t s) {
+__device__ __forceinline__ void tile_estimator(const TcArgs &a, const float *xP, const double *west, int64_t col0,
+                                               int nvalid, int64_t s) {
     const int nd = a.nd, tid = kTileThreads - 1 - (int)threadIdx.x;
     if (tid >= nvalid / nd || (s - 1) < a.imin) return;
     const int64_t ring = col0 / nd + tid;
-    const int lam = a.ringlam[ring];
     double contr = 0.0;
-    for (int j = 0; j < nd; j++)
-        contr += a.mass[j / a.ndim] * (-(double)ax->xP[tid * nd + j]) * a.dbdl[(size_t)lam * nd + j];
+    for (int j = 0; j < nd; j++) contr += west[tid * nd + j] * (-(double)xP[tid * nd + j]);
     RingAcc *r = &a.acc[ring];
     if (r->status == 0) r->dhdr_sum += contr;
     r->nsamples += 1;
@@ -732,7 +799,7 @@ __device__ __forceinline__ void quad_transpose(float (&z)[4], int e) {
     }
 }
 
-__device__ __forceinline__ void tile_normals(const TileAux *ax, int cb, int m, uint32_t st, int nv,
+__device__ __forceinline__ void tile_normals(const StepStage *ax, int cb, int m, uint32_t st, int nv,
                                              float (&zc)[32]) {
     const int e = threadIdx.x & 3;
 #pragma unroll
@@ -792,24 +859,14 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_final(TcArgs a) {
     extern __shared__ unsigned char dsm[];
     unsigned char *base = align1k(dsm);
     TcShared *sh = reinterpret_cast<TcShared *>(base + kTileSmemOps);
-    TileAux *ax = reinterpret_cast<TileAux *>(base + kTileSmemOps + 256);
+    StepAux *aux = reinterpret_cast<StepAux *>(base + kTileSmemOps + 256);
+    StepStage *sg = &aux->stg[0];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int nd = a.nd;
     const int64_t col0 = (int64_t)blockIdx.x * kNc;
     const int nvalid = (int)min((int64_t)kNc, a.nrings * nd - col0);
     const int64_t s = *a.step0 + a.sofs;
-    if (tid < kNc) {
-        float xa = 0.f, xs = 0.f;
-        if (tid < nvalid) {
-            const int64_t ring = (col0 + tid) / nd;
-            const int j = (int)(col0 + tid - ring * nd);
-            const int lam = a.ringlam[ring];
-            xa = (float)a.avec[j];
-            xs = (float)((a.bvec[(size_t)lam * nd + j] - a.avec[j]) / (double)(kP + 1));
-        }
-        ax->xa[tid] = xa;
-        ax->xs[tid] = xs;
-    }
+    if (tid < kNc) stage_columns(sg, a, col0, nvalid, false);
     const uint32_t tmem = tile_begin(base, sh, a.gT, a.q + col0 * kP, nvalid);
     tile_issue(base, sh, tmem, true);
     const bool ok = tile_wait(sh, 0);
@@ -820,7 +877,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_final(TcArgs a) {
 #pragma unroll 1
         for (int c0 = 0; c0 < 32; c0 += kGrp) {
             float xv[kGrp];
-            group_positions(ax, taddr, cb, c0, m, a.do_est != 0, xv, ax->xP);
+            group_positions(sg->xa, sg->xs, taddr, cb, c0, m, a.do_est != 0, xv, aux->xP);
             const int nvg = nvalid - cb - c0;
             float *xo = a.x + (size_t)(col0 + cb + c0) * kP + m;
 #pragma unroll
@@ -829,7 +886,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_final(TcArgs a) {
         }
     }
     __syncthreads();  // xP complete
-    if (ok && a.do_est) tile_estimator(a, ax, col0, nvalid, s);
+    if (ok && a.do_est) tile_estimator(a, aux->xP, sg->west, col0, nvalid, s);
     tile_release(sh, tmem, a.err, 0);
 }
 
@@ -840,15 +897,16 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_final(TcArgs a) {
 //   GEMM 1: x = T q + x*; estimator of step s-1; forces F(x) split straight
 //           into the B operand;
 //   GEMM 2: T F; kick, half rotation, OU (normals drawn while GEMM 1 runs),
-//           half rotation of (q, pi), written back.
-// mma_bar completes two phases per chunk (parities 0 and 1).
+//           half rotation of (q, pi) as one linear map per mode, written back.
+// mma_bar completes two phases per chunk (parities 0 and 1).  The per-column
+// values of the next chunk are copied in (cp.async) while a chunk runs.
 template <int PESK>
 __global__ void __launch_bounds__(kTileThreads, 2) k_tc_step(TcArgs a) {
     extern __shared__ unsigned char dsm[];
     unsigned char *base = align1k(dsm);
     unsigned char *Xhi = base + 2 * kOpBytes, *Xlo = Xhi + kXPlane;
     TcShared *sh = reinterpret_cast<TcShared *>(base + kTileSmemOps);
-    TileAux *ax = reinterpret_cast<TileAux *>(base + kTileSmemOps + 256);
+    StepAux *aux = reinterpret_cast<StepAux *>(base + kTileSmemOps + 256);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int nd = a.nd;
     const int64_t s = *a.step0 + a.sofs;
@@ -857,47 +915,43 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_step(TcArgs a) {
     const int rpc = kNc / nd;  // rings per chunk
     const int m = 32 * (warp & 3) + lane;  // bead (GEMM 1) / mode (GEMM 2)
     const int cb = 32 * (warp >> 2);        // first column of this thread's half
+    if (tid < kNc) {  // first chunk's column values, in flight during the set-up
+        stage_columns(&aux->stg[0], a, r0 * nd, (int)(min((int64_t)rpc, r1 - r0) * nd), true);
+        cp_async_commit();
+    }
     const uint32_t tmem = tile_setup(base, sh, a.gT);
     const uint32_t taddr = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)cb;
+    // kick + rotation + OU + rotation of mode m as one linear map
+    const float4 k1 = *reinterpret_cast<const float4 *>(a.fold + (size_t)m * 8);
+    const float4 k2 = *reinterpret_cast<const float4 *>(a.fold + (size_t)m * 8 + 4);
     bool ok = true;
     uint32_t last_phase = 0;  // parity of the last GEMM issued (for the drain on a timeout)
     bool first = true;
-    for (int64_t rc = r0; rc < r1 && ok; rc += rpc) {
+    int buf = 0;
+    for (int64_t rc = r0; rc < r1 && ok; rc += rpc, buf ^= 1) {
         const int64_t col0 = rc * nd;
         const int nvalid = (int)(min((int64_t)rpc, r1 - rc) * nd);
         const int nv = nvalid - cb;  // valid columns of the half (may be <= 0)
-        if (tid < kNc) {
-            float xa = 0.f, xs = 0.f;
-            uint64_t sd = 0;
-            uint32_t sm = 0;
-            if (tid < nvalid) {
-                const int64_t ring = (col0 + tid) / nd;
-                const int j = (int)(col0 + tid - ring * nd);
-                const int lam = a.ringlam[ring];
-                xa = (float)a.avec[j];
-                xs = (float)((a.bvec[(size_t)lam * nd + j] - a.avec[j]) / (double)(kP + 1));
-                sd = a.ringseed[ring];
-                sm = a.ringstream[ring];
-            }
-            ax->xa[tid] = xa;
-            ax->xs[tid] = xs;
-            ax->seed[tid] = sd;
-            ax->stream[tid] = sm;
-            ax->jdof[tid] = (int32_t)((col0 + tid) % nd);
+        const StepStage *sg = &aux->stg[buf];
+        if (tid < kNc) {  // next chunk's column values into the other buffer
+            const int64_t rn = rc + rpc;
+            if (rn < r1) stage_columns(&aux->stg[buf ^ 1], a, rn * nd, (int)(min((int64_t)rpc, r1 - rn) * nd), true);
+            cp_async_commit();
+            cp_async_wait<1>();  // this chunk's copies (made visible by the barrier in tile_load)
         }
         tile_load(base, a.q + col0 * kP, nvalid);
         tile_issue(base, sh, tmem, first);
         last_phase = 0;
         first = false;
         float zc[32];
-        tile_normals(ax, cb, m, (uint32_t)s, nv, zc);
+        tile_normals(sg, cb, m, (uint32_t)s, nv, zc);
         ok = tile_wait(sh, 0);
         if (ok) {
 #pragma unroll 1
             for (int c0 = 0; c0 < 32; c0 += kGrp) {
                 if (c0 >= nv) break;  // warp-uniform
                 float xv[kGrp], fv[kGrp];
-                group_positions(ax, taddr, cb, c0, m, a.do_est != 0, xv, ax->xP);
+                group_positions(sg->xa, sg->xs, taddr, cb, c0, m, a.do_est != 0, xv, aux->xP);
                 group_forces<PESK>(a, xv, fv);
                 group_store_operand(Xhi, Xlo, cb, c0, m, fv);
             }
@@ -909,13 +963,10 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_step(TcArgs a) {
         if (ok) {
             tile_issue(base, sh, tmem, false);
             last_phase = 1;
-            if (a.do_est) tile_estimator(a, ax, col0, nvalid, s);
+            if (a.do_est) tile_estimator(a, aux->xP, sg->west, col0, nvalid, s);
             ok = tile_wait(sh, 1);
         }
         if (ok) {
-            const float4 c4 = *reinterpret_cast<const float4 *>(a.coef + (size_t)m * 8);
-            const float2 c2 = *reinterpret_cast<const float2 *>(a.coef + (size_t)m * 8 + 4);
-            const float dt = a.dt;
             uint32_t badbits = 0;
 #pragma unroll
             for (int c0 = 0; c0 < 32; c0 += kGrp) {
@@ -934,13 +985,8 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_step(TcArgs a) {
 #pragma unroll
                     for (int i = 0; i < kGrp; i++) {
                         const float zk = zc[c0 + i];
-                        const float p0 = pv[i] - dt * gv[i];
-                        const float q0 = qv[i];
-                        float p1 = c4.x * p0 + c4.y * q0;
-                        const float q1 = c4.z * p0 + c4.w * q0;
-                        p1 = c2.x * p1 + c2.y * zk;
-                        const float pn = c4.x * p1 + c4.y * q1;
-                        const float qn = c4.z * p1 + c4.w * q1;
+                        const float pn = fmaf(k1.x, pv[i], fmaf(-k1.w, gv[i], fmaf(k1.y, qv[i], k1.z * zk)));
+                        const float qn = fmaf(k2.x, pv[i], fmaf(-k2.w, gv[i], fmaf(k2.y, qv[i], k2.z * zk)));
                         if (i < nvg) {
                             qo[(size_t)i * kP] = qn;
                             po[(size_t)i * kP] = pn;
@@ -962,6 +1008,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_step(TcArgs a) {
         __syncthreads();  // TMEM and shared memory of this chunk fully read
         tc_after();
     }
+    if (tid < kNc) cp_async_wait<0>();  // no copy left in flight at exit
     tile_release(sh, tmem, a.err, last_phase);
 }
 
@@ -1445,6 +1492,24 @@ __global__ void k_tb_and_est(TbArgs a) {
     }
 }
 
+// Column table of the step kernel (once per batch): column c = ring * nd + j.
+__global__ void k_tc_cols(int64_t ncols, int nd, int ndim, int P, const int32_t *ringlam, const uint64_t *ringseed,
+                          const uint32_t *ringstream, const double *avec, const double *bvec, const double *dbdl,
+                          const double *mass, float *cxa, float *cxs, uint32_t *cstream, int32_t *cjdof,
+                          uint64_t *cseed, double *cwest) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncols) return;
+    const int64_t ring = c / nd;
+    const int j = (int)(c - ring * nd);
+    const int lam = ringlam[ring];
+    cxa[c] = (float)avec[j];
+    cxs[c] = (float)((bvec[(size_t)lam * nd + j] - avec[j]) / (double)(P + 1));
+    cstream[c] = ringstream[ring];
+    cjdof[c] = j;
+    cseed[c] = ringseed[ring];
+    cwest[c] = mass[j / ndim] * dbdl[(size_t)lam * nd + j];
+}
+
 // Host: split-BF16 image of T, zero-padded to mb x mb blocks of 128 x 128
 // (mb = ceil(P / 128)); block (ib, kb) is a 64 KB [hi | lo] pair in the K-major
 // core-matrix layout of the A operand, at (ib mb + kb) 64 KB.
@@ -1468,13 +1533,16 @@ static void build_split_image(int P, std::vector<unsigned char> &img) {
         }
 }
 
-static size_t tc_smem_bytes() { return (size_t)kTileSmemOps + 1024 + 256 + sizeof(TileAux) + 64; }
+static size_t tc_smem_bytes() {
+    return (size_t)kTileSmemOps + 1024 + 256 + std::max(sizeof(TileAux), sizeof(StepAux)) + 64;
+}
 
 // Tbf layout: [T image mb^2 x 64 KB | FP32 coefficients natom x P x 8 | error word | pad]
 static size_t tbf_coef_off(const TiState &st) { return (size_t)st.tc_mb * st.tc_mb * 2 * kOpBytes; }
 static size_t tbf_err_off(const TiState &st, int natom) {
     return tbf_coef_off(st) + (size_t)natom * st.P * 8 * sizeof(float);
 }
+static size_t tbf_fold_off(const TiState &st, int natom) { return tbf_err_off(st, natom) + 64; }
 
 }  // namespace
 
@@ -1500,7 +1568,7 @@ int tc_prepare(pg_ctx *ctx, TiState &st) {
     build_split_image(st.P, img);
     const int P = st.P;
     size_t ncoef = (size_t)ctx->natom * P * 8;
-    size_t bytes = tbf_err_off(st, ctx->natom) + 64;
+    size_t bytes = tbf_fold_off(st, ctx->natom) + ncoef * sizeof(float);
     cudaError_t e = st.Tbf.ensure(bytes);
     if (e != cudaSuccess) return cuda_fail(e, "tensor-core tables");
     std::vector<ModeCoef> mc((size_t)ctx->natom * P);
@@ -1520,11 +1588,44 @@ int tc_prepare(pg_ctx *ctx, TiState &st) {
             o[5] = (float)c.ou_s;
             o[6] = (float)c.pscale;  // sqrt(beadmass / betan): Andersen momentum scale
         }
+    // (p, q) <- R O R (p - dt g, q) as one map: R the half rotation [rA rB; rC rD],
+    // O the OU step p <- ou_a p + ou_s z, composed in FP64.
+    std::vector<float> fold(ncoef, 0.f);
+    for (int at = 0; at < ctx->natom; at++)
+        for (int k = 0; k < P; k++) {
+            const ModeCoef &c = mc[(size_t)at + (size_t)ctx->natom * k];
+            const double k11 = c.ou_a * c.rA * c.rA + c.rB * c.rC, k12 = c.ou_a * c.rA * c.rB + c.rB * c.rD;
+            const double k21 = c.rC * (c.ou_a * c.rA + c.rD), k22 = c.ou_a * c.rB * c.rC + c.rD * c.rD;
+            float *o = &fold[((size_t)at * P + k) * 8];
+            o[0] = (float)k11;
+            o[1] = (float)k12;
+            o[2] = (float)(c.rA * c.ou_s);
+            o[3] = (float)(k11 * st.cfg.dt);
+            o[4] = (float)k21;
+            o[5] = (float)k22;
+            o[6] = (float)(c.rC * c.ou_s);
+            o[7] = (float)(k21 * st.cfg.dt);
+        }
     unsigned char *d = st.Tbf.as<unsigned char>();
     PG_CUDA(cudaMemcpyAsync(d, img.data(), img.size(), cudaMemcpyHostToDevice, ctx->stream));
     PG_CUDA(cudaMemcpyAsync(d + tbf_coef_off(st), cf.data(), cf.size() * sizeof(float), cudaMemcpyHostToDevice,
                             ctx->stream));
     PG_CUDA(cudaMemsetAsync(d + tbf_err_off(st, ctx->natom), 0, 64, ctx->stream));
+    PG_CUDA(cudaMemcpyAsync(d + tbf_fold_off(st, ctx->natom), fold.data(), fold.size() * sizeof(float),
+                            cudaMemcpyHostToDevice, ctx->stream));
+    {
+        const int64_t ncols = st.nrings * st.nd;
+        e = st.tccol.ensure((size_t)ncols * 32);
+        if (e != cudaSuccess) return cuda_fail(e, "tensor-core column table");
+        unsigned char *cb = st.tccol.as<unsigned char>();
+        k_tc_cols<<<(unsigned)((ncols + 255) / 256), 256, 0, ctx->stream>>>(
+            ncols, st.nd, ctx->ndim, P, st.ringlam.as<int32_t>(), st.ringseed.as<uint64_t>(),
+            st.ringstream.as<uint32_t>(), st.avec.as<double>(), st.bvec.as<double>(), st.dbdl.as<double>(),
+            ctx->d_mass.as<double>(), reinterpret_cast<float *>(cb), reinterpret_cast<float *>(cb + 4 * ncols),
+            reinterpret_cast<uint32_t *>(cb + 8 * ncols), reinterpret_cast<int32_t *>(cb + 12 * ncols),
+            reinterpret_cast<uint64_t *>(cb + 16 * ncols), reinterpret_cast<double *>(cb + 24 * ncols));
+        PG_CUDA(cudaGetLastError());
+    }
     PG_CUDA(cudaStreamSynchronize(ctx->stream));
     size_t sm = tc_smem_bytes();
     PG_CUDA(cudaFuncSetAttribute(k_tc_step<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
@@ -1572,6 +1673,17 @@ static void tc_make_args(pg_ctx *ctx, TiState &st, TcArgs &a, int &pesk) {
     a.pi = st.pi.as<float>();
     a.x = st.x.as<float>();
     a.acc = st.acc.as<RingAcc>();
+    {
+        const int64_t ncols = st.nrings * st.nd;
+        unsigned char *cb = st.tccol.as<unsigned char>();
+        a.cxa = reinterpret_cast<const float *>(cb);
+        a.cxs = reinterpret_cast<const float *>(cb + 4 * ncols);
+        a.cstream = reinterpret_cast<const uint32_t *>(cb + 8 * ncols);
+        a.cjdof = reinterpret_cast<const int32_t *>(cb + 12 * ncols);
+        a.cseed = reinterpret_cast<const uint64_t *>(cb + 16 * ncols);
+        a.cwest = reinterpret_cast<const double *>(cb + 24 * ncols);
+        a.fold = reinterpret_cast<const float *>(d + tbf_fold_off(st, ctx->natom));
+    }
     pesk = ctx->pes_id == PG_PES_2DTEST ? 2 : 1;
     const std::vector<double> &p = ctx->params;
     if (pesk == 2) {

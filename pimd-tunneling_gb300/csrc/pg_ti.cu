@@ -800,7 +800,7 @@ static std::string graph_signature(const pg_ctx *ctx, const TiState &st) {
     add(&ctx->V0, sizeof(double));
     add(ctx->params.data(), ctx->params.size() * sizeof(double));
     add(ctx->mass.data(), ctx->mass.size() * sizeof(double));
-    const void *ptrs[] = {st.q.ptr, st.pi.ptr, st.x.ptr, st.f.ptr, st.T.ptr, st.Tbf.ptr, st.coef.ptr, st.bv.ptr, st.kickflag.ptr,
+    const void *ptrs[] = {st.q.ptr, st.pi.ptr, st.x.ptr, st.f.ptr, st.T.ptr, st.Tbf.ptr, st.coef.ptr, st.bv.ptr, st.kickflag.ptr, st.tccol.ptr,
                           st.dbdl.ptr, st.avec.ptr, st.bvec.ptr, st.xref.ptr, st.ringlam.ptr, st.ringseed.ptr,
                           st.ringstream.ptr, st.acc.ptr, st.red.ptr, ctx->d_params.ptr, ctx->d_fparams.ptr,
                           ctx->d_mass.ptr};
