@@ -597,6 +597,15 @@ __device__ __forceinline__ bool tile_wait(TcShared *sh, uint32_t parity) {
     return sh->err == 0;
 }
 
+// Every thread waits for the GEMM of the given phase itself (no CTA barrier);
+// a timeout is recorded in the CTA error word, which the caller checks after
+// its next barrier.  The chunk structure keeps every thread within one phase
+// of the barrier, so the parity cannot alias.
+__device__ __forceinline__ void tile_wait_own(TcShared *sh, uint32_t parity) {
+    if (!mbar_wait(&sh->mma_bar, parity)) atomicOr(&sh->err, 2);
+    tc_after();
+}
+
 __device__ __forceinline__ void tile_release(TcShared *sh, uint32_t tmem, int32_t *gerr, uint32_t parity) {
     const int tid = threadIdx.x, warp = tid >> 5;
     if (tid == 0 && sh->err) atomicOr(gerr, sh->err);
@@ -924,11 +933,13 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_step(TcArgs a) {
     // kick + rotation + OU + rotation of mode m as one linear map
     const float4 k1 = *reinterpret_cast<const float4 *>(a.fold + (size_t)m * 8);
     const float4 k2 = *reinterpret_cast<const float4 *>(a.fold + (size_t)m * 8 + 4);
-    bool ok = true;
     uint32_t last_phase = 0;  // parity of the last GEMM issued (for the drain on a timeout)
     bool first = true;
     int buf = 0;
-    for (int64_t rc = r0; rc < r1 && ok; rc += rpc, buf ^= 1) {
+    // Three CTA barriers per chunk: operand of GEMM 1 written (tile_load), F
+    // operand written, chunk done.  An error (a bounded wait that gave up)
+    // ends the loop at the chunk-end barrier.
+    for (int64_t rc = r0; rc < r1; rc += rpc, buf ^= 1) {
         const int64_t col0 = rc * nd;
         const int nvalid = (int)(min((int64_t)rpc, r1 - rc) * nd);
         const int nv = nvalid - cb;  // valid columns of the half (may be <= 0)
@@ -945,8 +956,8 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_step(TcArgs a) {
         first = false;
         float zc[32];
         tile_normals(sg, cb, m, (uint32_t)s, nv, zc);
-        ok = tile_wait(sh, 0);
-        if (ok) {
+        tile_wait_own(sh, 0);
+        {
 #pragma unroll 1
             for (int c0 = 0; c0 < 32; c0 += kGrp) {
                 if (c0 >= nv) break;  // warp-uniform
@@ -960,13 +971,11 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_step(TcArgs a) {
         tc_before();
         __syncthreads();  // F operand complete, TMEM reads of GEMM 1 done, xP staged
         tc_after();
-        if (ok) {
-            tile_issue(base, sh, tmem, false);
-            last_phase = 1;
-            if (a.do_est) tile_estimator(a, aux->xP, sg->west, col0, nvalid, s);
-            ok = tile_wait(sh, 1);
-        }
-        if (ok) {
+        tile_issue(base, sh, tmem, false);
+        last_phase = 1;
+        if (a.do_est) tile_estimator(a, aux->xP, sg->west, col0, nvalid, s);
+        tile_wait_own(sh, 1);
+        {
             uint32_t badbits = 0;
 #pragma unroll
             for (int c0 = 0; c0 < 32; c0 += kGrp) {
@@ -1007,6 +1016,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_step(TcArgs a) {
         tc_before();
         __syncthreads();  // TMEM and shared memory of this chunk fully read
         tc_after();
+        if (sh->err) break;  // CTA-uniform: read after the barrier
     }
     if (tid < kNc) cp_async_wait<0>();  // no copy left in flight at exit
     tile_release(sh, tmem, a.err, last_phase);
