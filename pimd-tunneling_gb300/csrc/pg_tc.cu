@@ -684,7 +684,7 @@ __device__ __forceinline__ float ex2f(float v) {
 // The POW10 six-well gradient of grad_2d_n for NR beads (NR even), two rings
 // per packed f32x2 operation: per well dx, dy, u = dx^2 + dy^2,
 // eb = 2^(u (-b0 log2 e)), ea = eb^10, cc = a0 ea + b0 eb, g += cc d.
-template <int NR>
+template <int NR, int NW = 0>  // NW > 0: the well count is NW (loop fully unrolled)
 __device__ __forceinline__ void grad_2d_pow10_x2(const TcArgs &a, const float (&xv)[2 * NR], float (&gx)[NR],
                                                  float (&gy)[NR]) {
     static_assert(NR % 2 == 0, "pairs of rings");
@@ -698,7 +698,9 @@ __device__ __forceinline__ void grad_2d_pow10_x2(const TcArgs &a, const float (&
     }
     const float nb = -a.b0 * 1.4426950408889634f;
     const uint64_t A0 = pk2(a.a0, a.a0), B0 = pk2(a.b0, a.b0), NB = pk2(nb, nb);
-    for (int k = 0; k < a.nwell; k++) {
+    const int nw = NW > 0 ? NW : a.nwell;
+#pragma unroll
+    for (int k = 0; k < nw; k++) {
         const uint64_t MWX = pk2(-a.wc[2 * k], -a.wc[2 * k]), MWY = pk2(-a.wc[2 * k + 1], -a.wc[2 * k + 1]);
 #pragma unroll
         for (int r = 0; r < NR / 2; r++) {
@@ -728,7 +730,9 @@ __device__ __forceinline__ void group_forces(const TcArgs &a, const float (&xv)[
     if constexpr (PESK == 2) {
         constexpr int NR = kGrp / 2;
         float gx[NR], gy[NR];
-        if (a.pow10)
+        if (a.pow10 && a.nwell == 6)  // the mcmod_2dtest default (m = 6)
+            grad_2d_pow10_x2<NR, 6>(a, xv, gx, gy);
+        else if (a.pow10)
             grad_2d_pow10_x2<NR>(a, xv, gx, gy);
         else
             grad_2d_n<false, NR>(a, xv, gx, gy);
@@ -808,32 +812,22 @@ __device__ __forceinline__ void quad_transpose(float (&z)[4], int e) {
     }
 }
 
-__device__ __forceinline__ void tile_normals(const StepStage *ax, int cb, int m, uint32_t st, int nv,
-                                             float (&zc)[32]) {
+// The 8 OU normals of this thread's mode m for columns cb + c0 .. + 7: lane e
+// of a quad draws the blocks of columns cb + c0 + e and cb + c0 + 4 + e.
+__device__ __forceinline__ void group_normals(const StepStage *ax, int cb, int c0, int m, uint32_t st,
+                                              float (&zg)[kGrp]) {
     const int e = threadIdx.x & 3;
 #pragma unroll
-    for (int g0 = 0; g0 < 8; g0 += 4) {
-        if (4 * g0 >= nv) {  // no valid column in these 16 (warp-uniform)
+    for (int g = 0; g < 2; g++) {
+        const int cc = cb + c0 + 4 * g + e;
+        const U4 o = philox_block(ax->seed[cc], ax->stream[cc], st, kRngLangevin,
+                                  (uint32_t)((ax->jdof[cc] * kP + m) >> 2));
+        float z[4];
+        box_muller_f(o.x, o.y, z[0], z[1]);
+        box_muller_f(o.z, o.w, z[2], z[3]);
+        quad_transpose(z, e);
 #pragma unroll
-            for (int k = 0; k < 16; k++) zc[4 * g0 + k] = 0.f;
-            continue;
-        }
-        U4 o[4];
-#pragma unroll
-        for (int g = 0; g < 4; g++) {
-            const int cc = cb + 4 * (g0 + g) + e;
-            o[g] = philox_block(ax->seed[cc], ax->stream[cc], st, kRngLangevin,
-                                (uint32_t)((ax->jdof[cc] * kP + m) >> 2));
-        }
-#pragma unroll
-        for (int g = 0; g < 4; g++) {
-            float z[4];
-            box_muller_f(o[g].x, o[g].y, z[0], z[1]);
-            box_muller_f(o[g].z, o[g].w, z[2], z[3]);
-            quad_transpose(z, e);
-#pragma unroll
-            for (int k = 0; k < 4; k++) zc[4 * (g0 + g) + k] = z[k];
-        }
+        for (int k = 0; k < 4; k++) zg[4 * g + k] = z[k];
     }
 }
 
@@ -905,8 +899,10 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_final(TcArgs a) {
 // up to 64 columns.  T is copied in and TMEM allocated once per CTA.  Per chunk:
 //   GEMM 1: x = T q + x*; estimator of step s-1; forces F(x) split straight
 //           into the B operand;
-//   GEMM 2: T F; kick, half rotation, OU (normals drawn while GEMM 1 runs),
-//           half rotation of (q, pi) as one linear map per mode, written back.
+//   GEMM 2: T F; kick, half rotation, OU, half rotation of (q, pi) as one
+//           linear map per mode (normals drawn while the state loads), written back.
+// The chunk's 8-column groups alternate between the two warp halves (half h
+// takes groups h, h + 2, ...), so that a partial chunk loads both halves alike.
 // mma_bar completes two phases per chunk (parities 0 and 1).  The per-column
 // values of the next chunk are copied in (cp.async) while a chunk runs.
 template <int PESK>
@@ -923,13 +919,13 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_step(TcArgs a) {
     const int64_t r1 = ((int64_t)blockIdx.x + 1) * a.nrings / gridDim.x;
     const int rpc = kNc / nd;  // rings per chunk
     const int m = 32 * (warp & 3) + lane;  // bead (GEMM 1) / mode (GEMM 2)
-    const int cb = 32 * (warp >> 2);        // first column of this thread's half
+    const int hh = warp >> 2;               // warp half: column groups hh, hh + 2, hh + 4, hh + 6
     if (tid < kNc) {  // first chunk's column values, in flight during the set-up
         stage_columns(&aux->stg[0], a, r0 * nd, (int)(min((int64_t)rpc, r1 - r0) * nd), true);
         cp_async_commit();
     }
     const uint32_t tmem = tile_setup(base, sh, a.gT);
-    const uint32_t taddr = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)cb;
+    const uint32_t tlane = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
     // kick + rotation + OU + rotation of mode m as one linear map
     const float4 k1 = *reinterpret_cast<const float4 *>(a.fold + (size_t)m * 8);
     const float4 k2 = *reinterpret_cast<const float4 *>(a.fold + (size_t)m * 8 + 4);
@@ -942,7 +938,6 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_step(TcArgs a) {
     for (int64_t rc = r0; rc < r1; rc += rpc, buf ^= 1) {
         const int64_t col0 = rc * nd;
         const int nvalid = (int)(min((int64_t)rpc, r1 - rc) * nd);
-        const int nv = nvalid - cb;  // valid columns of the half (may be <= 0)
         const StepStage *sg = &aux->stg[buf];
         if (tid < kNc) {  // next chunk's column values into the other buffer
             const int64_t rn = rc + rpc;
@@ -954,17 +949,16 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_step(TcArgs a) {
         tile_issue(base, sh, tmem, first);
         last_phase = 0;
         first = false;
-        float zc[32];
-        tile_normals(sg, cb, m, (uint32_t)s, nv, zc);
         tile_wait_own(sh, 0);
         {
 #pragma unroll 1
-            for (int c0 = 0; c0 < 32; c0 += kGrp) {
-                if (c0 >= nv) break;  // warp-uniform
+            for (int g = 0; g < 4; g++) {
+                const int gc = 16 * g + 8 * hh;  // first column of the group
+                if (gc >= nvalid) break;         // warp-uniform
                 float xv[kGrp], fv[kGrp];
-                group_positions(sg->xa, sg->xs, taddr, cb, c0, m, a.do_est != 0, xv, aux->xP);
+                group_positions(sg->xa, sg->xs, tlane + (uint32_t)gc, gc, 0, m, a.do_est != 0, xv, aux->xP);
                 group_forces<PESK>(a, xv, fv);
-                group_store_operand(Xhi, Xlo, cb, c0, m, fv);
+                group_store_operand(Xhi, Xlo, gc, 0, m, fv);
             }
             fence_async_smem();
         }
@@ -977,29 +971,31 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_step(TcArgs a) {
         tile_wait_own(sh, 1);
         {
             uint32_t badbits = 0;
-#pragma unroll
-            for (int c0 = 0; c0 < 32; c0 += kGrp) {
-                if (c0 < nv) {  // warp-uniform
-                    const int nvg = nv - c0;
-                    float *qo = a.q + (size_t)(col0 + cb + c0) * kP + m;
-                    float *po = a.pi + (size_t)(col0 + cb + c0) * kP + m;
-                    float qv[kGrp], pv[kGrp], gv[kGrp];
+#pragma unroll 1
+            for (int g = 0; g < 4; g++) {
+                const int gc = 16 * g + 8 * hh;
+                if (gc < nvalid) {  // warp-uniform
+                    const int nvg = nvalid - gc;
+                    float *qo = a.q + (size_t)(col0 + gc) * kP + m;
+                    float *po = a.pi + (size_t)(col0 + gc) * kP + m;
+                    float qv[kGrp], pv[kGrp], gv[kGrp], zg[kGrp];
 #pragma unroll
                     for (int i = 0; i < kGrp; i++) {
                         qv[i] = i < nvg ? qo[(size_t)i * kP] : 0.f;
                         pv[i] = i < nvg ? po[(size_t)i * kP] : 0.f;
                     }
+                    group_normals(sg, gc, 0, m, (uint32_t)s, zg);  // while the loads are in flight
                     __syncwarp();
-                    tmem_ldn<kGrp>(taddr + (uint32_t)c0, gv);
+                    tmem_ldn<kGrp>(tlane + (uint32_t)gc, gv);
 #pragma unroll
                     for (int i = 0; i < kGrp; i++) {
-                        const float zk = zc[c0 + i];
+                        const float zk = zg[i];
                         const float pn = fmaf(k1.x, pv[i], fmaf(-k1.w, gv[i], fmaf(k1.y, qv[i], k1.z * zk)));
                         const float qn = fmaf(k2.x, pv[i], fmaf(-k2.w, gv[i], fmaf(k2.y, qv[i], k2.z * zk)));
                         if (i < nvg) {
                             qo[(size_t)i * kP] = qn;
                             po[(size_t)i * kP] = pn;
-                            if (pn != pn) badbits |= 1u << (c0 + i);
+                            if (pn != pn) badbits |= 1u << (8 * g + i);
                         }
                     }
                 }
@@ -1008,7 +1004,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_step(TcArgs a) {
             if (lane == 0 && badbits) {
                 for (int i = 0; i < 32; i++)
                     if (badbits & (1u << i)) {
-                        const int64_t ring = (col0 + cb + i) / nd;
+                        const int64_t ring = (col0 + 16 * (i >> 3) + 8 * hh + (i & 7)) / nd;
                         if (atomicOr(&a.acc[ring].status, PG_RING_NAN) == 0) a.acc[ring].pad = (int32_t)s;
                     }
             }
