@@ -437,6 +437,12 @@ __device__ __forceinline__ void cp_async8(void *dst, const void *src) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// Programmatic dependent launch: both are no-ops for a launch without the
+// programmatic-serialization attribute.
+__device__ __forceinline__ void griddep_launch_dependents() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() {
     asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
@@ -913,8 +919,10 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_step(TcArgs a) {
     TcShared *sh = reinterpret_cast<TcShared *>(base + kTileSmemOps);
     StepAux *aux = reinterpret_cast<StepAux *>(base + kTileSmemOps + 256);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // The next launch of the advance may begin its set-up now (programmatic
+    // dependent launch); it reads no ring state before griddep_wait().
+    griddep_launch_dependents();
     const int nd = a.nd;
-    const int64_t s = *a.step0 + a.sofs;
     const int64_t r0 = (int64_t)blockIdx.x * a.nrings / gridDim.x;
     const int64_t r1 = ((int64_t)blockIdx.x + 1) * a.nrings / gridDim.x;
     const int rpc = kNc / nd;  // rings per chunk
@@ -929,6 +937,10 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_step(TcArgs a) {
     // kick + rotation + OU + rotation of mode m as one linear map
     const float4 k1 = *reinterpret_cast<const float4 *>(a.fold + (size_t)m * 8);
     const float4 k2 = *reinterpret_cast<const float4 *>(a.fold + (size_t)m * 8 + 4);
+    // Set-up above used constant tables only; q, pi, the accumulators and the
+    // step counter are read after the previous launch has completed.
+    griddep_wait();
+    const int64_t s = *a.step0 + a.sofs;
     uint32_t last_phase = 0;  // parity of the last GEMM issued (for the drain on a timeout)
     bool first = true;
     int buf = 0;
@@ -1722,11 +1734,20 @@ static int tc_launch_step(pg_ctx *ctx, TiState &st, int64_t i, cudaStream_t s) {
     // persistent: two CTAs per SM (the shared-memory limit), equal ring ranges
     const unsigned grid = (unsigned)std::min<int64_t>(2 * (int64_t)(ctx->sm_count > 0 ? ctx->sm_count : 1),
                                                       (int64_t)tc_grid(st));
-    if (pesk == 2)
-        k_tc_step<2><<<grid, kTileThreads, sm, s>>>(a);
-    else
-        k_tc_step<1><<<grid, kTileThreads, sm, s>>>(a);
-    cudaError_t e = cudaGetLastError();
+    // programmatic serialization: this launch's set-up overlaps the tail of the
+    // previous one (the kernel waits for it before touching the ring state)
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kTileThreads);
+    cfg.dynamicSmemBytes = sm;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaError_t e = pesk == 2 ? cudaLaunchKernelEx(&cfg, k_tc_step<2>, a) : cudaLaunchKernelEx(&cfg, k_tc_step<1>, a);
+    if (e == cudaSuccess) e = cudaGetLastError();
     return e == cudaSuccess ? PG_OK : cuda_fail(e, "k_tc_step launch");
 }
 
