@@ -38,6 +38,7 @@ import numpy as np  # noqa: E402
 METRIC = "bead-force-steps/s, batched mixed-prec vs plain FP64 on 1 GB300 at <=1% split err"
 UNIT = "bead-force-steps/s"
 MD_PER_STEP = 500
+KT_STEPS = 50  # MD steps of the per-kernel timing (one k_tc_step launch of the tensor form)
 
 
 def _peaks():
@@ -306,7 +307,7 @@ def main():
 
     peaks, peak_kind = _peaks()
     # Dominant kernel, timed live with CUDA events on the library stream.
-    kt = ctx.ti_kernel_times(20) if not (ws > 1 and rank != 0) else []
+    kt = ctx.ti_kernel_times(KT_STEPS) if not (ws > 1 and rank != 0) else []
     roof = None
     if kt:
         name, kms, kcount, kbytes = max(kt, key=lambda t: t[1] * t[2])
@@ -317,8 +318,10 @@ def main():
                 traffic = json.load(f).get(name.split()[0])
         except Exception:
             pass
-        # tensor view: one transform (2 P ndof flops per bead) per launch
-        tflops = 2.0 * ti.P * ti.nd * beads / (kms / 1e3) / 1e12
+        # tensor view: two transforms per MD step (T q and T F), 2 P ndof useful
+        # flops per bead each; MD steps per launch from the state bytes per step
+        msteps = max(1, round(kbytes / (16.0 * beads * ti.nd)))
+        tflops = 4.0 * ti.P * ti.nd * beads * msteps / (kms / 1e3) / 1e12
         roof = {"bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved_gbs / peaks["hbm_gbs"], "traffic": traffic, "peak_source": peak_kind,
                 "kernel": name, "kernel_ms": kms, "algorithmic_bytes_per_launch": kbytes,

@@ -156,8 +156,9 @@ int pg_ti_advance_group(pg_ctx *const *ctxs, int64_t nctx, int64_t nsteps, doubl
 /* Advance nsteps with one CUDA-event pair around every kernel launch (no graph)
  * and report, for up to 4 kernel kinds of the chosen form, the mean device time
  * per launch (ms_per_launch[k]), the launches (count[k]), and the algorithmic
- * HBM bytes one launch moves (bytes_per_launch[k]); names[k] points to a static
- * kernel name.  Returns the number of kinds in *nkinds. */
+ * HBM bytes one launch moves (bytes_per_launch[k]); names[k] points to the
+ * kernel's name (valid until the next call on the same thread).  Returns the
+ * number of kinds in *nkinds. */
 int pg_ti_kernel_times(pg_ctx *ctx, int64_t nsteps, int32_t *nkinds, double *ms_per_launch,
                        int64_t *count, double *bytes_per_launch, const char **names);
 /* Cartesian positions and momenta of every ring (nrings*ndof*P each; either may be NULL). */

@@ -132,5 +132,6 @@ int tc_prepare(pg_ctx *ctx, TiState &st);
 int tc_launch(pg_ctx *ctx, TiState &st, int64_t step0, int64_t nsteps, cudaStream_t s);
 int tc_nm_transform(pg_ctx *ctx, int64_t P, int64_t ncol, const double *in, double *out);
 int32_t tc_error(pg_ctx *ctx, TiState &st);
-int tc_kernel_times(pg_ctx *ctx, TiState &st, int64_t nsteps, double *ms, int64_t *count);
+int tc_kernel_times(pg_ctx *ctx, TiState &st, int64_t nsteps, double *ms, int64_t *count, int *nsub);
+int tc_steps_per_launch();  // MD steps per k_tc_step launch
 }  // namespace pg

@@ -359,6 +359,7 @@ struct TcArgs {
     const int64_t *step0;     // step counter at the start of the advance (not written by these kernels)
     int64_t sofs;             // this launch's step offset within the advance
     int do_est;               // accumulate the estimator of step s-1
+    int nsub;                 // k_tc_step: MD steps sofs .. sofs + nsub - 1 in this launch
     int32_t *err;
     // PES parameters (FP32)
     float wc[12];
@@ -940,20 +941,31 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_step(TcArgs a) {
     // Set-up above used constant tables only; q, pi, the accumulators and the
     // step counter are read after the previous launch has completed.
     griddep_wait();
-    const int64_t s = *a.step0 + a.sofs;
+    const int64_t s0 = *a.step0 + a.sofs;
     uint32_t last_phase = 0;  // parity of the last GEMM issued (for the drain on a timeout)
     bool first = true;
     int buf = 0;
-    // Three CTA barriers per chunk: operand of GEMM 1 written (tile_load), F
-    // operand written, chunk done.  An error (a bounded wait that gave up)
-    // ends the loop at the chunk-end barrier.
-    for (int64_t rc = r0; rc < r1; rc += rpc, buf ^= 1) {
+    // Chunks of the CTA's rings, step after step (the rings of a CTA are the
+    // same in every step, so no step waits for another CTA).  Three CTA
+    // barriers per chunk: operand of GEMM 1 written (tile_load), F operand
+    // written, chunk done.  An error (a bounded wait that gave up) ends the
+    // loop at the chunk-end barrier.
+    int sub = 0;
+    for (int64_t rc = r0; sub < a.nsub; buf ^= 1) {
+        const int64_t s = s0 + sub;
+        const bool est = a.sofs + sub > 0;  // the estimator of step s - 1
         const int64_t col0 = rc * nd;
         const int nvalid = (int)(min((int64_t)rpc, r1 - rc) * nd);
         const StepStage *sg = &aux->stg[buf];
+        int64_t rn = rc + rpc;  // the next chunk (the first one of the next step after the last)
+        int subn = sub;
+        if (rn >= r1) {
+            rn = r0;
+            subn = sub + 1;
+        }
         if (tid < kNc) {  // next chunk's column values into the other buffer
-            const int64_t rn = rc + rpc;
-            if (rn < r1) stage_columns(&aux->stg[buf ^ 1], a, rn * nd, (int)(min((int64_t)rpc, r1 - rn) * nd), true);
+            if (subn < a.nsub)
+                stage_columns(&aux->stg[buf ^ 1], a, rn * nd, (int)(min((int64_t)rpc, r1 - rn) * nd), true);
             cp_async_commit();
             cp_async_wait<1>();  // this chunk's copies (made visible by the barrier in tile_load)
         }
@@ -968,7 +980,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_step(TcArgs a) {
                 const int gc = 16 * g + 8 * hh;  // first column of the group
                 if (gc >= nvalid) break;         // warp-uniform
                 float xv[kGrp], fv[kGrp];
-                group_positions(sg->xa, sg->xs, tlane + (uint32_t)gc, gc, 0, m, a.do_est != 0, xv, aux->xP);
+                group_positions(sg->xa, sg->xs, tlane + (uint32_t)gc, gc, 0, m, est, xv, aux->xP);
                 group_forces<PESK>(a, xv, fv);
                 group_store_operand(Xhi, Xlo, gc, 0, m, fv);
             }
@@ -979,7 +991,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_step(TcArgs a) {
         tc_after();
         tile_issue(base, sh, tmem, false);
         last_phase = 1;
-        if (a.do_est) tile_estimator(a, aux->xP, sg->west, col0, nvalid, s);
+        if (est) tile_estimator(a, aux->xP, sg->west, col0, nvalid, s);
         tile_wait_own(sh, 1);
         {
             uint32_t badbits = 0;
@@ -1025,6 +1037,8 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_step(TcArgs a) {
         __syncthreads();  // TMEM and shared memory of this chunk fully read
         tc_after();
         if (sh->err) break;  // CTA-uniform: read after the barrier
+        rc = rn;
+        sub = subn;
     }
     if (tid < kNc) cp_async_wait<0>();  // no copy left in flight at exit
     tile_release(sh, tmem, a.err, last_phase);
@@ -1724,12 +1738,13 @@ static void tc_make_args(pg_ctx *ctx, TiState &st, TcArgs &a, int &pesk) {
 static unsigned tc_grid(const TiState &st) { return (unsigned)((st.nrings * st.nd + kNc - 1) / kNc); }
 
 // Step i of an advance (k_tc_step), or the final pass after n steps (k_tc_final).
-static int tc_launch_step(pg_ctx *ctx, TiState &st, int64_t i, cudaStream_t s) {
+static int tc_launch_step(pg_ctx *ctx, TiState &st, int64_t i, int nsub, cudaStream_t s) {
     TcArgs a;
     int pesk;
     tc_make_args(ctx, st, a, pesk);
     a.sofs = i;
     a.do_est = i > 0 ? 1 : 0;
+    a.nsub = nsub;
     const size_t sm = tc_smem_bytes();
     // persistent: two CTAs per SM (the shared-memory limit), equal ring ranges
     const unsigned grid = (unsigned)std::min<int64_t>(2 * (int64_t)(ctx->sm_count > 0 ? ctx->sm_count : 1),
@@ -1871,11 +1886,16 @@ static int tb_launch(pg_ctx *ctx, TiState &st, int64_t nsteps, cudaStream_t s) {
     return e == cudaSuccess ? PG_OK : cuda_fail(e, "step counter launch");
 }
 
+// MD steps per k_tc_step launch (the per-launch set-up, mainly the 64 KB copy
+// of T into every CTA, is paid once per launch).
+constexpr int kStepsPerLaunch = 50;
+int tc_steps_per_launch() { return kStepsPerLaunch; }
+
 int tc_launch(pg_ctx *ctx, TiState &st, int64_t, int64_t nsteps, cudaStream_t s) {
     if (nsteps < 0) return PG_OK;  // the HBM copy of the state is current after every advance
     if (st.tc_blocked) return tb_launch(ctx, st, nsteps, s);
-    for (int64_t i = 0; i < nsteps; i++) {
-        int rc = tc_launch_step(ctx, st, i, s);
+    for (int64_t i = 0; i < nsteps; i += kStepsPerLaunch) {
+        int rc = tc_launch_step(ctx, st, i, (int)std::min<int64_t>(kStepsPerLaunch, nsteps - i), s);
         if (rc) return rc;
     }
     return tc_launch_final(ctx, st, nsteps, s);
@@ -1938,34 +1958,44 @@ static int tb_kernel_times(pg_ctx *ctx, TiState &st, int64_t nsteps, double *ms,
     return PG_OK;
 }
 
-int tc_kernel_times(pg_ctx *ctx, TiState &st, int64_t nsteps, double *ms, int64_t *count) {
-    if (st.tc_blocked) return tb_kernel_times(ctx, st, nsteps, ms, count);
+// Per-kernel event timing of nsteps steps (direct launches, no graph): ms[0] =
+// k_tc_step per launch (count[0] launches of nsub[0] steps each; a shorter
+// last launch is not timed), ms[1] = k_tc_final.
+int tc_kernel_times(pg_ctx *ctx, TiState &st, int64_t nsteps, double *ms, int64_t *count, int *nsub) {
+    if (st.tc_blocked) {
+        *nsub = 1;
+        return tb_kernel_times(ctx, st, nsteps, ms, count);
+    }
     cudaStream_t s = ctx->stream;
-    std::vector<cudaEvent_t> ev(nsteps + 3);
+    const int per = (int)std::min<int64_t>(kStepsPerLaunch, nsteps);
+    const int64_t nl = (nsteps + per - 1) / per;
+    std::vector<cudaEvent_t> ev(nl + 2);
     for (auto &e : ev) PG_CUDA(cudaEventCreate(&e));
-    for (int64_t i = 0; i < nsteps; i++) {
-        PG_CUDA(cudaEventRecord(ev[i], s));
-        int rc = tc_launch_step(ctx, st, i, s);
+    for (int64_t l = 0; l < nl; l++) {
+        PG_CUDA(cudaEventRecord(ev[l], s));
+        int rc = tc_launch_step(ctx, st, l * per, (int)std::min<int64_t>(per, nsteps - l * per), s);
         if (rc) return rc;
     }
-    PG_CUDA(cudaEventRecord(ev[nsteps], s));
+    PG_CUDA(cudaEventRecord(ev[nl], s));
     int rc = tc_launch_final(ctx, st, nsteps, s);  // includes the step-counter add
     if (rc) return rc;
-    PG_CUDA(cudaEventRecord(ev[nsteps + 1], s));
+    PG_CUDA(cudaEventRecord(ev[nl + 1], s));
     PG_CUDA(cudaStreamSynchronize(s));
+    const int64_t nfull = nsteps / per;  // launches of exactly `per` steps
     double t1 = 0.0;
-    for (int64_t i = 0; i < nsteps; i++) {
+    for (int64_t l = 0; l < nfull; l++) {
         float a = 0.f;
-        PG_CUDA(cudaEventElapsedTime(&a, ev[i], ev[i + 1]));
+        PG_CUDA(cudaEventElapsedTime(&a, ev[l], ev[l + 1]));
         t1 += a;
     }
     float a2 = 0.f;
-    PG_CUDA(cudaEventElapsedTime(&a2, ev[nsteps], ev[nsteps + 1]));
+    PG_CUDA(cudaEventElapsedTime(&a2, ev[nl], ev[nl + 1]));
     for (auto &e : ev) cudaEventDestroy(e);
-    ms[0] = t1 / (double)nsteps;
+    ms[0] = t1 / (double)nfull;
     ms[1] = a2;
-    count[0] = nsteps;
+    count[0] = nfull;
     count[1] = 1;
+    *nsub = per;
     return PG_OK;
 }
 

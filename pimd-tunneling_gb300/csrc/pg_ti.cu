@@ -1207,7 +1207,8 @@ extern "C" int pg_ti_kernel_times(pg_ctx *ctx, int64_t nsteps, int32_t *nkinds, 
         if (st.tc_blocked && st.cfg.thermostat == PG_ANDERSEN) {
             double ms3[3];
             int64_t n3[3];
-            rc = tc_kernel_times(ctx, st, nsteps, ms3, n3);
+            int nsub = 1;
+            rc = tc_kernel_times(ctx, st, nsteps, ms3, n3, &nsub);
             if (rc) return rc;
             *nkinds = 1;
             ms_per_launch[0] = ms3[0];
@@ -1217,7 +1218,8 @@ extern "C" int pg_ti_kernel_times(pg_ctx *ctx, int64_t nsteps, int32_t *nkinds, 
         } else if (st.tc_blocked) {
             double ms3[3];
             int64_t n3[3];
-            rc = tc_kernel_times(ctx, st, nsteps, ms3, n3);
+            int nsub = 1;
+            rc = tc_kernel_times(ctx, st, nsteps, ms3, n3, &nsub);
             if (rc) return rc;
             *nkinds = 3;
             for (int k = 0; k < 3; k++) {
@@ -1233,17 +1235,21 @@ extern "C" int pg_ti_kernel_times(pg_ctx *ctx, int64_t nsteps, int32_t *nkinds, 
                 names[2] = "k_tb_kick (T F: blocked split-BF16 tcgen05 GEMM; kick, rotation, OU)";
             }
         } else {
-            rc = tc_kernel_times(ctx, st, nsteps, ms, n);
+            int nsub = 1;
+            rc = tc_kernel_times(ctx, st, nsteps, ms, n, &nsub);
             if (rc) return rc;
             *nkinds = 2;
             ms_per_launch[0] = ms[0];
             ms_per_launch[1] = ms[1];
             count[0] = n[0];
             count[1] = n[1];
-            bytes_per_launch[0] = 4.0 * arr;  // k_tc_step: read q, pi; write q, pi
-            bytes_per_launch[1] = 2.0 * arr;  // k_tc_final: read q, write x
+            bytes_per_launch[0] = 4.0 * arr * nsub;  // k_tc_step: read q, pi; write q, pi; per MD step
+            bytes_per_launch[1] = 2.0 * arr;         // k_tc_final: read q, write x
             if (names) {
-                names[0] = "k_tc_step (one MD step: two split-BF16 tcgen05 GEMMs, forces, OU)";
+                static thread_local std::string step_name;
+                step_name = "k_tc_step (" + std::to_string(nsub) +
+                            " MD steps per launch, each two split-BF16 tcgen05 GEMMs, forces, OU)";
+                names[0] = step_name.c_str();
                 names[1] = "k_tc_final (positions and last estimator; one split-BF16 tcgen05 GEMM)";
             }
         }
@@ -1275,8 +1281,8 @@ extern "C" int pg_ti_get_form(pg_ctx *ctx, int64_t nsteps, int32_t *form, int64_
             *launches = nsteps > 0 ? 6 * nsteps + 2 : 0;  // six per step; positions, counter
         else if (st.form == PG_FORM_TENSOR && st.tc_blocked)
             *launches = nsteps > 0 ? 3 * nsteps + 3 : 0;  // pos, force, kick per step; pos, estimator, counter
-        else if (st.form == PG_FORM_TENSOR)
-            *launches = nsteps > 0 ? nsteps + 2 : 0;  // one step kernel per step; final pass, counter
+        else if (st.form == PG_FORM_TENSOR)  // step kernels of up to tc_steps_per_launch() steps; final pass, counter
+            *launches = nsteps > 0 ? (nsteps + tc_steps_per_launch() - 1) / tc_steps_per_launch() + 2 : 0;
         else if (st.form == PG_FORM_FUSED)
             *launches = nsteps > 0 ? 2 : 0;  // fused kernel + step counter
         else
