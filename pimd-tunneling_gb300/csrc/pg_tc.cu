@@ -188,6 +188,17 @@ __device__ __forceinline__ void tmem_ldn(uint32_t taddr, float (&out)[N]) {
         for (int i = 0; i < 8; i++) out[i] = __uint_as_float(v[i]);
     }
 }
+// 8 FP32 values into consecutive TMEM columns of this thread's lane; the
+// store and its wait are one asm statement (a later tcgen05.ld of the same
+// columns by this thread sees them).
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const float (&v)[8]) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};\n"
+        "tcgen05.wait::st.sync.aligned;" ::"r"(taddr),
+        "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])), "r"(__float_as_uint(v[3])),
+        "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])), "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7]))
+        : "memory");
+}
 // Write 32 FP32 values of row `row`, K = k0..k0+31, into the hi / lo operand images.
 __device__ __forceinline__ void write_split32(unsigned char *Ahi, unsigned char *Alo, int row, int k0,
                                               const float (&v)[32]) {
@@ -507,7 +518,8 @@ __device__ __forceinline__ void split8(const float (&v)[8], uint4 &hi, uint4 &lo
 
 // One-time set-up of a CTA: barriers, the T image by bulk copy (completes
 // tma_bar phase 0), kNc TMEM columns.  Returns the TMEM base address.
-__device__ __forceinline__ uint32_t tile_setup(unsigned char *base, TcShared *sh, const unsigned char *gT) {
+__device__ __forceinline__ uint32_t tile_setup(unsigned char *base, TcShared *sh, const unsigned char *gT,
+                                               uint32_t ncols = kNc) {
     const int tid = threadIdx.x, warp = tid >> 5;
     if (tid == 0) {
         mbar_init(&sh->mma_bar, 1);
@@ -519,7 +531,7 @@ __device__ __forceinline__ uint32_t tile_setup(unsigned char *base, TcShared *sh
     load_transform(base, gT, sh);
     if (warp == 0) {
         __syncwarp();
-        tmem_alloc(&sh->tmem_slot, kNc);
+        tmem_alloc(&sh->tmem_slot, ncols);
     }
     tc_before();
     __syncthreads();
@@ -613,7 +625,8 @@ __device__ __forceinline__ void tile_wait_own(TcShared *sh, uint32_t parity) {
     tc_after();
 }
 
-__device__ __forceinline__ void tile_release(TcShared *sh, uint32_t tmem, int32_t *gerr, uint32_t parity) {
+__device__ __forceinline__ void tile_release(TcShared *sh, uint32_t tmem, int32_t *gerr, uint32_t parity,
+                                             uint32_t ncols = kNc) {
     const int tid = threadIdx.x, warp = tid >> 5;
     if (tid == 0 && sh->err) atomicOr(gerr, sh->err);
     if (sh->err & 2) mbar_wait(&sh->mma_bar, parity);  // let an overdue MMA drain (bounded)
@@ -621,7 +634,7 @@ __device__ __forceinline__ void tile_release(TcShared *sh, uint32_t tmem, int32_
     __syncthreads();
     if (warp == 0) {
         __syncwarp();
-        tmem_dealloc(tmem, kNc);
+        tmem_dealloc(tmem, ncols);
     }
 }
 
@@ -912,7 +925,12 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_final(TcArgs a) {
 // takes groups h, h + 2, ...), so that a partial chunk loads both halves alike.
 // mma_bar completes two phases per chunk (parities 0 and 1).  The per-column
 // values of the next chunk are copied in (cp.async) while a chunk runs.
-template <int PESK>
+// QT (a CTA holds at most two chunks): q stays in tensor memory for the whole
+// launch, TMEM columns 64 (k + 1) .. + 63 for chunk k (lane = mode, as the
+// accumulator); it is read from HBM / L2 at the start and written back at the
+// end, and only pi goes through global memory every step.
+constexpr uint32_t kTmemQt = 256;  // accumulator 64 + two chunks of q, rounded to a power of 2
+template <int PESK, bool QT>
 __global__ void __launch_bounds__(kTileThreads, 2) k_tc_step(TcArgs a) {
     extern __shared__ unsigned char dsm[];
     unsigned char *base = align1k(dsm);
@@ -933,7 +951,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_step(TcArgs a) {
         stage_columns(&aux->stg[0], a, r0 * nd, (int)(min((int64_t)rpc, r1 - r0) * nd), true);
         cp_async_commit();
     }
-    const uint32_t tmem = tile_setup(base, sh, a.gT);
+    const uint32_t tmem = tile_setup(base, sh, a.gT, QT ? kTmemQt : (uint32_t)kNc);
     const uint32_t tlane = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
     // kick + rotation + OU + rotation of mode m as one linear map
     const float4 k1 = *reinterpret_cast<const float4 *>(a.fold + (size_t)m * 8);
@@ -942,6 +960,23 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_step(TcArgs a) {
     // step counter are read after the previous launch has completed.
     griddep_wait();
     const int64_t s0 = *a.step0 + a.sofs;
+    if (QT) {  // q of the CTA's chunks into TMEM (zeros beyond the valid columns)
+        int kc = 0;
+        for (int64_t rc = r0; rc < r1; rc += rpc, kc++) {
+            const int64_t col0 = rc * nd;
+            const int nvalid = (int)(min((int64_t)rpc, r1 - rc) * nd);
+#pragma unroll 1
+            for (int g = 0; g < 4; g++) {
+                const int gc = 16 * g + 8 * hh;
+                const float *src = a.q + (size_t)(col0 + gc) * kP + m;
+                float v[kGrp];
+#pragma unroll
+                for (int i = 0; i < kGrp; i++) v[i] = gc + i < nvalid ? src[(size_t)i * kP] : 0.f;
+                __syncwarp();
+                tmem_st8(tlane + (uint32_t)(64 * (kc + 1) + gc), v);
+            }
+        }
+    }
     uint32_t last_phase = 0;  // parity of the last GEMM issued (for the drain on a timeout)
     bool first = true;
     int buf = 0;
@@ -952,6 +987,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_step(TcArgs a) {
     // loop at the chunk-end barrier.
     int sub = 0;
     for (int64_t rc = r0; sub < a.nsub; buf ^= 1) {
+        const uint32_t tq = tlane + (uint32_t)(rc == r0 ? 64 : 128);  // QT: this chunk's q columns
         const int64_t s = s0 + sub;
         const bool est = a.sofs + sub > 0;  // the estimator of step s - 1
         const int64_t col0 = rc * nd;
@@ -969,7 +1005,22 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_step(TcArgs a) {
             cp_async_commit();
             cp_async_wait<1>();  // this chunk's copies (made visible by the barrier in tile_load)
         }
-        tile_load(base, a.q + col0 * kP, nvalid);
+        if (QT) {  // the B operand of GEMM 1 from the q columns in TMEM
+#pragma unroll 1
+            for (int g = 0; g < 4; g++) {
+                const int gc = 16 * g + 8 * hh;
+                float v[kGrp];
+                __syncwarp();
+                tmem_ldn<kGrp>(tq + (uint32_t)gc, v);
+                group_store_operand(Xhi, Xlo, gc, 0, m, v);
+            }
+            fence_async_smem();
+            tc_before();
+            __syncthreads();
+            tc_after();
+        } else {
+            tile_load(base, a.q + col0 * kP, nvalid);
+        }
         tile_issue(base, sh, tmem, first);
         last_phase = 0;
         first = false;
@@ -1005,22 +1056,32 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_step(TcArgs a) {
                     float qv[kGrp], pv[kGrp], gv[kGrp], zg[kGrp];
 #pragma unroll
                     for (int i = 0; i < kGrp; i++) {
-                        qv[i] = i < nvg ? qo[(size_t)i * kP] : 0.f;
+                        if (!QT) qv[i] = i < nvg ? qo[(size_t)i * kP] : 0.f;
                         pv[i] = i < nvg ? po[(size_t)i * kP] : 0.f;
                     }
                     group_normals(sg, gc, 0, m, (uint32_t)s, zg);  // while the loads are in flight
                     __syncwarp();
                     tmem_ldn<kGrp>(tlane + (uint32_t)gc, gv);
+                    if (QT) {
+                        __syncwarp();
+                        tmem_ldn<kGrp>(tq + (uint32_t)gc, qv);
+                    }
+                    float qnv[kGrp];
 #pragma unroll
                     for (int i = 0; i < kGrp; i++) {
                         const float zk = zg[i];
                         const float pn = fmaf(k1.x, pv[i], fmaf(-k1.w, gv[i], fmaf(k1.y, qv[i], k1.z * zk)));
                         const float qn = fmaf(k2.x, pv[i], fmaf(-k2.w, gv[i], fmaf(k2.y, qv[i], k2.z * zk)));
+                        qnv[i] = qn;
                         if (i < nvg) {
-                            qo[(size_t)i * kP] = qn;
+                            if (!QT) qo[(size_t)i * kP] = qn;
                             po[(size_t)i * kP] = pn;
                             if (pn != pn) badbits |= 1u << (8 * g + i);
                         }
+                    }
+                    if (QT) {
+                        __syncwarp();
+                        tmem_st8(tq + (uint32_t)gc, qnv);
                     }
                 }
             }
@@ -1041,7 +1102,25 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_step(TcArgs a) {
         sub = subn;
     }
     if (tid < kNc) cp_async_wait<0>();  // no copy left in flight at exit
-    tile_release(sh, tmem, a.err, last_phase);
+    if (QT) {  // q back to global memory
+        int kc = 0;
+        for (int64_t rc = r0; rc < r1; rc += rpc, kc++) {
+            const int64_t col0 = rc * nd;
+            const int nvalid = (int)(min((int64_t)rpc, r1 - rc) * nd);
+#pragma unroll 1
+            for (int g = 0; g < 4; g++) {
+                const int gc = 16 * g + 8 * hh;
+                float v[kGrp];
+                __syncwarp();
+                tmem_ldn<kGrp>(tlane + (uint32_t)(64 * (kc + 1) + gc), v);
+                float *dst = a.q + (size_t)(col0 + gc) * kP + m;
+#pragma unroll
+                for (int i = 0; i < kGrp; i++)
+                    if (gc + i < nvalid) dst[(size_t)i * kP] = v[i];
+            }
+        }
+    }
+    tile_release(sh, tmem, a.err, last_phase, QT ? kTmemQt : (uint32_t)kNc);
 }
 
 __global__ void k_tc_step_add(int64_t *step, int64_t n) { *step += n; }
@@ -1660,8 +1739,10 @@ int tc_prepare(pg_ctx *ctx, TiState &st) {
     }
     PG_CUDA(cudaStreamSynchronize(ctx->stream));
     size_t sm = tc_smem_bytes();
-    PG_CUDA(cudaFuncSetAttribute(k_tc_step<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    PG_CUDA(cudaFuncSetAttribute(k_tc_step<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    PG_CUDA(cudaFuncSetAttribute(k_tc_step<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    PG_CUDA(cudaFuncSetAttribute(k_tc_step<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    PG_CUDA(cudaFuncSetAttribute(k_tc_step<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    PG_CUDA(cudaFuncSetAttribute(k_tc_step<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     PG_CUDA(cudaFuncSetAttribute(k_tc_final, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     PG_CUDA(cudaFuncSetAttribute(k_tb_pos, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     PG_CUDA(cudaFuncSetAttribute(k_tb_kick, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
@@ -1761,7 +1842,14 @@ static int tc_launch_step(pg_ctx *ctx, TiState &st, int64_t i, int nsub, cudaStr
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    cudaError_t e = pesk == 2 ? cudaLaunchKernelEx(&cfg, k_tc_step<2>, a) : cudaLaunchKernelEx(&cfg, k_tc_step<1>, a);
+    // q resident in tensor memory when no CTA holds more than two chunks
+    const int64_t rpc = kNc / st.nd, maxr = (st.nrings + grid - 1) / grid;
+    const bool qt = (maxr + rpc - 1) / rpc <= 2;
+    cudaError_t e;
+    if (pesk == 2)
+        e = qt ? cudaLaunchKernelEx(&cfg, k_tc_step<2, true>, a) : cudaLaunchKernelEx(&cfg, k_tc_step<2, false>, a);
+    else
+        e = qt ? cudaLaunchKernelEx(&cfg, k_tc_step<1, true>, a) : cudaLaunchKernelEx(&cfg, k_tc_step<1, false>, a);
     if (e == cudaSuccess) e = cudaGetLastError();
     return e == cudaSuccess ? PG_OK : cuda_fail(e, "k_tc_step launch");
 }
