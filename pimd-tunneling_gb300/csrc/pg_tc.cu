@@ -449,6 +449,11 @@ __device__ __forceinline__ void cp_async8(void *dst, const void *src) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// Bulk prefetch of [p, p + bytes) into L2 (a hint: p 16-byte aligned, bytes a
+// multiple of 16).
+__device__ __forceinline__ void prefetch_l2(const void *p, uint32_t bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
 // Programmatic dependent launch: both are no-ops for a launch without the
 // programmatic-serialization attribute.
 __device__ __forceinline__ void griddep_launch_dependents() {
@@ -1278,6 +1283,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tb_pos(TbArgs a) {
     const int nd = a.nd, P = a.P;
     const int64_t col0 = (int64_t)blockIdx.x * kNc;
     const int nvalid = (int)min((int64_t)kNc, a.nrings * nd - col0);
+    if (tid == 0) prefetch_l2(a.q + col0 * P, (uint32_t)((size_t)nvalid * P * sizeof(float)));  // the tile's rows
     if (tid < kNc) {
         float xa = 0.f, xs = 0.f;
         if (tid < nvalid) {
@@ -1336,6 +1342,11 @@ __global__ void __launch_bounds__(kForceThreads) k_tb_force(TbArgs a) {
     const int ldx = force_stride(a.nd);
     float *sx = reinterpret_cast<float *>(fsm + ((size_t)np * sizeof(float) + 15) / 16 * 16) + threadIdx.x * ldx;
     float *sg = sx + kForceThreads * ldx;
+    if (threadIdx.x == 0) {  // the x rows of this block's rings
+        const int64_t t0 = (int64_t)blockIdx.x * kForceThreads;
+        const int64_t ra = t0 / a.P, rb = min((t0 + kForceThreads - 1) / a.P, a.nrings - 1);
+        prefetch_l2(a.x + (size_t)ra * a.nd * a.P, (uint32_t)((size_t)(rb - ra + 1) * a.nd * a.P * sizeof(float)));
+    }
     for (int i = threadIdx.x; i < np; i += kForceThreads) sp[i] = a.pes.fparams[i];
     __syncthreads();
     PesArgs pa = a.pes;
@@ -1374,6 +1385,12 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tb_kick(TbArgs a) {
     const int nd = a.nd, P = a.P;
     const int64_t col0 = (int64_t)blockIdx.x * kNc;
     const int nvalid = (int)min((int64_t)kNc, a.nrings * nd - col0);
+    if (tid == 0) {  // the tile's rows of F, q and pi, on their way into L2 while the GEMMs run
+        const uint32_t tb = (uint32_t)((size_t)nvalid * P * sizeof(float));
+        prefetch_l2(a.f + col0 * P, tb);
+        prefetch_l2(a.q + col0 * P, tb);
+        prefetch_l2(a.pi + col0 * P, tb);
+    }
     const int64_t s = *a.step0 + a.sofs;
     if (tid < kNc) {
         uint64_t sd = 0;
@@ -1518,6 +1535,12 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tb_kick_nm(TbArgs a) {
     const int nd = a.nd, P = a.P;
     const int64_t col0 = (int64_t)blockIdx.x * kNc;
     const int nvalid = (int)min((int64_t)kNc, a.nrings * nd - col0);
+    if (tid == 0) {  // the tile's rows of F, q and pi, on their way into L2 while the GEMMs run
+        const uint32_t tb = (uint32_t)((size_t)nvalid * P * sizeof(float));
+        prefetch_l2(a.f + col0 * P, tb);
+        prefetch_l2(a.q + col0 * P, tb);
+        prefetch_l2(a.pi + col0 * P, tb);
+    }
     if (tid < kNc) {
         const int64_t ring = (col0 + tid) / nd;
         const int j = (int)(col0 + tid - ring * nd);
