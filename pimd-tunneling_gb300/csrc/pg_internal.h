@@ -82,6 +82,15 @@ struct TiState {
     DevBuf x0, p0;           // FP64 staging of caller-given start positions / momenta
     DevBuf kickflag;         // per-ring Andersen kick flag (blocked tensor form)
     DevBuf tccol;            // per-column table of the tcgen05 step kernel (spring line, Philox key, weight)
+    // host-side caches across batches: T of the last P, the mode coefficients,
+    // and what the tensor-core tables on the device were built from
+    std::vector<double> hostT;
+    int hostT_P = 0;
+    std::vector<ModeCoef> hcoef;
+    std::vector<float> tc_tabs;    // FP32 coefficient + folded-map tables last uploaded
+    int tc_img_P = 0;              // P of the split image in Tbf (0: none)
+    const void *tc_img_ptr = nullptr;
+    bool tc_attr = false;          // kernel attributes set
     DevBuf dbdl;             // nlambda*nd
     DevBuf avec, bvec;       // nd start point, nlambda*nd end points
     DevBuf xref;             // nlambda*nd*P

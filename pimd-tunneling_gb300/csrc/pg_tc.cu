@@ -1696,20 +1696,20 @@ int tc_supported(const TiState &st, const pg_ctx &ctx) {
     return 0;
 }
 
+// Tensor-core tables of a batch: the split image of T (rebuilt only when P or
+// the buffer changes), the FP32 coefficient and folded-map tables (uploaded
+// when they differ from the last upload), the error word, and the column table.
 int tc_prepare(pg_ctx *ctx, TiState &st) {
     st.tc_mb = blocks_for(st.P);
-    std::vector<unsigned char> img;
-    build_split_image(st.P, img);
     const int P = st.P;
     size_t ncoef = (size_t)ctx->natom * P * 8;
     size_t bytes = tbf_fold_off(st, ctx->natom) + ncoef * sizeof(float);
     cudaError_t e = st.Tbf.ensure(bytes);
     if (e != cudaSuccess) return cuda_fail(e, "tensor-core tables");
-    std::vector<ModeCoef> mc((size_t)ctx->natom * P);
-    PG_CUDA(cudaMemcpyAsync(mc.data(), st.coef.ptr, mc.size() * sizeof(ModeCoef), cudaMemcpyDeviceToHost,
-                            ctx->stream));
-    PG_CUDA(cudaStreamSynchronize(ctx->stream));
-    std::vector<float> cf(ncoef, 0.f);
+    if (st.hcoef.size() != (size_t)ctx->natom * P) return fail(PG_ERR_STATE, "mode coefficients missing");
+    const std::vector<ModeCoef> &mc = st.hcoef;
+    std::vector<float> tabs(2 * ncoef, 0.f);  // [coefficients | folded map]
+    float *cf = tabs.data(), *fold = tabs.data() + ncoef;
     for (int at = 0; at < ctx->natom; at++)
         for (int k = 0; k < P; k++) {
             const ModeCoef &c = mc[(size_t)at + (size_t)ctx->natom * k];
@@ -1724,7 +1724,6 @@ int tc_prepare(pg_ctx *ctx, TiState &st) {
         }
     // (p, q) <- R O R (p - dt g, q) as one map: R the half rotation [rA rB; rC rD],
     // O the OU step p <- ou_a p + ou_s z, composed in FP64.
-    std::vector<float> fold(ncoef, 0.f);
     for (int at = 0; at < ctx->natom; at++)
         for (int k = 0; k < P; k++) {
             const ModeCoef &c = mc[(size_t)at + (size_t)ctx->natom * k];
@@ -1741,12 +1740,25 @@ int tc_prepare(pg_ctx *ctx, TiState &st) {
             o[7] = (float)(k21 * st.cfg.dt);
         }
     unsigned char *d = st.Tbf.as<unsigned char>();
-    PG_CUDA(cudaMemcpyAsync(d, img.data(), img.size(), cudaMemcpyHostToDevice, ctx->stream));
-    PG_CUDA(cudaMemcpyAsync(d + tbf_coef_off(st), cf.data(), cf.size() * sizeof(float), cudaMemcpyHostToDevice,
-                            ctx->stream));
+    const bool same_buf = st.tc_img_ptr == (const void *)d;
+    if (!same_buf || st.tc_img_P != P) {
+        std::vector<unsigned char> img;
+        build_split_image(P, img);
+        PG_CUDA(cudaMemcpyAsync(d, img.data(), img.size(), cudaMemcpyHostToDevice, ctx->stream));
+        PG_CUDA(cudaStreamSynchronize(ctx->stream));  // img is a local pageable buffer
+        st.tc_img_P = P;
+        st.tc_img_ptr = d;
+        st.tc_tabs.clear();
+    }
+    if (st.tc_tabs != tabs) {
+        PG_CUDA(cudaMemcpyAsync(d + tbf_coef_off(st), cf, ncoef * sizeof(float), cudaMemcpyHostToDevice,
+                                ctx->stream));
+        PG_CUDA(cudaMemcpyAsync(d + tbf_fold_off(st, ctx->natom), fold, ncoef * sizeof(float),
+                                cudaMemcpyHostToDevice, ctx->stream));
+        PG_CUDA(cudaStreamSynchronize(ctx->stream));  // tabs is a local pageable buffer
+        st.tc_tabs.swap(tabs);
+    }
     PG_CUDA(cudaMemsetAsync(d + tbf_err_off(st, ctx->natom), 0, 64, ctx->stream));
-    PG_CUDA(cudaMemcpyAsync(d + tbf_fold_off(st, ctx->natom), fold.data(), fold.size() * sizeof(float),
-                            cudaMemcpyHostToDevice, ctx->stream));
     {
         const int64_t ncols = st.nrings * st.nd;
         e = st.tccol.ensure((size_t)ncols * 32);
@@ -1761,15 +1773,19 @@ int tc_prepare(pg_ctx *ctx, TiState &st) {
         PG_CUDA(cudaGetLastError());
     }
     PG_CUDA(cudaStreamSynchronize(ctx->stream));
-    size_t sm = tc_smem_bytes();
-    PG_CUDA(cudaFuncSetAttribute(k_tc_step<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    PG_CUDA(cudaFuncSetAttribute(k_tc_step<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    PG_CUDA(cudaFuncSetAttribute(k_tc_step<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    PG_CUDA(cudaFuncSetAttribute(k_tc_step<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    PG_CUDA(cudaFuncSetAttribute(k_tc_final, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    PG_CUDA(cudaFuncSetAttribute(k_tb_pos, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    PG_CUDA(cudaFuncSetAttribute(k_tb_kick, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    PG_CUDA(cudaFuncSetAttribute(k_tb_kick_nm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    if (!st.tc_attr) {
+        size_t sm = tc_smem_bytes();
+        PG_CUDA(cudaFuncSetAttribute(k_tc_step<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        PG_CUDA(cudaFuncSetAttribute(k_tc_step<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        PG_CUDA(cudaFuncSetAttribute(k_tc_step<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        PG_CUDA(cudaFuncSetAttribute(k_tc_step<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        PG_CUDA(cudaFuncSetAttribute(k_tc_final, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        PG_CUDA(cudaFuncSetAttribute(k_tb_pos, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        PG_CUDA(cudaFuncSetAttribute(k_tb_kick, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        PG_CUDA(cudaFuncSetAttribute(k_tb_kick_nm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        st.tc_attr = true;
+    }
+    // the force kernel's shared memory depends on the surface and the dof count
     PG_CUDA(cudaFuncSetAttribute(k_tb_force, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)tb_force_smem(st.nd, (int)ctx->fparams.size())));
     return PG_OK;

@@ -884,8 +884,11 @@ extern "C" int pg_ti_setup(pg_ctx *ctx, const pg_ti_config *cfg, int64_t nrings,
     const double betan = st.betan;
 
     // init_nm (verletmodule.f90:306-338): lam, beadmass, beadvec; transmatrix
-    std::vector<double> T;
-    build_transmatrix(P, T);
+    if (st.hostT_P != P) {  // T depends on P only
+        build_transmatrix(P, st.hostT);
+        st.hostT_P = P;
+    }
+    const std::vector<double> &T = st.hostT;
     std::vector<double> lam(P);
     for (int i = 1; i <= P; i++) lam[i - 1] = 2.0 * std::sin((double)i * kPiRef / (double)(2 * P + 2)) / betan;
     std::vector<ModeCoef> coef((size_t)natom * P);
@@ -915,6 +918,7 @@ extern "C" int pg_ti_setup(pg_ctx *ctx, const pg_ti_config *cfg, int64_t nrings,
             c.bm = bm;
             coef[(size_t)k + (size_t)natom * i] = c;
         }
+    st.hcoef = coef;
     // beadvec tables (verletmodule.f90:326-335); the nlambda x nd x P values are
     // formed on the device by k_beadvec
     std::vector<double> bvtab(3 * (size_t)P);
