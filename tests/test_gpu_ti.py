@@ -300,6 +300,28 @@ def test_tensor_tile_two_chunks_per_cta_multi_launch(ctx, pg):
     np.testing.assert_allclose(s1, s3, rtol=2e-4, atol=1e-6 * np.max(np.abs(s3)))
 
 
+def test_tensor_tile_three_chunks_per_cta_state_in_l2(ctx, pg):
+    """20,000 rings at P = 128: three 64-column chunks on most CTAs, so q stays
+    in global memory (the other step-kernel variant); 60 steps as 50 + 10 against
+    30 + 30 bitwise, and against the FP32 SIMT form."""
+    c, ti = _small_2d(P=128, nrep=1000, nint=20)
+    _set_system(ctx, c)
+    x1, p1, s1, n1, st1 = _run(ctx, pg, c, ti, pg.PG_MIXED, pg.PG_FORM_TENSOR, 60)
+    cfg = _gpu_cfg(pg, c, ti, pg.PG_MIXED, pg.PG_FORM_TENSOR)
+    ctx.ti_setup(cfg, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
+    ctx.ti_advance(30)
+    ctx.ti_advance(30)
+    x2, p2 = ctx.ti_state()
+    s2 = ctx.ti_results()[0]
+    np.testing.assert_array_equal(x1, x2)
+    np.testing.assert_array_equal(s1, s2)
+    x3, p3, s3, n3, st3 = _run(ctx, pg, c, ti, pg.PG_MIXED, pg.PG_FORM_FUSED, 60)
+    assert np.all(st1 == 0) and np.all(st3 == 0)
+    np.testing.assert_array_equal(n1, n3)
+    assert np.max(np.abs(x1 - x3)) < 2e-3
+    np.testing.assert_allclose(s1, s3, rtol=2e-4, atol=1e-6 * np.max(np.abs(s3)))
+
+
 @pytest.mark.parametrize("nrep,nint", [(4, 2), (50, 3)])
 def test_tensor_form_tracks_simt_fp32(ctx, pg, nrep, nint):
     """tcgen05 split-BF16 kernel vs the FP32 SIMT kernel over a short run from the
