@@ -240,6 +240,8 @@ __device__ __forceinline__ void issue_gemm(uint32_t tmem, uint32_t dcol, uint32_
 struct TcShared {
     uint64_t mma_bar;
     uint64_t tma_bar;
+    uint64_t mma_bar2;  // blocked GEMM: second MMA-completion barrier (T_lo products)
+    uint64_t tma_bar2;  // blocked GEMM: second copy barrier (T_lo half)
     uint32_t tmem_slot;
     int32_t err;
 };
@@ -1177,6 +1179,8 @@ __device__ __forceinline__ uint32_t tb_begin(TcShared *sh, int mb) {
     if (tid == 0) {
         mbar_init(&sh->mma_bar, 1);
         mbar_init(&sh->tma_bar, 1);
+        mbar_init(&sh->mma_bar2, 1);
+        mbar_init(&sh->tma_bar2, 1);
         sh->err = 0;
         fence_barrier_init();
     }
@@ -1191,9 +1195,15 @@ __device__ __forceinline__ uint32_t tb_begin(TcShared *sh, int mb) {
     return sh->tmem_slot;
 }
 
-// D_i = sum_k T_ik X_k for the tile whose column c is src[c * P ..].  Returns
-// whether every GEMM completed (CTA-uniform); *phase counts the mbarrier phases
-// used (the parity of the last one is (*phase - 1) & 1).
+// D_i = sum_k T_ik X_k for the tile whose column c is src[c * P ..].  Thread 0
+// drives the blocks j = (k, i) in order, each as two halves: T_hi (copy on
+// tma_bar, the 16 T_hi X_hi / T_hi X_lo products committed to mma_bar) and T_lo
+// (tma_bar2, the 8 T_lo X_hi products on mma_bar2).  A half's copy for block j
+// waits only until the same half of block j - 1 has been read, so copies
+// overlap the other half's products, and every mbarrier has at most one phase
+// outstanding when it is waited on.  The CTA synchronises once per K block
+// (before X is reloaded) and once at the end, after thread 0 has seen the last
+// products complete.  Returns whether every wait completed (CTA-uniform).
 __device__ __forceinline__ bool tb_gemm(unsigned char *base, TcShared *sh, const TbArgs &a, const float *src,
                                         int nvalid, uint32_t tmem, uint32_t *phase) {
     unsigned char *Xhi = base + 2 * kOpBytes, *Xlo = Xhi + kXPlane;
@@ -1202,6 +1212,7 @@ __device__ __forceinline__ bool tb_gemm(unsigned char *base, TcShared *sh, const
     const int c = 8 * warp + (lane & 7);  // operand row written by this thread
     const bool v = c < nvalid;
     const float *row = src + (size_t)(v ? c : 0) * P;
+    int j = 0, hi_last = -1, lo_last = -1;  // thread 0: blocks started; last committed halves
     for (int kb = 0; kb < mb; kb++) {
         // X_kb: K = beads 128 kb .. 128 kb + 127 of every column (zero beyond P;
         // P % 4 == 0, so each float4 is wholly inside or outside a row)
@@ -1226,39 +1237,82 @@ __device__ __forceinline__ bool tb_gemm(unsigned char *base, TcShared *sh, const
         }
         fence_async_smem();
         tc_before();
-        __syncthreads();
+        __syncthreads();  // X_kb written
         tc_after();
-        for (int ib = 0; ib < mb; ib++) {
-            const uint32_t par = *phase & 1u;
-            if (tid == 0 && sh->err == 0) {
+        if (tid == 0 && sh->err == 0) {
+            const uint32_t th = smem_u32(base), tl = th + kOpBytes, xh = smem_u32(Xhi), xl = smem_u32(Xlo);
+            for (int ib = 0; ib < mb; ib++, j++) {
                 const unsigned char *blk = a.gT + (size_t)(ib * mb + kb) * 2 * kOpBytes;
-                mbar_expect_tx(&sh->tma_bar, 2 * kOpBytes);
-#pragma unroll
-                for (int i = 0; i < 4; i++) bulk_g2s(base + i * 16384, blk + i * 16384, 16384, &sh->tma_bar);
-                if (!mbar_wait(&sh->tma_bar, par)) {
-                    sh->err |= 1;
-                } else {
-                    const uint32_t th = smem_u32(base), tl = th + kOpBytes, xh = smem_u32(Xhi), xl = smem_u32(Xlo);
-                    const uint32_t d = tmem + (uint32_t)(64 * ib);
-#pragma unroll
-                    for (int ks = 0; ks < kP / 16; ks++) {
-                        const uint64_t dth = make_desc(th + (uint32_t)ks * 2 * kLBO),
-                                       dtl = make_desc(tl + (uint32_t)ks * 2 * kLBO);
-                        const uint64_t dxh = make_desc_x(xh + (uint32_t)ks * 2 * kXLbo),
-                                       dxl = make_desc_x(xl + (uint32_t)ks * 2 * kXLbo);
-                        mma_bf16_n64(d, dth, dxh, (kb > 0 || ks > 0) ? 1u : 0u);
-                        mma_bf16_n64(d, dth, dxl, 1u);
-                        mma_bf16_n64(d, dtl, dxh, 1u);
-                    }
-                    mma_commit(&sh->mma_bar);
+                const uint32_t d = tmem + (uint32_t)(64 * ib);
+                // T_hi half: its buffer is free once the T_hi products of block j - 1 are done
+                if (hi_last >= 0 && !mbar_wait(&sh->mma_bar, (uint32_t)hi_last & 1u)) {
+                    sh->err |= 2;
+                    break;
                 }
+                mbar_expect_tx(&sh->tma_bar, kOpBytes);
+                bulk_g2s(base, blk, 16384, &sh->tma_bar);
+                bulk_g2s(base + 16384, blk + 16384, 16384, &sh->tma_bar);
+                // T_lo half: free once the T_lo products of block j - 1 are done
+                if (lo_last >= 0 && !mbar_wait(&sh->mma_bar2, (uint32_t)lo_last & 1u)) {
+                    sh->err |= 2;
+                    mbar_wait(&sh->tma_bar, (uint32_t)j & 1u);  // let the T_hi copy land (bounded)
+                    break;
+                }
+                mbar_expect_tx(&sh->tma_bar2, kOpBytes);
+                bulk_g2s(base + kOpBytes, blk + kOpBytes, 16384, &sh->tma_bar2);
+                bulk_g2s(base + kOpBytes + 16384, blk + kOpBytes + 16384, 16384, &sh->tma_bar2);
+                if (!mbar_wait(&sh->tma_bar, (uint32_t)j & 1u)) {
+                    sh->err |= 1;
+                    mbar_wait(&sh->tma_bar2, (uint32_t)j & 1u);
+                    break;
+                }
+                tc_after();
+#pragma unroll
+                for (int ks = 0; ks < kP / 16; ks++) {
+                    const uint64_t dth = make_desc(th + (uint32_t)ks * 2 * kLBO);
+                    const uint64_t dxh = make_desc_x(xh + (uint32_t)ks * 2 * kXLbo),
+                                   dxl = make_desc_x(xl + (uint32_t)ks * 2 * kXLbo);
+                    mma_bf16_n64(d, dth, dxh, (kb > 0 || ks > 0) ? 1u : 0u);
+                    mma_bf16_n64(d, dth, dxl, 1u);
+                }
+                mma_commit(&sh->mma_bar);
+                hi_last = j;
+                if (!mbar_wait(&sh->tma_bar2, (uint32_t)j & 1u)) {
+                    sh->err |= 1;
+                    break;
+                }
+                tc_after();
+#pragma unroll
+                for (int ks = 0; ks < kP / 16; ks++) {
+                    const uint64_t dtl = make_desc(tl + (uint32_t)ks * 2 * kLBO);
+                    const uint64_t dxh = make_desc_x(xh + (uint32_t)ks * 2 * kXLbo);
+                    mma_bf16_n64(d, dtl, dxh, 1u);
+                }
+                mma_commit(&sh->mma_bar2);
+                lo_last = j;
             }
-            *phase += 1;
-            // the GEMM has read T and X before either is overwritten
-            if (!tile_wait(sh, par)) return false;
+            // products still reading X_kb: complete before X is reloaded
+            if (kb + 1 < mb && sh->err == 0 && !mbar_wait(&sh->mma_bar2, (uint32_t)lo_last & 1u)) sh->err |= 2;
+        }
+        if (kb + 1 < mb) {
+            tc_before();
+            __syncthreads();
+            tc_after();
+            if (sh->err) break;  // CTA-uniform
         }
     }
-    return true;
+    if (tid == 0) {
+        // the last products (and any still outstanding after an error) complete
+        // before the CTA reads TMEM or releases it; each barrier has at most one
+        // phase outstanding here
+        if (lo_last >= 0 && !mbar_wait(&sh->mma_bar2, (uint32_t)lo_last & 1u)) sh->err |= 2;
+        if (hi_last > lo_last && !mbar_wait(&sh->mma_bar, (uint32_t)hi_last & 1u)) sh->err |= 2;
+        tc_before();
+    }
+    __syncthreads();
+    tc_after();
+    *phase = 0;  // nothing left for tb_release to drain
+    return sh->err == 0;
 }
 
 __device__ __forceinline__ void tb_release(TcShared *sh, uint32_t tmem, int mb, int32_t *gerr, uint32_t phase) {
