@@ -1213,10 +1213,11 @@ __device__ __forceinline__ bool tb_gemm(unsigned char *base, TcShared *sh, const
     const bool v = c < nvalid;
     const float *row = src + (size_t)(v ? c : 0) * P;
     int j = 0, hi_last = -1, lo_last = -1;  // thread 0: blocks started; last committed halves
-    for (int kb = 0; kb < mb; kb++) {
-        // X_kb: K = beads 128 kb .. 128 kb + 127 of every column (zero beyond P;
-        // P % 4 == 0, so each float4 is wholly inside or outside a row)
-        float4 w[8];
+    // X_kb: K = beads 128 kb .. 128 kb + 127 of every column (zero beyond P;
+    // P % 4 == 0, so each float4 is wholly inside or outside a row); the loads
+    // of X_(kb+1) are in flight while the GEMMs of X_kb run
+    float4 w[8];
+    auto fetch = [&](int kb) {
 #pragma unroll
         for (int it = 0; it < 4; it++) {
             const int kg = 128 * kb + 8 * (4 * it + (lane >> 3));
@@ -1224,6 +1225,9 @@ __device__ __forceinline__ bool tb_gemm(unsigned char *base, TcShared *sh, const
             w[2 * it] = (v && kg + 4 <= P) ? __ldg(reinterpret_cast<const float4 *>(row + kg)) : z4;
             w[2 * it + 1] = (v && kg + 8 <= P) ? __ldg(reinterpret_cast<const float4 *>(row + kg + 4)) : z4;
         }
+    };
+    fetch(0);
+    for (int kb = 0; kb < mb; kb++) {
 #pragma unroll
         for (int it = 0; it < 4; it++) {
             const int kl = 8 * (4 * it + (lane >> 3));
@@ -1239,6 +1243,7 @@ __device__ __forceinline__ bool tb_gemm(unsigned char *base, TcShared *sh, const
         tc_before();
         __syncthreads();  // X_kb written
         tc_after();
+        if (kb + 1 < mb) fetch(kb + 1);
         if (tid == 0 && sh->err == 0) {
             const uint32_t th = smem_u32(base), tl = th + kOpBytes, xh = smem_u32(Xhi), xl = smem_u32(Xlo);
             for (int ib = 0; ib < mb; ib++, j++) {
