@@ -1154,7 +1154,6 @@ struct TbArgs {
     int64_t imin;
     const unsigned char *gT;  // mb x mb block image
     const float *coef;        // natom x P x 8: rA rB rC rD ou_a ou_s pscale
-    const float *fold;        // natom x P x 8: the kick / rotation / OU / rotation map (k_tc_step's table)
     const double *mass;
     const double *avec, *bvec, *dbdl;
     const float *Tf;          // P x P FP32 transform (the bead-P row for the Andersen estimator)
@@ -1473,6 +1472,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tb_kick(TbArgs a) {
         const int cb = 32 * (warp >> 2);
         const int nv = nvalid - cb;
         const int e = lane & 3;
+        const float dt = a.dt;
         uint32_t badbits = 0;
         for (int ib = 0; ib < a.mb; ib++) {
             const int m = 128 * ib + 32 * (warp & 3) + lane;  // mode
@@ -1484,15 +1484,16 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tb_kick(TbArgs a) {
                 float *qo = a.q + (size_t)(col0 + cb + c0) * P + m;
                 float *po = a.pi + (size_t)(col0 + cb + c0) * P + m;
                 float qv[kGrp], pv[kGrp];
-                float4 cfa[kGrp], cfb[kGrp];  // the folded map of column i's atom at mode m
+                float4 cfa[kGrp];
+                float2 cfb[kGrp];
 #pragma unroll
                 for (int i = 0; i < kGrp; i++) {  // state and coefficients first, then the normals
                     const bool in = m < P && i < nvg;
                     qv[i] = in ? qo[(size_t)i * P] : 0.f;
                     pv[i] = in ? po[(size_t)i * P] : 0.f;
-                    const float *cf = a.fold + ((size_t)ax->atom[cb + c0 + i] * P + mc) * 8;
+                    const float *cf = a.coef + ((size_t)ax->atom[cb + c0 + i] * P + mc) * 8;
                     cfa[i] = __ldg(reinterpret_cast<const float4 *>(cf));
-                    cfb[i] = __ldg(reinterpret_cast<const float4 *>(cf + 4));
+                    cfb[i] = __ldg(reinterpret_cast<const float2 *>(cf + 4));
                 }
                 float gv[kGrp];
                 __syncwarp();
@@ -1511,10 +1512,16 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tb_kick(TbArgs a) {
                     for (int k = 0; k < 4; k++) {
                         const int i = 4 * g + k;
                         if (m < P && i < nvg) {
-                            const float4 k1 = cfa[i], k2 = cfb[i];
+                            const float4 c4 = cfa[i];
+                            const float2 c2 = cfb[i];
                             const float zk = z[k];
-                            const float pn = fmaf(k1.x, pv[i], fmaf(-k1.w, gv[i], fmaf(k1.y, qv[i], k1.z * zk)));
-                            const float qn = fmaf(k2.x, pv[i], fmaf(-k2.w, gv[i], fmaf(k2.y, qv[i], k2.z * zk)));
+                            const float p0 = pv[i] - dt * gv[i];
+                            const float q0 = qv[i];
+                            float p1 = c4.x * p0 + c4.y * q0;
+                            const float q1 = c4.z * p0 + c4.w * q0;
+                            p1 = c2.x * p1 + c2.y * zk;
+                            const float pn = c4.x * p1 + c4.y * q1;
+                            const float qn = c4.z * p1 + c4.w * q1;
                             qo[(size_t)i * P] = qn;
                             po[(size_t)i * P] = pn;
                             if (pn != pn) badbits |= 1u << (c0 + i);
@@ -1864,7 +1871,6 @@ static void tc_make_args(pg_ctx *ctx, TiState &st, TcArgs &a, int &pesk) {
     unsigned char *d = st.Tbf.as<unsigned char>();
     a.gT = d;
     a.coef = reinterpret_cast<const float *>(d + tbf_coef_off(st));
-    a.fold = reinterpret_cast<const float *>(d + tbf_fold_off(st, ctx->natom));
     a.err = reinterpret_cast<int32_t *>(d + tbf_err_off(st, ctx->natom));
     a.step0 = reinterpret_cast<const int64_t *>(st.red.as<double>() + 3 * st.nlambda);
     a.mass = ctx->d_mass.as<double>();
@@ -1887,6 +1893,7 @@ static void tc_make_args(pg_ctx *ctx, TiState &st, TcArgs &a, int &pesk) {
         a.cjdof = reinterpret_cast<const int32_t *>(cb + 12 * ncols);
         a.cseed = reinterpret_cast<const uint64_t *>(cb + 16 * ncols);
         a.cwest = reinterpret_cast<const double *>(cb + 24 * ncols);
+        a.fold = reinterpret_cast<const float *>(d + tbf_fold_off(st, ctx->natom));
     }
     pesk = ctx->pes_id == PG_PES_2DTEST ? 2 : 1;
     const std::vector<double> &p = ctx->params;
@@ -1972,7 +1979,6 @@ static void tb_make_args(pg_ctx *ctx, TiState &st, TbArgs &a) {
     unsigned char *d = st.Tbf.as<unsigned char>();
     a.gT = d;
     a.coef = reinterpret_cast<const float *>(d + tbf_coef_off(st));
-    a.fold = reinterpret_cast<const float *>(d + tbf_fold_off(st, ctx->natom));
     a.err = reinterpret_cast<int32_t *>(d + tbf_err_off(st, ctx->natom));
     a.step0 = reinterpret_cast<const int64_t *>(st.red.as<double>() + 3 * st.nlambda);
     a.mass = ctx->d_mass.as<double>();
