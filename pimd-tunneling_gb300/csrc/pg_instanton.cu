@@ -110,7 +110,6 @@ __global__ void __launch_bounds__(512) k_inst_lbfgs(InstArgs A, LbfgsArgs L, dou
                                                     double *__restrict__ scratch, double *__restrict__ um_out,
                                                     int64_t *__restrict__ iters, int32_t *__restrict__ status) {
     __shared__ double sred[32];
-    __shared__ double s_f;
     const int k = blockIdx.x;
     const int n = A.nd * A.N, m = L.m;
     double *ws = scratch + (size_t)k * ((size_t)(5 + 2 * m) * n + 2 * m);
@@ -218,7 +217,6 @@ __global__ void __launch_bounds__(512) k_inst_lbfgs(InstArgs A, LbfgsArgs L, dou
     }
     for (int i = threadIdx.x; i < n; i += blockDim.x) xk[i] = x[i];
     if (threadIdx.x == 0) {
-        s_f = f;
         um_out[k] = f;
         iters[k] = it;
         status[k] = st;
@@ -340,6 +338,136 @@ __global__ void k_band_ldl(int64_t n, int kd, const double *__restrict__ band, c
     if (threadIdx.x == 0) {
         logabs[k] = la;
         nneg[k] = nn;
+    }
+}
+
+// One warp per factorisation f (polymer fpoly[f] at the shift fsig[f]): the
+// banded LDL^T of k_band_ldl with warp synchronisation only.  The (kd+1)^2
+// window lives in shared memory (one per warp); the columns entering the window
+// are loaded kLdlAhead steps early into a register ring (lane r holds rows r
+// and r + 32); |det| is carried as a mantissa in [0.5, 1) and a binary exponent
+// (one log at the end); the Sylvester inertia counts the negative pivots.
+// Requires kd + 1 <= 64.  One warp per CTA, so that the factorisations of a
+// round spread over the SMs (their FP64 pipes bound the kernel).
+constexpr int kLdlWarps = 1;
+constexpr int kLdlAhead = 8;
+__global__ void __launch_bounds__(32 * kLdlWarps) k_band_ldl_w(int64_t n, int kd, const double *__restrict__ band,
+                                                               int nfac, const int32_t *__restrict__ fpoly,
+                                                               const double *__restrict__ fsig,
+                                                               double *__restrict__ logabs,
+                                                               int64_t *__restrict__ nneg) {
+    extern __shared__ double smw[];
+    const int ld = kd + 1;
+    const int ntri = kd * (kd + 1) / 2;
+    double *Ls = smw + (size_t)kLdlWarps * ld * ld;  // per warp: the pivot column scaled by 1/d
+    uint16_t *tri = reinterpret_cast<uint16_t *>(Ls + (size_t)kLdlWarps * ld);
+    for (int q = threadIdx.x; q < ntri; q += blockDim.x) {  // (ii, kk), 1 <= kk <= ii <= kd
+        int ii = 1;
+        while ((ii + 1) * ii / 2 <= q) ii++;
+        tri[q] = (uint16_t)((ii << 8) | (q - ii * (ii - 1) / 2 + 1));
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int f = blockIdx.x * kLdlWarps + warp;
+    if (f >= nfac) return;  // whole warps
+    double *W = smw + (size_t)warp * ld * ld;
+    double *L = Ls + (size_t)warp * ld;
+    const double *bk = band + (size_t)fpoly[f] * ld * n;
+    const double sg = fsig[f];
+    auto colv = [&](int64_t c, int r) -> double {  // row r of column c of (A - sigma I), 0 outside
+        if (r >= ld || c >= n || c + r >= n) return 0.0;
+        const double v = bk[r + (size_t)ld * c];
+        return r == 0 ? v - sg : v;
+    };
+    for (int e = lane; e < ld * ld; e += 32) {
+        const int c = e / ld, r = e - c * ld;
+        W[c * ld + r] = colv(c, r);  // column c < ld in slot c
+    }
+    double pre[kLdlAhead][2];
+#pragma unroll
+    for (int u = 0; u < kLdlAhead; u++) {
+        pre[u][0] = colv(ld + u, lane);
+        pre[u][1] = colv(ld + u, lane + 32);
+    }
+    __syncwarp();
+    double mant = 1.0;
+    int64_t ex = 0, nn = 0;
+    int sl = 0;  // window slot of column j
+    for (int64_t j0 = 0; j0 < n; j0 += kLdlAhead) {
+#pragma unroll
+        for (int u = 0; u < kLdlAhead; u++) {
+            const int64_t j = j0 + u;
+            if (j >= n) break;  // warp-uniform
+            double dj = W[sl * ld];
+            if (dj == 0.0) dj = 1e-300;
+            nn += dj < 0.0 ? 1 : 0;
+            {  // mant <- mant |d_j| scaled back into [0.5, 1) through its IEEE exponent field
+                const long long bits = __double_as_longlong(mant * fabs(dj));
+                ex += ((bits >> 52) & 0x7ff) - 1022;
+                mant = __longlong_as_double((bits & ~(0x7ffLL << 52)) | (1022LL << 52));
+            }
+            const double rinv = 1.0 / dj;
+            if (lane < ld) L[lane] = W[sl * ld + lane] * rinv;
+            if (lane + 32 < ld) L[lane + 32] = W[sl * ld + lane + 32] * rinv;
+            __syncwarp();
+            for (int q = lane; q < ntri; q += 32) {  // W(j+kk, j+ii) -= l_ii d l_kk = L[ii] W(j, j+kk)
+                const int tv = tri[q], ii = tv >> 8, kk = tv & 255;
+                if (j + ii >= n) continue;
+                int sk = sl + kk;
+                if (sk >= ld) sk -= ld;
+                W[sk * ld + (ii - kk)] -= L[ii] * W[sl * ld + kk];
+            }
+            __syncwarp();
+            // slot sl takes column j + ld; its ring entry is refilled kLdlAhead columns on
+            if (lane < ld) W[sl * ld + lane] = pre[u][0];
+            if (lane + 32 < ld) W[sl * ld + lane + 32] = pre[u][1];
+            pre[u][0] = colv(j + ld + kLdlAhead, lane);
+            pre[u][1] = colv(j + ld + kLdlAhead, lane + 32);
+            __syncwarp();
+            sl = sl + 1 == ld ? 0 : sl + 1;
+        }
+    }
+    if (lane == 0) {
+        logabs[f] = log(mant) + (double)ex * 0.6931471805599453;
+        nneg[f] = nn;
+    }
+}
+
+// Gershgorin lower bound of every band and its smallest diagonal element, one
+// CTA per polymer.
+__global__ void k_band_bounds(int64_t n, int kd, const double *__restrict__ band, double *__restrict__ glo,
+                              double *__restrict__ dmin) {
+    __shared__ double s_lo[32], s_mn[32];
+    const int ld = kd + 1;
+    const double *bk = band + (size_t)blockIdx.x * ld * n;
+    double lo = 1e300, mn = 1e300;
+    for (int64_t c = threadIdx.x; c < n; c += blockDim.x) {
+        double rad = 0.0;
+        for (int r = 1; r <= kd; r++) {
+            if (c + r < n) rad += fabs(bk[r + (size_t)ld * c]);
+            if (c - r >= 0) rad += fabs(bk[r + (size_t)ld * (c - r)]);
+        }
+        const double dg = bk[(size_t)ld * c];
+        lo = fmin(lo, dg - rad);
+        mn = fmin(mn, dg);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        s_lo[threadIdx.x >> 5] = lo;
+        s_mn[threadIdx.x >> 5] = mn;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) {
+            lo = fmin(lo, s_lo[w]);
+            mn = fmin(mn, s_mn[w]);
+        }
+        glo[blockIdx.x] = lo;
+        dmin[blockIdx.x] = mn;
     }
 }
 
@@ -471,19 +599,52 @@ extern "C" int pg_um_hessian(pg_ctx *ctx, int64_t N, double betan, const double 
     return PG_OK;
 }
 
-// log|det(H - sigma_k I)| and inertia for every polymer at the shifts sigma[nbeta].
-static int band_factor(pg_ctx *ctx, int64_t nbeta, int64_t n, int kd, const double *hsig, double *hlog,
-                       int64_t *hneg, DevBuf &dsig, DevBuf &dlog, DevBuf &dneg) {
-    PG_CUDA(cudaMemcpyAsync(dsig.ptr, hsig, nbeta * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-    int ld = kd + 1;
-    int th = kd * (kd + 1) / 2;
-    th = th < 32 ? 32 : (th > 512 ? 512 : ((th + 31) / 32) * 32);
-    if (kd * (kd + 1) / 2 > 4 * th) return fail(PG_ERR_UNSUPPORTED, "band width too large for the LDL kernel");
-    k_band_ldl<<<(unsigned)nbeta, th, (size_t)ld * ld * sizeof(double), ctx->stream>>>(
-        n, kd, ctx->scratch_d.as<double>(), dsig.as<double>(), dlog.as<double>(), dneg.as<int64_t>());
-    PG_CUDA(cudaGetLastError());
-    PG_CUDA(cudaMemcpyAsync(hlog, dlog.ptr, nbeta * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    PG_CUDA(cudaMemcpyAsync(hneg, dneg.ptr, nbeta * sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+// log|det(H_p - sigma I)| and inertia of factorisations f = (fpoly[f], fsig[f]).
+struct LdlBufs {
+    DevBuf poly, sig, logv, neg;
+};
+static int band_factor(pg_ctx *ctx, int64_t nbeta, int64_t n, int kd, const std::vector<int32_t> &fpoly,
+                       const std::vector<double> &fsig, std::vector<double> &hlog, std::vector<int64_t> &hneg,
+                       LdlBufs &b) {
+    const int nfac = (int)fpoly.size();
+    hlog.assign(nfac, 0.0);
+    hneg.assign(nfac, 0);
+    if (nfac == 0) return PG_OK;
+    PG_CUDA(b.poly.ensure((size_t)nfac * sizeof(int32_t)));
+    PG_CUDA(b.sig.ensure((size_t)nfac * sizeof(double)));
+    PG_CUDA(b.logv.ensure((size_t)nfac * sizeof(double)));
+    PG_CUDA(b.neg.ensure((size_t)nfac * sizeof(int64_t)));
+    PG_CUDA(cudaMemcpyAsync(b.poly.ptr, fpoly.data(), nfac * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+    PG_CUDA(cudaMemcpyAsync(b.sig.ptr, fsig.data(), nfac * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    const int ld = kd + 1;
+    if (ld <= 64) {
+        const size_t sm = (size_t)kLdlWarps * (ld + 1) * ld * sizeof(double) +
+                          (size_t)kd * (kd + 1) / 2 * sizeof(uint16_t);
+        if (sm > 48 * 1024)
+            PG_CUDA(cudaFuncSetAttribute(k_band_ldl_w, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        k_band_ldl_w<<<(unsigned)((nfac + kLdlWarps - 1) / kLdlWarps), 32 * kLdlWarps, sm, ctx->stream>>>(
+            n, kd, ctx->scratch_d.as<double>(), nfac, b.poly.as<int32_t>(), b.sig.as<double>(), b.logv.as<double>(),
+            b.neg.as<int64_t>());
+        PG_CUDA(cudaGetLastError());
+    } else {  // wide bands: one CTA per polymer and shift, per polymer in turn
+        int th = kd * (kd + 1) / 2;
+        th = th < 32 ? 32 : (th > 512 ? 512 : ((th + 31) / 32) * 32);
+        if (kd * (kd + 1) / 2 > 4 * th) return fail(PG_ERR_UNSUPPORTED, "band width too large for the LDL kernel");
+        std::vector<double> sig1(nbeta, 0.0);
+        for (int f = 0; f < nfac; f++) {
+            // the polymer-indexed kernel: polymer fpoly[f] only, at its shift
+            PG_CUDA(cudaMemcpyAsync(b.sig.as<double>() + nfac - 1, &fsig[f], sizeof(double), cudaMemcpyHostToDevice,
+                                    ctx->stream));
+            (void)sig1;
+            k_band_ldl<<<1, th, (size_t)ld * ld * sizeof(double), ctx->stream>>>(
+                n, kd, ctx->scratch_d.as<double>() + (size_t)fpoly[f] * ld * n, b.sig.as<double>() + nfac - 1,
+                b.logv.as<double>() + f, b.neg.as<int64_t>() + f);
+            PG_CUDA(cudaGetLastError());
+            PG_CUDA(cudaStreamSynchronize(ctx->stream));  // the shift slot is reused
+        }
+    }
+    PG_CUDA(cudaMemcpyAsync(hlog.data(), b.logv.ptr, nfac * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    PG_CUDA(cudaMemcpyAsync(hneg.data(), b.neg.ptr, nfac * sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
     PG_CUDA(cudaStreamSynchronize(ctx->stream));
     return PG_OK;
 }
@@ -496,44 +657,34 @@ extern "C" int pg_instanton_logdet(pg_ctx *ctx, int64_t nbeta, int64_t N, const 
     if (nbeta < 1 || N < 2 || !x || !betan || !lndet) return fail(PG_ERR_ARG, "bad logdet arguments");
     const int nd = ctx->nd, kd = nd, ld = nd + 1;
     const int64_t n = N * nd;
-    DevBuf dx, dbn, dsig, dlog, dneg;
+    DevBuf dx, dbn, dglo, ddmin;
+    LdlBufs lb;
     if ((rc = upload(ctx, dx, x, (size_t)nbeta * n))) return rc;
     if ((rc = upload(ctx, dbn, betan, nbeta))) return rc;
-    PG_CUDA(dsig.ensure(nbeta * sizeof(double)));
-    PG_CUDA(dlog.ensure(nbeta * sizeof(double)));
-    PG_CUDA(dneg.ensure(nbeta * sizeof(int64_t)));
+    PG_CUDA(dglo.ensure(nbeta * sizeof(double)));
+    PG_CUDA(ddmin.ensure(nbeta * sizeof(double)));
     rc = build_bands(ctx, nbeta, N, dx.as<double>(), dbn.as<double>(), singlewell, quirks);
     if (rc) return rc;
-    // Gershgorin bounds of every band (host copy of the band is avoided: bounds
-    // from a reduction over rows on the host would need the band; instead use the
-    // diagonal extremes and the row sums read back once).
-    std::vector<double> band((size_t)nbeta * ld * n);
-    PG_CUDA(cudaMemcpyAsync(band.data(), ctx->scratch_d.ptr, band.size() * sizeof(double), cudaMemcpyDeviceToHost,
-                            ctx->stream));
-    PG_CUDA(cudaStreamSynchronize(ctx->stream));
+    // Gershgorin lower bound and smallest diagonal element of every band
     std::vector<double> glo(nbeta), dmin(nbeta);
-    for (int64_t k = 0; k < nbeta; k++) {
-        const double *bk = band.data() + (size_t)k * ld * n;
-        std::vector<double> rad(n, 0.0);
-        double mn = 1e300;
-        for (int64_t c = 0; c < n; c++) {
-            mn = std::fmin(mn, bk[ld * c]);
-            for (int r = 1; r < ld && c + r < n; r++) {
-                double v = std::fabs(bk[r + ld * c]);
-                rad[c] += v;
-                rad[c + r] += v;
-            }
-        }
-        double lo = 1e300;
-        for (int64_t c = 0; c < n; c++) lo = std::fmin(lo, bk[ld * c] - rad[c]);
-        glo[k] = lo;
-        dmin[k] = mn;
-    }
-    std::vector<double> sig(nbeta, 0.0), la0(nbeta), lac(nbeta);
-    std::vector<int64_t> nn0(nbeta), nnc(nbeta);
-    rc = band_factor(ctx, nbeta, n, kd, sig.data(), la0.data(), nn0.data(), dsig, dlog, dneg);
+    k_band_bounds<<<(unsigned)nbeta, 256, 0, ctx->stream>>>(n, kd, ctx->scratch_d.as<double>(), dglo.as<double>(),
+                                                              ddmin.as<double>());
+    PG_CUDA(cudaGetLastError());
+    PG_CUDA(cudaMemcpyAsync(glo.data(), dglo.ptr, nbeta * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    PG_CUDA(cudaMemcpyAsync(dmin.data(), ddmin.ptr, nbeta * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    PG_CUDA(cudaStreamSynchronize(ctx->stream));
+    std::vector<int32_t> fpoly(nbeta);
+    std::vector<double> fsig(nbeta, 0.0), la0, lac;
+    std::vector<int64_t> nn0, nnc;
+    for (int64_t k = 0; k < nbeta; k++) fpoly[k] = (int32_t)k;
+    rc = band_factor(ctx, nbeta, n, kd, fpoly, fsig, la0, nn0, lb);  // sigma = 0: log|det| and inertia
     if (rc) return rc;
-    // eigenvalues below zero (and the lowest one) by bisection on the inertia count
+    // eigenvalues below zero (and the lowest one) by multisection on the inertia
+    // count: S shifts per polymer and round split its interval into S + 1 parts.
+    // A factorisation is a chain of n dependent pivots (its time hardly depends
+    // on how many run at once), so a round uses about ten warps per SM.
+    const int S = ld <= 64 ? (int)std::max<int64_t>(3, std::min<int64_t>(63, 10 * (int64_t)std::max(ctx->sm_count, 1) / nbeta))
+                           : 1;
     const int kMaxNeg = 8;
     std::vector<std::vector<double>> negs(nbeta);
     std::vector<double> lmin(nbeta, 0.0);
@@ -559,22 +710,29 @@ extern "C" int pg_instanton_logdet(pg_ctx *ctx, int64_t nbeta, int64_t N, const 
         }
         if (!any) break;
         for (int itb = 0; itb < 200; itb++) {
-            bool done = true;
-            for (int64_t k = 0; k < nbeta; k++) {
-                sig[k] = act[k] ? 0.5 * (lo[k] + hi[k]) : 0.0;
-                if (act[k] && (hi[k] - lo[k]) > 1e-13 * std::fmax(std::fabs(lo[k]), std::fabs(hi[k])) &&
-                    (hi[k] - lo[k]) > 1e-300)
-                    done = false;
-            }
-            if (done) break;
-            rc = band_factor(ctx, nbeta, n, kd, sig.data(), lac.data(), nnc.data(), dsig, dlog, dneg);
-            if (rc) return rc;
+            fpoly.clear();
+            fsig.clear();
             for (int64_t k = 0; k < nbeta; k++) {
                 if (!act[k]) continue;
-                if (nnc[k] >= idx)
-                    hi[k] = sig[k];
-                else
-                    lo[k] = sig[k];
+                if (!((hi[k] - lo[k]) > 1e-13 * std::fmax(std::fabs(lo[k]), std::fabs(hi[k])) &&
+                      (hi[k] - lo[k]) > 1e-300))
+                    continue;  // converged
+                for (int t = 0; t < S; t++) {
+                    fpoly.push_back((int32_t)k);
+                    fsig.push_back(lo[k] + (hi[k] - lo[k]) * (double)(t + 1) / (double)(S + 1));
+                }
+            }
+            if (fpoly.empty()) break;
+            rc = band_factor(ctx, nbeta, n, kd, fpoly, fsig, lac, nnc, lb);
+            if (rc) return rc;
+            for (size_t f0 = 0; f0 < fpoly.size(); f0 += S) {  // the S shifts of one polymer, ascending
+                const int64_t k = fpoly[f0];
+                int t = 0;
+                while (t < S && nnc[f0 + t] < idx) t++;  // first shift with >= idx eigenvalues below
+                const double nlo = t > 0 ? fsig[f0 + t - 1] : lo[k];
+                const double nhi = t < S ? fsig[f0 + t] : hi[k];
+                lo[k] = nlo;
+                hi[k] = nhi;
             }
         }
         for (int64_t k = 0; k < nbeta; k++) {
