@@ -152,7 +152,7 @@ def part_c3(out, factr=1e2, pgtol=1e-8):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--out", default=os.path.join(ROOT, "gpurun_out", "validation.json"))
+    ap.add_argument("--out", default="validation.json")
     ap.add_argument("--parts", default="c0,c1,c2,c3")
     args = ap.parse_args()
     B.build()
