@@ -184,6 +184,22 @@ int pg_ti_get_step(pg_ctx *ctx, int64_t *step);
 /* Execution form chosen for the batch (PG_FORM_PLAIN / _FUSED / _TENSOR) and the
  * number of kernel launches one pg_ti_advance(nsteps) issues. */
 int pg_ti_get_form(pg_ctx *ctx, int64_t nsteps, int32_t *form, int64_t *launches);
+
+/* Autotuning of batches set up with form PG_FORM_AUTO (a project addition; the
+ * reference has no launch parameters).  mode PG_TUNE_CACHE: pg_ti_setup takes the
+ * form and the SIMT threads per ring recorded for the batch's key (device, P,
+ * dofs, surface, precision, thermostat, batch-size bucket) in the JSON-lines file
+ * cache_path, else its built-in choice; PG_TUNE_ON: a key not in the file is
+ * tuned on the batch (each candidate set up and advanced for a short timed
+ * probe), the fastest is appended to the file, and the batch is set up again
+ * with it.  PG_TUNE_OFF (the default) disables both. */
+#define PG_TUNE_OFF 0
+#define PG_TUNE_CACHE 1
+#define PG_TUNE_ON 2
+int pg_set_tuning(pg_ctx *ctx, const char *cache_path, int32_t mode);
+/* Launch parameters of the current batch: form, SIMT threads per ring and MD
+ * steps per tensor-step launch (0: built-in choice).  Any pointer may be NULL. */
+int pg_ti_get_tuning(pg_ctx *ctx, int32_t *form, int32_t *simt_threads, int32_t *tc_steps);
 /* Bitwise checkpoint of the whole batch state (positions, momenta, estimator
  * accumulators, RNG step counters); replaces write_restart / restart=2
  * (verletmodule.f90:162-185, pimd_par.f90:331-370). */

@@ -91,6 +91,9 @@ struct TiState {
     int tc_img_P = 0;              // P of the split image in Tbf (0: none)
     const void *tc_img_ptr = nullptr;
     bool tc_attr = false;          // kernel attributes set
+    // launch parameters chosen by the autotuner (0: the built-in choice)
+    int simt_threads = 0;          // threads per ring CTA of the fused SIMT kernel (32, 64 or 128)
+    int tc_steps = 0;              // MD steps per k_tc_step launch
     DevBuf dbdl;             // nlambda*nd
     DevBuf avec, bvec;       // nd start point, nlambda*nd end points
     DevBuf xref;             // nlambda*nd*P
@@ -117,6 +120,9 @@ struct pg_ctx {
     pg::DevBuf d_params, d_fparams, d_mass;
     pg::DevBuf scratch_a, scratch_b, scratch_c, scratch_d;
     pg::TiState *ti = nullptr;
+    // autotuning of AUTO batches (pg_set_tuning): JSON-lines cache file and mode
+    std::string tune_path;
+    int tune_mode = 0;
     pg::PesArgs pes_args() const {
         pg::PesArgs pa;
         pa.id = pes_id;
@@ -142,5 +148,5 @@ int tc_launch(pg_ctx *ctx, TiState &st, int64_t step0, int64_t nsteps, cudaStrea
 int tc_nm_transform(pg_ctx *ctx, int64_t P, int64_t ncol, const double *in, double *out);
 int32_t tc_error(pg_ctx *ctx, TiState &st);
 int tc_kernel_times(pg_ctx *ctx, TiState &st, int64_t nsteps, double *ms, int64_t *count, int *nsub);
-int tc_steps_per_launch();  // MD steps per k_tc_step launch
+int tc_steps_per_launch(const TiState &st);  // MD steps per k_tc_step launch
 }  // namespace pg

@@ -2075,13 +2075,14 @@ static int tb_launch(pg_ctx *ctx, TiState &st, int64_t nsteps, cudaStream_t s) {
 // MD steps per k_tc_step launch (the per-launch set-up, mainly the 64 KB copy
 // of T into every CTA, is paid once per launch).
 constexpr int kStepsPerLaunch = 50;
-int tc_steps_per_launch() { return kStepsPerLaunch; }
+int tc_steps_per_launch(const TiState &st) { return st.tc_steps > 0 ? st.tc_steps : kStepsPerLaunch; }
 
 int tc_launch(pg_ctx *ctx, TiState &st, int64_t, int64_t nsteps, cudaStream_t s) {
     if (nsteps < 0) return PG_OK;  // the HBM copy of the state is current after every advance
     if (st.tc_blocked) return tb_launch(ctx, st, nsteps, s);
-    for (int64_t i = 0; i < nsteps; i += kStepsPerLaunch) {
-        int rc = tc_launch_step(ctx, st, i, (int)std::min<int64_t>(kStepsPerLaunch, nsteps - i), s);
+    const int per = tc_steps_per_launch(st);
+    for (int64_t i = 0; i < nsteps; i += per) {
+        int rc = tc_launch_step(ctx, st, i, (int)std::min<int64_t>(per, nsteps - i), s);
         if (rc) return rc;
     }
     return tc_launch_final(ctx, st, nsteps, s);
@@ -2153,7 +2154,7 @@ int tc_kernel_times(pg_ctx *ctx, TiState &st, int64_t nsteps, double *ms, int64_
         return tb_kernel_times(ctx, st, nsteps, ms, count);
     }
     cudaStream_t s = ctx->stream;
-    const int per = (int)std::min<int64_t>(kStepsPerLaunch, nsteps);
+    const int per = (int)std::min<int64_t>(tc_steps_per_launch(st), nsteps);
     const int64_t nl = (nsteps + per - 1) / per;
     std::vector<cudaEvent_t> ev(nl + 2);
     for (auto &e : ev) PG_CUDA(cudaEventCreate(&e));

@@ -729,7 +729,7 @@ static int threads_for(int P, int nd) {
 static int launch_steps(pg_ctx *ctx, TiState &st, int64_t nsteps, cudaStream_t s) {
     TiArgs a = make_args(ctx, st, step_ptr(st));
     const int P = st.P, nd = st.nd;
-    int th = threads_for(P, nd);
+    int th = st.simt_threads > 0 ? st.simt_threads : threads_for(P, nd);
     unsigned grid = (unsigned)st.nrings;
     if (st.form == PG_FORM_TENSOR) return tc_launch(ctx, st, 0, nsteps, s);
     if (st.form == PG_FORM_FUSED) {
@@ -795,7 +795,7 @@ static std::string graph_signature(const pg_ctx *ctx, const TiState &st) {
     add(&st.nlambda, sizeof(st.nlambda));
     int ints[6] = {st.P, st.nd, st.form, st.tc_blocked, st.fp32 ? 1 : 0, ctx->sm_count};
     add(ints, sizeof(ints));
-    int sys[4] = {ctx->pes_id, ctx->ndim, ctx->natom, ctx->nd};
+    int sys[6] = {ctx->pes_id, ctx->ndim, ctx->natom, ctx->nd, st.simt_threads, st.tc_steps};
     add(sys, sizeof(sys));
     add(&ctx->V0, sizeof(double));
     add(ctx->params.data(), ctx->params.size() * sizeof(double));
@@ -839,11 +839,10 @@ static int resolve_form(pg_ctx *ctx, TiState &st) {
 
 using namespace pg;
 
-extern "C" int pg_ti_setup(pg_ctx *ctx, const pg_ti_config *cfg, int64_t nrings, int64_t nlambda,
-                           const int32_t *ring_lambda, const uint64_t *ring_seed,
-                           const uint32_t *ring_stream, const double *a, const double *b,
-                           const double *dbdl, const double *xref, const double *x0,
-                           const double *p0) {
+static int ti_setup_impl(pg_ctx *ctx, const pg_ti_config *cfg, int64_t nrings, int64_t nlambda,
+                         const int32_t *ring_lambda, const uint64_t *ring_seed, const uint32_t *ring_stream,
+                         const double *a, const double *b, const double *dbdl, const double *xref, const double *x0,
+                         const double *p0, int simt_threads, int tc_steps) {
     int rc = check_ctx(ctx, true);
     if (rc) return rc;
     if (!cfg) return fail(PG_ERR_ARG, "cfg is NULL");
@@ -875,6 +874,8 @@ extern "C" int pg_ti_setup(pg_ctx *ctx, const pg_ti_config *cfg, int64_t nrings,
     st.nd = ctx->nd;
     st.betan = cfg->beta / (double)(cfg->nbeads + 1);  // pimd_par.f90:94
     st.step = 0;
+    st.simt_threads = simt_threads;
+    st.tc_steps = tc_steps;
     rc = resolve_form(ctx, st);
     if (rc) {
         ti_release(ctx);
@@ -1038,6 +1039,136 @@ extern "C" int pg_ti_setup(pg_ctx *ctx, const pg_ti_config *cfg, int64_t nrings,
 }
 
 static int ti_advance_impl(pg_ctx *ctx, int64_t nsteps, double *device_ms);
+
+// ---------------------------------------------------------------- autotuning of AUTO batches
+// pg_set_tuning(path, mode): with mode PG_TUNE_CACHE a setup with form AUTO takes
+// the form and SIMT block size recorded in the JSON-lines file `path` for its
+// key; with PG_TUNE_ON a key that is not there is tuned on the batch itself:
+// every candidate (tensor form where it applies, fused SIMT form with 32, 64 or
+// 128 threads per ring) is set up and advanced for a short timed probe, the
+// fastest is appended to the file, and the batch is set up again with it (so
+// its initial state is that of a plain setup with the chosen parameters).
+struct TuneChoice {
+    int form = PG_FORM_AUTO, simt_threads = 0, tc_steps = 0;
+    double ms_per_step = 0.0;
+};
+
+static std::string tune_key(pg_ctx *ctx, const pg_ti_config *cfg, int64_t nrings) {
+    cudaDeviceProp prop;
+    std::string dev = cudaGetDeviceProperties(&prop, ctx->device) == cudaSuccess ? prop.name : "unknown";
+    for (char &ch : dev)
+        if (ch == '"' || ch == '\\') ch = '_';
+    int64_t nb = 1;
+    while (nb < nrings) nb <<= 1;  // batch size bucket
+    char buf[512];
+    snprintf(buf, sizeof(buf), "%s|sm%d|P%lld|nd%d|natom%d|pes%d|prec%d|th%d|cay%d|lim%d|rings%lld", dev.c_str(),
+             ctx->sm_count, (long long)cfg->nbeads, ctx->nd, ctx->natom, ctx->pes_id, (int)cfg->precision,
+             (int)cfg->thermostat, (int)cfg->cayley, cfg->dhdr_limit >= 0.0 ? 1 : 0, (long long)nb);
+    return buf;
+}
+
+static bool tune_int(const char *line, const char *name, int &v) {
+    const char *q = strstr(line, name);
+    return q && sscanf(q + strlen(name), " : %d", &v) == 1;
+}
+
+static bool tune_lookup(const std::string &path, const std::string &key, TuneChoice &c) {
+    FILE *fp = fopen(path.c_str(), "r");
+    if (!fp) return false;
+    const std::string kq = "\"key\": \"" + key + "\"";
+    char line[2048];
+    bool found = false;
+    while (fgets(line, sizeof(line), fp))  // the last record of a key wins
+        if (strstr(line, kq.c_str())) {
+            TuneChoice t;
+            if (tune_int(line, "\"form\"", t.form) && tune_int(line, "\"simt_threads\"", t.simt_threads) &&
+                tune_int(line, "\"tc_steps\"", t.tc_steps)) {
+                c = t;
+                found = true;
+            }
+        }
+    fclose(fp);
+    return found;
+}
+
+static void tune_record(const std::string &path, const std::string &key, const TuneChoice &c) {
+    FILE *fp = fopen(path.c_str(), "a");
+    if (!fp) return;  // a cache that cannot be written is not an error
+    fprintf(fp, "{\"key\": \"%s\", \"form\": %d, \"simt_threads\": %d, \"tc_steps\": %d, \"ms_per_step\": %.6g}\n",
+            key.c_str(), c.form, c.simt_threads, c.tc_steps, c.ms_per_step);
+    fclose(fp);
+}
+
+extern "C" int pg_set_tuning(pg_ctx *ctx, const char *cache_path, int32_t mode) {
+    int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    if (mode < PG_TUNE_OFF || mode > PG_TUNE_ON) return fail(PG_ERR_ARG, "bad tuning mode");
+    if (mode != PG_TUNE_OFF && (!cache_path || !*cache_path)) return fail(PG_ERR_ARG, "tuning needs a cache path");
+    ctx->tune_mode = mode;
+    ctx->tune_path = mode != PG_TUNE_OFF ? cache_path : "";
+    return PG_OK;
+}
+
+extern "C" int pg_ti_get_tuning(pg_ctx *ctx, int32_t *form, int32_t *simt_threads, int32_t *tc_steps) {
+    int rc = check_ctx(ctx, true);
+    if (rc) return rc;
+    if (!ctx->ti) return fail(PG_ERR_STATE, "pg_ti_setup has not been called");
+    if (form) *form = ctx->ti->form;
+    if (simt_threads) *simt_threads = ctx->ti->simt_threads;
+    if (tc_steps) *tc_steps = ctx->ti->tc_steps;
+    return PG_OK;
+}
+
+extern "C" int pg_ti_setup(pg_ctx *ctx, const pg_ti_config *cfg, int64_t nrings, int64_t nlambda,
+                           const int32_t *ring_lambda, const uint64_t *ring_seed,
+                           const uint32_t *ring_stream, const double *a, const double *b,
+                           const double *dbdl, const double *xref, const double *x0,
+                           const double *p0) {
+    auto setup = [&](const pg_ti_config *c, int th, int steps) {
+        return ti_setup_impl(ctx, c, nrings, nlambda, ring_lambda, ring_seed, ring_stream, a, b, dbdl, xref, x0,
+                             p0, th, steps);
+    };
+    if (!ctx || !cfg || cfg->form != PG_FORM_AUTO || ctx->tune_mode == PG_TUNE_OFF || !ctx->have_system ||
+        nrings < 1)
+        return setup(cfg, 0, 0);
+    const std::string key = tune_key(ctx, cfg, nrings);
+    TuneChoice c;
+    pg_ti_config cc = *cfg;
+    if (tune_lookup(ctx->tune_path, key, c)) {
+        cc.form = c.form;
+        if (setup(&cc, c.simt_threads, c.tc_steps) == PG_OK) return PG_OK;
+        return setup(cfg, 0, 0);  // a record that no longer applies
+    }
+    if (ctx->tune_mode != PG_TUNE_ON) return setup(cfg, 0, 0);
+    std::vector<TuneChoice> cand;
+    {
+        TuneChoice t;
+        t.form = PG_FORM_TENSOR;
+        cand.push_back(t);
+        for (int th : {32, 64, 128}) {
+            t.form = PG_FORM_FUSED;
+            t.simt_threads = th;
+            cand.push_back(t);
+        }
+    }
+    int best = -1;
+    for (size_t i = 0; i < cand.size(); i++) {
+        cc.form = cand[i].form;
+        if (setup(&cc, cand[i].simt_threads, cand[i].tc_steps) != PG_OK) continue;  // does not apply
+        // probe: a two-step estimate, then about 20 ms (4 .. 200 steps) after a warm-up advance
+        double ms = 0.0;
+        if (ti_advance_impl(ctx, 2, &ms) != PG_OK) continue;
+        const int64_t k = std::max<int64_t>(4, std::min<int64_t>(200, (int64_t)(20.0 / std::max(ms / 2.0, 1e-4))));
+        if (ti_advance_impl(ctx, k, nullptr) != PG_OK || ti_advance_impl(ctx, k, &ms) != PG_OK) continue;
+        cand[i].ms_per_step = ms / (double)k;
+        if (best < 0 || cand[i].ms_per_step < cand[best].ms_per_step) best = (int)i;
+    }
+    if (best < 0) return setup(cfg, 0, 0);  // report the plain setup's outcome
+    tune_record(ctx->tune_path, key, cand[best]);
+    cc.form = cand[best].form;
+    return setup(&cc, cand[best].simt_threads, cand[best].tc_steps);
+}
+
 static int ti_advance_group(pg_ctx *const *ctxs, int64_t nctx, int64_t nsteps, double *device_ms);
 
 extern "C" int pg_ti_advance(pg_ctx *ctx, int64_t nsteps) { return ti_advance_impl(ctx, nsteps, nullptr); }
@@ -1286,7 +1417,7 @@ extern "C" int pg_ti_get_form(pg_ctx *ctx, int64_t nsteps, int32_t *form, int64_
         else if (st.form == PG_FORM_TENSOR && st.tc_blocked)
             *launches = nsteps > 0 ? 3 * nsteps + 3 : 0;  // pos, force, kick per step; pos, estimator, counter
         else if (st.form == PG_FORM_TENSOR)  // step kernels of up to tc_steps_per_launch() steps; final pass, counter
-            *launches = nsteps > 0 ? (nsteps + tc_steps_per_launch() - 1) / tc_steps_per_launch() + 2 : 0;
+            *launches = nsteps > 0 ? (nsteps + tc_steps_per_launch(st) - 1) / tc_steps_per_launch(st) + 2 : 0;
         else if (st.form == PG_FORM_FUSED)
             *launches = nsteps > 0 ? 2 : 0;  // fused kernel + step counter
         else

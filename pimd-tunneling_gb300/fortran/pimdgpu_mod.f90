@@ -17,6 +17,7 @@ module pimdgpu
   integer(c_int32_t), parameter :: PG_FORM_AUTO = 0, PG_FORM_PLAIN = 1, PG_FORM_FUSED = 2, &
        PG_FORM_TENSOR = 3
   integer(c_int32_t), parameter :: PG_ANDERSEN = 1, PG_LANGEVIN = 2
+  integer(c_int32_t), parameter :: PG_TUNE_OFF = 0, PG_TUNE_CACHE = 1, PG_TUNE_ON = 2
 
   type, bind(c) :: pg_ti_config
      integer(c_int64_t) :: nbeads
@@ -164,6 +165,19 @@ module pimdgpu
        type(c_ptr), value :: ctx
        character(kind=c_char), intent(in) :: path(*)
      end function pg_ti_checkpoint_load
+
+     integer(c_int) function pg_set_tuning(ctx, cache_path, mode) bind(c, name="pg_set_tuning")
+       import :: c_int, c_ptr, c_char, c_int32_t
+       type(c_ptr), value :: ctx
+       character(kind=c_char), intent(in) :: cache_path(*)   ! NUL-terminated
+       integer(c_int32_t), value :: mode
+     end function pg_set_tuning
+
+     integer(c_int) function pg_ti_get_tuning(ctx, form, simt_threads, tc_steps) bind(c, name="pg_ti_get_tuning")
+       import :: c_int, c_ptr, c_int32_t
+       type(c_ptr), value :: ctx
+       integer(c_int32_t), intent(out) :: form, simt_threads, tc_steps
+     end function pg_ti_get_tuning
 
      integer(c_int) function pg_gauleg(x1, x2, x, w, n) bind(c, name="pg_gauleg")
        import :: c_int, c_int64_t, c_double

@@ -18,13 +18,14 @@ PG_OK, PG_ERR_ARG, PG_ERR_CUDA, PG_ERR_STATE, PG_ERR_UNSUPPORTED, PG_ERR_IO, PG_
 PG_PES_1D, PG_PES_2DTEST, PG_PES_SYNTH9, PG_PES_SYNTH18, PG_PES_HARMONIC, PG_PES_DISTGAUSS = 1, 2, 3, 4, 5, 6
 PG_FP64, PG_MIXED = 0, 1
 PG_FORM_AUTO, PG_FORM_PLAIN, PG_FORM_FUSED, PG_FORM_TENSOR = 0, 1, 2, 3
+PG_TUNE_OFF, PG_TUNE_CACHE, PG_TUNE_ON = 0, 1, 2
 PG_ANDERSEN, PG_LANGEVIN = 1, 2
 
 # Every symbol include/pimdgpu.h declares.
 EXPORTS = [
     "pg_create", "pg_destroy", "pg_last_error", "pg_version", "pg_set_system", "pg_pes_eval",
     "pg_pes_hessian", "pg_nm_transform", "pg_ti_setup", "pg_ti_advance", "pg_ti_get_state",
-    "pg_ti_get_results", "pg_ti_lambda_reduce", "pg_ti_get_step", "pg_ti_advance_timed", "pg_ti_get_form", "pg_ti_kernel_times", "pg_ti_checkpoint_save",
+    "pg_ti_get_results", "pg_ti_lambda_reduce", "pg_ti_get_step", "pg_ti_advance_timed", "pg_ti_get_form", "pg_ti_kernel_times", "pg_set_tuning", "pg_ti_get_tuning", "pg_ti_checkpoint_save",
     "pg_ti_checkpoint_load", "pg_ti_release", "pg_propagate_pimd", "pg_gauleg", "pg_spline",
     "pg_splint", "pg_ti_assemble", "pg_splitting_from_ratio", "pg_instanton_fg",
     "pg_instanton_optimize", "pg_um_hessian", "pg_instanton_logdet", "pg_rpi_assemble",
@@ -81,6 +82,8 @@ def lib():
         L.pg_ti_lambda_reduce.argtypes = [P, P, P, P]
         L.pg_ti_get_step.argtypes = [P, P]
         L.pg_ti_get_form.argtypes = [P, I64, P, P]
+        L.pg_set_tuning.argtypes = [P, C.c_char_p, I32]
+        L.pg_ti_get_tuning.argtypes = [P, P, P, P]
         L.pg_ti_kernel_times.argtypes = [P, I64, P, P, P, P, P]
         L.pg_ti_checkpoint_save.argtypes = [P, C.c_char_p]
         L.pg_ti_checkpoint_load.argtypes = [P, C.c_char_p]
@@ -284,6 +287,17 @@ class Context:
         n = np.zeros(1, dtype=np.int64)
         check(lib().pg_ti_get_form(self.h, nsteps, _p(f), _p(n)))
         return int(f[0]), int(n[0])
+
+    def set_tuning(self, cache_path, mode):
+        """Autotuning of AUTO batches: mode PG_TUNE_OFF / PG_TUNE_CACHE / PG_TUNE_ON,
+        records in the JSON-lines file cache_path."""
+        check(lib().pg_set_tuning(self.h, None if cache_path is None else str(cache_path).encode(), int(mode)))
+
+    def ti_tuning(self):
+        """(form, SIMT threads per ring, MD steps per tensor-step launch) of the batch; 0 = built-in."""
+        v = np.zeros(3, dtype=np.int32)
+        check(lib().pg_ti_get_tuning(self.h, _p(v[0:1]), _p(v[1:2]), _p(v[2:3])))
+        return int(v[0]), int(v[1]), int(v[2])
 
     def ti_kernel_times(self, nsteps):
         """[(name, mean ms per launch, launches, algorithmic bytes per launch)] over nsteps steps."""

@@ -536,3 +536,45 @@ def test_tensor_blocked_andersen_tracks_simt(ctx, pg, cfgname, P, nrep):
     assert np.max(np.abs(x1 - x2)) < 2e-3
     assert np.max(np.abs(p1 - p2)) < 2e-3 * np.max(np.abs(p1))
     np.testing.assert_allclose(s2, s1, rtol=2e-4)
+
+
+def test_autotune_records_and_reuses_its_choice(ctx, pg, tmp_path):
+    """PG_TUNE_ON tunes an AUTO batch once (one record in the JSON-lines cache),
+    PG_TUNE_CACHE takes the record without tuning again, and both give the same
+    trajectory (the tuned setup ends with a fresh setup); a cache miss in
+    PG_TUNE_CACHE mode keeps the built-in choice and writes nothing."""
+    c, ti = _small_2d(P=128, nrep=20, nint=4)
+    _set_system(ctx, c)
+    path = tmp_path / "tune.jsonl"
+    cfg = _gpu_cfg(pg, c, ti, pg.PG_MIXED, pg.PG_FORM_AUTO)
+    args = (ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
+    try:
+        ctx.set_tuning(path, pg.PG_TUNE_CACHE)  # miss: built-in choice, nothing written
+        ctx.ti_setup(cfg, *args)
+        assert ctx.ti_tuning()[1:] == (0, 0)
+        assert not path.exists()
+        ctx.set_tuning(path, pg.PG_TUNE_ON)
+        ctx.ti_setup(cfg, *args)
+        choice = ctx.ti_tuning()
+        lines = path.read_text().splitlines()
+        assert len(lines) == 1 and '"form": %d' % choice[0] in lines[0]
+        assert choice[0] in (pg.PG_FORM_FUSED, pg.PG_FORM_TENSOR)
+        ctx.ti_advance(30)
+        x1 = ctx.ti_state()[0]
+        s1 = ctx.ti_results()[0]
+        ctx.set_tuning(path, pg.PG_TUNE_CACHE)
+        ctx.ti_setup(cfg, *args)
+        assert ctx.ti_tuning() == choice
+        ctx.ti_advance(30)
+        np.testing.assert_array_equal(ctx.ti_state()[0], x1)
+        np.testing.assert_array_equal(ctx.ti_results()[0], s1)
+        assert len(path.read_text().splitlines()) == 1
+        # FP64: the fused SIMT form only, tuned over threads per ring
+        cfg64 = _gpu_cfg(pg, c, ti, pg.PG_FP64, pg.PG_FORM_AUTO)
+        ctx.set_tuning(path, pg.PG_TUNE_ON)
+        ctx.ti_setup(cfg64, *args)
+        f64, th64, _ = ctx.ti_tuning()
+        assert f64 == pg.PG_FORM_FUSED and th64 in (32, 64, 128)
+        assert len(path.read_text().splitlines()) == 2
+    finally:
+        ctx.set_tuning(None, pg.PG_TUNE_OFF)
