@@ -10,7 +10,9 @@
 // seed (RNG key base; replica j uses seed + j, lambda point i uses stream i),
 // init ('path': beads on the path as init_path does, verletmodule.f90:40-48;
 // 'well': every bead at well 1), init_sigma (Gaussian noise on the start
-// positions), chunk (steps per device launch sequence).
+// positions), chunk (steps per device launch sequence), tune (JSON-lines cache
+// of the autotuner: with form 'auto' the launch parameters are tuned on the
+// first run of each batch shape and read back afterwards).
 // restart >= 1 writes, after the run, the reference's restart files
 // restart_proc<iproc>_<ii>.xyz (verletmodule.f90:162-185; the task -> (rank,
 // local index) split of pimd_par.f90:109-110, 332-353 for nproc ranks, key
@@ -164,6 +166,7 @@ int main(int argc, char **argv) {
     const double init_sigma = nl.real("init_sigma", 0.0);
     const int64_t chunk = nl.integer("chunk", 5000);
     const std::string pesfile = nl.str("pes_params", "");
+    const std::string tune = nl.str("tune", "");
     if (parse_only) {
         std::printf("{\"n\": %lld, \"beta\": %.17g, \"NMC\": %lld, \"Noutput\": %lld, \"dt\": %.17g, "
                     "\"nintegral\": %lld, \"nrep\": %lld, \"thermostat\": %d, \"ndim\": %d, \"natom\": %d, "
@@ -171,13 +174,13 @@ int main(int argc, char **argv) {
                     "\"readpath\": %s, \"cayley\": %s, \"npath\": %lld, \"restart\": %d, \"pes\": \"%s\", "
                     "\"precision\": \"%s\", \"form\": \"%s\", \"seed\": %llu, \"init\": \"%s\", "
                     "\"init_sigma\": %.17g, \"nproc\": %lld, \"instapath\": %s, \"centre\": %s, "
-                    "\"fixedends\": %s}\n",
+                    "\"fixedends\": %s, \"tune\": \"%s\"}\n",
                     (long long)n, beta, (long long)NMC, (long long)Noutput, dt, (long long)nintegral,
                     (long long)nrep, thermostat, ndim, natom, xunit, (long long)imin, tau, gamma, dHdrlimit,
                     readpath ? "true" : "false", cayley ? "true" : "false", (long long)npath, restart,
                     pes.c_str(), prec.c_str(), form.c_str(), (unsigned long long)seed, init.c_str(), init_sigma,
                     (long long)nproc, instapath ? "true" : "false", centre ? "true" : "false",
-                    fixedends ? "true" : "false");
+                    fixedends ? "true" : "false", tune.c_str());
         return 0;
     }
     auto t0 = std::chrono::steady_clock::now();
@@ -398,6 +401,7 @@ int main(int argc, char **argv) {
         }
         from_files = true;
     }
+    if (!tune.empty()) CHECK(pg_set_tuning(ctx, tune.c_str(), PG_TUNE_ON));
     CHECK(pg_ti_setup(ctx, &cfg, nrings, nintegral, rlam.data(), rseed.data(), rstream.data(), a.data(), b.data(),
                       dbdl.data(), xref.data(), from_files ? x0.data() : nullptr, from_files ? p0.data() : nullptr));
     if (restart == 2) {

@@ -25,7 +25,7 @@ import pimdgpu as pg
 
 
 def run_ti(cfg, precision=pg.PG_MIXED, form=pg.PG_FORM_AUTO, nmc=None, nrep=None, nintegral=None,
-           seed_offset=0, chunk=2000, device=0, ctx=None, verbose=False):
+           seed_offset=0, chunk=2000, device=0, ctx=None, verbose=False, tune=None):
     c = dict(cfg)
     if nrep is not None:
         c["nrep"] = nrep
@@ -39,6 +39,8 @@ def run_ti(cfg, precision=pg.PG_MIXED, form=pg.PG_FORM_AUTO, nmc=None, nrep=None
     try:
         ctx.set_system(c["ndim"], c["natom"], c["mass"], c["pes_id"], c["params"], c["V0"])
         tcfg = ti.ti_config(pg, precision, form)
+        if tune:  # autotuner cache (AUTO form): tuned on the first batch of each shape
+            ctx.set_tuning(tune, pg.PG_TUNE_ON)
         ctx.ti_setup(tcfg, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
         form_used, _ = ctx.ti_form(1)
         t0 = time.perf_counter()
