@@ -341,11 +341,12 @@ __global__ void k_build_split_image(unsigned char *img) {
 }
 
 // ---------------------------------------------------------------- TI step on the tensor cores
-// One launch per MD step (k_tc_step): two split-BF16 GEMMs per column tile
-// with the forces in between, and one final launch per advance (k_tc_final)
-// for the positions and the estimator of the last step.  The ring state
-// (q, pi, x) stays resident in L2 between launches; the launches of an advance
-// are replayed from one captured CUDA graph, followed by one step-counter add.
+// k_tc_step runs up to 50 MD steps per launch (two split-BF16 GEMMs per column
+// tile and step with the forces in between); one final launch per advance
+// (k_tc_final) writes the positions and the estimator of the last step.  The
+// ring state stays resident in L2 (and q in tensor memory within a launch);
+// the launches of an advance are replayed from one captured CUDA graph,
+// followed by one step-counter add.
 struct TcArgs {
     int64_t nrings;
     int nd, ndim, natom;
@@ -920,10 +921,11 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tc_final(TcArgs a) {
     tile_release(sh, tmem, a.err, 0);
 }
 
-// One MD step (verletmodule.f90:423-435 in normal-mode form) of the rings
-// [r0, r1) of this CTA, r0 = floor(b R / G), r1 = floor((b + 1) R / G) for
-// CTA b of G (so every SM gets the same number of rings), walked in chunks of
-// up to 64 columns.  T is copied in and TMEM allocated once per CTA.  Per chunk:
+// MD steps sofs .. sofs + nsub - 1 (verletmodule.f90:423-435 in normal-mode
+// form) of the rings [r0, r1) of this CTA, r0 = floor(b R / G), r1 =
+// floor((b + 1) R / G) for CTA b of G (so every SM gets the same number of
+// rings), walked in chunks of up to 64 columns, step after step.  T is copied
+// in and TMEM allocated once per launch.  Per chunk and step:
 //   GEMM 1: x = T q + x*; estimator of step s-1; forces F(x) split straight
 //           into the B operand;
 //   GEMM 2: T F; kick, half rotation, OU, half rotation of (q, pi) as one
