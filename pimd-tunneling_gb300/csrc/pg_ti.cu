@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "pg_internal.h"
+#include "pg_tune.h"
 
 namespace pg {
 
@@ -1048,11 +1049,6 @@ static int ti_advance_impl(pg_ctx *ctx, int64_t nsteps, double *device_ms);
 // 128 threads per ring) is set up and advanced for a short timed probe, the
 // fastest is appended to the file, and the batch is set up again with it (so
 // its initial state is that of a plain setup with the chosen parameters).
-struct TuneChoice {
-    int form = PG_FORM_AUTO, simt_threads = 0, tc_steps = 0;
-    double ms_per_step = 0.0;
-};
-
 static std::string tune_key(pg_ctx *ctx, const pg_ti_config *cfg, int64_t nrings) {
     cudaDeviceProp prop;
     std::string dev = cudaGetDeviceProperties(&prop, ctx->device) == cudaSuccess ? prop.name : "unknown";
@@ -1065,38 +1061,6 @@ static std::string tune_key(pg_ctx *ctx, const pg_ti_config *cfg, int64_t nrings
              ctx->sm_count, (long long)cfg->nbeads, ctx->nd, ctx->natom, ctx->pes_id, (int)cfg->precision,
              (int)cfg->thermostat, (int)cfg->cayley, cfg->dhdr_limit >= 0.0 ? 1 : 0, (long long)nb);
     return buf;
-}
-
-static bool tune_int(const char *line, const char *name, int &v) {
-    const char *q = strstr(line, name);
-    return q && sscanf(q + strlen(name), " : %d", &v) == 1;
-}
-
-static bool tune_lookup(const std::string &path, const std::string &key, TuneChoice &c) {
-    FILE *fp = fopen(path.c_str(), "r");
-    if (!fp) return false;
-    const std::string kq = "\"key\": \"" + key + "\"";
-    char line[2048];
-    bool found = false;
-    while (fgets(line, sizeof(line), fp))  // the last record of a key wins
-        if (strstr(line, kq.c_str())) {
-            TuneChoice t;
-            if (tune_int(line, "\"form\"", t.form) && tune_int(line, "\"simt_threads\"", t.simt_threads) &&
-                tune_int(line, "\"tc_steps\"", t.tc_steps)) {
-                c = t;
-                found = true;
-            }
-        }
-    fclose(fp);
-    return found;
-}
-
-static void tune_record(const std::string &path, const std::string &key, const TuneChoice &c) {
-    FILE *fp = fopen(path.c_str(), "a");
-    if (!fp) return;  // a cache that cannot be written is not an error
-    fprintf(fp, "{\"key\": \"%s\", \"form\": %d, \"simt_threads\": %d, \"tc_steps\": %d, \"ms_per_step\": %.6g}\n",
-            key.c_str(), c.form, c.simt_threads, c.tc_steps, c.ms_per_step);
-    fclose(fp);
 }
 
 extern "C" int pg_set_tuning(pg_ctx *ctx, const char *cache_path, int32_t mode) {
