@@ -10,7 +10,8 @@ module pimdgpu
   use, intrinsic :: iso_c_binding
   implicit none
 
-  integer(c_int), parameter :: PG_OK = 0
+  integer(c_int), parameter :: PG_OK = 0, PG_ERR_ARG = 1, PG_ERR_CUDA = 2, PG_ERR_STATE = 3, &
+       PG_ERR_UNSUPPORTED = 4, PG_ERR_IO = 5, PG_ERR_NUMERIC = 6
   integer(c_int32_t), parameter :: PG_PES_1D = 1, PG_PES_2DTEST = 2, PG_PES_SYNTH9 = 3, &
        PG_PES_SYNTH18 = 4, PG_PES_HARMONIC = 5, PG_PES_DISTGAUSS = 6
   integer(c_int32_t), parameter :: PG_FP64 = 0, PG_MIXED = 1
@@ -18,6 +19,7 @@ module pimdgpu
        PG_FORM_TENSOR = 3
   integer(c_int32_t), parameter :: PG_ANDERSEN = 1, PG_LANGEVIN = 2
   integer(c_int32_t), parameter :: PG_TUNE_OFF = 0, PG_TUNE_CACHE = 1, PG_TUNE_ON = 2
+  integer(c_int32_t), parameter :: PG_RING_NAN = 1, PG_RING_TIMEOUT = 2   ! per-ring status bits
 
   type, bind(c) :: pg_ti_config
      integer(c_int64_t) :: nbeads

@@ -20,6 +20,7 @@ PG_FP64, PG_MIXED = 0, 1
 PG_FORM_AUTO, PG_FORM_PLAIN, PG_FORM_FUSED, PG_FORM_TENSOR = 0, 1, 2, 3
 PG_TUNE_OFF, PG_TUNE_CACHE, PG_TUNE_ON = 0, 1, 2
 PG_ANDERSEN, PG_LANGEVIN = 1, 2
+PG_RING_NAN, PG_RING_TIMEOUT = 1, 2  # per-ring status bits
 
 # Every symbol include/pimdgpu.h declares.
 EXPORTS = [

@@ -102,3 +102,22 @@ def test_ti_inputs_layout():
     assert list(ti.ring_lambda) == [0, 0, 0, 1, 1, 1, 2, 2, 2, 3, 3, 3]
     assert list(ti.ring_seed[:4]) == [0, 1, 2, 0]
     assert ti.b.shape == (4, 2) and ti.xref.shape == (4, 2 * c["P"])
+
+
+def _header_constants():
+    txt = open(os.path.join(ROOT, "include", "pimdgpu.h")).read()
+    return {k: int(v) for k, v in re.findall(r"^#define (PG_[A-Z0-9_]+) (-?\d+)\b", txt, flags=re.M)}
+
+
+def test_constants_agree_across_header_python_and_fortran(pg):
+    """Every numeric constant of include/pimdgpu.h has the same value in the
+    Python binding and, where the Fortran module declares it, in pimdgpu_mod.f90."""
+    h = _header_constants()
+    assert len(h) >= 20
+    for k, v in h.items():
+        assert getattr(pg, k) == v, k
+    ftxt = open(os.path.join(ROOT, "pimd-tunneling_gb300", "fortran", "pimdgpu_mod.f90")).read()
+    fortran = {k: int(v) for k, v in re.findall(r"\b(PG_[A-Z0-9_]+)\s*=\s*(-?\d+)", ftxt)}
+    assert len(fortran) >= 15
+    for k, v in fortran.items():
+        assert h[k] == v, k
