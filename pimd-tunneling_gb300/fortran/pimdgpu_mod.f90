@@ -168,6 +168,85 @@ module pimdgpu
        character(kind=c_char), intent(in) :: path(*)
      end function pg_ti_checkpoint_load
 
+     integer(c_int32_t) function pg_version() bind(c, name="pg_version")
+       import :: c_int32_t
+     end function pg_version
+
+     integer(c_int) function pg_nm_transform(ctx, P, ncol, xin, xout, precision) bind(c, name="pg_nm_transform")
+       import :: c_int, c_ptr, c_int64_t, c_int32_t, c_double
+       type(c_ptr), value :: ctx
+       integer(c_int64_t), value :: P, ncol
+       real(c_double), intent(in) :: xin(*)
+       real(c_double), intent(out) :: xout(*)
+       integer(c_int32_t), value :: precision
+     end function pg_nm_transform
+
+     integer(c_int) function pg_nm_transform_noalloc(P, ncol, d_in, d_out, stream) &
+          bind(c, name="pg_nm_transform_noalloc")
+       import :: c_int, c_ptr, c_int64_t
+       integer(c_int64_t), value :: P, ncol
+       type(c_ptr), value :: d_in, d_out, stream   ! device pointers, CUDA stream
+     end function pg_nm_transform_noalloc
+
+     integer(c_int) function pg_ti_advance_timed(ctx, nsteps, device_ms) bind(c, name="pg_ti_advance_timed")
+       import :: c_int, c_ptr, c_int64_t, c_double
+       type(c_ptr), value :: ctx
+       integer(c_int64_t), value :: nsteps
+       real(c_double), intent(out) :: device_ms
+     end function pg_ti_advance_timed
+
+     integer(c_int) function pg_ti_get_step(ctx, step) bind(c, name="pg_ti_get_step")
+       import :: c_int, c_ptr, c_int64_t
+       type(c_ptr), value :: ctx
+       integer(c_int64_t), intent(out) :: step
+     end function pg_ti_get_step
+
+     integer(c_int) function pg_ti_get_form(ctx, nsteps, form, launches) bind(c, name="pg_ti_get_form")
+       import :: c_int, c_ptr, c_int64_t, c_int32_t
+       type(c_ptr), value :: ctx
+       integer(c_int64_t), value :: nsteps
+       integer(c_int32_t), intent(out) :: form
+       integer(c_int64_t), intent(out) :: launches
+     end function pg_ti_get_form
+
+     integer(c_int) function pg_ti_kernel_times(ctx, nsteps, nkinds, ms_per_launch, count, bytes_per_launch, &
+          names) bind(c, name="pg_ti_kernel_times")
+       import :: c_int, c_ptr, c_int64_t, c_int32_t, c_double
+       type(c_ptr), value :: ctx
+       integer(c_int64_t), value :: nsteps
+       integer(c_int32_t), intent(out) :: nkinds
+       real(c_double), intent(out) :: ms_per_launch(*), bytes_per_launch(*)
+       integer(c_int64_t), intent(out) :: count(*)
+       type(c_ptr), intent(out) :: names(*)   ! C strings (c_f_pointer to read them)
+     end function pg_ti_kernel_times
+
+     integer(c_int) function pg_ti_release(ctx) bind(c, name="pg_ti_release")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function pg_ti_release
+
+     integer(c_int) function pg_spline(x, y, n, yp1, ypn, y2) bind(c, name="pg_spline")
+       import :: c_int, c_int64_t, c_double
+       real(c_double), intent(in) :: x(*), y(*)
+       integer(c_int64_t), value :: n
+       real(c_double), value :: yp1, ypn
+       real(c_double), intent(out) :: y2(*)
+     end function pg_spline
+
+     integer(c_int) function pg_splint(xa, ya, y2a, n, x, y, dydx) bind(c, name="pg_splint")
+       import :: c_int, c_int64_t, c_double
+       real(c_double), intent(in) :: xa(*), ya(*), y2a(*)
+       integer(c_int64_t), value :: n
+       real(c_double), value :: x
+       real(c_double), intent(out) :: y, dydx
+     end function pg_splint
+
+     integer(c_int) function pg_splitting_from_ratio(beta, qratio, delta) bind(c, name="pg_splitting_from_ratio")
+       import :: c_int, c_double
+       real(c_double), value :: beta, qratio
+       real(c_double), intent(out) :: delta
+     end function pg_splitting_from_ratio
+
      integer(c_int) function pg_set_tuning(ctx, cache_path, mode) bind(c, name="pg_set_tuning")
        import :: c_int, c_ptr, c_char, c_int32_t
        type(c_ptr), value :: ctx

@@ -121,3 +121,17 @@ def test_constants_agree_across_header_python_and_fortran(pg):
     assert len(fortran) >= 15
     for k, v in fortran.items():
         assert h[k] == v, k
+
+
+def test_fortran_module_binds_every_function():
+    """pimdgpu_mod.f90 has a bind(c) interface for every function of the header,
+    each interface body is closed by its own end function, and no line passes the
+    132 characters of free-form Fortran (no Fortran compiler is available here)."""
+    ftxt = open(os.path.join(ROOT, "pimd-tunneling_gb300", "fortran", "pimdgpu_mod.f90")).read()
+    bound = set(re.findall(r'bind\(c, name="(pg_[a-z0-9_]+)"\)', ftxt))
+    assert set(_header_functions()) <= bound
+    opened = re.findall(r"^\s*(?:[a-z_]+\([a-z0-9_]+\)\s+)?function\s+(pg_[a-z0-9_]+)\s*\(", ftxt, flags=re.M)
+    closed = re.findall(r"^\s*end function\s+(pg_[a-z0-9_]+)\s*$", ftxt, flags=re.M)
+    assert opened == closed
+    for line in ftxt.splitlines():
+        assert len(line) <= 132, line
