@@ -151,6 +151,7 @@ int main(int argc, char **argv) {
     const double dHdrlimit = nl.real("dHdrlimit", -1.0);
     const bool readpath = nl.logical("readpath", true);
     const bool cayley = nl.logical("cayley", false);
+    const bool readhess = nl.logical("readhess", false);  // pimd_par.f90:83
     const bool iprint = nl.logical("iprint", false);
     const int64_t npath = nl.integer("npath", 0);
     const int restart = (int)nl.integer("restart", 0);
@@ -174,14 +175,19 @@ int main(int argc, char **argv) {
                     "\"readpath\": %s, \"cayley\": %s, \"npath\": %lld, \"restart\": %d, \"pes\": \"%s\", "
                     "\"precision\": \"%s\", \"form\": \"%s\", \"seed\": %llu, \"init\": \"%s\", "
                     "\"init_sigma\": %.17g, \"nproc\": %lld, \"instapath\": %s, \"centre\": %s, "
-                    "\"fixedends\": %s, \"tune\": \"%s\"}\n",
+                    "\"fixedends\": %s, \"tune\": \"%s\", \"readhess\": %s}\n",
                     (long long)n, beta, (long long)NMC, (long long)Noutput, dt, (long long)nintegral,
                     (long long)nrep, thermostat, ndim, natom, xunit, (long long)imin, tau, gamma, dHdrlimit,
                     readpath ? "true" : "false", cayley ? "true" : "false", (long long)npath, restart,
                     pes.c_str(), prec.c_str(), form.c_str(), (unsigned long long)seed, init.c_str(), init_sigma,
                     (long long)nproc, instapath ? "true" : "false", centre ? "true" : "false",
-                    fixedends ? "true" : "false", tune.c_str());
+                    fixedends ? "true" : "false", tune.c_str(), readhess ? "true" : "false");
         return 0;
+    }
+    if (readhess) {  // needs every eigenvector of the polymer Hessian: numpy's eigh in the Python driver
+        std::fprintf(stderr, "readhess = .true.: run the Python driver (drivers.run_ti(..., readhess=True)); "
+                             "this driver has no dense eigensolver\n");
+        return 1;
     }
     auto t0 = std::chrono::steady_clock::now();
     const int nd = ndim * natom;

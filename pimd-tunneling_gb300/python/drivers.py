@@ -24,8 +24,64 @@ import pgconfigs
 import pimdgpu as pg
 
 
+def readhess_displacements(band, P, ndim, natom, mass, beta, z):
+    """Bead displacements of init_path with readhess (verletmodule.f90:49-88).
+
+    band: the (nd + 1) x (P nd) lower band of the polymer Hessian at the path
+    beads (pg_um_hessian, singlewell false), whose full eigendecomposition is
+    what detJ(x, etasquared, .false., interphess, eigvecs) returns
+    (instantonmod.f90:782-827; the interpolated Hessian it is passed is not used).
+    z: (nrep, P nd) standard normals, scaled here by sqrt(1/beta) (tempx).
+    Every mode but the lowest with eta^2 > 0 displaces the beads by
+    sqrt(1 / (eta^2 m_k)) tempx eigvec, reading the eigenvector component of
+    bead i, dimension j, atom k at natom (j + ndim i) + k as the reference does
+    (verletmodule.f90:75-83; for several atoms this differs from the Hessian's
+    atom-major dof order, reference behaviour).  eta^2 = 0 is skipped (the
+    reference divides by it).  Returns (nrep, nd P) in the ring layout
+    dx[(k ndim + j) P + i]."""
+    nd = ndim * natom
+    n = P * nd
+    band = np.asarray(band, dtype=float).reshape(nd + 1, n)
+    H = np.zeros((n, n))
+    for r in range(nd + 1):
+        i = np.arange(n - r)
+        H[i + r, i] = band[r, :n - r]
+        H[i, i + r] = band[r, :n - r]
+    w, v = np.linalg.eigh(H)
+    sel = np.arange(n) >= 1
+    sel &= w > 0.0
+    z = np.atleast_2d(np.asarray(z, dtype=float)) * np.sqrt(1.0 / beta)
+    u = (z[:, sel] / np.sqrt(w[sel])) @ v[:, sel].T  # (nrep, n): components in the eigenvector index
+    bead = np.arange(P)
+    dx = np.zeros((z.shape[0], n))
+    for j in range(ndim):
+        for k in range(natom):
+            dx[:, (k * ndim + j) * P + bead] = u[:, bead * nd + j * natom + k] / np.sqrt(mass[k])
+    return dx
+
+
+def readhess_start(ctx, c, ti, quirks=False):
+    """Start positions of every ring: the path at the ring's lambda point plus
+    the readhess displacements, one eigendecomposition per lambda point and
+    normals from each ring's own seed (numpy's Philox; the reference draws them
+    with MKL VSL)."""
+    nd, P = ti.nd, ti.P
+    x0 = np.zeros((ti.nrings, nd * P))
+    for lam in range(ti.nint):
+        rings = np.nonzero(np.asarray(ti.ring_lambda) == lam)[0]
+        if rings.size == 0:
+            continue
+        band = ctx.um_hessian(P, ti.betan, ti.xref[lam], singlewell=False, quirks=quirks)
+        z = np.stack([np.random.Generator(np.random.Philox(key=int(ti.ring_seed[r]),
+                                                           counter=[int(ti.ring_stream[r]), 49, 0, 0]))
+                      .standard_normal(nd * P) for r in rings])
+        x0[rings] = ti.xref[lam][None, :] + readhess_displacements(band, P, c["ndim"], c["natom"], c["mass"],
+                                                                   c["beta"], z)
+    return x0.ravel()
+
+
 def run_ti(cfg, precision=pg.PG_MIXED, form=pg.PG_FORM_AUTO, nmc=None, nrep=None, nintegral=None,
-           seed_offset=0, chunk=2000, device=0, ctx=None, verbose=False, tune=None):
+           seed_offset=0, chunk=2000, device=0, ctx=None, verbose=False, tune=None, readhess=False):
     c = dict(cfg)
     if nrep is not None:
         c["nrep"] = nrep
@@ -41,7 +97,8 @@ def run_ti(cfg, precision=pg.PG_MIXED, form=pg.PG_FORM_AUTO, nmc=None, nrep=None
         tcfg = ti.ti_config(pg, precision, form)
         if tune:  # autotuner cache (AUTO form): tuned on the first batch of each shape
             ctx.set_tuning(tune, pg.PG_TUNE_ON)
-        ctx.ti_setup(tcfg, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
+        x0 = readhess_start(ctx, c, ti) if readhess else None
+        ctx.ti_setup(tcfg, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref, x0=x0)
         form_used, _ = ctx.ti_form(1)
         t0 = time.perf_counter()
         dev_ms = 0.0

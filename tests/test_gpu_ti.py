@@ -578,3 +578,17 @@ def test_autotune_records_and_reuses_its_choice(ctx, pg, tmp_path):
         assert len(path.read_text().splitlines()) == 2
     finally:
         ctx.set_tuning(None, pg.PG_TUNE_OFF)
+
+
+def test_readhess_start_runs_through_the_driver(pg):
+    """run_ti(readhess=True): the polymer Hessian of each lambda point from the
+    library, the readhess displacements on the path (numpy), the batch set up
+    from them; a short run stays finite and differs from the undisplaced start."""
+    import drivers
+    c = dict(pgconfigs.load("c1"))
+    c["P"] = 32
+    c["imin"] = 0  # estimator samples from the first step
+    r1 = drivers.run_ti(c, nmc=40, nrep=2, nintegral=3, chunk=40, readhess=True)
+    r0 = drivers.run_ti(c, nmc=40, nrep=2, nintegral=3, chunk=40)
+    assert r1["nan_rings"] == 0 and np.all(np.isfinite(r1["integrand_mean"]))
+    assert r1["integrand_mean"] != r0["integrand_mean"]

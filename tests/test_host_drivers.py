@@ -37,7 +37,7 @@ def test_mcdata_namelist_parsing(drivers_built):
     assert abs(d["beta"] - 538.47) < 1e-12 and abs(d["dt"] - 0.0276) < 1e-15
     assert d["readpath"] is False and d["cayley"] is True and d["thermostat"] == 2
     assert d["pes"] == "1d" and d["precision"] == "fp64" and d["imin"] == 1000
-    assert d["tune"] == ""
+    assert d["tune"] == "" and d["readhess"] is False
     r = _run("pimd_ti", "&MCDATA n=16, tune='tune.jsonl' /", args=["--parse-only"])
     assert json.loads(r.stdout)["tune"] == "tune.jsonl"
     # reference defaults (pimd_par.f90:60-88) for keys not given
