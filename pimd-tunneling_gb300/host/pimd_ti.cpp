@@ -28,13 +28,19 @@
 #include <cstdio>
 #include <fstream>
 #include <iostream>
+#include <random>
 #include <string>
 #include <vector>
 
 #include "../../include/pimdgpu.h"
+#include "eigsym.hpp"
 #include "namelist.hpp"
 
 using namespace pgdrv;
+
+// readhess diagonalises the polymer Hessian with the host Jacobi solver: at most
+// this many dofs (n * ndim * natom) per lambda point.
+constexpr int kReadhessMaxDof = 1024;
 
 static int pes_id_of(const std::string &s) {
     std::string p = lower(s);
@@ -184,9 +190,10 @@ int main(int argc, char **argv) {
                     fixedends ? "true" : "false", tune.c_str(), readhess ? "true" : "false");
         return 0;
     }
-    if (readhess) {  // needs every eigenvector of the polymer Hessian: numpy's eigh in the Python driver
-        std::fprintf(stderr, "readhess = .true.: run the Python driver (drivers.run_ti(..., readhess=True)); "
-                             "this driver has no dense eigensolver\n");
+    if (readhess && n * ndim * natom > kReadhessMaxDof) {  // Jacobi eigensolver: O(n^3) per sweep
+        std::fprintf(stderr, "readhess = .true. with %lld polymer dofs: this driver diagonalises at most %d; "
+                             "run the Python driver (drivers.run_ti(..., readhess=True))\n",
+                     (long long)(n * ndim * natom), kReadhessMaxDof);
         return 1;
     }
     auto t0 = std::chrono::steady_clock::now();
@@ -408,8 +415,57 @@ int main(int argc, char **argv) {
         from_files = true;
     }
     if (!tune.empty()) CHECK(pg_set_tuning(ctx, tune.c_str(), PG_TUNE_ON));
+    // readhess (verletmodule.f90:49-88): the beads on the path plus displacements
+    // along the eigenvectors of the polymer Hessian at the path beads, which is
+    // what detJ diagonalises (instantonmod.f90:782-827; the interpolated Hessian
+    // it is passed is not used).  Every mode but the lowest with eta^2 > 0 moves
+    // bead i, dimension j, atom k by sqrt(1 / (eta^2 m_k)) tempx(mode) times the
+    // eigenvector component natom (j + ndim i) + k, the reference's indexing.
+    // tempx ~ N(0, 1 / beta) from a generator seeded with the ring's seed and
+    // stream (the reference uses MKL VSL).
+    std::vector<double> xh;
+    if (readhess && !from_files) {
+        const int tot = (int)(n * nd);
+        xh.resize(nstate);
+        std::vector<double> band((size_t)(nd + 1) * tot), H, ev, vec;
+        for (int64_t i = 0; i < nintegral; i++) {
+            const double *xp = &xref[(size_t)i * nd * n];
+            CHECK(pg_um_hessian(ctx, n, betan, xp, 0, 0, band.data()));
+            H.assign((size_t)tot * tot, 0.0);
+            for (int r = 0; r <= nd; r++)
+                for (int c = 0; c + r < tot; c++) {
+                    const double h = band[(size_t)r + (size_t)(nd + 1) * c];
+                    H[(size_t)(c + r) * tot + c] = h;
+                    H[(size_t)c * tot + c + r] = h;
+                }
+            if (pgh::eigsym_jacobi(tot, H, ev, vec) < 0) {
+                std::fprintf(stderr, "readhess: the Jacobi eigensolver did not converge\n");
+                return 1;
+            }
+            for (int64_t j = 0; j < nrep; j++) {
+                const int64_t r = i * nrep + j;
+                std::mt19937_64 gen(rseed[r] * 0x9E3779B97F4A7C15ull ^ ((uint64_t)rstream[r] << 32) ^ 0x52454144ull);
+                std::normal_distribution<double> gauss(0.0, std::sqrt(1.0 / beta));
+                std::vector<double> tempx(tot);
+                for (auto &t : tempx) t = gauss(gen);
+                double *xr = &xh[(size_t)r * nd * n];
+                std::copy(xp, xp + (size_t)nd * n, xr);
+                for (int m = 1; m < tot; m++) {
+                    if (!(ev[m] > 0.0)) continue;  // the reference skips eta^2 < 0 (and divides by eta^2 = 0)
+                    for (int64_t i2 = 0; i2 < n; i2++)
+                        for (int j2 = 0; j2 < ndim; j2++)
+                            for (int k2 = 0; k2 < natom; k2++) {
+                                const int64_t idof2 = (int64_t)natom * (j2 + (int64_t)ndim * i2) + k2;
+                                xr[((int64_t)k2 * ndim + j2) * n + i2] +=
+                                    std::sqrt(1.0 / (ev[m] * mass[k2])) * tempx[m] * vec[(size_t)idof2 * tot + m];
+                            }
+                }
+            }
+        }
+    }
+    const double *xstart = from_files ? x0.data() : (readhess ? xh.data() : nullptr);
     CHECK(pg_ti_setup(ctx, &cfg, nrings, nintegral, rlam.data(), rseed.data(), rstream.data(), a.data(), b.data(),
-                      dbdl.data(), xref.data(), from_files ? x0.data() : nullptr, from_files ? p0.data() : nullptr));
+                      dbdl.data(), xref.data(), xstart, from_files ? p0.data() : nullptr));
     if (restart == 2) {
         if (from_files) {
             std::vector<int64_t> ns(nrings, std::max<int64_t>(0, step0 - imin));

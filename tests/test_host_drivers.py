@@ -46,6 +46,14 @@ def test_mcdata_namelist_parsing(drivers_built):
     assert d["n"] == 100 and d["NMC"] == 5000000 and d["thermostat"] == 1 and d["ndim"] == 3
 
 
+def test_readhess_size_limit_of_the_namelist_driver(drivers_built, tmp_path):
+    """readhess diagonalises the polymer Hessian on the host (Jacobi): larger
+    polymers are refused before any device work, pointing to the Python driver."""
+    r = _run("pimd_ti", "&MCDATA n=1000, ndim=3, natom=9, readhess=.true. /", cwd=str(tmp_path))
+    assert r.returncode == 1
+    assert "readhess" in r.stderr and "Python driver" in r.stderr
+
+
 def test_rpidata_namelist_parsing(drivers_built):
     r = _run("rpi", "&RPIDATA n=512, beta=3157.75, ndim=3, natom=9, readpath=.false., pes='synth9', m=10 /",
              args=["--parse-only"])
