@@ -4,6 +4,7 @@ Each .cu translation unit is compiled in parallel, then linked with -shared.
 Outputs go to pimd-tunneling_gb300/lib/ (git-ignored).
 """
 import concurrent.futures as cf
+import glob
 import os
 import subprocess
 import sys
@@ -52,8 +53,8 @@ def build(verbose=False):
     for d in DRIVERS:
         src = os.path.join(HERE, "host", d + ".cpp")
         exe = os.path.join(OUT, d)
-        hdr = os.path.join(HERE, "host", "namelist.hpp")
-        if os.path.exists(exe) and os.path.getmtime(exe) >= max(os.path.getmtime(p) for p in (src, hdr, so)):
+        deps = [src, so] + glob.glob(os.path.join(HERE, "host", "*.hpp"))
+        if os.path.exists(exe) and os.path.getmtime(exe) >= max(os.path.getmtime(p) for p in deps):
             continue
         cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-o", exe, src, "-L" + OUT, "-lpimdgpu",
                "-Wl,-rpath,$ORIGIN"]

@@ -4,6 +4,7 @@
 // (masses.dat, well1.dat, well2.dat, path.xyz).
 #pragma once
 #include <cctype>
+#include <cstdio>
 #include <cstdlib>
 #include <fstream>
 #include <map>
@@ -165,6 +166,46 @@ inline std::vector<std::vector<double>> read_path_xyz(const std::string &path, i
         frames.push_back(fr);
     }
     return frames;
+}
+
+// Frames as xyz in Angstrom (bohr * 0.529177), each "natom / comment /
+// label x y z" (the aligned_wells.xyz / aligned_ends.xyz layout,
+// pimd_par.f90:170-183, rpi_ser.f90:81-92).  Frames are x[atom*ndim + dim].
+inline bool write_xyz(const std::string &path, const std::vector<std::vector<double>> &frames,
+                      const std::vector<std::string> &comments, int ndim, int natom,
+                      const std::vector<std::string> &label) {
+    FILE *f = std::fopen(path.c_str(), "w");
+    if (!f) return false;
+    for (size_t i = 0; i < frames.size(); i++) {
+        std::fprintf(f, " %d\n %s\n", natom, i < comments.size() ? comments[i].c_str() : "");
+        for (int j = 0; j < natom; j++) {
+            std::fprintf(f, " %s", j < (int)label.size() ? label[j].c_str() : "X");
+            for (int d = 0; d < ndim; d++) std::fprintf(f, " %.17g", frames[i][(size_t)j * ndim + d] * 0.529177);
+            std::fprintf(f, "\n");
+        }
+    }
+    return std::fclose(f) == 0;
+}
+
+// {"well1": [...], "well2": [...], "path": [[...], ...]} on standard output
+// (bohr, x[atom*ndim + dim]): the start configurations a driver run would use.
+inline void print_frames_json(const std::vector<double> &w1, const std::vector<double> &w2,
+                              const std::vector<std::vector<double>> &frames) {
+    auto arr = [](const std::vector<double> &v) {
+        std::printf("[");
+        for (size_t k = 0; k < v.size(); k++) std::printf("%s%.17g", k ? ", " : "", v[k]);
+        std::printf("]");
+    };
+    std::printf("{\"well1\": ");
+    arr(w1);
+    std::printf(", \"well2\": ");
+    arr(w2);
+    std::printf(", \"path\": [");
+    for (size_t i = 0; i < frames.size(); i++) {
+        if (i) std::printf(", ");
+        arr(frames[i]);
+    }
+    std::printf("]}\n");
 }
 
 }  // namespace pgdrv

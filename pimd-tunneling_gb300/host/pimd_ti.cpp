@@ -13,6 +13,9 @@
 // positions), chunk (steps per device launch sequence), tune (JSON-lines cache
 // of the autotuner: with form 'auto' the launch parameters are tuned on the
 // first run of each batch shape and read back afterwards).
+// Three-dimensional wells and path frames are aligned as the reference does
+// (keys alignwell, atom1, atom2, atom3; aligned_wells.xyz with alignwell);
+// --prepare-only prints the aligned start configurations and stops.
 // restart >= 1 writes, after the run, the reference's restart files
 // restart_proc<iproc>_<ii>.xyz (verletmodule.f90:162-185; the task -> (rank,
 // local index) split of pimd_par.f90:109-110, 332-353 for nproc ranks, key
@@ -33,6 +36,7 @@
 #include <vector>
 
 #include "../../include/pimdgpu.h"
+#include "align.hpp"
 #include "eigsym.hpp"
 #include "namelist.hpp"
 
@@ -132,6 +136,7 @@ static bool read_restart_xyz(const std::string &path, int64_t n, int ndim, int n
 
 int main(int argc, char **argv) {
     bool parse_only = argc > 1 && std::string(argv[1]) == "--parse-only";
+    bool prepare_only = argc > 1 && std::string(argv[1]) == "--prepare-only";
     Namelist nl;
     try {
         nl = Namelist::parse(read_all(std::cin), "MCDATA");
@@ -158,6 +163,9 @@ int main(int argc, char **argv) {
     const bool readpath = nl.logical("readpath", true);
     const bool cayley = nl.logical("cayley", false);
     const bool readhess = nl.logical("readhess", false);  // pimd_par.f90:83
+    const bool alignwell = nl.logical("alignwell", false);  // pimd_par.f90:80
+    const int atom1 = (int)nl.integer("atom1", 1), atom2 = (int)nl.integer("atom2", 2),
+              atom3 = (int)nl.integer("atom3", 3);  // pimd_par.f90:84-86
     const bool iprint = nl.logical("iprint", false);
     const int64_t npath = nl.integer("npath", 0);
     const int restart = (int)nl.integer("restart", 0);
@@ -181,16 +189,18 @@ int main(int argc, char **argv) {
                     "\"readpath\": %s, \"cayley\": %s, \"npath\": %lld, \"restart\": %d, \"pes\": \"%s\", "
                     "\"precision\": \"%s\", \"form\": \"%s\", \"seed\": %llu, \"init\": \"%s\", "
                     "\"init_sigma\": %.17g, \"nproc\": %lld, \"instapath\": %s, \"centre\": %s, "
-                    "\"fixedends\": %s, \"tune\": \"%s\", \"readhess\": %s}\n",
+                    "\"fixedends\": %s, \"tune\": \"%s\", \"readhess\": %s, \"alignwell\": %s, "
+                    "\"atom1\": %d, \"atom2\": %d, \"atom3\": %d}\n",
                     (long long)n, beta, (long long)NMC, (long long)Noutput, dt, (long long)nintegral,
                     (long long)nrep, thermostat, ndim, natom, xunit, (long long)imin, tau, gamma, dHdrlimit,
                     readpath ? "true" : "false", cayley ? "true" : "false", (long long)npath, restart,
                     pes.c_str(), prec.c_str(), form.c_str(), (unsigned long long)seed, init.c_str(), init_sigma,
                     (long long)nproc, instapath ? "true" : "false", centre ? "true" : "false",
-                    fixedends ? "true" : "false", tune.c_str(), readhess ? "true" : "false");
+                    fixedends ? "true" : "false", tune.c_str(), readhess ? "true" : "false",
+                    alignwell ? "true" : "false", atom1, atom2, atom3);
         return 0;
     }
-    if (readhess && n * ndim * natom > kReadhessMaxDof) {  // Jacobi eigensolver: O(n^3) per sweep
+    if (readhess && !prepare_only && n * ndim * natom > kReadhessMaxDof) {  // Jacobi eigensolver: O(n^3) per sweep
         std::fprintf(stderr, "readhess = .true. with %lld polymer dofs: this driver diagonalises at most %d; "
                              "run the Python driver (drivers.run_ti(..., readhess=True))\n",
                      (long long)(n * ndim * natom), kReadhessMaxDof);
@@ -213,6 +223,40 @@ int main(int argc, char **argv) {
         std::fprintf(stderr, "%s\n", e.what());
         return 1;
     }
+    // wells aligned as pimd_par.f90:159-183 does (three-dimensional systems;
+    // others are left as read, where the reference stops,
+    // instantonmod.f90:234-237)
+    const bool can_align = pgh::align_supported(ndim, natom, atom1, atom2, atom3);
+    if (can_align) {
+        const pgh::AlignAngles ang = pgh::align_wells_ti(w1, w2, natom, atom1, atom2, atom3, alignwell);
+        if (alignwell) {
+            char c[160];
+            std::snprintf(c, sizeof c, "rotation angles: %.17g %.17g %.17g", ang.theta1, ang.theta2, ang.theta3);
+            if (!write_xyz("aligned_wells.xyz", {w1, w2}, {c, c}, ndim, natom, label)) {
+                std::fprintf(stderr, "cannot write aligned_wells.xyz\n");
+                return 1;
+            }
+        }
+    }
+    // path: spline of path.xyz against normalised arc length, or the straight
+    // line; the frames of path.xyz aligned by the angles of the first
+    // (instantonmod.f90:916-932)
+    std::vector<std::vector<double>> frames;
+    if (readpath && npath >= 2) {
+        try {
+            frames = read_path_xyz("path.xyz", (int)npath, ndim, natom, xunit);
+        } catch (std::exception &e) {
+            std::fprintf(stderr, "%s\n", e.what());
+            return 1;
+        }
+        if (can_align) pgh::align_frames(frames, natom, atom1, atom2, atom3);
+    } else {
+        frames = {w1, w2};
+    }
+    if (prepare_only) {  // the inputs as the run would use them, no device
+        print_frames_json(w1, w2, frames);
+        return 0;
+    }
     std::printf(" Running with parameters (in a.u.):\n beta, betan, n= %.10g %.10g %lld\n", beta, betan, (long long)n);
     std::printf(" NMC, Noutput, dt= %lld %lld %.10g\n with integration points %lld\n and %lld repetitions\n",
                 (long long)NMC, (long long)Noutput, dt, (long long)nintegral, (long long)nrep);
@@ -231,19 +275,7 @@ int main(int argc, char **argv) {
     CHECK(pg_pes_eval(ctx, 2, ww.data(), vw, nullptr, PG_FP64));
     std::printf(" Potential at wells: %.12g %.12g\n", vw[0], vw[1]);
 
-    // path: spline of path.xyz against normalised arc length, or the straight line
-    std::vector<std::vector<double>> frames;
-    if (readpath && npath >= 2) {
-        try {
-            frames = read_path_xyz("path.xyz", (int)npath, ndim, natom, xunit);
-        } catch (std::exception &e) {
-            std::fprintf(stderr, "%s\n", e.what());
-            return 1;
-        }
-    } else {
-        frames = {w1, w2};
-    }
-    // normalised arc length of the path frames (instantonmod.f90:928-937, no alignment)
+    // normalised arc length of the path frames (instantonmod.f90:928-937)
     auto arc_length = [&](const std::vector<std::vector<double>> &fr) {
         std::vector<double> l(fr.size(), 0.0);
         for (size_t i = 1; i < fr.size(); i++) {

@@ -9,6 +9,9 @@
 // Keys beyond the reference's namelist: pes, pes_params (as pimd_ti), m (L-BFGS
 // history, reference 8), pgtol (reference eps2 = 1e-5), factr (1e6), maxiter,
 // quirks (1: the reference's Hessian band and mcmod_2dtest Hessian).
+// Three-dimensional wells are aligned with alignwell (aligned_ends.xyz) and
+// path frames always, as the reference does; --prepare-only prints the aligned
+// start configurations and stops.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -18,6 +21,7 @@
 #include <vector>
 
 #include "../../include/pimdgpu.h"
+#include "align.hpp"
 #include "namelist.hpp"
 
 using namespace pgdrv;
@@ -54,6 +58,7 @@ static std::vector<double> read_numbers(const std::string &path) {
 
 int main(int argc, char **argv) {
     bool parse_only = argc > 1 && std::string(argv[1]) == "--parse-only";
+    bool prepare_only = argc > 1 && std::string(argv[1]) == "--prepare-only";
     Namelist nl;
     try {
         nl = Namelist::parse(read_all(std::cin), "RPIDATA");
@@ -80,13 +85,17 @@ int main(int argc, char **argv) {
     const int64_t npoints = nl.integer("npoints", 10);                  // rpi_ser.f90:34
     const double cutofftheta = nl.real("cutofftheta", 2.0 * 3.14159265358979);  // no reference default
     const double cutoffphi = nl.real("cutoffphi", 3.14159265358979);            // no reference default
+    const bool alignwell = nl.logical("alignwell", false);              // rpi_ser.f90:38
+    const int atom1 = (int)nl.integer("atom1", 1), atom2 = (int)nl.integer("atom2", 2),
+              atom3 = (int)nl.integer("atom3", 3);  // rpi_par.f90:53-55
     if (parse_only) {
         std::printf("{\"n\": %lld, \"beta\": %.17g, \"ndim\": %d, \"natom\": %d, \"xunit\": %d, \"npath\": %lld, "
                     "\"readpath\": %s, \"pes\": \"%s\", \"m\": %d, \"pgtol\": %.17g, \"factr\": %.17g, "
-                    "\"maxiter\": %lld, \"quirks\": %d, \"angular\": %s, \"npoints\": %lld}\n",
+                    "\"maxiter\": %lld, \"quirks\": %d, \"angular\": %s, \"npoints\": %lld, \"alignwell\": %s, "
+                    "\"atom1\": %d, \"atom2\": %d, \"atom3\": %d}\n",
                     (long long)n, beta, ndim, natom, xunit, (long long)npath, readpath ? "true" : "false",
                     pes.c_str(), m, pgtol, factr, (long long)maxiter, quirks, angular ? "true" : "false",
-                    (long long)npoints);
+                    (long long)npoints, alignwell ? "true" : "false", atom1, atom2, atom3);
         return 0;
     }
     auto t0 = std::chrono::steady_clock::now();
@@ -105,6 +114,33 @@ int main(int argc, char **argv) {
         std::fprintf(stderr, "%s\n", e.what());
         return 1;
     }
+    // with alignwell each well aligned by its own angles (rpi_ser.f90:74-92);
+    // the frames of path.xyz always, by the angles of the first
+    // (instantonmod.f90:926-932); three-dimensional systems only (the
+    // reference stops otherwise, instantonmod.f90:234-237)
+    const bool can_align = pgh::align_supported(ndim, natom, atom1, atom2, atom3);
+    if (can_align && alignwell) {
+        w1 = pgh::align_atoms(w1, natom, atom1, pgh::get_align(w1, natom, atom1, atom2, atom3));
+        w2 = pgh::align_atoms(w2, natom, atom1, pgh::get_align(w2, natom, atom1, atom2, atom3));
+        if (!write_xyz("aligned_ends.xyz", {w1, w2}, {"Well1", "Well2"}, ndim, natom, label)) {
+            std::fprintf(stderr, "cannot write aligned_ends.xyz\n");
+            return 1;
+        }
+    }
+    std::vector<std::vector<double>> fr;
+    if (readpath && npath >= 2) {
+        try {
+            fr = read_path_xyz("path.xyz", (int)npath, ndim, natom, xunit);
+        } catch (std::exception &e) {
+            std::fprintf(stderr, "%s\n", e.what());
+            return 1;
+        }
+        if (can_align) pgh::align_frames(fr, natom, atom1, atom2, atom3);
+    }
+    if (prepare_only) {  // the inputs as the run would use them, no device
+        print_frames_json(w1, w2, fr.empty() ? std::vector<std::vector<double>>{w1, w2} : fr);
+        return 0;
+    }
     pg_ctx *ctx = nullptr;
     CHECK(pg_create(&ctx, 0));
     CHECK(pg_set_system(ctx, ndim, natom, mass.data(), pid, params.data(), (int64_t)params.size(), 0.0));
@@ -114,14 +150,7 @@ int main(int argc, char **argv) {
     std::printf(" beta= %.10g n= %lld\n beta_n= %.10g\n", beta, (long long)n, betan);
     // start path (x[dof*n + bead])
     std::vector<double> x((size_t)nd * n);
-    if (readpath && npath >= 2) {
-        std::vector<std::vector<double>> fr;
-        try {
-            fr = read_path_xyz("path.xyz", (int)npath, ndim, natom, xunit);
-        } catch (std::exception &e) {
-            std::fprintf(stderr, "%s\n", e.what());
-            return 1;
-        }
+    if (!fr.empty()) {
         std::vector<double> lam(fr.size(), 0.0);
         for (size_t i = 1; i < fr.size(); i++) {
             double d = 0.0;
