@@ -335,6 +335,17 @@ def instanton_lbfgs(pes, mass, N, betan, x0, a, b, m=8, factr=1.0e6, pgtol=1.0e-
     return r.x, r.fun, r
 
 
+def crossover_beta(pes, mass, ts, quirks=False):
+    """crossover.f90:49-71: eigenvalues of the mass-weighted Hessian at the
+    transition state (dsyevd there, LAPACK syevd through numpy here) and
+    beta_c = 2 pi / sqrt(-eta^2_min).  Every atom pair is mass-weighted (the
+    reference's second atom loop stops at ndim, crossover.f90:56)."""
+    H = pes.Vdoubleprime(_f64(ts), quirks=quirks)
+    s = 1.0 / np.sqrt(np.repeat(_f64(mass), pes.ndim))
+    eta2 = np.linalg.eigvalsh(H * s[:, None] * s[None, :])
+    return 2.0 * PI_REF / np.sqrt(-eta2[0]), eta2
+
+
 # ---------------------------------------------------------------- quadrature / splines
 def gauleg(x1, x2, n):
     x = np.zeros(n)

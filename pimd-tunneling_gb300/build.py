@@ -17,7 +17,7 @@ NVCC = os.environ.get("NVCC", "nvcc")
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-I" + os.path.join(HERE, "..", "include")]
 SOURCES = ["pg_api.cu", "pg_ti.cu", "pg_tc.cu", "pg_instanton.cu"]
-DRIVERS = ["pimd_ti", "rpi"]  # C++ front ends (host/*.cpp), linked against libpimdgpu.so
+DRIVERS = ["pimd_ti", "rpi", "crossover"]  # C++ front ends (host/*.cpp), linked against libpimdgpu.so
 
 
 def _compile(src, verbose=False):

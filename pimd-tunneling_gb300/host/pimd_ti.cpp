@@ -39,33 +39,13 @@
 #include "align.hpp"
 #include "eigsym.hpp"
 #include "namelist.hpp"
+#include "pes_names.hpp"
 
 using namespace pgdrv;
 
 // readhess diagonalises the polymer Hessian with the host Jacobi solver: at most
 // this many dofs (n * ndim * natom) per lambda point.
 constexpr int kReadhessMaxDof = 1024;
-
-static int pes_id_of(const std::string &s) {
-    std::string p = lower(s);
-    if (p == "1d") return PG_PES_1D;
-    if (p == "2dtest") return PG_PES_2DTEST;
-    if (p == "synth9") return PG_PES_SYNTH9;
-    if (p == "synth18") return PG_PES_SYNTH18;
-    if (p == "distgauss") return PG_PES_DISTGAUSS;
-    if (p == "harmonic") return PG_PES_HARMONIC;
-    throw std::runtime_error("unknown pes '" + s + "'");
-}
-
-static std::vector<double> read_numbers(const std::string &path) {
-    std::vector<double> v;
-    if (path.empty()) return v;
-    std::ifstream f(path);
-    if (!f) throw std::runtime_error("cannot open " + path);
-    double x;
-    while (f >> x) v.push_back(x);
-    return v;
-}
 
 // restart_proc<iproc>_<ii>.xyz of task r: nproc contiguous blocks of
 // ncalcs = ceil(ntask / nproc) tasks (pimd_par.f90:109-110, 352).

@@ -13,6 +13,7 @@ run_rpi  -- rpi_ser.f90:157-177, 222-237, 354-381 for a batch of beta values:
             linear-interpolation guess, instanton by on-device L-BFGS, log-det at
             the wells (single well, all eigenvalues) and at the instanton
             (lowest eigenvalue dropped), S = betan UM, Omega and Delta.
+crossover_beta -- crossover.f90:49-71: beta_c of a transition state.
 Every number is computed by libpimdgpu on the GPU; this module only sequences
 the calls and assembles the scalars.
 """
@@ -187,6 +188,21 @@ def run_ti_mixed(cfg, precision=pg.PG_MIXED, form=pg.PG_FORM_AUTO, nmc=None, chu
             g[3].close()
     return dict(per_P=per_P, nrings=int(len(Pr)), beads=int(beads), nmc=nmc, device_s=dev_ms / 1e3, wall_s=wall,
                 bead_steps_per_s=beads * nmc / (dev_ms / 1e3))
+
+
+def crossover_beta(ctx, ts, mass, quirks=False):
+    """crossover.f90:49-71 for the system set on ctx (mass: per atom): the Hessian at the
+    transition state ts from the library, the ascending eigenvalues eta^2 of its
+    mass-weighted form (every atom pair; the reference's second atom loop stops
+    at ndim, crossover.f90:56) and beta_c = 2 pi / sqrt(-eta^2_min), with the
+    reference's pi.  Returns (beta_c, eta2); beta_c is NaN when no eigenvalue
+    is negative."""
+    ts = np.ascontiguousarray(ts, dtype=float)
+    H = ctx.pes_hessian(ts, quirks=quirks)[0]
+    s = 1.0 / np.sqrt(np.repeat(np.asarray(mass, float), ctx.ndim))
+    eta2 = np.linalg.eigvalsh(H * s[:, None] * s[None, :])
+    beta_c = 2.0 * 3.14159265358979 / np.sqrt(-eta2[0]) if eta2[0] < 0.0 else float("nan")
+    return float(beta_c), eta2
 
 
 def linear_guess(w1, w2, N):
