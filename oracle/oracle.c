@@ -1,10 +1,11 @@
 /*
  * oracle.c -- CPU FP64 restatement of the reference ring-polymer algorithms.
  *
- * TEST INFRASTRUCTURE ONLY (the checker and the timed CPU baseline).  The
- * product library never links or calls this file.  Parity with the reference
- * is UNPINNED: the Fortran/MKL/MPI reference cannot be built here, and it ships
- * no golden vectors; the pins are analytic known answers (see oracle.h).
+ * TEST INFRASTRUCTURE ONLY (the parity reference of the tests and the timed
+ * CPU baseline).  The product library never links or calls this file.
+ * Parity with the reference is UNPINNED: the Fortran/MKL/MPI reference cannot
+ * be built here, and it ships no golden vectors; the pins are analytic known
+ * answers (see oracle.h).
  *
  * Each function names the reference routine (file:line) whose arithmetic it
  * restates.  Deliberate deviations from the reference:

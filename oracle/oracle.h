@@ -4,7 +4,7 @@
  * TEST INFRASTRUCTURE ONLY.  Nothing in the product (the pimdgpu library, its
  * host drivers) links, loads or calls this code.  Only tests/, the smoke()
  * entry point and the cpu_baseline / reference legs of bench.py use it, and
- * only as the checker or as the timed CPU baseline.
+ * only as the parity reference or as the timed CPU baseline.
  *
  * PARITY UNPINNED: the reference (Fortran + MKL + MPI) cannot be compiled on
  * this machine or on the GPU host (no Fortran compiler, no MKL, no MPI), and
