@@ -349,6 +349,8 @@ def main():
     if rank == 0 and not args.no_cpu:
         v, cores, sample = cpu_reference_rate(c, ti, target_s=12.0)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+        v1, _, sample1 = cpu_reference_rate(c, ti, target_s=3.0, nthreads=1)
+        line["cpu_baseline"]["single_core"] = {"value": v1, "sample": sample1}
     if "e2e" not in line:
         line["e2e"] = None
     if rank == 0:
