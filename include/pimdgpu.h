@@ -232,6 +232,20 @@ int pg_ti_assemble(int64_t nintegral, const double *weights, const double *mean,
 /* Tunnelling splitting from the fixed-end ratio q/q0 = tanh(beta Delta/2)
  * (python_utils/multiwell_waterdimer.py:6-10). */
 int pg_splitting_from_ratio(double beta, double qratio, double *delta);
+/* Splitting from ratios at two inverse temperatures, which removes an offset
+ * beta_bar in artanh(ratio) = Delta (beta - beta_bar) / 2
+ * (python_utils/multiwell_waterdimer.py:6-16): with y_k = artanh(ratio_k),
+ * Delta = 2 (y2 - y1) / (beta2 - beta1) and
+ * beta_bar = (beta1 y2 - beta2 y1) / (y2 - y1).  betabar may be NULL; it is
+ * NaN when y1 = y2. */
+int pg_splitting_two_beta(double beta1, double ratio1, double beta2, double ratio2, double *delta,
+                          double *betabar);
+/* Ratio of one tunnelling level pair per irreducible representation of a
+ * multi-well system (python_utils/multiwell_waterdimer.py:67-75): with
+ * rho[g] the path ratio of operation g (rho of the identity = 1) and
+ * chars[i*nop + g] the character of representation i,
+ * ratio[i] = sum_g (1 - chars[i*nop+g]) rho[g] / sum_g (1 + chars[i*nop+g]) rho[g]. */
+int pg_irrep_ratios(int64_t nirrep, int64_t nop, const double *chars, const double *rho, double *ratio);
 
 /* ---------------------------------------------------------------- instanton */
 typedef struct pg_lbfgs_opts {

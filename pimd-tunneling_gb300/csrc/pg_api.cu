@@ -456,6 +456,33 @@ extern "C" int pg_splitting_from_ratio(double beta, double qratio, double *delta
     return PG_OK;
 }
 
+extern "C" int pg_splitting_two_beta(double beta1, double ratio1, double beta2, double ratio2, double *delta,
+                                     double *betabar) {
+    if (!delta || !(beta1 > 0.0) || !(beta2 > 0.0) || beta1 == beta2)
+        return fail(PG_ERR_ARG, "bad two-beta splitting arguments");
+    if (!(ratio1 > -1.0 && ratio1 < 1.0) || !(ratio2 > -1.0 && ratio2 < 1.0))
+        return fail(PG_ERR_NUMERIC, "ratio outside (-1, 1)");
+    const double y1 = std::atanh(ratio1), y2 = std::atanh(ratio2);
+    *delta = 2.0 * (y2 - y1) / (beta2 - beta1);
+    if (betabar) *betabar = y2 != y1 ? (beta1 * y2 - beta2 * y1) / (y2 - y1) : std::nan("");
+    return PG_OK;
+}
+
+extern "C" int pg_irrep_ratios(int64_t nirrep, int64_t nop, const double *chars, const double *rho,
+                               double *ratio) {
+    if (nirrep < 0 || nop < 1 || (nirrep > 0 && (!chars || !rho || !ratio)))
+        return fail(PG_ERR_ARG, "bad irrep-ratio arguments");
+    for (int64_t i = 0; i < nirrep; i++) {
+        double em = 0.0, ep = 0.0;
+        for (int64_t g = 0; g < nop; g++) {
+            em += (1.0 - chars[i * nop + g]) * rho[g];
+            ep += (1.0 + chars[i * nop + g]) * rho[g];
+        }
+        ratio[i] = em / ep;
+    }
+    return PG_OK;
+}
+
 extern "C" int pg_rpi_assemble(double betan, double UM, double lndetJ, double lndetJ0, double *S,
                                double *omega, double *delta) {
     double s = betan * UM;

@@ -247,6 +247,20 @@ module pimdgpu
        real(c_double), intent(out) :: delta
      end function pg_splitting_from_ratio
 
+     integer(c_int) function pg_splitting_two_beta(beta1, ratio1, beta2, ratio2, delta, betabar) &
+          bind(c, name="pg_splitting_two_beta")
+       import :: c_int, c_double
+       real(c_double), value :: beta1, ratio1, beta2, ratio2
+       real(c_double), intent(out) :: delta, betabar
+     end function pg_splitting_two_beta
+
+     integer(c_int) function pg_irrep_ratios(nirrep, nop, chars, rho, ratio) bind(c, name="pg_irrep_ratios")
+       import :: c_int, c_int64_t, c_double
+       integer(c_int64_t), value :: nirrep, nop
+       real(c_double), intent(in) :: chars(*), rho(*)
+       real(c_double), intent(out) :: ratio(*)
+     end function pg_irrep_ratios
+
      integer(c_int) function pg_set_tuning(ctx, cache_path, mode) bind(c, name="pg_set_tuning")
        import :: c_int, c_ptr, c_char, c_int32_t
        type(c_ptr), value :: ctx

@@ -14,6 +14,8 @@ run_rpi  -- rpi_ser.f90:157-177, 222-237, 354-381 for a batch of beta values:
             the wells (single well, all eigenvalues) and at the instanton
             (lowest eigenvalue dropped), S = betan UM, Omega and Delta.
 crossover_beta -- crossover.f90:49-71: beta_c of a transition state.
+multiwell_levels -- python_utils/multiwell_waterdimer.py: splittings per
+            irreducible representation from path ratios at two temperatures.
 Every number is computed by libpimdgpu on the GPU; this module only sequences
 the calls and assembles the scalars.
 """
@@ -203,6 +205,18 @@ def crossover_beta(ctx, ts, mass, quirks=False):
     eta2 = np.linalg.eigvalsh(H * s[:, None] * s[None, :])
     beta_c = 2.0 * 3.14159265358979 / np.sqrt(-eta2[0]) if eta2[0] < 0.0 else float("nan")
     return float(beta_c), eta2
+
+
+def multiwell_levels(chars, rho1, rho2, beta1, beta2):
+    """python_utils/multiwell_waterdimer.py:65-84: per irreducible
+    representation (rows of chars, columns the operations g), the level-pair
+    ratios I at two inverse temperatures from the path ratios rho_g (rho of
+    the identity = 1), then Delta = 2 (artanh I2 - artanh I1) / (beta2 - beta1)
+    in Hartree (the script prints 219475 Delta, cm^-1) and the offset beta_bar.
+    Returns (delta, betabar, I1, I2)."""
+    I1, I2 = pg.irrep_ratios(chars, rho1), pg.irrep_ratios(chars, rho2)
+    out = [pg.splitting_two_beta(beta1, a, beta2, b) for a, b in zip(I1, I2)]
+    return np.array([d for d, _ in out]), np.array([b for _, b in out]), I1, I2
 
 
 def linear_guess(w1, w2, N):

@@ -28,7 +28,8 @@ EXPORTS = [
     "pg_pes_hessian", "pg_nm_transform", "pg_ti_setup", "pg_ti_advance", "pg_ti_get_state",
     "pg_ti_get_results", "pg_ti_lambda_reduce", "pg_ti_get_step", "pg_ti_advance_timed", "pg_ti_get_form", "pg_ti_kernel_times", "pg_set_tuning", "pg_ti_get_tuning", "pg_ti_checkpoint_save",
     "pg_ti_checkpoint_load", "pg_ti_release", "pg_propagate_pimd", "pg_gauleg", "pg_spline",
-    "pg_splint", "pg_ti_assemble", "pg_splitting_from_ratio", "pg_instanton_fg",
+    "pg_splint", "pg_ti_assemble", "pg_splitting_from_ratio", "pg_splitting_two_beta", "pg_irrep_ratios",
+    "pg_instanton_fg",
     "pg_instanton_optimize", "pg_um_hessian", "pg_instanton_logdet", "pg_rpi_assemble",
     "pg_nm_transform_noalloc", "pg_ti_advance_group", "pg_ti_set_accumulators",
 ]
@@ -95,6 +96,8 @@ def lib():
         L.pg_splint.argtypes = [P, P, P, I64, D, P, P]
         L.pg_ti_assemble.argtypes = [I64, P, P, P, D, P, P, P]
         L.pg_splitting_from_ratio.argtypes = [D, D, P]
+        L.pg_splitting_two_beta.argtypes = [D, D, D, D, P, P]
+        L.pg_irrep_ratios.argtypes = [I64, I64, P, P, P]
         L.pg_instanton_fg.argtypes = [P, I64, I64, P, P, P, P, P, P]
         L.pg_instanton_optimize.argtypes = [P, I64, I64, P, P, P, P, P, P, P, P]
         L.pg_um_hessian.argtypes = [P, I64, D, P, I32, I32, P]
@@ -151,6 +154,24 @@ def splitting_from_ratio(beta, qratio):
     d = C.c_double()
     check(lib().pg_splitting_from_ratio(beta, qratio, C.byref(d)))
     return d.value
+
+
+def splitting_two_beta(beta1, ratio1, beta2, ratio2):
+    """(Delta, beta_bar) from ratios at two inverse temperatures."""
+    d, b = C.c_double(), C.c_double()
+    check(lib().pg_splitting_two_beta(beta1, ratio1, beta2, ratio2, C.byref(d), C.byref(b)))
+    return d.value, b.value
+
+
+def irrep_ratios(chars, rho):
+    """Level-pair ratio per irreducible representation; chars: (nirrep, nop)."""
+    ch = _f64(np.atleast_2d(chars))
+    r = _f64(rho)
+    if ch.shape[1] != r.size:
+        raise ValueError("chars has %d columns for %d operations" % (ch.shape[1], r.size))
+    out = np.zeros(ch.shape[0])
+    check(lib().pg_irrep_ratios(ch.shape[0], ch.shape[1], _p(ch), _p(r), _p(out)))
+    return out
 
 
 def rpi_assemble(betan, UM, lndetJ, lndetJ0):
