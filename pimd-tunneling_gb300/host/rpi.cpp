@@ -22,6 +22,7 @@
 
 #include "../../include/pimdgpu.h"
 #include "align.hpp"
+#include "eigsym.hpp"
 #include "namelist.hpp"
 #include "pes_names.hpp"
 
@@ -66,16 +67,19 @@ int main(int argc, char **argv) {
     const double cutofftheta = nl.real("cutofftheta", 2.0 * 3.14159265358979);  // no reference default
     const double cutoffphi = nl.real("cutoffphi", 3.14159265358979);            // no reference default
     const bool alignwell = nl.logical("alignwell", false);              // rpi_ser.f90:38
+    const bool checkhess = nl.logical("checkhess", false);              // rpi_ser.f90:42
+    const bool output_instanton = nl.logical("output_instanton", false);  // rpi_ser.f90:36
     const int atom1 = (int)nl.integer("atom1", 1), atom2 = (int)nl.integer("atom2", 2),
               atom3 = (int)nl.integer("atom3", 3);  // rpi_par.f90:53-55
     if (parse_only) {
         std::printf("{\"n\": %lld, \"beta\": %.17g, \"ndim\": %d, \"natom\": %d, \"xunit\": %d, \"npath\": %lld, "
                     "\"readpath\": %s, \"pes\": \"%s\", \"m\": %d, \"pgtol\": %.17g, \"factr\": %.17g, "
                     "\"maxiter\": %lld, \"quirks\": %d, \"angular\": %s, \"npoints\": %lld, \"alignwell\": %s, "
-                    "\"atom1\": %d, \"atom2\": %d, \"atom3\": %d}\n",
+                    "\"atom1\": %d, \"atom2\": %d, \"atom3\": %d, \"checkhess\": %s, \"output_instanton\": %s}\n",
                     (long long)n, beta, ndim, natom, xunit, (long long)npath, readpath ? "true" : "false",
                     pes.c_str(), m, pgtol, factr, (long long)maxiter, quirks, angular ? "true" : "false",
-                    (long long)npoints, alignwell ? "true" : "false", atom1, atom2, atom3);
+                    (long long)npoints, alignwell ? "true" : "false", atom1, atom2, atom3,
+                    checkhess ? "true" : "false", output_instanton ? "true" : "false");
         return 0;
     }
     auto t0 = std::chrono::steady_clock::now();
@@ -151,6 +155,32 @@ int main(int argc, char **argv) {
             for (int64_t bead = 1; bead <= n; bead++)  // rpi_ser.f90:157-163
                 x[(size_t)k * n + bead - 1] = ((double)(n - bead) * w1[k] + (double)(bead - 1) * w2[k]) / (double)(n - 1);
     }
+    if (checkhess) {
+        // Hessian at well 1 written row by row (hessian_well1.dat) and the
+        // eigenvalues of its mass-weighted form times 219475 (rpi_ser.f90:105-129)
+        std::printf(" Calculating Hessian as test\n");
+        std::vector<double> h((size_t)nd * nd), a((size_t)nd * nd), eta2, vec;
+        CHECK(pg_pes_hessian(ctx, 1, w1.data(), h.data(), quirks));
+        FILE *fh = std::fopen("hessian_well1.dat", "w");
+        if (!fh) {
+            std::fprintf(stderr, "cannot write hessian_well1.dat\n");
+            return 1;
+        }
+        for (int r = 0; r < nd; r++) {  // row (atom j, dim i) = dof r; columns dof c, atom-major
+            for (int c = 0; c < nd; c++) std::fprintf(fh, " %.17g", h[(size_t)r + (size_t)nd * c]);
+            std::fprintf(fh, "\n");
+        }
+        std::fclose(fh);
+        for (int r = 0; r < nd; r++)
+            for (int c = 0; c < nd; c++)
+                a[(size_t)r * nd + c] = h[(size_t)r + (size_t)nd * c] / std::sqrt(mass[r / ndim] * mass[c / ndim]);
+        if (pgh::eigsym_jacobi(nd, a, eta2, vec) < 0) {
+            std::fprintf(stderr, "checkhess: the eigensolver did not converge\n");
+            return 1;
+        }
+        std::printf(" normal modes:\n");
+        for (int j = 0; j < nd; j++) std::printf(" %d %.15g\n", j + 1, eta2[j] * 219475.0);
+    }
     std::printf(" Locating instanton\n");
     pg_lbfgs_opts o;
     o.m = m;
@@ -163,6 +193,56 @@ int main(int argc, char **argv) {
     int32_t st = 0;
     CHECK(pg_instanton_optimize(ctx, 1, n, x.data(), w1.data(), w2.data(), &betan, &o, &UM, &it, &st));
     std::printf(" Found instanton after %lld iterations (status %d).\n", (long long)it, st);
+    // V along the instanton (rpi_ser.f90:180-190): when a bead lies below
+    // well 1 the reference moves V0 to that bead's energy, which lowers every
+    // action that follows by n * min V; instanton.xyz and
+    // instantonpathenergy.csv carry the energies before that shift
+    // (rpi_ser.f90:192-218)
+    std::vector<double> vpath(n);
+    {
+        std::vector<double> xc((size_t)n * nd);
+        for (int64_t bead = 0; bead < n; bead++)
+            for (int k = 0; k < nd; k++) xc[(size_t)bead * nd + k] = x[(size_t)k * n + bead];
+        CHECK(pg_pes_eval(ctx, n, xc.data(), vpath.data(), nullptr, PG_FP64));
+    }
+    const double vmin = *std::min_element(vpath.begin(), vpath.end());
+    const double vshift = vmin < 0.0 ? vmin : 0.0;
+    if (vmin < 0.0) {
+        double vw2 = 0.0;
+        CHECK(pg_pes_eval(ctx, 1, w2.data(), &vw2, nullptr, PG_FP64));
+        std::printf(" New V0= %.15g\n New wells= %.15g %.15g\n", v0 + vmin, -vmin, vw2 - vmin);
+    }
+    {
+        FILE *fi = std::fopen("instanton.xyz", "w");
+        FILE *fe = std::fopen("instantonpathenergy.csv", "w");
+        if (!fi || !fe) {
+            std::fprintf(stderr, "cannot write instanton.xyz / instantonpathenergy.csv\n");
+            return 1;
+        }
+        std::vector<double> lam(n, 0.0);
+        for (int64_t bead = 0; bead < n; bead++) {
+            std::fprintf(fi, " %d\n Energy of minimum %.17g\n", natom, vpath[bead]);
+            for (int j = 0; j < natom; j++) {
+                std::fprintf(fi, " %s", label[j].c_str());
+                for (int d = 0; d < 3; d++)
+                    std::fprintf(fi, " %.17g", d < ndim ? x[(size_t)(j * ndim + d) * n + bead] * 0.529177 : 0.0);
+                std::fprintf(fi, "\n");
+            }
+            if (bead > 0) {
+                double dd = 0.0;
+                for (int k = 0; k < nd; k++) {
+                    const double e = x[(size_t)k * n + bead] - x[(size_t)k * n + bead - 1];
+                    dd += e * e;
+                }
+                lam[bead] = lam[bead - 1] + std::sqrt(dd);
+            }
+        }
+        for (int64_t bead = 0; bead < n; bead++)
+            std::fprintf(fe, " %.17g %.17g\n", n > 1 && lam[n - 1] > 0.0 ? lam[bead] / lam[n - 1] : 0.0, vpath[bead]);
+        std::fclose(fi);
+        std::fclose(fe);
+    }
+    UM -= (double)n * vshift;
     std::vector<double> xharm((size_t)nd * n);
     for (int k = 0; k < nd; k++)
         for (int64_t bead = 0; bead < n; bead++) xharm[(size_t)k * n + bead] = w1[k];
@@ -240,9 +320,30 @@ int main(int argc, char **argv) {
             std::fprintf(stderr, "cannot write angularI.dat\n");
             return 1;
         }
+        if (output_instanton) {
+            // the last orientation's instanton, as the reference's per-orientation
+            // overwrites leave it (rpi_ser.f90:261-270, 311-320: Angstrom in 3-D,
+            // bohr in 2-D)
+            const double *xl = xs.data() + (size_t)(nb - 1) * nd * n;
+            FILE *fi = std::fopen("instanton.xyz", "w");
+            if (!fi) {
+                std::fprintf(stderr, "cannot write instanton.xyz\n");
+                return 1;
+            }
+            for (int64_t bead = 0; bead < n; bead++) {
+                std::fprintf(fi, " %d\n Energy of minimum %lld\n", natom, (long long)(bead + 1));
+                for (int j = 0; j < natom; j++) {
+                    std::fprintf(fi, " %s", label[j].c_str());
+                    for (int d = 0; d < ndim; d++)
+                        std::fprintf(fi, " %.17g", xl[(size_t)(j * ndim + d) * n + bead] * (three ? 0.529177 : 1.0));
+                    std::fprintf(fi, "\n");
+                }
+            }
+            std::fclose(fi);
+        }
         for (int64_t q = 0; q < nb; q++) {
             double Sq, om, dq;
-            CHECK(pg_rpi_assemble(betan, um[q], ld[q], ld0, &Sq, &om, &dq));
+            CHECK(pg_rpi_assemble(betan, um[q] - (double)n * vshift, ld[q], ld0, &Sq, &om, &dq));
             double ib = std::tanh(om * (double)n);
             if (three && om * (double)n > 1.0) ib = 1.0;
             if (three) {

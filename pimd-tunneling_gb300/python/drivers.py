@@ -9,8 +9,9 @@ run_ti_mixed -- a task list whose rings have different bead numbers P (one
             context per P, all advanced together by pg_ti_advance_group on
             concurrent streams); TI is assembled per P, since betan = beta/(P+1)
             and the estimate itself depend on P.
-run_rpi  -- rpi_ser.f90:157-177, 222-237, 354-381 for a batch of beta values:
-            linear-interpolation guess, instanton by on-device L-BFGS, log-det at
+run_rpi  -- rpi_ser.f90:157-190, 222-237, 354-381 for a batch of beta values:
+            linear-interpolation guess, instanton by on-device L-BFGS (V0 moved
+            to the lowest bead when one lies below well 1), log-det at
             the wells (single well, all eigenvalues) and at the instanton
             (lowest eigenvalue dropped), S = betan UM, Omega and Delta.
 crossover_beta -- crossover.f90:49-71: beta_c of a transition state.
@@ -244,6 +245,12 @@ def run_rpi(cfg, N=None, betas=None, m=8, factr=1.0e6, pgtol=1.0e-5, maxiter=200
         x, UM, it, st = ctx.instanton_optimize(N, x0, w1, np.tile(w2, nb), betan, m=m, factr=factr, pgtol=pgtol,
                                                maxiter=maxiter)
         t_opt = time.perf_counter() - t0
+        # V along each instanton: a bead below well 1 moves V0 to its energy,
+        # which raises the action by -N min V (rpi_ser.f90:180-190)
+        beads = np.asarray(x).reshape(nb, nd, N).transpose(0, 2, 1).reshape(nb * N, nd)
+        vpath = ctx.pes_eval(beads)[0].reshape(nb, N)
+        vshift = np.minimum(vpath.min(axis=1), 0.0)
+        UM = np.asarray(UM) - N * vshift
         xharm = np.concatenate([np.repeat(w1, N) for _ in range(nb)])
         t0 = time.perf_counter()
         ld0, _, _ = ctx.instanton_logdet(N, xharm, betan, singlewell=True, skip_lowest=False, quirks=quirks)
@@ -258,4 +265,4 @@ def run_rpi(cfg, N=None, betas=None, m=8, factr=1.0e6, pgtol=1.0e-5, maxiter=200
         out.append(dict(beta=float(betas[k]), betan=float(betan[k]), UM=float(UM[k]), S=S, omega=om, delta=de,
                         lndetJ=float(ld[k]), lndetJ0=float(ld0[k]), eta2_min=float(emin[k]),
                         skipped=int(nsk[k]), iterations=int(it[k]), status=int(st[k])))
-    return dict(N=N, results=out, x=x, optimize_s=t_opt, logdet_s=t_det)
+    return dict(N=N, results=out, x=x, vpath=vpath, optimize_s=t_opt, logdet_s=t_det)

@@ -60,6 +60,7 @@ def test_rpidata_namelist_parsing(drivers_built):
     d = json.loads(r.stdout)
     assert d["n"] == 512 and d["natom"] == 9 and d["readpath"] is False and d["m"] == 10
     assert d["pgtol"] == 1e-5 and d["factr"] == 1e6
+    assert d["checkhess"] is False and d["output_instanton"] is False and d["alignwell"] is False
 
 
 def test_driver_fails_loudly_without_gpu(drivers_built, tmp_path):
@@ -113,6 +114,43 @@ def test_rpi_driver_matches_python_driver(drivers_built, tmp_path):
     S = float(re.search(r"s_kink=\s*(\S+)", r.stdout).group(1))
     ref = drivers.run_rpi(c, N=64, betas=[beta], m=10, factr=1e2, pgtol=1e-8)["results"][0]
     assert abs(S - ref["S"]) <= 1e-10 * abs(ref["S"])
+
+
+@pytest.mark.gpu
+def test_rpi_driver_side_outputs(drivers_built, tmp_path):
+    """checkhess (hessian_well1.dat and the mass-weighted eigenvalues,
+    rpi_ser.f90:105-129), instanton.xyz with the bead energies and
+    instantonpathenergy.csv (rpi_ser.f90:180-218)."""
+    import drivers
+    import pimdgpu as pg
+    c = dict(pgconfigs.load("c3"))
+    _write_inputs(tmp_path, c, ["O", "O", "C", "C", "C", "H", "H", "H", "H"])
+    beta, n, nd = c["betas"][5], 64, 27
+    text = ("&RPIDATA n=%d, beta=%.17g, ndim=3, natom=9, readpath=.false., pes='synth9', pes_params='pes.dat',\n"
+            " m=10, pgtol=1d-8, factr=1d2, checkhess=.true. /\n" % (n, beta))
+    r = _run("rpi", text, cwd=str(tmp_path))
+    assert r.returncode == 0, r.stderr
+    w1 = np.array(c["well1"])
+    ctx = pg.Context(0)
+    try:
+        ctx.set_system(c["ndim"], c["natom"], c["mass"], c["pes_id"], c["params"], c["V0"])
+        H = ctx.pes_hessian(w1)[0]
+    finally:
+        ctx.close()
+    Hf = np.loadtxt(str(tmp_path / "hessian_well1.dat"))
+    np.testing.assert_allclose(Hf, H, rtol=1e-14, atol=1e-16)
+    s = 1.0 / np.sqrt(np.repeat(c["mass"], 3))
+    eta = np.linalg.eigvalsh(H * s[:, None] * s[None, :]) * 219475.0
+    modes = re.search(r"normal modes:\n((?:\s*\d+\s+\S+\n){%d})" % nd, r.stdout).group(1).split()
+    np.testing.assert_allclose(np.array(modes[1::2], float), eta, rtol=0, atol=1e-10 * np.max(np.abs(eta)))
+    ref = drivers.run_rpi(c, N=n, betas=[beta], m=10, factr=1e2, pgtol=1e-8)
+    lines = (tmp_path / "instanton.xyz").read_text().split("\n")
+    assert len([l for l in lines if l.strip()]) == n * (2 + 9)
+    energies = np.array([float(lines[b * 11 + 1].split()[-1]) for b in range(n)])
+    np.testing.assert_allclose(energies, ref["vpath"][0], rtol=1e-8, atol=1e-12)
+    lam, vp = np.loadtxt(str(tmp_path / "instantonpathenergy.csv"), unpack=True)
+    assert lam[0] == 0.0 and lam[-1] == pytest.approx(1.0) and np.all(np.diff(lam) > 0)
+    np.testing.assert_allclose(vp, energies, rtol=1e-15, atol=0)
 
 
 @pytest.mark.gpu
