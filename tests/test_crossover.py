@@ -146,6 +146,73 @@ def test_driver_reads_inputs_then_fails_loudly_without_gpu(pg, tmp_path):
     assert "no CPU fallback" in r.stderr
 
 
+# The driver's host logic end to end on the CPU: crossover.cpp linked, in a
+# scratch directory, against a stand-in for the five C-ABI calls it makes,
+# whose Hessian is the oracle's.  Test infrastructure only: the shipped driver
+# links libpimdgpu.
+STUB = r'''
+#include <stdint.h>
+#include <stdlib.h>
+#include "oracle.h"
+#include "pimdgpu.h"
+struct pg_ctx { or_pes pes; double params[4096]; };
+const char *pg_last_error(void) { return "stand-in"; }
+int pg_create(pg_ctx **c, int32_t dev) { *c = (pg_ctx *)calloc(1, sizeof(pg_ctx)); return PG_OK; }
+int pg_destroy(pg_ctx *c) { free(c); return PG_OK; }
+int pg_set_system(pg_ctx *c, int64_t ndim, int64_t natom, const double *mass, int32_t pes_id,
+                  const double *params, int64_t nparams, double V0) {
+    for (int64_t i = 0; i < nparams; i++) c->params[i] = params[i];
+    or_pes p = {pes_id, (int32_t)ndim, (int32_t)natom, (int32_t)nparams, V0, c->params};
+    c->pes = p;
+    return PG_OK;
+}
+int pg_pes_hessian(pg_ctx *c, int64_t nconf, const double *x, double *hess, int32_t quirks) {
+    const int64_t nd = (int64_t)c->pes.ndim * c->pes.natom;
+    for (int64_t k = 0; k < nconf; k++) or_Vdoubleprime(&c->pes, x + k * nd, hess + k * nd * nd, quirks);
+    return PG_OK;
+}
+'''
+
+
+@pytest.fixture(scope="module")
+def driver_on_oracle(oracle, tmp_path_factory):
+    cxx, cc = shutil.which(os.environ.get("CXX", "g++")), shutil.which(os.environ.get("CC", "gcc"))
+    if not cxx or not cc:
+        pytest.skip("no C/C++ compiler")
+    d = tmp_path_factory.mktemp("xdrv")
+    (d / "stub.c").write_text(STUB)
+    inc = ["-I", os.path.join(ROOT, "oracle"), "-I", os.path.join(ROOT, "include")]
+    subprocess.run([cc, "-O2", "-std=c11", "-c", str(d / "stub.c"), "-o", str(d / "stub.o")] + inc, check=True)
+    exe = d / "crossover"
+    subprocess.run([cxx, "-O2", "-std=c++17", os.path.join(ROOT, "pimd-tunneling_gb300", "host", "crossover.cpp"),
+                    str(d / "stub.o"), "-o", str(exe), "-L" + os.path.join(ROOT, "oracle"), "-loracle",
+                    "-Wl,-rpath," + os.path.join(ROOT, "oracle")] + inc, check=True)
+    return str(exe)
+
+
+@pytest.mark.parametrize("case", ["c1", "synth9"])
+def test_driver_host_logic_on_the_oracle(oracle, driver_on_oracle, tmp_path, case):
+    if case == "c1":
+        c = pgconfigs.load("c1")
+        pes, mass, ts, labels = oracle.Pes(oracle.PES_2DTEST, 2, 1, c["params"]), c["mass"], c["ts"], ["H"]
+        text = "&CROSSDATA ndim=2, natom=1, pes='2dtest', pes_params='pes.dat' /"
+    else:
+        c = pgconfigs.load("c3")
+        pes = oracle.Pes(c["pes_id"], 3, 9, c["params"])
+        mass, labels = c["mass"], ["O", "O", "C", "C", "C", "H", "H", "H", "H"]
+        ts = 0.5 * (np.array(c["well1"]) + np.array(c["well2"]))
+        text = "&CROSSDATA ndim=3, natom=9, xunit=2, pes='synth9', pes_params='pes.dat' /"
+    _write_inputs(tmp_path, labels, mass, ts, pes.ndim, c["params"])
+    r = subprocess.run([driver_on_oracle], input=text, capture_output=True, text=True, cwd=str(tmp_path),
+                       timeout=120)
+    assert r.returncode == 0, r.stderr
+    b = float(re.search(r"Crossover beta=\s*(\S+)", r.stdout).group(1))
+    eta = np.array(r.stdout.split("Crossover")[0].split(), dtype=float)
+    b_ref, eta_ref = oracle.crossover_beta(pes, mass, ts)
+    assert b == pytest.approx(b_ref, rel=1e-9)
+    np.testing.assert_allclose(eta, eta_ref, rtol=0, atol=1e-10 * np.max(np.abs(eta_ref)))
+
+
 @pytest.mark.gpu
 def test_driver_matches_oracle(pg, oracle, tmp_path):
     c1 = pgconfigs.load("c1")
