@@ -146,48 +146,12 @@ def test_driver_reads_inputs_then_fails_loudly_without_gpu(pg, tmp_path):
     assert "no CPU fallback" in r.stderr
 
 
-# The driver's host logic end to end on the CPU: crossover.cpp linked, in a
-# scratch directory, against a stand-in for the five C-ABI calls it makes,
-# whose Hessian is the oracle's.  Test infrastructure only: the shipped driver
-# links libpimdgpu.
-STUB = r'''
-#include <stdint.h>
-#include <stdlib.h>
-#include "oracle.h"
-#include "pimdgpu.h"
-struct pg_ctx { or_pes pes; double params[4096]; };
-const char *pg_last_error(void) { return "stand-in"; }
-int pg_create(pg_ctx **c, int32_t dev) { *c = (pg_ctx *)calloc(1, sizeof(pg_ctx)); return PG_OK; }
-int pg_destroy(pg_ctx *c) { free(c); return PG_OK; }
-int pg_set_system(pg_ctx *c, int64_t ndim, int64_t natom, const double *mass, int32_t pes_id,
-                  const double *params, int64_t nparams, double V0) {
-    for (int64_t i = 0; i < nparams; i++) c->params[i] = params[i];
-    or_pes p = {pes_id, (int32_t)ndim, (int32_t)natom, (int32_t)nparams, V0, c->params};
-    c->pes = p;
-    return PG_OK;
-}
-int pg_pes_hessian(pg_ctx *c, int64_t nconf, const double *x, double *hess, int32_t quirks) {
-    const int64_t nd = (int64_t)c->pes.ndim * c->pes.natom;
-    for (int64_t k = 0; k < nconf; k++) or_Vdoubleprime(&c->pes, x + k * nd, hess + k * nd * nd, quirks);
-    return PG_OK;
-}
-'''
-
-
 @pytest.fixture(scope="module")
 def driver_on_oracle(oracle, tmp_path_factory):
-    cxx, cc = shutil.which(os.environ.get("CXX", "g++")), shutil.which(os.environ.get("CC", "gcc"))
-    if not cxx or not cc:
-        pytest.skip("no C/C++ compiler")
-    d = tmp_path_factory.mktemp("xdrv")
-    (d / "stub.c").write_text(STUB)
-    inc = ["-I", os.path.join(ROOT, "oracle"), "-I", os.path.join(ROOT, "include")]
-    subprocess.run([cc, "-O2", "-std=c11", "-c", str(d / "stub.c"), "-o", str(d / "stub.o")] + inc, check=True)
-    exe = d / "crossover"
-    subprocess.run([cxx, "-O2", "-std=c++17", os.path.join(ROOT, "pimd-tunneling_gb300", "host", "crossover.cpp"),
-                    str(d / "stub.o"), "-o", str(exe), "-L" + os.path.join(ROOT, "oracle"), "-loracle",
-                    "-Wl,-rpath," + os.path.join(ROOT, "oracle")] + inc, check=True)
-    return str(exe)
+    """The driver's host logic end to end on the CPU: crossover.cpp linked
+    against the oracle-backed stand-in for its C-ABI calls (tests/standin)."""
+    import standin
+    return standin.build_driver("crossover", tmp_path_factory.mktemp("xdrv"))
 
 
 @pytest.mark.parametrize("case", ["c1", "synth9"])

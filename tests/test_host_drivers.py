@@ -262,3 +262,57 @@ def test_rpi_angular_grid_batch_matches_single_solves(drivers_built, tmp_path):
             S, om, _ = pg.rpi_assemble(betan, UM[0], ld[0], ld0[0])
             assert abs(rows[k, 0] - eta[k]) < 1e-14
             np.testing.assert_allclose(rows[k, 2], np.tanh(om * N), rtol=1e-9, atol=1e-300)
+
+
+def test_rpi_driver_host_logic_on_the_oracle(oracle, tmp_path):
+    """rpi.cpp end to end on the CPU, linked against the oracle-backed stand-in
+    for its C-ABI calls (tests/standin; its optimiser returns the start path
+    unchanged): checkhess output, instanton.xyz / instantonpathenergy.csv, and
+    the action after V0 moves to the lowest bead (rpi_ser.f90:105-129, 180-218,
+    368-381).  Well 1 lies 0.3 bohr beyond a minimum of the 2-D surface, so the
+    straight start path passes below it."""
+    import standin
+    exe = standin.build_driver("rpi", tmp_path)
+    c = pgconfigs.load("c1")
+    m1, m2 = np.array(c["well1"]), np.array(c["well2"])
+    u = (m1 - m2) / np.linalg.norm(m1 - m2)
+    w1, w2 = m1 + 0.3 * u, m2
+    cc = dict(c, well1=list(w1), well2=list(w2))
+    _write_inputs(tmp_path, cc, ["H"])
+    n, beta = 8, c["beta"] / 16
+    text = ("&RPIDATA n=%d, beta=%.17g, ndim=2, natom=1, readpath=.false., pes='2dtest', pes_params='pes.dat',\n"
+            " checkhess=.true. /\n" % (n, beta))
+    r = subprocess.run([exe], input=text, capture_output=True, text=True, cwd=str(tmp_path), timeout=120)
+    assert r.returncode == 0, r.stderr
+    v0 = oracle.Pes(oracle.PES_2DTEST, 2, 1, c["params"]).V(w1)
+    pes = oracle.Pes(oracle.PES_2DTEST, 2, 1, c["params"], V0=v0)
+    k = np.arange(1, n + 1)
+    x = np.concatenate([((n - k) * w1[d] + (k - 1) * w2[d]) / (n - 1) for d in range(2)])  # rpi_ser.f90:157-163
+    vpath = np.array([pes.V(x.reshape(2, n)[:, b]) for b in range(n)])
+    vmin = vpath.min()
+    assert vmin < 0
+    assert float(re.search(r"New V0=\s*(\S+)", r.stdout).group(1)) == pytest.approx(v0 + vmin, rel=1e-12)
+    betan, mass = beta / n, c["mass"]
+    UM = oracle.UM(pes, mass, n, betan, x, w1, w2) - n * vmin
+    ld0 = oracle.logdet_band(oracle.UMhessian(pes, mass, n, betan, np.repeat(w1, n), singlewell=True), False)[0]
+    ld = oracle.logdet_band(oracle.UMhessian(pes, mass, n, betan, x), True)[0]
+    S = betan * UM
+    om = betan * np.exp(-S) * np.sqrt(S / (2 * oracle.PI_REF)) / np.exp(0.5 * (ld - ld0))
+    assert float(re.search(r"s_kink=\s*(\S+)", r.stdout).group(1)) == pytest.approx(S, rel=1e-12)
+    delta = re.search(r"RPI delta=\s*(\S+)", r.stdout).group(1)
+    assert float(delta) == pytest.approx(2 * om / betan, rel=1e-8)
+    # instanton.xyz (Angstrom, padded to three coordinates) and instantonpathenergy.csv
+    lines = (tmp_path / "instanton.xyz").read_text().split("\n")
+    energies = np.array([float(lines[3 * b + 1].split()[-1]) for b in range(n)])
+    np.testing.assert_allclose(energies, vpath, rtol=1e-14, atol=1e-16)
+    xyz = np.array([list(map(float, lines[3 * b + 2].split()[1:])) for b in range(n)])
+    np.testing.assert_allclose(xyz[:, :2] / 0.529177, x.reshape(2, n).T, rtol=1e-14)
+    assert np.all(xyz[:, 2] == 0.0)
+    lam, vp = np.loadtxt(str(tmp_path / "instantonpathenergy.csv"), unpack=True)
+    np.testing.assert_allclose(lam, (k - 1) / (n - 1), atol=1e-14)  # equally spaced straight path
+    np.testing.assert_array_equal(vp, energies)
+    # checkhess: the Hessian at well 1 and its mass-weighted eigenvalues times 219475
+    H = pes.Vdoubleprime(w1)
+    np.testing.assert_allclose(np.loadtxt(str(tmp_path / "hessian_well1.dat")), H, rtol=1e-14)
+    modes = re.search(r"normal modes:\n\s*1\s+(\S+)\n\s*2\s+(\S+)\n", r.stdout).groups()
+    np.testing.assert_allclose(np.array(modes, float), np.linalg.eigvalsh(H / mass[0]) * 219475.0, rtol=1e-10)
