@@ -7,9 +7,13 @@
 //
 // pg_instanton_optimize does not optimise: it returns the path it is given and
 // its action, which is enough to check what the drivers do with the result.
-// pg_instanton_logdet diagonalises the oracle's band Hessian densely.
+// pg_instanton_logdet diagonalises the oracle's band Hessian densely.  The TI
+// batch runs the oracle's ring propagation (the reference step order for
+// PG_FORM_PLAIN, the normal-mode-resident order otherwise); no checkpoint
+// file is written, so restarts read the restart_proc files.
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
 #include <cstdlib>
 #include <vector>
 
@@ -17,9 +21,20 @@
 #include "oracle.h"
 #include "pimdgpu.h"
 
+struct TiBatch {
+    or_ti_params prm{};
+    int64_t nrings = 0, nlam = 0, step = 0;
+    std::vector<int32_t> lam;
+    std::vector<uint64_t> seed;
+    std::vector<uint32_t> stream;
+    std::vector<double> a, b, dbdl, xref, x, p;
+    std::vector<or_ring_result> res;
+};
+
 struct pg_ctx {
     or_pes pes;
     std::vector<double> params, mass;
+    TiBatch ti;
 };
 
 extern "C" {
@@ -110,6 +125,136 @@ int pg_rpi_assemble(double betan, double UM, double lndetJ, double lndetJ0, doub
     if (S) *S = s;
     if (omega) *omega = om;
     if (delta) *delta = 2.0 * om / betan;
+    return PG_OK;
+}
+
+int pg_splitting_from_ratio(double beta, double qratio, double *delta) {
+    if (!(qratio > -1.0 && qratio < 1.0)) return PG_ERR_NUMERIC;
+    *delta = 2.0 * std::atanh(qratio) / beta;
+    return PG_OK;
+}
+int pg_um_hessian(pg_ctx *c, int64_t N, double betan, const double *x, int32_t singlewell, int32_t quirks,
+                  double *band) {
+    or_UMhessian(&c->pes, c->mass.data(), N, betan, x, singlewell, quirks, band);
+    return PG_OK;
+}
+int pg_set_tuning(pg_ctx *, const char *, int32_t) { return PG_OK; }
+// no checkpoint file: a restart then goes through the restart_proc files
+int pg_ti_checkpoint_save(pg_ctx *, const char *) { return PG_OK; }
+int pg_ti_checkpoint_load(pg_ctx *, const char *) { return PG_ERR_ARG; }
+
+// TI batch: every ring advanced by the oracle's ring propagation with the
+// same Philox streams (purposes 2 / 1 for the start positions / momenta).
+// PG_STANDIN_X0 names a file that receives the start positions x0 the driver
+// passes (text, one number per line).
+int pg_ti_setup(pg_ctx *c, const pg_ti_config *cfg, int64_t nrings, int64_t nlambda, const int32_t *ring_lambda,
+                const uint64_t *ring_seed, const uint32_t *ring_stream, const double *a, const double *b,
+                const double *dbdl, const double *xref, const double *x0, const double *p0) {
+    TiBatch &t = c->ti;
+    const int64_t nd = ndof(c), P = cfg->nbeads, ns = nd * P;
+    t.prm = or_ti_params{P, cfg->beta, cfg->beta / (double)(P + 1), cfg->dt, cfg->tau, cfg->gamma, cfg->thermostat,
+                         cfg->cayley, cfg->form == PG_FORM_PLAIN ? 0 : 1, 0, cfg->imin, cfg->noutput,
+                         cfg->dhdr_limit, cfg->init_sigma};
+    t.nrings = nrings;
+    t.nlam = nlambda;
+    t.step = 0;
+    t.lam.assign(ring_lambda, ring_lambda + nrings);
+    t.seed.assign(ring_seed, ring_seed + nrings);
+    t.stream.assign(ring_stream, ring_stream + nrings);
+    t.a.assign(a, a + nd);
+    t.b.assign(b, b + nlambda * nd);
+    t.dbdl.assign(dbdl, dbdl + nlambda * nd);
+    t.xref.assign(xref, xref + nlambda * ns);
+    t.x.assign((size_t)nrings * ns, 0.0);
+    t.p.assign((size_t)nrings * ns, 0.0);
+    t.res.assign(nrings, or_ring_result{});
+    std::vector<double> T((size_t)P * P), lam(P), bm((size_t)c->pes.natom * P), bv((size_t)P * nd);
+    or_init_nm(P, c->pes.ndim, c->pes.natom, c->mass.data(), t.prm.betan, t.prm.tau, a, b, T.data(), lam.data(),
+               bm.data(), bv.data());
+    for (int64_t r = 0; r < nrings; r++) {
+        or_ring_init(&c->pes, c->mass.data(), &t.prm, T.data(), bm.data(), &t.xref[(size_t)t.lam[r] * ns], t.seed[r],
+                     t.stream[r], 0, 2, 1, &t.x[(size_t)r * ns], &t.p[(size_t)r * ns]);
+        if (x0) std::copy(x0 + r * ns, x0 + (r + 1) * ns, t.x.begin() + r * ns);
+        if (p0) std::copy(p0 + r * ns, p0 + (r + 1) * ns, t.p.begin() + r * ns);
+        t.res[r].and_rkick = -1;
+    }
+    if (x0 && std::getenv("PG_STANDIN_X0")) {
+        FILE *f = std::fopen(std::getenv("PG_STANDIN_X0"), "w");
+        if (!f) return PG_ERR_ARG;
+        for (int64_t i = 0; i < nrings * ns; i++) std::fprintf(f, "%.17g\n", x0[i]);
+        std::fclose(f);
+    }
+    return PG_OK;
+}
+int pg_ti_advance(pg_ctx *c, int64_t nsteps) {
+    TiBatch &t = c->ti;
+    const int64_t nd = ndof(c), ns = nd * t.prm.P;
+    for (int64_t r = 0; r < t.nrings; r++) {
+        const int64_t l = t.lam[r];
+        or_ring_propagate(&c->pes, c->mass.data(), &t.prm, t.a.data(), &t.b[(size_t)l * nd], &t.dbdl[(size_t)l * nd],
+                          &t.xref[(size_t)l * ns], t.seed[r], t.stream[r], t.step, nsteps, &t.x[(size_t)r * ns],
+                          &t.p[(size_t)r * ns], &t.res[r]);
+    }
+    t.step += nsteps;
+    return PG_OK;
+}
+int pg_ti_get_step(pg_ctx *c, int64_t *step) {
+    *step = c->ti.step;
+    return PG_OK;
+}
+int pg_ti_get_state(pg_ctx *c, double *x, double *p) {
+    if (x) std::copy(c->ti.x.begin(), c->ti.x.end(), x);
+    if (p) std::copy(c->ti.p.begin(), c->ti.p.end(), p);
+    return PG_OK;
+}
+int pg_ti_get_results(pg_ctx *c, double *dhdr_sum, int64_t *nsamples, int64_t *nreinit, int32_t *status) {
+    for (int64_t r = 0; r < c->ti.nrings; r++) {
+        const or_ring_result &q = c->ti.res[r];
+        if (dhdr_sum) dhdr_sum[r] = q.dhdr_sum;
+        if (nsamples) nsamples[r] = q.nsamples;
+        if (nreinit) nreinit[r] = q.nreinit;
+        if (status) status[r] = q.status ? PG_RING_NAN : 0;
+    }
+    return PG_OK;
+}
+int pg_ti_set_accumulators(pg_ctx *c, const double *dhdr_sum, const int64_t *nsamples, int64_t step) {
+    for (int64_t r = 0; r < c->ti.nrings; r++) {
+        c->ti.res[r].dhdr_sum = dhdr_sum[r];
+        c->ti.res[r].nsamples = nsamples[r];
+    }
+    c->ti.step = step;
+    return PG_OK;
+}
+int pg_ti_lambda_reduce(pg_ctx *c, double *mean, double *var, int64_t *count) {
+    const TiBatch &t = c->ti;
+    const double bn2 = t.prm.betan * t.prm.betan;
+    for (int64_t l = 0; l < t.nlam; l++) {
+        double s = 0.0, s2 = 0.0, n = 0.0;
+        for (int64_t r = 0; r < t.nrings; r++) {
+            if (t.lam[r] != l) continue;
+            const double ns = (double)t.res[r].nsamples;
+            const double v = ns > 0.0 ? t.res[r].dhdr_sum / ns / bn2 : 0.0;
+            s += v;
+            s2 += v * v;
+            n += 1.0;
+        }
+        const double m = n > 0 ? s / n : 0.0;
+        if (mean) mean[l] = m;
+        if (var) var[l] = n > 0 ? s2 / n - m * m : 0.0;
+        if (count) count[l] = (int64_t)n;
+    }
+    return PG_OK;
+}
+int pg_ti_assemble(int64_t nintegral, const double *weights, const double *mean, const double *var, double betan,
+                   double *dA, double *sigmaA, double *qratio) {
+    double d = 0.0, s = 0.0;
+    for (int64_t i = 0; i < nintegral; i++) {
+        d += weights[i] * mean[i];
+        s += weights[i] * weights[i] * var[i];
+    }
+    *dA = d;
+    *sigmaA = s;
+    *qratio = std::exp(-d * betan);
     return PG_OK;
 }
 

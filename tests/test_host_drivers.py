@@ -316,3 +316,154 @@ def test_rpi_driver_host_logic_on_the_oracle(oracle, tmp_path):
     np.testing.assert_allclose(np.loadtxt(str(tmp_path / "hessian_well1.dat")), H, rtol=1e-14)
     modes = re.search(r"normal modes:\n\s*1\s+(\S+)\n\s*2\s+(\S+)\n", r.stdout).groups()
     np.testing.assert_allclose(np.array(modes, float), np.linalg.eigvalsh(H / mass[0]) * 219475.0, rtol=1e-10)
+
+
+def _oracle_ti(oracle, c, nmc, nm_resident=True):
+    """Delta A of the TI batch the driver sets up for c (all beads at well 1,
+    seeds 0.., stream = lambda point), by the oracle ring by ring."""
+    ti = pgconfigs.TiInputs(c, gauleg=oracle.gauleg)
+    pes = oracle.Pes(c["pes_id"], c["ndim"], c["natom"], c["params"])
+    prm = oracle.TiParams(ti.P, c["beta"], c["dt"], tau=c["tau"], gamma=c["gamma"], thermostat=2,
+                          nm_resident=nm_resident, imin=c["imin"], init_sigma=c["init_sigma"])
+    ints = np.zeros(ti.nrings)
+    for r in range(ti.nrings):
+        li = int(ti.ring_lambda[r])
+        x, p = oracle.ring_init(pes, c["mass"], prm, ti.xref[li], int(ti.ring_seed[r]), int(ti.ring_stream[r]),
+                                a=ti.a, b=ti.b[li])
+        res = oracle.ring_propagate(pes, c["mass"], prm, ti.a, ti.b[li], ti.dbdl[li], ti.xref[li],
+                                    int(ti.ring_seed[r]), int(ti.ring_stream[r]), 0, nmc, x, p)
+        ints[r] = res.dhdr_sum / res.nsamples / ti.betan ** 2
+    mean = np.array([ints[ti.ring_lambda == i].mean() for i in range(ti.nint)])
+    return float(np.dot(ti.w, mean))
+
+
+def _ti_text(c, nmc, nrep, extra=""):
+    return ("&MCDATA n=%d, beta=%.17g, NMC=%d, dt=%.17g, imin=%d, tau=%.17g, gamma=%.17g, nintegral=%d,\n"
+            " nrep=%d, thermostat=2, ndim=1, natom=1, readpath=F, pes='1d', pes_params='pes.dat',\n"
+            " precision='fp64', form='fused', init='well', init_sigma=%.17g, seed=0 %s/\n"
+            % (c["P"], c["beta"], nmc, c["dt"], c["imin"], c["tau"], c["gamma"], c["nintegral"], nrep,
+               c["init_sigma"], extra))
+
+
+def test_pimd_ti_driver_host_logic_on_the_oracle(oracle, tmp_path):
+    """pimd_ti.cpp end to end on the CPU against the oracle-backed stand-in for
+    its C-ABI calls (tests/standin): the lambda points, end points, start
+    positions, seeds and streams it sets up, and its assembly of Delta A, agree
+    with the oracle run ring by ring on the inputs the Python driver builds."""
+    import standin
+    exe = standin.build_driver("pimd_ti", tmp_path)
+    c = dict(pgconfigs.load("c0"), imin=50)
+    _write_inputs(tmp_path, c, ["H"])
+    r = subprocess.run([exe], input=_ti_text(c, 300, 2), capture_output=True, text=True, cwd=str(tmp_path),
+                       timeout=300)
+    assert r.returncode == 0, r.stderr
+    dA = float(re.search(r"final Delta A=\s*(\S+)", r.stdout).group(1))
+    ref = _oracle_ti(oracle, dict(c, nrep=2, seeds=[0, 1]), 300)
+    assert dA == pytest.approx(ref, rel=1e-12)
+
+
+def test_pimd_ti_restart_files_on_the_oracle(oracle, tmp_path):
+    """restart = 1 writes restart_proc<iproc>_<ii>.xyz; restart = 2 reads them
+    (no checkpoint file in the stand-in) and continues: 150 + 150 steps match
+    one 300-step run."""
+    import standin
+    exe = standin.build_driver("pimd_ti", tmp_path)
+    c = dict(pgconfigs.load("c0"), imin=50, P=16)
+    _write_inputs(tmp_path, c, ["H"])
+
+    def run(nmc, restart, cwd):
+        r = subprocess.run([exe], input=_ti_text(c, nmc, 3, "restart=%d, nproc=2 " % restart),
+                           capture_output=True, text=True, cwd=str(cwd), timeout=300)
+        assert r.returncode == 0, r.stderr
+        return float(re.search(r"final Delta A=\s*(\S+)", r.stdout).group(1))
+
+    run(150, 1, tmp_path)
+    names = {p.name for p in tmp_path.glob("restart_proc*.xyz")}
+    ntask = c["nintegral"] * 3  # two ranks of ceil(ntask / 2) tasks (pimd_par.f90:109-110)
+    assert len(names) == ntask and {"restart_proc0_1.xyz", "restart_proc1_1.xyz"} <= names
+    assert "restart_proc0_%d.xyz" % ((ntask + 1) // 2) in names
+    two_legs = run(150, 2, tmp_path)
+    other = tmp_path / "one"
+    other.mkdir()
+    _write_inputs(other, c, ["H"])
+    one = run(300, 0, other)
+    assert two_legs == pytest.approx(one, rel=1e-8)  # the files carry 17 significant digits
+
+
+def test_pimd_ti_readhess_on_the_oracle(oracle, tmp_path):
+    """readhess in the namelist driver (verletmodule.f90:49-88, host Jacobi
+    eigensolver), end to end on the CPU against the stand-in: every start
+    displacement lies in the span of the positive modes of the polymer Hessian
+    at the path beads other than the lowest, with N(0, 1/beta) coefficients,
+    and depends only on the ring's seed and stream."""
+    import standin
+    exe = standin.build_driver("pimd_ti", tmp_path)
+    c = pgconfigs.load("c1")
+    _write_inputs(tmp_path, c, ["H"])
+    n, nint, nrep = 8, 2, 3
+    text = ("&MCDATA n=%d, beta=%.17g, NMC=4, dt=%.17g, imin=0, tau=1.0, gamma=%.17g, nintegral=%d, nrep=%d,\n"
+            " thermostat=2, ndim=2, natom=1, readpath=F, pes='2dtest', pes_params='pes.dat', precision='fp64',\n"
+            " form='fused', init='path', seed=5, readhess=.true. /\n" % (n, c["beta"], c["dt"], c["gamma"], nint, nrep))
+    env = dict(os.environ, PG_STANDIN_X0=str(tmp_path / "x0.txt"))
+    r = subprocess.run([exe], input=text, capture_output=True, text=True, cwd=str(tmp_path), timeout=300, env=env)
+    assert r.returncode == 0, r.stderr
+    x0 = np.loadtxt(str(tmp_path / "x0.txt")).reshape(nint * nrep, 2, n)
+    ti = pgconfigs.TiInputs(dict(c, P=n, nintegral=nint, nrep=nrep), init="path", gauleg=oracle.gauleg)
+    pes = oracle.Pes(oracle.PES_2DTEST, 2, 1, c["params"], V0=c["V0"])
+    betan, m = c["beta"] / (n + 1), c["mass"][0]
+    coefs = []
+    for ring in range(nint * nrep):
+        li = ring // nrep
+        xref = ti.xref[li].reshape(2, n)
+        band = oracle.UMhessian(pes, c["mass"], n, betan, ti.xref[li])
+        tot = 2 * n
+        H = np.zeros((tot, tot))
+        for rr in range(3):
+            for col in range(tot - rr):
+                H[col + rr, col] = H[col, col + rr] = band[rr, col]
+        w, V = np.linalg.eigh(H)
+        d = (x0[ring] - xref).T.ravel()  # UMhessian order: bead-major, dimension fastest
+        t = np.sqrt(np.clip(w, 0.0, None) * m) * (V.T @ d)
+        assert abs(V[:, 0] @ d) < 1e-9 * np.linalg.norm(d)  # the lowest mode is left out
+        np.testing.assert_allclose(V[:, w <= 0].T @ d, 0.0, atol=1e-9 * np.linalg.norm(d))
+        coefs.append(t[1:][w[1:] > 0] * np.sqrt(c["beta"]))
+    z = np.concatenate(coefs)
+    assert np.all(np.abs(z) < 6.0) and 0.6 < z.std() < 1.4 and abs(z.mean()) < 0.5
+    # the same seeds and streams give the same displacements; rings of one lambda point differ
+    r2 = subprocess.run([exe], input=text, capture_output=True, text=True, cwd=str(tmp_path), timeout=300,
+                        env=dict(env, PG_STANDIN_X0=str(tmp_path / "x0b.txt")))
+    assert r2.returncode == 0, r2.stderr
+    np.testing.assert_array_equal(np.loadtxt(str(tmp_path / "x0b.txt")), x0.ravel())
+    assert not np.allclose(x0[0], x0[1])
+
+
+def test_pimd_ti_path_and_centre_on_the_oracle(oracle, tmp_path):
+    """readpath + instapath + centre through pimd_ti.cpp on the CPU against the
+    stand-in, whose optimiser keeps the spline path: here the straight segment
+    between points 10 % inside two adjacent wells (an optimised path's end
+    beads also sit off the wells, which the path [well 1, beads, well 2] needs,
+    instantonmod.f90:961-966).  instanton.xyz holds the n beads and the
+    centring finds the barrier top at 1/2 by the mirror symmetry."""
+    import standin
+    exe = standin.build_driver("pimd_ti", tmp_path)
+    c = dict(pgconfigs.load("c1"))
+    _write_inputs(tmp_path, c, ["H"])
+    m1, m2 = np.array(c["well1"]), np.array(c["well2"])
+    w1, w2 = m1 + 0.1 * (m2 - m1), m2 - 0.1 * (m2 - m1)
+    (tmp_path / "path.xyz").write_text("".join(" 1\n frame %d\n H %.17g %.17g\n" % (i, *w) for i, w in
+                                               enumerate((w1, w2))))
+    n = 24
+    text = ("&MCDATA n=%d, beta=%.17g, NMC=20, dt=%.17g, imin=10, tau=1.0, gamma=%.17g, nintegral=3,\n"
+            " nrep=2, thermostat=2, ndim=2, natom=1, readpath=T, npath=2, instapath=T, centre=T,\n"
+            " pes='2dtest', pes_params='pes.dat', precision='fp64', form='fused', init='path', seed=0 /\n"
+            % (n, c["beta"], c["dt"], c["gamma"]))
+    r = subprocess.run([exe], input=text, capture_output=True, text=True, cwd=str(tmp_path), timeout=300)
+    assert r.returncode == 0, r.stderr
+    lines = (tmp_path / "instanton.xyz").read_text().strip().split("\n")
+    assert len(lines) == 3 * n
+    beads = np.array([[float(v) for v in lines[3 * i + 2].split()[1:]] for i in range(n)]) / 0.529177
+    k = np.arange(n)[:, None] / (n - 1)
+    np.testing.assert_allclose(beads, (1 - k) * w1 + k * w2, atol=1e-12)
+    xm = float(re.search(r"Centred,\s*\S+\s+\S+\s+(\S+)", r.stdout).group(1))
+    assert abs(xm - 0.5) < 1e-6
+    assert np.isfinite(float(re.search(r"final Delta A=\s*(\S+)", r.stdout).group(1)))
