@@ -6,7 +6,8 @@
 // the drivers; the shipped drivers link libpimdgpu.
 //
 // pg_instanton_optimize does not optimise: it returns the path it is given and
-// its action, which is enough to check what the drivers do with the result.
+// its action, which is enough to check what the drivers do with the result;
+// PG_STANDIN_ENDS names a file that receives the end points of a batched call.
 // pg_instanton_logdet diagonalises the oracle's band Hessian densely.  The TI
 // batch runs the oracle's ring propagation (the reference step order for
 // PG_FORM_PLAIN, the normal-mode-resident order otherwise); no checkpoint
@@ -85,6 +86,12 @@ int pg_splint(const double *xa, const double *ya, const double *y2a, int64_t n, 
 int pg_instanton_optimize(pg_ctx *c, int64_t nbeta, int64_t N, double *x, const double *a, const double *b,
                           const double *betan, const pg_lbfgs_opts *, double *UM, int64_t *niter, int32_t *status) {
     const int64_t nd = ndof(c);
+    if (nbeta > 1 && std::getenv("PG_STANDIN_ENDS")) {  // the end points of a batch, one number per line
+        FILE *f = std::fopen(std::getenv("PG_STANDIN_ENDS"), "w");
+        if (!f) return PG_ERR_ARG;
+        for (int64_t i = 0; i < nbeta * nd; i++) std::fprintf(f, "%.17g\n", b[i]);
+        std::fclose(f);
+    }
     for (int64_t k = 0; k < nbeta; k++) {
         if (UM) UM[k] = or_UM(&c->pes, c->mass.data(), N, betan[k], x + k * nd * N, a, b + k * nd, 1);
         if (niter) niter[k] = 0;

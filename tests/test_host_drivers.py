@@ -467,3 +467,54 @@ def test_pimd_ti_path_and_centre_on_the_oracle(oracle, tmp_path):
     xm = float(re.search(r"Centred,\s*\S+\s+\S+\s+(\S+)", r.stdout).group(1))
     assert abs(xm - 0.5) < 1e-6
     assert np.isfinite(float(re.search(r"final Delta A=\s*(\S+)", r.stdout).group(1)))
+
+
+def test_rpi_angular_grid_on_the_oracle(oracle, tmp_path):
+    """angular = T for a 3-D system through rpi.cpp on the CPU against the
+    stand-in (its optimiser keeps the start path): the Gauss-Legendre angles and
+    weights, well 2 turned by R_x(theta) R_z(phi) R_x(eta) in the reference's
+    rotation convention (rpi_ser.f90:245-257, instantonmod.f90:346-376), and
+    I = tanh(Omega N) per row of angularI.dat (rpi_ser.f90:273-296; 0 here,
+    since the unoptimised path's action is large)."""
+    import align
+    import standin
+    exe = standin.build_driver("rpi", tmp_path)
+    c = pgconfigs.load("c3")
+    _write_inputs(tmp_path, c, ["O", "O", "C", "C", "C", "H", "H", "H", "H"])
+    n, npts, beta = 4, 2, 40.0
+    text = ("&RPIDATA n=%d, beta=%.17g, ndim=3, natom=9, readpath=.false., pes='synth9', pes_params='pes.dat',\n"
+            " angular=.true., npoints=%d, cutofftheta=1.0, cutoffphi=0.5 /\n" % (n, beta, npts))
+    env = dict(os.environ, PG_STANDIN_ENDS=str(tmp_path / "ends.txt"))
+    r = subprocess.run([exe], input=text, capture_output=True, text=True, cwd=str(tmp_path), timeout=300, env=env)
+    assert r.returncode == 0, r.stderr
+    rows = np.loadtxt(str(tmp_path / "angularI.dat"))
+    ends = np.loadtxt(str(tmp_path / "ends.txt")).reshape(npts ** 3, 27)
+    assert rows.shape == (npts ** 3, 5)
+    w1, w2, mass = np.array(c["well1"]), np.array(c["well2"]), c["mass"]
+    pes0 = oracle.Pes(c["pes_id"], 3, 9, c["params"])
+    pes = oracle.Pes(c["pes_id"], 3, 9, c["params"], V0=pes0.V(w1))
+    betan, nd = beta / n, 27
+    k = np.arange(1, n + 1)
+    x = np.concatenate([((n - k) * w1[d] + (k - 1) * w2[d]) / (n - 1) for d in range(nd)])
+    vshift = min(0.0, min(pes.V(x.reshape(nd, n)[:, b]) for b in range(n)))
+    ld0 = oracle.logdet_band(oracle.UMhessian(pes, mass, n, betan, np.repeat(w1, n), singlewell=True), False)[0]
+    ld = oracle.logdet_band(oracle.UMhessian(pes, mass, n, betan, x), True)[0]
+    th, wth = oracle.gauleg(0.0, 1.0, npts)
+    ph, wph = oracle.gauleg(0.0, 0.5, npts)
+    q = 0
+    for ii in range(npts):
+        for jj in range(npts):
+            for kk in range(npts):
+                wr = w2.reshape(9, 3)
+                wr = align.rotate_atoms(wr, 1, th[kk])  # eta shares theta's range
+                wr = align.rotate_atoms(wr, 3, ph[jj])
+                wr = align.rotate_atoms(wr, 1, th[ii])
+                np.testing.assert_allclose(ends[q], wr.ravel(), rtol=0, atol=1e-13)
+                UM = oracle.UM(pes, mass, n, betan, x, w1, wr.ravel()) - n * vshift
+                S = betan * UM
+                om = betan * np.exp(-S) * np.sqrt(S / (2 * oracle.PI_REF)) / np.exp(0.5 * (ld - ld0))
+                ib = 1.0 if om * n > 1.0 else np.tanh(om * n)
+                np.testing.assert_allclose(rows[q, :3], [th[ii], ph[jj], th[kk]], rtol=1e-15)
+                assert rows[q, 3] == pytest.approx(wth[ii] * wph[jj] * wth[kk], rel=1e-14)
+                assert rows[q, 4] == pytest.approx(ib, rel=1e-8, abs=1e-300)
+                q += 1
