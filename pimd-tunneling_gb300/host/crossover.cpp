@@ -37,6 +37,7 @@ int main(int argc, char **argv) {
     const std::string pes = nl.str("pes", "1d");
     const std::string pesfile = nl.str("pes_params", "");
     const int quirks = (int)nl.integer("quirks", 0);
+    if (!nl.check(std::cerr)) return 1;
     if (parse_only) {
         std::printf("{\"ndim\": %d, \"natom\": %d, \"xunit\": %d, \"pes\": \"%s\", \"quirks\": %d}\n", ndim, natom,
                     xunit, pes.c_str(), quirks);

@@ -7,7 +7,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <fstream>
+#include <iostream>
 #include <map>
+#include <set>
 #include <sstream>
 #include <stdexcept>
 #include <string>
@@ -21,9 +23,14 @@ inline std::string lower(std::string s) {
 }
 
 // Key -> raw value text (lower-case keys, quotes stripped from strings).
+// Like a Fortran namelist read, a run stops on a key the program does not take
+// or a value that does not convert: the accessors record the keys they are
+// asked for and the values that fail, and check() reports both.
 class Namelist {
   public:
     std::map<std::string, std::string> kv;
+    mutable std::set<std::string> used;
+    mutable std::vector<std::string> errors;
 
     // Parses the first group named `group` ("&group ... /") from text.
     static Namelist parse(const std::string &text, const std::string &group) {
@@ -51,6 +58,7 @@ class Namelist {
                 continue;
             }
             if (c == '/') break;
+            if (c == '&' && lower(t.substr(i, 4)) == "&end") break;
             if (c == '!') {  // comment to end of line
                 while (i < t.size() && t[i] != '\n') i++;
                 body += ' ';
@@ -89,28 +97,59 @@ class Namelist {
     bool has(const std::string &k) const { return kv.count(lower(k)) > 0; }
 
     double real(const std::string &k, double def) const {
-        auto it = kv.find(lower(k));
+        auto it = find(k);
         if (it == kv.end()) return def;
         std::string v = it->second;
         for (auto &c : v)
             if (c == 'd' || c == 'D') c = 'e';  // Fortran double exponent
-        return std::strtod(v.c_str(), nullptr);
+        char *end = nullptr;
+        const double x = std::strtod(v.c_str(), &end);
+        if (v.empty() || end != v.c_str() + v.size()) {
+            errors.push_back("namelist: " + lower(k) + " = '" + it->second + "' is not a number");
+            return def;
+        }
+        return x;
     }
     long long integer(const std::string &k, long long def) const {
-        auto it = kv.find(lower(k));
+        auto it = find(k);
         if (it == kv.end()) return def;
         return (long long)real(k, (double)def);  // accepts 5e6-style integers
     }
     bool logical(const std::string &k, bool def) const {
-        auto it = kv.find(lower(k));
+        auto it = find(k);
         if (it == kv.end()) return def;
         std::string v = lower(it->second);
         if (v.size() && v[0] == '.') v = v.substr(1);
-        return !v.empty() && v[0] == 't';
+        if (v.empty() || (v[0] != 't' && v[0] != 'f')) {
+            errors.push_back("namelist: " + lower(k) + " = '" + it->second + "' is not a logical");
+            return def;
+        }
+        return v[0] == 't';
     }
     std::string str(const std::string &k, const std::string &def) const {
-        auto it = kv.find(lower(k));
+        auto it = find(k);
         return it == kv.end() ? def : it->second;
+    }
+    // Reference keys that have no effect in this program.
+    void accept(std::initializer_list<const char *> keys) const {
+        for (const char *k : keys) used.insert(lower(k));
+    }
+    // Reports unknown keys and unconvertible values on err; false if any.
+    bool check(std::ostream &err) const {
+        bool ok = errors.empty();
+        for (const auto &e : errors) err << e << "\n";
+        for (const auto &p : kv)
+            if (!used.count(p.first)) {
+                err << "namelist: unknown key '" << p.first << "'\n";
+                ok = false;
+            }
+        return ok;
+    }
+
+  private:
+    std::map<std::string, std::string>::const_iterator find(const std::string &k) const {
+        used.insert(lower(k));
+        return kv.find(lower(k));
     }
 };
 

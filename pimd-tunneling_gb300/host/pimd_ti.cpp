@@ -162,6 +162,8 @@ int main(int argc, char **argv) {
     const int64_t chunk = nl.integer("chunk", 5000);
     const std::string pesfile = nl.str("pes_params", "");
     const std::string tune = nl.str("tune", "");
+    nl.accept({"use_mkl", "basename"});  // pimd_par.f90:43-44: no effect here
+    if (!nl.check(std::cerr)) return 1;
     if (parse_only) {
         std::printf("{\"n\": %lld, \"beta\": %.17g, \"NMC\": %lld, \"Noutput\": %lld, \"dt\": %.17g, "
                     "\"nintegral\": %lld, \"nrep\": %lld, \"thermostat\": %d, \"ndim\": %d, \"natom\": %d, "

@@ -69,17 +69,23 @@ int main(int argc, char **argv) {
     const bool alignwell = nl.logical("alignwell", false);              // rpi_ser.f90:38
     const bool checkhess = nl.logical("checkhess", false);              // rpi_ser.f90:42
     const bool output_instanton = nl.logical("output_instanton", false);  // rpi_ser.f90:36
+    // the action with or without the end-point springs (rpi_ser.f90:39, 370-374);
+    // the angular grid always has them (rpi_ser.f90:53)
+    const bool fixedends = nl.logical("fixedends", true) || angular;
+    nl.accept({"alignpath", "basename"});  // rpi_ser.f90:23: no effect in the reference's flow
+    if (!nl.check(std::cerr)) return 1;
     const int atom1 = (int)nl.integer("atom1", 1), atom2 = (int)nl.integer("atom2", 2),
               atom3 = (int)nl.integer("atom3", 3);  // rpi_par.f90:53-55
     if (parse_only) {
         std::printf("{\"n\": %lld, \"beta\": %.17g, \"ndim\": %d, \"natom\": %d, \"xunit\": %d, \"npath\": %lld, "
                     "\"readpath\": %s, \"pes\": \"%s\", \"m\": %d, \"pgtol\": %.17g, \"factr\": %.17g, "
                     "\"maxiter\": %lld, \"quirks\": %d, \"angular\": %s, \"npoints\": %lld, \"alignwell\": %s, "
-                    "\"atom1\": %d, \"atom2\": %d, \"atom3\": %d, \"checkhess\": %s, \"output_instanton\": %s}\n",
+                    "\"atom1\": %d, \"atom2\": %d, \"atom3\": %d, \"checkhess\": %s, \"output_instanton\": %s, "
+                    "\"fixedends\": %s}\n",
                     (long long)n, beta, ndim, natom, xunit, (long long)npath, readpath ? "true" : "false",
                     pes.c_str(), m, pgtol, factr, (long long)maxiter, quirks, angular ? "true" : "false",
                     (long long)npoints, alignwell ? "true" : "false", atom1, atom2, atom3,
-                    checkhess ? "true" : "false", output_instanton ? "true" : "false");
+                    checkhess ? "true" : "false", output_instanton ? "true" : "false", fixedends ? "true" : "false");
         return 0;
     }
     auto t0 = std::chrono::steady_clock::now();
@@ -243,6 +249,14 @@ int main(int argc, char **argv) {
         std::fclose(fe);
     }
     UM -= (double)n * vshift;
+    if (!fixedends) {  // S from UM(xtilde) without the end-point springs (instantonmod.f90:17-46)
+        double e = 0.0;
+        for (int k = 0; k < nd; k++) {
+            const double d1 = x[(size_t)k * n] - w1[k], d2 = w2[k] - x[(size_t)k * n + n - 1];
+            e += mass[k / ndim] * (d1 * d1 + d2 * d2);
+        }
+        UM -= e / (2.0 * betan * betan);
+    }
     std::vector<double> xharm((size_t)nd * n);
     for (int k = 0; k < nd; k++)
         for (int64_t bead = 0; bead < n; bead++) xharm[(size_t)k * n + bead] = w1[k];

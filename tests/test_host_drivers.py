@@ -63,6 +63,28 @@ def test_rpidata_namelist_parsing(drivers_built):
     assert d["checkhess"] is False and d["output_instanton"] is False and d["alignwell"] is False
 
 
+def test_namelist_errors_stop_the_run(drivers_built):
+    """As a Fortran namelist read does: an unknown key or a value that does not
+    convert stops the program before any work; '&end' also closes a group, and
+    the reference keys without effect here are accepted."""
+    r = _run("pimd_ti", "&MCDATA n=8, NMCC=100 /", args=["--parse-only"])
+    assert r.returncode == 1 and "unknown key 'nmcc'" in r.stderr
+    r = _run("pimd_ti", "&MCDATA n=8, beta=1.0x /", args=["--parse-only"])
+    assert r.returncode == 1 and "beta" in r.stderr and "not a number" in r.stderr
+    r = _run("pimd_ti", "&MCDATA cayley=yes /", args=["--parse-only"])
+    assert r.returncode == 1 and "not a logical" in r.stderr
+    r = _run("pimd_ti", "&MCDATA n=12, use_mkl=.false., basename='w' &end", args=["--parse-only"])
+    assert r.returncode == 0, r.stderr
+    assert json.loads(r.stdout)["n"] == 12
+    r = _run("rpi", "&RPIDATA n=12, alignpath=.true., fixedends=.false. /", args=["--parse-only"])
+    assert r.returncode == 0, r.stderr
+    assert json.loads(r.stdout)["fixedends"] is False
+    r = _run("rpi", "&RPIDATA fixedends=.false., angular=.true. /", args=["--parse-only"])
+    assert json.loads(r.stdout)["fixedends"] is True  # rpi_ser.f90:53
+    r = _run("crossover", "&CROSSDATA ndim=2, natom=1, nmc=3 /", args=["--parse-only"])
+    assert r.returncode == 1 and "unknown key 'nmc'" in r.stderr
+
+
 def test_driver_fails_loudly_without_gpu(drivers_built, tmp_path):
     import torch
     if torch.cuda.is_available():
@@ -316,6 +338,12 @@ def test_rpi_driver_host_logic_on_the_oracle(oracle, tmp_path):
     np.testing.assert_allclose(np.loadtxt(str(tmp_path / "hessian_well1.dat")), H, rtol=1e-14)
     modes = re.search(r"normal modes:\n\s*1\s+(\S+)\n\s*2\s+(\S+)\n", r.stdout).groups()
     np.testing.assert_allclose(np.array(modes, float), np.linalg.eigvalsh(H / mass[0]) * 219475.0, rtol=1e-10)
+    # fixedends = F: the action without the end-point springs (rpi_ser.f90:370-374)
+    r = subprocess.run([exe], input=text.replace("checkhess=.true.", "fixedends=.false."), capture_output=True,
+                       text=True, cwd=str(tmp_path), timeout=120)
+    assert r.returncode == 0, r.stderr
+    UMf = oracle.UM(pes, mass, n, betan, x, w1, w2, fixedends=False) - n * vmin
+    assert float(re.search(r"s_kink=\s*(\S+)", r.stdout).group(1)) == pytest.approx(betan * UMf, rel=1e-12)
 
 
 def _oracle_ti(oracle, c, nmc, nm_resident=True):
