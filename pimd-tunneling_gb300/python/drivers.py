@@ -227,7 +227,7 @@ def linear_guess(w1, w2, N):
 
 
 def run_rpi(cfg, N=None, betas=None, m=8, factr=1.0e6, pgtol=1.0e-5, maxiter=200000, quirks=False,
-            device=0, ctx=None):
+            device=0, ctx=None, fixedends=True):
     c = dict(cfg)
     N = int(N if N is not None else c["N"])
     betas = np.asarray(betas if betas is not None else c["betas"], dtype=float)
@@ -251,6 +251,11 @@ def run_rpi(cfg, N=None, betas=None, m=8, factr=1.0e6, pgtol=1.0e-5, maxiter=200
         vpath = ctx.pes_eval(beads)[0].reshape(nb, N)
         vshift = np.minimum(vpath.min(axis=1), 0.0)
         UM = np.asarray(UM) - N * vshift
+        if not fixedends:  # S from UM(xtilde) without the end-point springs (rpi_ser.f90:370-374)
+            xb = np.asarray(x).reshape(nb, nd, N)
+            mdof = np.repeat(np.asarray(c["mass"], float), c["ndim"])
+            ends = ((xb[:, :, 0] - w1) ** 2 + (np.tile(w2, (nb, 1)) - xb[:, :, -1]) ** 2) @ mdof
+            UM = UM - ends / (2.0 * betan ** 2)
         xharm = np.concatenate([np.repeat(w1, N) for _ in range(nb)])
         t0 = time.perf_counter()
         ld0, _, _ = ctx.instanton_logdet(N, xharm, betan, singlewell=True, skip_lowest=False, quirks=quirks)
