@@ -54,7 +54,9 @@ class TiInputs:
             self.xref = np.array(xr)
         nr = self.nint * self.nrep
         self.ring_lambda = np.repeat(np.arange(self.nint, dtype=np.int32), self.nrep)
-        seeds = cfg.get("seeds", list(range(self.nrep)))
+        seeds = list(cfg.get("seeds", []))
+        if len(seeds) < self.nrep:  # one key per replica: the base seed + j, as the namelist driver does
+            seeds = [(seeds[0] if seeds else 0) + j for j in range(self.nrep)]
         self.ring_seed = np.array([seeds[j % len(seeds)] for _ in range(self.nint) for j in range(self.nrep)],
                                   dtype=np.uint64)
         self.ring_stream = self.ring_lambda.astype(np.uint32)

@@ -12,6 +12,7 @@
 // batch runs the oracle's ring propagation (the reference step order for
 // PG_FORM_PLAIN, the normal-mode-resident order otherwise); no checkpoint
 // file is written, so restarts read the restart_proc files.
+#include <chrono>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -264,5 +265,64 @@ int pg_ti_assemble(int64_t nintegral, const double *weights, const double *mean,
     *qratio = std::exp(-d * betan);
     return PG_OK;
 }
+
+int pg_ti_advance_timed(pg_ctx *c, int64_t nsteps, double *ms) {  // host wall time
+    const auto t0 = std::chrono::steady_clock::now();
+    const int rc = pg_ti_advance(c, nsteps);
+    if (ms) *ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return rc;
+}
+int pg_ti_get_form(pg_ctx *c, int64_t, int32_t *form, int64_t *launches) {
+    if (form) *form = c->ti.prm.nm_resident ? PG_FORM_FUSED : PG_FORM_PLAIN;
+    if (launches) *launches = 1;
+    return PG_OK;
+}
+int pg_ti_release(pg_ctx *c) {
+    c->ti = TiBatch();
+    return PG_OK;
+}
+int32_t pg_version(void) { return 0; }
+int pg_instanton_fg(pg_ctx *c, int64_t nbeta, int64_t N, const double *x, const double *a, const double *b,
+                    const double *betan, double *UM, double *grad) {
+    const int64_t nd = ndof(c);
+    std::vector<double> g((size_t)nd * N);
+    for (int64_t k = 0; k < nbeta; k++) {
+        const double u = or_UMforceenergy(&c->pes, c->mass.data(), N, betan[k], x + k * nd * N, a, b + k * nd, 1,
+                                          g.data());
+        if (UM) UM[k] = u;
+        if (grad) std::copy(g.begin(), g.end(), grad + k * nd * N);
+    }
+    return PG_OK;
+}
+int pg_splitting_two_beta(double beta1, double ratio1, double beta2, double ratio2, double *delta,
+                          double *betabar) {
+    const double y1 = std::atanh(ratio1), y2 = std::atanh(ratio2);
+    *delta = 2.0 * (y2 - y1) / (beta2 - beta1);
+    if (betabar) *betabar = y2 != y1 ? (beta1 * y2 - beta2 * y1) / (y2 - y1) : std::nan("");
+    return PG_OK;
+}
+int pg_irrep_ratios(int64_t nirrep, int64_t nop, const double *chars, const double *rho, double *ratio) {
+    for (int64_t i = 0; i < nirrep; i++) {
+        double em = 0.0, ep = 0.0;
+        for (int64_t g = 0; g < nop; g++) {
+            em += (1.0 - chars[i * nop + g]) * rho[g];
+            ep += (1.0 + chars[i * nop + g]) * rho[g];
+        }
+        ratio[i] = em / ep;
+    }
+    return PG_OK;
+}
+// not in the stand-in
+int pg_nm_transform(pg_ctx *, int64_t, int64_t, const double *, double *, int32_t) { return PG_ERR_ARG; }
+int pg_nm_transform_noalloc(int64_t, int64_t, const double *, double *, void *) { return PG_ERR_ARG; }
+int pg_propagate_pimd(pg_ctx *, const pg_ti_config *, int64_t, int64_t, const double *, const double *,
+                      const double *, const uint64_t *, const uint32_t *, double *, double *, double *, int32_t *) {
+    return PG_ERR_ARG;
+}
+int pg_ti_advance_group(pg_ctx *const *, int64_t, int64_t, double *) { return PG_ERR_ARG; }
+int pg_ti_kernel_times(pg_ctx *, int64_t, int32_t *, double *, int64_t *, double *, const char **) {
+    return PG_ERR_ARG;
+}
+int pg_ti_get_tuning(pg_ctx *, int32_t *, int32_t *, int32_t *) { return PG_ERR_ARG; }
 
 }  // extern "C"

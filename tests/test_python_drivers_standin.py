@@ -1,0 +1,124 @@
+"""The Python drivers' host logic on the CPU (python/drivers.py): each runs in a
+subprocess whose binding loads the oracle-backed stand-in for the C-ABI
+(tests/standin) in place of libpimdgpu, and its results are checked against
+the oracle here.  The stand-in's optimiser returns the start path, so the RPI
+checks cover what the driver does around the optimisation: the V0 move, the
+end-point springs, the log-dets and the assembly."""
+import json
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+import pgconfigs
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+SCRIPT = r'''
+import json, sys
+sys.path[:0] = [%(py)r, %(pkg)r]
+import numpy as np
+import pimdgpu as pg
+pg.LIBPATH = %(so)r
+import drivers, pgconfigs
+job = json.loads(sys.stdin.read())
+out = {}
+if job["kind"] == "rpi":
+    c = dict(pgconfigs.load("c1"), well1=job["w1"], well2=job["w2"], V0=job["V0"])
+    for fe in (True, False):
+        r = drivers.run_rpi(c, N=job["N"], betas=job["betas"], fixedends=fe)
+        out[str(fe)] = dict(S=[q["S"] for q in r["results"]], delta=[q["delta"] for q in r["results"]],
+                            vpath=r["vpath"].tolist())
+elif job["kind"] == "ti":
+    c = dict(pgconfigs.load("c0"), imin=50)
+    r = drivers.run_ti(c, precision=pg.PG_FP64, form=pg.PG_FORM_FUSED, nmc=job["nmc"], nrep=2)
+    out = dict(dA=r["dA"], qratio=r["qratio"], delta=r["delta"], mean=r["integrand_mean"])
+elif job["kind"] == "crossover":
+    c = pgconfigs.load("c1")
+    ctx = pg.Context(0)
+    ctx.set_system(2, 1, c["mass"], c["pes_id"], c["params"], c["V0"])
+    b, eta = drivers.crossover_beta(ctx, c["ts"], c["mass"])
+    ctx.close()
+    out = dict(beta_c=b, eta2=list(eta))
+print(json.dumps(out))
+'''
+
+
+@pytest.fixture(scope="module")
+def run_job(oracle, tmp_path_factory):
+    import standin
+    so = standin.build_library(tmp_path_factory.mktemp("standin_so"))
+    src = SCRIPT % dict(py=os.path.join(ROOT, "pimd-tunneling_gb300", "python"),
+                        pkg=os.path.join(ROOT, "pimd-tunneling_gb300"), so=so)
+
+    def run(job):
+        r = subprocess.run([sys.executable, "-c", src], input=json.dumps(job), capture_output=True, text=True,
+                           timeout=300)
+        assert r.returncode == 0, r.stderr
+        return json.loads(r.stdout.strip().split("\n")[-1])
+
+    return run
+
+
+def test_run_rpi_host_logic(oracle, run_job):
+    c = pgconfigs.load("c1")
+    m1, m2 = np.array(c["well1"]), np.array(c["well2"])
+    u = (m1 - m2) / np.linalg.norm(m1 - m2)
+    w1, w2 = m1 + 0.3 * u, m2  # the straight start path passes below well 1
+    N, betas = 8, [c["beta"] / 16, c["beta"] / 12]
+    v0 = oracle.Pes(c["pes_id"], 2, 1, c["params"]).V(w1)  # V0 = V(well 1), rpi_ser.f90:95
+    out = run_job(dict(kind="rpi", w1=list(w1), w2=list(w2), V0=v0, N=N, betas=betas))
+    pes = oracle.Pes(c["pes_id"], 2, 1, c["params"], V0=v0)
+    mass = c["mass"]
+    k = np.arange(1, N + 1)
+    x = np.concatenate([((N - k) * w1[d] + (k - 1) * w2[d]) / (N - 1) for d in range(2)])
+    vpath = np.array([pes.V(x.reshape(2, N)[:, b]) for b in range(N)])
+    vmin = min(vpath.min(), 0.0)
+    assert vmin < 0
+    for fe in (True, False):
+        got = out[str(fe)]
+        for i, beta in enumerate(betas):
+            betan = beta / N  # rpi_ser.f90:45
+            np.testing.assert_allclose(got["vpath"][i], vpath, rtol=1e-13, atol=1e-15)
+            UM = oracle.UM(pes, mass, N, betan, x, w1, w2, fixedends=fe) - N * vmin
+            ld0 = oracle.logdet_band(oracle.UMhessian(pes, mass, N, betan, np.repeat(w1, N), singlewell=True),
+                                     False)[0]
+            ld = oracle.logdet_band(oracle.UMhessian(pes, mass, N, betan, x), True)[0]
+            S = betan * UM
+            om = betan * np.exp(-S) * np.sqrt(S / (2 * oracle.PI_REF)) / np.exp(0.5 * (ld - ld0))
+            assert got["S"][i] == pytest.approx(S, rel=1e-12)
+            assert got["delta"][i] == pytest.approx(2 * om / betan, rel=1e-8)
+
+
+def test_run_ti_host_logic(oracle, run_job):
+    out = run_job(dict(kind="ti", nmc=300))
+    c = dict(pgconfigs.load("c0"), imin=50, nrep=2, seeds=[0, 1])
+    ti = pgconfigs.TiInputs(c, gauleg=oracle.gauleg)
+    pes = oracle.Pes(c["pes_id"], c["ndim"], c["natom"], c["params"])
+    prm = oracle.TiParams(ti.P, c["beta"], c["dt"], tau=c["tau"], gamma=c["gamma"], thermostat=2,
+                          nm_resident=True, imin=c["imin"], init_sigma=c["init_sigma"])
+    ints = np.zeros(ti.nrings)
+    for r in range(ti.nrings):
+        li = int(ti.ring_lambda[r])
+        x, p = oracle.ring_init(pes, c["mass"], prm, ti.xref[li], int(ti.ring_seed[r]), int(ti.ring_stream[r]),
+                                a=ti.a, b=ti.b[li])
+        res = oracle.ring_propagate(pes, c["mass"], prm, ti.a, ti.b[li], ti.dbdl[li], ti.xref[li],
+                                    int(ti.ring_seed[r]), int(ti.ring_stream[r]), 0, 300, x, p)
+        ints[r] = res.dhdr_sum / res.nsamples / ti.betan ** 2
+    mean = np.array([ints[ti.ring_lambda == i].mean() for i in range(ti.nint)])
+    np.testing.assert_allclose(out["mean"], mean, rtol=1e-12)
+    dA = float(np.dot(ti.w, mean))
+    assert out["dA"] == pytest.approx(dA, rel=1e-12)
+    q = np.exp(-dA * ti.betan)  # pimd_par.f90:420
+    assert out["qratio"] == pytest.approx(q, rel=1e-12)
+    assert out["delta"] == pytest.approx(2.0 * np.arctanh(q) / c["beta"], rel=1e-10)
+
+
+def test_crossover_beta_host_logic(oracle, run_job):
+    out = run_job(dict(kind="crossover"))
+    c = pgconfigs.load("c1")
+    b, eta = oracle.crossover_beta(oracle.Pes(c["pes_id"], 2, 1, c["params"]), c["mass"], c["ts"])
+    assert out["beta_c"] == pytest.approx(b, rel=1e-12)
+    np.testing.assert_allclose(out["eta2"], eta, rtol=1e-12)
