@@ -319,7 +319,13 @@ int pg_propagate_pimd(pg_ctx *, const pg_ti_config *, int64_t, int64_t, const do
                       const double *, const uint64_t *, const uint32_t *, double *, double *, double *, int32_t *) {
     return PG_ERR_ARG;
 }
-int pg_ti_advance_group(pg_ctx *const *, int64_t, int64_t, double *) { return PG_ERR_ARG; }
+int pg_ti_advance_group(pg_ctx *const *ctxs, int64_t nctx, int64_t nsteps, double *ms) {  // one after another
+    const auto t0 = std::chrono::steady_clock::now();
+    for (int64_t i = 0; i < nctx; i++)
+        if (int rc = pg_ti_advance(ctxs[i], nsteps)) return rc;
+    if (ms) *ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return PG_OK;
+}
 int pg_ti_kernel_times(pg_ctx *, int64_t, int32_t *, double *, int64_t *, double *, const char **) {
     return PG_ERR_ARG;
 }

@@ -35,6 +35,10 @@ elif job["kind"] == "ti":
     c = dict(pgconfigs.load("c0"), imin=50)
     r = drivers.run_ti(c, precision=pg.PG_FP64, form=pg.PG_FORM_FUSED, nmc=job["nmc"], nrep=2)
     out = dict(dA=r["dA"], qratio=r["qratio"], delta=r["delta"], mean=r["integrand_mean"])
+elif job["kind"] == "ti_mixed":
+    c = dict(pgconfigs.load("c0"), imin=20, nintegral=2, P_per_ring=job["P_per_ring"])
+    r = drivers.run_ti_mixed(c, precision=pg.PG_FP64, form=pg.PG_FORM_FUSED, nmc=job["nmc"], chunk=50)
+    out = dict(per_P=[dict(P=q["P"], dA=q["dA"], nrings=q["nrings"]) for q in r["per_P"]])
 elif job["kind"] == "crossover":
     c = pgconfigs.load("c1")
     ctx = pg.Context(0)
@@ -122,3 +126,28 @@ def test_crossover_beta_host_logic(oracle, run_job):
     b, eta = oracle.crossover_beta(oracle.Pes(c["pes_id"], 2, 1, c["params"]), c["mass"], c["ts"])
     assert out["beta_c"] == pytest.approx(b, rel=1e-12)
     np.testing.assert_allclose(out["eta2"], eta, rtol=1e-12)
+
+
+def test_run_ti_mixed_host_logic(oracle, run_job):
+    """run_ti_mixed: one batch per bead number, advanced together; Delta A per P
+    from the rings of that P, each against the oracle ring by ring."""
+    Pr = [8, 16, 8, 16]  # 2 lambda points x 2 replicas, ring r = point * nrep + replica
+    out = run_job(dict(kind="ti_mixed", P_per_ring=Pr, nmc=120))
+    c = dict(pgconfigs.load("c0"), imin=20, nintegral=2)
+    pes = oracle.Pes(c["pes_id"], c["ndim"], c["natom"], c["params"])
+    got = {q["P"]: q for q in out["per_P"]}
+    assert sorted(got) == [8, 16] and all(q["nrings"] == 2 for q in got.values())
+    for P in (8, 16):
+        ti = pgconfigs.TiInputs(dict(c, P=P), nrep=2, nintegral=2, P=P, gauleg=oracle.gauleg)
+        prm = oracle.TiParams(P, c["beta"], c["dt"], tau=c["tau"], gamma=c["gamma"], thermostat=2,
+                              nm_resident=True, imin=c["imin"], init_sigma=c["init_sigma"])
+        ints = {}
+        for r in [i for i, p in enumerate(Pr) if p == P]:
+            li = int(ti.ring_lambda[r])
+            x, p = oracle.ring_init(pes, c["mass"], prm, ti.xref[li], int(ti.ring_seed[r]),
+                                    int(ti.ring_stream[r]), a=ti.a, b=ti.b[li])
+            res = oracle.ring_propagate(pes, c["mass"], prm, ti.a, ti.b[li], ti.dbdl[li], ti.xref[li],
+                                        int(ti.ring_seed[r]), int(ti.ring_stream[r]), 0, 120, x, p)
+            ints.setdefault(li, []).append(res.dhdr_sum / res.nsamples / ti.betan ** 2)
+        dA = sum(ti.w[li] * np.mean(v) for li, v in ints.items())
+        assert got[P]["dA"] == pytest.approx(dA, rel=1e-12)
