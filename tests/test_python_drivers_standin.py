@@ -39,6 +39,10 @@ elif job["kind"] == "ti_mixed":
     c = dict(pgconfigs.load("c0"), imin=20, nintegral=2, P_per_ring=job["P_per_ring"])
     r = drivers.run_ti_mixed(c, precision=pg.PG_FP64, form=pg.PG_FORM_FUSED, nmc=job["nmc"], chunk=50)
     out = dict(per_P=[dict(P=q["P"], dA=q["dA"], nrings=q["nrings"]) for q in r["per_P"]])
+elif job["kind"] == "ti_readhess":
+    c = dict(pgconfigs.load("c1"), P=8, imin=0)
+    r = drivers.run_ti(c, precision=pg.PG_FP64, form=pg.PG_FORM_FUSED, nmc=4, nrep=2, nintegral=2, readhess=True)
+    out = dict(dA=r["dA"])
 elif job["kind"] == "crossover":
     c = pgconfigs.load("c1")
     ctx = pg.Context(0)
@@ -57,9 +61,9 @@ def run_job(oracle, tmp_path_factory):
     src = SCRIPT % dict(py=os.path.join(ROOT, "pimd-tunneling_gb300", "python"),
                         pkg=os.path.join(ROOT, "pimd-tunneling_gb300"), so=so)
 
-    def run(job):
+    def run(job, env=None):
         r = subprocess.run([sys.executable, "-c", src], input=json.dumps(job), capture_output=True, text=True,
-                           timeout=300)
+                           timeout=300, env=dict(os.environ, **(env or {})))
         assert r.returncode == 0, r.stderr
         return json.loads(r.stdout.strip().split("\n")[-1])
 
@@ -151,3 +155,25 @@ def test_run_ti_mixed_host_logic(oracle, run_job):
             ints.setdefault(li, []).append(res.dhdr_sum / res.nsamples / ti.betan ** 2)
         dA = sum(ti.w[li] * np.mean(v) for li, v in ints.items())
         assert got[P]["dA"] == pytest.approx(dA, rel=1e-12)
+
+
+def test_run_ti_readhess_host_logic(oracle, run_job, tmp_path):
+    """run_ti(readhess=True): the start positions handed to the batch are the
+    path beads of each ring's lambda point plus the readhess displacements of
+    the polymer Hessian there (pg_um_hessian, singlewell false, betan =
+    beta/(P+1)) with normals from the ring's own Philox stream."""
+    import drivers
+    out = run_job(dict(kind="ti_readhess"), env=dict(PG_STANDIN_X0=str(tmp_path / "x0.txt")))
+    assert np.isfinite(out["dA"])
+    c = dict(pgconfigs.load("c1"), P=8, imin=0)
+    ti = pgconfigs.TiInputs(c, nrep=2, nintegral=2, gauleg=oracle.gauleg)
+    pes = oracle.Pes(c["pes_id"], 2, 1, c["params"], V0=c["V0"])
+    x0 = np.loadtxt(str(tmp_path / "x0.txt")).reshape(ti.nrings, -1)
+    for r in range(ti.nrings):
+        li = int(ti.ring_lambda[r])
+        band = oracle.UMhessian(pes, c["mass"], ti.P, ti.betan, ti.xref[li])
+        z = np.random.Generator(np.random.Philox(key=int(ti.ring_seed[r]), counter=[int(ti.ring_stream[r]), 49, 0,
+                                                                                      0])).standard_normal(2 * ti.P)
+        dx = drivers.readhess_displacements(band, ti.P, 2, 1, c["mass"], c["beta"], z[None, :])[0]
+        np.testing.assert_allclose(x0[r], ti.xref[li] + dx, rtol=0, atol=1e-12)
+    assert not np.allclose(x0[0], x0[1])
