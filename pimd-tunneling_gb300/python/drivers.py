@@ -9,8 +9,9 @@ run_ti_mixed -- a task list whose rings have different bead numbers P (one
             context per P, all advanced together by pg_ti_advance_group on
             concurrent streams); TI is assembled per P, since betan = beta/(P+1)
             and the estimate itself depend on P.
-run_rpi  -- rpi_ser.f90:157-190, 222-237, 354-381 for a batch of beta values:
-            linear-interpolation guess, instanton by on-device L-BFGS (V0 moved
+run_rpi  -- rpi_ser.f90:133-190, 222-237, 354-381 for a batch of beta values:
+            linear-interpolation or path.xyz spline guess (path=frames),
+            instanton by on-device L-BFGS (V0 moved
             to the lowest bead when one lies below well 1), log-det at
             the wells (single well, all eigenvalues) and at the instanton
             (lowest eigenvalue dropped), S = betan UM, Omega and Delta.
@@ -220,6 +221,27 @@ def multiwell_levels(chars, rho1, rho2, beta1, beta2):
     return np.array([d for d, _ in out]), np.array([b for _, b in out]), I1, I2
 
 
+def path_guess(frames, N, ndim=None, natom=None, atoms=(1, 2, 3)):
+    """Start path from the frames of path.xyz (read_path, instantonmod.f90:916-950;
+    rpi_ser.f90:133-146): three-dimensional frames aligned by the angles of the
+    first (instantonmod.f90:926-932), normalised arc length between frames, a
+    natural cubic spline per dof and N beads at (k-1)/(N-1).  frames: (npath, nd)
+    arrays x[atom*ndim + dim]; returns the path x[dof*N + bead]."""
+    import align
+    fr = [np.asarray(f, dtype=float) for f in frames]
+    if ndim is not None and natom is not None and align.supported(ndim, natom, atoms):
+        fr = align.align_frames(fr, atoms)
+    fr = np.array(fr)
+    lam = np.concatenate([[0.0], np.cumsum(np.linalg.norm(np.diff(fr, axis=0), axis=1))])
+    lam /= lam[-1]
+    t = np.arange(N) / (N - 1)
+    out = []
+    for d in range(fr.shape[1]):
+        y2 = pg.spline(lam, fr[:, d])
+        out.append([pg.splint(lam, fr[:, d], y2, v)[0] for v in t])
+    return np.concatenate(out)
+
+
 def linear_guess(w1, w2, N):
     """rpi_ser.f90:157-163."""
     k = np.arange(1, N + 1)
@@ -227,7 +249,7 @@ def linear_guess(w1, w2, N):
 
 
 def run_rpi(cfg, N=None, betas=None, m=8, factr=1.0e6, pgtol=1.0e-5, maxiter=200000, quirks=False,
-            device=0, ctx=None, fixedends=True):
+            device=0, ctx=None, fixedends=True, path=None):
     c = dict(cfg)
     N = int(N if N is not None else c["N"])
     betas = np.asarray(betas if betas is not None else c["betas"], dtype=float)
@@ -240,7 +262,9 @@ def run_rpi(cfg, N=None, betas=None, m=8, factr=1.0e6, pgtol=1.0e-5, maxiter=200
         ctx = pg.Context(device)
     try:
         ctx.set_system(c["ndim"], c["natom"], c["mass"], c["pes_id"], c["params"], c["V0"])
-        x0 = np.concatenate([linear_guess(w1, w2, N) for _ in range(nb)])
+        guess = (linear_guess(w1, w2, N) if path is None
+                 else path_guess(path, N, c["ndim"], c["natom"]))  # rpi_ser.f90:133-163
+        x0 = np.concatenate([guess for _ in range(nb)])
         t0 = time.perf_counter()
         x, UM, it, st = ctx.instanton_optimize(N, x0, w1, np.tile(w2, nb), betan, m=m, factr=factr, pgtol=pgtol,
                                                maxiter=maxiter)

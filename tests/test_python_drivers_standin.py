@@ -43,6 +43,10 @@ elif job["kind"] == "ti_readhess":
     c = dict(pgconfigs.load("c1"), P=8, imin=0)
     r = drivers.run_ti(c, precision=pg.PG_FP64, form=pg.PG_FORM_FUSED, nmc=4, nrep=2, nintegral=2, readhess=True)
     out = dict(dA=r["dA"])
+elif job["kind"] == "rpi_path":
+    c = pgconfigs.load("c3")
+    r = drivers.run_rpi(c, N=job["N"], betas=job["betas"], path=[np.array(f) for f in job["frames"]])
+    out = dict(S=[q["S"] for q in r["results"]], x=np.asarray(r["x"]).tolist())
 elif job["kind"] == "crossover":
     c = pgconfigs.load("c1")
     ctx = pg.Context(0)
@@ -177,3 +181,27 @@ def test_run_ti_readhess_host_logic(oracle, run_job, tmp_path):
         dx = drivers.readhess_displacements(band, ti.P, 2, 1, c["mass"], c["beta"], z[None, :])[0]
         np.testing.assert_allclose(x0[r], ti.xref[li] + dx, rtol=0, atol=1e-12)
     assert not np.allclose(x0[0], x0[1])
+
+
+def test_run_rpi_path_guess_host_logic(oracle, run_job):
+    """run_rpi(path=frames): the frames of a 3-D system aligned by the first
+    frame's angles, splined against normalised arc length, N beads at
+    (k-1)/(N-1) (instantonmod.f90:916-950, rpi_ser.f90:133-146)."""
+    import align
+    c = pgconfigs.load("c3")
+    w1, w2 = np.array(c["well1"]), np.array(c["well2"])
+    rng = np.random.default_rng(9)
+    frames = [w1, 0.5 * (w1 + w2) + 0.05 * rng.normal(size=27), w2]
+    N, betas = 6, [c["betas"][3]]
+    out = run_job(dict(kind="rpi_path", frames=[list(f) for f in frames], N=N, betas=betas))
+    fr = np.array(align.align_frames(frames))
+    lam = np.concatenate([[0.0], np.cumsum(np.linalg.norm(np.diff(fr, axis=0), axis=1))])
+    lam /= lam[-1]
+    x = np.concatenate([[oracle.splint(lam, fr[:, d], oracle.spline(lam, fr[:, d]), t)
+                         for t in np.arange(N) / (N - 1)] for d in range(27)])
+    np.testing.assert_allclose(out["x"], x, rtol=0, atol=1e-12)
+    pes = oracle.Pes(c["pes_id"], 3, 9, c["params"], V0=c["V0"])
+    vmin = min(0.0, min(pes.V(x.reshape(27, N)[:, b]) for b in range(N)))
+    betan = betas[0] / N
+    S = betan * (oracle.UM(pes, c["mass"], N, betan, x, w1, w2) - N * vmin)
+    assert out["S"][0] == pytest.approx(S, rel=1e-12)
