@@ -85,20 +85,100 @@ def readhess_start(ctx, c, ti, quirks=False):
     return x0.ravel()
 
 
+def _arc_length(frames):
+    lam = np.concatenate([[0.0], np.cumsum(np.linalg.norm(np.diff(frames, axis=0), axis=1))])
+    return lam / lam[-1]
+
+
+def _bisect_top(dv, x1=0.3, x2=0.7, xacc=1.0e-6, jmax=40):
+    """findmiddle (instantonmod.f90:832-871): bisection for the zero of dV/dlambda."""
+    f1, f2 = dv(x1), dv(x2)
+    if f1 * f2 >= 0.0:
+        raise ValueError("centre: the barrier top is not bracketed in (%g, %g)" % (x1, x2))
+    xm, dx = (x1, x2 - x1) if f1 < 0.0 else (x2, x1 - x2)
+    for _ in range(jmax):
+        dx *= 0.5
+        xmid = xm + dx
+        fm = dv(xmid)
+        if fm <= 0.0:
+            xm = xmid
+        if abs(dx) < xacc or fm == 0.0:
+            break
+    return xm
+
+
+def ti_path_inputs(ctx, c, ti, frames, instapath=False, centre=False, init="path"):
+    """The read_path flow of pimd_par (instantonmod.f90:895-1004, pimd_par.f90:212-221)
+    for the batch ti (modified in place): the frames of path.xyz (3-D frames
+    aligned by the first frame's angles) splined against normalised arc length;
+    with instapath the instanton of that path guess (n = P beads at
+    (k-1)/(n-1), fixed ends at the wells, the driver's betan) replaces it as
+    [well 1, beads, well 2]; with centre the arc length is remapped so that the
+    barrier top of V along the path sits at 1/2.  Then a = path(0), b_i =
+    path(xi_i), dbdl_i = path'(xi_i) and the start beads at
+    xi_eff = (k-1) xi_i / (P-1) (init 'path', verletmodule.f90:40-48) or at
+    well 1 ('well').  Returns the centring's barrier top (or None)."""
+    import align
+    nd, P = ti.nd, ti.P
+    w1, w2 = np.asarray(c["well1"], float), np.asarray(c["well2"], float)
+    fr = [np.asarray(f, dtype=float) for f in frames]
+    if align.supported(c["ndim"], c["natom"]):
+        fr = align.align_frames(fr)
+    fr = np.array(fr)
+    lam = _arc_length(fr)
+
+    def splines(lam, fr):
+        return [pg.spline(lam, fr[:, d]) for d in range(nd)]
+
+    if instapath:
+        y2 = splines(lam, fr)
+        t = np.arange(P) / (P - 1)
+        xt = np.concatenate([[pg.splint(lam, fr[:, d], y2[d], v)[0] for v in t] for d in range(nd)])
+        x, _, _, _ = ctx.instanton_optimize(P, xt, w1, w2, [ti.betan], m=8, factr=1.0e6, pgtol=1.0e-5,
+                                            maxiter=200000)
+        fr = np.vstack([w1, np.asarray(x).reshape(nd, P).T, w2])
+        lam = _arc_length(fr)
+    xm = None
+    if centre:
+        V = ctx.pes_eval(fr)[0]
+        v2 = pg.spline(lam, V)
+        xm = _bisect_top(lambda l: pg.splint(lam, V, v2, l)[1])
+        ca, cb = 2.0 - 4.0 * xm, 4.0 * xm - 1.0  # instantonmod.f90:993-1004
+        lam = 2.0 * lam / (cb + np.sqrt(cb * cb + 4.0 * ca * lam))
+    y2 = splines(lam, fr)
+
+    def at(v, d):
+        return pg.splint(lam, fr[:, d], y2[d], v)
+
+    ti.a = np.array([at(0.0, d)[0] for d in range(nd)])
+    ti.b = np.array([[at(x, d)[0] for d in range(nd)] for x in ti.xi])
+    ti.dbdl = np.array([[at(x, d)[1] for d in range(nd)] for x in ti.xi])
+    if init == "path":
+        ti.xref = np.array([np.concatenate([[at(k * x / (P - 1), d)[0] for k in range(P)] for d in range(nd)])
+                            for x in ti.xi])
+    else:
+        ti.xref = np.array([np.repeat(w1, P) for _ in ti.xi])
+    return xm
+
+
 def run_ti(cfg, precision=pg.PG_MIXED, form=pg.PG_FORM_AUTO, nmc=None, nrep=None, nintegral=None,
-           seed_offset=0, chunk=2000, device=0, ctx=None, verbose=False, tune=None, readhess=False):
+           seed_offset=0, chunk=2000, device=0, ctx=None, verbose=False, tune=None, readhess=False,
+           frames=None, instapath=False, centre=False, init="well"):
     c = dict(cfg)
     if nrep is not None:
         c["nrep"] = nrep
     nrep = c.get("nrep", 1)
     c["seeds"] = [seed_offset + s for s in range(nrep)] if "seeds" not in cfg or seed_offset else c["seeds"]
-    ti = pgconfigs.TiInputs(c, nrep=nrep, nintegral=nintegral, gauleg=pg.gauleg)
+    ti = pgconfigs.TiInputs(c, nrep=nrep, nintegral=nintegral, gauleg=pg.gauleg, init=init)
     nmc = int(nmc if nmc is not None else c["nmc"])
     own = ctx is None
     if own:
         ctx = pg.Context(device)
     try:
         ctx.set_system(c["ndim"], c["natom"], c["mass"], c["pes_id"], c["params"], c["V0"])
+        if frames is not None or instapath or centre:  # path.xyz / instanton / centring
+            ti_path_inputs(ctx, c, ti, frames if frames is not None else [c["well1"], c["well2"]],
+                           instapath=instapath, centre=centre, init=init)
         tcfg = ti.ti_config(pg, precision, form)
         if tune:  # autotuner cache (AUTO form): tuned on the first batch of each shape
             ctx.set_tuning(tune, pg.PG_TUNE_ON)

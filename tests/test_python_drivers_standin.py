@@ -47,6 +47,11 @@ elif job["kind"] == "rpi_path":
     c = pgconfigs.load("c3")
     r = drivers.run_rpi(c, N=job["N"], betas=job["betas"], path=[np.array(f) for f in job["frames"]])
     out = dict(S=[q["S"] for q in r["results"]], x=np.asarray(r["x"]).tolist())
+elif job["kind"] == "ti_path":
+    c = dict(pgconfigs.load("c1"), P=job["P"], imin=job["imin"])
+    r = drivers.run_ti(c, precision=pg.PG_FP64, form=pg.PG_FORM_FUSED, nmc=job["nmc"], nrep=2, nintegral=3,
+                       frames=[np.array(f) for f in job["frames"]], instapath=True, centre=True, init="path")
+    out = dict(dA=r["dA"])
 elif job["kind"] == "crossover":
     c = pgconfigs.load("c1")
     ctx = pg.Context(0)
@@ -205,3 +210,30 @@ def test_run_rpi_path_guess_host_logic(oracle, run_job):
     betan = betas[0] / N
     S = betan * (oracle.UM(pes, c["mass"], N, betan, x, w1, w2) - N * vmin)
     assert out["S"][0] == pytest.approx(S, rel=1e-12)
+
+
+def test_run_ti_path_flow_matches_the_namelist_driver(oracle, run_job, tmp_path):
+    """run_ti(frames=..., instapath=True, centre=True, init='path') and the
+    namelist driver with readpath / instapath / centre build the same batch:
+    both through the stand-in, Delta A agrees to round-off."""
+    import standin
+    c = pgconfigs.load("c1")
+    m1, m2 = np.array(c["well1"]), np.array(c["well2"])
+    f1, f2 = m1 + 0.1 * (m2 - m1), m2 - 0.1 * (m2 - m1)
+    P, nmc, imin = 24, 30, 10
+    out = run_job(dict(kind="ti_path", frames=[list(f1), list(f2)], P=P, nmc=nmc, imin=imin))
+    exe = standin.build_driver("pimd_ti", tmp_path)
+    (tmp_path / "masses.dat").write_text("H %.17g\n" % c["mass"][0])
+    for name, w in (("well1", m1), ("well2", m2)):
+        (tmp_path / (name + ".dat")).write_text("%.17g %.17g\n" % tuple(w))
+    (tmp_path / "pes.dat").write_text("\n".join("%.17g" % v for v in c["params"]) + "\n")
+    (tmp_path / "path.xyz").write_text("".join(" 1\n frame %d\n H %.17g %.17g\n" % (i, *w) for i, w in
+                                               enumerate((f1, f2))))
+    text = ("&MCDATA n=%d, beta=%.17g, NMC=%d, dt=%.17g, imin=%d, tau=1.0, gamma=%.17g, nintegral=3,\n"
+            " nrep=2, thermostat=2, ndim=2, natom=1, readpath=T, npath=2, instapath=T, centre=T,\n"
+            " pes='2dtest', pes_params='pes.dat', precision='fp64', form='fused', init='path',\n"
+            " init_sigma=%.17g, seed=0 /\n" % (P, c["beta"], nmc, c["dt"], imin, c["gamma"], c["init_sigma"]))
+    r = subprocess.run([exe], input=text, capture_output=True, text=True, cwd=str(tmp_path), timeout=300)
+    assert r.returncode == 0, r.stderr
+    dA = float(__import__("re").search(r"final Delta A=\s*(\S+)", r.stdout).group(1))
+    assert out["dA"] == pytest.approx(dA, rel=1e-12)
