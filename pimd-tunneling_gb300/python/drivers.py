@@ -161,9 +161,74 @@ def ti_path_inputs(ctx, c, ti, frames, instapath=False, centre=False, init="path
     return xm
 
 
+def restart_name(r, ntask, nproc=1):
+    """restart_proc<iproc>_<ii>.xyz of task r: nproc contiguous blocks of
+    ceil(ntask / nproc) tasks (pimd_par.f90:109-110, 352)."""
+    ncalcs = -(-ntask // nproc)
+    return "restart_proc%d_%d.xyz" % (r // ncalcs, r % ncalcs + 1)
+
+
+def write_restart_files(ctx, c, labels=None, nproc=1, directory="."):
+    """write_restart (verletmodule.f90:162-185) for every ring of the batch on
+    ctx: per bead natom, the running dHdr sum, label x y z; then per bead natom,
+    the step count, label px py pz (coordinates beyond ndim written as 0), in
+    the files of restart_name."""
+    import os
+    ndim, natom = c["ndim"], c["natom"]
+    labels = labels or ["X"] * natom
+    x, p = ctx.ti_state()
+    dsum = ctx.ti_results()[0]
+    step = ctx.ti_step()
+    nr = dsum.size
+    P = x.size // (nr * ndim * natom)
+    x = x.reshape(nr, natom, ndim, P)
+    p = p.reshape(nr, natom, ndim, P)
+    for r in range(nr):
+        with open(os.path.join(directory, restart_name(r, nr, nproc)), "w") as f:
+            for v, head in ((x[r], "%.17g" % dsum[r]), (p[r], "%d" % step)):
+                for i in range(P):
+                    f.write(" %d\n %s\n" % (natom, head))
+                    for j in range(natom):
+                        f.write(" %s %s\n" % (labels[j], " ".join("%.17g" % (v[j, d, i] if d < ndim else 0.0)
+                                                                for d in range(3))))
+
+
+def read_restart_files(c, nrings, P, nproc=1, directory="."):
+    """The files of write_restart_files back: (x0, p0, dhdr_sum, step) in the ring
+    layout x[r][(atom ndim + dim) P + bead]; the files must agree on the step."""
+    import os
+    ndim, natom = c["ndim"], c["natom"]
+    x0 = np.zeros((nrings, natom, ndim, P))
+    p0 = np.zeros((nrings, natom, ndim, P))
+    dsum = np.zeros(nrings)
+    steps = set()
+    for r in range(nrings):
+        with open(os.path.join(directory, restart_name(r, nrings, nproc))) as f:
+            tok = f.read().split()
+        k = 0
+        for dest in (x0, p0):
+            for i in range(P):
+                if int(tok[k]) != natom:
+                    raise ValueError("restart file %s: natom mismatch" % restart_name(r, nrings, nproc))
+                head = tok[k + 1]
+                k += 2
+                if dest is x0:
+                    dsum[r] = float(head)
+                else:
+                    steps.add(int(head))
+                for j in range(natom):
+                    vals = [float(v) for v in tok[k + 1:k + 4]]
+                    dest[r, j, :, i] = vals[:ndim]
+                    k += 4
+    if len(steps) != 1:
+        raise ValueError("restart files disagree on the step count")
+    return x0.reshape(nrings, -1), p0.reshape(nrings, -1), dsum, steps.pop()
+
+
 def run_ti(cfg, precision=pg.PG_MIXED, form=pg.PG_FORM_AUTO, nmc=None, nrep=None, nintegral=None,
            seed_offset=0, chunk=2000, device=0, ctx=None, verbose=False, tune=None, readhess=False,
-           frames=None, instapath=False, centre=False, init="well"):
+           frames=None, instapath=False, centre=False, init="well", restart=0, nproc=1, labels=None,
+           directory="."):
     c = dict(cfg)
     if nrep is not None:
         c["nrep"] = nrep
@@ -182,19 +247,29 @@ def run_ti(cfg, precision=pg.PG_MIXED, form=pg.PG_FORM_AUTO, nmc=None, nrep=None
         tcfg = ti.ti_config(pg, precision, form)
         if tune:  # autotuner cache (AUTO form): tuned on the first batch of each shape
             ctx.set_tuning(tune, pg.PG_TUNE_ON)
-        x0 = readhess_start(ctx, c, ti) if readhess else None
-        ctx.ti_setup(tcfg, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref, x0=x0)
+        p0 = None
+        if restart == 2:  # continue from the restart files, nmc further steps (pimd_par.f90:356-369)
+            x0, p0, dsum, step0 = read_restart_files(c, ti.nrings, ti.P, nproc, directory)
+        else:
+            x0 = readhess_start(ctx, c, ti) if readhess else None
+        ctx.ti_setup(tcfg, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref, x0=x0, p0=p0)
+        done = 0
+        if restart == 2:
+            ctx.ti_set_accumulators(dsum, np.full(ti.nrings, max(0, step0 - int(c.get("imin", 0)))), step0)
+            done = step0
+        target = done + nmc
         form_used, _ = ctx.ti_form(1)
         t0 = time.perf_counter()
         dev_ms = 0.0
-        done = 0
-        while done < nmc:
-            n = min(chunk, nmc - done)
+        while done < target:
+            n = min(chunk, target - done)
             dev_ms += ctx.ti_advance_timed(n)
             done += n
             if verbose:
-                print("  %d / %d steps" % (done, nmc), flush=True)
+                print("  %d / %d steps" % (done, target), flush=True)
         wall = time.perf_counter() - t0
+        if restart >= 1:
+            write_restart_files(ctx, c, labels, nproc, directory)
         mean, var, cnt = ctx.ti_lambda_reduce()
         _, _, _, status = ctx.ti_results()
     finally:

@@ -52,6 +52,11 @@ elif job["kind"] == "ti_path":
     r = drivers.run_ti(c, precision=pg.PG_FP64, form=pg.PG_FORM_FUSED, nmc=job["nmc"], nrep=2, nintegral=3,
                        frames=[np.array(f) for f in job["frames"]], instapath=True, centre=True, init="path")
     out = dict(dA=r["dA"])
+elif job["kind"] == "ti_restart":
+    c = dict(pgconfigs.load("c0"), imin=50, P=16)
+    r = drivers.run_ti(c, precision=pg.PG_FP64, form=pg.PG_FORM_FUSED, nmc=job["nmc"], nrep=3,
+                       restart=job["restart"], nproc=2, labels=["H"], directory=job["dir"])
+    out = dict(dA=r["dA"])
 elif job["kind"] == "crossover":
     c = pgconfigs.load("c1")
     ctx = pg.Context(0)
@@ -237,3 +242,42 @@ def test_run_ti_path_flow_matches_the_namelist_driver(oracle, run_job, tmp_path)
     assert r.returncode == 0, r.stderr
     dA = float(__import__("re").search(r"final Delta A=\s*(\S+)", r.stdout).group(1))
     assert out["dA"] == pytest.approx(dA, rel=1e-12)
+
+
+def test_run_ti_restart_files(oracle, run_job, tmp_path):
+    """run_ti(restart=1) writes the restart_proc files the namelist driver writes
+    for the same batch (same numbers, same layout); run_ti(restart=2) continues
+    from them: 150 + 150 steps equal one 300-step run."""
+    import re
+    import standin
+    c = dict(pgconfigs.load("c0"), imin=50, P=16)
+    py_dir, cc_dir, one_dir = tmp_path / "py", tmp_path / "cc", tmp_path / "one"
+    for d in (py_dir, cc_dir, one_dir):
+        d.mkdir()
+    run_job(dict(kind="ti_restart", nmc=150, restart=1, dir=str(py_dir)))
+    exe = standin.build_driver("pimd_ti", tmp_path)
+    (cc_dir / "masses.dat").write_text("H %.17g\n" % c["mass"][0])
+    (cc_dir / "well1.dat").write_text("%.17g\n" % c["well1"][0])
+    (cc_dir / "well2.dat").write_text("%.17g\n" % c["well2"][0])
+    (cc_dir / "pes.dat").write_text("\n".join("%.17g" % v for v in c["params"]) + "\n")
+    text = ("&MCDATA n=16, beta=%.17g, NMC=150, dt=%.17g, imin=50, tau=%.17g, gamma=%.17g, nintegral=%d,\n"
+            " nrep=3, thermostat=2, ndim=1, natom=1, readpath=F, pes='1d', pes_params='pes.dat',\n"
+            " precision='fp64', form='fused', init='well', init_sigma=%.17g, seed=0, restart=1, nproc=2 /\n"
+            % (c["beta"], c["dt"], c["tau"], c["gamma"], c["nintegral"], c["init_sigma"]))
+    r = subprocess.run([exe], input=text, capture_output=True, text=True, cwd=str(cc_dir), timeout=300)
+    assert r.returncode == 0, r.stderr
+    names = sorted(p.name for p in cc_dir.glob("restart_proc*.xyz"))
+    assert names == sorted(p.name for p in py_dir.glob("restart_proc*.xyz")) and len(names) == 3 * c["nintegral"]
+    for name in names:
+        a, b = (cc_dir / name).read_text().split(), (py_dir / name).read_text().split()
+        assert len(a) == len(b)
+        for u, v in zip(a, b):
+            if re.fullmatch(r"[A-Za-z]+", u):
+                assert u == v
+            else:
+                # the namelist driver's end points come from a spline through the two wells,
+                # the Python driver's from the straight line: round-off apart
+                assert float(u) == pytest.approx(float(v), rel=1e-9, abs=1e-12)
+    two_legs = run_job(dict(kind="ti_restart", nmc=150, restart=2, dir=str(cc_dir)))["dA"]
+    one = run_job(dict(kind="ti_restart", nmc=300, restart=0, dir=str(one_dir)))["dA"]
+    assert two_legs == pytest.approx(one, rel=1e-8)
