@@ -75,7 +75,7 @@ class TiInputs:
         t.thermostat = c.get("thermostat", 2)
         t.precision = precision
         t.form = pimdgpu.PG_FORM_AUTO if form is None else form
-        t.cayley = 0
+        t.cayley = int(bool(c.get("cayley", False)))
         t.imin = c.get("imin", 0)
         t.noutput = c.get("noutput", 100000)
         t.dhdr_limit = c.get("dhdr_limit", -1.0)
