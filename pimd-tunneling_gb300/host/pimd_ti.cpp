@@ -92,6 +92,7 @@ static bool read_restart_xyz(const std::string &path, int64_t n, int ndim, int n
             } else {
                 long long st = 0;
                 if (!(f >> st)) return false;
+                if (i > 0 && st != *step) return false;  // one step count per file
                 *step = st;
             }
             double *v = pass == 0 ? x : p;
@@ -490,25 +491,43 @@ int main(int argc, char **argv) {
     }
     int64_t done = 0;
     CHECK(pg_ti_get_step(ctx, &done));
-    const int64_t target = restart == 2 ? done + NMC : NMC;
-    while (done < target) {
-        int64_t k = std::min(chunk, target - done);
-        CHECK(pg_ti_advance(ctx, k));
-        done += k;
-        if (iprint) std::printf(" %.2f %% of the steps done\n", 100.0 * (double)done / (double)target);
-    }
-    if (restart >= 1) {
+    const int64_t start = done, target = restart == 2 ? done + NMC : NMC;
+    // restart files (and restart.ckpt) every Noutput steps past imin and at the
+    // end, as propagate_pimd_pile does (verletmodule.f90:389-395, 412): the
+    // reference writes before its step ii when ii >= Noutput steps have passed
+    // since the last write and ii > imin (ii counted from 1 in this run), and
+    // labels that state with ii; here the label is the number of steps the state
+    // has taken, so that a continuation resumes the Philox streams exactly
+    auto write_files = [&](int64_t step_count) -> int {
         CHECK(pg_ti_checkpoint_save(ctx, "restart.ckpt"));
         std::vector<double> xs(nstate), ps(nstate), ds(nrings);
         CHECK(pg_ti_get_state(ctx, xs.data(), ps.data()));
         CHECK(pg_ti_get_results(ctx, ds.data(), nullptr, nullptr, nullptr));
         for (int64_t r = 0; r < nrings; r++)
             if (!write_restart_xyz(restart_name(r, nrings, nproc), n, ndim, natom, label, &xs[r * nd * n],
-                                   &ps[r * nd * n], ds[r], done)) {
+                                   &ps[r * nd * n], ds[r], step_count)) {
                 std::fprintf(stderr, "cannot write restart file for task %lld\n", (long long)r);
                 return 1;
             }
+        return 0;
+    };
+    const int64_t never = INT64_MAX / 4;
+    int64_t next_ii = restart >= 1 && Noutput > 0 ? std::max<int64_t>(Noutput, imin + 1) : never;
+    while (done < target) {
+        const int64_t at = next_ii < never ? start + next_ii - 1 : never;  // state before step next_ii
+        const int64_t k = std::min(chunk, std::min(target, at) - done);
+        if (k > 0) {
+            CHECK(pg_ti_advance(ctx, k));
+            done += k;
+            if (iprint) std::printf(" %.2f %% of the steps done\n", 100.0 * (double)(done - start) / (double)NMC);
+        }
+        if (done == at && done < target) {
+            if (int rc = write_files(done)) return rc;
+            next_ii += Noutput;
+        }
     }
+    if (restart >= 1)
+        if (int rc = write_files(done)) return rc;
     std::vector<double> mean(nintegral), var(nintegral);
     std::vector<int64_t> cnt(nintegral);
     CHECK(pg_ti_lambda_reduce(ctx, mean.data(), var.data(), cnt.data()));

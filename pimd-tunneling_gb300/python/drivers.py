@@ -203,23 +203,29 @@ def read_restart_files(c, nrings, P, nproc=1, directory="."):
     dsum = np.zeros(nrings)
     steps = set()
     for r in range(nrings):
-        with open(os.path.join(directory, restart_name(r, nrings, nproc))) as f:
+        name = restart_name(r, nrings, nproc)
+        with open(os.path.join(directory, name)) as f:
             tok = f.read().split()
         k = 0
-        for dest in (x0, p0):
-            for i in range(P):
-                if int(tok[k]) != natom:
-                    raise ValueError("restart file %s: natom mismatch" % restart_name(r, nrings, nproc))
-                head = tok[k + 1]
-                k += 2
-                if dest is x0:
-                    dsum[r] = float(head)
-                else:
-                    steps.add(int(head))
-                for j in range(natom):
-                    vals = [float(v) for v in tok[k + 1:k + 4]]
-                    dest[r, j, :, i] = vals[:ndim]
-                    k += 4
+        try:
+            for dest in (x0, p0):
+                for i in range(P):
+                    if int(tok[k]) != natom:
+                        raise ValueError("natom mismatch")
+                    head = tok[k + 1]
+                    k += 2
+                    if dest is x0:
+                        dsum[r] = float(head)
+                    else:
+                        steps.add(int(head))
+                    for j in range(natom):
+                        vals = [float(v) for v in tok[k + 1:k + 4]]
+                        if len(vals) != 3:
+                            raise ValueError("short file")
+                        dest[r, j, :, i] = vals[:ndim]
+                        k += 4
+        except (IndexError, ValueError) as e:
+            raise ValueError("cannot read restart file %s (%s)" % (name, e)) from None
     if len(steps) != 1:
         raise ValueError("restart files disagree on the step count")
     return x0.reshape(nrings, -1), p0.reshape(nrings, -1), dsum, steps.pop()

@@ -194,8 +194,12 @@ int pg_ti_setup(pg_ctx *c, const pg_ti_config *cfg, int64_t nrings, int64_t nlam
     }
     return PG_OK;
 }
+// PG_STANDIN_FAIL_AT = k: a call that would take the batch past step k fails
+// without advancing (a run that dies there, for the restart tests).
 int pg_ti_advance(pg_ctx *c, int64_t nsteps) {
     TiBatch &t = c->ti;
+    if (const char *f = std::getenv("PG_STANDIN_FAIL_AT"))
+        if (t.step + nsteps > std::atoll(f)) return PG_ERR_CUDA;
     const int64_t nd = ndof(c), ns = nd * t.prm.P;
     for (int64_t r = 0; r < t.nrings; r++) {
         const int64_t l = t.lam[r];

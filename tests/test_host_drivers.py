@@ -546,3 +546,71 @@ def test_rpi_angular_grid_on_the_oracle(oracle, tmp_path):
                 assert rows[q, 3] == pytest.approx(wth[ii] * wph[jj] * wth[kk], rel=1e-14)
                 assert rows[q, 4] == pytest.approx(ib, rel=1e-8, abs=1e-300)
                 q += 1
+
+
+def test_pimd_ti_resumes_after_a_failed_run(oracle, tmp_path):
+    """Restart files every Noutput steps (verletmodule.f90:389-395): a run that
+    fails at step 250 (injected on the host: the stand-in's advance refuses to
+    pass it) has left the files of its state after 199 steps; restart = 2 from
+    them runs to step 300 and matches an uninterrupted run."""
+    import standin
+    exe = standin.build_driver("pimd_ti", tmp_path)
+    c = dict(pgconfigs.load("c0"), imin=50, P=16)
+    run_dir, ref_dir = tmp_path / "run", tmp_path / "ref"
+    for d in (run_dir, ref_dir):
+        d.mkdir()
+        _write_inputs(d, c, ["H"])
+
+    def text(nmc, restart):
+        return _ti_text(c, nmc, 2, "restart=%d, Noutput=100, chunk=30 " % restart)
+
+    r = subprocess.run([exe], input=text(300, 1), capture_output=True, text=True, cwd=str(run_dir), timeout=300,
+                       env=dict(os.environ, PG_STANDIN_FAIL_AT="250"))
+    assert r.returncode == 2 and "pg_ti_advance" in r.stderr
+    lines = (run_dir / "restart_proc0_1.xyz").read_text().split("\n")
+    assert lines[16 * 3 + 1].strip() == "199"  # written before step 200 (the second write)
+    r = subprocess.run([exe], input=text(101, 2), capture_output=True, text=True, cwd=str(run_dir), timeout=300)
+    assert r.returncode == 0, r.stderr
+    resumed = float(re.search(r"final Delta A=\s*(\S+)", r.stdout).group(1))
+    r = subprocess.run([exe], input=text(300, 0), capture_output=True, text=True, cwd=str(ref_dir), timeout=300)
+    assert r.returncode == 0, r.stderr
+    whole = float(re.search(r"final Delta A=\s*(\S+)", r.stdout).group(1))
+    assert resumed == pytest.approx(whole, rel=1e-8)
+
+
+def test_pimd_ti_rejects_corrupted_restart_files(oracle, tmp_path):
+    """Corrupted restart files stop restart = 2 with a message naming the file:
+    a truncated file, a wrong atom count, step counts that disagree."""
+    import standin
+    exe = standin.build_driver("pimd_ti", tmp_path)
+    c = dict(pgconfigs.load("c0"), imin=50, P=16)
+    _write_inputs(tmp_path, c, ["H"])
+    r = subprocess.run([exe], input=_ti_text(c, 60, 2, "restart=1 "), capture_output=True, text=True,
+                       cwd=str(tmp_path), timeout=300)
+    assert r.returncode == 0, r.stderr
+    good = {p.name: p.read_text() for p in tmp_path.glob("restart_proc*.xyz")}
+    f = tmp_path / "restart_proc0_3.xyz"
+
+    def resume():
+        return subprocess.run([exe], input=_ti_text(c, 10, 2, "restart=2 "), capture_output=True, text=True,
+                              cwd=str(tmp_path), timeout=300)
+
+    f.write_text(good[f.name][: len(good[f.name]) // 2])  # truncated
+    r = resume()
+    assert r.returncode == 1 and "restart_proc0_3.xyz" in r.stderr
+    f.write_text(good[f.name].replace(" 1\n", " 2\n", 1))  # natom 2 in the first frame
+    r = resume()
+    assert r.returncode == 1 and "restart_proc0_3.xyz" in r.stderr
+    lines = good[f.name].split("\n")
+    lines[16 * 3 + 1] = " 61"  # two step counts in one file
+    f.write_text("\n".join(lines))
+    r = resume()
+    assert r.returncode == 1 and "restart_proc0_3.xyz" in r.stderr
+    for b in range(16):
+        lines[(16 + b) * 3 + 1] = " 61"  # another step count than the other files
+    f.write_text("\n".join(lines))
+    r = resume()
+    assert r.returncode == 1 and "disagree" in r.stderr
+    f.write_text(good[f.name])
+    r = resume()
+    assert r.returncode == 0, r.stderr
