@@ -263,16 +263,25 @@ def run_ti(cfg, precision=pg.PG_MIXED, form=pg.PG_FORM_AUTO, nmc=None, nrep=None
         if restart == 2:
             ctx.ti_set_accumulators(dsum, np.full(ti.nrings, max(0, step0 - int(c.get("imin", 0)))), step0)
             done = step0
-        target = done + nmc
+        start, target = done, done + nmc
+        # restart files every Noutput steps past imin (verletmodule.f90:389-395), as the namelist
+        # driver writes them: the state before step ii of this run, labelled with its step count
+        noutput = int(c.get("noutput", 100000))
+        next_ii = max(noutput, int(c.get("imin", 0)) + 1) if restart >= 1 and noutput > 0 else None
         form_used, _ = ctx.ti_form(1)
         t0 = time.perf_counter()
         dev_ms = 0.0
         while done < target:
-            n = min(chunk, target - done)
-            dev_ms += ctx.ti_advance_timed(n)
-            done += n
-            if verbose:
-                print("  %d / %d steps" % (done, target), flush=True)
+            at = start + next_ii - 1 if next_ii is not None else target
+            n = min(chunk, min(target, at) - done)
+            if n > 0:
+                dev_ms += ctx.ti_advance_timed(n)
+                done += n
+                if verbose:
+                    print("  %d / %d steps" % (done, target), flush=True)
+            if next_ii is not None and done == at and done < target:
+                write_restart_files(ctx, c, labels, nproc, directory)
+                next_ii += noutput
         wall = time.perf_counter() - t0
         if restart >= 1:
             write_restart_files(ctx, c, labels, nproc, directory)

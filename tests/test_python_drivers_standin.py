@@ -53,9 +53,9 @@ elif job["kind"] == "ti_path":
                        frames=[np.array(f) for f in job["frames"]], instapath=True, centre=True, init="path")
     out = dict(dA=r["dA"])
 elif job["kind"] == "ti_restart":
-    c = dict(pgconfigs.load("c0"), imin=50, P=16)
+    c = dict(pgconfigs.load("c0"), imin=50, P=16, noutput=job.get("noutput", 100000))
     r = drivers.run_ti(c, precision=pg.PG_FP64, form=pg.PG_FORM_FUSED, nmc=job["nmc"], nrep=3,
-                       restart=job["restart"], nproc=2, labels=["H"], directory=job["dir"])
+                       restart=job["restart"], nproc=2, labels=["H"], directory=job["dir"], chunk=30)
     out = dict(dA=r["dA"])
 elif job["kind"] == "crossover":
     c = pgconfigs.load("c1")
@@ -282,3 +282,20 @@ def test_run_ti_restart_files(oracle, run_job, tmp_path):
     two_legs = run_job(dict(kind="ti_restart", nmc=150, restart=2, dir=str(cc_dir)))["dA"]
     one = run_job(dict(kind="ti_restart", nmc=300, restart=0, dir=str(one_dir)))["dA"]
     assert two_legs == pytest.approx(one, rel=1e-8)
+
+
+def test_run_ti_resumes_after_a_failed_run(oracle, run_job, tmp_path):
+    """run_ti(restart=1) with noutput = 100 writes the restart files before steps
+    100 and 200; a run that fails at step 250 (injected on the host through the
+    stand-in) resumes from them (restart=2) and matches an uninterrupted run."""
+    run_dir, ref_dir = tmp_path / "run", tmp_path / "ref"
+    run_dir.mkdir()
+    ref_dir.mkdir()
+    with pytest.raises(AssertionError, match="pg_ti_advance|pimdgpu error"):
+        run_job(dict(kind="ti_restart", nmc=300, restart=1, noutput=100, dir=str(run_dir)),
+                env=dict(PG_STANDIN_FAIL_AT="250"))
+    lines = (run_dir / "restart_proc0_1.xyz").read_text().split("\n")
+    assert lines[16 * 3 + 1].strip() == "199"
+    resumed = run_job(dict(kind="ti_restart", nmc=101, restart=2, noutput=100, dir=str(run_dir)))["dA"]
+    whole = run_job(dict(kind="ti_restart", nmc=300, restart=0, dir=str(ref_dir)))["dA"]
+    assert resumed == pytest.approx(whole, rel=1e-8)
