@@ -545,6 +545,7 @@ extern "C" int pg_instanton_fg(pg_ctx *ctx, int64_t nbeta, int64_t N, const doub
 extern "C" int pg_instanton_optimize(pg_ctx *ctx, int64_t nbeta, int64_t N, double *x, const double *a,
                                      const double *b, const double *betan, const pg_lbfgs_opts *opts, double *UM,
                                      int64_t *niter, int32_t *status) {
+    NvtxRange nvtx_range("pg_instanton_optimize");
     int rc = check_ctx(ctx, true);
     if (rc) return rc;
     if (nbeta < 1 || N < 2 || !x || !a || !b || !betan || !opts) return fail(PG_ERR_ARG, "bad optimize arguments");
@@ -652,6 +653,7 @@ static int band_factor(pg_ctx *ctx, int64_t nbeta, int64_t n, int kd, const std:
 extern "C" int pg_instanton_logdet(pg_ctx *ctx, int64_t nbeta, int64_t N, const double *x, const double *betan,
                                    int32_t singlewell, int32_t skip_lowest, int32_t quirks, double *lndet,
                                    double *eta2_min, int64_t *nskipped) {
+    NvtxRange nvtx_range("pg_instanton_logdet");
     int rc = check_ctx(ctx, true);
     if (rc) return rc;
     if (nbeta < 1 || N < 2 || !x || !betan || !lndet) return fail(PG_ERR_ARG, "bad logdet arguments");

@@ -1,6 +1,7 @@
 // pg_internal.h -- context layout and helpers shared by the library's translation units.
 #pragma once
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cstdint>
 #include <map>
@@ -11,6 +12,15 @@
 #include "pg_device.cuh"
 
 namespace pg {
+
+// NVTX range over an API call (header-only NVTX3: a no-op unless a profiler
+// attaches), so that ncu --nvtx filters and timeline tools name the calls.
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 void set_error(const std::string &msg);
 int fail(int code, const std::string &msg);

@@ -250,7 +250,6 @@ __global__ void __launch_bounds__(128) k_ti_fused(TiArgs a, R *__restrict__ gq, 
     const size_t off = (size_t)r * nd * P;
     R *q = gq + off, *pi = gpi + off, *x = gx + off, *f = gf + off;
     const int lam = a.ringlam[r];
-    const double *bv = a.bv + (size_t)lam * nd * P;
     const double *dbdl = a.dbdl + (size_t)lam * nd;
     const uint64_t seed = a.ringseed[r];
     const uint32_t stream = a.ringstream[r];
@@ -882,7 +881,7 @@ static int ti_setup_impl(pg_ctx *ctx, const pg_ti_config *cfg, int64_t nrings, i
         ti_release(ctx);
         return rc;
     }
-    const int P = st.P, nd = st.nd, natom = ctx->natom, ndim = ctx->ndim;
+    const int P = st.P, nd = st.nd, natom = ctx->natom;
     const double betan = st.betan;
 
     // init_nm (verletmodule.f90:306-338): lam, beadmass, beadvec; transmatrix
@@ -1088,6 +1087,7 @@ extern "C" int pg_ti_setup(pg_ctx *ctx, const pg_ti_config *cfg, int64_t nrings,
                            const uint32_t *ring_stream, const double *a, const double *b,
                            const double *dbdl, const double *xref, const double *x0,
                            const double *p0) {
+    NvtxRange nvtx_range("pg_ti_setup");
     auto setup = [&](const pg_ti_config *c, int th, int steps) {
         return ti_setup_impl(ctx, c, nrings, nlambda, ring_lambda, ring_seed, ring_stream, a, b, dbdl, xref, x0,
                              p0, th, steps);
@@ -1203,6 +1203,7 @@ static int ti_finish(pg_ctx *ctx, int64_t nsteps) {
 }
 
 static int ti_advance_impl(pg_ctx *ctx, int64_t nsteps, double *device_ms) {
+    NvtxRange nvtx_range("pg_ti_advance");
     pg_ctx *one[1] = {ctx};
     return ti_advance_group(one, 1, nsteps, device_ms);
 }
@@ -1577,6 +1578,7 @@ extern "C" int pg_propagate_pimd(pg_ctx *ctx, const pg_ti_config *cfg, int64_t n
                                  const double *a, const double *b, const double *dbdl,
                                  const uint64_t *seed, const uint32_t *stream, double *x, double *p,
                                  double *dHdr, int32_t *status) {
+    NvtxRange nvtx_range("pg_propagate_pimd");
     int rc = check_ctx(ctx, true);
     if (rc) return rc;
     if (!x || !p || !dHdr || ntask < 1 || nmc < 0) return fail(PG_ERR_ARG, "bad propagate arguments");
