@@ -1281,6 +1281,7 @@ static int ti_advance_group(pg_ctx *const *ctxs, int64_t nctx, int64_t nsteps, d
 }
 
 extern "C" int pg_ti_advance_group(pg_ctx *const *ctxs, int64_t nctx, int64_t nsteps, double *device_ms) {
+    NvtxRange nvtx_range("pg_ti_advance_group");
     return ti_advance_group(ctxs, nctx, nsteps, device_ms);
 }
 
