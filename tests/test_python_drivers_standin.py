@@ -32,7 +32,8 @@ if job["kind"] == "rpi":
         out[str(fe)] = dict(S=[q["S"] for q in r["results"]], delta=[q["delta"] for q in r["results"]],
                             vpath=r["vpath"].tolist())
 elif job["kind"] == "ti":
-    c = dict(pgconfigs.load("c0"), imin=50, cayley=job.get("cayley", False))
+    c = dict(pgconfigs.load("c0"), imin=50, cayley=job.get("cayley", False), thermostat=job.get("thermostat", 2),
+             noutput=job.get("noutput", 100000))
     r = drivers.run_ti(c, precision=pg.PG_FP64, form=pg.PG_FORM_FUSED, nmc=job["nmc"], nrep=2)
     out = dict(dA=r["dA"], qratio=r["qratio"], delta=r["delta"], mean=r["integrand_mean"])
 elif job["kind"] == "ti_mixed":
@@ -114,14 +115,16 @@ def test_run_rpi_host_logic(oracle, run_job):
             assert got["delta"][i] == pytest.approx(2 * om / betan, rel=1e-8)
 
 
-@pytest.mark.parametrize("cayley", [False, True])
-def test_run_ti_host_logic(oracle, run_job, cayley):
-    out = run_job(dict(kind="ti", nmc=300, cayley=cayley))
+@pytest.mark.parametrize("cayley,thermostat", [(False, 2), (True, 2), (False, 1)])
+def test_run_ti_host_logic(oracle, run_job, cayley, thermostat):
+    """Langevin, Cayley and Andersen (Poisson mean noutput = 25) batches of run_ti
+    against the oracle ring by ring."""
+    out = run_job(dict(kind="ti", nmc=300, cayley=cayley, thermostat=thermostat, noutput=25))
     c = dict(pgconfigs.load("c0"), imin=50, nrep=2, seeds=[0, 1])
     ti = pgconfigs.TiInputs(c, gauleg=oracle.gauleg)
     pes = oracle.Pes(c["pes_id"], c["ndim"], c["natom"], c["params"])
-    prm = oracle.TiParams(ti.P, c["beta"], c["dt"], tau=c["tau"], gamma=c["gamma"], thermostat=2, cayley=cayley,
-                          nm_resident=True, imin=c["imin"], init_sigma=c["init_sigma"])
+    prm = oracle.TiParams(ti.P, c["beta"], c["dt"], tau=c["tau"], gamma=c["gamma"], thermostat=thermostat,
+                          cayley=cayley, nm_resident=True, imin=c["imin"], init_sigma=c["init_sigma"], noutput=25)
     ints = np.zeros(ti.nrings)
     for r in range(ti.nrings):
         li = int(ti.ring_lambda[r])
