@@ -346,13 +346,14 @@ def test_rpi_driver_host_logic_on_the_oracle(oracle, tmp_path):
     assert float(re.search(r"s_kink=\s*(\S+)", r.stdout).group(1)) == pytest.approx(betan * UMf, rel=1e-12)
 
 
-def _oracle_ti(oracle, c, nmc, nm_resident=True):
+def _oracle_ti(oracle, c, nmc, nm_resident=True, thermostat=2, noutput=100000, dhdr_limit=-1.0):
     """Delta A of the TI batch the driver sets up for c (all beads at well 1,
     seeds 0.., stream = lambda point), by the oracle ring by ring."""
     ti = pgconfigs.TiInputs(c, gauleg=oracle.gauleg)
     pes = oracle.Pes(c["pes_id"], c["ndim"], c["natom"], c["params"])
-    prm = oracle.TiParams(ti.P, c["beta"], c["dt"], tau=c["tau"], gamma=c["gamma"], thermostat=2,
-                          nm_resident=nm_resident, imin=c["imin"], init_sigma=c["init_sigma"])
+    prm = oracle.TiParams(ti.P, c["beta"], c["dt"], tau=c["tau"], gamma=c["gamma"], thermostat=thermostat,
+                          nm_resident=nm_resident, imin=c["imin"], init_sigma=c["init_sigma"], noutput=noutput,
+                          dhdr_limit=dhdr_limit)
     ints = np.zeros(ti.nrings)
     for r in range(ti.nrings):
         li = int(ti.ring_lambda[r])
@@ -388,6 +389,24 @@ def test_pimd_ti_driver_host_logic_on_the_oracle(oracle, tmp_path):
     dA = float(re.search(r"final Delta A=\s*(\S+)", r.stdout).group(1))
     ref = _oracle_ti(oracle, dict(c, nrep=2, seeds=[0, 1]), 300)
     assert dA == pytest.approx(ref, rel=1e-12)
+
+
+@pytest.mark.parametrize("extra,kw", [("thermostat=1, Noutput=25 ", dict(thermostat=1, noutput=25)),
+                                      ("dHdrlimit=0.02 ", dict(dhdr_limit=0.02))])
+def test_pimd_ti_thermostat_keys_on_the_oracle(oracle, tmp_path, extra, kw):
+    """The namelist keys thermostat / Noutput (Andersen) and dHdrlimit reach the
+    batch: pimd_ti.cpp through the stand-in against the oracle ring by ring."""
+    import standin
+    exe = standin.build_driver("pimd_ti", tmp_path)
+    c = dict(pgconfigs.load("c0"), imin=50)
+    _write_inputs(tmp_path, c, ["H"])
+    text = _ti_text(c, 300, 2, extra).replace("thermostat=2, ", "" if "thermostat" in extra else "thermostat=2, ")
+    r = subprocess.run([exe], input=text, capture_output=True, text=True, cwd=str(tmp_path), timeout=300)
+    assert r.returncode == 0, r.stderr
+    dA = float(re.search(r"final Delta A=\s*(\S+)", r.stdout).group(1))
+    ref = _oracle_ti(oracle, dict(c, nrep=2, seeds=[0, 1]), 300, **kw)
+    assert dA == pytest.approx(ref, rel=1e-12)
+    assert ref != pytest.approx(_oracle_ti(oracle, dict(c, nrep=2, seeds=[0, 1]), 300), rel=1e-9)  # keys matter
 
 
 def test_pimd_ti_restart_files_on_the_oracle(oracle, tmp_path):
