@@ -226,6 +226,36 @@ inline bool write_xyz(const std::string &path, const std::vector<std::vector<dou
     return std::fclose(f) == 0;
 }
 
+// The side files read_path leaves (instantonmod.f90:1013-1031): testspline.csv
+// with "dim atom y2(1..npath)" per coordinate (dimension outer, atom inner) for
+// the path's spline second derivatives y2[dof], dof = atom*ndim + dim; and
+// aligned.xyz with the n start beads xt[dof*n + bead] in Angstrom under the
+// rotation angles of the path's alignment.
+inline bool write_read_path_files(const std::vector<std::vector<double>> &y2, const std::vector<double> &xt,
+                                  int64_t n, int ndim, int natom, const std::vector<std::string> &label,
+                                  const double angles[3]) {
+    FILE *f = std::fopen("testspline.csv", "w");
+    if (!f) return false;
+    for (int d = 0; d < ndim; d++)
+        for (int j = 0; j < natom; j++) {
+            std::fprintf(f, " %d %d", d + 1, j + 1);
+            for (double v : y2[(size_t)j * ndim + d]) std::fprintf(f, " %.17g", v);
+            std::fprintf(f, "\n");
+        }
+    if (std::fclose(f) != 0) return false;
+    f = std::fopen("aligned.xyz", "w");
+    if (!f) return false;
+    for (int64_t b = 0; b < n; b++) {
+        std::fprintf(f, " %d\n rotation angles: %.17g %.17g %.17g\n", natom, angles[0], angles[1], angles[2]);
+        for (int j = 0; j < natom; j++) {
+            std::fprintf(f, " %s", j < (int)label.size() ? label[j].c_str() : "X");
+            for (int d = 0; d < ndim; d++) std::fprintf(f, " %.17g", xt[(size_t)(j * ndim + d) * n + b] * 0.529177);
+            std::fprintf(f, "\n");
+        }
+    }
+    return std::fclose(f) == 0;
+}
+
 // {"well1": [...], "well2": [...], "path": [[...], ...]} on standard output
 // (bohr, x[atom*ndim + dim]): the start configurations a driver run would use.
 inline void print_frames_json(const std::vector<double> &w1, const std::vector<double> &w2,

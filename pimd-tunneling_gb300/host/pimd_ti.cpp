@@ -225,14 +225,19 @@ int main(int argc, char **argv) {
     // line; the frames of path.xyz aligned by the angles of the first
     // (instantonmod.f90:916-932)
     std::vector<std::vector<double>> frames;
-    if (readpath && npath >= 2) {
+    pgh::AlignAngles path_ang;  // of the path's first frame (aligned.xyz)
+    const bool from_path = readpath && npath >= 2;
+    if (from_path) {
         try {
             frames = read_path_xyz("path.xyz", (int)npath, ndim, natom, xunit);
         } catch (std::exception &e) {
             std::fprintf(stderr, "%s\n", e.what());
             return 1;
         }
-        if (can_align) pgh::align_frames(frames, natom, atom1, atom2, atom3);
+        if (can_align) {
+            path_ang = pgh::get_align(frames[0], natom, atom1, atom2, atom3);
+            pgh::align_frames(frames, natom, atom1, atom2, atom3);
+        }
     } else {
         frames = {w1, w2};
     }
@@ -270,6 +275,21 @@ int main(int argc, char **argv) {
         return l;
     };
     std::vector<double> lam = arc_length(frames);
+    // start beads xtilde at (k-1)/(n-1) on the path's spline (instantonmod.f90:940-950),
+    // replaced by the instanton with instapath; written to aligned.xyz
+    std::vector<double> xtilde;
+    if (from_path) {
+        const int64_t npf = (int64_t)frames.size();
+        std::vector<double> yk(npf), y2k(npf);
+        xtilde.resize((size_t)nd * n);
+        for (int k = 0; k < nd; k++) {
+            for (int64_t i = 0; i < npf; i++) yk[i] = frames[i][k];
+            CHECK(pg_spline(lam.data(), yk.data(), npf, 1.0e31, 1.0e31, y2k.data()));
+            for (int64_t bead = 0; bead < n; bead++)
+                CHECK(pg_splint(lam.data(), yk.data(), y2k.data(), npf, (double)bead / (double)(n - 1),
+                                &xtilde[(size_t)k * n + bead], nullptr));
+        }
+    }
     if (instapath) {
         // instanton from the path guess (instantonmod.f90:945-983): beads at
         // xi = (k-1)/(n-1) on the spline, optimised with fixed ends at the wells
@@ -299,6 +319,7 @@ int main(int argc, char **argv) {
         int32_t ist = 0;
         CHECK(pg_instanton_optimize(ctx, 1, n, xt.data(), w1.data(), w2.data(), &betan, &o, &um, &it, &ist));
         std::printf(" Found instanton after %lld iterations (status %d).\n", (long long)it, ist);
+        if (from_path) xtilde = xt;
         frames.assign(1, w1);
         for (int64_t bead = 0; bead < n; bead++) {
             std::vector<double> f(nd);
@@ -359,6 +380,13 @@ int main(int argc, char **argv) {
     for (int k = 0; k < nd; k++) {
         for (int64_t i = 0; i < np; i++) ycol[k][i] = frames[i][k];
         CHECK(pg_spline(lam.data(), ycol[k].data(), np, 1.0e31, 1.0e31, y2[k].data()));
+    }
+    if (from_path) {
+        const double ang[3] = {path_ang.theta1, path_ang.theta2, path_ang.theta3};
+        if (!write_read_path_files(y2, xtilde, n, ndim, natom, label, ang)) {
+            std::fprintf(stderr, "cannot write testspline.csv / aligned.xyz\n");
+            return 1;
+        }
     }
     auto path_at = [&](double xi, int k, double *y, double *g) {
         return pg_splint(lam.data(), ycol[k].data(), y2[k].data(), np, xi, y, g);

@@ -118,6 +118,7 @@ int main(int argc, char **argv) {
         }
     }
     std::vector<std::vector<double>> fr;
+    pgh::AlignAngles path_ang;  // of the path's first frame (aligned.xyz)
     if (readpath && npath >= 2) {
         try {
             fr = read_path_xyz("path.xyz", (int)npath, ndim, natom, xunit);
@@ -125,7 +126,10 @@ int main(int argc, char **argv) {
             std::fprintf(stderr, "%s\n", e.what());
             return 1;
         }
-        if (can_align) pgh::align_frames(fr, natom, atom1, atom2, atom3);
+        if (can_align) {
+            path_ang = pgh::get_align(fr[0], natom, atom1, atom2, atom3);
+            pgh::align_frames(fr, natom, atom1, atom2, atom3);
+        }
     }
     if (prepare_only) {  // the inputs as the run would use them, no device
         print_frames_json(w1, w2, fr.empty() ? std::vector<std::vector<double>>{w1, w2} : fr);
@@ -148,18 +152,35 @@ int main(int argc, char **argv) {
             lam[i] = lam[i - 1] + std::sqrt(d);
         }
         for (auto &l : lam) l /= lam.back();
+        std::vector<std::vector<double>> y2all(nd);
         for (int k = 0; k < nd; k++) {
-            std::vector<double> y(fr.size()), y2(fr.size());
+            std::vector<double> y(fr.size());
+            std::vector<double> &y2 = y2all[k];
+            y2.resize(fr.size());
             for (size_t i = 0; i < fr.size(); i++) y[i] = fr[i][k];
             CHECK(pg_spline(lam.data(), y.data(), (int64_t)fr.size(), 1.0e31, 1.0e31, y2.data()));
             for (int64_t bead = 0; bead < n; bead++)
                 CHECK(pg_splint(lam.data(), y.data(), y2.data(), (int64_t)fr.size(), (double)bead / (double)(n - 1),
                                 &x[(size_t)k * n + bead], nullptr));
         }
+        const double ang[3] = {path_ang.theta1, path_ang.theta2, path_ang.theta3};
+        if (!write_read_path_files(y2all, x, n, ndim, natom, label, ang)) {  // instantonmod.f90:1013-1031
+            std::fprintf(stderr, "cannot write testspline.csv / aligned.xyz\n");
+            return 1;
+        }
     } else {
         for (int k = 0; k < nd; k++)
             for (int64_t bead = 1; bead <= n; bead++)  // rpi_ser.f90:157-163
                 x[(size_t)k * n + bead - 1] = ((double)(n - bead) * w1[k] + (double)(bead - 1) * w2[k]) / (double)(n - 1);
+        std::vector<std::string> notes;
+        for (int64_t bead = 1; bead <= n; bead++) notes.push_back("Energy of minimum " + std::to_string(bead));
+        std::vector<std::vector<double>> beads(n, std::vector<double>(nd));
+        for (int k = 0; k < nd; k++)
+            for (int64_t bead = 0; bead < n; bead++) beads[bead][k] = x[(size_t)k * n + bead];
+        if (!write_xyz("aligned.xyz", beads, notes, ndim, natom, label)) {  // rpi_ser.f90:164-172
+            std::fprintf(stderr, "cannot write aligned.xyz\n");
+            return 1;
+        }
     }
     if (checkhess) {
         // Hessian at well 1 written row by row (hessian_well1.dat) and the

@@ -333,6 +333,11 @@ def test_rpi_driver_host_logic_on_the_oracle(oracle, tmp_path):
     lam, vp = np.loadtxt(str(tmp_path / "instantonpathenergy.csv"), unpack=True)
     np.testing.assert_allclose(lam, (k - 1) / (n - 1), atol=1e-14)  # equally spaced straight path
     np.testing.assert_array_equal(vp, energies)
+    # aligned.xyz: the linear start path (rpi_ser.f90:164-172)
+    al = (tmp_path / "aligned.xyz").read_text().strip().split("\n")
+    assert al[1].strip() == "Energy of minimum 1"
+    np.testing.assert_allclose(np.array([[float(v) for v in al[3 * b + 2].split()[1:]] for b in range(n)]) / 0.529177,
+                               x.reshape(2, n).T, rtol=1e-14)
     # checkhess: the Hessian at well 1 and its mass-weighted eigenvalues times 219475
     H = pes.Vdoubleprime(w1)
     np.testing.assert_allclose(np.loadtxt(str(tmp_path / "hessian_well1.dat")), H, rtol=1e-14)
@@ -514,6 +519,14 @@ def test_pimd_ti_path_and_centre_on_the_oracle(oracle, tmp_path):
     xm = float(re.search(r"Centred,\s*\S+\s+\S+\s+(\S+)", r.stdout).group(1))
     assert abs(xm - 0.5) < 1e-6
     assert np.isfinite(float(re.search(r"final Delta A=\s*(\S+)", r.stdout).group(1)))
+    # read_path's side files: the instanton beads under the alignment angles (0 in 2-D), and one row of
+    # spline second derivatives per coordinate over the n + 2 points [well 1, beads, well 2]
+    al = (tmp_path / "aligned.xyz").read_text().strip().split("\n")
+    assert al[1].split()[:2] == ["rotation", "angles:"] and [float(v) for v in al[1].split()[2:]] == [0.0] * 3
+    np.testing.assert_allclose(np.array([[float(v) for v in al[3 * i + 2].split()[1:]] for i in range(n)]) / 0.529177,
+                               beads, rtol=0, atol=1e-12)
+    ts = [l.split() for l in (tmp_path / "testspline.csv").read_text().strip().split("\n")]
+    assert [t[:2] for t in ts] == [["1", "1"], ["2", "1"]] and all(len(t) == 2 + n + 2 for t in ts)
 
 
 def test_rpi_angular_grid_on_the_oracle(oracle, tmp_path):
@@ -633,3 +646,43 @@ def test_pimd_ti_rejects_corrupted_restart_files(oracle, tmp_path):
     f.write_text(good[f.name])
     r = resume()
     assert r.returncode == 0, r.stderr
+
+
+def test_rpi_path_xyz_on_the_oracle(oracle, tmp_path):
+    """readpath for a 3-D system through rpi.cpp on the CPU against the stand-in:
+    the frames of path.xyz aligned by the first frame's angles, splined against
+    arc length, n start beads; aligned.xyz carries them under those angles and
+    testspline.csv the spline's second derivatives (instantonmod.f90:916-1031)."""
+    import align
+    import standin
+    exe = standin.build_driver("rpi", tmp_path)
+    c = pgconfigs.load("c3")
+    labels = ["O", "O", "C", "C", "C", "H", "H", "H", "H"]
+    _write_inputs(tmp_path, c, labels)
+    w1, w2 = np.array(c["well1"]), np.array(c["well2"])
+    rng = np.random.default_rng(3)
+    frames = [w1 + 0.02 * rng.normal(size=27), 0.5 * (w1 + w2) + 0.05 * rng.normal(size=27), w2]
+    (tmp_path / "path.xyz").write_text("".join(
+        " 9\n frame %d\n" % i + "".join(" %s %.17g %.17g %.17g\n" % (labels[j], *(f.reshape(9, 3)[j] * 0.529177))
+                                         for j in range(9)) for i, f in enumerate(frames)))
+    n = 6
+    text = ("&RPIDATA n=%d, beta=%.17g, ndim=3, natom=9, xunit=2, readpath=.true., npath=3, pes='synth9',\n"
+            " pes_params='pes.dat' /\n" % (n, c["betas"][2]))
+    (tmp_path / "well1.dat").write_text("\n".join("%.17g" % v for v in w1 * 0.529177) + "\n")
+    (tmp_path / "well2.dat").write_text("\n".join("%.17g" % v for v in w2 * 0.529177) + "\n")
+    r = subprocess.run([exe], input=text, capture_output=True, text=True, cwd=str(tmp_path), timeout=300)
+    assert r.returncode == 0, r.stderr
+    fa = np.array(align.align_frames(frames))
+    lam = np.concatenate([[0.0], np.cumsum(np.linalg.norm(np.diff(fa, axis=0), axis=1))])
+    lam /= lam[-1]
+    y2 = [oracle.spline(lam, fa[:, d]) for d in range(27)]
+    x = np.array([[oracle.splint(lam, fa[:, d], y2[d], b / (n - 1)) for d in range(27)] for b in range(n)])
+    al = (tmp_path / "aligned.xyz").read_text().strip().split("\n")
+    np.testing.assert_allclose([float(v) for v in al[1].split()[2:]], align.get_align(frames[0]), atol=1e-12)
+    got = np.array([[float(v) for j in range(9) for v in al[11 * b + 2 + j].split()[1:]] for b in range(n)])
+    np.testing.assert_allclose(got / 0.529177, x, rtol=0, atol=1e-10)
+    ts = [l.split() for l in (tmp_path / "testspline.csv").read_text().strip().split("\n")]
+    assert [(int(t[0]), int(t[1])) for t in ts] == [(d, j) for d in (1, 2, 3) for j in range(1, 10)]
+    for t in ts:
+        d, j = int(t[0]) - 1, int(t[1]) - 1
+        np.testing.assert_allclose([float(v) for v in t[2:]], y2[j * 3 + d], rtol=1e-10, atol=1e-10)
