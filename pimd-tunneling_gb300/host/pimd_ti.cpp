@@ -398,6 +398,15 @@ int main(int argc, char **argv) {
     for (int k = 0; k < nd; k++) CHECK(path_at(0.0, k, &a[k], nullptr));
     for (int64_t i = 0; i < nintegral; i++)
         for (int k = 0; k < nd; k++) CHECK(path_at(xi[i], k, &b[i * nd + k], &dbdl[i * nd + k]));
+    {  // xi, V(path(xi)) and |db/dxi| per point (pimd_par.f90:223-225)
+        std::vector<double> vb(nintegral);
+        CHECK(pg_pes_eval(ctx, nintegral, b.data(), vb.data(), nullptr, PG_FP64));
+        for (int64_t i = 0; i < nintegral; i++) {
+            double g2 = 0.0;
+            for (int k = 0; k < nd; k++) g2 += dbdl[i * nd + k] * dbdl[i * nd + k];
+            std::printf(" %.15g %.15g %.15g\n", xi[i], vb[i], std::sqrt(g2));
+        }
+    }
     // start positions per lambda point
     std::vector<double> xref((size_t)nintegral * nd * n);
     for (int64_t i = 0; i < nintegral; i++)
