@@ -647,9 +647,11 @@ __global__ void k_lambda_reduce(const RingAcc *__restrict__ acc, const int32_t *
     const int lam = blockIdx.x;
     double s = 0.0, s2 = 0.0, n = 0.0;
     for (int64_t r = threadIdx.x; r < nrings; r += blockDim.x) {
-        if (ringlam[r] != lam) continue;
+        // rings that met a NaN (their trajectory stopped there) or hold no
+        // sample yet carry no estimate: left out of the mean and the count
+        if (ringlam[r] != lam || (acc[r].status & PG_RING_NAN) || acc[r].nsamples <= 0) continue;
         double ns = (double)acc[r].nsamples;
-        double v = ns > 0.0 ? acc[r].dhdr_sum / ns / (betan * betan) : 0.0;
+        double v = acc[r].dhdr_sum / ns / (betan * betan);
         s += v;
         s2 += v * v;
         n += 1.0;

@@ -186,6 +186,10 @@ int pg_ti_setup(pg_ctx *c, const pg_ti_config *cfg, int64_t nrings, int64_t nlam
         if (p0) std::copy(p0 + r * ns, p0 + (r + 1) * ns, t.p.begin() + r * ns);
         t.res[r].and_rkick = -1;
     }
+    if (const char *k = std::getenv("PG_STANDIN_NAN_RING")) {  // a NaN in one ring's start (fault injection)
+        const int64_t r = std::atoll(k);
+        if (r >= 0 && r < nrings) t.x[(size_t)r * ns] = std::nan("");
+    }
     if (x0 && std::getenv("PG_STANDIN_X0")) {
         FILE *f = std::fopen(std::getenv("PG_STANDIN_X0"), "w");
         if (!f) return PG_ERR_ARG;
@@ -243,9 +247,9 @@ int pg_ti_lambda_reduce(pg_ctx *c, double *mean, double *var, int64_t *count) {
     for (int64_t l = 0; l < t.nlam; l++) {
         double s = 0.0, s2 = 0.0, n = 0.0;
         for (int64_t r = 0; r < t.nrings; r++) {
-            if (t.lam[r] != l) continue;
+            if (t.lam[r] != l || t.res[r].status || t.res[r].nsamples <= 0) continue;  // as the library
             const double ns = (double)t.res[r].nsamples;
-            const double v = ns > 0.0 ? t.res[r].dhdr_sum / ns / bn2 : 0.0;
+            const double v = t.res[r].dhdr_sum / ns / bn2;
             s += v;
             s2 += v * v;
             n += 1.0;
@@ -261,7 +265,7 @@ int pg_ti_assemble(int64_t nintegral, const double *weights, const double *mean,
                    double *dA, double *sigmaA, double *qratio) {
     double d = 0.0, s = 0.0;
     for (int64_t i = 0; i < nintegral; i++) {
-        d += weights[i] * mean[i];
+        if (mean[i] == mean[i]) d += weights[i] * mean[i];  // as the library
         s += weights[i] * weights[i] * var[i];
     }
     *dA = d;
