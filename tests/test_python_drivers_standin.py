@@ -35,7 +35,7 @@ elif job["kind"] == "ti":
     c = dict(pgconfigs.load("c0"), imin=50, cayley=job.get("cayley", False), thermostat=job.get("thermostat", 2),
              noutput=job.get("noutput", 100000))
     r = drivers.run_ti(c, precision=pg.PG_FP64, form=pg.PG_FORM_FUSED, nmc=job["nmc"], nrep=2)
-    out = dict(dA=r["dA"], qratio=r["qratio"], delta=r["delta"], mean=r["integrand_mean"])
+    out = dict(dA=r["dA"], qratio=r["qratio"], delta=r["delta"], mean=r["integrand_mean"], nan_rings=r["nan_rings"])
 elif job["kind"] == "ti_mixed":
     c = dict(pgconfigs.load("c0"), imin=20, nintegral=2, P_per_ring=job["P_per_ring"])
     r = drivers.run_ti_mixed(c, precision=pg.PG_FP64, form=pg.PG_FORM_FUSED, nmc=job["nmc"], chunk=50)
@@ -302,3 +302,20 @@ def test_run_ti_resumes_after_a_failed_run(oracle, run_job, tmp_path):
     resumed = run_job(dict(kind="ti_restart", nmc=101, restart=2, noutput=100, dir=str(run_dir)))["dA"]
     whole = run_job(dict(kind="ti_restart", nmc=300, restart=0, dir=str(ref_dir)))["dA"]
     assert resumed == pytest.approx(whole, rel=1e-8)
+
+
+def test_run_ti_reports_a_nan_ring(oracle, run_job):
+    """A NaN written into ring 1's start (lambda point 0, replica 1) on the host:
+    run_ti reports it and its lambda point's mean is that of the other ring."""
+    clean = run_job(dict(kind="ti", nmc=300))
+    out = run_job(dict(kind="ti", nmc=300), env=dict(PG_STANDIN_NAN_RING="1"))
+    assert clean["nan_rings"] == 0 and out["nan_rings"] == 1
+    assert out["mean"][1:] == clean["mean"][1:]
+    c = dict(pgconfigs.load("c0"), imin=50)
+    ti = pgconfigs.TiInputs(dict(c, nrep=2, seeds=[0, 1]), gauleg=oracle.gauleg)
+    pes = oracle.Pes(c["pes_id"], 1, 1, c["params"])
+    prm = oracle.TiParams(ti.P, c["beta"], c["dt"], tau=c["tau"], gamma=c["gamma"], thermostat=2,
+                          nm_resident=True, imin=50, init_sigma=c["init_sigma"])
+    x, p = oracle.ring_init(pes, c["mass"], prm, ti.xref[0], 0, 0, a=ti.a, b=ti.b[0])
+    res = oracle.ring_propagate(pes, c["mass"], prm, ti.a, ti.b[0], ti.dbdl[0], ti.xref[0], 0, 0, 0, 300, x, p)
+    assert out["mean"][0] == pytest.approx(res.dhdr_sum / res.nsamples / ti.betan ** 2, rel=1e-12)
