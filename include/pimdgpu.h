@@ -177,7 +177,8 @@ int pg_ti_get_results(pg_ctx *ctx, double *dhdr_sum, int64_t *nsamples, int64_t 
 int pg_ti_set_accumulators(pg_ctx *ctx, const double *dhdr_sum, const int64_t *nsamples, int64_t step);
 /* Per-lambda reduction of integrand = dHdr/betan^2 over the rings of each lambda
  * (pimd_par.f90:379, 401-409), on the device: mean[nlambda], var[nlambda]
- * (E[I^2]-E[I]^2), count[nlambda]. */
+ * (E[I^2]-E[I]^2), count[nlambda].  Rings flagged PG_RING_NAN and rings with
+ * no sample yet are left out; count is the number of rings used. */
 int pg_ti_lambda_reduce(pg_ctx *ctx, double *mean, double *var, int64_t *count);
 /* Global step counter of the batch (steps already taken). */
 int pg_ti_get_step(pg_ctx *ctx, int64_t *step);
