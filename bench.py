@@ -346,7 +346,7 @@ def main():
             "form": {pg.PG_FORM_FUSED: "fused-simt", pg.PG_FORM_TENSOR: "tcgen05", pg.PG_FORM_PLAIN: "plain"}[form_used],
             "nan_rings": nan_rings}
     line.update(extras)
-    if rank == 0 and not args.no_cpu:
+    if rank == 0 and ws == 1 and not args.no_cpu:  # the CPU baseline: rank 0 at N = 1 only
         v, cores, sample = cpu_reference_rate(c, ti, target_s=12.0)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
         v1, _, sample1 = cpu_reference_rate(c, ti, target_s=3.0, nthreads=1)
