@@ -15,6 +15,7 @@ run_rpi  -- rpi_ser.f90:133-190, 222-237, 354-381 for a batch of beta values:
             to the lowest bead when one lies below well 1), log-det at
             the wells (single well, all eigenvalues) and at the instanton
             (lowest eigenvalue dropped), S = betan UM, Omega and Delta.
+run_rpi_angular -- rpi_ser.f90:241-348: the solid-angle grid for one beta.
 crossover_beta -- crossover.f90:49-71: beta_c of a transition state.
 multiwell_levels -- python_utils/multiwell_waterdimer.py: splittings per
             irreducible representation from path ratios at two temperatures.
@@ -465,3 +466,73 @@ def run_rpi(cfg, N=None, betas=None, m=8, factr=1.0e6, pgtol=1.0e-5, maxiter=200
                         lndetJ=float(ld[k]), lndetJ0=float(ld0[k]), eta2_min=float(emin[k]),
                         skipped=int(nsk[k]), iterations=int(it[k]), status=int(st[k])))
     return dict(N=N, results=out, x=x, vpath=vpath, optimize_s=t_opt, logdet_s=t_det)
+
+
+def _rotate(w, ndim, axis, theta):
+    """rotate_atoms (instantonmod.f90:346-376) on x[atom*ndim + dim]; in 2-D the
+    rotation in the plane (axis 3)."""
+    import align
+    if ndim == 3:
+        return align.rotate_atoms(np.asarray(w, float).reshape(-1, 3), axis, theta).ravel()
+    if abs(theta) <= 1.0e-10:
+        return np.asarray(w, float)
+    v = np.asarray(w, float).reshape(-1, 2)
+    c, s = np.cos(theta), np.sin(theta)
+    return np.stack([c * v[:, 0] + s * v[:, 1], -s * v[:, 0] + c * v[:, 1]], axis=1).ravel()
+
+
+def run_rpi_angular(cfg, N, beta, npoints, cutofftheta=2.0 * 3.14159265358979, cutoffphi=3.14159265358979,
+                    m=8, factr=1.0e6, pgtol=1.0e-5, maxiter=200000, quirks=False, device=0, ctx=None, path=None):
+    """The solid-angle grid of rpi_ser.f90:241-348 for one beta, as the namelist
+    driver runs it: the instanton of run_rpi, then well 2 turned by
+    R_x(theta) R_z(phi) R_x(eta) at Gauss-Legendre angles (3-D; in 2-D by eta in
+    the plane), every orientation re-optimised from that instanton in one batched
+    call, log-dets with the lowest eigenvalue left out, and per orientation
+    I = tanh(Omega N) (3-D: 1 when Omega N > 1).  Returns the rows of
+    angularI.dat: (theta, phi, eta, weight, I) in 3-D, (eta, weight, I) in 2-D."""
+    c = dict(cfg)
+    ndim = c["ndim"]
+    if ndim not in (2, 3):
+        raise ValueError("the angular grid needs ndim = 2 or 3")
+    own = ctx is None
+    if own:
+        ctx = pg.Context(device)
+    try:
+        base = run_rpi(c, N=N, betas=[beta], m=m, factr=factr, pgtol=pgtol, maxiter=maxiter, quirks=quirks,
+                       ctx=ctx, path=path)
+        ld0 = base["results"][0]["lndetJ0"]
+        vshift = min(float(np.min(base["vpath"])), 0.0)
+        betan = beta / N
+        w1, w2 = np.asarray(c["well1"], float), np.asarray(c["well2"], float)
+        et, wet = pg.gauleg(0.0, min(2.0 * 3.14159265358979, cutofftheta), npoints)
+        rows, ends = [], []
+        if ndim == 3:
+            th, wth = et, wet
+            ph, wph = pg.gauleg(0.0, min(3.14159265358979, cutoffphi), npoints)
+            for ii in range(npoints):
+                for jj in range(npoints):
+                    for kk in range(npoints):
+                        w = _rotate(_rotate(_rotate(w2, 3, 1, et[kk]), 3, 3, ph[jj]), 3, 1, th[ii])
+                        ends.append(w)
+                        rows.append([th[ii], ph[jj], et[kk], wth[ii] * wph[jj] * wet[kk]])
+        else:
+            for kk in range(npoints):
+                ends.append(_rotate(w2, 2, 3, et[kk]))
+                rows.append([et[kk], wet[kk]])
+        nb = len(ends)
+        xs = np.tile(np.asarray(base["x"], float), nb)
+        bn = np.full(nb, betan)
+        xs, UM, _, _ = ctx.instanton_optimize(N, xs, w1, np.concatenate(ends), bn, m=m, factr=factr, pgtol=pgtol,
+                                              maxiter=maxiter)
+        ld, _, _ = ctx.instanton_logdet(N, xs, bn, singlewell=False, skip_lowest=True, quirks=quirks)
+    finally:
+        if own:
+            ctx.close()
+    out = []
+    for q in range(nb):
+        _, om, _ = pg.rpi_assemble(betan, UM[q] - N * vshift, ld[q], ld0)
+        ib = np.tanh(om * N)
+        if ndim == 3 and om * N > 1.0:
+            ib = 1.0
+        out.append(rows[q] + [float(ib)])
+    return np.array(out)

@@ -58,6 +58,11 @@ elif job["kind"] == "ti_restart":
     r = drivers.run_ti(c, precision=pg.PG_FP64, form=pg.PG_FORM_FUSED, nmc=job["nmc"], nrep=3,
                        restart=job["restart"], nproc=2, labels=["H"], directory=job["dir"], chunk=30)
     out = dict(dA=r["dA"])
+elif job["kind"] == "angular":
+    c = pgconfigs.load(job["cfg"])
+    rows = drivers.run_rpi_angular(c, job["N"], job["beta"], job["npoints"], cutofftheta=job["ct"],
+                                   cutoffphi=job["cp"])
+    out = dict(rows=rows.tolist())
 elif job["kind"] == "crossover":
     c = pgconfigs.load("c1")
     ctx = pg.Context(0)
@@ -319,3 +324,27 @@ def test_run_ti_reports_a_nan_ring(oracle, run_job):
     x, p = oracle.ring_init(pes, c["mass"], prm, ti.xref[0], 0, 0, a=ti.a, b=ti.b[0])
     res = oracle.ring_propagate(pes, c["mass"], prm, ti.a, ti.b[0], ti.dbdl[0], ti.xref[0], 0, 0, 0, 300, x, p)
     assert out["mean"][0] == pytest.approx(res.dhdr_sum / res.nsamples / ti.betan ** 2, rel=1e-12)
+
+
+@pytest.mark.parametrize("cfg,npts", [("c3", 2), ("c1", 4)])
+def test_run_rpi_angular_matches_the_namelist_driver(oracle, run_job, tmp_path, cfg, npts):
+    """run_rpi_angular and rpi.cpp with angular = T give the same angularI.dat
+    rows (3-D: c3's 9-atom surface; 2-D: c1), both through the stand-in."""
+    import standin
+    c = pgconfigs.load(cfg)
+    n, beta, ct, cp = 4, 40.0, 1.0, 0.5
+    out = run_job(dict(kind="angular", cfg=cfg, N=n, beta=beta, npoints=npts, ct=ct, cp=cp))
+    exe = standin.build_driver("rpi", tmp_path)
+    natom, ndim = c["natom"], c["ndim"]
+    (tmp_path / "masses.dat").write_text("".join("X%d %.17g\n" % (j, mm) for j, mm in enumerate(c["mass"])))
+    for name in ("well1", "well2"):
+        w = np.array(c[name]).reshape(natom, ndim)
+        (tmp_path / (name + ".dat")).write_text("".join(" ".join("%.17g" % v for v in row) + "\n" for row in w))
+    (tmp_path / "pes.dat").write_text("\n".join("%.17g" % v for v in c["params"]) + "\n")
+    text = ("&RPIDATA n=%d, beta=%.17g, ndim=%d, natom=%d, readpath=.false., pes='%s', pes_params='pes.dat',\n"
+            " angular=.true., npoints=%d, cutofftheta=%.17g, cutoffphi=%.17g /\n"
+            % (n, beta, ndim, natom, "synth9" if cfg == "c3" else "2dtest", npts, ct, cp))
+    r = subprocess.run([exe], input=text, capture_output=True, text=True, cwd=str(tmp_path), timeout=300)
+    assert r.returncode == 0, r.stderr
+    rows = np.loadtxt(str(tmp_path / "angularI.dat"))
+    np.testing.assert_allclose(np.array(out["rows"]), rows, rtol=1e-12, atol=1e-300)
