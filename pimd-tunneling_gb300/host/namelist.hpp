@@ -153,6 +153,19 @@ class Namelist {
     }
 };
 
+// Range checks of namelist values: each failed condition prints "namelist:
+// <what>" on err; returns false if any failed.
+struct RangeCheck {
+    std::ostream &err;
+    bool ok = true;
+    void need(bool cond, const char *what) {
+        if (!cond) {
+            err << "namelist: " << what << "\n";
+            ok = false;
+        }
+    }
+};
+
 inline std::string read_all(std::istream &in) {
     std::stringstream ss;
     ss << in.rdbuf();

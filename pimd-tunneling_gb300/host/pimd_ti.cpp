@@ -165,6 +165,21 @@ int main(int argc, char **argv) {
     const std::string tune = nl.str("tune", "");
     nl.accept({"use_mkl", "basename"});  // pimd_par.f90:43-44: no effect here
     if (!nl.check(std::cerr)) return 1;
+    {
+        RangeCheck rc{std::cerr};
+        rc.need(n >= 2, "n (beads) must be at least 2");
+        rc.need(beta > 0.0, "beta must be positive");
+        rc.need(dt > 0.0, "dt must be positive");
+        rc.need(tau > 0.0, "tau must be positive");
+        rc.need(gamma >= 0.0, "gamma must not be negative");
+        rc.need(NMC >= 0 && imin >= 0, "NMC and imin must not be negative");
+        rc.need(nintegral >= 1 && nrep >= 1, "nintegral and nrep must be at least 1");
+        rc.need(ndim >= 1 && natom >= 1, "ndim and natom must be at least 1");
+        rc.need(thermostat == 1 || thermostat == 2, "thermostat must be 1 (Andersen) or 2 (Langevin)");
+        rc.need(chunk >= 1, "chunk must be at least 1");
+        rc.need(!readpath || npath == 0 || npath >= 2, "npath must be at least 2 with readpath");
+        if (!rc.ok) return 1;
+    }
     if (parse_only) {
         std::printf("{\"n\": %lld, \"beta\": %.17g, \"NMC\": %lld, \"Noutput\": %lld, \"dt\": %.17g, "
                     "\"nintegral\": %lld, \"nrep\": %lld, \"thermostat\": %d, \"ndim\": %d, \"natom\": %d, "

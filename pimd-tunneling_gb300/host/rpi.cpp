@@ -74,6 +74,15 @@ int main(int argc, char **argv) {
     const bool fixedends = nl.logical("fixedends", true) || angular;
     nl.accept({"alignpath", "basename"});  // rpi_ser.f90:23: no effect in the reference's flow
     if (!nl.check(std::cerr)) return 1;
+    {
+        RangeCheck rc{std::cerr};
+        rc.need(n >= 2, "n (beads) must be at least 2");
+        rc.need(beta > 0.0, "beta must be positive");
+        rc.need(ndim >= 1 && natom >= 1, "ndim and natom must be at least 1");
+        rc.need(m >= 1 && maxiter >= 1, "m and maxiter must be at least 1");
+        rc.need(!angular || npoints >= 1, "npoints must be at least 1");
+        if (!rc.ok) return 1;
+    }
     const int atom1 = (int)nl.integer("atom1", 1), atom2 = (int)nl.integer("atom2", 2),
               atom3 = (int)nl.integer("atom3", 3);  // rpi_par.f90:53-55
     if (parse_only) {

@@ -83,6 +83,12 @@ def test_namelist_errors_stop_the_run(drivers_built):
     assert json.loads(r.stdout)["fixedends"] is True  # rpi_ser.f90:53
     r = _run("crossover", "&CROSSDATA ndim=2, natom=1, nmc=3 /", args=["--parse-only"])
     assert r.returncode == 1 and "unknown key 'nmc'" in r.stderr
+    # values out of range stop the programs with every problem named
+    r = _run("pimd_ti", "&MCDATA n=1, dt=-0.1, thermostat=3 /", args=["--parse-only"])
+    assert r.returncode == 1
+    assert all(w in r.stderr for w in ("n (beads)", "dt must be positive", "thermostat must be"))
+    r = _run("rpi", "&RPIDATA n=100, beta=0 /", args=["--parse-only"])
+    assert r.returncode == 1 and "beta must be positive" in r.stderr
 
 
 def test_driver_fails_loudly_without_gpu(drivers_built, tmp_path):
