@@ -353,12 +353,12 @@ int main(int argc, char **argv) {
             std::copy(w.begin(), w.end(), bb.begin() + q * nd);
             std::copy(x.begin(), x.end(), xs.begin() + q * nd * n);
         }
-        std::vector<double> um(nb), ld(nb);
-        std::vector<int64_t> its(nb), nsk(nb);
+        std::vector<double> um(nb), lda(nb);
+        std::vector<int64_t> its(nb), nska(nb);
         std::vector<int32_t> sts(nb);
         CHECK(pg_instanton_optimize(ctx, nb, n, xs.data(), w1.data(), bb.data(), bn.data(), &o, um.data(), its.data(),
                                     sts.data()));
-        CHECK(pg_instanton_logdet(ctx, nb, n, xs.data(), bn.data(), 0, 1, quirks, ld.data(), nullptr, nsk.data()));
+        CHECK(pg_instanton_logdet(ctx, nb, n, xs.data(), bn.data(), 0, 1, quirks, lda.data(), nullptr, nska.data()));
         FILE *fa = std::fopen("angularI.dat", "w");
         if (!fa) {
             std::fprintf(stderr, "cannot write angularI.dat\n");
@@ -387,16 +387,16 @@ int main(int argc, char **argv) {
         }
         for (int64_t q = 0; q < nb; q++) {
             double Sq, om, dq;
-            CHECK(pg_rpi_assemble(betan, um[q] - (double)n * vshift, ld[q], ld0, &Sq, &om, &dq));
+            CHECK(pg_rpi_assemble(betan, um[q] - (double)n * vshift, lda[q], ld0, &Sq, &om, &dq));
             double ib = std::tanh(om * (double)n);
             if (three && om * (double)n > 1.0) ib = 1.0;
             if (three) {
                 std::fprintf(fa, " %.17g %.17g %.17g %.17g %.17g\n", ang[3 * q], ang[3 * q + 1], ang[3 * q + 2], wts[q], ib);
                 std::printf(" %.10g %.10g %.10g %.10g %.10g %.15g\n", ang[3 * q], ang[3 * q + 1], ang[3 * q + 2], wts[q],
-                            ib, ld[q]);
+                            ib, lda[q]);
             } else {
                 std::fprintf(fa, " %.17g %.17g %.17g\n", ang[3 * q + 2], wts[q], ib);
-                std::printf(" %.10g %.10g %.10g %.15g %.15g\n", ang[3 * q + 2], wts[q], ib, ld[q], Sq);
+                std::printf(" %.10g %.10g %.10g %.15g %.15g\n", ang[3 * q + 2], wts[q], ib, lda[q], Sq);
             }
         }
         std::fclose(fa);
