@@ -21,6 +21,7 @@
 #include <algorithm>
 
 #include <cstdio>
+#include <mutex>
 #include <vector>
 
 #include "pg_internal.h"
@@ -2218,15 +2219,17 @@ int tc_nm_transform(pg_ctx *ctx, int64_t P, int64_t ncol, const double *in, doub
 }  // namespace pg
 
 // ---------------------------------------------------------------- allocation-free transform
-// Some callers cannot call cudaMalloc: a host application that hands all device
-// memory to its own pool allocator at start-up (an MPI / Fortran driver that
-// pre-allocates the GPU), or code that must not allocate while a CUDA graph is
-// being captured or a latency-critical stream is running, because cudaMalloc
-// can synchronise the device.  For them, pg_nm_transform_noalloc runs the
+// Some callers cannot call cudaMalloc.  A Fortran or MPI host program often
+// hands all of the GPU's memory to its own pool allocator at start-up and sizes
+// every device array once, so a library allocation would fail or fragment that
+// pool; other callers run inside a section where cudaMalloc's implicit device
+// synchronisation is not allowed.  For them, pg_nm_transform_noalloc runs the
 // split-BF16 tcgen05 transform on caller-owned device buffers and keeps its only
 // scratch -- the 64 KB split-BF16 image of T and an error word -- in the static
 // device array below, sized for P = 128 (every GPU that loads the library holds
-// it until the process exits).
+// it until the process exits).  The first call on each device builds the image
+// there (make that first call before any stream capture); calls that overlap on
+// the GPU share the array and race.
 namespace pg {
 namespace {
 constexpr size_t kNoAllocScratchBytes = 2 * (size_t)kOpBytes + 256;  // image + error word
@@ -2234,6 +2237,7 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 constexpr int kMaxDevices = 64;
 static void *g_noalloc_ptr[kMaxDevices];  // device address of g_noalloc_scratch, per device
 static bool g_noalloc_ready[kMaxDevices];
+static std::mutex g_noalloc_setup;  // one host thread at a time runs a device's set-up
 }  // namespace
 }  // namespace pg
 
@@ -2243,26 +2247,30 @@ extern "C" int pg_nm_transform_noalloc(int64_t P, int64_t ncol, const double *d_
     if (P != kP)
         return fail(PG_ERR_ARG, "pg_nm_transform_noalloc: the static scratch holds one 128 x 128 split-BF16 "
                                 "image, so P must be 128");
-    if (ncol < 0 || ncol > ((int64_t)1 << 31) * kRows) return fail(PG_ERR_ARG, "pg_nm_transform_noalloc: bad ncol");
+    if (ncol < 0 || ncol > (((int64_t)1 << 31) - 1) * kRows)  // grid.x <= 2^31 - 1
+        return fail(PG_ERR_ARG, "pg_nm_transform_noalloc: bad ncol");
     if (ncol == 0) return PG_OK;
     if (!d_in || !d_out) return fail(PG_ERR_ARG, "pg_nm_transform_noalloc: NULL device buffer");
     int dev = 0;
     PG_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kMaxDevices) return fail(PG_ERR_ARG, "pg_nm_transform_noalloc: device index too large");
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-    if (!g_noalloc_ready[dev]) {
-        // one-time set-up on this device (must come before any stream capture):
-        // the host-side name of the array is not a device address; ask the runtime.
-        void *ptr = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
-        k_build_split_image<<<(kP * kP + 255) / 256, 256, 0, s>>>(reinterpret_cast<unsigned char *>(ptr));
-        PG_CUDA(cudaGetLastError());
-        PG_CUDA(cudaStreamSynchronize(s));
-        size_t sm = (size_t)kSmemOps + 1024 + sizeof(TcShared) + 64;
-        PG_CUDA(cudaFuncSetAttribute(k_tc_transform, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        g_noalloc_ptr[dev] = ptr;
-        g_noalloc_ready[dev] = true;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_setup);
+        if (!g_noalloc_ready[dev]) {
+            // one-time set-up on this device (make it before any stream capture):
+            // the host-side name of the array is not a device address; ask the runtime.
+            void *ptr = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+            if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+            k_build_split_image<<<(kP * kP + 255) / 256, 256, 0, s>>>(reinterpret_cast<unsigned char *>(ptr));
+            PG_CUDA(cudaGetLastError());
+            PG_CUDA(cudaStreamSynchronize(s));
+            size_t sm = (size_t)kSmemOps + 1024 + sizeof(TcShared) + 64;
+            PG_CUDA(cudaFuncSetAttribute(k_tc_transform, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            g_noalloc_ptr[dev] = ptr;
+            g_noalloc_ready[dev] = true;
+        }
     }
     unsigned char *img = reinterpret_cast<unsigned char *>(g_noalloc_ptr[dev]);
     int32_t *derr = reinterpret_cast<int32_t *>(img + 2 * kOpBytes);

@@ -1,7 +1,8 @@
 """The allocation-free transform entry point (pg_nm_transform_noalloc).
 
-Callers whose device memory belongs to their own pool allocator, or that run
-while a CUDA graph is being captured, cannot call cudaMalloc; this entry point
+Some callers cannot call cudaMalloc: a Fortran / MPI host program that gives
+all of the GPU's memory to its own pool at start-up, or code in a section where
+cudaMalloc's implicit device synchronisation is not allowed.  This entry point
 uses only a static device array for its scratch.  The test calls it through the
 C-ABI on caller-owned device buffers, twice in a row (the scratch keeps the
 previous call's contents), and compares each result with the allocating entry
