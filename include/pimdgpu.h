@@ -98,16 +98,18 @@ int pg_nm_transform(pg_ctx *ctx, int64_t P, int64_t ncol, const double *in, doub
                     int32_t precision);
 
 /* Allocation-free variant of the split-BF16 tcgen05 transform (pg_nm_transform
- * with PG_MIXED, P = 128), for callers that cannot call cudaMalloc: applications
- * whose device memory is owned by their own pool allocator, or code running
- * while a CUDA graph is captured.  No counterpart in the reference.  d_in / d_out
- * are caller-owned device buffers of ncol*128 doubles; stream is a cudaStream_t
- * (NULL = default stream); synchronous at return.  The only scratch is a static
- * 64 KB device array (the split image of T plus an error word) that every GPU
- * loading the library holds until exit; P must be 128 (anything else is
- * PG_ERR_ARG).  The first call on a device builds the image there, so make it
- * before any stream capture.  All calls share the array: calls that overlap on
- * the GPU race.  Allocates no device or pinned memory. */
+ * with PG_MIXED, P = 128).  No counterpart in the reference.  It is for callers
+ * that cannot call cudaMalloc: a Fortran / MPI host program that gives all of
+ * the GPU's memory to its own pool allocator at start-up, or code in a section
+ * where cudaMalloc's implicit device synchronisation is not allowed.  d_in /
+ * d_out are caller-owned device buffers of ncol*128 doubles; stream is a
+ * cudaStream_t (NULL = default stream); synchronous at return.  The only
+ * scratch is a static 64 KB device array (the split image of T plus an error
+ * word) that every GPU loading the library holds until exit; P must be 128
+ * (anything else is PG_ERR_ARG).  The first call on a device builds the image
+ * there; make that first call before any stream capture.  All calls share the
+ * array: calls that overlap on the GPU race.  Allocates no device or pinned
+ * memory. */
 int pg_nm_transform_noalloc(int64_t P, int64_t ncol, const double *d_in, double *d_out, void *stream);
 
 /* ---------------------------------------------------------------- TI-PIMD */
@@ -257,9 +259,18 @@ typedef struct pg_lbfgs_opts {
     double pgtol;            /* gradient infinity-norm tolerance (reference eps2) */
 } pg_lbfgs_opts;
 
+/* Fixed or free end points of the polymer action (instantonmod's module
+ * variable fixedends, instantonmod.f90:7; namelist key fixedends of
+ * rpi_ser.f90:23 and pimd_par.f90:44).  1 (default): springs of m/(2 betan^2)
+ * tie bead 1 to a and bead N to b.  0: no end springs, so an end bead feels only
+ * its one neighbour (instantonmod.f90:35-44, 63-72, 115-124, 138-151); a and b
+ * may then be NULL in pg_instanton_fg / pg_instanton_optimize.  Applies to those
+ * two calls; the Hessian of pg_um_hessian / pg_instanton_logdet is the same
+ * either way, as UMhessian is. */
+int pg_set_fixedends(pg_ctx *ctx, int32_t fixedends);
 /* Batched UMforceenergy over nbeta independent polymers (instantonmod.f90:17-151):
  * x[nbeta*ndof*N], UM[nbeta], grad[nbeta*ndof*N] (either may be NULL);
- * fixed ends a[ndof], b[nbeta*ndof]; betan[nbeta]. */
+ * end points a[ndof], b[nbeta*ndof] (NULL allowed with free ends); betan[nbeta]. */
 int pg_instanton_fg(pg_ctx *ctx, int64_t nbeta, int64_t N, const double *x, const double *a,
                     const double *b, const double *betan, double *UM, double *grad);
 /* Batched instanton optimisation (instantonmod.f90:679-777) by an on-device FP64

@@ -321,12 +321,18 @@ def logdet_band(band, skip_lowest):
     return float(np.sum(np.log(ww[pos]))), int(np.sum(~pos)), float(w[0])
 
 
-def instanton_lbfgs(pes, mass, N, betan, x0, a, b, m=8, factr=1.0e6, pgtol=1.0e-5, maxiter=15000):
-    """scipy L-BFGS-B on UM, unbounded (instantonmod.f90:679-777)."""
+def instanton_lbfgs(pes, mass, N, betan, x0, a, b, m=8, factr=1.0e6, pgtol=1.0e-5, maxiter=15000,
+                    fixedends=True):
+    """scipy L-BFGS-B on UM, unbounded (instantonmod.f90:679-777); with
+    fixedends False the action without the end-point springs (a, b unused)."""
     from scipy.optimize import minimize
+    nd = pes.ndim * pes.natom
+    if not fixedends:
+        a = np.zeros(nd) if a is None else a
+        b = np.zeros(nd) if b is None else b
 
     def fg(x):
-        v, g = UMforceenergy(pes, mass, N, betan, x, a, b, True)
+        v, g = UMforceenergy(pes, mass, N, betan, x, a, b, fixedends)
         return v, g
 
     r = minimize(fg, _f64(x0), jac=True, method="L-BFGS-B",

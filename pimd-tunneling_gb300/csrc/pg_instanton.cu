@@ -24,6 +24,7 @@ namespace {
 struct InstArgs {
     PesArgs pes;
     int N, nd, ndim, natom;
+    int fixedends;        // 0: no springs to a and b (instantonmod.f90:35-44, 63-72, 115-124, 138)
     const double *mass;   // natom
     const double *a;      // nd, fixed start
     const double *b;      // nbeta*nd, fixed ends
@@ -67,17 +68,20 @@ __device__ double polymer_fg(const InstArgs &A, int k, const double *__restrict_
         for (int d = 0; d < nd; d++) g[d * N + i] = gb[d];
     }
     __syncthreads();
-    // springs between neighbours and to the fixed ends (instantonmod.f90:25-43, 59-78)
+    // springs between neighbours and, with fixed ends, to a and b
+    // (instantonmod.f90:25-43, 59-78); free ends: an end bead has one neighbour,
+    // m (x_1 - x_2) / betan^2 and m (x_N - x_N-1) / betan^2 (instantonmod.f90:66, 72)
+    const bool fixed = A.fixedends != 0;
     for (int e = threadIdx.x; e < nd * N; e += blockDim.x) {
         const int dof = e / N, i = e - dof * N;
         const double m = A.mass[dof / A.ndim];
-        const double xl = i > 0 ? x[e - 1] : A.a[dof];
-        const double xr = i < N - 1 ? x[e + 1] : b[dof];
+        const double xl = i > 0 ? x[e - 1] : (fixed ? A.a[dof] : x[e]);
+        const double xr = i < N - 1 ? x[e + 1] : (fixed ? b[dof] : x[e]);
         g[e] = m * (2.0 * x[e] - xl - xr) / (bn * bn) + g[e];
         const double c = 0.5 * m / (bn * bn);
         if (i < N - 1) part += c * (x[e + 1] - x[e]) * (x[e + 1] - x[e]);
-        if (i == 0) part += c * (x[e] - A.a[dof]) * (x[e] - A.a[dof]);
-        if (i == N - 1) part += c * (b[dof] - x[e]) * (b[dof] - x[e]);
+        if (fixed && i == 0) part += c * (x[e] - A.a[dof]) * (x[e] - A.a[dof]);
+        if (fixed && i == N - 1) part += c * (b[dof] - x[e]) * (b[dof] - x[e]);
     }
     double um = block_sum(part, sred);
     __syncthreads();
@@ -475,6 +479,7 @@ InstArgs make_inst_args(pg_ctx *ctx, int N, const double *da, const double *db, 
     InstArgs A;
     A.pes = ctx->pes_args();
     A.N = N;
+    A.fixedends = ctx->fixedends;
     A.nd = ctx->nd;
     A.ndim = ctx->ndim;
     A.natom = ctx->natom;
@@ -517,20 +522,46 @@ static int upload(pg_ctx *ctx, DevBuf &buf, const double *h, size_t n) {
     return PG_OK;
 }
 
+// [a (nd) | b (nbeta nd) | betan (nbeta)] on the device.  With free ends
+// (pg_set_fixedends(ctx, 0)) a and b may be NULL: the action never reads them,
+// and zeros stand in (the reference passes neither, instantonmod.f90:756-762).
+static int upload_ends(pg_ctx *ctx, DevBuf &dab, int64_t nbeta, const double *a, const double *b,
+                       const double *betan) {
+    const int nd = ctx->nd;
+    if (ctx->fixedends && (!a || !b)) return fail(PG_ERR_ARG, "fixed ends need the end points a and b");
+    PG_CUDA(dab.ensure((size_t)(nd + nbeta * nd + nbeta) * sizeof(double)));
+    if (a)
+        PG_CUDA(cudaMemcpyAsync(dab.ptr, a, nd * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    else
+        PG_CUDA(cudaMemsetAsync(dab.ptr, 0, nd * sizeof(double), ctx->stream));
+    if (b)
+        PG_CUDA(cudaMemcpyAsync(dab.as<double>() + nd, b, nbeta * nd * sizeof(double), cudaMemcpyHostToDevice,
+                                ctx->stream));
+    else
+        PG_CUDA(cudaMemsetAsync(dab.as<double>() + nd, 0, nbeta * nd * sizeof(double), ctx->stream));
+    PG_CUDA(cudaMemcpyAsync(dab.as<double>() + nd + nbeta * nd, betan, nbeta * sizeof(double), cudaMemcpyHostToDevice,
+                            ctx->stream));
+    return PG_OK;
+}
+
+extern "C" int pg_set_fixedends(pg_ctx *ctx, int32_t fixedends) {
+    int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    if (fixedends != 0 && fixedends != 1) return fail(PG_ERR_ARG, "fixedends must be 0 or 1");
+    ctx->fixedends = fixedends;
+    return PG_OK;
+}
+
 extern "C" int pg_instanton_fg(pg_ctx *ctx, int64_t nbeta, int64_t N, const double *x, const double *a,
                                const double *b, const double *betan, double *UM, double *grad) {
     int rc = check_ctx(ctx, true);
     if (rc) return rc;
-    if (nbeta < 1 || N < 2 || !x || !a || !b || !betan) return fail(PG_ERR_ARG, "bad instanton_fg arguments");
+    if (nbeta < 1 || N < 2 || !x || !betan) return fail(PG_ERR_ARG, "bad instanton_fg arguments");
     const int nd = ctx->nd;
     const size_t n = (size_t)nbeta * nd * N;
     DevBuf dx, dg, dab, dum;
     if ((rc = upload(ctx, dx, x, n))) return rc;
-    PG_CUDA(dab.ensure((size_t)(nd + nbeta * nd + nbeta) * sizeof(double)));
-    PG_CUDA(cudaMemcpyAsync(dab.ptr, a, nd * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-    PG_CUDA(cudaMemcpyAsync(dab.as<double>() + nd, b, nbeta * nd * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-    PG_CUDA(cudaMemcpyAsync(dab.as<double>() + nd + nbeta * nd, betan, nbeta * sizeof(double), cudaMemcpyHostToDevice,
-                            ctx->stream));
+    if ((rc = upload_ends(ctx, dab, nbeta, a, b, betan))) return rc;
     PG_CUDA(dg.ensure(n * sizeof(double)));
     PG_CUDA(dum.ensure(nbeta * sizeof(double)));
     InstArgs A = make_inst_args(ctx, (int)N, dab.as<double>(), dab.as<double>() + nd, dab.as<double>() + nd + nbeta * nd);
@@ -548,18 +579,14 @@ extern "C" int pg_instanton_optimize(pg_ctx *ctx, int64_t nbeta, int64_t N, doub
     NvtxRange nvtx_range("pg_instanton_optimize");
     int rc = check_ctx(ctx, true);
     if (rc) return rc;
-    if (nbeta < 1 || N < 2 || !x || !a || !b || !betan || !opts) return fail(PG_ERR_ARG, "bad optimize arguments");
+    if (nbeta < 1 || N < 2 || !x || !betan || !opts) return fail(PG_ERR_ARG, "bad optimize arguments");
     if (opts->m < 1 || opts->m > 64 || opts->maxiter < 1 || opts->max_backtracks < 0)
         return fail(PG_ERR_ARG, "bad L-BFGS options");
     const int nd = ctx->nd;
     const size_t n1 = (size_t)nd * N, n = (size_t)nbeta * n1;
     DevBuf dx, dab, dum, dit, dst;
     if ((rc = upload(ctx, dx, x, n))) return rc;
-    PG_CUDA(dab.ensure((size_t)(nd + nbeta * nd + nbeta) * sizeof(double)));
-    PG_CUDA(cudaMemcpyAsync(dab.ptr, a, nd * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-    PG_CUDA(cudaMemcpyAsync(dab.as<double>() + nd, b, nbeta * nd * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-    PG_CUDA(cudaMemcpyAsync(dab.as<double>() + nd + nbeta * nd, betan, nbeta * sizeof(double), cudaMemcpyHostToDevice,
-                            ctx->stream));
+    if ((rc = upload_ends(ctx, dab, nbeta, a, b, betan))) return rc;
     const size_t per = (size_t)(5 + 2 * opts->m) * n1 + 2 * opts->m;
     PG_CUDA(ctx->scratch_b.ensure((size_t)nbeta * per * sizeof(double)));
     PG_CUDA(dum.ensure(nbeta * sizeof(double)));

@@ -133,6 +133,9 @@ struct pg_ctx {
     // autotuning of AUTO batches (pg_set_tuning): JSON-lines cache file and mode
     std::string tune_path;
     int tune_mode = 0;
+    // instantonmod's module variable fixedends (instantonmod.f90:7): with 0 the
+    // polymer action drops the springs to the end points a, b (pg_set_fixedends)
+    int fixedends = 1;
     pg::PesArgs pes_args() const {
         pg::PesArgs pa;
         pa.id = pes_id;

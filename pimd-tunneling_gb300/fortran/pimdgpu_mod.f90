@@ -290,13 +290,21 @@ module pimdgpu
        real(c_double), intent(out) :: dA, sigmaA, qratio
      end function pg_ti_assemble
 
-     ! instanton: UMforceenergy, instanton, UMhessian, detJ + log sums
+     ! instanton: fixedends, UMforceenergy, instanton, UMhessian, detJ + log sums
+     integer(c_int) function pg_set_fixedends(ctx, fixedends) bind(c, name="pg_set_fixedends")
+       import :: c_int, c_int32_t, c_ptr
+       type(c_ptr), value :: ctx
+       integer(c_int32_t), value :: fixedends
+     end function pg_set_fixedends
+
+     ! a and b are optional (passed as NULL when absent, Fortran 2018) for free ends
      integer(c_int) function pg_instanton_fg(ctx, nbeta, N, x, a, b, betan, UM, grad) &
           bind(c, name="pg_instanton_fg")
        import :: c_int, c_int64_t, c_double, c_ptr
        type(c_ptr), value :: ctx
        integer(c_int64_t), value :: nbeta, N
-       real(c_double), intent(in) :: x(*), a(*), b(*), betan(*)
+       real(c_double), intent(in) :: x(*), betan(*)
+       real(c_double), intent(in), optional :: a(*), b(*)
        real(c_double), intent(out) :: UM(*), grad(*)
      end function pg_instanton_fg
 
@@ -306,7 +314,8 @@ module pimdgpu
        type(c_ptr), value :: ctx
        integer(c_int64_t), value :: nbeta, N
        real(c_double), intent(inout) :: x(*)
-       real(c_double), intent(in) :: a(*), b(*), betan(*)
+       real(c_double), intent(in) :: betan(*)
+       real(c_double), intent(in), optional :: a(*), b(*)
        type(pg_lbfgs_opts), intent(in) :: opts
        real(c_double), intent(out) :: UM(*)
        integer(c_int64_t), intent(out) :: niter(*)

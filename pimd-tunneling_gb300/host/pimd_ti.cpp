@@ -308,11 +308,8 @@ int main(int argc, char **argv) {
     if (instapath) {
         // instanton from the path guess (instantonmod.f90:945-983): beads at
         // xi = (k-1)/(n-1) on the spline, optimised with fixed ends at the wells
-        // (the action's betan is that of the driver, pimd_par.f90:94)
-        if (!fixedends) {
-            std::fprintf(stderr, "instapath needs fixedends = .true. (the free-ended action is not built)\n");
-            return 1;
-        }
+        // or, with fixedends = F, free-ended (instanton(xtilde)); the action's
+        // betan is that of the driver (pimd_par.f90:94)
         const int64_t npf = (int64_t)frames.size();
         std::vector<double> xt((size_t)nd * n), yk(npf), y2k(npf);
         for (int k = 0; k < nd; k++) {
@@ -332,16 +329,22 @@ int main(int argc, char **argv) {
         double um = 0.0;
         int64_t it = 0;
         int32_t ist = 0;
-        CHECK(pg_instanton_optimize(ctx, 1, n, xt.data(), w1.data(), w2.data(), &betan, &o, &um, &it, &ist));
+        CHECK(pg_set_fixedends(ctx, fixedends ? 1 : 0));
+        CHECK(pg_instanton_optimize(ctx, 1, n, xt.data(), fixedends ? w1.data() : nullptr,
+                                    fixedends ? w2.data() : nullptr, &betan, &o, &um, &it, &ist));
+        CHECK(pg_set_fixedends(ctx, 1));
         std::printf(" Found instanton after %lld iterations (status %d).\n", (long long)it, ist);
         if (from_path) xtilde = xt;
-        frames.assign(1, w1);
+        // the new path: [well 1, beads, well 2] with fixed ends, the n beads
+        // alone with free ends (instantonmod.f90:959-970)
+        frames.clear();
+        if (fixedends) frames.push_back(w1);
         for (int64_t bead = 0; bead < n; bead++) {
             std::vector<double> f(nd);
             for (int k = 0; k < nd; k++) f[k] = xt[(size_t)k * n + bead];
             frames.push_back(f);
         }
-        frames.push_back(w2);
+        if (fixedends) frames.push_back(w2);
         FILE *fi = std::fopen("instanton.xyz", "w");
         if (fi) {
             for (int64_t bead = 0; bead < n; bead++) {
@@ -589,14 +592,25 @@ int main(int argc, char **argv) {
     for (auto s : status) bad += s != 0;
     std::printf(" final answers per integration point:\n");
     for (int64_t i = 0; i < nintegral; i++) std::printf(" %lld %.15g %.15g\n", (long long)(i + 1), xi[i], mean[i]);
+    // a lambda point whose rings were all left out (NaN-flagged, or no sample
+    // yet) has no estimate: stop rather than integrate a zero
+    for (int64_t i = 0; i < nintegral; i++)
+        if (cnt[i] <= 0) {
+            std::fprintf(stderr, "integration point %lld has no valid ring (all NaN-flagged or without samples)\n",
+                         (long long)(i + 1));
+            return 3;
+        }
     double dA, sA, q;
     CHECK(pg_ti_assemble(nintegral, wq.data(), mean.data(), var.data(), betan, &dA, &sA, &q));
+    // standard error of dA: sum w_i^2 var_i / n_i over the rings each point kept
+    // (the reference's sigmaA / nrep when every ring counts, pimd_par.f90:422)
+    double sA_n = 0.0;
+    for (int64_t i = 0; i < nintegral; i++) sA_n += wq[i] * wq[i] * var[i] / (double)cnt[i];
     // pimd_par.f90:420-424
     std::printf(" beta, betan, n= %.10g %.10g %lld\n", beta, betan, (long long)n);
-    std::printf(" final Delta A= %.15g +/- %.15g %.15g\n", dA, std::sqrt(sA), std::sqrt(sA / (double)nrep));
-    std::printf(" q/q0= %.15g %.15g %.15g\n", q, betan * std::sqrt(sA) * q, betan * std::sqrt(sA / (double)nrep) * q);
-    std::printf(" q0/q= %.15g %.15g %.15g\n", 1.0 / q, betan * std::sqrt(sA) / q,
-                betan * std::sqrt(sA / (double)nrep) / q);
+    std::printf(" final Delta A= %.15g +/- %.15g %.15g\n", dA, std::sqrt(sA), std::sqrt(sA_n));
+    std::printf(" q/q0= %.15g %.15g %.15g\n", q, betan * std::sqrt(sA) * q, betan * std::sqrt(sA_n) * q);
+    std::printf(" q0/q= %.15g %.15g %.15g\n", 1.0 / q, betan * std::sqrt(sA) / q, betan * std::sqrt(sA_n) / q);
     double delta = 0.0;
     if (pg_splitting_from_ratio(beta, q, &delta) == PG_OK)
         std::printf(" splitting Delta= %.15g (%.10g cm-1)\n", delta, delta * 219474.63);

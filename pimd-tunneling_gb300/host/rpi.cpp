@@ -227,7 +227,11 @@ int main(int argc, char **argv) {
     double UM = 0.0;
     int64_t it = 0;
     int32_t st = 0;
-    CHECK(pg_instanton_optimize(ctx, 1, n, x.data(), w1.data(), w2.data(), &betan, &o, &UM, &it, &st));
+    // fixedends = F: the free-ended action, optimised without the end points
+    // (instanton(xtilde), instantonmod.f90:724-762)
+    CHECK(pg_set_fixedends(ctx, fixedends ? 1 : 0));
+    CHECK(pg_instanton_optimize(ctx, 1, n, x.data(), fixedends ? w1.data() : nullptr,
+                                fixedends ? w2.data() : nullptr, &betan, &o, &UM, &it, &st));
     std::printf(" Found instanton after %lld iterations (status %d).\n", (long long)it, st);
     // V along the instanton (rpi_ser.f90:180-190): when a bead lies below
     // well 1 the reference moves V0 to that bead's energy, which lowers every
@@ -278,15 +282,9 @@ int main(int argc, char **argv) {
         std::fclose(fi);
         std::fclose(fe);
     }
+    // S = betan UM(xtilde[, well1, well2]) (rpi_ser.f90:370-374): the optimiser's
+    // action, with or without the end springs as it was optimised
     UM -= (double)n * vshift;
-    if (!fixedends) {  // S from UM(xtilde) without the end-point springs (instantonmod.f90:17-46)
-        double e = 0.0;
-        for (int k = 0; k < nd; k++) {
-            const double d1 = x[(size_t)k * n] - w1[k], d2 = w2[k] - x[(size_t)k * n + n - 1];
-            e += mass[k / ndim] * (d1 * d1 + d2 * d2);
-        }
-        UM -= e / (2.0 * betan * betan);
-    }
     std::vector<double> xharm((size_t)nd * n);
     for (int k = 0; k < nd; k++)
         for (int64_t bead = 0; bead < n; bead++) xharm[(size_t)k * n + bead] = w1[k];

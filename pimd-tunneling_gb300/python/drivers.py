@@ -30,6 +30,29 @@ import pgconfigs
 import pimdgpu as pg
 
 
+def set_system_at_well1(ctx, c):
+    """Select the surface with V0 = V(well1) evaluated by the library in FP64,
+    as both reference drivers set it (pimd_par.f90:166, rpi_ser.f90:95) and the
+    namelist drivers do: every front end then hands the device the same energy
+    zero, so the L-BFGS objective (and its stopping test) is bit-identical."""
+    ctx.set_system(c["ndim"], c["natom"], c["mass"], c["pes_id"], c["params"], 0.0)
+    v0 = float(ctx.pes_eval(np.asarray(c["well1"], float).reshape(1, -1))[0][0])
+    ctx.set_system(c["ndim"], c["natom"], c["mass"], c["pes_id"], c["params"], v0)
+    return v0
+
+
+def _lambda_stderr2(w, var, cnt):
+    """sum_i w_i^2 var_i / n_i over the rings each lambda point kept (the
+    reference's sigmaA / nrep when every ring counts, pimd_par.f90:422); a point
+    whose rings were all left out (NaN-flagged or without samples) has no
+    estimate, and the run stops instead of integrating a zero."""
+    cnt = np.asarray(cnt)
+    if np.any(cnt <= 0):
+        raise RuntimeError("integration point(s) %s have no valid ring (all NaN-flagged or without samples)"
+                           % (np.nonzero(cnt <= 0)[0] + 1).tolist())
+    return float(np.sum(np.asarray(w) ** 2 * np.asarray(var) / cnt))
+
+
 def readhess_displacements(band, P, ndim, natom, mass, beta, z):
     """Bead displacements of init_path with readhess (verletmodule.f90:49-88).
 
@@ -108,13 +131,14 @@ def _bisect_top(dv, x1=0.3, x2=0.7, xacc=1.0e-6, jmax=40):
     return xm
 
 
-def ti_path_inputs(ctx, c, ti, frames, instapath=False, centre=False, init="path"):
+def ti_path_inputs(ctx, c, ti, frames, instapath=False, centre=False, init="path", fixedends=True):
     """The read_path flow of pimd_par (instantonmod.f90:895-1004, pimd_par.f90:212-221)
     for the batch ti (modified in place): the frames of path.xyz (3-D frames
     aligned by the first frame's angles) splined against normalised arc length;
     with instapath the instanton of that path guess (n = P beads at
-    (k-1)/(n-1), fixed ends at the wells, the driver's betan) replaces it as
-    [well 1, beads, well 2]; with centre the arc length is remapped so that the
+    (k-1)/(n-1), the driver's betan) replaces it: optimised with fixed ends at
+    the wells as [well 1, beads, well 2], or free-ended (fixedends False) as the
+    beads alone (instantonmod.f90:952-970); with centre the arc length is remapped so that the
     barrier top of V along the path sits at 1/2.  Then a = path(0), b_i =
     path(xi_i), dbdl_i = path'(xi_i) and the start beads at
     xi_eff = (k-1) xi_i / (P-1) (init 'path', verletmodule.f90:40-48) or at
@@ -135,9 +159,14 @@ def ti_path_inputs(ctx, c, ti, frames, instapath=False, centre=False, init="path
         y2 = splines(lam, fr)
         t = np.arange(P) / (P - 1)
         xt = np.concatenate([[pg.splint(lam, fr[:, d], y2[d], v)[0] for v in t] for d in range(nd)])
-        x, _, _, _ = ctx.instanton_optimize(P, xt, w1, w2, [ti.betan], m=8, factr=1.0e6, pgtol=1.0e-5,
-                                            maxiter=200000)
-        fr = np.vstack([w1, np.asarray(x).reshape(nd, P).T, w2])
+        ctx.set_fixedends(fixedends)
+        try:
+            x, _, _, _ = ctx.instanton_optimize(P, xt, w1 if fixedends else None, w2 if fixedends else None,
+                                                [ti.betan], m=8, factr=1.0e6, pgtol=1.0e-5, maxiter=200000)
+        finally:
+            ctx.set_fixedends(True)
+        beads = np.asarray(x).reshape(nd, P).T
+        fr = np.vstack([w1, beads, w2]) if fixedends else beads
         lam = _arc_length(fr)
     xm = None
     if centre:
@@ -235,7 +264,7 @@ def read_restart_files(c, nrings, P, nproc=1, directory="."):
 def run_ti(cfg, precision=pg.PG_MIXED, form=pg.PG_FORM_AUTO, nmc=None, nrep=None, nintegral=None,
            seed_offset=0, chunk=2000, device=0, ctx=None, verbose=False, tune=None, readhess=False,
            frames=None, instapath=False, centre=False, init="well", restart=0, nproc=1, labels=None,
-           directory="."):
+           directory=".", fixedends=True):
     c = dict(cfg)
     if nrep is not None:
         c["nrep"] = nrep
@@ -247,10 +276,10 @@ def run_ti(cfg, precision=pg.PG_MIXED, form=pg.PG_FORM_AUTO, nmc=None, nrep=None
     if own:
         ctx = pg.Context(device)
     try:
-        ctx.set_system(c["ndim"], c["natom"], c["mass"], c["pes_id"], c["params"], c["V0"])
+        set_system_at_well1(ctx, c)
         if frames is not None or instapath or centre:  # path.xyz / instanton / centring
             ti_path_inputs(ctx, c, ti, frames if frames is not None else [c["well1"], c["well2"]],
-                           instapath=instapath, centre=centre, init=init)
+                           instapath=instapath, centre=centre, init=init, fixedends=fixedends)
         tcfg = ti.ti_config(pg, precision, form)
         if tune:  # autotuner cache (AUTO form): tuned on the first batch of each shape
             ctx.set_tuning(tune, pg.PG_TUNE_ON)
@@ -291,13 +320,14 @@ def run_ti(cfg, precision=pg.PG_MIXED, form=pg.PG_FORM_AUTO, nmc=None, nrep=None
     finally:
         if own:
             ctx.close()
+    se2 = _lambda_stderr2(ti.w, var, cnt)
     dA, sigA, q = pg.ti_assemble(ti.w, mean, var, ti.betan)
     try:
         delta = pg.splitting_from_ratio(c["beta"], q)
     except pg.PgError:
         delta = float("nan")
     lnq = -dA * ti.betan
-    lnq_err = ti.betan * np.sqrt(max(sigA, 0.0) / max(nrep, 1))
+    lnq_err = ti.betan * np.sqrt(max(se2, 0.0))
     beads = ti.nrings * ti.P
     return dict(dA=dA, sigmaA=sigA, qratio=q, ln_qratio=lnq, ln_qratio_stderr=lnq_err, delta=delta,
                 integrand_mean=list(mean), integrand_var=list(var), nrings=ti.nrings, P=ti.P, nmc=nmc,
@@ -327,7 +357,7 @@ def run_ti_mixed(cfg, precision=pg.PG_MIXED, form=pg.PG_FORM_AUTO, nmc=None, chu
             ti = pgconfigs.TiInputs(cg, nrep=nrep, nintegral=nint, P=P, gauleg=pg.gauleg)
             ctx = pg.Context(device)
             groups.append((P, idx, ti, ctx))
-            ctx.set_system(c["ndim"], c["natom"], c["mass"], c["pes_id"], c["params"], c["V0"])
+            set_system_at_well1(ctx, c)
             ctx.ti_setup(ti.ti_config(pg, precision, form), ti.ring_lambda[idx], ti.ring_seed[idx],
                          ti.ring_stream[idx], ti.a, ti.b, ti.dbdl, ti.xref)
         t0 = time.perf_counter()
@@ -347,14 +377,14 @@ def run_ti_mixed(cfg, precision=pg.PG_MIXED, form=pg.PG_FORM_AUTO, nmc=None, chu
             mean, var, cnt = ctx.ti_lambda_reduce()
             _, _, _, status = ctx.ti_results()
             form_used, _ = ctx.ti_form(1)
+            se2 = _lambda_stderr2(ti.w, var, cnt)
             dA, sigA, q = pg.ti_assemble(ti.w, mean, var, ti.betan)
             try:
                 delta = pg.splitting_from_ratio(c["beta"], q)
             except pg.PgError:
                 delta = float("nan")
-            nper = max(int(np.min(cnt)), 1)
             per_P.append(dict(P=P, nrings=int(len(idx)), dA=dA, sigmaA=sigA, qratio=q, ln_qratio=-dA * ti.betan,
-                              ln_qratio_stderr=ti.betan * np.sqrt(max(sigA, 0.0) / nper), delta=delta,
+                              ln_qratio_stderr=ti.betan * np.sqrt(max(se2, 0.0)), delta=delta,
                               betan=ti.betan, dt=ti.cfg["dt"], form=form_used,
                               nan_rings=int(np.sum(status != 0))))
             beads += len(idx) * P
@@ -432,25 +462,29 @@ def run_rpi(cfg, N=None, betas=None, m=8, factr=1.0e6, pgtol=1.0e-5, maxiter=200
     if own:
         ctx = pg.Context(device)
     try:
-        ctx.set_system(c["ndim"], c["natom"], c["mass"], c["pes_id"], c["params"], c["V0"])
+        set_system_at_well1(ctx, c)
         guess = (linear_guess(w1, w2, N) if path is None
                  else path_guess(path, N, c["ndim"], c["natom"]))  # rpi_ser.f90:133-163
         x0 = np.concatenate([guess for _ in range(nb)])
         t0 = time.perf_counter()
-        x, UM, it, st = ctx.instanton_optimize(N, x0, w1, np.tile(w2, nb), betan, m=m, factr=factr, pgtol=pgtol,
-                                               maxiter=maxiter)
+        # fixedends False: the free-ended action, optimised without the end
+        # points (instanton(xtilde), instantonmod.f90:724-762)
+        ctx.set_fixedends(fixedends)
+        try:
+            x, UM, it, st = ctx.instanton_optimize(N, x0, w1 if fixedends else None,
+                                                   np.tile(w2, nb) if fixedends else None, betan, m=m,
+                                                   factr=factr, pgtol=pgtol, maxiter=maxiter)
+        finally:
+            ctx.set_fixedends(True)
         t_opt = time.perf_counter() - t0
         # V along each instanton: a bead below well 1 moves V0 to its energy,
         # which raises the action by -N min V (rpi_ser.f90:180-190)
         beads = np.asarray(x).reshape(nb, nd, N).transpose(0, 2, 1).reshape(nb * N, nd)
         vpath = ctx.pes_eval(beads)[0].reshape(nb, N)
         vshift = np.minimum(vpath.min(axis=1), 0.0)
+        # S = betan UM(xtilde[, well1, well2]) (rpi_ser.f90:370-374): the action
+        # as it was optimised, with or without the end springs
         UM = np.asarray(UM) - N * vshift
-        if not fixedends:  # S from UM(xtilde) without the end-point springs (rpi_ser.f90:370-374)
-            xb = np.asarray(x).reshape(nb, nd, N)
-            mdof = np.repeat(np.asarray(c["mass"], float), c["ndim"])
-            ends = ((xb[:, :, 0] - w1) ** 2 + (np.tile(w2, (nb, 1)) - xb[:, :, -1]) ** 2) @ mdof
-            UM = UM - ends / (2.0 * betan ** 2)
         xharm = np.concatenate([np.repeat(w1, N) for _ in range(nb)])
         t0 = time.perf_counter()
         ld0, _, _ = ctx.instanton_logdet(N, xharm, betan, singlewell=True, skip_lowest=False, quirks=quirks)

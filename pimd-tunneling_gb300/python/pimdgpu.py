@@ -29,7 +29,7 @@ EXPORTS = [
     "pg_ti_get_results", "pg_ti_lambda_reduce", "pg_ti_get_step", "pg_ti_advance_timed", "pg_ti_get_form", "pg_ti_kernel_times", "pg_set_tuning", "pg_ti_get_tuning", "pg_ti_checkpoint_save",
     "pg_ti_checkpoint_load", "pg_ti_release", "pg_propagate_pimd", "pg_gauleg", "pg_spline",
     "pg_splint", "pg_ti_assemble", "pg_splitting_from_ratio", "pg_splitting_two_beta", "pg_irrep_ratios",
-    "pg_instanton_fg",
+    "pg_set_fixedends", "pg_instanton_fg",
     "pg_instanton_optimize", "pg_um_hessian", "pg_instanton_logdet", "pg_rpi_assemble",
     "pg_nm_transform_noalloc", "pg_ti_advance_group", "pg_ti_set_accumulators",
 ]
@@ -98,6 +98,7 @@ def lib():
         L.pg_splitting_from_ratio.argtypes = [D, D, P]
         L.pg_splitting_two_beta.argtypes = [D, D, D, D, P, P]
         L.pg_irrep_ratios.argtypes = [I64, I64, P, P, P]
+        L.pg_set_fixedends.argtypes = [P, I32]
         L.pg_instanton_fg.argtypes = [P, I64, I64, P, P, P, P, P, P]
         L.pg_instanton_optimize.argtypes = [P, I64, I64, P, P, P, P, P, P, P, P]
         L.pg_um_hessian.argtypes = [P, I64, D, P, I32, I32, P]
@@ -363,8 +364,15 @@ class Context:
         return x, p, dh, st
 
     # ---- instanton
+    def set_fixedends(self, fixedends):
+        """instantonmod's fixedends: False drops the end-point springs of the
+        action and its gradient (pg_set_fixedends)."""
+        check(lib().pg_set_fixedends(self.h, int(bool(fixedends))))
+
     def instanton_fg(self, N, x, a, b, betan):
-        x, a, b, betan = map(_f64, (x, a, np.atleast_1d(b), np.atleast_1d(betan)))
+        x, betan = _f64(x), _f64(np.atleast_1d(betan))
+        a = None if a is None else _f64(a)
+        b = None if b is None else _f64(np.atleast_1d(b))
         nb = betan.size
         UM = np.zeros(nb)
         g = np.zeros(x.size)
@@ -374,7 +382,9 @@ class Context:
     def instanton_optimize(self, N, x, a, b, betan, m=8, factr=1.0e6, pgtol=1.0e-5, maxiter=20000,
                            max_backtracks=40):
         x = np.array(x, dtype=np.float64)
-        a, b, betan = map(_f64, (a, np.atleast_1d(b), np.atleast_1d(betan)))
+        betan = _f64(np.atleast_1d(betan))
+        a = None if a is None else _f64(a)
+        b = None if b is None else _f64(np.atleast_1d(b))
         nb = betan.size
         o = LbfgsOpts(m, max_backtracks, maxiter, factr, pgtol)
         UM = np.zeros(nb)

@@ -37,6 +37,7 @@ struct pg_ctx {
     or_pes pes;
     std::vector<double> params, mass;
     TiBatch ti;
+    int fixedends = 1;
 };
 
 extern "C" {
@@ -84,17 +85,22 @@ int pg_splint(const double *xa, const double *ya, const double *y2a, int64_t n, 
     if (dydx) *dydx = or_splin_grad(xa, ya, y2a, n, x);
     return PG_OK;
 }
+int pg_set_fixedends(pg_ctx *c, int32_t fixedends) {
+    c->fixedends = fixedends;
+    return PG_OK;
+}
 int pg_instanton_optimize(pg_ctx *c, int64_t nbeta, int64_t N, double *x, const double *a, const double *b,
                           const double *betan, const pg_lbfgs_opts *, double *UM, int64_t *niter, int32_t *status) {
     const int64_t nd = ndof(c);
-    if (nbeta > 1 && std::getenv("PG_STANDIN_ENDS")) {  // the end points of a batch, one number per line
+    if (nbeta > 1 && b && std::getenv("PG_STANDIN_ENDS")) {  // the end points of a batch, one number per line
         FILE *f = std::fopen(std::getenv("PG_STANDIN_ENDS"), "w");
         if (!f) return PG_ERR_ARG;
         for (int64_t i = 0; i < nbeta * nd; i++) std::fprintf(f, "%.17g\n", b[i]);
         std::fclose(f);
     }
     for (int64_t k = 0; k < nbeta; k++) {
-        if (UM) UM[k] = or_UM(&c->pes, c->mass.data(), N, betan[k], x + k * nd * N, a, b + k * nd, 1);
+        if (UM) UM[k] = or_UM(&c->pes, c->mass.data(), N, betan[k], x + k * nd * N, a, b ? b + k * nd : nullptr,
+                              c->fixedends);
         if (niter) niter[k] = 0;
         if (status) status[k] = 0;
     }
@@ -186,9 +192,14 @@ int pg_ti_setup(pg_ctx *c, const pg_ti_config *cfg, int64_t nrings, int64_t nlam
         if (p0) std::copy(p0 + r * ns, p0 + (r + 1) * ns, t.p.begin() + r * ns);
         t.res[r].and_rkick = -1;
     }
-    if (const char *k = std::getenv("PG_STANDIN_NAN_RING")) {  // a NaN in one ring's start (fault injection)
-        const int64_t r = std::atoll(k);
-        if (r >= 0 && r < nrings) t.x[(size_t)r * ns] = std::nan("");
+    if (const char *k = std::getenv("PG_STANDIN_NAN_RING")) {  // a NaN in the start of the listed rings
+        for (const char *q = k; *q;) {                           // (fault injection; comma-separated)
+            char *e = nullptr;
+            const int64_t r = std::strtoll(q, &e, 10);
+            if (e == q) break;
+            if (r >= 0 && r < nrings) t.x[(size_t)r * ns] = std::nan("");
+            q = *e == ',' ? e + 1 : e;
+        }
     }
     if (x0 && std::getenv("PG_STANDIN_X0")) {
         FILE *f = std::fopen(std::getenv("PG_STANDIN_X0"), "w");
@@ -295,8 +306,8 @@ int pg_instanton_fg(pg_ctx *c, int64_t nbeta, int64_t N, const double *x, const 
     const int64_t nd = ndof(c);
     std::vector<double> g((size_t)nd * N);
     for (int64_t k = 0; k < nbeta; k++) {
-        const double u = or_UMforceenergy(&c->pes, c->mass.data(), N, betan[k], x + k * nd * N, a, b + k * nd, 1,
-                                          g.data());
+        const double u = or_UMforceenergy(&c->pes, c->mass.data(), N, betan[k], x + k * nd * N, a,
+                                          b ? b + k * nd : nullptr, c->fixedends, g.data());
         if (UM) UM[k] = u;
         if (grad) std::copy(g.begin(), g.end(), grad + k * nd * N);
     }

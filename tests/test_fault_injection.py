@@ -77,6 +77,36 @@ def test_driver_leaves_a_nan_ring_out(oracle, tmp_path):
     assert dA == pytest.approx(ref, rel=1e-12)
 
 
+def test_driver_stops_when_a_lambda_point_loses_every_ring(oracle, tmp_path):
+    """Every ring of lambda point 2 (rings 3, 4, 5) starts from a NaN: that point
+    has no estimate, so the driver stops with a message naming it instead of
+    integrating a zero (exit status 3)."""
+    import standin
+    exe = standin.build_driver("pimd_ti", tmp_path)
+    c = dict(pgconfigs.load("c0"), imin=20, P=16, nintegral=3)
+    _write_inputs(tmp_path, c)
+    text = ("&MCDATA n=16, beta=%.17g, NMC=60, dt=%.17g, imin=20, tau=%.17g, gamma=%.17g, nintegral=3,\n"
+            " nrep=3, thermostat=2, ndim=1, natom=1, readpath=F, pes='1d', pes_params='pes.dat',\n"
+            " precision='fp64', form='fused', init='well', init_sigma=%.17g, seed=0 /\n"
+            % (c["beta"], c["dt"], c["tau"], c["gamma"], c["init_sigma"]))
+    r = subprocess.run([exe], input=text, capture_output=True, text=True, cwd=str(tmp_path), timeout=300,
+                       env=dict(os.environ, PG_STANDIN_NAN_RING="3,4,5"))
+    assert r.returncode == 3, (r.returncode, r.stderr)
+    assert "integration point 2 has no valid ring" in r.stderr
+    assert "final Delta A" not in r.stdout
+
+
+def test_python_driver_error_bar_uses_the_rings_each_point_kept():
+    """The standard error of Delta A divides each point's variance by the rings
+    it kept (sigmaA / nrep when all count, pimd_par.f90:422); a point with none
+    stops the Python driver as it stops the namelist driver."""
+    import drivers
+    assert drivers._lambda_stderr2([0.5, 0.5], [4.0, 9.0], [4, 9]) == pytest.approx(0.5, rel=1e-15)
+    assert drivers._lambda_stderr2([1.0, 2.0], [3.0, 3.0], [3, 3]) == pytest.approx((3.0 + 12.0) / 3, rel=1e-15)
+    with pytest.raises(RuntimeError, match=r"\[2\]"):
+        drivers._lambda_stderr2([0.5, 0.5], [1.0, 0.0], [3, 0])
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("form", ["fused", "plain"])
 def test_nan_ring_is_flagged_and_isolated(ctx, pg, form):

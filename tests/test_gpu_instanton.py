@@ -120,3 +120,72 @@ def test_lbfgs_matches_scipy_lbfgsb(ctx, pg, oracle):
         assert abs(UM[k] - fo) <= 1e-8 * abs(fo), (UM[k], fo)
         _, g = ctx.instanton_fg(N, x[k * n:(k + 1) * n], w1, w2, [betans[k]])
         assert np.max(np.abs(g)) < 1e-6
+
+
+@pytest.mark.parametrize("name", ["c1", "c3", "c0"])
+def test_free_ended_action_and_gradient_match_oracle_and_fd(ctx, pg, oracle, name):
+    """fixedends = .false.: the action and gradient without the end-point springs
+    (instantonmod.f90:35-44, 63-72, 115-124, 138) against the oracle to 1e-11 and
+    against central differences of the GPU action (step 1e-5); the end points
+    are not passed (NULL), as instanton(xtilde) passes none."""
+    c, pes, mass = _system(ctx, oracle, name)
+    w1, w2 = np.array(c["well1"]), np.array(c["well2"])
+    N = 24
+    betans = np.array([3.0, 11.0, 40.0])
+    xs = np.concatenate([_linear_path(w1, w2, N, 0.02, s) for s in range(3)])
+    n = N * len(w1)
+    ctx.set_fixedends(False)
+    try:
+        UM, g = ctx.instanton_fg(N, xs, None, None, betans)
+        for k in range(3):
+            uo, go = oracle.UMforceenergy(pes, mass, N, betans[k], xs[k * n:(k + 1) * n], w1, w2, False)
+            assert abs(UM[k] - uo) <= 1e-12 * max(1.0, abs(uo))
+            np.testing.assert_allclose(g[k * n:(k + 1) * n], go, rtol=1e-11, atol=1e-13)
+        h = 1e-5
+        x = xs[:n]
+        idx = np.random.RandomState(1).choice(n, min(n, 30), replace=False)
+        # the end beads of every dof, where the free ends change the gradient
+        idx = np.unique(np.concatenate([idx, np.arange(len(w1)) * N, np.arange(len(w1)) * N + N - 1]))
+        pts = []
+        for i in idx:
+            for sgn in (1, -1):
+                xx = x.copy()
+                xx[i] += sgn * h
+                pts.append(xx)
+        U, _ = ctx.instanton_fg(N, np.concatenate(pts), None, None, np.full(len(pts), betans[0]))
+        fd = (U[0::2] - U[1::2]) / (2 * h)
+        np.testing.assert_allclose(g[idx], fd, rtol=1e-6, atol=1e-8)
+    finally:
+        ctx.set_fixedends(True)
+    # back to fixed ends: the end springs are there again
+    UMf, _ = ctx.instanton_fg(N, xs[:n], w1, w2, betans[:1])
+    uo = oracle.UM(pes, mass, N, betans[0], xs[:n], w1, w2, True)
+    assert abs(UMf[0] - uo) <= 1e-12 * max(1.0, abs(uo))
+
+
+@pytest.mark.parametrize("name", ["c3", "c0"])
+def test_free_ended_lbfgs_matches_scipy_lbfgsb(ctx, pg, oracle, name):
+    """The free-ended instanton (instanton(xtilde), instantonmod.f90:724-762): the
+    on-device L-BFGS reaches scipy L-BFGS-B's action on the oracle's free-ended
+    UM to 1e-8, both started from the rpi_ser linear path."""
+    c, pes, mass = _system(ctx, oracle, name)
+    w1, w2 = np.array(c["well1"]), np.array(c["well2"])
+    N = 16 if name == "c3" else 32
+    betas = np.array(c["betas"])[[0, -1]] if "betas" in c else np.array([c["beta"], 0.5 * c["beta"]])
+    betans = betas / N
+    x0 = np.concatenate([_linear_path(w1, w2, N) for _ in range(2)])
+    ctx.set_fixedends(False)
+    try:
+        x, UM, it, st = ctx.instanton_optimize(N, x0, None, None, betans, m=10, factr=1e2, pgtol=1e-9,
+                                               maxiter=200000)
+    finally:
+        ctx.set_fixedends(True)
+    assert np.all(st == 0), (st, it)
+    n = N * len(w1)
+    for k in range(2):
+        xo, fo, r = oracle.instanton_lbfgs(pes, mass, N, betans[k], x0[k * n:(k + 1) * n], None, None, m=10,
+                                           factr=1e2, pgtol=1e-9, maxiter=200000, fixedends=False)
+        assert abs(UM[k] - fo) <= 1e-8 * abs(fo), (UM[k], fo)
+        # the optimiser's value is the free-ended action of the path it returns
+        uo = oracle.UM(pes, mass, N, betans[k], x[k * n:(k + 1) * n], w1, w2, False)
+        assert abs(UM[k] - uo) <= 1e-12 * max(1.0, abs(uo))

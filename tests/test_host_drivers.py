@@ -145,10 +145,45 @@ def test_rpi_driver_matches_python_driver(drivers_built, tmp_path):
 
 
 @pytest.mark.gpu
+def test_rpi_driver_free_ends_match_python_driver_and_scipy(drivers_built, tmp_path, oracle):
+    """fixedends = .false. (rpi_ser.f90:39, 370-374): both front ends optimise the
+    free-ended action (instanton(xtilde)) and report S = betan UM(xtilde); they
+    agree to round-off, and S matches scipy L-BFGS-B on the oracle's free-ended
+    action from the same linear start to 1e-8."""
+    import drivers
+    c = dict(pgconfigs.load("c3"))
+    _write_inputs(tmp_path, c, ["O", "O", "C", "C", "C", "H", "H", "H", "H"])
+    beta, n = c["betas"][5], 32
+    text = ("&RPIDATA n=%d, beta=%.17g, ndim=3, natom=9, readpath=.false., pes='synth9', pes_params='pes.dat',\n"
+            " m=10, pgtol=1d-9, factr=1d2, fixedends=.false. /\n" % (n, beta))
+    r = _run("rpi", text, cwd=str(tmp_path))
+    assert r.returncode == 0, r.stderr
+    S = float(re.search(r"s_kink=\s*(\S+)", r.stdout).group(1))
+    ref = drivers.run_rpi(c, N=n, betas=[beta], m=10, factr=1e2, pgtol=1e-9, fixedends=False)
+    assert abs(S - ref["results"][0]["S"]) <= 1e-12 * abs(S)
+    assert ref["results"][0]["status"] == 0
+    fixed = drivers.run_rpi(c, N=n, betas=[beta], m=10, factr=1e2, pgtol=1e-9)["results"][0]["S"]
+    pes = oracle.Pes(c["pes_id"], c["ndim"], c["natom"], c["params"], V0=c["V0"])
+    w1, w2 = np.array(c["well1"]), np.array(c["well2"])
+    k = np.arange(1, n + 1)
+    x0 = np.concatenate([((n - k) * w1[d] + (k - 1) * w2[d]) / (n - 1) for d in range(len(w1))])
+    _, fo, _ = oracle.instanton_lbfgs(pes, np.array(c["mass"]), n, beta / n, x0, None, None, m=10, factr=1e2,
+                                      pgtol=1e-9, maxiter=200000, fixedends=False)
+    vmin = min(float(np.min(ref["vpath"])), 0.0)
+    assert abs(S - (beta / n) * (fo - n * vmin)) <= 1e-8 * abs(S)
+    # the free-ended optimum differs from the fixed-ended one (no end springs)
+    assert S != fixed
+
+
+@pytest.mark.gpu
 def test_rpi_driver_side_outputs(drivers_built, tmp_path):
     """checkhess (hessian_well1.dat and the mass-weighted eigenvalues,
     rpi_ser.f90:105-129), instanton.xyz with the bead energies and
-    instantonpathenergy.csv (rpi_ser.f90:180-218)."""
+    instantonpathenergy.csv (rpi_ser.f90:180-218).  Both front ends set
+    V0 = V(well1) on the device (rpi_ser.f90:95), so they hand the optimiser
+    bit-identical inputs and reach the same path: the bead energies agree to
+    round-off, and the checkhess branch leaves the instanton unchanged (byte-
+    identical instanton.xyz with and without it)."""
     import drivers
     import pimdgpu as pg
     c = dict(pgconfigs.load("c3"))
@@ -175,10 +210,16 @@ def test_rpi_driver_side_outputs(drivers_built, tmp_path):
     lines = (tmp_path / "instanton.xyz").read_text().split("\n")
     assert len([l for l in lines if l.strip()]) == n * (2 + 9)
     energies = np.array([float(lines[b * 11 + 1].split()[-1]) for b in range(n)])
-    np.testing.assert_allclose(energies, ref["vpath"][0], rtol=1e-8, atol=1e-12)
+    np.testing.assert_allclose(energies, ref["vpath"][0], rtol=1e-12, atol=1e-20)
     lam, vp = np.loadtxt(str(tmp_path / "instantonpathenergy.csv"), unpack=True)
     assert lam[0] == 0.0 and lam[-1] == pytest.approx(1.0) and np.all(np.diff(lam) > 0)
     np.testing.assert_allclose(vp, energies, rtol=1e-15, atol=0)
+    plain = tmp_path / "no_checkhess"
+    plain.mkdir()
+    _write_inputs(plain, c, ["O", "O", "C", "C", "C", "H", "H", "H", "H"])
+    r2 = _run("rpi", text.replace(", checkhess=.true.", ""), cwd=str(plain))
+    assert r2.returncode == 0, r2.stderr
+    assert (plain / "instanton.xyz").read_bytes() == (tmp_path / "instanton.xyz").read_bytes()
 
 
 @pytest.mark.gpu
