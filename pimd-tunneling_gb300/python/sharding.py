@@ -3,8 +3,9 @@
 The (trajectory x lambda) rings are independent (pimd_par.f90 sends each MPI
 rank its tasks once, pimd_par.f90:282-308, and gathers one integrand per task,
 :389).  Here each rank takes a contiguous block of rings balanced by its bead
-count, propagates it on its own GPU, and the only collective is one all-reduce
-of the per-lambda (sum, sum of squares, count) triples at the end.
+count, propagates it on its own GPU, and the only exchange is one gather of
+the per-lambda (sum, sum of squares, count) triples at the end, through the
+caller's own communicator.
 """
 import numpy as np
 
@@ -31,16 +32,22 @@ def lambda_partials(integrands, ring_lambda, nlambda):
     return out
 
 
-def allreduce_partials(partials, group=None):
-    """Sum the (sum, sumsq, count) triples over ranks (one small all-reduce)."""
-    import torch
-    import torch.distributed as dist
-    t = torch.from_numpy(np.ascontiguousarray(partials, dtype=np.float64))
-    if dist.is_available() and dist.is_initialized() and dist.get_world_size(group) > 1:
-        if dist.get_backend(group) == "nccl":
-            t = t.cuda()
-        dist.all_reduce(t, op=dist.ReduceOp.SUM, group=group)
-    return t.cpu().numpy()
+def combine_partials(partials, allgather=None):
+    """Sum the (sum, sum of squares, count) triples over ranks: the one exchange
+    of the run, replacing pimd_par's MPI_Gather of the integrands (:389).
+    allgather is the caller's communicator: a callable that takes this rank's
+    array and returns the list of every rank's array in rank order (mpi4py's
+    comm.allgather, or a wrapper of the caller's torch.distributed group); None
+    for a single rank.  The sum runs in rank order, so every rank gets the same
+    bits."""
+    p = np.ascontiguousarray(partials, dtype=np.float64)
+    if allgather is None:
+        return p.copy()
+    parts = [np.asarray(a, dtype=np.float64).reshape(p.shape) for a in allgather(p)]
+    tot = np.zeros_like(p)
+    for a in parts:
+        tot += a
+    return tot
 
 
 def mean_var(partials):

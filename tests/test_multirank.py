@@ -1,6 +1,6 @@
 """Multi-rank host logic on CPU (gloo, world size 2): ring sharding balanced by
-bead count and the one all-reduce of per-lambda partial sums reproduce the
-single-process reduction and assembly."""
+bead count and the one gather of per-lambda partial sums (through the
+caller's communicator) reproduce the single-process reduction and assembly."""
 import os
 import socket
 
@@ -35,7 +35,13 @@ def _worker(rank, ws, port, integrands, lam, nl, q):
     dist.init_process_group("gloo", rank=rank, world_size=ws)
     a, b = sharding.shard_rings(np.ones(len(lam)), ws, rank)
     part = sharding.lambda_partials(integrands[a:b], lam[a:b], nl)
-    tot = sharding.allreduce_partials(part)
+
+    def allgather(arr):  # the caller's communicator (here a gloo group)
+        out = [None] * ws
+        dist.all_gather_object(out, arr)
+        return out
+
+    tot = sharding.combine_partials(part, allgather)
     q.put((rank, tot))
     dist.destroy_process_group()
 
@@ -59,6 +65,7 @@ def test_two_rank_gloo_reduction_matches_single_process():
     ref = sharding.lambda_partials(integrands, lam, nl)
     for _, tot in res:
         np.testing.assert_allclose(tot, ref, rtol=1e-13)
+    np.testing.assert_array_equal(res[0][1], res[1][1])  # every rank gets the same bits
     mean, var = sharding.mean_var(res[0][1])
     m2 = integrands.reshape(nl, nrep).mean(1)
     np.testing.assert_allclose(mean, m2, rtol=1e-13)
