@@ -12,6 +12,12 @@ tensor-core normal-mode transform, FP64 estimator accumulation).  One bench
             drop-in for propagate_pimd_pile) with host x/p buffers: H2D of the
             ring state, the MD steps, D2H of state and estimators, every step
   plain / fused FP64: the same rings through the FP64 forms (denominators)
+  split_check: ln q/q0 and the splitting of the benchmarked mixed-precision
+            batch against the FP64 form (itself parity-tested against the CPU
+            oracle) on the same rings, seeds and number of MD steps
+  roofline: compute-bound terms of the dominant kernel (tensor: the two NM
+            transforms; SIMT: surface, operand splitting, update, normals;
+            HBM: ncu DRAM bytes), the kernel timed inside the replayed advance
   cpu_baseline: the CPU restatement of the reference step (ten dense NM
             transforms per step, FP64) on all host cores, bounded sample
 
@@ -38,7 +44,6 @@ import numpy as np  # noqa: E402
 METRIC = "bead-force-steps/s, batched mixed-prec vs plain FP64 on 1 GB300 at <=1% split err"
 UNIT = "bead-force-steps/s"
 MD_PER_STEP = 500
-KT_STEPS = 50  # MD steps of the per-kernel timing (one k_tc_step launch of the tensor form)
 
 
 def _peaks():
@@ -131,6 +136,120 @@ def _config(M, form, name="c1"):
     return {"workload": WORKLOADS[name] + ", Langevin, %d MD steps per bench step" % M,
             "precision": "FP32 forces/state, split-BF16 NM transform, FP64 estimator",
             "l2": "flushed (256 MB write) between timed steps", "form": form}
+
+
+def simt_flops_per_bead_step(c):
+    """Algorithmic FP32 SIMT flops per bead-force-step of the mixed step kernels
+    (MUFU exponentials count as one): the surface gradient per bead plus 28 per
+    dof -- positions x = T q + x* (2), splitting the two BF16 operands (4), the
+    kick / rotation / OU map of (q, pi) (16), the OU normal's Box-Muller share
+    and scale (6).  Surface gradients: mcmod_2dtest 16 per well (offsets 2,
+    u 3, two exponentials 4, coefficient 3, gradient 4); the 9-atom surface 30
+    per Morse pair (distance, exponential, Morse value and its gradient through
+    the B-matrix) for 36 pairs plus 20 for the quartic coordinate."""
+    nd = c["ndim"] * c["natom"]
+    pid = c["pes_id"]
+    if pid == 2:
+        fpes = 16.0 * c["params"][0]
+    elif pid == 3:
+        fpes = 30.0 * 36 + 20.0
+    elif pid == 1:
+        fpes = 8.0 * nd
+    else:
+        return None
+    return fpes + 28.0 * nd
+
+
+def roofline(ctx, pg, c, ti, beads, M, adv_ms, peaks, peak_kind, fp32_tflops):
+    """The dominant kernel's place under its compute roofline.  Its time per
+    launch inside the replayed advance is the advance time less the other
+    kernels (timed alone) over its launches; achieved = algorithmic work per
+    launch / that time, per term; the bound is the largest fraction."""
+    kt = ctx.ti_kernel_times(M)  # per-kernel events, direct launches (advances the batch M steps)
+    if not kt:
+        return None
+    try:
+        with open(os.path.join(ROOT, "profiles", "tensor_kernels_traffic.json")) as f:
+            tj = json.load(f)
+    except Exception:
+        tj = {}
+    if any(n.startswith("k_tc_step") for n, _, _, _ in kt):
+        # the persistent step kernel does the whole MD step: it is the unit
+        dom = [i for i, t in enumerate(kt) if t[0].startswith("k_tc_step")][0]
+        name, kms_alone, kcount, kbytes = kt[dom]
+        minor = sum(m * n for i, (_, m, n, _) in enumerate(kt) if i != dom)
+        kms = (adv_ms - minor) / max(kcount, 1)
+        traffic = tj.get("k_tc_step")
+    else:
+        # several kernels per MD step (blocked form): the MD step is the unit
+        name = " + ".join(n.split()[0] for n, _, _, _ in kt) + " (one MD step)"
+        kcount = M
+        kms = adv_ms / M
+        kms_alone = sum(m for _, m, _, _ in kt)
+        kbytes = sum(b for _, _, _, b in kt)
+        tr = [tj.get(n.split()[0]) for n, _, _, _ in kt]
+        traffic = sum(tr) if all(t is not None for t in tr) else None
+    md_per_launch = M / max(kcount, 1)  # MD steps one launch of the unit covers
+    units = beads * md_per_launch        # bead-force-steps per launch
+    secs = kms / 1e3
+    terms = {}
+    # tensor: two NM transforms per MD step (T q to positions, T F to modes), 2 P d flops per bead each
+    tc_flops = 4.0 * ti.P * ti.nd * units
+    terms["tensor"] = {"flops_per_bead_step": 4.0 * ti.P * ti.nd, "achieved": tc_flops / secs / 1e12,
+                       "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
+                       "peak_basis": "dense bf16 cuBLAS burst (%s)" % peak_kind}
+    fs = simt_flops_per_bead_step(c)
+    if fs is not None and fp32_tflops:
+        terms["simt"] = {"flops_per_bead_step": fs, "achieved": fs * units / secs / 1e12, "peak": fp32_tflops,
+                         "unit": "TFLOP/s", "peak_basis": "FP32 FMA chains measured live (pg_fp32_peak)"}
+    if traffic:
+        terms["hbm"] = {"bytes_per_launch": traffic, "achieved": traffic / secs / 1e9, "peak": peaks["hbm_gbs"],
+                        "unit": "GB/s", "peak_basis": "STREAM copy (%s); bytes: ncu DRAM read + write of one "
+                                                      "launch" % peak_kind}
+    for t in terms.values():
+        t["frac"] = t["achieved"] / t["peak"]
+    bind = max(terms, key=lambda k: terms[k]["frac"])
+    b = terms[bind]
+    return {"bound": "compute", "binding_term": bind, "achieved": b["achieved"], "peak": b["peak"],
+            "unit": b["unit"], "frac": b["frac"], "traffic": traffic, "peak_source": peak_kind,
+            "kernel": name, "kernel_ms": kms, "kernel_ms_alone": kms_alone, "launches_per_bench_step": kcount,
+            "bead_steps_per_launch": units, "algorithmic_bytes_per_launch": kbytes, "terms": terms,
+            "kernels": [{"name": n, "ms_per_launch_alone": m, "launches_per_bench_step": k, "bytes_per_launch": by}
+                        for (n, m, k, by) in kt]}
+
+
+def split_check(ctx, pg, c, ti, nsteps, mixed, chunk=1000):
+    """ln q/q0 and the splitting Delta = (2/beta) artanh(q/q0) of the mixed batch
+    after nsteps MD steps (its per-lambda mean / var / count in mixed) against
+    the FP64 fused form on the same rings, seeds and steps (pimd_par.f90:399-424)."""
+    import drivers
+
+    def assemble(mean, var, cnt):
+        se2 = drivers._lambda_stderr2(ti.w, var, cnt)
+        dA, _, q = pg.ti_assemble(ti.w, mean, var, ti.betan)
+        try:
+            delta = pg.splitting_from_ratio(c["beta"], q)
+        except pg.PgError:
+            delta = float("nan")
+        return {"ln_qratio": -dA * ti.betan, "ln_qratio_stderr": ti.betan * float(np.sqrt(max(se2, 0.0))),
+                "delta": delta}
+
+    t0 = time.perf_counter()
+    m = assemble(*mixed)
+    cfg64 = ti.ti_config(pg, pg.PG_FP64, pg.PG_FORM_FUSED)
+    ctx.ti_setup(cfg64, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
+    done = 0
+    while done < nsteps:
+        k = min(chunk, nsteps - done)
+        ctx.ti_advance(k)
+        done += k
+    r = assemble(*ctx.ti_lambda_reduce())
+    _, _, _, st = ctx.ti_results()
+    rel = abs(m["delta"] / r["delta"] - 1.0) if r["delta"] else float("nan")
+    return {"md_steps": int(nsteps), "imin": int(ti.cfg["imin"]), "rings": int(ti.nrings), "mixed": m, "fp64": r,
+            "delta_rel_err": rel, "ln_qratio_diff": m["ln_qratio"] - r["ln_qratio"], "within_1pct": bool(rel <= 0.01),
+            "fp64_nan_rings": int(np.sum(st != 0)), "seconds": time.perf_counter() - t0,
+            "fp64_form": "fused SIMT FP64 (parity-tested against the CPU oracle to 1e-9 per step)"}
 
 
 def cpu_reference_rate(c, ti, target_s=12.0, nthreads=None):
@@ -245,6 +364,8 @@ def main():
     ap.add_argument("--md-per-step", type=int, default=MD_PER_STEP)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-extras", action="store_true", help="skip the e2e and FP64 legs")
+    ap.add_argument("--no-split-check", action="store_true",
+                    help="skip the splitting check of the benchmarked batch against the FP64 form")
     ap.add_argument("--form", default="auto", choices=["auto", "fused", "tensor"])
     ap.add_argument("--workload", default="c1", choices=sorted(WORKLOADS),
                     help="c1 (the headline configuration) or c2 (27-dof surface, P = 256)")
@@ -304,35 +425,27 @@ def main():
     kernel_ms = 1e3 * dev_s / K
     s, n, _, st = ctx.ti_results()
     nan_rings = int(np.sum(st != 0))
+    mixed_red = ctx.ti_lambda_reduce()  # the benchmarked batch, for the splitting check
+    mixed_steps = ctx.ti_step()
 
     peaks, peak_kind = _peaks()
-    # Dominant kernel, timed live with CUDA events on the library stream.
-    kt = ctx.ti_kernel_times(KT_STEPS) if not (ws > 1 and rank != 0) else []
-    roof = None
-    if kt:
-        name, kms, kcount, kbytes = max(kt, key=lambda t: t[1] * t[2])
-        achieved_gbs = kbytes / (kms / 1e3) / 1e9
-        traffic = None
-        try:
-            with open(os.path.join(ROOT, "profiles", "tensor_kernels_traffic.json")) as f:
-                traffic = json.load(f).get(name.split()[0])
-        except Exception:
-            pass
-        # tensor view: two transforms per MD step (T q and T F), 2 P ndof useful
-        # flops per bead each; MD steps per launch from the state bytes per step
-        msteps = max(1, round(kbytes / (16.0 * beads * ti.nd)))
-        tflops = 4.0 * ti.P * ti.nd * beads * msteps / (kms / 1e3) / 1e12
-        roof = {"bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": achieved_gbs / peaks["hbm_gbs"], "traffic": traffic, "peak_source": peak_kind,
-                "kernel": name, "kernel_ms": kms, "algorithmic_bytes_per_launch": kbytes,
-                "kernels": [{"name": n, "ms_per_launch": m, "launches": k, "bytes_per_launch": b}
-                            for (n, m, k, b) in kt],
-                "tensor_view": {"achieved_tflops": tflops, "peak_tflops": peaks["bf16_tflops"],
-                                "frac": tflops / peaks["bf16_tflops"]}}
-
-    extras = {}
     print("[bench] timed advance: %.3f ms per step of %d MD steps, %.3e %s" % (kernel_ms, M, value, UNIT),
           file=sys.stderr, flush=True)
+    roof = None
+    extras = {}
+    if rank == 0:
+        try:
+            fp32 = ctx.fp32_peak()
+            # the dominant kernel, timed with CUDA events on the library stream
+            roof = roofline(ctx, pg, c, ti, beads, M, kernel_ms, peaks, peak_kind, fp32)
+            roof["fp32_peak_tflops_measured"] = fp32
+        except Exception as e:
+            extras["roofline_error"] = repr(e)
+    try:
+        if not args.no_split_check and rank == 0:
+            extras["split_check"] = split_check(ctx, pg, c, ti, mixed_steps, mixed_red)
+    except Exception as e:
+        extras["split_check_error"] = repr(e)
     try:
         if not args.no_extras and rank == 0:
             _extras(ctx, pg, cfg, ti, M, K, value, ws, beads, extras)

@@ -97,6 +97,20 @@ int pg_pes_hessian(pg_ctx *ctx, int64_t nconf, const double *x, double *hess, in
 int pg_nm_transform(pg_ctx *ctx, int64_t P, int64_t ncol, const double *in, double *out,
                     int32_t precision);
 
+/* Measurement helper (no counterpart in the reference): the FP32 FMA
+ * throughput of the context's GPU in TFLOP/s (best of three timed launches of
+ * scalar and packed f32x2 FMA chains), the peak of the SIMT term of the
+ * roofline. */
+int pg_fp32_peak(pg_ctx *ctx, double *tflops);
+/* Failure detection: wall-time bound, in ns, of the device-side waits (for the
+ * bulk copy of T and for the GEMM) of the tensor-core transform of
+ * pg_nm_transform (PG_MIXED, P = 128); default 2e9 (2 s), 0 gives up at the
+ * first test that finds the wait unfinished.  A wait that runs out makes the
+ * call return PG_ERR_NUMERIC; the kernel first lets the copy or GEMM it waited
+ * for finish (bounded by 2 s), so the context stays usable.  No counterpart in
+ * the reference, which has no device waits (it stops on a NaN,
+ * verletmodule.f90:533-536). */
+int pg_set_wait_limit(pg_ctx *ctx, int64_t ns);
 /* Allocation-free variant of the split-BF16 tcgen05 transform (pg_nm_transform
  * with PG_MIXED, P = 128).  No counterpart in the reference.  It is for callers
  * that cannot call cudaMalloc: a Fortran / MPI host program that gives all of

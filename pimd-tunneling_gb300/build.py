@@ -14,7 +14,10 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "lib")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
-FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+# Host code: no floating-point contraction (-ffp-contract=off), so that host
+# arithmetic gives the same bits on x86_64 and aarch64 (where GCC would
+# otherwise fuse a*b + c into an FMA) and matches numpy.
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "--expt-relaxed-constexpr",
          "-I" + os.path.join(HERE, "..", "include")]
 SOURCES = ["pg_api.cu", "pg_ti.cu", "pg_tc.cu", "pg_instanton.cu"]
 DRIVERS = ["pimd_ti", "rpi", "crossover"]  # C++ front ends (host/*.cpp), linked against libpimdgpu.so
@@ -56,7 +59,8 @@ def build(verbose=False):
         deps = [src, so] + glob.glob(os.path.join(HERE, "host", "*.hpp"))
         if os.path.exists(exe) and os.path.getmtime(exe) >= max(os.path.getmtime(p) for p in deps):
             continue
-        cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-o", exe, src, "-L" + OUT, "-lpimdgpu",
+        cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-ffp-contract=off", "-o", exe, src, "-L" + OUT,
+               "-lpimdgpu",
                "-Wl,-rpath,$ORIGIN"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

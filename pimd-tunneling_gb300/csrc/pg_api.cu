@@ -1,5 +1,6 @@
 // pg_api.cu -- context management, PES evaluation, the batched NM transform
 // and the host-side assembly helpers of the C-ABI (include/pimdgpu.h).
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -295,6 +296,89 @@ extern "C" int pg_pes_hessian(pg_ctx *ctx, int64_t nconf, const double *x, doubl
     PG_CUDA(cudaGetLastError());
     PG_CUDA(cudaMemcpyAsync(hess, ctx->scratch_b.ptr, nh * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     PG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return PG_OK;
+}
+
+// ---------------------------------------------------------------- FP32 peak
+// Measurement helper for the roofline of the SIMT work: FP32 FMA throughput of
+// this GPU, 8 independent chains per thread, as scalar FMAs or as packed f32x2
+// FMAs (one instruction, two lanes of work).
+template <bool PAIRED>
+__global__ void __launch_bounds__(256) k_fp32_fma(float *__restrict__ out, int iters, float mul, float add) {
+    const float s = 1e-3f * (float)(threadIdx.x + 1);
+    if (PAIRED) {
+        uint64_t acc[8], m2, a2;
+        asm("mov.b64 %0, {%1, %1};" : "=l"(m2) : "f"(mul));
+        asm("mov.b64 %0, {%1, %1};" : "=l"(a2) : "f"(add));
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const float v = s + (float)j;
+            asm("mov.b64 %0, {%1, %2};" : "=l"(acc[j]) : "f"(v), "f"(-v));
+        }
+        for (int it = 0; it < iters; it++)
+#pragma unroll
+            for (int j = 0; j < 8; j++) asm volatile("fma.rn.f32x2 %0, %0, %1, %2;" : "+l"(acc[j]) : "l"(m2), "l"(a2));
+        float t = 0.f;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            float lo, hi;
+            asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(acc[j]));
+            t += lo + hi;
+        }
+        if (t == 12345.678f) out[0] = t;  // keeps the chains live; never true in practice
+    } else {
+        float acc[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) acc[j] = s + (float)j;
+        for (int it = 0; it < iters; it++)
+#pragma unroll
+            for (int j = 0; j < 8; j++) asm volatile("fma.rn.f32 %0, %0, %1, %2;" : "+f"(acc[j]) : "f"(mul), "f"(add));
+        float t = 0.f;
+#pragma unroll
+        for (int j = 0; j < 8; j++) t += acc[j];
+        if (t == 12345.678f) out[0] = t;
+    }
+}
+
+extern "C" int pg_fp32_peak(pg_ctx *ctx, double *tflops) {
+    int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    if (!tflops) return fail(PG_ERR_ARG, "NULL tflops");
+    PG_CUDA(ctx->scratch_a.ensure(64));
+    float *out = ctx->scratch_a.as<float>();
+    const unsigned grid = (unsigned)ctx->sm_count * 4;
+    const int iters = 16384;
+    cudaEvent_t e0, e1;
+    PG_CUDA(cudaEventCreate(&e0));
+    PG_CUDA(cudaEventCreate(&e1));
+    double best = 0.0;
+    for (int paired = 0; paired < 2; paired++) {
+        for (int rep = 0; rep < 4; rep++) {
+            PG_CUDA(cudaEventRecord(e0, ctx->stream));
+            if (paired)
+                k_fp32_fma<true><<<grid, 256, 0, ctx->stream>>>(out, iters, 0.999f, 1e-4f);
+            else
+                k_fp32_fma<false><<<grid, 256, 0, ctx->stream>>>(out, iters, 0.999f, 1e-4f);
+            PG_CUDA(cudaGetLastError());
+            PG_CUDA(cudaEventRecord(e1, ctx->stream));
+            PG_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            PG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            const double flops = 2.0 * 8.0 * (paired ? 2.0 : 1.0) * iters * (double)grid * 256.0;
+            if (rep > 0 && ms > 0.f) best = std::max(best, flops / (ms * 1e-3) / 1e12);  // rep 0: warm-up
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *tflops = best;
+    return PG_OK;
+}
+
+extern "C" int pg_set_wait_limit(pg_ctx *ctx, int64_t ns) {
+    int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    if (ns < 0 || ns > (int64_t)60000000000LL) return fail(PG_ERR_ARG, "wait limit must lie in [0, 60 s]");
+    ctx->wait_ns = ns;
     return PG_OK;
 }
 

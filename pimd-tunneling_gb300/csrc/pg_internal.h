@@ -136,6 +136,8 @@ struct pg_ctx {
     // instantonmod's module variable fixedends (instantonmod.f90:7): with 0 the
     // polymer action drops the springs to the end points a, b (pg_set_fixedends)
     int fixedends = 1;
+    // wall-time bound of the tensor-core transform's device waits (pg_set_wait_limit)
+    int64_t wait_ns = 2000000000;
     pg::PesArgs pes_args() const {
         pg::PesArgs pa;
         pa.id = pes_id;

@@ -89,6 +89,29 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
     }
     return false;
 }
+// Non-blocking test of a phase (mbarrier.test_wait never suspends the thread).
+__device__ __forceinline__ bool mbar_test_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Wait bounded by a caller-set wall-time limit (the context's wait limit):
+// the clock is read after every unsuccessful test, so a limit of 0 gives up at
+// the first test that finds the phase incomplete.  A caller whose wait gives up
+// must still let the operation it waited for finish (mbar_wait, bounded by the
+// fixed limit) before the CTA frees tensor memory or exits.
+__device__ __forceinline__ bool mbar_wait_ns(uint64_t *bar, uint32_t parity, uint64_t limit_ns) {
+    const uint64_t t0 = globaltimer_ns();
+    for (long long i = 0; i < kSpinLimit; i++) {
+        if (mbar_test_wait(bar, parity)) return true;
+        if (globaltimer_ns() - t0 >= limit_ns) return false;
+    }
+    return false;
+}
 __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
                  : "memory");
@@ -266,10 +289,15 @@ __device__ __forceinline__ void load_transform(unsigned char *Thi, const unsigne
 
 // ---------------------------------------------------------------- standalone transform
 // out[c][:] = T in[c][:] for 128 columns per CTA (used by pg_nm_transform, P = 128).
+// The waits for the T copy and for the GEMM are bounded by wait_ns (the
+// context's wait limit).  A wait that gives up records the error and then waits
+// (bounded by the fixed 2 s limit) for that copy or GEMM to finish, so that no
+// asynchronous write into shared or tensor memory outlives the CTA's
+// deallocation and exit; the GEMM is not issued after a failed copy wait.
 __global__ void __launch_bounds__(128, 1) k_tc_transform(const unsigned char *__restrict__ gT,
                                                           const double *__restrict__ in,
                                                           double *__restrict__ out, int64_t ncol,
-                                                          int32_t *__restrict__ err) {
+                                                          int32_t *__restrict__ err, uint64_t wait_ns) {
     extern __shared__ unsigned char dsm[];
     unsigned char *base = align1k(dsm);
     unsigned char *Thi = base, *Tlo = base + kOpBytes, *Ahi = base + 2 * kOpBytes, *Alo = base + 3 * kOpBytes;
@@ -297,17 +325,20 @@ __global__ void __launch_bounds__(128, 1) k_tc_transform(const unsigned char *__
     __syncthreads();
     tc_after();
     const uint32_t tmem = sh->tmem_slot;
-    bool ok = mbar_wait(&sh->tma_bar, 0);
     if (tid == 0) {
-        if (ok) {
+        if (mbar_wait_ns(&sh->tma_bar, 0, wait_ns)) {
             issue_gemm(tmem, 0, smem_u32(Ahi), smem_u32(Alo), smem_u32(Thi), smem_u32(Tlo), &sh->mma_bar);
         } else {
             sh->err = 1;
+            mbar_wait(&sh->tma_bar, 0);  // the copy lands before the CTA may exit
         }
     }
     __syncthreads();
     bool issued = sh->err == 0;
-    if (issued && !mbar_wait(&sh->mma_bar, 0)) atomicOr(&sh->err, 2);
+    if (issued && !mbar_wait_ns(&sh->mma_bar, 0, wait_ns)) {
+        atomicOr(&sh->err, 2);
+        mbar_wait(&sh->mma_bar, 0);  // the GEMM finishes before TMEM is read or freed
+    }
     tc_after();
     __syncthreads();
     if (sh->err == 0) {
@@ -2206,13 +2237,14 @@ int tc_nm_transform(pg_ctx *ctx, int64_t P, int64_t ncol, const double *in, doub
     size_t sm = (size_t)kSmemOps + 1024 + sizeof(TcShared) + 64;
     PG_CUDA(cudaFuncSetAttribute(k_tc_transform, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     unsigned grid = (unsigned)((ncol + kRows - 1) / kRows);
-    k_tc_transform<<<grid, 128, sm, s>>>(dimg, ctx->scratch_a.as<double>(), ctx->scratch_b.as<double>(), ncol, derr);
+    k_tc_transform<<<grid, 128, sm, s>>>(dimg, ctx->scratch_a.as<double>(), ctx->scratch_b.as<double>(), ncol, derr,
+                                         (uint64_t)ctx->wait_ns);
     PG_CUDA(cudaGetLastError());
     int32_t herr = 0;
     PG_CUDA(cudaMemcpyAsync(&herr, derr, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     PG_CUDA(cudaMemcpyAsync(out, ctx->scratch_b.ptr, n * sizeof(double), cudaMemcpyDeviceToHost, s));
     PG_CUDA(cudaStreamSynchronize(s));
-    if (herr) return fail(PG_ERR_NUMERIC, "tensor-core transform: barrier wait timed out");
+    if (herr) return fail(PG_ERR_NUMERIC, "tensor-core transform: a device wait exceeded the wait limit");
     return PG_OK;
 }
 
@@ -2278,7 +2310,7 @@ extern "C" int pg_nm_transform_noalloc(int64_t P, int64_t ncol, const double *d_
     PG_CUDA(cudaMemsetAsync(derr, 0, sizeof(int32_t), s));
     size_t sm = (size_t)kSmemOps + 1024 + sizeof(TcShared) + 64;
     unsigned grid = (unsigned)((ncol + kRows - 1) / kRows);
-    k_tc_transform<<<grid, 128, sm, s>>>(img, d_in, d_out, ncol, derr);
+    k_tc_transform<<<grid, 128, sm, s>>>(img, d_in, d_out, ncol, derr, kWaitLimitNs);
     PG_CUDA(cudaGetLastError());
     int32_t herr = 0;
     PG_CUDA(cudaMemcpyAsync(&herr, derr, sizeof(int32_t), cudaMemcpyDeviceToHost, s));

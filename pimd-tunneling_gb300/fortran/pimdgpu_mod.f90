@@ -290,6 +290,18 @@ module pimdgpu
        real(c_double), intent(out) :: dA, sigmaA, qratio
      end function pg_ti_assemble
 
+     integer(c_int) function pg_fp32_peak(ctx, tflops) bind(c, name="pg_fp32_peak")
+       import :: c_int, c_double, c_ptr
+       type(c_ptr), value :: ctx
+       real(c_double), intent(out) :: tflops
+     end function pg_fp32_peak
+
+     integer(c_int) function pg_set_wait_limit(ctx, ns) bind(c, name="pg_set_wait_limit")
+       import :: c_int, c_int64_t, c_ptr
+       type(c_ptr), value :: ctx
+       integer(c_int64_t), value :: ns
+     end function pg_set_wait_limit
+
      ! instanton: fixedends, UMforceenergy, instanton, UMhessian, detJ + log sums
      integer(c_int) function pg_set_fixedends(ctx, fixedends) bind(c, name="pg_set_fixedends")
        import :: c_int, c_int32_t, c_ptr

@@ -31,7 +31,7 @@ EXPORTS = [
     "pg_splint", "pg_ti_assemble", "pg_splitting_from_ratio", "pg_splitting_two_beta", "pg_irrep_ratios",
     "pg_set_fixedends", "pg_instanton_fg",
     "pg_instanton_optimize", "pg_um_hessian", "pg_instanton_logdet", "pg_rpi_assemble",
-    "pg_nm_transform_noalloc", "pg_ti_advance_group", "pg_ti_set_accumulators",
+    "pg_nm_transform_noalloc", "pg_set_wait_limit", "pg_fp32_peak", "pg_ti_advance_group", "pg_ti_set_accumulators",
 ]
 
 
@@ -74,6 +74,8 @@ def lib():
         L.pg_pes_hessian.argtypes = [P, I64, P, P, I32]
         L.pg_nm_transform.argtypes = [P, I64, I64, P, P, I32]
         L.pg_nm_transform_noalloc.argtypes = [I64, I64, P, P, P]
+        L.pg_set_wait_limit.argtypes = [P, I64]
+        L.pg_fp32_peak.argtypes = [P, P]
         L.pg_ti_setup.argtypes = [P, P, I64, I64, P, P, P, P, P, P, P, P, P]
         L.pg_ti_advance.argtypes = [P, I64]
         L.pg_ti_advance_timed.argtypes = [P, I64, P]
@@ -291,6 +293,12 @@ class Context:
         check(lib().pg_ti_get_results(self.h, _p(s), _p(n), _p(ri), _p(st)))
         return s, n, ri, st
 
+    def ti_step(self):
+        """MD steps the batch has taken (pg_ti_get_step)."""
+        v = np.zeros(1, dtype=np.int64)
+        check(lib().pg_ti_get_step(self.h, _p(v)))
+        return int(v[0])
+
     def ti_lambda_reduce(self):
         _, _, nl = self._ti
         m = np.zeros(nl)
@@ -364,6 +372,17 @@ class Context:
         return x, p, dh, st
 
     # ---- instanton
+    def fp32_peak(self):
+        """Measured FP32 FMA throughput of this GPU, TFLOP/s (pg_fp32_peak)."""
+        v = C.c_double(0.0)
+        check(lib().pg_fp32_peak(self.h, C.byref(v)))
+        return v.value
+
+    def set_wait_limit(self, ns):
+        """Wall-time bound (ns) of the tensor-core transform's device waits
+        (pg_set_wait_limit); 2e9 by default."""
+        check(lib().pg_set_wait_limit(self.h, int(ns)))
+
     def set_fixedends(self, fixedends):
         """instantonmod's fixedends: False drops the end-point springs of the
         action and its gradient (pg_set_fixedends)."""

@@ -18,8 +18,8 @@ def build_driver(name, outdir):
     inc = ["-I", os.path.join(ROOT, "oracle"), "-I", os.path.join(ROOT, "include"),
            "-I", os.path.join(ROOT, "pimd-tunneling_gb300", "host")]
     exe = os.path.join(str(outdir), name)
-    subprocess.run([cxx, "-O2", "-std=c++17", os.path.join(ROOT, "pimd-tunneling_gb300", "host", name + ".cpp"),
-                    os.path.join(HERE, "pg_standin.cpp"), "-o", exe, "-L" + os.path.join(ROOT, "oracle"),
+    subprocess.run([cxx, "-O2", "-std=c++17", "-ffp-contract=off",
+                    os.path.join(ROOT, "pimd-tunneling_gb300", "host", name + ".cpp"), os.path.join(HERE, "pg_standin.cpp"), "-o", exe, "-L" + os.path.join(ROOT, "oracle"),
                     "-loracle", "-Wl,-rpath," + os.path.join(ROOT, "oracle")] + inc, check=True)
     return exe
 
@@ -32,7 +32,8 @@ def build_library(outdir):
     if not cxx:
         pytest.skip("no C++ compiler")
     so = os.path.join(str(outdir), "libpimdgpu_standin.so")
-    subprocess.run([cxx, "-O2", "-std=c++17", "-shared", "-fPIC", os.path.join(HERE, "pg_standin.cpp"), "-o", so,
+    subprocess.run([cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-shared", "-fPIC",
+                    os.path.join(HERE, "pg_standin.cpp"), "-o", so,
                     "-I", os.path.join(ROOT, "oracle"), "-I", os.path.join(ROOT, "include"),
                     "-I", os.path.join(ROOT, "pimd-tunneling_gb300", "host"), "-L" + os.path.join(ROOT, "oracle"),
                     "-loracle", "-Wl,-rpath," + os.path.join(ROOT, "oracle")], check=True)

@@ -85,6 +85,8 @@ int pg_splint(const double *xa, const double *ya, const double *y2a, int64_t n, 
     if (dydx) *dydx = or_splin_grad(xa, ya, y2a, n, x);
     return PG_OK;
 }
+int pg_set_wait_limit(pg_ctx *, int64_t ns) { return ns < 0 ? PG_ERR_ARG : PG_OK; }
+int pg_fp32_peak(pg_ctx *, double *) { return PG_ERR_UNSUPPORTED; }
 int pg_set_fixedends(pg_ctx *c, int32_t fixedends) {
     c->fixedends = fixedends;
     return PG_OK;

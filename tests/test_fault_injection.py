@@ -136,3 +136,26 @@ def test_nan_ring_is_flagged_and_isolated(ctx, pg, form):
     integ = s0 / n0 / ti.betan ** 2
     assert m1[0] == m0[0]
     assert m1[1] == pytest.approx(np.mean(integ[[3, 5]]), rel=1e-13)
+
+
+@pytest.mark.gpu
+def test_transform_wait_that_runs_out_is_reported_and_the_context_stays_usable(ctx, pg):
+    """Failure detection without a GPU fault: with the wait limit at 0 the
+    tensor-core transform's bounded wait gives up at its first unfinished test
+    (the GEMM of a single 128-column tile takes far longer than one test), the
+    kernel lets the copy / GEMM it waited for finish, and the call returns
+    PG_ERR_NUMERIC; back at the default limit, the same context transforms the
+    same columns correctly."""
+    P = 128
+    cols = np.random.RandomState(5).randn(128 * P)  # one tile
+    ref = ctx.nm_transform(P, cols, pg.PG_FP64)
+    ctx.set_wait_limit(0)
+    try:
+        with pytest.raises(pg.PgError) as e:
+            ctx.nm_transform(P, cols, pg.PG_MIXED)
+        assert e.value.code == pg.PG_ERR_NUMERIC
+        assert "wait limit" in str(e.value)
+    finally:
+        ctx.set_wait_limit(2000000000)
+    out = ctx.nm_transform(P, cols, pg.PG_MIXED)
+    assert np.max(np.abs(out - ref)) <= 3e-5 * np.max(np.abs(ref))
