@@ -102,12 +102,12 @@ int pg_nm_transform(pg_ctx *ctx, int64_t P, int64_t ncol, const double *in, doub
  * scalar and packed f32x2 FMA chains), the peak of the SIMT term of the
  * roofline. */
 int pg_fp32_peak(pg_ctx *ctx, double *tflops);
-/* Failure detection: wall-time bound, in ns, of the device-side waits (for the
- * bulk copy of T and for the GEMM) of the tensor-core transform of
- * pg_nm_transform (PG_MIXED, P = 128); default 2e9 (2 s), 0 gives up at the
- * first test that finds the wait unfinished.  A wait that runs out makes the
- * call return PG_ERR_NUMERIC; the kernel first lets the copy or GEMM it waited
- * for finish (bounded by 2 s), so the context stays usable.  No counterpart in
+/* Failure detection: deadline, in ns from the kernel's start, of the
+ * device-side waits (for the bulk copy of T and for the GEMM) of the
+ * tensor-core transform of pg_nm_transform (PG_MIXED, P = 128); default 2e9
+ * (2 s); 0 makes the first wait give up.  A wait that runs out makes the call
+ * return PG_ERR_NUMERIC; the kernel first lets the copy or GEMM it waited for
+ * finish (bounded by 2 s), so the context stays usable.  No counterpart in
  * the reference, which has no device waits (it stops on a NaN,
  * verletmodule.f90:533-536). */
 int pg_set_wait_limit(pg_ctx *ctx, int64_t ns);
@@ -162,12 +162,14 @@ int pg_ti_advance(pg_ctx *ctx, int64_t nsteps);
  * milliseconds, measured with CUDA events recorded on the context's stream. */
 int pg_ti_advance_timed(pg_ctx *ctx, int64_t nsteps, double *device_ms);
 
-/* Advances the TI batches of nctx contexts on one device by nsteps each, every
- * context's steps launched on its own stream before any is waited for, so that
- * batches of different bead numbers (one context per P) run concurrently: the
- * mixed-P task list of pimd_par.f90:245-381 as one call.  device_ms (may be
- * NULL) is the device time from the first launch to the last completion.
- * No counterpart in the reference (its ranks run one task at a time). */
+/* Advances the TI batches of nctx contexts on one device by nsteps each: the
+ * mixed-P task list of pimd_par.f90:245-381 (one context per bead number P) as
+ * one call.  The step kernels of every context are captured into one CUDA
+ * graph (a concurrent branch per context, forked from and joined to the first
+ * context's stream) and the whole advance is a single graph launch; batches in
+ * the plain form run on their own streams instead.  device_ms (may be NULL) is
+ * the device time from the launch to the last completion.  No counterpart in
+ * the reference (its ranks run one task at a time). */
 int pg_ti_advance_group(pg_ctx *const *ctxs, int64_t nctx, int64_t nsteps, double *device_ms);
 /* Advance nsteps with one CUDA-event pair around every kernel launch (no graph)
  * and report, for up to 4 kernel kinds of the chosen form, the mean device time
@@ -271,6 +273,10 @@ typedef struct pg_lbfgs_opts {
     int64_t maxiter;         /* iteration cap */
     double factr;            /* relative decrease tolerance factr*eps (reference 1e6) */
     double pgtol;            /* gradient infinity-norm tolerance (reference eps2) */
+    int32_t cluster_ctas;    /* CTAs (one thread-block cluster) per polymer: 1, 2, 4 or 8; 0 = as
+                                many as the GPU holds for the batch (the sums then run in a
+                                different order, so results differ at round-off) */
+    int32_t reserved;        /* 0 */
 } pg_lbfgs_opts;
 
 /* Fixed or free end points of the polymer action (instantonmod's module
@@ -288,8 +294,9 @@ int pg_set_fixedends(pg_ctx *ctx, int32_t fixedends);
 int pg_instanton_fg(pg_ctx *ctx, int64_t nbeta, int64_t N, const double *x, const double *a,
                     const double *b, const double *betan, double *UM, double *grad);
 /* Batched instanton optimisation (instantonmod.f90:679-777) by an on-device FP64
- * L-BFGS driven by the adjoint gradient; x in/out; UM[nbeta], niter[nbeta],
- * status[nbeta] (0 converged, 1 iteration cap, 2 line-search failure). */
+ * L-BFGS driven by the adjoint gradient, each polymer on a thread-block cluster
+ * of opts->cluster_ctas CTAs; x in/out; UM[nbeta], niter[nbeta], status[nbeta]
+ * (0 converged, 1 iteration cap, 2 line-search failure). */
 int pg_instanton_optimize(pg_ctx *ctx, int64_t nbeta, int64_t N, double *x, const double *a,
                           const double *b, const double *betan, const pg_lbfgs_opts *opts,
                           double *UM, int64_t *niter, int32_t *status);

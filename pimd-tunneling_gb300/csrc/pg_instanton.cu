@@ -2,8 +2,8 @@
 //   * batched fixed-end polymer action UM and its gradient (instantonmod.f90:17-151);
 //     the PES gradient is the hand-written reverse mode of each surface, which
 //     recomputes every pair distance instead of storing forward intermediates;
-//   * batched L-BFGS driven by that gradient, one persistent CTA per beta
-//     (replaces the setulb loop of instantonmod.f90:679-777);
+//   * batched L-BFGS driven by that gradient, one thread-block cluster of up to
+//     8 CTAs per beta (replaces the setulb loop of instantonmod.f90:679-777);
 //   * mass-weighted polymer Hessian in LAPACK lower band storage (UMhessian,
 //     instantonmod.f90:155-217) and its log-determinant by a banded LDL^T with
 //     Sylvester inertia, eigenvalues below zero / the lowest one by bisection
@@ -103,88 +103,221 @@ struct LbfgsArgs {
     double factr, pgtol;
 };
 
-// Scratch per polymer: x, g, d, xt, gt (5n) + S, Y (2 m n) + rho, alpha (2m).
-__device__ __forceinline__ double dot_n(const double *a, const double *b, int n, double *sred) {
-    double s = 0.0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) s += a[i] * b[i];
-    return block_sum(s, sred);
+// Scratch per polymer: x, g, d, xt, gt (5n) + S, Y (2 m n) + 2 m (unused: rho and alpha live in
+// each CTA's shared memory).
+
+// ---------------------------------------------------------------- L-BFGS over a thread-block cluster
+// The same optimiser with each polymer spread over a cluster of CS CTAs (CS =
+// 1, 2, 4, 8): CTA r of the cluster owns beads [r N / CS, (r + 1) N / CS) of
+// every dof, evaluates their surface terms and springs and keeps its slice of
+// x, g, d, S, Y.  On GB300 the FP64 pipe of one SM bounds a polymer's
+// evaluation and two-loop recursion, so CS SMs per polymer divide that time.
+// Every dot product, norm and maximum is a CTA reduction followed by a
+// cluster reduction: each CTA writes its partial to its own shared memory,
+// the cluster synchronises (release / acquire), and every CTA reads the CS
+// partials through distributed shared memory and combines them in rank order.
+// All CTAs therefore hold bit-identical scalars and take every branch alike,
+// so they reach the same cluster barriers.  Two partial slots alternate, so one
+// cluster barrier per reduction suffices: a slot is written again only after
+// the next reduction's barrier, which every CTA reaches after reading it.
+// Neighbour beads across a slice boundary are read from global memory after a
+// cluster barrier at the start of each evaluation.
+__device__ __forceinline__ uint32_t cluster_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ double ld_dsmem(const double *p, uint32_t rank) {
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+    uint32_t ra;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(a), "r"(rank));
+    double v;
+    asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(ra) : "memory");
+    return v;
 }
 
-__global__ void __launch_bounds__(512) k_inst_lbfgs(InstArgs A, LbfgsArgs L, double *__restrict__ xio,
-                                                    double *__restrict__ scratch, double *__restrict__ um_out,
-                                                    int64_t *__restrict__ iters, int32_t *__restrict__ status) {
+struct ClRed {
+    double *sred;   // CTA reduction scratch (32 doubles)
+    double *cslot;  // this CTA's two partial slots
+    int ph;         // slot of the next reduction
+};
+
+template <int CS, bool MAX>
+__device__ __forceinline__ double cl_reduce(double v, ClRed &R) {
+    v = MAX ? block_max(v, R.sred) : block_sum(v, R.sred);
+    if (CS == 1) return v;
+    if (threadIdx.x == 0) R.cslot[R.ph] = v;
+    cluster_sync_all();
+    double t = ld_dsmem(&R.cslot[R.ph], 0);
+#pragma unroll
+    for (uint32_t r = 1; r < (uint32_t)CS; r++) {
+        const double u = ld_dsmem(&R.cslot[R.ph], r);
+        t = MAX ? fmax(t, u) : t + u;
+    }
+    R.ph ^= 1;
+    return t;
+}
+
+// The slice of one CTA: elements e = dof N + i, i in [i0, i1), walked as
+// t = dof ns + (i - i0) so that consecutive threads take consecutive beads.
+struct Slice {
+    int N, nd, i0, ns;
+    __device__ __forceinline__ int count() const { return nd * ns; }
+    __device__ __forceinline__ int elem(int t) const {
+        const int dof = t / ns;
+        return dof * N + i0 + (t - dof * ns);
+    }
+};
+
+template <int CS>
+__device__ __forceinline__ double cl_dot(const double *a, const double *b, const Slice &sl, ClRed &R) {
+    double s = 0.0;
+    for (int t = threadIdx.x; t < sl.count(); t += blockDim.x) {
+        const int e = sl.elem(t);
+        s += a[e] * b[e];
+    }
+    return cl_reduce<CS, false>(s, R);
+}
+
+// UM and dUM/dx on this CTA's slice (x and g: [dof][N]; every thread gets UM).
+template <int CS>
+__device__ double polymer_fg_cl(const InstArgs &A, int k, const double *__restrict__ x, double *__restrict__ g,
+                                const Slice &sl, ClRed &R) {
+    if (CS > 1)
+        cluster_sync_all();  // every slice of the point x is written (neighbour beads cross slices)
+    else
+        __syncthreads();
+    const int N = A.N, nd = A.nd;
+    const double bn = A.betan[k];
+    const double *b = A.b + (size_t)k * nd;
+    double part = 0.0;
+    for (int i = sl.i0 + threadIdx.x; i < sl.i0 + sl.ns; i += blockDim.x) {
+        double xb[kMaxDof], gb[kMaxDof];
+        for (int d = 0; d < nd; d++) xb[d] = x[d * N + i];
+        part += pes_vgrad<double>(A.pes, xb, gb);
+        for (int d = 0; d < nd; d++) g[d * N + i] = gb[d];
+    }
+    __syncthreads();
+    const bool fixed = A.fixedends != 0;
+    for (int t = threadIdx.x; t < sl.count(); t += blockDim.x) {
+        const int e = sl.elem(t);
+        const int dof = e / N, i = e - dof * N;
+        const double m = A.mass[dof / A.ndim];
+        const double xl = i > 0 ? x[e - 1] : (fixed ? A.a[dof] : x[e]);
+        const double xr = i < N - 1 ? x[e + 1] : (fixed ? b[dof] : x[e]);
+        g[e] = m * (2.0 * x[e] - xl - xr) / (bn * bn) + g[e];
+        const double c = 0.5 * m / (bn * bn);
+        if (i < N - 1) part += c * (x[e + 1] - x[e]) * (x[e + 1] - x[e]);
+        if (fixed && i == 0) part += c * (x[e] - A.a[dof]) * (x[e] - A.a[dof]);
+        if (fixed && i == N - 1) part += c * (b[dof] - x[e]) * (b[dof] - x[e]);
+    }
+    return cl_reduce<CS, false>(part, R);
+}
+
+template <int CS>
+__global__ void __launch_bounds__(512) k_inst_lbfgs_cl(InstArgs A, LbfgsArgs L, double *__restrict__ xio,
+                                                       double *__restrict__ scratch, double *__restrict__ um_out,
+                                                       int64_t *__restrict__ iters, int32_t *__restrict__ status) {
     __shared__ double sred[32];
-    const int k = blockIdx.x;
+    __shared__ double cslot[2];
+    __shared__ double s_rho[64], s_alpha[64];
+    const uint32_t rank = CS > 1 ? cluster_rank() : 0u;
+    const int k = (int)(blockIdx.x / CS);
     const int n = A.nd * A.N, m = L.m;
+    Slice sl;
+    sl.N = A.N;
+    sl.nd = A.nd;
+    sl.i0 = (int)((int64_t)rank * A.N / CS);
+    sl.ns = (int)((int64_t)(rank + 1) * A.N / CS) - sl.i0;
+    ClRed R{sred, cslot, 0};
     double *ws = scratch + (size_t)k * ((size_t)(5 + 2 * m) * n + 2 * m);
     double *x = ws, *g = ws + n, *d = ws + 2 * (size_t)n, *xt = ws + 3 * (size_t)n, *gt = ws + 4 * (size_t)n;
     double *S = ws + 5 * (size_t)n, *Y = S + (size_t)m * n;
-    double *rho = Y + (size_t)m * n, *alpha = rho + m;
     double *xk = xio + (size_t)k * n;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = xk[i];
-    __syncthreads();
-    double f = polymer_fg(A, k, x, g, sred);
+    const int cnt = sl.count();
+    for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+        const int e = sl.elem(t);
+        x[e] = xk[e];
+    }
+    double f = polymer_fg_cl<CS>(A, k, x, g, sl, R);
     const double eps = 2.220446049250313e-16;
     int npair = 0, head = 0;  // circular history
     int st = 1;
     int64_t it = 0;
     for (; it < L.maxiter; it++) {
         double gmax = 0.0;
-        for (int i = threadIdx.x; i < n; i += blockDim.x) gmax = fmax(gmax, fabs(g[i]));
-        gmax = block_max(gmax, sred);
+        for (int t = threadIdx.x; t < cnt; t += blockDim.x) gmax = fmax(gmax, fabs(g[sl.elem(t)]));
+        gmax = cl_reduce<CS, true>(gmax, R);
         if (gmax <= L.pgtol) {
             st = 0;
             break;
         }
         // two-loop recursion: d = -H g
-        for (int i = threadIdx.x; i < n; i += blockDim.x) d[i] = -g[i];
+        for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+            const int e = sl.elem(t);
+            d[e] = -g[e];
+        }
         __syncthreads();
         for (int c = 0; c < npair; c++) {
-            int j = (head - 1 - c + m) % m;
-            double a_ = rho[j] * dot_n(S + (size_t)j * n, d, n, sred);
-            if (threadIdx.x == 0) alpha[j] = a_;
-            for (int i = threadIdx.x; i < n; i += blockDim.x) d[i] -= a_ * Y[(size_t)j * n + i];
+            const int j = (head - 1 - c + m) % m;
+            const double a_ = s_rho[j] * cl_dot<CS>(S + (size_t)j * n, d, sl, R);
+            if (threadIdx.x == 0) s_alpha[j] = a_;
+            for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+                const int e = sl.elem(t);
+                d[e] -= a_ * Y[(size_t)j * n + e];
+            }
             __syncthreads();
         }
         if (npair > 0) {
-            int j = (head - 1 + m) % m;
-            double yy = dot_n(Y + (size_t)j * n, Y + (size_t)j * n, n, sred);
-            double gam = 1.0 / (rho[j] * yy);
-            for (int i = threadIdx.x; i < n; i += blockDim.x) d[i] *= gam;
+            const int j = (head - 1 + m) % m;
+            const double yy = cl_dot<CS>(Y + (size_t)j * n, Y + (size_t)j * n, sl, R);
+            const double gam = 1.0 / (s_rho[j] * yy);
+            for (int t = threadIdx.x; t < cnt; t += blockDim.x) d[sl.elem(t)] *= gam;
             __syncthreads();
         }
         for (int c = npair - 1; c >= 0; c--) {
-            int j = (head - 1 - c + m) % m;
-            double bt = rho[j] * dot_n(Y + (size_t)j * n, d, n, sred);
-            double a_ = alpha[j];
-            for (int i = threadIdx.x; i < n; i += blockDim.x) d[i] += (a_ - bt) * S[(size_t)j * n + i];
+            const int j = (head - 1 - c + m) % m;
+            const double bt = s_rho[j] * cl_dot<CS>(Y + (size_t)j * n, d, sl, R);
+            const double a_ = s_alpha[j];
+            for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+                const int e = sl.elem(t);
+                d[e] += (a_ - bt) * S[(size_t)j * n + e];
+            }
             __syncthreads();
         }
-        double gd = dot_n(g, d, n, sred);
+        double gd = cl_dot<CS>(g, d, sl, R);
         if (!(gd < 0.0)) {  // not a descent direction: restart from steepest descent
             npair = 0;
-            for (int i = threadIdx.x; i < n; i += blockDim.x) d[i] = -g[i];
+            for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+                const int e = sl.elem(t);
+                d[e] = -g[e];
+            }
             __syncthreads();
-            gd = dot_n(g, d, n, sred);
+            gd = cl_dot<CS>(g, d, sl, R);
         }
         // initial step: 1, or 1/|d| before any curvature pair (as L-BFGS-B's first iteration)
         double t = 1.0;
         if (npair == 0) {
-            double dn = sqrt(dot_n(d, d, n, sred));
+            const double dn = sqrt(cl_dot<CS>(d, d, sl, R));
             t = dn > 0.0 ? fmin(1.0, 1.0 / dn) : 1.0;
         }
         bool accepted = false;
         double ft = 0.0;
         for (int bt = 0; bt <= L.max_bt; bt++) {
-            for (int i = threadIdx.x; i < n; i += blockDim.x) xt[i] = x[i] + t * d[i];
-            __syncthreads();
-            ft = polymer_fg(A, k, xt, gt, sred);
+            for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
+                const int e = sl.elem(q);
+                xt[e] = x[e] + t * d[e];
+            }
+            ft = polymer_fg_cl<CS>(A, k, xt, gt, sl, R);
             if (ft <= f + 1.0e-4 * t * gd) {
                 accepted = true;
                 break;
             }
             // safeguarded quadratic interpolation of f(t)
-            double tq = -gd * t * t / (2.0 * (ft - f - gd * t));
+            const double tq = -gd * t * t / (2.0 * (ft - f - gd * t));
             t = (tq > 0.1 * t && tq < 0.5 * t) ? tq : 0.5 * t;
         }
         if (!accepted) {
@@ -193,22 +326,24 @@ __global__ void __launch_bounds__(512) k_inst_lbfgs(InstArgs A, LbfgsArgs L, dou
         }
         // new curvature pair s = xt - x, y = gt - g
         double *Sj = S + (size_t)head * n, *Yj = Y + (size_t)head * n;
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            Sj[i] = xt[i] - x[i];
-            Yj[i] = gt[i] - g[i];
+        for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
+            const int e = sl.elem(q);
+            Sj[e] = xt[e] - x[e];
+            Yj[e] = gt[e] - g[e];
         }
         __syncthreads();
-        double sy = dot_n(Sj, Yj, n, sred);
-        double yy = dot_n(Yj, Yj, n, sred);
+        const double sy = cl_dot<CS>(Sj, Yj, sl, R);
+        const double yy = cl_dot<CS>(Yj, Yj, sl, R);
         if (sy > eps * yy) {
-            if (threadIdx.x == 0) rho[head] = 1.0 / sy;
+            if (threadIdx.x == 0) s_rho[head] = 1.0 / sy;
             head = (head + 1) % m;
             npair = npair < m ? npair + 1 : m;
         }
         const double fold = f;
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            x[i] = xt[i];
-            g[i] = gt[i];
+        for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
+            const int e = sl.elem(q);
+            x[e] = xt[e];
+            g[e] = gt[e];
         }
         f = ft;
         __syncthreads();
@@ -219,12 +354,16 @@ __global__ void __launch_bounds__(512) k_inst_lbfgs(InstArgs A, LbfgsArgs L, dou
             break;
         }
     }
-    for (int i = threadIdx.x; i < n; i += blockDim.x) xk[i] = x[i];
-    if (threadIdx.x == 0) {
+    for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
+        const int e = sl.elem(q);
+        xk[e] = x[e];
+    }
+    if (threadIdx.x == 0 && rank == 0) {
         um_out[k] = f;
         iters[k] = it;
         status[k] = st;
     }
+    if (CS > 1) cluster_sync_all();  // no CTA leaves while another may still read its partial slots
 }
 
 // Per-bead PES Hessians of polymer k (FD surfaces: one thread per (bead, column)).
@@ -582,6 +721,10 @@ extern "C" int pg_instanton_optimize(pg_ctx *ctx, int64_t nbeta, int64_t N, doub
     if (nbeta < 1 || N < 2 || !x || !betan || !opts) return fail(PG_ERR_ARG, "bad optimize arguments");
     if (opts->m < 1 || opts->m > 64 || opts->maxiter < 1 || opts->max_backtracks < 0)
         return fail(PG_ERR_ARG, "bad L-BFGS options");
+    const int cs_req = opts->cluster_ctas;
+    if (cs_req != 0 && cs_req != 1 && cs_req != 2 && cs_req != 4 && cs_req != 8)
+        return fail(PG_ERR_ARG, "cluster_ctas must be 0, 1, 2, 4 or 8");
+    if (cs_req > N) return fail(PG_ERR_ARG, "cluster_ctas exceeds the number of beads");
     const int nd = ctx->nd;
     const size_t n1 = (size_t)nd * N, n = (size_t)nbeta * n1;
     DevBuf dx, dab, dum, dit, dst;
@@ -599,8 +742,35 @@ extern "C" int pg_instanton_optimize(pg_ctx *ctx, int64_t nbeta, int64_t N, doub
     L.maxiter = opts->maxiter;
     L.factr = opts->factr;
     L.pgtol = opts->pgtol;
-    k_inst_lbfgs<<<(unsigned)nbeta, 512, 0, ctx->stream>>>(A, L, dx.as<double>(), ctx->scratch_b.as<double>(),
-                                                            dum.as<double>(), dit.as<int64_t>(), dst.as<int32_t>());
+    // CTAs per polymer: as many as the GPU holds for the whole batch in one
+    // wave (at most 8, a portable cluster), keeping at least 16 beads per CTA
+    int cs = cs_req;
+    if (cs == 0) {
+        cs = 1;
+        while (cs < 8 && nbeta * (cs * 2) <= (int64_t)ctx->sm_count && N >= 16 * (int64_t)(cs * 2)) cs *= 2;
+    }
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3((unsigned)(nbeta * cs));
+    lc.blockDim = dim3(512);
+    lc.stream = ctx->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)cs;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    lc.attrs = attr;
+    lc.numAttrs = 1;
+    double *xdev = dx.as<double>(), *sdev = ctx->scratch_b.as<double>(), *udev = dum.as<double>();
+    int64_t *idev = dit.as<int64_t>();
+    int32_t *stdev = dst.as<int32_t>();
+    cudaError_t e = cudaSuccess;
+    switch (cs) {
+        case 1: e = cudaLaunchKernelEx(&lc, k_inst_lbfgs_cl<1>, A, L, xdev, sdev, udev, idev, stdev); break;
+        case 2: e = cudaLaunchKernelEx(&lc, k_inst_lbfgs_cl<2>, A, L, xdev, sdev, udev, idev, stdev); break;
+        case 4: e = cudaLaunchKernelEx(&lc, k_inst_lbfgs_cl<4>, A, L, xdev, sdev, udev, idev, stdev); break;
+        default: e = cudaLaunchKernelEx(&lc, k_inst_lbfgs_cl<8>, A, L, xdev, sdev, udev, idev, stdev); break;
+    }
+    PG_CUDA(e);
     PG_CUDA(cudaGetLastError());
     PG_CUDA(cudaMemcpyAsync(x, dx.ptr, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     if (UM) PG_CUDA(cudaMemcpyAsync(UM, dum.ptr, nbeta * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));

@@ -112,6 +112,9 @@ struct TiState {
     DevBuf red;              // reduction output
     std::map<int64_t, cudaGraphExec_t> graphs;
     std::string graph_sig;   // signature of the batch the graphs were captured for
+    // pg_ti_advance_group with this context first: one graph over every context
+    // of the group, keyed by the step count and all the batches' signatures
+    std::map<std::string, cudaGraphExec_t> group_graphs;
     ~TiState();
 };
 

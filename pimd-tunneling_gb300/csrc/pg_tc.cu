@@ -99,16 +99,16 @@ __device__ __forceinline__ bool mbar_test_wait(uint64_t *bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// Wait bounded by a caller-set wall-time limit (the context's wait limit):
-// the clock is read after every unsuccessful test, so a limit of 0 gives up at
-// the first test that finds the phase incomplete.  A caller whose wait gives up
-// must still let the operation it waited for finish (mbar_wait, bounded by the
-// fixed limit) before the CTA frees tensor memory or exits.
-__device__ __forceinline__ bool mbar_wait_ns(uint64_t *bar, uint32_t parity, uint64_t limit_ns) {
-    const uint64_t t0 = globaltimer_ns();
+// Wait bounded by a deadline: it gives up once limit_ns have passed since t0
+// (the kernel's start), and the deadline is checked before each test, so a
+// limit of 0 gives up at the first wait whatever the state of the phase.  A
+// caller whose wait gives up must still let the operation it waited for finish
+// (mbar_wait, bounded by the fixed limit) before the CTA frees tensor memory or
+// exits.
+__device__ __forceinline__ bool mbar_wait_until(uint64_t *bar, uint32_t parity, uint64_t t0, uint64_t limit_ns) {
     for (long long i = 0; i < kSpinLimit; i++) {
-        if (mbar_test_wait(bar, parity)) return true;
         if (globaltimer_ns() - t0 >= limit_ns) return false;
+        if (mbar_test_wait(bar, parity)) return true;
     }
     return false;
 }
@@ -289,15 +289,17 @@ __device__ __forceinline__ void load_transform(unsigned char *Thi, const unsigne
 
 // ---------------------------------------------------------------- standalone transform
 // out[c][:] = T in[c][:] for 128 columns per CTA (used by pg_nm_transform, P = 128).
-// The waits for the T copy and for the GEMM are bounded by wait_ns (the
-// context's wait limit).  A wait that gives up records the error and then waits
-// (bounded by the fixed 2 s limit) for that copy or GEMM to finish, so that no
-// asynchronous write into shared or tensor memory outlives the CTA's
-// deallocation and exit; the GEMM is not issued after a failed copy wait.
+// The waits for the T copy and for the GEMM share a deadline of wait_ns (the
+// context's wait limit) from the kernel's start.  A wait that gives up records
+// the error and then waits (bounded by the fixed 2 s limit) for that copy or
+// GEMM to finish, so that no asynchronous write into shared or tensor memory
+// outlives the CTA's deallocation and exit; the GEMM is not issued after a
+// failed copy wait.
 __global__ void __launch_bounds__(128, 1) k_tc_transform(const unsigned char *__restrict__ gT,
                                                           const double *__restrict__ in,
                                                           double *__restrict__ out, int64_t ncol,
                                                           int32_t *__restrict__ err, uint64_t wait_ns) {
+    const uint64_t t_start = globaltimer_ns();
     extern __shared__ unsigned char dsm[];
     unsigned char *base = align1k(dsm);
     unsigned char *Thi = base, *Tlo = base + kOpBytes, *Ahi = base + 2 * kOpBytes, *Alo = base + 3 * kOpBytes;
@@ -326,7 +328,7 @@ __global__ void __launch_bounds__(128, 1) k_tc_transform(const unsigned char *__
     tc_after();
     const uint32_t tmem = sh->tmem_slot;
     if (tid == 0) {
-        if (mbar_wait_ns(&sh->tma_bar, 0, wait_ns)) {
+        if (mbar_wait_until(&sh->tma_bar, 0, t_start, wait_ns)) {
             issue_gemm(tmem, 0, smem_u32(Ahi), smem_u32(Alo), smem_u32(Thi), smem_u32(Tlo), &sh->mma_bar);
         } else {
             sh->err = 1;
@@ -335,7 +337,7 @@ __global__ void __launch_bounds__(128, 1) k_tc_transform(const unsigned char *__
     }
     __syncthreads();
     bool issued = sh->err == 0;
-    if (issued && !mbar_wait_ns(&sh->mma_bar, 0, wait_ns)) {
+    if (issued && !mbar_wait_until(&sh->mma_bar, 0, t_start, wait_ns)) {
         atomicOr(&sh->err, 2);
         mbar_wait(&sh->mma_bar, 0);  // the GEMM finishes before TMEM is read or freed
     }

@@ -27,6 +27,8 @@ void build_transmatrix(int P, std::vector<double> &T);
 TiState::~TiState() {
     for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
     graphs.clear();
+    for (auto &kv : group_graphs) cudaGraphExecDestroy(kv.second);
+    group_graphs.clear();
 }
 
 // ---------------------------------------------------------------- device params
@@ -970,6 +972,8 @@ static int ti_setup_impl(pg_ctx *ctx, const pg_ti_config *cfg, int64_t nrings, i
         if (sig != st.graph_sig) {
             for (auto &kv : st.graphs) cudaGraphExecDestroy(kv.second);
             st.graphs.clear();
+            for (auto &kv : st.group_graphs) cudaGraphExecDestroy(kv.second);
+            st.group_graphs.clear();
             st.graph_sig = sig;
         }
     }
@@ -1034,6 +1038,8 @@ static int ti_setup_impl(pg_ctx *ctx, const pg_ti_config *cfg, int64_t nrings, i
         if (sig != st.graph_sig) {
             for (auto &kv : st.graphs) cudaGraphExecDestroy(kv.second);
             st.graphs.clear();
+            for (auto &kv : st.group_graphs) cudaGraphExecDestroy(kv.second);
+            st.group_graphs.clear();
             st.graph_sig = sig;
         }
     }
@@ -1167,6 +1173,58 @@ static int ti_graph(pg_ctx *ctx, int64_t n, cudaGraphExec_t *out) {
     return PG_OK;
 }
 
+// One executable graph for an nsteps advance of every context of a group (one
+// batch per bead number): the first context's stream forks to the others by an
+// event, each context's step kernels are captured on its own stream, and the
+// branches join back, so the whole uneven-P advance is a single graph launch
+// whose branches run concurrently.  Cached on the first context, keyed by the
+// step count and every batch's graph signature (which holds each buffer
+// address the launches bake in).
+static int group_graph(pg_ctx *const *ctxs, int64_t nctx, int64_t n, cudaGraphExec_t *out) {
+    TiState &st0 = *ctxs[0]->ti;
+    std::string key(reinterpret_cast<const char *>(&n), sizeof(n));
+    for (int64_t i = 0; i < nctx; i++) {
+        const std::string &g = ctxs[i]->ti->graph_sig;
+        const uint64_t len = g.size();
+        key.append(reinterpret_cast<const char *>(&len), sizeof(len));
+        key += g;
+    }
+    auto it = st0.group_graphs.find(key);
+    if (it != st0.group_graphs.end()) {
+        *out = it->second;
+        return PG_OK;
+    }
+    cudaStream_t s0 = ctxs[0]->stream;
+    std::vector<cudaEvent_t> ev((size_t)nctx, nullptr);
+    for (auto &e : ev) PG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    cudaGraph_t g = nullptr;
+    int lrc = PG_OK;
+    cudaError_t ce = cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal);
+    if (ce == cudaSuccess) {
+        cudaEventRecord(ev[0], s0);
+        for (int64_t i = 1; i < nctx; i++) cudaStreamWaitEvent(ctxs[i]->stream, ev[0], 0);
+        for (int64_t i = 0; i < nctx && !lrc; i++) lrc = launch_steps(ctxs[i], *ctxs[i]->ti, n, ctxs[i]->stream);
+        for (int64_t i = 1; i < nctx; i++) {  // every branch joins stream 0, also after a failed launch
+            cudaEventRecord(ev[i], ctxs[i]->stream);
+            cudaStreamWaitEvent(s0, ev[i], 0);
+        }
+        ce = cudaStreamEndCapture(s0, &g);
+    }
+    for (auto e : ev) cudaEventDestroy(e);
+    if (lrc) {
+        if (g) cudaGraphDestroy(g);
+        return lrc;
+    }
+    if (ce != cudaSuccess) return cuda_fail(ce, "capture of the group graph");
+    cudaGraphExec_t exec = nullptr;
+    ce = cudaGraphInstantiate(&exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) return cuda_fail(ce, "cudaGraphInstantiate (group)");
+    st0.group_graphs[key] = exec;
+    *out = exec;
+    return PG_OK;
+}
+
 // Checks an advance of nsteps and captures the graphs it needs.  launch = true
 // also replays them on the context's stream (without waiting).  Plain form:
 // graphs of up to 64 steps; fused forms: one graph per nsteps.
@@ -1230,10 +1288,39 @@ static int ti_advance_group(pg_ctx *const *ctxs, int64_t nctx, int64_t nsteps, d
     }
     PG_CUDA(cudaSetDevice(ctxs[0]->device));
     for (int64_t i = 0; i < nctx; i++) {
-        int rc = ti_enqueue(ctxs[i], nsteps, false);  // capture outside the timed span
+        int rc = ti_enqueue(ctxs[i], nsteps, false);  // checks; captures outside the timed span
         if (rc) return rc;
     }
     cudaStream_t s0 = ctxs[0]->stream;
+    bool combined = nctx > 1;  // the plain form replays graphs of up to 64 steps: per-stream path
+    for (int64_t i = 0; i < nctx; i++)
+        if (ctxs[i]->ti->form == PG_FORM_PLAIN) combined = false;
+    if (combined) {
+        cudaGraphExec_t exec = nullptr;
+        int rc = group_graph(ctxs, nctx, nsteps, &exec);
+        if (rc) return rc;
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        PG_CUDA(cudaEventCreate(&e0));
+        cudaError_t ce = cudaEventCreate(&e1);
+        if (ce == cudaSuccess) ce = cudaEventRecord(e0, s0);
+        if (ce == cudaSuccess) ce = cudaGraphLaunch(exec, s0);
+        if (ce == cudaSuccess) ce = cudaEventRecord(e1, s0);
+        // the group's work ran on stream 0: wait for it there first
+        for (int64_t i = 0; i < nctx; i++) {
+            int r = ti_finish(ctxs[i], nsteps);
+            if (r && !rc) rc = r;
+        }
+        if (ce != cudaSuccess && !rc) rc = cuda_fail(ce, "group graph launch");
+        if (!rc && device_ms) {
+            float ms = 0.f;
+            ce = cudaEventElapsedTime(&ms, e0, e1);
+            if (ce != cudaSuccess) rc = cuda_fail(ce, "cudaEventElapsedTime");
+            *device_ms = (double)ms;
+        }
+        cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        return rc;
+    }
     std::vector<cudaEvent_t> ev;
     auto cleanup = [&]() {
         for (auto e : ev) cudaEventDestroy(e);

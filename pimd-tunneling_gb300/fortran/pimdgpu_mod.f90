@@ -33,6 +33,7 @@ module pimdgpu
      integer(c_int32_t) :: m, max_backtracks
      integer(c_int64_t) :: maxiter
      real(c_double)     :: factr, pgtol
+     integer(c_int32_t) :: cluster_ctas = 0, reserved = 0
   end type pg_lbfgs_opts
 
   interface

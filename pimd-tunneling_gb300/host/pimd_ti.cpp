@@ -320,7 +320,7 @@ int main(int argc, char **argv) {
                                 &xt[(size_t)k * n + bead], nullptr));
         }
         std::printf(" Finding instanton\n");
-        pg_lbfgs_opts o;
+        pg_lbfgs_opts o{};
         o.m = 8;  // instantonmod.f90:716
         o.max_backtracks = 40;
         o.maxiter = 200000;

@@ -218,7 +218,7 @@ int main(int argc, char **argv) {
         for (int j = 0; j < nd; j++) std::printf(" %d %.15g\n", j + 1, eta2[j] * 219475.0);
     }
     std::printf(" Locating instanton\n");
-    pg_lbfgs_opts o;
+    pg_lbfgs_opts o{};
     o.m = m;
     o.max_backtracks = 40;
     o.maxiter = maxiter;

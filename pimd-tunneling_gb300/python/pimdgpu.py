@@ -45,7 +45,8 @@ class TiConfig(C.Structure):
 
 class LbfgsOpts(C.Structure):
     _fields_ = [("m", C.c_int32), ("max_backtracks", C.c_int32), ("maxiter", C.c_int64),
-                ("factr", C.c_double), ("pgtol", C.c_double)]
+                ("factr", C.c_double), ("pgtol", C.c_double), ("cluster_ctas", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 class PgError(RuntimeError):
@@ -399,13 +400,13 @@ class Context:
         return UM, g
 
     def instanton_optimize(self, N, x, a, b, betan, m=8, factr=1.0e6, pgtol=1.0e-5, maxiter=20000,
-                           max_backtracks=40):
+                           max_backtracks=40, cluster_ctas=0):
         x = np.array(x, dtype=np.float64)
         betan = _f64(np.atleast_1d(betan))
         a = None if a is None else _f64(a)
         b = None if b is None else _f64(np.atleast_1d(b))
         nb = betan.size
-        o = LbfgsOpts(m, max_backtracks, maxiter, factr, pgtol)
+        o = LbfgsOpts(m, max_backtracks, maxiter, factr, pgtol, cluster_ctas, 0)
         UM = np.zeros(nb)
         it = np.zeros(nb, dtype=np.int64)
         st = np.zeros(nb, dtype=np.int32)

@@ -140,12 +140,11 @@ def test_nan_ring_is_flagged_and_isolated(ctx, pg, form):
 
 @pytest.mark.gpu
 def test_transform_wait_that_runs_out_is_reported_and_the_context_stays_usable(ctx, pg):
-    """Failure detection without a GPU fault: with the wait limit at 0 the
-    tensor-core transform's bounded wait gives up at its first unfinished test
-    (the GEMM of a single 128-column tile takes far longer than one test), the
-    kernel lets the copy / GEMM it waited for finish, and the call returns
-    PG_ERR_NUMERIC; back at the default limit, the same context transforms the
-    same columns correctly."""
+    """Failure detection without a GPU fault: with the wait limit (a deadline
+    from the kernel's start) at 0, the tensor-core transform's first bounded
+    wait -- for the bulk copy of T -- gives up, the kernel lets the copy land and
+    issues no GEMM, and the call returns PG_ERR_NUMERIC; back at the default
+    limit, the same context transforms the same columns correctly."""
     P = 128
     cols = np.random.RandomState(5).randn(128 * P)  # one tile
     ref = ctx.nm_transform(P, cols, pg.PG_FP64)

@@ -189,3 +189,31 @@ def test_free_ended_lbfgs_matches_scipy_lbfgsb(ctx, pg, oracle, name):
         # the optimiser's value is the free-ended action of the path it returns
         uo = oracle.UM(pes, mass, N, betans[k], x[k * n:(k + 1) * n], w1, w2, False)
         assert abs(UM[k] - uo) <= 1e-12 * max(1.0, abs(uo))
+
+
+def test_lbfgs_cluster_sizes_reach_the_same_instanton(ctx, pg, oracle):
+    """The optimiser spread over a thread-block cluster of 1, 2, 4 or 8 CTAs per
+    polymer (dot products reduced across the cluster through distributed shared
+    memory): every cluster size converges, and the actions agree with each other
+    and with scipy L-BFGS-B on the oracle's action to 1e-9 (the sums run in
+    different orders, so the iterates differ at round-off)."""
+    c, pes, mass = _system(ctx, oracle, "c3")
+    w1, w2 = np.array(c["well1"]), np.array(c["well2"])
+    N = 64
+    betas = np.array(c["betas"])[[0, 15, -1]]
+    betans = betas / N
+    x0 = np.concatenate([_linear_path(w1, w2, N) for _ in range(3)])
+    res = {}
+    for cs in (1, 2, 4, 8, 0):
+        x, UM, it, st = ctx.instanton_optimize(N, x0, w1, np.tile(w2, 3), betans, m=10, factr=1e2, pgtol=1e-9,
+                                               maxiter=200000, cluster_ctas=cs)
+        assert np.all(st == 0), (cs, st, it)
+        res[cs] = UM
+    n = N * len(w1)
+    for k in range(3):
+        _, fo, _ = oracle.instanton_lbfgs(pes, mass, N, betans[k], x0[k * n:(k + 1) * n], w1, w2, m=10, factr=1e2,
+                                          pgtol=1e-9, maxiter=200000)
+        for cs, UM in res.items():
+            assert abs(UM[k] - fo) <= 1e-9 * abs(fo), (cs, k, UM[k], fo)
+    with pytest.raises(pg.PgError):
+        ctx.instanton_optimize(N, x0, w1, np.tile(w2, 3), betans, cluster_ctas=3)

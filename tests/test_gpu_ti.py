@@ -423,6 +423,41 @@ def test_advance_group_equals_separate_advances(pg):
             np.testing.assert_array_equal(u, v)
 
 
+def test_advance_group_one_graph_over_tensor_and_simt_batches(pg):
+    """An uneven-P group in one graph launch: the persistent tcgen05 step kernel
+    (P = 128, 2-D surface), the blocked tcgen05 form (P = 256, 27-dof surface) and
+    the fused SIMT form (P = 64) as concurrent branches of one captured graph,
+    advanced twice by 25 steps (the second call replays the cached graph), give
+    bitwise the state and estimator sums of advancing each batch alone by 50."""
+    specs = [("c1", 128, pg.PG_FORM_TENSOR, 40), ("c2", 256, pg.PG_FORM_TENSOR, 3), ("c1", 64, pg.PG_FORM_FUSED, 5)]
+    runs = []
+    for together in (False, True):
+        ctxs = []
+        for name, P, form, nrep in specs:
+            c = dict(pgconfigs.load(name))
+            c["P"] = P
+            ti = pgconfigs.TiInputs(c, nrep=nrep, nintegral=2)
+            cx = pg.Context(0)
+            _set_system(cx, c)
+            cfg = _gpu_cfg(pg, c, ti, pg.PG_MIXED, form)
+            cx.ti_setup(cfg, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
+            assert cx.ti_form(1)[0] == form
+            ctxs.append(cx)
+        if together:
+            for _ in range(2):
+                assert pg.Context.ti_advance_group(ctxs, 25) > 0.0
+        else:
+            for cx in ctxs:
+                cx.ti_advance(50)
+        runs.append([(cx.ti_state(), cx.ti_results()[:2], cx.ti_step()) for cx in ctxs])
+        for cx in ctxs:
+            cx.close()
+    for (st_a, res_a, step_a), (st_b, res_b, step_b) in zip(*runs):
+        assert step_a == step_b == 50
+        for u, v in zip(st_a + res_a, st_b + res_b):
+            np.testing.assert_array_equal(u, v)
+
+
 def _tensor_vs_simt(ctx, pg, c, ti, nsteps=20):
     _set_system(ctx, c)
     x1, p1, s1, n1, st1 = _run(ctx, pg, c, ti, pg.PG_MIXED, pg.PG_FORM_FUSED, nsteps)
