@@ -206,13 +206,16 @@ __device__ double polymer_fg_cl(const InstArgs &A, int k, const double *__restri
         const int e = sl.elem(t);
         const int dof = e / N, i = e - dof * N;
         const double m = A.mass[dof / A.ndim];
-        const double xl = i > 0 ? x[e - 1] : (fixed ? A.a[dof] : x[e]);
-        const double xr = i < N - 1 ? x[e + 1] : (fixed ? b[dof] : x[e]);
-        g[e] = m * (2.0 * x[e] - xl - xr) / (bn * bn) + g[e];
+        const double xe = x[e];
+        // neighbours may lie in another CTA's slice: read them from L2 (__ldcg)
+        const double xn = i < N - 1 ? __ldcg(x + e + 1) : 0.0;
+        const double xl = i > 0 ? __ldcg(x + e - 1) : (fixed ? A.a[dof] : xe);
+        const double xr = i < N - 1 ? xn : (fixed ? b[dof] : xe);
+        g[e] = m * (2.0 * xe - xl - xr) / (bn * bn) + g[e];
         const double c = 0.5 * m / (bn * bn);
-        if (i < N - 1) part += c * (x[e + 1] - x[e]) * (x[e + 1] - x[e]);
-        if (fixed && i == 0) part += c * (x[e] - A.a[dof]) * (x[e] - A.a[dof]);
-        if (fixed && i == N - 1) part += c * (b[dof] - x[e]) * (b[dof] - x[e]);
+        if (i < N - 1) part += c * (xn - xe) * (xn - xe);
+        if (fixed && i == 0) part += c * (xe - A.a[dof]) * (xe - A.a[dof]);
+        if (fixed && i == N - 1) part += c * (b[dof] - xe) * (b[dof] - xe);
     }
     return cl_reduce<CS, false>(part, R);
 }
