@@ -219,6 +219,18 @@ extern "C" int pg_set_system(pg_ctx *ctx, int64_t ndim, int64_t natom, const dou
     ctx->V0 = V0;
     ctx->mass.assign(mass, mass + natom);
     ctx->params.assign(params, params + nparams);
+    ctx->canon9 = 0;
+    if (pes_id == PG_PES_SYNTH9 && natom == 9 && ndim == 3 && nparams >= 1 + 5 * 36 + 5 && params[0] == 36.0) {
+        int q = 0, ok = 1;
+        for (int i = 0; i < 9; i++)
+            for (int j = i + 1; j < 9; j++, q++)
+                if (params[1 + 5 * q] != (double)i || params[2 + 5 * q] != (double)j) ok = 0;
+        for (int k = 0; k < 3; k++) {  // the quartic's atoms lie in 0..8
+            const double a = params[1 + 5 * 36 + k];
+            if (!(a >= 0.0 && a <= 8.0 && a == (double)(int)a)) ok = 0;
+        }
+        ctx->canon9 = ok;
+    }
     PG_CUDA(ctx->d_params.ensure(sizeof(double) * (nparams > 0 ? nparams : 1)));
     if (nparams > 0)
         PG_CUDA(cudaMemcpyAsync(ctx->d_params.ptr, ctx->params.data(), sizeof(double) * nparams,

@@ -171,6 +171,7 @@ constexpr int kMaxDofPes = 64;  // = kMaxDof (the largest surface: 18 atoms x 3 
 
 struct PesArgs {
     int id, ndim, natom, nd, nparams;
+    int canon9;  // 9-atom surface whose table lists all 36 pairs i < j in order (unrolled FP32 path)
     double V0;
     const double *params;  // device (or shared) pointer
     // FP32 copy of params (device or shared), read by the FP32 surfaces so that
@@ -290,11 +291,93 @@ template <typename R> __device__ __forceinline__ R my_acos(R v);
 template <> __device__ __forceinline__ double my_acos<double>(double v) { return acos(v); }
 template <> __device__ __forceinline__ float my_acos<float>(float v) { return acosf(v); }
 
+// The 9-atom surface when its table lists all 36 pairs i < j in order: the
+// pair loops are unrolled, so every atom index is a compile-time constant and
+// the 27 coordinates and gradient components stay in registers (the table's
+// indices need local or shared arrays).  The arithmetic and its order are those
+// of pes_synth9; the quartic's three atoms are picked by comparisons.
+template <typename R>
+__device__ __forceinline__ R pes_synth9_canon(const PesArgs &pa, const R *x, R *g) {
+    const R *pp = pes_params<R>(pa);
+    R xr[27], gr[27];
+#pragma unroll
+    for (int k = 0; k < 27; k++) {
+        xr[k] = x[k];
+        gr[k] = 0;
+    }
+    R v = 0;
+#pragma unroll
+    for (int i = 0; i < 9; i++)
+#pragma unroll
+        for (int j = i + 1; j < 9; j++) {
+            const int q = i * 8 - i * (i - 1) / 2 + (j - i - 1);  // position of (i, j) in the list
+            const R *r = pp + 1 + 5 * q;
+            const R D = (R)r[2], a = (R)r[3], r0 = (R)r[4];
+            const R d0 = xr[3 * i] - xr[3 * j], d1 = xr[3 * i + 1] - xr[3 * j + 1], d2 = xr[3 * i + 2] - xr[3 * j + 2];
+            const R rr = my_sqrt<R>(d0 * d0 + d1 * d1 + d2 * d2);
+            const R e = my_exp<R>(-a * (rr - r0));
+            const R om = (R)1.0 - e;
+            v += D * om * om;
+            if (g) {
+                const R dvdr = pdiv<R>((R)2.0 * D * a * om * e, rr);
+                gr[3 * i] += dvdr * d0;
+                gr[3 * i + 1] += dvdr * d1;
+                gr[3 * i + 2] += dvdr * d2;
+                gr[3 * j] -= dvdr * d0;
+                gr[3 * j + 1] -= dvdr * d1;
+                gr[3 * j + 2] -= dvdr * d2;
+            }
+        }
+    const R *w = pp + 1 + 5 * 36;
+    const int iH = (int)w[0], iO1 = (int)w[1], iO2 = (int)w[2];
+    const R B = (R)w[3], s0 = (R)w[4];
+    R xH[3] = {0, 0, 0}, xO1[3] = {0, 0, 0}, xO2[3] = {0, 0, 0};
+#pragma unroll
+    for (int at = 0; at < 9; at++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            if (at == iH) xH[c] = xr[3 * at + c];
+            if (at == iO1) xO1[c] = xr[3 * at + c];
+            if (at == iO2) xO2[c] = xr[3 * at + c];
+        }
+    R e1[3], e2[3], r1 = 0, r2 = 0;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        e1[c] = xH[c] - xO1[c];
+        e2[c] = xH[c] - xO2[c];
+        r1 += e1[c] * e1[c];
+        r2 += e2[c] * e2[c];
+    }
+    r1 = my_sqrt<R>(r1);
+    r2 = my_sqrt<R>(r2);
+    const R s = r1 - r2;
+    const R t = (s / s0) * (s / s0) - (R)1.0;
+    v += B * t * t;
+    if (g) {
+        const R dvds = (R)4.0 * B * t * s / (s0 * s0);
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const R a1 = dvds * e1[c] / r1, a2 = dvds * e2[c] / r2;
+#pragma unroll
+            for (int at = 0; at < 9; at++) {
+                if (at == iH) gr[3 * at + c] += a1 - a2;
+                if (at == iO1) gr[3 * at + c] -= a1;
+                if (at == iO2) gr[3 * at + c] += a2;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 27; k++) g[k] = gr[k];
+    }
+    return v - (R)pa.V0;
+}
+
 // Synthetic 9-atom surface: Morse pair network + quartic double well in
 // s = |r_H - r_O1| - |r_H - r_O2|.  Reverse-mode gradient: each pair's
 // distance is recomputed, dV/dr is scattered through dr/dx (Wilson B row).
 template <typename R>
 __device__ __forceinline__ R pes_synth9(const PesArgs &pa, const R *x, R *g) {
+    if constexpr (sizeof(R) == 4)  // FP32 only: the FP64 callers run 512-thread CTAs whose registers it would exceed
+        if (pa.canon9) return pes_synth9_canon<R>(pa, x, g);
     const R *pp = pes_params<R>(pa);
     int npair = (int)pp[0];
     if (g)

@@ -127,6 +127,7 @@ struct pg_ctx {
     // system (mcmod_mass module state)
     bool have_system = false;
     int ndim = 0, natom = 0, nd = 0, pes_id = 0;
+    int canon9 = 0;  // the 9-atom surface's table lists all 36 pairs i < j in order
     double V0 = 0.0;
     std::vector<double> mass, params;
     std::vector<float> fparams;  // host copy of the FP32 surface parameters (PesArgs::fparams)
@@ -148,6 +149,7 @@ struct pg_ctx {
         pa.natom = natom;
         pa.nd = nd;
         pa.nparams = (int)params.size();
+        pa.canon9 = canon9;
         pa.V0 = V0;
         pa.params = d_params.as<double>();
         pa.fparams = d_fparams.as<float>();

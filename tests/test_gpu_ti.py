@@ -88,6 +88,34 @@ def test_pes_eval_matches_oracle(ctx, pg, oracle, name):
     assert np.max(np.abs(Gf - G)) < 2e-5 * gs + 1e-6
 
 
+def test_unrolled_nine_atom_surface_matches_the_table_driven_one(ctx, pg, oracle):
+    """The FP32 9-atom surface runs fully unrolled (coordinates and gradient in
+    registers) when its table lists all 36 pairs i < j in order; the same terms
+    with the table's rows reversed take the table-driven path.  Both agree with
+    each other to FP32 rounding and with the oracle (FP64)."""
+    c = pgconfigs.load("c2")
+    p = np.array(c["params"], dtype=float)
+    npair = int(p[0])
+    rows = p[1:1 + 5 * npair].reshape(npair, 5)
+    p_rev = np.concatenate([[npair], rows[::-1].ravel(), p[1 + 5 * npair:]])
+    rs = np.random.RandomState(8)
+    w = np.array(c["well1"])
+    X = np.array([w + 0.1 * rs.randn(w.size) for _ in range(64)])
+    out = []
+    for params in (p, p_rev):
+        ctx.set_system(c["ndim"], c["natom"], c["mass"], c["pes_id"], list(params), c["V0"])
+        out.append(ctx.pes_eval(X.ravel(), pg.PG_MIXED))
+    (Vu, Gu), (Vt, Gt) = out
+    pes = _pes(oracle, c)
+    Vo = np.array([pes.V(x) for x in X])
+    Go = np.array([pes.Vprime(x) for x in X])
+    gs = np.max(np.abs(Go))
+    assert np.max(np.abs(Gu - Gt.reshape(Gu.shape))) < 4e-6 * gs
+    assert np.max(np.abs(Gu - Go)) < 2e-5 * gs + 1e-6
+    assert np.max(np.abs(Vu - Vo)) < 2e-6 * max(1.0, np.max(np.abs(Vo)))
+    assert np.max(np.abs(Vu - Vt)) < 2e-6 * max(1.0, np.max(np.abs(Vo)))
+
+
 @pytest.mark.parametrize("name", ["c0", "c1", "c2", "c4"])
 def test_pes_hessian_matches_oracle(ctx, pg, oracle, name):
     c = pgconfigs.load(name)
@@ -468,11 +496,12 @@ def _tensor_vs_simt(ctx, pg, c, ti, nsteps=20):
     return x1, p1, s1, x2, p2, s2
 
 
-@pytest.mark.parametrize("P,nrep", [(256, 3), (384, 2)])
+@pytest.mark.parametrize("P,nrep", [(256, 3), (384, 2), (512, 2)])
 def test_tensor_blocked_many_dofs_tracks_simt(ctx, pg, P, nrep):
-    """Blocked split-BF16 GEMMs (P = 256: 2 x 2 blocks of T; P = 384: 3 x 3, 192 TMEM
-    columns) on the 27-dof surface, 6 or 4 rings = 162 or 108 columns (a partial
-    64-column tile), against the FP32 SIMT form from the same state."""
+    """Blocked split-BF16 GEMMs on the 27-dof surface, 6 or 4 rings = 162 or 108
+    columns (a partial 64-column tile), against the FP32 SIMT form from the same
+    state: P = 256 (2 x 2 blocks of T), P = 384 (3 x 3, 192 TMEM columns),
+    P = 512 (4 x 4, 256 TMEM columns)."""
     c = dict(pgconfigs.load("c2"))
     c["P"] = P
     ti = pgconfigs.TiInputs(c, nrep=nrep, nintegral=2)
