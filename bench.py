@@ -18,6 +18,8 @@ tensor-core normal-mode transform, FP64 estimator accumulation).  One bench
   roofline: compute-bound terms of the dominant kernel (tensor: the two NM
             transforms; SIMT: surface, operand splitting, update, normals;
             HBM: ncu DRAM bytes), the kernel timed inside the replayed advance
+  instanton_c3 / uneven_p_c4: the instanton batch (32 beta, N = 512) and the
+            uneven-P batch (4,096 rings, P in {64..512}) timed through the API
   cpu_baseline: the CPU restatement of the reference step (ten dense NM
             transforms per step, FP64) on all host cores, bounded sample
 
@@ -252,6 +254,43 @@ def split_check(ctx, pg, c, ti, nsteps, mixed, chunk=1000):
             "fp64_form": "fused SIMT FP64 (parity-tested against the CPU oracle to 1e-9 per step)"}
 
 
+def instanton_leg(pg, device):
+    """The c3 instanton batch: 32 beta values, N = 512 beads of the 9-atom surface,
+    one batched L-BFGS to pgtol 1e-8 from the rpi_ser linear path (thread-block
+    clusters per polymer), then the log-determinants at the instantons."""
+    import drivers
+    import pgconfigs
+    c = pgconfigs.load("c3")
+    with pg.Context(device) as ctx:
+        ctx.set_system(c["ndim"], c["natom"], c["mass"], c["pes_id"], c["params"], c["V0"])
+        w1, w2 = np.array(c["well1"]), np.array(c["well2"])
+        N, betas = c["N"], np.array(c["betas"])
+        nb = len(betas)
+        betan = betas / N
+        x0 = np.tile(drivers.linear_guess(w1, w2, N), nb)
+        t0 = time.perf_counter()
+        x, UM, it, st = ctx.instanton_optimize(N, x0, w1, np.tile(w2, nb), betan, m=10, factr=1e2, pgtol=1e-8,
+                                               maxiter=200000)
+        t_opt = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        ctx.instanton_logdet(N, x, betan, singlewell=False, skip_lowest=True)
+        t_det = time.perf_counter() - t0
+    return {"betas": nb, "N": N, "dofs": c["ndim"] * c["natom"], "optimize_s": t_opt, "logdet_s": t_det,
+            "iterations_mean": float(np.mean(it)), "converged": int(np.sum(st == 0)),
+            "note": "one batched L-BFGS, each polymer on a thread-block cluster; host-timed calls"}
+
+
+def uneven_p_leg(pg, nmc=200):
+    """The c4 batch: 4,096 rings of the 18-atom surface with P in {64, 128, 256,
+    512}, one context per P advanced together as one CUDA-graph launch."""
+    import drivers
+    import pgconfigs
+    c = dict(pgconfigs.load("c4"), imin=0)
+    r = drivers.run_ti_mixed(c, precision=pg.PG_MIXED, form=pg.PG_FORM_AUTO, nmc=nmc, chunk=nmc // 2)
+    return {"value": r["bead_steps_per_s"], "unit": UNIT, "rings": r["nrings"], "md_steps": nmc,
+            "device_s": r["device_s"], "note": "pg_ti_advance_group: every P's step kernels in one graph launch"}
+
+
 def cpu_reference_rate(c, ti, target_s=12.0, nthreads=None):
     """Bead-force-steps/s of the CPU restatement of the reference step on all host
     cores (one ring per thread at a time), on a bounded sample of the workload."""
@@ -451,6 +490,12 @@ def main():
             _extras(ctx, pg, cfg, ti, M, K, value, ws, beads, extras)
     except Exception as e:  # report, keep the main measurement
         extras["extras_error"] = repr(e)
+    if not args.no_extras and rank == 0:
+        for key, leg in (("instanton_c3", lambda: instanton_leg(pg, local)), ("uneven_p_c4", lambda: uneven_p_leg(pg))):
+            try:
+                extras[key] = leg()
+            except Exception as e:
+                extras[key + "_error"] = repr(e)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
             "ms_per_step": kernel_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",

@@ -169,4 +169,7 @@ int tc_nm_transform(pg_ctx *ctx, int64_t P, int64_t ncol, const double *in, doub
 int32_t tc_error(pg_ctx *ctx, TiState &st);
 int tc_kernel_times(pg_ctx *ctx, TiState &st, int64_t nsteps, double *ms, int64_t *count, int *nsub);
 int tc_steps_per_launch(const TiState &st);  // MD steps per k_tc_step launch
+// dHdrlimit re-initialisation of the flagged rings of a blocked tensor-form
+// batch after the estimator computed at step offset sofs (pg_ti.cu)
+int ti_launch_reinit(pg_ctx *ctx, TiState &st, int64_t sofs, cudaStream_t s);
 }  // namespace pg

@@ -1194,7 +1194,8 @@ struct TbArgs {
     const double *avec, *bvec, *dbdl;
     const float *Tf;          // P x P FP32 transform (the bead-P row for the Andersen estimator)
     double betan, noutput;
-    uint8_t *kick;            // per-ring Andersen kick flag of the current step
+    double dhdr_limit;        // >= 0: re-initialise rings whose estimator exceeds it (Langevin)
+    uint8_t *kick;            // per-ring flag: Andersen kick of the current step, or (Langevin) re-initialisation
     const int32_t *ringlam;
     const uint64_t *ringseed;
     const uint32_t *ringstream;
@@ -1459,13 +1460,19 @@ __global__ void __launch_bounds__(kForceThreads) k_tb_force(TbArgs a) {
     }
     const int64_t s = *a.step0 + a.sofs;
     if (a.do_est && bead == P - 1 && (s - 1) >= a.imin) {
-        // verletmodule.f90:397-403
+        // verletmodule.f90:397-409: an estimate over dHdrlimit is not added; the
+        // ring is flagged for re-initialisation (k_ti_reinit, before the kick)
         const int lam = a.ringlam[ring];
         double contr = 0.0;
         for (int j = 0; j < nd; j++)
             contr += a.mass[j / a.ndim] * (-(double)sx[j]) * a.dbdl[(size_t)lam * nd + j];
         RingAcc *r = &a.acc[ring];
-        if (r->status == 0) r->dhdr_sum += contr;
+        if (a.dhdr_limit < 0.0 || fabs(contr) < a.dhdr_limit) {
+            if (r->status == 0) r->dhdr_sum += contr;
+        } else if (r->status == 0) {
+            r->nreinit += 1;
+            a.kick[ring] = 1;
+        }
         r->nsamples += 1;
     }
 }
@@ -1779,10 +1786,11 @@ int tc_built() { return 1; }
 
 // 0: unsupported; 1: fused 64-column tiles (P = 128, one-atom 1-D or 2-D
 // surface, Langevin); 2: blocked GEMMs (P <= 512 with P % 4 == 0, any surface,
-// Langevin or Andersen).  dHdrlimit re-initialisation (a Langevin option) is
-// not built into either.
+// Langevin or Andersen).  dHdrlimit re-initialisation (a Langevin option) runs
+// in the blocked form (force kernel flags, k_ti_reinit re-initialises).
 int tc_supported(const TiState &st, const pg_ctx &ctx) {
-    if (st.cfg.dhdr_limit >= 0.0 && st.cfg.thermostat == PG_LANGEVIN) return 0;
+    if (st.cfg.dhdr_limit >= 0.0 && st.cfg.thermostat == PG_LANGEVIN)
+        return (st.P % 4 == 0 && st.P <= kMaxMb * kP && ctx.nd <= kMaxDof) ? 2 : 0;
     if (st.cfg.thermostat == PG_ANDERSEN) return (st.P % 4 == 0 && st.P <= kMaxMb * kP && ctx.nd <= kMaxDof) ? 2 : 0;
     if (st.P == kP && ctx.natom == 1 &&
         ((ctx.pes_id == PG_PES_2DTEST && ctx.nd == 2) || (ctx.pes_id == PG_PES_1D && ctx.nd == 1)))
@@ -2034,6 +2042,7 @@ static void tb_make_args(pg_ctx *ctx, TiState &st, TbArgs &a) {
     a.betan = st.betan;
     a.noutput = (double)st.cfg.noutput;
     a.kick = st.kickflag.as<uint8_t>();
+    a.dhdr_limit = st.cfg.dhdr_limit;
 }
 
 // Blocked form: kernel k (0 positions, 1 forces / estimator, 2 kick) of step
@@ -2092,15 +2101,22 @@ static int tb_launch(pg_ctx *ctx, TiState &st, int64_t nsteps, cudaStream_t s) {
         cudaError_t e = cudaGetLastError();
         return e == cudaSuccess ? PG_OK : cuda_fail(e, "blocked Andersen final launch");
     }
+    // dHdrlimit: after each estimator (step i - 1, in the force kernel of step
+    // i, and of the last step in the final pass) the flagged rings are
+    // re-initialised with their forces before the next kick
+    const bool reinit = st.cfg.dhdr_limit >= 0.0;
     for (int64_t i = 0; i < nsteps; i++)
         for (int k = 0; k < 3; k++) {
             int rc = tb_launch_kernel(ctx, st, k, i, false, s);
             if (rc) return rc;
+            if (k == 1 && reinit && i > 0 && (rc = ti_launch_reinit(ctx, st, i, s))) return rc;
         }
     for (int k = 0; k < 2; k++) {
         int rc = tb_launch_kernel(ctx, st, k, nsteps, true, s);
         if (rc) return rc;
     }
+    if (reinit)
+        if (int rc = ti_launch_reinit(ctx, st, nsteps, s)) return rc;
     TbArgs a;
     tb_make_args(ctx, st, a);
     k_tc_step_add<<<1, 1, 0, s>>>(const_cast<int64_t *>(a.step0), nsteps);

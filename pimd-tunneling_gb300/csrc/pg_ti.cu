@@ -357,6 +357,29 @@ __global__ void __launch_bounds__(128) k_ti_fused(TiArgs a, R *__restrict__ gq, 
     if (threadIdx.x == 0) a.acc[r] = acc;
 }
 
+// dHdrlimit re-initialisation for the blocked tensor form
+// (verletmodule.f90:404-409): a ring whose estimate of step s - 1 went over the
+// limit (flagged by the force kernel of step s) starts again from init_path's
+// state with the streams the SIMT form uses after step s - 1, and gets the
+// forces at its new positions, so that the kick of step s, which follows, runs
+// from the re-initialised state.  One CTA per ring; unflagged rings return.
+template <typename R>
+__global__ void __launch_bounds__(128) k_ti_reinit(TiArgs a, uint8_t *__restrict__ flag, int64_t sofs,
+                                                   R *__restrict__ gq, R *__restrict__ gpi, R *__restrict__ gx,
+                                                   R *__restrict__ gf) {
+    extern __shared__ unsigned char smem_raw[];
+    R *sbuf = reinterpret_cast<R *>(smem_raw);
+    const int64_t r = blockIdx.x;
+    if (r >= a.nrings || !flag[r]) return;  // uniform over the CTA
+    const size_t off = (size_t)r * a.nd * a.P;
+    const uint32_t st = (uint32_t)(*a.step_dev + sofs - 1);
+    ring_init_state<R>(a, r, st, kRngReinitX, kRngReinitP, gx + off, gq + off, gpi + off, sbuf, true, true);
+    __syncthreads();
+    ring_forces<R>(a, gx + off, gf + off);
+    __syncthreads();
+    if (threadIdx.x == 0) flag[r] = 0;
+}
+
 // Initial state: x from x0 or xref + noise, momenta from p0 or NM Maxwell.
 template <typename R>
 __global__ void k_ti_init(TiArgs a, R *__restrict__ gq, R *__restrict__ gpi, R *__restrict__ gx,
@@ -780,6 +803,14 @@ static int launch_steps(pg_ctx *ctx, TiState &st, int64_t nsteps, cudaStream_t s
     return PG_OK;
 }
 
+int ti_launch_reinit(pg_ctx *ctx, TiState &st, int64_t sofs, cudaStream_t s) {
+    TiArgs a = make_args(ctx, st, step_ptr(st));
+    k_ti_reinit<float><<<(unsigned)st.nrings, threads_for(st.P, st.nd), ring_smem_bytes(st.P, true), s>>>(
+        a, st.kickflag.as<uint8_t>(), sofs, st.q.as<float>(), st.pi.as<float>(), st.x.as<float>(), st.f.as<float>());
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? PG_OK : cuda_fail(e, "k_ti_reinit launch");
+}
+
 int ti_release(pg_ctx *ctx) {
     if (ctx && ctx->ti) {
         delete ctx->ti;
@@ -829,8 +860,8 @@ static int resolve_form(pg_ctx *ctx, TiState &st) {
     const int tcv = tc_supported(st, *ctx);
     if (form == PG_FORM_TENSOR && !tcv)
         return fail(PG_ERR_UNSUPPORTED,
-                    "the tensor-core form supports the Langevin thermostat without dHdrlimit and the Andersen "
-                    "thermostat, with P <= 512 and P % 4 == 0");
+                    "the tensor-core form supports the Langevin (with or without dHdrlimit) and Andersen "
+                    "thermostats with P <= 512 and P % 4 == 0");
     // AUTO: the fused tiles whenever they apply; the blocked GEMMs for batches of at
     // least 2^20 bead-dofs (smaller batches leave most of the GPU idle in them).
     bool use = tcv == 1 || (tcv == 2 && (form == PG_FORM_TENSOR || st.nrings * st.nd * st.P >= (1 << 20)));
@@ -962,7 +993,7 @@ static int ti_setup_impl(pg_ctx *ctx, const pg_ti_config *cfg, int64_t nrings, i
     ENS(st.ringstream, (size_t)nrings * sizeof(uint32_t));
     ENS(st.acc, (size_t)nrings * sizeof(RingAcc));
     ENS(st.red, (size_t)(3 * nlambda + 1) * sizeof(double));
-    ENS(st.kickflag, (size_t)nrings);  // Andersen kick flags of the blocked tensor form
+    ENS(st.kickflag, (size_t)nrings);  // per-ring flags of the blocked tensor form (Andersen kick / re-init)
     if (x0) ENS(st.x0, nstate * sizeof(double));
     if (p0) ENS(st.p0, nstate * sizeof(double));
     DevBuf &dx0 = st.x0, &dp0 = st.p0;
@@ -979,6 +1010,7 @@ static int ti_setup_impl(pg_ctx *ctx, const pg_ti_config *cfg, int64_t nrings, i
     }
     std::vector<float> Tf(T.begin(), T.end());
     cudaStream_t s = ctx->stream;
+    PG_CUDA(cudaMemsetAsync(st.kickflag.ptr, 0, (size_t)nrings, s));  // no ring flagged
     PG_CUDA(cudaMemcpyAsync(st.T.ptr, T.data(), T.size() * sizeof(double), cudaMemcpyHostToDevice, s));
     PG_CUDA(cudaMemcpyAsync(st.T.as<double>() + (size_t)P * P, Tf.data(), Tf.size() * sizeof(float), cudaMemcpyHostToDevice, s));
     PG_CUDA(cudaMemcpyAsync(st.coef.ptr, coef.data(), coef.size() * sizeof(ModeCoef), cudaMemcpyHostToDevice, s));
@@ -1469,6 +1501,8 @@ extern "C" int pg_ti_get_form(pg_ctx *ctx, int64_t nsteps, int32_t *form, int64_
     if (launches) {
         if (st.form == PG_FORM_TENSOR && st.tc_blocked && st.cfg.thermostat == PG_ANDERSEN)
             *launches = nsteps > 0 ? 6 * nsteps + 2 : 0;  // six per step; positions, counter
+        else if (st.form == PG_FORM_TENSOR && st.tc_blocked && st.cfg.dhdr_limit >= 0.0)
+            *launches = nsteps > 0 ? 4 * nsteps + 3 : 0;  // pos, force, re-init, kick (the first step: no re-init); pos, estimator, re-init, counter
         else if (st.form == PG_FORM_TENSOR && st.tc_blocked)
             *launches = nsteps > 0 ? 3 * nsteps + 3 : 0;  // pos, force, kick per step; pos, estimator, counter
         else if (st.form == PG_FORM_TENSOR)  // step kernels of up to tc_steps_per_launch() steps; final pass, counter

@@ -212,6 +212,49 @@ def test_dhdr_limit_reinit_matches_oracle(ctx, pg, oracle):
     np.testing.assert_allclose(s, so, rtol=1e-9, atol=1e-9)
 
 
+@pytest.mark.parametrize("P", [32, 128])
+def test_tensor_blocked_dhdr_limit_tracks_simt(ctx, pg, P):
+    """dHdrlimit re-initialisation in the blocked tcgen05 form
+    (verletmodule.f90:404-409): the force kernel of step s flags a ring whose
+    estimate of step s - 1 is over the limit, and k_ti_reinit re-initialises it
+    (the SIMT form's streams for that step) with its forces before the kick.  The
+    estimator weights db/dlambda of the three lambda points are scaled by 0.1, 1
+    and 10 (the dynamics do not use them), so with a limit of 2e4 the last point
+    goes over at every step and the others never do (|contr| ~ 7e3 here).
+    Against the FP32 SIMT form on the same streams: the same re-initialisation
+    and sample counts, positions and sums; and the rings that are never flagged
+    run bitwise as under a limit that is never reached.  P = 128 also goes to
+    the blocked form."""
+    c, ti = _small_2d(P=P, nrep=2, nint=3)
+    ti.dbdl = np.array(ti.dbdl, dtype=float) * np.array([0.1, 1.0, 10.0])[:, None]
+    _set_system(ctx, c)
+    nsteps, lim = 40, 2.0e4
+    runs = {}
+    for name, form, dl in (("tensor", pg.PG_FORM_TENSOR, lim), ("simt", pg.PG_FORM_FUSED, lim),
+                           ("tensor_nolim", pg.PG_FORM_TENSOR, 1.0e30)):
+        cfg = _gpu_cfg(pg, c, ti, pg.PG_MIXED, form, dhdr_limit=dl)
+        ctx.ti_setup(cfg, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
+        assert ctx.ti_form(1)[0] == form
+        ctx.ti_advance(nsteps)
+        x, p = ctx.ti_state()
+        s, n, ri, st = ctx.ti_results()
+        runs[name] = (x.reshape(ti.nrings, -1), p.reshape(ti.nrings, -1), s, n, ri, st)
+    xt, pt, st_, nt, rt, stat = runs["tensor"]
+    xs, ps, ss, ns, rs, _ = runs["simt"]
+    flagged = np.asarray(ti.ring_lambda) == 2
+    assert np.all(stat == 0)
+    assert np.all(rt[flagged] == nsteps - 3) and np.all(rt[~flagged] == 0)
+    np.testing.assert_array_equal(rt, rs)
+    np.testing.assert_array_equal(nt, ns)
+    assert np.all(st_[flagged] == 0.0) and np.all(ss[flagged] == 0.0)
+    np.testing.assert_allclose(xt, xs, rtol=0, atol=2e-3)
+    np.testing.assert_allclose(st_, ss, rtol=2e-4, atol=0)
+    xn, pn, sn, nn, _, _ = runs["tensor_nolim"]
+    np.testing.assert_array_equal(xt[~flagged], xn[~flagged])
+    np.testing.assert_array_equal(pt[~flagged], pn[~flagged])
+    np.testing.assert_array_equal(st_[~flagged], sn[~flagged])
+
+
 @pytest.mark.parametrize("form", ["fused64", "plain", "mixed", "tensor_tile", "tensor_blocked"])
 def test_chunked_advance_and_checkpoint_are_bitwise(ctx, pg, tmp_path, form):
     c, ti = _small_2d(P=128 if form == "tensor_tile" else 32)
@@ -563,11 +606,11 @@ def test_fused_fp64_odd_shapes_match_oracle(ctx, pg, oracle, P, nrep, nint):
 def test_tensor_form_single_ring_and_rejections(ctx, pg):
     """One ring on the fused tiles (a 2-column chunk) tracks the SIMT form; the
     tensor form is refused where it does not apply (P % 4 != 0 with either
-    thermostat; dHdrlimit re-initialisation)."""
+    thermostat, with or without dHdrlimit)."""
     c, ti = _small_2d(P=128, nrep=1, nint=1)
     x1, p1, s1, x2, p2, s2 = _tensor_vs_simt(ctx, pg, c, ti)
     assert np.max(np.abs(x1 - x2)) < 2e-3
-    for P, thermostat, lim in ((30, 1, -1.0), (30, 2, -1.0), (128, 2, 1.0)):
+    for P, thermostat, lim in ((30, 1, -1.0), (30, 2, -1.0), (30, 2, 1.0)):
         c, ti = _small_2d(P=P, nrep=1, nint=1)
         cfg = _gpu_cfg(pg, c, ti, pg.PG_MIXED, pg.PG_FORM_TENSOR, thermostat, dhdr_limit=lim)
         with pytest.raises(pg.PgError):
