@@ -175,13 +175,14 @@ def roofline(ctx, pg, c, ti, beads, M, adv_ms, peaks, peak_kind, fp32_tflops):
             tj = json.load(f)
     except Exception:
         tj = {}
-    if any(n.startswith("k_tc_step") for n, _, _, _ in kt):
-        # the persistent step kernel does the whole MD step: it is the unit
-        dom = [i for i, t in enumerate(kt) if t[0].startswith("k_tc_step")][0]
+    persistent = [i for i, t in enumerate(kt) if t[0].startswith(("k_tc_step", "k_tf_step ("))]
+    if persistent:
+        # a persistent step kernel does the whole MD step: it is the unit
+        dom = persistent[0]
         name, kms_alone, kcount, kbytes = kt[dom]
         minor = sum(m * n for i, (_, m, n, _) in enumerate(kt) if i != dom)
         kms = (adv_ms - minor) / max(kcount, 1)
-        traffic = tj.get("k_tc_step")
+        traffic = tj.get(name.split()[0])
     else:
         # several kernels per MD step (blocked form): the MD step is the unit
         name = " + ".join(n.split()[0] for n, _, _, _ in kt) + " (one MD step)"

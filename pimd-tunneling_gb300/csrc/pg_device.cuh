@@ -291,11 +291,44 @@ template <typename R> __device__ __forceinline__ R my_acos(R v);
 template <> __device__ __forceinline__ double my_acos<double>(double v) { return acos(v); }
 template <> __device__ __forceinline__ float my_acos<float>(float v) { return acosf(v); }
 
+// Pair (I, J) of the 9-atom surface's canonical table (all 36 pairs i < j in
+// order, pair q at q = 8 I - I (I - 1) / 2 + J - I - 1), then its successors.
+// Template recursion makes every coordinate index a compile-time constant
+// whatever the caller's loops (a nest of unrolled loops inside a caller's loop
+// can be left rolled, which puts the coordinate arrays in local memory).
+template <typename R, int I, int J>
+__device__ __forceinline__ void s9_pairs(const R *pp, const R (&xr)[27], R (&gr)[27], R &v, bool grad) {
+    if constexpr (I < 8) {
+        constexpr int q = I * 8 - I * (I - 1) / 2 + (J - I - 1);
+        const R *r = pp + 1 + 5 * q;
+        const R D = (R)r[2], a = (R)r[3], r0 = (R)r[4];
+        const R d0 = xr[3 * I] - xr[3 * J], d1 = xr[3 * I + 1] - xr[3 * J + 1], d2 = xr[3 * I + 2] - xr[3 * J + 2];
+        const R rr = my_sqrt<R>(d0 * d0 + d1 * d1 + d2 * d2);
+        const R e = my_exp<R>(-a * (rr - r0));
+        const R om = (R)1.0 - e;
+        v += D * om * om;
+        if (grad) {
+            const R dvdr = pdiv<R>((R)2.0 * D * a * om * e, rr);
+            gr[3 * I] += dvdr * d0;
+            gr[3 * I + 1] += dvdr * d1;
+            gr[3 * I + 2] += dvdr * d2;
+            gr[3 * J] -= dvdr * d0;
+            gr[3 * J + 1] -= dvdr * d1;
+            gr[3 * J + 2] -= dvdr * d2;
+        }
+        if constexpr (J < 8)
+            s9_pairs<R, I, J + 1>(pp, xr, gr, v, grad);
+        else
+            s9_pairs<R, I + 1, I + 2>(pp, xr, gr, v, grad);
+    }
+}
+
 // The 9-atom surface when its table lists all 36 pairs i < j in order: the
-// pair loops are unrolled, so every atom index is a compile-time constant and
-// the 27 coordinates and gradient components stay in registers (the table's
-// indices need local or shared arrays).  The arithmetic and its order are those
-// of pes_synth9; the quartic's three atoms are picked by comparisons.
+// pairs are expanded at compile time (s9_pairs), so every atom index is a
+// constant and the 27 coordinates and gradient components stay in registers
+// (the table's indices need local or shared arrays).  The arithmetic and its
+// order are those of pes_synth9; the quartic's three atoms are picked by
+// comparisons.
 template <typename R>
 __device__ __forceinline__ R pes_synth9_canon(const PesArgs &pa, const R *x, R *g) {
     const R *pp = pes_params<R>(pa);
@@ -306,28 +339,7 @@ __device__ __forceinline__ R pes_synth9_canon(const PesArgs &pa, const R *x, R *
         gr[k] = 0;
     }
     R v = 0;
-#pragma unroll
-    for (int i = 0; i < 9; i++)
-#pragma unroll
-        for (int j = i + 1; j < 9; j++) {
-            const int q = i * 8 - i * (i - 1) / 2 + (j - i - 1);  // position of (i, j) in the list
-            const R *r = pp + 1 + 5 * q;
-            const R D = (R)r[2], a = (R)r[3], r0 = (R)r[4];
-            const R d0 = xr[3 * i] - xr[3 * j], d1 = xr[3 * i + 1] - xr[3 * j + 1], d2 = xr[3 * i + 2] - xr[3 * j + 2];
-            const R rr = my_sqrt<R>(d0 * d0 + d1 * d1 + d2 * d2);
-            const R e = my_exp<R>(-a * (rr - r0));
-            const R om = (R)1.0 - e;
-            v += D * om * om;
-            if (g) {
-                const R dvdr = pdiv<R>((R)2.0 * D * a * om * e, rr);
-                gr[3 * i] += dvdr * d0;
-                gr[3 * i + 1] += dvdr * d1;
-                gr[3 * i + 2] += dvdr * d2;
-                gr[3 * j] -= dvdr * d0;
-                gr[3 * j + 1] -= dvdr * d1;
-                gr[3 * j + 2] -= dvdr * d2;
-            }
-        }
+    s9_pairs<R, 0, 1>(pp, xr, gr, v, g != nullptr);
     const R *w = pp + 1 + 5 * 36;
     const int iH = (int)w[0], iO1 = (int)w[1], iO2 = (int)w[2];
     const R B = (R)w[3], s0 = (R)w[4];

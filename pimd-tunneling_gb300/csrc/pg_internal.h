@@ -81,6 +81,7 @@ struct TiState {
     int form = 0;            // resolved PG_FORM_*
     int tc_blocked = 0;      // tensor form: 0 = fused 64-column tiles (P = 128), 1 = blocked GEMMs (any P)
     int tc_mb = 1;           // blocked tensor form: 128-row blocks of the zero-padded T
+    int tf_fused = 0;        // blocked batch run by the persistent folded step (P = 256, k_tf_step)
     bool fp32 = false;       // state held in FP32
     DevBuf q, pi, x, f;      // ring state (fused: NM q/pi + Cartesian x; plain: x/p in x/pi)
     DevBuf T;                // P*P FP64 transform (reference values)
@@ -92,6 +93,8 @@ struct TiState {
     DevBuf x0, p0;           // FP64 staging of caller-given start positions / momenta
     DevBuf kickflag;         // per-ring Andersen kick flag (blocked tensor form)
     DevBuf tccol;            // per-column table of the tcgen05 step kernel (spring line, Philox key, weight)
+    DevBuf tfimg;            // folded split-BF16 image of T (P = 256) of the persistent folded step
+    const void *tf_img_ptr = nullptr;  // the buffer tfimg's image was written to
     // host-side caches across batches: T of the last P, the mode coefficients,
     // and what the tensor-core tables on the device were built from
     std::vector<double> hostT;
@@ -163,6 +166,7 @@ int check_ctx(pg_ctx *ctx, bool need_system);
 int ti_release(pg_ctx *ctx);
 int tc_built();
 int tc_supported(const TiState &st, const pg_ctx &ctx);
+int tf_supported(const TiState &st, const pg_ctx &ctx);  // blocked batch for the persistent folded step
 int tc_prepare(pg_ctx *ctx, TiState &st);
 int tc_launch(pg_ctx *ctx, TiState &st, int64_t step0, int64_t nsteps, cudaStream_t s);
 int tc_nm_transform(pg_ctx *ctx, int64_t P, int64_t ncol, const double *in, double *out);

@@ -1746,6 +1746,633 @@ __global__ void k_tc_cols(int64_t ncols, int nd, int ndim, int P, const int32_t 
     cwest[c] = mass[j / ndim] * dbdl[(size_t)lam * nd + j];
 }
 
+// ---------------------------------------------------------------- persistent folded step (P = 256)
+// One launch runs nsub MD steps of a many-dof batch with P = 256, as k_tc_step
+// does for P = 128, with T resident in shared memory.  T alone (256 x 256,
+// split-BF16 hi and lo) would take 256 KB; the DST-I symmetry
+// T[i][P-1-b] = (-1)^i T[i][b] (0-based) folds it: with u_b = y_b + y_(P-1-b)
+// and v_b = y_b - y_(P-1-b), b < 128,
+//     (T y)_(2j) = sum_b T[2j][b] u_b,     (T y)_(2j+1) = sum_b T[2j+1][b] v_b,
+// so T y is two 128 x 128 products, T_e (even rows) u and T_o (odd rows) v,
+// whose images take 128 KB.  One CTA per SM owns an equal range of whole rings,
+// cut into chunks of RPC rings (RPC x ND <= 64 state columns); each chunk steps
+// on its own (no grid-wide synchronisation).  Per chunk and step:
+//   A  positions: the folded operands of q (u, then v, in one 64-column operand
+//      buffer) and two GEMMs, T_e u into TMEM columns 0-63 and T_o v into 64-127;
+//      TMEM lane j of the first holds bead 2j, of the second bead 2j+1;
+//   B  forces: the thread of lane j in warp quarter w % 4 and half h = w / 4
+//      reads its bead's ND dofs (x = T q + x*, the spring line added), evaluates
+//      the FP32 surface in registers and stages the gradient in shared memory;
+//      the thread of bead 256 forms the estimator of step s - 1;
+//   C  T F: the folded operands of the staged forces and two GEMMs;
+//   D  update: the thread of lane j holds modes 2j and 2j + 1 of 8-column groups
+//      (q, pi as float2, coalesced), draws the Langevin normals of both from the
+//      two Philox blocks of its quad (pairs exchanged by a quad transpose), and
+//      applies the folded kick / rotation / OU / rotation map per mode.
+// The step kernel (k_tf_step, 512 threads) runs two warp groups of 256 on
+// alternate chunks of the CTA's range, each with its own 256 TMEM columns
+// (positions 0-127, forces 128-255): B and D are long SIMT phases, and the two
+// groups' run side by side.  B leaves its gradients in the group's force
+// columns.  The operand buffer and the force staging in shared memory (the T
+// image leaves no room for a second copy) belong to one group at a time: a
+// group takes the shared-memory lock to copy its gradients to the staging and
+// run C and the A of its next chunk (the positions go to the position
+// columns), and releases it before D.
+// The read-out pass (k_tf_out, 256 threads) runs A and B only, with the
+// positions written out and the estimator of the last step.
+constexpr int kFP = 256;                                  // beads
+constexpr int kTfThreads = 256;                           // one warp group
+constexpr int kTpThreads = 512;                           // the step kernel's two groups
+constexpr int kTfStride = kFP + 4;                        // staged force row (floats): rows 4 banks apart
+constexpr int kTfCols = 54;                               // staged columns at most
+constexpr size_t kTfImg = 4 * (size_t)kOpBytes;           // T_e hi | T_e lo | T_o hi | T_o lo: 128 KB
+constexpr int kTfPlane = 64 * kP * 2;                     // one bf16 operand plane, 64 x 128, unpadded: 16 KB
+constexpr size_t kTfX = 2 * (size_t)kTfPlane;             // operand hi | lo: 32 KB
+constexpr int kTfParams = 1024;                           // surface tables up to 4 KB (staged in shared memory)
+constexpr size_t kTfS = (size_t)kTfCols * kTfStride * sizeof(float);
+
+struct TfArgs {
+    int64_t nrings;
+    int nd, ndim;
+    int64_t imin;
+    const unsigned char *gT;  // folded image (128 KB)
+    const float *fold;        // natom x P x 8 folded kick / rotation / OU map
+    float *q, *pi, *x;        // [ring][dof][P]
+    RingAcc *acc;
+    const float *cxa, *cxs;
+    const uint64_t *cseed;
+    const uint32_t *cstream;
+    const int32_t *cjdof;
+    const double *cwest;
+    const int64_t *step0;
+    int64_t sofs;
+    int nsub, do_est;
+    int32_t *err;
+    PesArgs pes;
+};
+
+struct TpShared {
+    uint64_t mma_bar[2];  // GEMM completion, per warp group
+    uint64_t tma_bar;     // the image copy
+    int32_t err;
+    int32_t lock;         // operand buffer and force staging: 0 free, 1 held
+    int32_t stop[2];      // a group's exit decision, written by its elected thread
+    uint32_t tmem_slot;
+};
+
+// A group's column values of its current chunk (shared memory), loaded at the
+// start of each chunk step.
+struct TfAux {
+    float xa[kTfCols], xs[kTfCols];
+    double west[kTfCols];
+    uint64_t seed[kTfCols];
+    uint32_t stream[kTfCols];
+    int32_t jdof[kTfCols];
+};
+
+static size_t tf_out_smem_bytes() { return 1024 + kTfImg + kTfX + sizeof(TcShared) + 64; }
+// 128-byte alignment (the image and operands need 16): the step kernel's layout
+// fills the 227 KB a CTA may have.
+static size_t tf_step_smem_bytes() {
+    return 128 + kTfImg + kTfX + kTfS + 2 * sizeof(TfAux) + kTfParams * sizeof(float) + sizeof(TpShared) + 64;
+}
+
+// The group that runs a phase, its barrier and the thread that issues its MMAs:
+// the whole CTA, or one 256-thread warp group on named barrier 1 + wg (the
+// non-aligned form: the elected thread may arrive after the rest of its warp).
+struct CtaSync {
+    __device__ __forceinline__ void bar() const { __syncthreads(); }
+    __device__ __forceinline__ bool elected() const { return threadIdx.x == 0; }
+};
+struct WgSync {
+    int wg;
+    __device__ __forceinline__ void bar() const { asm volatile("barrier.sync %0, 256;" ::"r"(wg + 1) : "memory"); }
+    __device__ __forceinline__ bool elected() const { return (threadIdx.x & 255) == 0; }
+};
+// The error word, which the other group may set at any time.
+__device__ __forceinline__ int32_t ld_err(const int32_t *e) { return *reinterpret_cast<const volatile int32_t *>(e); }
+
+// Shared-memory addresses of the image halves and the operand planes.
+struct TfOps {
+    uint32_t te_hi, te_lo, to_hi, to_lo, xh, xl;
+};
+// One group's GEMM state: ph counts GEMM slots (the same in every thread of the
+// group); nc, in the elected thread, the commits it really issued (after an
+// error it issues no more), which the drain at exit waits for.
+struct TfGemm {
+    uint64_t *mbar, *tbar;
+    int32_t *err;
+    uint32_t ph, nc;
+    bool first;  // the group's first GEMM waits for the image copy
+};
+
+// This thread's share of a folded operand: row c = 8 warp + lane % 8 of the 64,
+// K chunks kl = 8 (4 it + lane / 8), it = 0..3; u written to the operand now,
+// v returned for the second GEMM.  y(k) reads element k of the row (k < 256).
+// The operand has the unpadded core-matrix layout of the T image: a warp's
+// 16-byte stores cover 512 contiguous bytes, so no padding is needed against
+// bank conflicts.
+template <typename Ld>
+__device__ __forceinline__ void tf_fold_operand(unsigned char *Xhi, unsigned char *Xlo, int c, int lane, bool valid,
+                                                Ld ld, float4 (&v)[8]) {
+#pragma unroll
+    for (int it = 0; it < 4; it++) {
+        const int kl = 8 * (4 * it + (lane >> 3));
+        const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 x0 = valid ? ld(kl) : z4, x1 = valid ? ld(kl + 4) : z4;
+        const float4 r0 = valid ? ld(kFP - 4 - kl) : z4;  // .w .z .y .x: partners of kl .. kl + 3
+        const float4 r1 = valid ? ld(kFP - 8 - kl) : z4;  // partners of kl + 4 .. kl + 7
+        const float e8[8] = {x0.x + r0.w, x0.y + r0.z, x0.z + r0.y, x0.w + r0.x,
+                             x1.x + r1.w, x1.y + r1.z, x1.z + r1.y, x1.w + r1.x};
+        v[2 * it] = make_float4(x0.x - r0.w, x0.y - r0.z, x0.z - r0.y, x0.w - r0.x);
+        v[2 * it + 1] = make_float4(x1.x - r1.w, x1.y - r1.z, x1.z - r1.y, x1.w - r1.x);
+        uint4 hi, lo;
+        split8(e8, hi, lo);
+        const uint32_t off = op_offset(c, kl);
+        *reinterpret_cast<uint4 *>(Xhi + off) = hi;
+        *reinterpret_cast<uint4 *>(Xlo + off) = lo;
+    }
+}
+__device__ __forceinline__ void tf_store_v(unsigned char *Xhi, unsigned char *Xlo, int c, int lane,
+                                           const float4 (&v)[8]) {
+#pragma unroll
+    for (int it = 0; it < 4; it++) {
+        const int kl = 8 * (4 * it + (lane >> 3));
+        const float e8[8] = {v[2 * it].x, v[2 * it].y, v[2 * it].z, v[2 * it].w,
+                             v[2 * it + 1].x, v[2 * it + 1].y, v[2 * it + 1].z, v[2 * it + 1].w};
+        uint4 hi, lo;
+        split8(e8, hi, lo);
+        const uint32_t off = op_offset(c, kl);
+        *reinterpret_cast<uint4 *>(Xhi + off) = hi;
+        *reinterpret_cast<uint4 *>(Xlo + off) = lo;
+    }
+}
+
+// Operand complete -> the elected thread issues D = A X (3 split products per K
+// step of 16) into TMEM column dcol -> every thread of the group waits for it.
+template <class Sync>
+__device__ __forceinline__ void tf_gemm(const Sync &sy, TfGemm &g, uint32_t a_hi, uint32_t a_lo, uint32_t xh,
+                                        uint32_t xl, uint32_t dtmem) {
+    fence_async_smem();
+    tc_before();
+    sy.bar();
+    tc_after();
+    if (sy.elected() && ld_err(g.err) == 0) {
+        if (g.first && !mbar_wait(g.tbar, 0)) {
+            atomicOr(g.err, 1);
+        } else {
+#pragma unroll
+            for (int ks = 0; ks < kP / 16; ks++) {
+                const uint64_t dth = make_desc(a_hi + (uint32_t)ks * 2 * kLBO),
+                               dtl = make_desc(a_lo + (uint32_t)ks * 2 * kLBO);
+                const uint64_t dxh = make_desc(xh + (uint32_t)ks * 2 * kLBO),
+                               dxl = make_desc(xl + (uint32_t)ks * 2 * kLBO);
+                mma_bf16_n64(dtmem, dth, dxh, ks > 0 ? 1u : 0u);
+                mma_bf16_n64(dtmem, dth, dxl, 1u);
+                mma_bf16_n64(dtmem, dtl, dxh, 1u);
+            }
+            mma_commit(g.mbar);
+            g.nc++;
+        }
+    }
+    g.first = false;
+    sy.bar();  // issued, or an error recorded before any thread of the group waits
+    if (ld_err(g.err) == 0 && !mbar_wait(g.mbar, g.ph & 1u)) atomicOr(g.err, 2);
+    g.ph++;
+    tc_after();
+}
+
+// The chunk's operand rows and TMEM columns hold ring r's dof d at 32 r + d
+// (kTfRing = 32 per ring, 27 used): ring boundaries fall on 8-column TMEM groups,
+// so one rolled loop over the rings (one copy of the surface code) reads and
+// writes TMEM at aligned columns.  Column c's index among the chunk's state
+// columns (the staging row and the column-value index) is tf_srow(c).
+constexpr int kTfRing = 32;
+template <int ND>
+__device__ __forceinline__ int tf_srow(int c) { return (c / kTfRing) * ND + c % kTfRing; }
+template <int ND>
+__device__ __forceinline__ bool tf_valid(int c, int nvalid) { return c % kTfRing < ND && tf_srow<ND>(c) < nvalid; }
+
+// A: x = T q of the chunk's state columns [col0, col0 + nvalid) into TMEM
+// columns dt (even beads) and dt + 64 (odd beads).
+template <int ND, class Sync>
+__device__ __forceinline__ void tf_positions(const Sync &sy, TfGemm &g, const TfOps &op, const float *q, int64_t col0,
+                                             int nvalid, int c_row, int lane, unsigned char *Xhi, unsigned char *Xlo,
+                                             uint32_t dt) {
+    float4 v[8];
+    const bool valid = tf_valid<ND>(c_row, nvalid);
+    const float *row = q + (size_t)(col0 + (valid ? tf_srow<ND>(c_row) : 0)) * kFP;
+    tf_fold_operand(Xhi, Xlo, c_row, lane, valid, [&](int k) { return *reinterpret_cast<const float4 *>(row + k); },
+                    v);
+    tf_gemm(sy, g, op.te_hi, op.te_lo, op.xh, op.xl, dt);
+    tf_store_v(Xhi, Xlo, c_row, lane, v);
+    tf_gemm(sy, g, op.to_hi, op.to_lo, op.xh, op.xl, dt + 64);
+}
+
+// C: T F of the staged forces (staging row = state column) into TMEM columns dt
+// (even modes) and dt + 64.
+template <int ND, class Sync>
+__device__ __forceinline__ void tf_force_modes(const Sync &sy, TfGemm &g, const TfOps &op, const float *S, int nvalid,
+                                               int c_row, int lane, unsigned char *Xhi, unsigned char *Xlo,
+                                               uint32_t dt) {
+    float4 v[8];
+    const bool valid = tf_valid<ND>(c_row, nvalid);
+    const float *row = S + (size_t)(valid ? tf_srow<ND>(c_row) : 0) * kTfStride;
+    tc_before();
+    sy.bar();  // staged forces complete
+    tc_after();
+    tf_fold_operand(Xhi, Xlo, c_row, lane, valid, [&](int k) { return *reinterpret_cast<const float4 *>(row + k); },
+                    v);
+    tf_gemm(sy, g, op.te_hi, op.te_lo, op.xh, op.xl, dt);
+    tf_store_v(Xhi, Xlo, c_row, lane, v);
+    tf_gemm(sy, g, op.to_hi, op.to_lo, op.xh, op.xl, dt + 64);
+}
+
+// B: the thread's bead b = 2 j + hh of the chunk's rings [rc, rc + RPC): the
+// positions from TMEM (tp: the group's position columns at this warp's lane
+// quarter) plus the spring line, the estimator of step s - 1 (bead 256), then
+// the gradient into TMEM (ts: the group's force columns, free until C; same
+// column layout) or, OUT, the positions into x.  The 9-atom surface runs
+// unrolled: its coordinates and gradient stay in registers.  Warp-uniform (the
+// body issues warp-collective TMEM loads and stores): a wait that gave up in
+// another thread may set the error word at any moment.  xa, xs, west: the
+// chunk's column values (state column 0 of the chunk first).
+template <int ND, int RPC, bool OUT>
+__device__ __forceinline__ void tf_beads(const TfArgs &a, const PesArgs &pes, const float *xa, const float *xs,
+                                         const double *west, const int32_t *err, uint32_t tp, uint32_t ts, int j,
+                                         int hh, int64_t rc, int64_t col0, int nvalid, int64_t s, bool est) {
+    static_assert(ND == 27 && RPC * kTfRing <= 64, "k_tf_step evaluates the 9-atom surface, two rings per chunk");
+    if (!__all_sync(0xffffffffu, ld_err(err) == 0)) return;
+    const int b = 2 * j + hh;
+    const float fm = (float)(b + 1);
+#pragma unroll 1
+    for (int r = 0; r < RPC; r++) {
+        if (r * ND >= nvalid) break;  // uniform: whole rings
+        const uint32_t cb = (uint32_t)(64 * hh + kTfRing * r);
+        float x[ND];
+#pragma unroll
+        for (int k8 = 0; k8 * 8 < ND; k8++) {
+            float t8[8];
+            __syncwarp();
+            tmem_ldn<8>(tp + cb + (uint32_t)(8 * k8), t8);
+#pragma unroll
+            for (int i = 0; i < 8; i++)
+                if (8 * k8 + i < ND) x[8 * k8 + i] = t8[i];
+        }
+        const int64_t cr = col0 + r * ND;
+        const float *xar = xa + r * ND, *xsr = xs + r * ND;
+#pragma unroll
+        for (int d = 0; d < ND; d++) x[d] += xar[d] + xsr[d] * fm;
+        if (est && b == kFP - 1 && (s - 1) >= a.imin) {  // verletmodule.f90:397-403
+            double contr = 0.0;
+#pragma unroll
+            for (int d = 0; d < ND; d++) contr += west[r * ND + d] * (-(double)x[d]);
+            RingAcc *acc = &a.acc[rc + r];
+            if (acc->status == 0) acc->dhdr_sum += contr;
+            acc->nsamples += 1;
+        }
+        if (OUT) {
+#pragma unroll
+            for (int d = 0; d < ND; d++) a.x[(size_t)(cr + d) * kFP + b] = x[d];
+        } else {
+            float g[ND];
+            pes_synth9_canon<float>(pes, x, g);
+#pragma unroll
+            for (int k8 = 0; k8 * 8 < ND; k8++) {
+                float t8[8];
+#pragma unroll
+                for (int i = 0; i < 8; i++) t8[i] = 8 * k8 + i < ND ? g[8 * k8 + i] : 0.f;
+                __syncwarp();
+                tmem_st8(ts + cb + (uint32_t)(8 * k8), t8);
+            }
+        }
+    }
+}
+
+// The staged gradients (TMEM, as tf_beads left them) into the force staging in
+// shared memory, row r ND + d, bead b; warp-uniform, as B.
+template <int ND, int RPC>
+__device__ __forceinline__ void tf_stage_copy(const int32_t *err, uint32_t ts, int j, int hh, int nvalid, float *S) {
+    if (!__all_sync(0xffffffffu, ld_err(err) == 0)) return;
+    const int b = 2 * j + hh;
+#pragma unroll
+    for (int r = 0; r < RPC; r++) {
+        if (r * ND >= nvalid) break;
+#pragma unroll
+        for (int k8 = 0; k8 * 8 < ND; k8++) {
+            float t8[8];
+            __syncwarp();
+            tmem_ldn<8>(ts + (uint32_t)(64 * hh + kTfRing * r + 8 * k8), t8);
+#pragma unroll
+            for (int i = 0; i < 8; i++)
+                if (8 * k8 + i < ND) S[(r * ND + 8 * k8 + i) * kTfStride + b] = t8[i];
+        }
+    }
+}
+
+// D: kick, half rotation, OU, half rotation of modes 2j and 2j + 1 of the
+// chunk's columns, the forces in modes read from TMEM (tf: the group's force
+// columns at this warp's lane quarter), 8-column groups in two halves of 4 (a
+// half lies in one ring).  Each half first issues its loads (q, pi and the
+// folded maps of the at most two atoms its columns belong to: three dofs per
+// atom), then draws the normals while they are in flight.  Warp-uniform, as B.
+template <int ND>
+__device__ __forceinline__ void tf_update(const TfArgs &a, const TfAux &ax, const int32_t *err, uint32_t tf, int j,
+                                          int hh, int lane, int64_t col0, int nvalid, int64_t s) {
+    if (!__all_sync(0xffffffffu, ld_err(err) == 0)) return;
+    const int e = lane & 3;
+    const int mq = 2 * (j - e);  // the quad's modes mq .. mq + 7
+#pragma unroll 1
+    for (int g = 0; g < 4; g++) {
+        const int gc = 16 * g + 8 * hh;
+        if (!tf_valid<ND>(gc, nvalid)) continue;  // warp-uniform; the group's first column decides
+        float gE[8], gO[8];
+        __syncwarp();
+        tmem_ldn<8>(tf + (uint32_t)gc, gE);
+        __syncwarp();
+        tmem_ldn<8>(tf + (uint32_t)(64 + gc), gO);
+#pragma unroll
+        for (int t4 = 0; t4 < 8; t4 += 4) {
+            const int d0 = (gc + t4) % kTfRing;
+            if (d0 >= ND) break;  // warp-uniform: the ring's padding
+            const int sc0 = tf_srow<ND>(gc + t4);  // state column of the half's first column
+            const int nt = min(4, ND - d0);
+            float2 q2[4], p2[4];
+#pragma unroll
+            for (int t = 0; t < 4; t++) {
+                const int col = sc0 + (t < nt ? t : 0);
+                q2[t] = *reinterpret_cast<const float2 *>(a.q + (size_t)(col0 + col) * kFP + 2 * j);
+                p2[t] = *reinterpret_cast<const float2 *>(a.pi + (size_t)(col0 + col) * kFP + 2 * j);
+            }
+            const int atA = ax.jdof[sc0] / 3, atB = ax.jdof[sc0 + nt - 1] / 3;
+            float4 kA[4], kB[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                kA[i] = __ldg(reinterpret_cast<const float4 *>(a.fold + ((size_t)atA * kFP + 2 * j) * 8) + i);
+                kB[i] = __ldg(reinterpret_cast<const float4 *>(a.fold + ((size_t)atB * kFP + 2 * j) * 8) + i);
+            }
+            float zE[4], zO[4];
+            {
+                const bool ok = e < nt;  // this lane draws the blocks of state column sc0 + e
+                const int32_t jd = ok ? ax.jdof[sc0 + e] : 0;
+                const uint64_t sd = ok ? ax.seed[sc0 + e] : 0;
+                const uint32_t sm = ok ? ax.stream[sc0 + e] : 0;
+                const uint32_t blk = (uint32_t)((jd * kFP + mq) >> 2);
+                const U4 oa = philox_block(sd, sm, (uint32_t)s, kRngLangevin, blk);
+                const U4 ob = philox_block(sd, sm, (uint32_t)s, kRngLangevin, blk + 1);
+                box_muller_f(oa.x, oa.y, zE[0], zO[0]);  // modes mq, mq + 1
+                box_muller_f(oa.z, oa.w, zE[1], zO[1]);  // mq + 2, mq + 3
+                box_muller_f(ob.x, ob.y, zE[2], zO[2]);
+                box_muller_f(ob.z, ob.w, zE[3], zO[3]);
+                quad_transpose(zE, e);  // zE[t]: mode 2j of state column sc0 + t
+                quad_transpose(zO, e);  // zO[t]: mode 2j + 1
+            }
+#pragma unroll
+            for (int t = 0; t < 4; t++) {
+                if (t >= nt) break;
+                const int col = sc0 + t;
+                const bool A = ax.jdof[col] / 3 == atA;
+                const float4 k1e = A ? kA[0] : kB[0], k2e = A ? kA[1] : kB[1];
+                const float4 k1o = A ? kA[2] : kB[2], k2o = A ? kA[3] : kB[3];
+                const float ge = gE[t4 + t], go = gO[t4 + t];
+                float2 pn, qn;
+                pn.x = fmaf(k1e.x, p2[t].x, fmaf(-k1e.w, ge, fmaf(k1e.y, q2[t].x, k1e.z * zE[t])));
+                qn.x = fmaf(k2e.x, p2[t].x, fmaf(-k2e.w, ge, fmaf(k2e.y, q2[t].x, k2e.z * zE[t])));
+                pn.y = fmaf(k1o.x, p2[t].y, fmaf(-k1o.w, go, fmaf(k1o.y, q2[t].y, k1o.z * zO[t])));
+                qn.y = fmaf(k2o.x, p2[t].y, fmaf(-k2o.w, go, fmaf(k2o.y, q2[t].y, k2o.z * zO[t])));
+                *reinterpret_cast<float2 *>(a.q + (size_t)(col0 + col) * kFP + 2 * j) = qn;
+                *reinterpret_cast<float2 *>(a.pi + (size_t)(col0 + col) * kFP + 2 * j) = pn;
+                if (pn.x != pn.x || pn.y != pn.y) {
+                    const int64_t ring = (col0 + col) / ND;
+                    if (atomicOr(&a.acc[ring].status, PG_RING_NAN) == 0) a.acc[ring].pad = (int32_t)s;
+                }
+            }
+        }
+    }
+}
+
+// The shared-memory lock: the group's elected thread takes it (bounded spin;
+// on giving up it records an error and the group goes on without it, issuing
+// no further MMAs), then the group's barrier.
+__device__ __forceinline__ bool tf_lock(const WgSync &sy, TpShared *sh) {
+    bool held = false;
+    if (sy.elected()) {
+        const uint64_t t0 = globaltimer_ns();
+        for (long long i = 0; i < kSpinLimit; i++) {
+            if (atomicCAS(&sh->lock, 0, 1) == 0) {
+                held = true;
+                break;
+            }
+            if ((i & 63) == 63 && globaltimer_ns() - t0 > kWaitLimitNs) break;
+            __nanosleep(64);
+        }
+        __threadfence_block();
+        if (!held) atomicOr(&sh->err, 8);
+    }
+    tc_before();
+    sy.bar();
+    tc_after();
+    return held;
+}
+// Every thread of the group is done with the operand and the staging (its GEMMs
+// completed), then the elected thread releases the lock it holds.
+__device__ __forceinline__ void tf_unlock(const WgSync &sy, TpShared *sh, bool held) {
+    tc_before();
+    sy.bar();
+    tc_after();
+    if (sy.elected() && held) {
+        __threadfence_block();
+        atomicExch(&sh->lock, 0);
+    }
+}
+
+template <int ND, int RPC>
+__global__ void __launch_bounds__(kTpThreads, 1) k_tf_step(TfArgs a) {
+    extern __shared__ unsigned char dsm[];
+    unsigned char *base =
+        reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(dsm) + 127) & ~(uintptr_t)127);
+    unsigned char *Xhi = base + kTfImg, *Xlo = Xhi + kTfPlane;
+    float *S = reinterpret_cast<float *>(base + kTfImg + kTfX);
+    TfAux *auxes = reinterpret_cast<TfAux *>(base + kTfImg + kTfX + kTfS);
+    float *par = reinterpret_cast<float *>(base + kTfImg + kTfX + kTfS + 2 * sizeof(TfAux));
+    TpShared *sh = reinterpret_cast<TpShared *>(base + kTfImg + kTfX + kTfS + 2 * sizeof(TfAux) +
+                                                kTfParams * sizeof(float));
+    const int tid = threadIdx.x, wg = tid >> 8, wtid = tid & 255, wwarp = wtid >> 5, lane = tid & 31;
+    TfAux &ax = auxes[tid >> 8];
+    const WgSync sy{wg};
+    const TfOps op{smem_u32(base), smem_u32(base) + kOpBytes, smem_u32(base) + 2 * kOpBytes,
+                   smem_u32(base) + 3 * kOpBytes, smem_u32(Xhi), smem_u32(Xlo)};
+    if (tid == 0) {
+        mbar_init(&sh->mma_bar[0], 1);
+        mbar_init(&sh->mma_bar[1], 1);
+        mbar_init(&sh->tma_bar, 1);
+        sh->err = 0;
+        sh->lock = 0;
+        sh->stop[0] = sh->stop[1] = 0;
+        fence_barrier_init();
+    }
+    // the surface table (uniform reads in every evaluation: L1 is what shared
+    // memory leaves, so it is staged); the host checks that it fits
+    const int np = a.pes.nparams + pes_fparams_extra(a.pes.id);
+    for (int i = tid; i < np; i += kTpThreads) par[i] = a.pes.fparams[i];
+    __syncthreads();
+    if (tid == 0) {  // the folded image, 128 KB, once per launch
+        mbar_expect_tx(&sh->tma_bar, (uint32_t)kTfImg);
+#pragma unroll 1
+        for (int i = 0; i < (int)(kTfImg / 16384); i++) bulk_g2s(base + i * 16384, a.gT + i * 16384, 16384, &sh->tma_bar);
+    }
+    if (tid < 32) {
+        __syncwarp();
+        tmem_alloc(&sh->tmem_slot, 512);
+    }
+    tc_before();
+    __syncthreads();
+    tc_after();
+    const uint32_t tcol = sh->tmem_slot + 256u * (uint32_t)wg;  // positions: +0, forces: +128
+    const uint32_t tq = tcol + ((uint32_t)(32 * (wwarp & 3)) << 16);
+    const int j = 32 * (wwarp & 3) + lane;  // TMEM lane
+    const int hh = wwarp >> 2;              // half: even / odd beads (B), column groups (D)
+    const int c_row = 8 * wwarp + (lane & 7);
+    TfGemm G{&sh->mma_bar[wg], &sh->tma_bar, &sh->err, 0, 0, true};
+    PesArgs pes = a.pes;
+    pes.fparams = par;
+    const int64_t r0 = (int64_t)blockIdx.x * a.nrings / gridDim.x;
+    const int64_t r1 = ((int64_t)blockIdx.x + 1) * a.nrings / gridDim.x;
+    const int64_t s0 = *a.step0 + a.sofs;
+    // this group's chunks: wg, wg + 2, ... of the range's nch; item k is chunk
+    // k % nown at sub-step k / nown
+    const int64_t nch = (r1 - r0 + RPC - 1) / RPC;
+    const int64_t nown = nch > wg ? (nch - wg + 1) / 2 : 0;
+    const int64_t K = nown * a.nsub;
+    auto ring_of = [&](int64_t k) { return r0 + (int64_t)RPC * (wg + 2 * (k % nown)); };
+    auto nvalid_of = [&](int64_t rc) { return (int)(min((int64_t)RPC, r1 - rc) * ND); };
+    if (K > 0) {
+        const bool held = tf_lock(sy, sh);
+        const int64_t rc = ring_of(0);
+        tf_positions<ND>(sy, G, op, a.q, rc * ND, nvalid_of(rc), c_row, lane, Xhi, Xlo, tcol);
+        tf_unlock(sy, sh, held);
+    }
+#pragma unroll 1
+    for (int64_t k = 0; k < K; k++) {
+        const int64_t sub = k / nown, rc = ring_of(k), col0 = rc * ND;
+        const int nvalid = nvalid_of(rc);
+        const int64_t s = s0 + sub;
+        if (wtid < kTfCols) {  // the chunk's column values (the group's D of the last chunk has read them)
+            const bool ok = wtid < nvalid;
+            const int64_t c = col0 + wtid;
+            ax.xa[wtid] = ok ? a.cxa[c] : 0.f;
+            ax.xs[wtid] = ok ? a.cxs[c] : 0.f;
+            ax.west[wtid] = ok ? a.cwest[c] : 0.0;
+            ax.seed[wtid] = ok ? a.cseed[c] : 0;
+            ax.stream[wtid] = ok ? a.cstream[c] : 0;
+            ax.jdof[wtid] = ok ? a.cjdof[c] : 0;
+        }
+        sy.bar();
+        tf_beads<ND, RPC, false>(a, pes, ax.xa, ax.xs, ax.west, &sh->err, tq, tq + 128, j, hh, rc, col0, nvalid, s,
+                                 a.sofs + sub > 0);
+        const bool held = tf_lock(sy, sh);
+        tf_stage_copy<ND, RPC>(&sh->err, tq + 128, j, hh, nvalid, S);
+        tf_force_modes<ND>(sy, G, op, S, nvalid, c_row, lane, Xhi, Xlo, tcol + 128);
+        if (nown >= 2 && k + 1 < K) {  // the next chunk's positions (its q is final: it stepped before this one)
+            const int64_t rn = ring_of(k + 1);
+            tf_positions<ND>(sy, G, op, a.q, rn * ND, nvalid_of(rn), c_row, lane, Xhi, Xlo, tcol);
+        }
+        tf_unlock(sy, sh, held);
+        tf_update<ND>(a, ax, &sh->err, tq + 128, j, hh, lane, col0, nvalid, s);
+        if (nown == 1 && k + 1 < K) {  // one chunk: its next positions need this update
+            const bool h2 = tf_lock(sy, sh);
+            tf_positions<ND>(sy, G, op, a.q, col0, nvalid, c_row, lane, Xhi, Xlo, tcol);
+            tf_unlock(sy, sh, h2);
+        }
+        sy.bar();
+        if (sy.elected()) sh->stop[wg] = ld_err(&sh->err);
+        sy.bar();
+        if (sh->stop[wg]) break;  // group-uniform: written before the barrier, rewritten only after the next
+    }
+    // let whatever is in flight land (immediate when it has), then release TMEM:
+    // the group's last committed GEMM (after a failed wait it may still run) and
+    // the image copy (outstanding if no GEMM waited for it); both waits bounded
+    if (sy.elected() && G.nc > 0) mbar_wait(G.mbar, (G.nc - 1) & 1u);
+    tc_before();
+    __syncthreads();
+    if (tid == 0) {
+        mbar_wait(&sh->tma_bar, 0);
+        if (sh->err) atomicOr(a.err, sh->err);
+    }
+    __syncthreads();
+    if (tid < 32) {
+        __syncwarp();
+        tc_after();
+        tmem_dealloc(sh->tmem_slot, 512);
+    }
+}
+
+// Read-out pass: A and B of every chunk, positions written out, the estimator
+// of the last step when do_est.
+template <int ND, int RPC>
+__global__ void __launch_bounds__(kTfThreads, 1) k_tf_out(TfArgs a) {
+    extern __shared__ unsigned char dsm[];
+    unsigned char *base = align1k(dsm);
+    unsigned char *Xhi = base + kTfImg, *Xlo = Xhi + kTfPlane;
+    TcShared *sh = reinterpret_cast<TcShared *>(base + kTfImg + kTfX);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const CtaSync sy;
+    const TfOps op{smem_u32(base), smem_u32(base) + kOpBytes, smem_u32(base) + 2 * kOpBytes,
+                   smem_u32(base) + 3 * kOpBytes, smem_u32(Xhi), smem_u32(Xlo)};
+    if (tid == 0) {
+        mbar_init(&sh->mma_bar, 1);
+        mbar_init(&sh->tma_bar, 1);
+        sh->err = 0;
+        fence_barrier_init();
+    }
+    __syncthreads();
+    if (tid == 0) {
+        mbar_expect_tx(&sh->tma_bar, (uint32_t)kTfImg);
+#pragma unroll 1
+        for (int i = 0; i < (int)(kTfImg / 16384); i++) bulk_g2s(base + i * 16384, a.gT + i * 16384, 16384, &sh->tma_bar);
+    }
+    if (warp == 0) {
+        __syncwarp();
+        tmem_alloc(&sh->tmem_slot, 128);
+    }
+    tc_before();
+    __syncthreads();
+    tc_after();
+    const uint32_t tmem = sh->tmem_slot;
+    const uint32_t tq = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
+    const int j = 32 * (warp & 3) + lane;
+    const int hh = warp >> 2;
+    const int c_row = 8 * warp + (lane & 7);
+    TfGemm G{&sh->mma_bar, &sh->tma_bar, &sh->err, 0, 0, true};
+    const int64_t r0 = (int64_t)blockIdx.x * a.nrings / gridDim.x;
+    const int64_t r1 = ((int64_t)blockIdx.x + 1) * a.nrings / gridDim.x;
+    const int64_t s = *a.step0 + a.sofs;
+#pragma unroll 1
+    for (int64_t rc = r0; rc < r1; rc += RPC) {
+        const int64_t col0 = rc * ND;
+        const int nvalid = (int)(min((int64_t)RPC, r1 - rc) * ND);
+        tf_positions<ND>(sy, G, op, a.q, col0, nvalid, c_row, lane, Xhi, Xlo, tmem);
+        tf_beads<ND, RPC, true>(a, a.pes, a.cxa + col0, a.cxs + col0, a.cwest + col0, &sh->err, tq, 0, j, hh, rc,
+                                col0, nvalid, s, a.do_est != 0);
+        tc_before();
+        __syncthreads();  // TMEM and operand of this chunk fully read
+        tc_after();
+        if (sh->err) break;  // CTA-uniform: read after the barrier
+    }
+    if (tid == 0) {
+        if (sh->err) atomicOr(a.err, sh->err);
+        if (G.nc > 0) mbar_wait(&sh->mma_bar, (G.nc - 1) & 1u);
+        mbar_wait(&sh->tma_bar, 0);
+    }
+    tc_before();
+    __syncthreads();
+    if (warp == 0) {
+        __syncwarp();
+        tc_after();
+        tmem_dealloc(tmem, 128);
+    }
+}
+
 // Host: split-BF16 image of T, zero-padded to mb x mb blocks of 128 x 128
 // (mb = ceil(P / 128)); block (ib, kb) is a 64 KB [hi | lo] pair in the K-major
 // core-matrix layout of the A operand, at (ib mb + kb) 64 KB.
@@ -1767,6 +2394,26 @@ static void build_split_image(int P, std::vector<unsigned char> &img) {
             memcpy(&img[blk + off], &hi, 2);
             memcpy(&img[blk + kOpBytes + off], &lo, 2);
         }
+}
+
+// The folded image of T for P = 256 (k_tf_step): [T_e hi | T_e lo | T_o hi |
+// T_o lo], T_e[r][c] = T[2r][c] and T_o[r][c] = T[2r+1][c] for r, c < 128, each a
+// 128 x 128 K-major core-matrix image laid out as the P = 128 one.
+static void build_fold_image(std::vector<unsigned char> &img) {
+    std::vector<double> T;
+    build_transmatrix(kFP, T);
+    img.assign(kTfImg, 0);
+    for (int h = 0; h < 2; h++)
+        for (int r = 0; r < kFP / 2; r++)
+            for (int c = 0; c < kFP / 2; c++) {
+                const double v = T[(size_t)(2 * r + h) + (size_t)kFP * c];
+                __nv_bfloat16 hi = __float2bfloat16_rn((float)v);
+                const double rem = v - (double)__bfloat162float(hi);
+                __nv_bfloat16 lo = __float2bfloat16_rn((float)rem);
+                const uint32_t off = op_offset(r, c);
+                memcpy(&img[(size_t)(2 * h) * kOpBytes + off], &hi, 2);
+                memcpy(&img[(size_t)(2 * h + 1) * kOpBytes + off], &lo, 2);
+            }
 }
 
 static size_t tc_smem_bytes() {
@@ -1797,6 +2444,14 @@ int tc_supported(const TiState &st, const pg_ctx &ctx) {
         return 1;
     if (st.P % 4 == 0 && st.P <= kMaxMb * kP && ctx.nd <= kMaxDof) return 2;
     return 0;
+}
+
+// The persistent folded step (k_tf_step) applies to blocked batches with
+// P = 256, the Langevin thermostat without dHdrlimit, and the 9-atom surface
+// whose table lists its 36 pairs in order (evaluated unrolled, in registers).
+int tf_supported(const TiState &st, const pg_ctx &ctx) {
+    return st.P == kFP && st.cfg.thermostat == PG_LANGEVIN && st.cfg.dhdr_limit < 0.0 && ctx.canon9 &&
+           ctx.fparams.size() <= (size_t)kTfParams;
 }
 
 // Tensor-core tables of a batch: the split image of T (rebuilt only when P or
@@ -1891,6 +2546,20 @@ int tc_prepare(pg_ctx *ctx, TiState &st) {
     // the force kernel's shared memory depends on the surface and the dof count
     PG_CUDA(cudaFuncSetAttribute(k_tb_force, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)tb_force_smem(st.nd, (int)ctx->fparams.size())));
+    if (st.tf_fused) {
+        e = st.tfimg.ensure(kTfImg);
+        if (e != cudaSuccess) return cuda_fail(e, "folded transform image");
+        if (st.tf_img_ptr != st.tfimg.ptr) {  // written once per buffer
+            std::vector<unsigned char> img;
+            build_fold_image(img);
+            PG_CUDA(cudaMemcpyAsync(st.tfimg.ptr, img.data(), img.size(), cudaMemcpyHostToDevice, ctx->stream));
+            PG_CUDA(cudaStreamSynchronize(ctx->stream));  // img is a local pageable buffer
+            st.tf_img_ptr = st.tfimg.ptr;
+        }
+        const int sm = (int)tf_step_smem_bytes(), so = (int)tf_out_smem_bytes();
+        PG_CUDA(cudaFuncSetAttribute(k_tf_step<27, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+        PG_CUDA(cudaFuncSetAttribute(k_tf_out<27, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, so));
+    }
     return PG_OK;
 }
 
@@ -2124,13 +2793,81 @@ static int tb_launch(pg_ctx *ctx, TiState &st, int64_t nsteps, cudaStream_t s) {
     return e == cudaSuccess ? PG_OK : cuda_fail(e, "step counter launch");
 }
 
+// Persistent folded step (P = 256): launches of up to tc_steps_per_launch()
+// MD steps, one CTA per SM, then the read-out pass and the step counter.
+static void tf_make_args(pg_ctx *ctx, TiState &st, TfArgs &f) {
+    TcArgs a;
+    int pesk;
+    tc_make_args(ctx, st, a, pesk);
+    memset(&f, 0, sizeof(f));
+    f.nrings = st.nrings;
+    f.nd = st.nd;
+    f.ndim = ctx->ndim;
+    f.imin = st.cfg.imin;
+    f.gT = st.tfimg.as<unsigned char>();
+    f.fold = a.fold;
+    f.q = a.q;
+    f.pi = a.pi;
+    f.x = a.x;
+    f.acc = a.acc;
+    f.cxa = a.cxa;
+    f.cxs = a.cxs;
+    f.cseed = a.cseed;
+    f.cstream = a.cstream;
+    f.cjdof = a.cjdof;
+    f.cwest = a.cwest;
+    f.step0 = a.step0;
+    f.err = a.err;
+    f.pes = ctx->pes_args();
+}
+
+static int tf_launch_one(pg_ctx *ctx, TiState &st, int64_t sofs, int nsub, bool final_pass, cudaStream_t s) {
+    TfArgs f;
+    tf_make_args(ctx, st, f);
+    f.sofs = sofs;
+    f.nsub = nsub;
+    f.do_est = (final_pass && sofs > 0) ? 1 : 0;
+    const unsigned grid = (unsigned)std::min<int64_t>(ctx->sm_count > 0 ? ctx->sm_count : 1, st.nrings);
+    const size_t sm = tf_step_smem_bytes(), so = tf_out_smem_bytes();
+    if (final_pass)
+        k_tf_out<27, 2><<<grid, kTfThreads, so, s>>>(f);
+    else
+        k_tf_step<27, 2><<<grid, kTpThreads, sm, s>>>(f);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? PG_OK : cuda_fail(e, final_pass ? "k_tf_out launch" : "k_tf_step launch");
+}
+
+static int tf_launch(pg_ctx *ctx, TiState &st, int64_t nsteps, cudaStream_t s);
+
 // MD steps per k_tc_step launch (the per-launch set-up, mainly the 64 KB copy
 // of T into every CTA, is paid once per launch).
 constexpr int kStepsPerLaunch = 50;
 int tc_steps_per_launch(const TiState &st) { return st.tc_steps > 0 ? st.tc_steps : kStepsPerLaunch; }
 
+// The read-out pass (positions, estimator of the last step) and the step counter.
+static int tf_launch_final(pg_ctx *ctx, TiState &st, int64_t nsteps, cudaStream_t s) {
+    int rc = tf_launch_one(ctx, st, nsteps, 1, true, s);
+    if (rc) return rc;
+    TcArgs a;
+    int pesk;
+    tc_make_args(ctx, st, a, pesk);
+    k_tc_step_add<<<1, 1, 0, s>>>(const_cast<int64_t *>(a.step0), nsteps);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? PG_OK : cuda_fail(e, "step counter launch");
+}
+
+static int tf_launch(pg_ctx *ctx, TiState &st, int64_t nsteps, cudaStream_t s) {
+    const int per = tc_steps_per_launch(st);
+    for (int64_t i = 0; i < nsteps; i += per) {
+        int rc = tf_launch_one(ctx, st, i, (int)std::min<int64_t>(per, nsteps - i), false, s);
+        if (rc) return rc;
+    }
+    return tf_launch_final(ctx, st, nsteps, s);
+}
+
 int tc_launch(pg_ctx *ctx, TiState &st, int64_t, int64_t nsteps, cudaStream_t s) {
     if (nsteps < 0) return PG_OK;  // the HBM copy of the state is current after every advance
+    if (st.tf_fused) return tf_launch(ctx, st, nsteps, s);
     if (st.tc_blocked) return tb_launch(ctx, st, nsteps, s);
     const int per = tc_steps_per_launch(st);
     for (int64_t i = 0; i < nsteps; i += per) {
@@ -2201,10 +2938,11 @@ static int tb_kernel_times(pg_ctx *ctx, TiState &st, int64_t nsteps, double *ms,
 // k_tc_step per launch (count[0] launches of nsub[0] steps each; a shorter
 // last launch is not timed), ms[1] = k_tc_final.
 int tc_kernel_times(pg_ctx *ctx, TiState &st, int64_t nsteps, double *ms, int64_t *count, int *nsub) {
-    if (st.tc_blocked) {
+    if (st.tc_blocked && !st.tf_fused) {
         *nsub = 1;
         return tb_kernel_times(ctx, st, nsteps, ms, count);
     }
+    const bool tf = st.tf_fused != 0;  // k_tf_step: the same launch structure as k_tc_step
     cudaStream_t s = ctx->stream;
     const int per = (int)std::min<int64_t>(tc_steps_per_launch(st), nsteps);
     const int64_t nl = (nsteps + per - 1) / per;
@@ -2212,11 +2950,12 @@ int tc_kernel_times(pg_ctx *ctx, TiState &st, int64_t nsteps, double *ms, int64_
     for (auto &e : ev) PG_CUDA(cudaEventCreate(&e));
     for (int64_t l = 0; l < nl; l++) {
         PG_CUDA(cudaEventRecord(ev[l], s));
-        int rc = tc_launch_step(ctx, st, l * per, (int)std::min<int64_t>(per, nsteps - l * per), s);
+        const int n = (int)std::min<int64_t>(per, nsteps - l * per);
+        int rc = tf ? tf_launch_one(ctx, st, l * per, n, false, s) : tc_launch_step(ctx, st, l * per, n, s);
         if (rc) return rc;
     }
     PG_CUDA(cudaEventRecord(ev[nl], s));
-    int rc = tc_launch_final(ctx, st, nsteps, s);  // includes the step-counter add
+    int rc = tf ? tf_launch_final(ctx, st, nsteps, s) : tc_launch_final(ctx, st, nsteps, s);  // with the counter add
     if (rc) return rc;
     PG_CUDA(cudaEventRecord(ev[nl + 1], s));
     PG_CUDA(cudaStreamSynchronize(s));
@@ -2230,7 +2969,7 @@ int tc_kernel_times(pg_ctx *ctx, TiState &st, int64_t nsteps, double *ms, int64_
     float a2 = 0.f;
     PG_CUDA(cudaEventElapsedTime(&a2, ev[nl], ev[nl + 1]));
     for (auto &e : ev) cudaEventDestroy(e);
-    ms[0] = t1 / (double)nfull;
+    ms[0] = nfull > 0 ? t1 / (double)nfull : 0.0;
     ms[1] = a2;
     count[0] = nfull;
     count[1] = 1;

@@ -828,7 +828,7 @@ static std::string graph_signature(const pg_ctx *ctx, const TiState &st) {
     add(&st.cfg, sizeof(st.cfg));
     add(&st.nrings, sizeof(st.nrings));
     add(&st.nlambda, sizeof(st.nlambda));
-    int ints[6] = {st.P, st.nd, st.form, st.tc_blocked, st.fp32 ? 1 : 0, ctx->sm_count};
+    int ints[7] = {st.P, st.nd, st.form, st.tc_blocked, st.fp32 ? 1 : 0, ctx->sm_count, st.tf_fused};
     add(ints, sizeof(ints));
     int sys[6] = {ctx->pes_id, ctx->ndim, ctx->natom, ctx->nd, st.simt_threads, st.tc_steps};
     add(sys, sizeof(sys));
@@ -867,6 +867,7 @@ static int resolve_form(pg_ctx *ctx, TiState &st) {
     bool use = tcv == 1 || (tcv == 2 && (form == PG_FORM_TENSOR || st.nrings * st.nd * st.P >= (1 << 20)));
     st.form = use ? PG_FORM_TENSOR : PG_FORM_FUSED;
     st.tc_blocked = (use && tcv == 2) ? 1 : 0;
+    st.tf_fused = (st.tc_blocked && tf_supported(st, *ctx)) ? 1 : 0;
     return PG_OK;
 }
 
@@ -1190,13 +1191,17 @@ static int ti_graph(pg_ctx *ctx, int64_t n, cudaGraphExec_t *out) {
         *out = it->second;
         return PG_OK;
     }
-    cudaGraph_t g;
+    cudaGraph_t g = nullptr;
     cudaGraphExec_t exec = nullptr;
     PG_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     int lrc = launch_steps(ctx, st, n, ctx->stream);
     cudaError_t ee = cudaStreamEndCapture(ctx->stream, &g);
-    if (lrc) return lrc;
-    if (ee != cudaSuccess) return cuda_fail(ee, "cudaStreamEndCapture");
+    if (lrc || ee != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        (void)cudaGetLastError();  // the failed capture's error stays with this call
+        if (lrc) return lrc;
+        return cuda_fail(ee, "cudaStreamEndCapture");
+    }
     ee = cudaGraphInstantiate(&exec, g, 0);
     cudaGraphDestroy(g);
     if (ee != cudaSuccess) return cuda_fail(ee, "cudaGraphInstantiate");
@@ -1243,11 +1248,12 @@ static int group_graph(pg_ctx *const *ctxs, int64_t nctx, int64_t n, cudaGraphEx
         ce = cudaStreamEndCapture(s0, &g);
     }
     for (auto e : ev) cudaEventDestroy(e);
-    if (lrc) {
+    if (lrc || ce != cudaSuccess) {
         if (g) cudaGraphDestroy(g);
-        return lrc;
+        (void)cudaGetLastError();  // the failed capture's error stays with this call
+        if (lrc) return lrc;
+        return cuda_fail(ce, "capture of the group graph");
     }
-    if (ce != cudaSuccess) return cuda_fail(ce, "capture of the group graph");
     cudaGraphExec_t exec = nullptr;
     ce = cudaGraphInstantiate(&exec, g, 0);
     cudaGraphDestroy(g);
@@ -1426,7 +1432,25 @@ extern "C" int pg_ti_kernel_times(pg_ctx *ctx, int64_t nsteps, int32_t *nkinds, 
     if (st.form == PG_FORM_TENSOR) {
         double ms[2];
         int64_t n[2];
-        if (st.tc_blocked && st.cfg.thermostat == PG_ANDERSEN) {
+        if (st.tf_fused) {
+            int nsub = 1;
+            rc = tc_kernel_times(ctx, st, nsteps, ms, n, &nsub);
+            if (rc) return rc;
+            *nkinds = 2;
+            ms_per_launch[0] = ms[0];
+            ms_per_launch[1] = ms[1];
+            count[0] = n[0];
+            count[1] = n[1];
+            bytes_per_launch[0] = 4.0 * arr * nsub;  // k_tf_step: read q, pi; write q, pi; per MD step
+            bytes_per_launch[1] = 2.0 * arr;         // read-out pass: read q, write x
+            if (names) {
+                static thread_local std::string tf_name;
+                tf_name = "k_tf_step (" + std::to_string(nsub) +
+                          " MD steps per launch, P = 256: folded T resident, two warp groups on alternate chunks)";
+                names[0] = tf_name.c_str();
+                names[1] = "k_tf_out (read-out: positions and last estimator; two half GEMMs)";
+            }
+        } else if (st.tc_blocked && st.cfg.thermostat == PG_ANDERSEN) {
             double ms3[3];
             int64_t n3[3];
             int nsub = 1;
@@ -1501,6 +1525,8 @@ extern "C" int pg_ti_get_form(pg_ctx *ctx, int64_t nsteps, int32_t *form, int64_
     if (launches) {
         if (st.form == PG_FORM_TENSOR && st.tc_blocked && st.cfg.thermostat == PG_ANDERSEN)
             *launches = nsteps > 0 ? 6 * nsteps + 2 : 0;  // six per step; positions, counter
+        else if (st.form == PG_FORM_TENSOR && st.tf_fused)  // step launches of up to tc_steps_per_launch(); read-out, counter
+            *launches = nsteps > 0 ? (nsteps + tc_steps_per_launch(st) - 1) / tc_steps_per_launch(st) + 2 : 0;
         else if (st.form == PG_FORM_TENSOR && st.tc_blocked && st.cfg.dhdr_limit >= 0.0)
             *launches = nsteps > 0 ? 4 * nsteps + 3 : 0;  // pos, force, re-init, kick (the first step: no re-init); pos, estimator, re-init, counter
         else if (st.form == PG_FORM_TENSOR && st.tc_blocked)

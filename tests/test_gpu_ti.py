@@ -563,11 +563,65 @@ def test_tensor_blocked_padded_small_p(ctx, pg):
     np.testing.assert_allclose(s2, s1, rtol=2e-4)
 
 
+def _c_at_256(cfgname):
+    c = dict(pgconfigs.load(cfgname))
+    c["P"] = 256
+    if "dt_per_P" in c:
+        c["dt"] = c["dt_per_P"]["256"]
+    return c
+
+
+@pytest.mark.parametrize("cfgname,nrep,nint,kernel", [("c2", 3, 2, "k_tf_step ("), ("c2", 40, 12, "k_tf_step ("),
+                                                      ("c2", 120, 12, "k_tf_step ("), ("c4", 2, 2, "k_tb_")])
+def test_tensor_folded_p256_tracks_simt(ctx, pg, cfgname, nrep, nint, kernel):
+    """The persistent folded step (k_tf_step: P = 256 with T folded into two
+    resident 128 x 128 halves, one CTA per SM over whole rings, two warp groups
+    on alternate two-ring chunks) against the FP32 SIMT form from the same
+    state, on the 9-atom surface: 6 rings (one CTA per ring, the second group
+    idle), 480 rings (one chunk per group) and 1,440 rings (up to 3 chunks per
+    group, the next chunk's positions formed ahead).  The 18-atom (54-dof)
+    surface runs the blocked kernels at P = 256."""
+    c = _c_at_256(cfgname)
+    ti = pgconfigs.TiInputs(c, nrep=nrep, nintegral=nint, P=256)
+    x1, p1, s1, x2, p2, s2 = _tensor_vs_simt(ctx, pg, c, ti)
+    names = [k[0] for k in ctx.ti_kernel_times(5)]
+    assert names[0].startswith(kernel), names
+    assert np.max(np.abs(x1 - x2)) < 2e-3
+    assert np.max(np.abs(p1 - p2)) < 2e-3 * np.max(np.abs(p1))
+    np.testing.assert_allclose(s2, s1, rtol=2e-4)
+
+
+def test_tensor_folded_launch_boundaries_and_checkpoint_are_bitwise(ctx, pg, tmp_path):
+    """k_tf_step keeps the ring state in global memory between steps, so 70
+    steps in one advance (launches of 50 + 20) and 30 + 40 across a checkpoint
+    reload give the same bits."""
+    c = _c_at_256("c2")
+    ti = pgconfigs.TiInputs(c, nrep=5, nintegral=3, P=256)
+    _set_system(ctx, c)
+    cfg = _gpu_cfg(pg, c, ti, pg.PG_MIXED, pg.PG_FORM_TENSOR)
+    ctx.ti_setup(cfg, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
+    ctx.ti_advance(70)
+    x1, p1 = ctx.ti_state()
+    s1 = ctx.ti_results()[0]
+    ctx.ti_setup(cfg, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
+    ctx.ti_advance(30)
+    path = str(tmp_path / "ck.bin")
+    ctx.ti_checkpoint_save(path)
+    ctx.ti_advance(10)
+    ctx.ti_checkpoint_load(path)
+    ctx.ti_advance(40)
+    x2, p2 = ctx.ti_state()
+    s2 = ctx.ti_results()[0]
+    np.testing.assert_array_equal(x1, x2)
+    np.testing.assert_array_equal(p1, p2)
+    np.testing.assert_array_equal(s1, s2)
+
+
 @pytest.mark.parametrize("cfgname,P", [("c1", 128), ("c2", 256)])
 def test_tensor_forms_with_cayley_rotation(ctx, pg, cfgname, P):
     """cayley = 1 (verletmodule.f90:520-526): the per-mode rotation coefficients
-    the tensor forms apply are the Cayley ones; fused tile (P = 128) and blocked
-    (P = 256, 27 dofs) forms track the FP32 SIMT form."""
+    the tensor forms apply are the Cayley ones; fused tile (P = 128) and
+    persistent folded (P = 256, 27 dofs) forms track the FP32 SIMT form."""
     c = dict(pgconfigs.load(cfgname))
     c["P"] = P
     ti = pgconfigs.TiInputs(c, nrep=3, nintegral=2)
