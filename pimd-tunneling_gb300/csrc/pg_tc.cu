@@ -1969,25 +1969,6 @@ __device__ __forceinline__ void tf_positions(const Sync &sy, TfGemm &g, const Tf
     tf_gemm(sy, g, op.to_hi, op.to_lo, op.xh, op.xl, dt + 64);
 }
 
-// C: T F of the staged forces (staging row = state column) into TMEM columns dt
-// (even modes) and dt + 64.
-template <int ND, class Sync>
-__device__ __forceinline__ void tf_force_modes(const Sync &sy, TfGemm &g, const TfOps &op, const float *S, int nvalid,
-                                               int c_row, int lane, unsigned char *Xhi, unsigned char *Xlo,
-                                               uint32_t dt) {
-    float4 v[8];
-    const bool valid = tf_valid<ND>(c_row, nvalid);
-    const float *row = S + (size_t)(valid ? tf_srow<ND>(c_row) : 0) * kTfStride;
-    tc_before();
-    sy.bar();  // staged forces complete
-    tc_after();
-    tf_fold_operand(Xhi, Xlo, c_row, lane, valid, [&](int k) { return *reinterpret_cast<const float4 *>(row + k); },
-                    v);
-    tf_gemm(sy, g, op.te_hi, op.te_lo, op.xh, op.xl, dt);
-    tf_store_v(Xhi, Xlo, c_row, lane, v);
-    tf_gemm(sy, g, op.to_hi, op.to_lo, op.xh, op.xl, dt + 64);
-}
-
 // B: the thread's bead b = 2 j + hh of the chunk's rings [rc, rc + RPC): the
 // positions from TMEM (tp: the group's position columns at this warp's lane
 // quarter) plus the spring line, the estimator of step s - 1 (bead 256), then
@@ -2073,7 +2054,7 @@ __device__ __forceinline__ void tf_stage_copy(const int32_t *err, uint32_t ts, i
 // D: kick, half rotation, OU, half rotation of modes 2j and 2j + 1 of the
 // chunk's columns, the forces in modes read from TMEM (tf: the group's force
 // columns at this warp's lane quarter), 8-column groups in two halves of 4 (a
-// half lies in one ring).  Each half first issues its loads (q, pi and the
+// half lies in one ring).  Written for two 27-dof rings per chunk.  Each half first issues its loads (q, pi and the
 // folded maps of the at most two atoms its columns belong to: three dofs per
 // atom), then draws the normals while they are in flight.  Warp-uniform, as B.
 template <int ND>
@@ -2084,7 +2065,9 @@ __device__ __forceinline__ void tf_update(const TfArgs &a, const TfAux &ax, cons
     const int mq = 2 * (j - e);  // the quad's modes mq .. mq + 7
 #pragma unroll 1
     for (int g = 0; g < 4; g++) {
-        const int gc = 16 * g + 8 * hh;
+        // the 8 column groups of two rings (3 full and one with 3 dofs each) split
+        // 27 + 27: half 0 takes groups 0, 1, 2, 7, half 1 groups 3, 4, 5, 6
+        const int gc = 8 * (hh == 0 ? (g < 3 ? g : 7) : 3 + g);
         if (!tf_valid<ND>(gc, nvalid)) continue;  // warp-uniform; the group's first column decides
         float gE[8], gO[8];
         __syncwarp();
@@ -2149,6 +2132,134 @@ __device__ __forceinline__ void tf_update(const TfArgs &a, const TfAux &ax, cons
             }
         }
     }
+}
+
+// Step kernel, operands in pairs: u in X, v in the staging region (free once
+// the fold of the staged forces has read it), so that the two GEMMs of a
+// transform are issued back to back under one commit.
+struct TfPair {
+    unsigned char *uhi, *ulo, *vhi, *vlo;
+    uint32_t su_hi, su_lo, sv_hi, sv_lo;  // shared-space addresses of the same
+};
+// This thread's 16 loads of a folded operand row (x0, x1, r0, r1 per K quarter,
+// as tf_fold_operand reads them), issued together.
+template <typename Ld>
+__device__ __forceinline__ void tf_fold_load(float4 (&L)[16], int lane, bool valid, Ld ld) {
+#pragma unroll
+    for (int it = 0; it < 4; it++) {
+        const int kl = 8 * (4 * it + (lane >> 3));
+        const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        L[4 * it] = valid ? ld(kl) : z4;
+        L[4 * it + 1] = valid ? ld(kl + 4) : z4;
+        L[4 * it + 2] = valid ? ld(kFP - 4 - kl) : z4;
+        L[4 * it + 3] = valid ? ld(kFP - 8 - kl) : z4;
+    }
+}
+// u and v of the loaded row into both operands of the pair.
+__device__ __forceinline__ void tf_fold_store(const float4 (&L)[16], const TfPair &x, int c, int lane) {
+#pragma unroll
+    for (int it = 0; it < 4; it++) {
+        const int kl = 8 * (4 * it + (lane >> 3));
+        const float4 x0 = L[4 * it], x1 = L[4 * it + 1], r0 = L[4 * it + 2], r1 = L[4 * it + 3];
+        const float e8[8] = {x0.x + r0.w, x0.y + r0.z, x0.z + r0.y, x0.w + r0.x,
+                             x1.x + r1.w, x1.y + r1.z, x1.z + r1.y, x1.w + r1.x};
+        const float o8[8] = {x0.x - r0.w, x0.y - r0.z, x0.z - r0.y, x0.w - r0.x,
+                             x1.x - r1.w, x1.y - r1.z, x1.z - r1.y, x1.w - r1.x};
+        const uint32_t off = op_offset(c, kl);
+        uint4 hi, lo;
+        split8(e8, hi, lo);
+        *reinterpret_cast<uint4 *>(x.uhi + off) = hi;
+        *reinterpret_cast<uint4 *>(x.ulo + off) = lo;
+        split8(o8, hi, lo);
+        *reinterpret_cast<uint4 *>(x.vhi + off) = hi;
+        *reinterpret_cast<uint4 *>(x.vlo + off) = lo;
+    }
+}
+// Both operands complete -> the elected thread issues T_e u into TMEM column dt
+// and T_o v into dt + 64 under one commit.  The group waits with tf_gemm_wait.
+__device__ __forceinline__ void tf_gemm_pair_issue(const WgSync &sy, TfGemm &g, const TfOps &op, const TfPair &x,
+                                                   uint32_t dt) {
+    fence_async_smem();
+    tc_before();
+    sy.bar();
+    tc_after();
+    if (sy.elected() && ld_err(g.err) == 0) {
+        if (g.first && !mbar_wait(g.tbar, 0)) {
+            atomicOr(g.err, 1);
+        } else {
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const uint32_t a_hi = h ? op.to_hi : op.te_hi, a_lo = h ? op.to_lo : op.te_lo;
+                const uint32_t xh = h ? x.sv_hi : x.su_hi, xl = h ? x.sv_lo : x.su_lo;
+#pragma unroll
+                for (int ks = 0; ks < kP / 16; ks++) {
+                    const uint64_t dth = make_desc(a_hi + (uint32_t)ks * 2 * kLBO),
+                                   dtl = make_desc(a_lo + (uint32_t)ks * 2 * kLBO);
+                    const uint64_t dxh = make_desc(xh + (uint32_t)ks * 2 * kLBO),
+                                   dxl = make_desc(xl + (uint32_t)ks * 2 * kLBO);
+                    mma_bf16_n64(dt + 64 * h, dth, dxh, ks > 0 ? 1u : 0u);
+                    mma_bf16_n64(dt + 64 * h, dth, dxl, 1u);
+                    mma_bf16_n64(dt + 64 * h, dtl, dxh, 1u);
+                }
+            }
+            mma_commit(g.mbar);
+            g.nc++;
+        }
+    }
+    g.first = false;
+    sy.bar();  // issued, or an error recorded before any thread of the group waits
+}
+__device__ __forceinline__ void tf_gemm_wait(TfGemm &g) {
+    if (ld_err(g.err) == 0 && !mbar_wait(g.mbar, g.ph & 1u)) atomicOr(g.err, 2);
+    g.ph++;
+    tc_after();
+}
+// A of the step kernel (the group holds the lock): q of the chunk's state
+// columns [col0, col0 + nvalid) into TMEM columns dt (even beads), dt + 64.
+template <int ND>
+__device__ __forceinline__ void tf_positions_pair(const WgSync &sy, TfGemm &g, const TfOps &op, const TfPair &x,
+                                                  const float *q, int64_t col0, int nvalid, int c_row, int lane,
+                                                  uint32_t dt) {
+    float4 L[16];
+    const bool valid = tf_valid<ND>(c_row, nvalid);
+    const float *row = q + (size_t)(col0 + (valid ? tf_srow<ND>(c_row) : 0)) * kFP;
+    tf_fold_load(L, lane, valid, [&](int k) { return *reinterpret_cast<const float4 *>(row + k); });
+    tf_fold_store(L, x, c_row, lane);
+    tf_gemm_pair_issue(sy, g, op, x, dt);
+    tf_gemm_wait(g);
+}
+// C of the step kernel (the group holds the lock), then, when next, the A of
+// the group's next chunk: T F of the staged forces into TMEM columns df, df +
+// 64; the next chunk's q rows are loaded while those GEMMs run, then its
+// positions go to dp, dp + 64.  next is uniform over the group.
+template <int ND>
+__device__ __forceinline__ void tf_modes_then_positions(const WgSync &sy, TfGemm &g, const TfOps &op, const TfPair &x,
+                                                        const float *S, int nvalid, uint32_t df, bool next,
+                                                        const float *q, int64_t ncol0, int nnvalid, int c_row,
+                                                        int lane, uint32_t dp) {
+    {
+        float4 v[8];
+        const bool valid = tf_valid<ND>(c_row, nvalid);
+        const float *row = S + (size_t)(valid ? tf_srow<ND>(c_row) : 0) * kTfStride;
+        tc_before();
+        sy.bar();  // staged forces complete
+        tc_after();
+        tf_fold_operand(x.uhi, x.ulo, c_row, lane, valid,
+                        [&](int k) { return *reinterpret_cast<const float4 *>(row + k); }, v);
+        sy.bar();  // every thread has read the staging, which now takes v
+        tf_store_v(x.vhi, x.vlo, c_row, lane, v);
+    }
+    tf_gemm_pair_issue(sy, g, op, x, df);
+    if (next) {
+        float4 L[16];
+        const bool valid = tf_valid<ND>(c_row, nnvalid);
+        const float *row = q + (size_t)(ncol0 + (valid ? tf_srow<ND>(c_row) : 0)) * kFP;
+        tf_fold_load(L, lane, valid, [&](int k) { return *reinterpret_cast<const float4 *>(row + k); });
+        tf_gemm_wait(g);  // the operands are read: they take the next chunk's q
+        tf_fold_store(L, x, c_row, lane);
+        tf_gemm_pair_issue(sy, g, op, x, dp);
+    }
+    tf_gemm_wait(g);
 }
 
 // The shared-memory lock: the group's elected thread takes it (bounded spin;
@@ -2246,10 +2357,12 @@ __global__ void __launch_bounds__(kTpThreads, 1) k_tf_step(TfArgs a) {
     const int64_t K = nown * a.nsub;
     auto ring_of = [&](int64_t k) { return r0 + (int64_t)RPC * (wg + 2 * (k % nown)); };
     auto nvalid_of = [&](int64_t rc) { return (int)(min((int64_t)RPC, r1 - rc) * ND); };
+    const TfPair xp{Xhi, Xlo, reinterpret_cast<unsigned char *>(S), reinterpret_cast<unsigned char *>(S) + kTfPlane,
+                    op.xh, op.xl, smem_u32(S), smem_u32(S) + kTfPlane};
     if (K > 0) {
         const bool held = tf_lock(sy, sh);
         const int64_t rc = ring_of(0);
-        tf_positions<ND>(sy, G, op, a.q, rc * ND, nvalid_of(rc), c_row, lane, Xhi, Xlo, tcol);
+        tf_positions_pair<ND>(sy, G, op, xp, a.q, rc * ND, nvalid_of(rc), c_row, lane, tcol);
         tf_unlock(sy, sh, held);
     }
 #pragma unroll 1
@@ -2267,21 +2380,31 @@ __global__ void __launch_bounds__(kTpThreads, 1) k_tf_step(TfArgs a) {
             ax.stream[wtid] = ok ? a.cstream[c] : 0;
             ax.jdof[wtid] = ok ? a.cjdof[c] : 0;
         }
+        if (sy.elected()) {  // into L2 while the forces run: this chunk's state for D, the next chunk's q for A
+            prefetch_l2(a.pi + (size_t)col0 * kFP, (uint32_t)(nvalid * kFP * sizeof(float)));
+            prefetch_l2(a.q + (size_t)col0 * kFP, (uint32_t)(nvalid * kFP * sizeof(float)));
+            if (k + 1 < K) {
+                const int64_t rn = ring_of(k + 1);
+                prefetch_l2(a.q + (size_t)rn * ND * kFP, (uint32_t)(nvalid_of(rn) * kFP * sizeof(float)));
+            }
+        }
         sy.bar();
         tf_beads<ND, RPC, false>(a, pes, ax.xa, ax.xs, ax.west, &sh->err, tq, tq + 128, j, hh, rc, col0, nvalid, s,
                                  a.sofs + sub > 0);
         const bool held = tf_lock(sy, sh);
         tf_stage_copy<ND, RPC>(&sh->err, tq + 128, j, hh, nvalid, S);
-        tf_force_modes<ND>(sy, G, op, S, nvalid, c_row, lane, Xhi, Xlo, tcol + 128);
-        if (nown >= 2 && k + 1 < K) {  // the next chunk's positions (its q is final: it stepped before this one)
-            const int64_t rn = ring_of(k + 1);
-            tf_positions<ND>(sy, G, op, a.q, rn * ND, nvalid_of(rn), c_row, lane, Xhi, Xlo, tcol);
+        {
+            // the next chunk's positions (its q is final: it stepped before this one)
+            const bool next = nown >= 2 && k + 1 < K;
+            const int64_t rn = next ? ring_of(k + 1) : rc;
+            tf_modes_then_positions<ND>(sy, G, op, xp, S, nvalid, tcol + 128, next, a.q, rn * ND, nvalid_of(rn),
+                                        c_row, lane, tcol);
         }
         tf_unlock(sy, sh, held);
         tf_update<ND>(a, ax, &sh->err, tq + 128, j, hh, lane, col0, nvalid, s);
         if (nown == 1 && k + 1 < K) {  // one chunk: its next positions need this update
             const bool h2 = tf_lock(sy, sh);
-            tf_positions<ND>(sy, G, op, a.q, col0, nvalid, c_row, lane, Xhi, Xlo, tcol);
+            tf_positions_pair<ND>(sy, G, op, xp, a.q, col0, nvalid, c_row, lane, tcol);
             tf_unlock(sy, sh, h2);
         }
         sy.bar();
