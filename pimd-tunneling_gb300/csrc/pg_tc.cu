@@ -223,6 +223,37 @@ __device__ __forceinline__ void tmem_st8(uint32_t taddr, const float (&v)[8]) {
         "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])), "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7]))
         : "memory");
 }
+// 32 FP32 values into consecutive TMEM columns of this thread's lane; store and
+// wait in one asm statement, as tmem_st8.
+__device__ __forceinline__ void tmem_st32(uint32_t taddr, const float (&f)[32]) {
+    uint32_t v[32];
+#pragma unroll
+    for (int i = 0; i < 32; i++) v[i] = __float_as_uint(f[i]);
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,"
+        "%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};\n"
+        "tcgen05.wait::st.sync.aligned;" ::"r"(taddr),
+        PG_W32(v)
+        : "memory");
+}
+// Two groups of 8 consecutive FP32 columns (at ta and tb) of this thread's lane:
+// both loads, then one wait, in one asm statement.
+__device__ __forceinline__ void tmem_ld8x2(uint32_t ta, uint32_t tb, float (&a)[8], float (&b)[8]) {
+    uint32_t v[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%16];\n"
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%8,%9,%10,%11,%12,%13,%14,%15}, [%17];\n"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+        : "r"(ta), "r"(tb)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        a[i] = __uint_as_float(v[i]);
+        b[i] = __uint_as_float(v[8 + i]);
+    }
+}
 // Write 32 FP32 values of row `row`, K = k0..k0+31, into the hi / lo operand images.
 __device__ __forceinline__ void write_split32(unsigned char *Ahi, unsigned char *Alo, int row, int k0,
                                               const float (&v)[32]) {
@@ -1812,11 +1843,13 @@ struct TfArgs {
 };
 
 struct TpShared {
-    uint64_t mma_bar[2];  // GEMM completion, per warp group
+    uint64_t desc[8];     // operand descriptors: T_e hi, lo, T_o hi, lo, u hi, lo, v hi, lo
+    uint64_t mma_bar[2];  // GEMM completion, per warp group (two issuing threads arrive)
     uint64_t tma_bar;     // the image copy
     int32_t err;
     int32_t lock;         // operand buffer and force staging: 0 free, 1 held
     int32_t stop[2];      // a group's exit decision, written by its elected thread
+    int32_t go[2];        // a group's issue decision for its current GEMM pair
     uint32_t tmem_slot;
 };
 
@@ -1991,14 +2024,12 @@ __device__ __forceinline__ void tf_beads(const TfArgs &a, const PesArgs &pes, co
         if (r * ND >= nvalid) break;  // uniform: whole rings
         const uint32_t cb = (uint32_t)(64 * hh + kTfRing * r);
         float x[ND];
-#pragma unroll
-        for (int k8 = 0; k8 * 8 < ND; k8++) {
-            float t8[8];
+        {
+            float t32[kTfRing];
             __syncwarp();
-            tmem_ldn<8>(tp + cb + (uint32_t)(8 * k8), t8);
+            tmem_ld32(tp + cb, t32);
 #pragma unroll
-            for (int i = 0; i < 8; i++)
-                if (8 * k8 + i < ND) x[8 * k8 + i] = t8[i];
+            for (int d = 0; d < ND; d++) x[d] = t32[d];
         }
         const int64_t cr = col0 + r * ND;
         const float *xar = xa + r * ND, *xsr = xs + r * ND;
@@ -2018,14 +2049,11 @@ __device__ __forceinline__ void tf_beads(const TfArgs &a, const PesArgs &pes, co
         } else {
             float g[ND];
             pes_synth9_canon<float>(pes, x, g);
+            float t32[kTfRing];
 #pragma unroll
-            for (int k8 = 0; k8 * 8 < ND; k8++) {
-                float t8[8];
-#pragma unroll
-                for (int i = 0; i < 8; i++) t8[i] = 8 * k8 + i < ND ? g[8 * k8 + i] : 0.f;
-                __syncwarp();
-                tmem_st8(ts + cb + (uint32_t)(8 * k8), t8);
-            }
+            for (int d = 0; d < kTfRing; d++) t32[d] = d < ND ? g[d] : 0.f;
+            __syncwarp();
+            tmem_st32(ts + cb, t32);
         }
     }
 }
@@ -2039,15 +2067,11 @@ __device__ __forceinline__ void tf_stage_copy(const int32_t *err, uint32_t ts, i
 #pragma unroll
     for (int r = 0; r < RPC; r++) {
         if (r * ND >= nvalid) break;
+        float t32[kTfRing];
+        __syncwarp();
+        tmem_ld32(ts + (uint32_t)(64 * hh + kTfRing * r), t32);
 #pragma unroll
-        for (int k8 = 0; k8 * 8 < ND; k8++) {
-            float t8[8];
-            __syncwarp();
-            tmem_ldn<8>(ts + (uint32_t)(64 * hh + kTfRing * r + 8 * k8), t8);
-#pragma unroll
-            for (int i = 0; i < 8; i++)
-                if (8 * k8 + i < ND) S[(r * ND + 8 * k8 + i) * kTfStride + b] = t8[i];
-        }
+        for (int d = 0; d < ND; d++) S[(r * ND + d) * kTfStride + b] = t32[d];
     }
 }
 
@@ -2071,9 +2095,7 @@ __device__ __forceinline__ void tf_update(const TfArgs &a, const TfAux &ax, cons
         if (!tf_valid<ND>(gc, nvalid)) continue;  // warp-uniform; the group's first column decides
         float gE[8], gO[8];
         __syncwarp();
-        tmem_ldn<8>(tf + (uint32_t)gc, gE);
-        __syncwarp();
-        tmem_ldn<8>(tf + (uint32_t)(64 + gc), gO);
+        tmem_ld8x2(tf + (uint32_t)gc, tf + (uint32_t)(64 + gc), gE, gO);
 #pragma unroll
         for (int t4 = 0; t4 < 8; t4 += 4) {
             const int d0 = (gc + t4) % kTfRing;
@@ -2175,39 +2197,43 @@ __device__ __forceinline__ void tf_fold_store(const float4 (&L)[16], const TfPai
         *reinterpret_cast<uint4 *>(x.vlo + off) = lo;
     }
 }
-// Both operands complete -> the elected thread issues T_e u into TMEM column dt
-// and T_o v into dt + 64 under one commit.  The group waits with tf_gemm_wait.
-__device__ __forceinline__ void tf_gemm_pair_issue(const WgSync &sy, TfGemm &g, const TfOps &op, const TfPair &x,
-                                                   uint32_t dt) {
+// Both operands complete -> T_e u into TMEM column dt, issued by the group's
+// thread 0, and T_o v into dt + 64, issued by its thread 32, each under its own
+// commit (the group's barrier counts two arrivals).  The descriptors of K step
+// ks are the base ones (TpShared::desc) plus 16 ks: 256 bytes of start address.
+// The elected thread decides for both whether the pair is issued.  The group
+// waits with tf_gemm_wait.
+__device__ __forceinline__ void tf_gemm_pair_issue(const WgSync &sy, TfGemm &g, TpShared *sh, uint32_t dt) {
     fence_async_smem();
     tc_before();
+    const int wg = sy.wg, wt = threadIdx.x & 255;
+    if (wt == 0) {
+        int go = ld_err(g.err) == 0;
+        if (go && g.first && !mbar_wait(g.tbar, 0)) {
+            atomicOr(g.err, 1);
+            go = 0;
+        }
+        sh->go[wg] = go;
+    }
     sy.bar();
     tc_after();
-    if (sy.elected() && ld_err(g.err) == 0) {
-        if (g.first && !mbar_wait(g.tbar, 0)) {
-            atomicOr(g.err, 1);
-        } else {
+    if ((wt == 0 || wt == 32) && sh->go[wg]) {
+        const int h = wt >> 5;  // 0: T_e u, 1: T_o v
+        const uint64_t ah = sh->desc[2 * h], al = sh->desc[2 * h + 1];
+        const uint64_t xh = sh->desc[4 + 2 * h], xl = sh->desc[5 + 2 * h];
+        const uint32_t d = dt + 64u * (uint32_t)h;
 #pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const uint32_t a_hi = h ? op.to_hi : op.te_hi, a_lo = h ? op.to_lo : op.te_lo;
-                const uint32_t xh = h ? x.sv_hi : x.su_hi, xl = h ? x.sv_lo : x.su_lo;
-#pragma unroll
-                for (int ks = 0; ks < kP / 16; ks++) {
-                    const uint64_t dth = make_desc(a_hi + (uint32_t)ks * 2 * kLBO),
-                                   dtl = make_desc(a_lo + (uint32_t)ks * 2 * kLBO);
-                    const uint64_t dxh = make_desc(xh + (uint32_t)ks * 2 * kLBO),
-                                   dxl = make_desc(xl + (uint32_t)ks * 2 * kLBO);
-                    mma_bf16_n64(dt + 64 * h, dth, dxh, ks > 0 ? 1u : 0u);
-                    mma_bf16_n64(dt + 64 * h, dth, dxl, 1u);
-                    mma_bf16_n64(dt + 64 * h, dtl, dxh, 1u);
-                }
-            }
-            mma_commit(g.mbar);
-            g.nc++;
+        for (int ks = 0; ks < kP / 16; ks++) {
+            const uint64_t o = 16ull * (uint64_t)ks;
+            mma_bf16_n64(d, ah + o, xh + o, ks > 0 ? 1u : 0u);
+            mma_bf16_n64(d, ah + o, xl + o, 1u);
+            mma_bf16_n64(d, al + o, xh + o, 1u);
         }
+        mma_commit(g.mbar);
+        g.nc++;
     }
     g.first = false;
-    sy.bar();  // issued, or an error recorded before any thread of the group waits
+    sy.bar();  // issued, or not, before any thread of the group waits
 }
 __device__ __forceinline__ void tf_gemm_wait(TfGemm &g) {
     if (ld_err(g.err) == 0 && !mbar_wait(g.mbar, g.ph & 1u)) atomicOr(g.err, 2);
@@ -2217,7 +2243,7 @@ __device__ __forceinline__ void tf_gemm_wait(TfGemm &g) {
 // A of the step kernel (the group holds the lock): q of the chunk's state
 // columns [col0, col0 + nvalid) into TMEM columns dt (even beads), dt + 64.
 template <int ND>
-__device__ __forceinline__ void tf_positions_pair(const WgSync &sy, TfGemm &g, const TfOps &op, const TfPair &x,
+__device__ __forceinline__ void tf_positions_pair(const WgSync &sy, TfGemm &g, TpShared *sh, const TfPair &x,
                                                   const float *q, int64_t col0, int nvalid, int c_row, int lane,
                                                   uint32_t dt) {
     float4 L[16];
@@ -2225,7 +2251,7 @@ __device__ __forceinline__ void tf_positions_pair(const WgSync &sy, TfGemm &g, c
     const float *row = q + (size_t)(col0 + (valid ? tf_srow<ND>(c_row) : 0)) * kFP;
     tf_fold_load(L, lane, valid, [&](int k) { return *reinterpret_cast<const float4 *>(row + k); });
     tf_fold_store(L, x, c_row, lane);
-    tf_gemm_pair_issue(sy, g, op, x, dt);
+    tf_gemm_pair_issue(sy, g, sh, dt);
     tf_gemm_wait(g);
 }
 // C of the step kernel (the group holds the lock), then, when next, the A of
@@ -2233,7 +2259,7 @@ __device__ __forceinline__ void tf_positions_pair(const WgSync &sy, TfGemm &g, c
 // 64; the next chunk's q rows are loaded while those GEMMs run, then its
 // positions go to dp, dp + 64.  next is uniform over the group.
 template <int ND>
-__device__ __forceinline__ void tf_modes_then_positions(const WgSync &sy, TfGemm &g, const TfOps &op, const TfPair &x,
+__device__ __forceinline__ void tf_modes_then_positions(const WgSync &sy, TfGemm &g, TpShared *sh, const TfPair &x,
                                                         const float *S, int nvalid, uint32_t df, bool next,
                                                         const float *q, int64_t ncol0, int nnvalid, int c_row,
                                                         int lane, uint32_t dp) {
@@ -2249,7 +2275,7 @@ __device__ __forceinline__ void tf_modes_then_positions(const WgSync &sy, TfGemm
         sy.bar();  // every thread has read the staging, which now takes v
         tf_store_v(x.vhi, x.vlo, c_row, lane, v);
     }
-    tf_gemm_pair_issue(sy, g, op, x, df);
+    tf_gemm_pair_issue(sy, g, sh, df);
     if (next) {
         float4 L[16];
         const bool valid = tf_valid<ND>(c_row, nnvalid);
@@ -2257,7 +2283,7 @@ __device__ __forceinline__ void tf_modes_then_positions(const WgSync &sy, TfGemm
         tf_fold_load(L, lane, valid, [&](int k) { return *reinterpret_cast<const float4 *>(row + k); });
         tf_gemm_wait(g);  // the operands are read: they take the next chunk's q
         tf_fold_store(L, x, c_row, lane);
-        tf_gemm_pair_issue(sy, g, op, x, dp);
+        tf_gemm_pair_issue(sy, g, sh, dp);
     }
     tf_gemm_wait(g);
 }
@@ -2314,12 +2340,15 @@ __global__ void __launch_bounds__(kTpThreads, 1) k_tf_step(TfArgs a) {
     const TfOps op{smem_u32(base), smem_u32(base) + kOpBytes, smem_u32(base) + 2 * kOpBytes,
                    smem_u32(base) + 3 * kOpBytes, smem_u32(Xhi), smem_u32(Xlo)};
     if (tid == 0) {
-        mbar_init(&sh->mma_bar[0], 1);
-        mbar_init(&sh->mma_bar[1], 1);
+        mbar_init(&sh->mma_bar[0], 2);
+        mbar_init(&sh->mma_bar[1], 2);
         mbar_init(&sh->tma_bar, 1);
         sh->err = 0;
         sh->lock = 0;
         sh->stop[0] = sh->stop[1] = 0;
+        const uint32_t sv = smem_u32(S);
+        const uint32_t ad[8] = {op.te_hi, op.te_lo, op.to_hi, op.to_lo, op.xh, op.xl, sv, sv + (uint32_t)kTfPlane};
+        for (int i = 0; i < 8; i++) sh->desc[i] = make_desc(ad[i]);
         fence_barrier_init();
     }
     // the surface table (uniform reads in every evaluation: L1 is what shared
@@ -2362,7 +2391,7 @@ __global__ void __launch_bounds__(kTpThreads, 1) k_tf_step(TfArgs a) {
     if (K > 0) {
         const bool held = tf_lock(sy, sh);
         const int64_t rc = ring_of(0);
-        tf_positions_pair<ND>(sy, G, op, xp, a.q, rc * ND, nvalid_of(rc), c_row, lane, tcol);
+        tf_positions_pair<ND>(sy, G, sh, xp, a.q, rc * ND, nvalid_of(rc), c_row, lane, tcol);
         tf_unlock(sy, sh, held);
     }
 #pragma unroll 1
@@ -2397,14 +2426,14 @@ __global__ void __launch_bounds__(kTpThreads, 1) k_tf_step(TfArgs a) {
             // the next chunk's positions (its q is final: it stepped before this one)
             const bool next = nown >= 2 && k + 1 < K;
             const int64_t rn = next ? ring_of(k + 1) : rc;
-            tf_modes_then_positions<ND>(sy, G, op, xp, S, nvalid, tcol + 128, next, a.q, rn * ND, nvalid_of(rn),
+            tf_modes_then_positions<ND>(sy, G, sh, xp, S, nvalid, tcol + 128, next, a.q, rn * ND, nvalid_of(rn),
                                         c_row, lane, tcol);
         }
         tf_unlock(sy, sh, held);
         tf_update<ND>(a, ax, &sh->err, tq + 128, j, hh, lane, col0, nvalid, s);
         if (nown == 1 && k + 1 < K) {  // one chunk: its next positions need this update
             const bool h2 = tf_lock(sy, sh);
-            tf_positions_pair<ND>(sy, G, op, xp, a.q, col0, nvalid, c_row, lane, tcol);
+            tf_positions_pair<ND>(sy, G, sh, xp, a.q, col0, nvalid, c_row, lane, tcol);
             tf_unlock(sy, sh, h2);
         }
         sy.bar();
@@ -2415,7 +2444,7 @@ __global__ void __launch_bounds__(kTpThreads, 1) k_tf_step(TfArgs a) {
     // let whatever is in flight land (immediate when it has), then release TMEM:
     // the group's last committed GEMM (after a failed wait it may still run) and
     // the image copy (outstanding if no GEMM waited for it); both waits bounded
-    if (sy.elected() && G.nc > 0) mbar_wait(G.mbar, (G.nc - 1) & 1u);
+    if ((wtid == 0 || wtid == 32) && G.nc > 0) mbar_wait(G.mbar, (G.nc - 1) & 1u);
     tc_before();
     __syncthreads();
     if (tid == 0) {
