@@ -183,6 +183,9 @@ def roofline(ctx, pg, c, ti, beads, M, adv_ms, peaks, peak_kind, fp32_tflops):
         minor = sum(m * n for i, (_, m, n, _) in enumerate(kt) if i != dom)
         kms = (adv_ms - minor) / max(kcount, 1)
         traffic = tj.get(name.split()[0])
+        per_md = tj.get(name.split()[0] + "_per_md_step")  # traffic that scales with the MD steps of a launch
+        if traffic is None and per_md is not None:
+            traffic = per_md * M / max(kcount, 1)
     else:
         # several kernels per MD step (blocked form): the MD step is the unit
         name = " + ".join(n.split()[0] for n, _, _, _ in kt) + " (one MD step)"
@@ -279,6 +282,32 @@ def instanton_leg(pg, device):
     return {"betas": nb, "N": N, "dofs": c["ndim"] * c["natom"], "optimize_s": t_opt, "logdet_s": t_det,
             "iterations_mean": float(np.mean(it)), "converged": int(np.sum(st == 0)),
             "note": "one batched L-BFGS, each polymer on a thread-block cluster; host-timed calls"}
+
+
+def p256_leg(pg, device, peaks, peak_kind, fp32, M=100, K=3):
+    """The c2 batch (3,072 rings of the 9-atom surface, P = 256) in the persistent
+    folded step kernel: device time of K advances of M MD steps after one warm-up,
+    L2 flushed before each, and its roofline terms."""
+    import torch
+    c, ti = _workload(0, "c2")
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    with pg.Context(device) as ctx:
+        ctx.set_system(c["ndim"], c["natom"], c["mass"], c["pes_id"], c["params"], c["V0"])
+        cfg = ti.ti_config(pg, pg.PG_MIXED, pg.PG_FORM_AUTO)
+        ctx.ti_setup(cfg, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
+        ctx.ti_advance(M)
+        dev_s = 0.0
+        for _ in range(K):
+            flush.add_(1.0)
+            torch.cuda.synchronize()
+            dev_s += ctx.ti_advance_timed(M) / 1e3
+        form_used, launches = ctx.ti_form(M)
+        roof = roofline(ctx, pg, c, ti, ti.nrings * ti.P, M, 1e3 * dev_s / K, peaks, peak_kind, fp32)
+        _, _, _, st = ctx.ti_results()
+    return {"value": ti.nrings * ti.P * M * K / dev_s, "unit": UNIT, "rings": ti.nrings, "P": ti.P,
+            "md_steps": M * K, "device_s": dev_s, "launches_per_advance": launches, "roofline": roof,
+            "nan_rings": int(np.sum(st != 0)),
+            "note": "persistent folded step: T folded into two resident 128 x 128 halves, two warp groups per CTA"}
 
 
 def uneven_p_leg(pg, nmc=200):
@@ -492,7 +521,10 @@ def main():
     except Exception as e:  # report, keep the main measurement
         extras["extras_error"] = repr(e)
     if not args.no_extras and rank == 0:
-        for key, leg in (("instanton_c3", lambda: instanton_leg(pg, local)), ("uneven_p_c4", lambda: uneven_p_leg(pg))):
+        fp32 = roof["fp32_peak_tflops_measured"] if roof else None
+        for key, leg in (("p256_c2", lambda: p256_leg(pg, local, peaks, peak_kind, fp32)),
+                         ("instanton_c3", lambda: instanton_leg(pg, local)),
+                         ("uneven_p_c4", lambda: uneven_p_leg(pg))):
             try:
                 extras[key] = leg()
             except Exception as e:

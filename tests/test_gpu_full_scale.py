@@ -7,8 +7,8 @@ c1  mcmod_2dtest, P = 128, the full batch of 1,024 x 16 = 16,384 rings:
     mixed precision (persistent tcgen05 step kernel) against the FP64 form,
     same seeds, 600 steps: the splitting within the metric's 1 % and every
     lambda point's mean far inside its statistical error.
-c2  9-atom surface, P = 256, the full 256 x 12 = 3,072 rings: the blocked
-    tcgen05 form against FP64, same seeds, 300 steps, the same checks.
+c2  9-atom surface, P = 256, the full 256 x 12 = 3,072 rings: the persistent
+    folded tcgen05 step against FP64, same seeds, 300 steps, the same checks.
 c3  instanton, N = 512 beads, 27 dofs (13,824-dim Hessian): the batched GPU
     L-BFGS at the lowest and highest beta against scipy L-BFGS-B (the
     algorithm of the reference's lbfgsb.f) on the oracle's action to 1e-8,
