@@ -413,7 +413,7 @@ def _extras(ctx, pg, cfg, ti, M, K, value, ws, beads, extras):
     extras["e2e"] = {"value": beads * M / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                      "d2h_bytes_per_step": int(d2h), "call": "pg_propagate_pimd (host buffers)"}
     # FP64 denominators on the same rings
-    for name, form64, md in (("plain_fp64", pg.PG_FORM_PLAIN, 4), ("fused_fp64", pg.PG_FORM_FUSED, 20)):
+    for name, form64, md in (("plain_fp64", pg.PG_FORM_PLAIN, 20), ("fused_fp64", pg.PG_FORM_FUSED, 100)):
         cfg64 = ti.ti_config(pg, pg.PG_FP64, form64)
         ctx.ti_setup(cfg64, ti.ring_lambda, ti.ring_seed, ti.ring_stream, ti.a, ti.b, ti.dbdl, ti.xref)
         ctx.ti_advance(md)
