@@ -666,14 +666,15 @@ __device__ __forceinline__ void tile_issue(unsigned char *base, TcShared *sh, ui
         return;
     }
     const uint32_t th = smem_u32(base), tl = th + kOpBytes, xh = th + 2 * kOpBytes, xl = xh + kXPlane;
+    // descriptors of K step 0; step ks adds its byte offset / 16 to the start
+    // address field (shared addresses stay below 2^18, so no carry leaves it)
+    const uint64_t dth0 = make_desc(th), dtl0 = make_desc(tl), dxh0 = make_desc_x(xh), dxl0 = make_desc_x(xl);
 #pragma unroll
     for (int ks = 0; ks < kP / 16; ks++) {
-        const uint64_t dth = make_desc(th + (uint32_t)ks * 2 * kLBO), dtl = make_desc(tl + (uint32_t)ks * 2 * kLBO);
-        const uint64_t dxh = make_desc_x(xh + (uint32_t)ks * 2 * kXLbo),
-                       dxl = make_desc_x(xl + (uint32_t)ks * 2 * kXLbo);
-        mma_bf16_n64(tmem, dth, dxh, ks > 0 ? 1u : 0u);
-        mma_bf16_n64(tmem, dth, dxl, 1u);
-        mma_bf16_n64(tmem, dtl, dxh, 1u);
+        const uint64_t ot = (uint64_t)(ks * 2 * kLBO / 16), ox = (uint64_t)(ks * 2 * kXLbo / 16);
+        mma_bf16_n64(tmem, dth0 + ot, dxh0 + ox, ks > 0 ? 1u : 0u);
+        mma_bf16_n64(tmem, dth0 + ot, dxl0 + ox, 1u);
+        mma_bf16_n64(tmem, dtl0 + ot, dxh0 + ox, 1u);
     }
     mma_commit(&sh->mma_bar);
 }
@@ -1314,6 +1315,8 @@ __device__ __forceinline__ bool tb_gemm(unsigned char *base, TcShared *sh, const
         if (kb + 1 < mb) fetch(kb + 1);
         if (tid == 0 && sh->err == 0) {
             const uint32_t th = smem_u32(base), tl = th + kOpBytes, xh = smem_u32(Xhi), xl = smem_u32(Xlo);
+            // K-step descriptors as in tile_issue: step 0's plus the byte offset / 16
+            const uint64_t dth0 = make_desc(th), dtl0 = make_desc(tl), dxh0 = make_desc_x(xh), dxl0 = make_desc_x(xl);
             for (int ib = 0; ib < mb; ib++, j++) {
                 const unsigned char *blk = a.gT + (size_t)(ib * mb + kb) * 2 * kOpBytes;
                 const uint32_t d = tmem + (uint32_t)(64 * ib);
@@ -1342,11 +1345,9 @@ __device__ __forceinline__ bool tb_gemm(unsigned char *base, TcShared *sh, const
                 tc_after();
 #pragma unroll
                 for (int ks = 0; ks < kP / 16; ks++) {
-                    const uint64_t dth = make_desc(th + (uint32_t)ks * 2 * kLBO);
-                    const uint64_t dxh = make_desc_x(xh + (uint32_t)ks * 2 * kXLbo),
-                                   dxl = make_desc_x(xl + (uint32_t)ks * 2 * kXLbo);
-                    mma_bf16_n64(d, dth, dxh, (kb > 0 || ks > 0) ? 1u : 0u);
-                    mma_bf16_n64(d, dth, dxl, 1u);
+                    const uint64_t ot = (uint64_t)(ks * 2 * kLBO / 16), ox = (uint64_t)(ks * 2 * kXLbo / 16);
+                    mma_bf16_n64(d, dth0 + ot, dxh0 + ox, (kb > 0 || ks > 0) ? 1u : 0u);
+                    mma_bf16_n64(d, dth0 + ot, dxl0 + ox, 1u);
                 }
                 mma_commit(&sh->mma_bar);
                 hi_last = j;
@@ -1357,9 +1358,8 @@ __device__ __forceinline__ bool tb_gemm(unsigned char *base, TcShared *sh, const
                 tc_after();
 #pragma unroll
                 for (int ks = 0; ks < kP / 16; ks++) {
-                    const uint64_t dtl = make_desc(tl + (uint32_t)ks * 2 * kLBO);
-                    const uint64_t dxh = make_desc_x(xh + (uint32_t)ks * 2 * kXLbo);
-                    mma_bf16_n64(d, dtl, dxh, 1u);
+                    const uint64_t ot = (uint64_t)(ks * 2 * kLBO / 16), ox = (uint64_t)(ks * 2 * kXLbo / 16);
+                    mma_bf16_n64(d, dtl0 + ot, dxh0 + ox, 1u);
                 }
                 mma_commit(&sh->mma_bar2);
                 lo_last = j;
