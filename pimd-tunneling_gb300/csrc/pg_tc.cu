@@ -1828,6 +1828,8 @@ struct TfArgs {
     int64_t imin;
     const unsigned char *gT;  // folded image (128 KB)
     const float *fold;        // natom x P x 8 folded kick / rotation / OU map
+    const float *mbase;       // P x 8: the map of a unit mass (k_tf_step)
+    const float4 *ascale;     // natom: (m, sqrt m, 1 / m, 1 / sqrt m) of each atom (k_tf_step)
     float *q, *pi, *x;        // [ring][dof][P]
     RingAcc *acc;
     const float *cxa, *cxs;
@@ -1856,6 +1858,7 @@ struct TpShared {
 // A group's column values of its current chunk (shared memory), loaded at the
 // start of each chunk step.
 struct TfAux {
+    float4 msc[kTfCols];  // the column's atom mass factors (m, sqrt m, 1 / m, 1 / sqrt m)
     float xa[kTfCols], xs[kTfCols];
     double west[kTfCols];
     uint64_t seed[kTfCols];
@@ -2078,15 +2081,24 @@ __device__ __forceinline__ void tf_stage_copy(const int32_t *err, uint32_t ts, i
 // D: kick, half rotation, OU, half rotation of modes 2j and 2j + 1 of the
 // chunk's columns, the forces in modes read from TMEM (tf: the group's force
 // columns at this warp's lane quarter), 8-column groups in two halves of 4 (a
-// half lies in one ring).  Written for two 27-dof rings per chunk.  Each half first issues its loads (q, pi and the
-// folded maps of the at most two atoms its columns belong to: three dofs per
-// atom), then draws the normals while they are in flight.  Warp-uniform, as B.
+// half lies in one ring).  Written for two 27-dof rings per chunk.  The map of
+// (atom, mode) is the unit-mass map of the mode times the atom's mass factors:
+// the bead masses m (lambda_k tau)^2 make the mode frequencies 1 / tau and the
+// OU factor exp(-gamma dt / tau) mass-free, so [K11 K12 N1 D1 | K21 K22 N2 D2]
+// scale as [1, m, sqrt m, 1 | 1 / m, 1, 1 / sqrt m, 1 / m] (checked on the host
+// against the per-atom maps).  Each half first issues its q and pi loads, then
+// draws the normals while they are in flight.  Warp-uniform, as B.
 template <int ND>
 __device__ __forceinline__ void tf_update(const TfArgs &a, const TfAux &ax, const int32_t *err, uint32_t tf, int j,
                                           int hh, int lane, int64_t col0, int nvalid, int64_t s) {
     if (!__all_sync(0xffffffffu, ld_err(err) == 0)) return;
     const int e = lane & 3;
     const int mq = 2 * (j - e);  // the quad's modes mq .. mq + 7
+    // unit-mass maps of modes 2j and 2j + 1
+    const float4 b1e = __ldg(reinterpret_cast<const float4 *>(a.mbase + (size_t)(2 * j) * 8));
+    const float4 b2e = __ldg(reinterpret_cast<const float4 *>(a.mbase + (size_t)(2 * j) * 8 + 4));
+    const float4 b1o = __ldg(reinterpret_cast<const float4 *>(a.mbase + (size_t)(2 * j + 1) * 8));
+    const float4 b2o = __ldg(reinterpret_cast<const float4 *>(a.mbase + (size_t)(2 * j + 1) * 8 + 4));
 #pragma unroll 1
     for (int g = 0; g < 4; g++) {
         // the 8 column groups of two rings (3 full and one with 3 dofs each) split
@@ -2109,13 +2121,6 @@ __device__ __forceinline__ void tf_update(const TfArgs &a, const TfAux &ax, cons
                 q2[t] = *reinterpret_cast<const float2 *>(a.q + (size_t)(col0 + col) * kFP + 2 * j);
                 p2[t] = *reinterpret_cast<const float2 *>(a.pi + (size_t)(col0 + col) * kFP + 2 * j);
             }
-            const int atA = ax.jdof[sc0] / 3, atB = ax.jdof[sc0 + nt - 1] / 3;
-            float4 kA[4], kB[4];
-#pragma unroll
-            for (int i = 0; i < 4; i++) {
-                kA[i] = __ldg(reinterpret_cast<const float4 *>(a.fold + ((size_t)atA * kFP + 2 * j) * 8) + i);
-                kB[i] = __ldg(reinterpret_cast<const float4 *>(a.fold + ((size_t)atB * kFP + 2 * j) * 8) + i);
-            }
             float zE[4], zO[4];
             {
                 const bool ok = e < nt;  // this lane draws the blocks of state column sc0 + e
@@ -2136,15 +2141,15 @@ __device__ __forceinline__ void tf_update(const TfArgs &a, const TfAux &ax, cons
             for (int t = 0; t < 4; t++) {
                 if (t >= nt) break;
                 const int col = sc0 + t;
-                const bool A = ax.jdof[col] / 3 == atA;
-                const float4 k1e = A ? kA[0] : kB[0], k2e = A ? kA[1] : kB[1];
-                const float4 k1o = A ? kA[2] : kB[2], k2o = A ? kA[3] : kB[3];
+                const float4 ms = ax.msc[col];  // m, sqrt m, 1 / m, 1 / sqrt m
                 const float ge = gE[t4 + t], go = gO[t4 + t];
                 float2 pn, qn;
-                pn.x = fmaf(k1e.x, p2[t].x, fmaf(-k1e.w, ge, fmaf(k1e.y, q2[t].x, k1e.z * zE[t])));
-                qn.x = fmaf(k2e.x, p2[t].x, fmaf(-k2e.w, ge, fmaf(k2e.y, q2[t].x, k2e.z * zE[t])));
-                pn.y = fmaf(k1o.x, p2[t].y, fmaf(-k1o.w, go, fmaf(k1o.y, q2[t].y, k1o.z * zO[t])));
-                qn.y = fmaf(k2o.x, p2[t].y, fmaf(-k2o.w, go, fmaf(k2o.y, q2[t].y, k2o.z * zO[t])));
+                pn.x = fmaf(b1e.x, p2[t].x, fmaf(-b1e.w, ge, fmaf(b1e.y * ms.x, q2[t].x, (b1e.z * ms.y) * zE[t])));
+                qn.x = fmaf(b2e.x * ms.z, p2[t].x,
+                            fmaf(-(b2e.w * ms.z), ge, fmaf(b2e.y, q2[t].x, (b2e.z * ms.w) * zE[t])));
+                pn.y = fmaf(b1o.x, p2[t].y, fmaf(-b1o.w, go, fmaf(b1o.y * ms.x, q2[t].y, (b1o.z * ms.y) * zO[t])));
+                qn.y = fmaf(b2o.x * ms.z, p2[t].y,
+                            fmaf(-(b2o.w * ms.z), go, fmaf(b2o.y, q2[t].y, (b2o.z * ms.w) * zO[t])));
                 *reinterpret_cast<float2 *>(a.q + (size_t)(col0 + col) * kFP + 2 * j) = qn;
                 *reinterpret_cast<float2 *>(a.pi + (size_t)(col0 + col) * kFP + 2 * j) = pn;
                 if (pn.x != pn.x || pn.y != pn.y) {
@@ -2408,6 +2413,7 @@ __global__ void __launch_bounds__(kTpThreads, 1) k_tf_step(TfArgs a) {
             ax.seed[wtid] = ok ? a.cseed[c] : 0;
             ax.stream[wtid] = ok ? a.cstream[c] : 0;
             ax.jdof[wtid] = ok ? a.cjdof[c] : 0;
+            ax.msc[wtid] = ok ? a.ascale[a.cjdof[c] / a.ndim] : make_float4(0.f, 0.f, 0.f, 0.f);
         }
         if (sy.elected()) {  // into L2 while the forces run: this chunk's state for D, the next chunk's q for A
             prefetch_l2(a.pi + (size_t)col0 * kFP, (uint32_t)(nvalid * kFP * sizeof(float)));
@@ -2606,6 +2612,60 @@ int tf_supported(const TiState &st, const pg_ctx &ctx) {
            ctx.fparams.size() <= (size_t)kTfParams;
 }
 
+// (p, q) <- R O R (p - dt g, q) as one map: R the half rotation [rA rB; rC rD],
+// O the OU step p <- ou_a p + ou_s z, composed in FP64:
+// [K11 K12 N1 K11 dt | K21 K22 N2 K21 dt].
+static void fold_map(const ModeCoef &c, double dt, double (&o)[8]) {
+    const double k11 = c.ou_a * c.rA * c.rA + c.rB * c.rC, k12 = c.ou_a * c.rA * c.rB + c.rB * c.rD;
+    const double k21 = c.rC * (c.ou_a * c.rA + c.rD), k22 = c.ou_a * c.rB * c.rC + c.rD * c.rD;
+    o[0] = k11;
+    o[1] = k12;
+    o[2] = c.rA * c.ou_s;
+    o[3] = k11 * dt;
+    o[4] = k21;
+    o[5] = k22;
+    o[6] = c.rC * c.ou_s;
+    o[7] = k21 * dt;
+}
+
+// The folded step's update maps as a unit-mass map per mode (base, P x 8) and
+// mass factors per atom (scale, natom x 4: m, sqrt m, 1 / m, 1 / sqrt m): with
+// bead masses m (lambda_k tau)^2 the map of (atom, mode) is the mode's base
+// times [1, m, sqrt m, 1 | 1 / m, 1, 1 / sqrt m, 1 / m].  Checked against the
+// per-atom maps (relative 1e-9 in FP64); PG_ERR_STATE if they do not factor.
+static int tf_mass_tables(const pg_ctx *ctx, const TiState &st, float *base, float *scale) {
+    const int P = st.P, natom = ctx->natom;
+    auto factors = [](double m, double (&f)[8]) {
+        const double r = std::sqrt(m);
+        const double v[8] = {1.0, m, r, 1.0, 1.0 / m, 1.0, 1.0 / r, 1.0 / m};
+        for (int i = 0; i < 8; i++) f[i] = v[i];
+    };
+    double f0[8];
+    factors(ctx->mass[0], f0);
+    for (int k = 0; k < P; k++) {
+        double b[8];
+        fold_map(st.hcoef[(size_t)natom * k], st.cfg.dt, b);
+        for (int i = 0; i < 8; i++) b[i] /= f0[i];
+        for (int at = 0; at < natom; at++) {
+            double o[8], f[8];
+            fold_map(st.hcoef[(size_t)at + (size_t)natom * k], st.cfg.dt, o);
+            factors(ctx->mass[at], f);
+            for (int i = 0; i < 8; i++)
+                if (!(std::fabs(o[i] - b[i] * f[i]) <= 1e-9 * std::fabs(o[i]) + 1e-300))
+                    return fail(PG_ERR_STATE, "folded step: the update maps do not factor into mode and mass parts");
+        }
+        for (int i = 0; i < 8; i++) base[(size_t)k * 8 + i] = (float)b[i];
+    }
+    for (int at = 0; at < natom; at++) {
+        const double m = ctx->mass[at], r = std::sqrt(m);
+        scale[4 * at] = (float)m;
+        scale[4 * at + 1] = (float)r;
+        scale[4 * at + 2] = (float)(1.0 / m);
+        scale[4 * at + 3] = (float)(1.0 / r);
+    }
+    return PG_OK;
+}
+
 // Tensor-core tables of a batch: the split image of T (rebuilt only when P or
 // the buffer changes), the FP32 coefficient and folded-map tables (uploaded
 // when they differ from the last upload), the error word, and the column table.
@@ -2632,22 +2692,12 @@ int tc_prepare(pg_ctx *ctx, TiState &st) {
             o[5] = (float)c.ou_s;
             o[6] = (float)c.pscale;  // sqrt(beadmass / betan): Andersen momentum scale
         }
-    // (p, q) <- R O R (p - dt g, q) as one map: R the half rotation [rA rB; rC rD],
-    // O the OU step p <- ou_a p + ou_s z, composed in FP64.
     for (int at = 0; at < ctx->natom; at++)
         for (int k = 0; k < P; k++) {
-            const ModeCoef &c = mc[(size_t)at + (size_t)ctx->natom * k];
-            const double k11 = c.ou_a * c.rA * c.rA + c.rB * c.rC, k12 = c.ou_a * c.rA * c.rB + c.rB * c.rD;
-            const double k21 = c.rC * (c.ou_a * c.rA + c.rD), k22 = c.ou_a * c.rB * c.rC + c.rD * c.rD;
+            double m8[8];
+            fold_map(mc[(size_t)at + (size_t)ctx->natom * k], st.cfg.dt, m8);
             float *o = &fold[((size_t)at * P + k) * 8];
-            o[0] = (float)k11;
-            o[1] = (float)k12;
-            o[2] = (float)(c.rA * c.ou_s);
-            o[3] = (float)(k11 * st.cfg.dt);
-            o[4] = (float)k21;
-            o[5] = (float)k22;
-            o[6] = (float)(c.rC * c.ou_s);
-            o[7] = (float)(k21 * st.cfg.dt);
+            for (int i = 0; i < 8; i++) o[i] = (float)m8[i];
         }
     unsigned char *d = st.Tbf.as<unsigned char>();
     const bool same_buf = st.tc_img_ptr == (const void *)d;
@@ -2699,7 +2749,9 @@ int tc_prepare(pg_ctx *ctx, TiState &st) {
     PG_CUDA(cudaFuncSetAttribute(k_tb_force, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)tb_force_smem(st.nd, (int)ctx->fparams.size())));
     if (st.tf_fused) {
-        e = st.tfimg.ensure(kTfImg);
+        // [folded image 128 KB | unit-mass maps P x 8 | atom mass factors natom x 4]
+        const size_t nb = (size_t)kFP * 8, ns = (size_t)ctx->natom * 4;
+        e = st.tfimg.ensure(kTfImg + (nb + ns) * sizeof(float));
         if (e != cudaSuccess) return cuda_fail(e, "folded transform image");
         if (st.tf_img_ptr != st.tfimg.ptr) {  // written once per buffer
             std::vector<unsigned char> img;
@@ -2708,6 +2760,11 @@ int tc_prepare(pg_ctx *ctx, TiState &st) {
             PG_CUDA(cudaStreamSynchronize(ctx->stream));  // img is a local pageable buffer
             st.tf_img_ptr = st.tfimg.ptr;
         }
+        std::vector<float> mt(nb + ns);
+        if (int rc = tf_mass_tables(ctx, st, mt.data(), mt.data() + nb)) return rc;
+        PG_CUDA(cudaMemcpyAsync(st.tfimg.as<unsigned char>() + kTfImg, mt.data(), mt.size() * sizeof(float),
+                                cudaMemcpyHostToDevice, ctx->stream));
+        PG_CUDA(cudaStreamSynchronize(ctx->stream));  // mt is a local pageable buffer
         const int sm = (int)tf_step_smem_bytes(), so = (int)tf_out_smem_bytes();
         PG_CUDA(cudaFuncSetAttribute(k_tf_step<27, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
         PG_CUDA(cudaFuncSetAttribute(k_tf_out<27, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, so));
@@ -2958,6 +3015,8 @@ static void tf_make_args(pg_ctx *ctx, TiState &st, TfArgs &f) {
     f.imin = st.cfg.imin;
     f.gT = st.tfimg.as<unsigned char>();
     f.fold = a.fold;
+    f.mbase = reinterpret_cast<const float *>(st.tfimg.as<unsigned char>() + kTfImg);
+    f.ascale = reinterpret_cast<const float4 *>(st.tfimg.as<unsigned char>() + kTfImg + (size_t)kFP * 8 * sizeof(float));
     f.q = a.q;
     f.pi = a.pi;
     f.x = a.x;
