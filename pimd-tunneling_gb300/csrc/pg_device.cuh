@@ -483,12 +483,64 @@ __device__ __forceinline__ R pes_synth18(const PesArgs &pa, const R *x, R *g) {
             }
         }
     }
-    for (int m = 0; m < nmol; m++)
-        for (int n = m + 1; n < nmol; n++)
+    // site pairs of molecules m < n.  FP32: the two molecules' coordinates and
+    // gradient in registers for their nine site pairs (ia, ib unrolled), read
+    // from and written back to x / g once per molecule pair; every gradient
+    // component receives its terms in the same order as pair by pair (FP64 keeps
+    // the pair-by-pair loop: its 36 doubles would lower the occupancy of the FP64
+    // kernels for every surface).
+    if constexpr (sizeof(R) == 8) {
+        for (int m = 0; m < nmol; m++)
+            for (int n = m + 1; n < nmol; n++)
+                for (int ia = 0; ia < 3; ia++)
+                    for (int ib = 0; ib < 3; ib++) {
+                        const R *A = x + 9 * m + 3 * ia, *Bp = x + 9 * n + 3 * ib;
+                        R d0 = A[0] - Bp[0], d1 = A[1] - Bp[1], d2 = A[2] - Bp[2];
+                        R r2 = d0 * d0 + d1 * d1 + d2 * d2;
+                        R r = my_sqrt<R>(r2);
+                        R qa = ia == 0 ? qO : qH, qb = ib == 0 ? qO : qH;
+                        R e = pdiv<R>(qa * qb, r);
+                        R dvr = pdiv<R>(-e, r2);
+                        if (ia == 0 && ib == 0) {
+                            R sr2 = pdiv<R>(sig * sig, r2);
+                            R sr6 = sr2 * sr2 * sr2;
+                            R sr12 = sr6 * sr6;
+                            e += (R)4.0 * eps * (sr12 - sr6);
+                            dvr += pdiv<R>((R)4.0 * eps * ((R)-12.0 * sr12 + (R)6.0 * sr6), r2);
+                        }
+                        v += e;
+                        if (g) {
+                            int ai = 9 * m + 3 * ia, bi = 9 * n + 3 * ib;
+                            g[ai] += dvr * d0;
+                            g[ai + 1] += dvr * d1;
+                            g[ai + 2] += dvr * d2;
+                            g[bi] -= dvr * d0;
+                            g[bi + 1] -= dvr * d1;
+                            g[bi + 2] -= dvr * d2;
+                        }
+                    }
+        return v - (R)pa.V0;
+    }
+    for (int m = 0; m < nmol; m++) {
+        R xm[9], gm[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) {
+            xm[k] = x[9 * m + k];
+            gm[k] = g ? g[9 * m + k] : (R)0;
+        }
+        for (int n = m + 1; n < nmol; n++) {
+            R xn[9], gn[9];
+#pragma unroll
+            for (int k = 0; k < 9; k++) {
+                xn[k] = x[9 * n + k];
+                gn[k] = g ? g[9 * n + k] : (R)0;
+            }
+#pragma unroll
             for (int ia = 0; ia < 3; ia++)
+#pragma unroll
                 for (int ib = 0; ib < 3; ib++) {
-                    const R *A = x + 9 * m + 3 * ia, *Bp = x + 9 * n + 3 * ib;
-                    R d0 = A[0] - Bp[0], d1 = A[1] - Bp[1], d2 = A[2] - Bp[2];
+                    const R d0 = xm[3 * ia] - xn[3 * ib], d1 = xm[3 * ia + 1] - xn[3 * ib + 1],
+                            d2 = xm[3 * ia + 2] - xn[3 * ib + 2];
                     R r2 = d0 * d0 + d1 * d1 + d2 * d2;
                     R r = my_sqrt<R>(r2);
                     R qa = ia == 0 ? qO : qH, qb = ib == 0 ? qO : qH;
@@ -502,16 +554,23 @@ __device__ __forceinline__ R pes_synth18(const PesArgs &pa, const R *x, R *g) {
                         dvr += pdiv<R>((R)4.0 * eps * ((R)-12.0 * sr12 + (R)6.0 * sr6), r2);
                     }
                     v += e;
-                    if (g) {
-                        int ai = 9 * m + 3 * ia, bi = 9 * n + 3 * ib;
-                        g[ai] += dvr * d0;
-                        g[ai + 1] += dvr * d1;
-                        g[ai + 2] += dvr * d2;
-                        g[bi] -= dvr * d0;
-                        g[bi + 1] -= dvr * d1;
-                        g[bi + 2] -= dvr * d2;
-                    }
+                    gm[3 * ia] += dvr * d0;
+                    gm[3 * ia + 1] += dvr * d1;
+                    gm[3 * ia + 2] += dvr * d2;
+                    gn[3 * ib] -= dvr * d0;
+                    gn[3 * ib + 1] -= dvr * d1;
+                    gn[3 * ib + 2] -= dvr * d2;
                 }
+            if (g) {
+#pragma unroll
+                for (int k = 0; k < 9; k++) g[9 * n + k] = gn[k];
+            }
+        }
+        if (g) {
+#pragma unroll
+            for (int k = 0; k < 9; k++) g[9 * m + k] = gm[k];
+        }
+    }
     return v - (R)pa.V0;
 }
 
