@@ -496,8 +496,8 @@ def test_advance_group_equals_separate_advances(pg):
 
 def test_advance_group_one_graph_over_tensor_and_simt_batches(pg):
     """An uneven-P group in one graph launch: the persistent tcgen05 step kernel
-    (P = 128, 2-D surface), the blocked tcgen05 form (P = 256, 27-dof surface) and
-    the fused SIMT form (P = 64) as concurrent branches of one captured graph,
+    (P = 128, 2-D surface), the persistent folded step (P = 256, 27-dof surface)
+    and the fused SIMT form (P = 64) as concurrent branches of one captured graph,
     advanced twice by 25 steps (the second call replays the cached graph), give
     bitwise the state and estimator sums of advancing each batch alone by 50."""
     specs = [("c1", 128, pg.PG_FORM_TENSOR, 40), ("c2", 256, pg.PG_FORM_TENSOR, 3), ("c1", 64, pg.PG_FORM_FUSED, 5)]
