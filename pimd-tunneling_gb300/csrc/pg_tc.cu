@@ -487,6 +487,7 @@ __device__ __forceinline__ uint64_t make_desc_x(uint32_t saddr) {
 
 // Per-column values staged in shared memory by the CTA.
 struct TileAux {
+    float4 msc[kNc];     // the column's atom mass factors (m, sqrt m, 1 / m, 1 / sqrt m)
     float xa[kNc];       // spring-line start a_j
     float xs[kNc];       // spring-line slope (b_j - a_j) / (P + 1)
     float xP[kNc];       // bead-P position for the estimator
@@ -1222,6 +1223,8 @@ struct TbArgs {
     int64_t imin;
     const unsigned char *gT;  // mb x mb block image
     const float *coef;        // natom x P x 8: rA rB rC rD ou_a ou_s pscale
+    const float *kbase;       // P x 8: the same for a unit mass (k_tb_kick)
+    const float4 *kscale;     // natom: (m, sqrt m, 1 / m, 1 / sqrt m) (k_tb_kick)
     const double *mass;
     const double *avec, *bvec, *dbdl;
     const float *Tf;          // P x P FP32 transform (the bead-P row for the Andersen estimator)
@@ -1538,6 +1541,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tb_kick(TbArgs a) {
         ax->stream[tid] = sm;
         ax->jdof[tid] = j;
         ax->atom[tid] = j / a.ndim;
+        ax->msc[tid] = a.kscale[j / a.ndim];
     }
     const uint32_t tmem = tb_begin(sh, a.mb);
     uint32_t phase = 0;
@@ -1552,6 +1556,10 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tb_kick(TbArgs a) {
             const int m = 128 * ib + 32 * (warp & 3) + lane;  // mode
             const int mc = m < P ? m : P - 1;
             const uint32_t taddr = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(64 * ib + cb);
+            // this mode's coefficients for a unit mass; a column's are these times
+            // its atom's mass factors (rB m, rC / m, ou_s sqrt m)
+            const float4 kb4 = __ldg(reinterpret_cast<const float4 *>(a.kbase + (size_t)mc * 8));
+            const float2 kb2 = __ldg(reinterpret_cast<const float2 *>(a.kbase + (size_t)mc * 8 + 4));
 #pragma unroll 1
             for (int c0 = 0; c0 < 32; c0 += kGrp) {
                 const int nvg = nv - c0;
@@ -1561,13 +1569,13 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tb_kick(TbArgs a) {
                 float4 cfa[kGrp];
                 float2 cfb[kGrp];
 #pragma unroll
-                for (int i = 0; i < kGrp; i++) {  // state and coefficients first, then the normals
+                for (int i = 0; i < kGrp; i++) {  // state first, then the normals
                     const bool in = m < P && i < nvg;
                     qv[i] = in ? qo[(size_t)i * P] : 0.f;
                     pv[i] = in ? po[(size_t)i * P] : 0.f;
-                    const float *cf = a.coef + ((size_t)ax->atom[cb + c0 + i] * P + mc) * 8;
-                    cfa[i] = __ldg(reinterpret_cast<const float4 *>(cf));
-                    cfb[i] = __ldg(reinterpret_cast<const float2 *>(cf + 4));
+                    const float4 ms = ax->msc[cb + c0 + i];
+                    cfa[i] = make_float4(kb4.x, kb4.y * ms.x, kb4.z * ms.z, kb4.w);
+                    cfb[i] = make_float2(kb2.x, kb2.y * ms.y);
                 }
                 float gv[kGrp];
                 __syncwarp();
@@ -2584,6 +2592,12 @@ static size_t tbf_err_off(const TiState &st, int natom) {
     return tbf_coef_off(st) + (size_t)natom * st.P * 8 * sizeof(float);
 }
 static size_t tbf_fold_off(const TiState &st, int natom) { return tbf_err_off(st, natom) + 64; }
+static size_t tbf_kbase_off(const TiState &st, int natom) {
+    return tbf_fold_off(st, natom) + (size_t)natom * st.P * 8 * sizeof(float);
+}
+static size_t tbf_kscale_off(const TiState &st, int natom) {
+    return tbf_kbase_off(st, natom) + (size_t)st.P * 8 * sizeof(float);
+}
 
 }  // namespace
 
@@ -2673,13 +2687,15 @@ int tc_prepare(pg_ctx *ctx, TiState &st) {
     st.tc_mb = blocks_for(st.P);
     const int P = st.P;
     size_t ncoef = (size_t)ctx->natom * P * 8;
-    size_t bytes = tbf_fold_off(st, ctx->natom) + ncoef * sizeof(float);
+    const size_t nkb = (size_t)P * 8, nks = (size_t)ctx->natom * 4;
+    size_t bytes = tbf_kscale_off(st, ctx->natom) + nks * sizeof(float);
     cudaError_t e = st.Tbf.ensure(bytes);
     if (e != cudaSuccess) return cuda_fail(e, "tensor-core tables");
     if (st.hcoef.size() != (size_t)ctx->natom * P) return fail(PG_ERR_STATE, "mode coefficients missing");
     const std::vector<ModeCoef> &mc = st.hcoef;
-    std::vector<float> tabs(2 * ncoef, 0.f);  // [coefficients | folded map]
-    float *cf = tabs.data(), *fold = tabs.data() + ncoef;
+    // [coefficients | folded map | unit-mass coefficients | atom mass factors]
+    std::vector<float> tabs(2 * ncoef + nkb + nks, 0.f);
+    float *cf = tabs.data(), *fold = tabs.data() + ncoef, *kb = fold + ncoef, *ks = kb + nkb;
     for (int at = 0; at < ctx->natom; at++)
         for (int k = 0; k < P; k++) {
             const ModeCoef &c = mc[(size_t)at + (size_t)ctx->natom * k];
@@ -2699,6 +2715,31 @@ int tc_prepare(pg_ctx *ctx, TiState &st) {
             float *o = &fold[((size_t)at * P + k) * 8];
             for (int i = 0; i < 8; i++) o[i] = (float)m8[i];
         }
+    // the coefficients of a unit mass: with bead masses m (lambda_k tau)^2, rA, rD and
+    // ou_a do not depend on the atom, rB scales as m, rC as 1 / m, ou_s and pscale
+    // as sqrt m (checked against every atom's coefficients)
+    for (int k = 0; k < P; k++) {
+        const ModeCoef &c0 = mc[(size_t)ctx->natom * k];
+        const double m0 = ctx->mass[0], r0 = std::sqrt(m0);
+        const double b[7] = {c0.rA, c0.rB / m0, c0.rC * m0, c0.rD, c0.ou_a, c0.ou_s / r0, c0.pscale / r0};
+        for (int at = 0; at < ctx->natom; at++) {
+            const ModeCoef &c = mc[(size_t)at + (size_t)ctx->natom * k];
+            const double m = ctx->mass[at], r = std::sqrt(m);
+            const double o[7] = {c.rA, c.rB, c.rC, c.rD, c.ou_a, c.ou_s, c.pscale};
+            const double f[7] = {1.0, m, 1.0 / m, 1.0, 1.0, r, r};
+            for (int i = 0; i < 7; i++)
+                if (!(std::fabs(o[i] - b[i] * f[i]) <= 1e-9 * std::fabs(o[i]) + 1e-300))
+                    return fail(PG_ERR_STATE, "blocked kick: the mode coefficients do not factor into mode and mass parts");
+        }
+        for (int i = 0; i < 7; i++) kb[(size_t)k * 8 + i] = (float)b[i];
+    }
+    for (int at = 0; at < ctx->natom; at++) {
+        const double m = ctx->mass[at], r = std::sqrt(m);
+        ks[4 * at] = (float)m;
+        ks[4 * at + 1] = (float)r;
+        ks[4 * at + 2] = (float)(1.0 / m);
+        ks[4 * at + 3] = (float)(1.0 / r);
+    }
     unsigned char *d = st.Tbf.as<unsigned char>();
     const bool same_buf = st.tc_img_ptr == (const void *)d;
     if (!same_buf || st.tc_img_P != P) {
@@ -2713,7 +2754,7 @@ int tc_prepare(pg_ctx *ctx, TiState &st) {
     if (st.tc_tabs != tabs) {
         PG_CUDA(cudaMemcpyAsync(d + tbf_coef_off(st), cf, ncoef * sizeof(float), cudaMemcpyHostToDevice,
                                 ctx->stream));
-        PG_CUDA(cudaMemcpyAsync(d + tbf_fold_off(st, ctx->natom), fold, ncoef * sizeof(float),
+        PG_CUDA(cudaMemcpyAsync(d + tbf_fold_off(st, ctx->natom), fold, (ncoef + nkb + nks) * sizeof(float),
                                 cudaMemcpyHostToDevice, ctx->stream));
         PG_CUDA(cudaStreamSynchronize(ctx->stream));  // tabs is a local pageable buffer
         st.tc_tabs.swap(tabs);
@@ -2901,6 +2942,8 @@ static void tb_make_args(pg_ctx *ctx, TiState &st, TbArgs &a) {
     unsigned char *d = st.Tbf.as<unsigned char>();
     a.gT = d;
     a.coef = reinterpret_cast<const float *>(d + tbf_coef_off(st));
+    a.kbase = reinterpret_cast<const float *>(d + tbf_kbase_off(st, ctx->natom));
+    a.kscale = reinterpret_cast<const float4 *>(d + tbf_kscale_off(st, ctx->natom));
     a.err = reinterpret_cast<int32_t *>(d + tbf_err_off(st, ctx->natom));
     a.step0 = reinterpret_cast<const int64_t *>(st.red.as<double>() + 3 * st.nlambda);
     a.mass = ctx->d_mass.as<double>();
