@@ -1786,32 +1786,34 @@ __global__ void k_tc_cols(int64_t ncols, int nd, int ndim, int P, const int32_t 
 }
 
 // ---------------------------------------------------------------- persistent folded step (P = 256)
-// One launch runs nsub MD steps of a many-dof batch with P = 256, as k_tc_step
-// does for P = 128, with T resident in shared memory.  T alone (256 x 256,
-// split-BF16 hi and lo) would take 256 KB; the DST-I symmetry
+// One launch runs nsub MD steps of a batch of the 9-atom surface (27 dofs) with
+// P = 256, as k_tc_step does for P = 128, with T resident in shared memory.  T
+// alone (256 x 256, split-BF16 hi and lo) would take 256 KB; the DST-I symmetry
 // T[i][P-1-b] = (-1)^i T[i][b] (0-based) folds it: with u_b = y_b + y_(P-1-b)
 // and v_b = y_b - y_(P-1-b), b < 128,
 //     (T y)_(2j) = sum_b T[2j][b] u_b,     (T y)_(2j+1) = sum_b T[2j+1][b] v_b,
 // so T y is two 128 x 128 products, T_e (even rows) u and T_o (odd rows) v,
 // whose images take 128 KB.  One CTA per SM owns an equal range of whole rings,
-// cut into chunks of RPC rings (RPC x ND <= 64 state columns); each chunk steps
-// on its own (no grid-wide synchronisation).  Per chunk and step:
-//   A  positions: the folded operands of q (u, then v, in one 64-column operand
-//      buffer) and two GEMMs, T_e u into TMEM columns 0-63 and T_o v into 64-127;
-//      TMEM lane j of the first holds bead 2j, of the second bead 2j+1;
+// cut into chunks of two rings (ring r's dof d at operand row and TMEM column
+// 32 r + d); each chunk steps on its own (no grid-wide synchronisation).  Per
+// chunk and step:
+//   A  positions: the folded operands u and v of q and two GEMMs, T_e u into
+//      TMEM columns 0-63 and T_o v into 64-127; TMEM lane j of the first holds
+//      bead 2j, of the second bead 2j+1;
 //   B  forces: the thread of lane j in warp quarter w % 4 and half h = w / 4
-//      reads its bead's ND dofs (x = T q + x*, the spring line added), evaluates
-//      the FP32 surface in registers and stages the gradient in shared memory;
-//      the thread of bead 256 forms the estimator of step s - 1;
-//   C  T F: the folded operands of the staged forces and two GEMMs;
+//      reads its bead's 27 dofs (x = T q + x*, the spring line added), forms the
+//      estimator of step s - 1 (bead 256) and evaluates the unrolled surface in
+//      registers;
+//   C  T F: the folded operands of the forces (staged in shared memory) and two
+//      GEMMs;
 //   D  update: the thread of lane j holds modes 2j and 2j + 1 of 8-column groups
 //      (q, pi as float2, coalesced), draws the Langevin normals of both from the
 //      two Philox blocks of its quad (pairs exchanged by a quad transpose), and
-//      applies the folded kick / rotation / OU / rotation map per mode.
+//      applies the kick / rotation / OU / rotation map per mode.
 // The step kernel (k_tf_step, 512 threads) runs two warp groups of 256 on
 // alternate chunks of the CTA's range, each with its own 256 TMEM columns
 // (positions 0-127, forces 128-255): B and D are long SIMT phases, and the two
-// groups' run side by side.  B leaves its gradients in the group's force
+// groups run side by side.  B leaves its gradients in the group's force
 // columns.  The operand buffer and the force staging in shared memory (the T
 // image leaves no room for a second copy) belong to one group at a time: a
 // group takes the shared-memory lock to copy its gradients to the staging and
