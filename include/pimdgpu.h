@@ -55,7 +55,10 @@ extern "C" {
 #define PG_FORM_PLAIN 1    /* per-step kernel launches in the reference step order
                               (10 NM transforms per Langevin step), FP64 only */
 #define PG_FORM_FUSED 2    /* fused persistent SIMT kernel (FP64 or FP32) */
-#define PG_FORM_TENSOR 3   /* fused persistent tcgen05 kernel (PG_MIXED only) */
+#define PG_FORM_TENSOR 3   /* tcgen05 forms (PG_MIXED only): the persistent step kernel for
+                              P = 128 on the 1-D and 2-D surfaces, the persistent folded
+                              step for P = 256 on the 9-atom surface (Langevin without
+                              dHdrlimit), otherwise three blocked-GEMM kernels per step */
 
 #define PG_ANDERSEN 1
 #define PG_LANGEVIN 2
