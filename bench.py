@@ -157,6 +157,13 @@ def simt_flops_per_bead_step(c):
         fpes = 30.0 * 36 + 20.0
     elif pid == 1:
         fpes = 8.0 * nd
+    elif pid == 4:
+        # 18-atom surface: per molecule two bonds and the angle with their
+        # gradients (80); per site pair of different molecules the distance,
+        # the Coulomb term and its gradient through the B-matrix (20), plus the
+        # Lennard-Jones term of each O-O pair (15)
+        nmol = int(c["params"][0])
+        fpes = 80.0 * nmol + 20.0 * 9 * nmol * (nmol - 1) / 2 + 15.0 * nmol * (nmol - 1) / 2
     else:
         return None
     return fpes + 28.0 * nd
@@ -310,15 +317,39 @@ def p256_leg(pg, device, peaks, peak_kind, fp32, M=100, K=3):
             "note": "persistent folded step: T folded into two resident 128 x 128 halves, two warp groups per CTA"}
 
 
-def uneven_p_leg(pg, nmc=200):
+def uneven_p_leg(pg, peaks=None, fp32=None, nmc=200):
     """The c4 batch: 4,096 rings of the 18-atom surface with P in {64, 128, 256,
-    512}, one context per P advanced together as one CUDA-graph launch."""
+    512}, one context per P advanced together as one CUDA-graph launch; with
+    the measured peaks, its roofline terms from algorithmic work per
+    bead-force-step (the blocked form moves q and x (positions), x and F
+    (forces), F, q, pi in and q, pi out (kick): 36 d bytes; two NM transforms
+    of 2 P d flops each, P weighted by the beads of each bead number)."""
     import drivers
     import pgconfigs
     c = dict(pgconfigs.load("c4"), imin=0)
     r = drivers.run_ti_mixed(c, precision=pg.PG_MIXED, form=pg.PG_FORM_AUTO, nmc=nmc, chunk=nmc // 2)
-    return {"value": r["bead_steps_per_s"], "unit": UNIT, "rings": r["nrings"], "md_steps": nmc,
-            "device_s": r["device_s"], "note": "pg_ti_advance_group: every P's step kernels in one graph launch"}
+    out = {"value": r["bead_steps_per_s"], "unit": UNIT, "rings": r["nrings"], "md_steps": nmc,
+           "device_s": r["device_s"], "note": "pg_ti_advance_group: every P's step kernels in one graph launch"}
+    if peaks:
+        Pr = np.asarray(c["P_per_ring"], dtype=float)
+        nd = c["ndim"] * c["natom"]
+        rate = r["bead_steps_per_s"]
+        p_eff = float(np.sum(Pr * Pr) / np.sum(Pr))  # bead-weighted P
+        terms = {"tensor": {"flops_per_bead_step": 4.0 * p_eff * nd, "peak": peaks["bf16_tflops"],
+                            "unit": "TFLOP/s"},
+                 "hbm": {"bytes_per_bead_step": 36.0 * nd * 4, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                         "basis": "algorithmic bytes (no capture of the group)"}}
+        terms["tensor"]["achieved"] = terms["tensor"]["flops_per_bead_step"] * rate / 1e12
+        terms["hbm"]["achieved"] = terms["hbm"]["bytes_per_bead_step"] * rate / 1e9
+        fs = simt_flops_per_bead_step(c)
+        if fs is not None and fp32:
+            terms["simt"] = {"flops_per_bead_step": fs, "achieved": fs * rate / 1e12, "peak": fp32, "unit": "TFLOP/s"}
+        for t in terms.values():
+            t["frac"] = t["achieved"] / t["peak"]
+        bind = max(terms, key=lambda k: terms[k]["frac"])
+        out["roofline"] = {"binding_term": bind, "frac": terms[bind]["frac"], "p_bead_weighted": p_eff,
+                           "terms": terms}
+    return out
 
 
 def cpu_reference_rate(c, ti, target_s=12.0, nthreads=None):
@@ -524,7 +555,7 @@ def main():
         fp32 = roof["fp32_peak_tflops_measured"] if roof else None
         for key, leg in (("p256_c2", lambda: p256_leg(pg, local, peaks, peak_kind, fp32)),
                          ("instanton_c3", lambda: instanton_leg(pg, local)),
-                         ("uneven_p_c4", lambda: uneven_p_leg(pg))):
+                         ("uneven_p_c4", lambda: uneven_p_leg(pg, peaks, fp32))):
             try:
                 extras[key] = leg()
             except Exception as e:
