@@ -337,7 +337,7 @@ def uneven_p_leg(pg, peaks=None, fp32=None, nmc=200):
         p_eff = float(np.sum(Pr * Pr) / np.sum(Pr))  # bead-weighted P
         terms = {"tensor": {"flops_per_bead_step": 4.0 * p_eff * nd, "peak": peaks["bf16_tflops"],
                             "unit": "TFLOP/s"},
-                 "hbm": {"bytes_per_bead_step": 36.0 * nd * 4, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                 "hbm": {"bytes_per_bead_step": 36.0 * nd, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                          "basis": "algorithmic bytes (no capture of the group)"}}
         terms["tensor"]["achieved"] = terms["tensor"]["flops_per_bead_step"] * rate / 1e12
         terms["hbm"]["achieved"] = terms["hbm"]["bytes_per_bead_step"] * rate / 1e9
